@@ -1,0 +1,380 @@
+"""Benchmark of the GB300 CG assembly + Krylov path.
+
+Workload (the plain-FP64-at-scale configuration): the P1 pressure-Poisson
+system on the 128^3 six-tet unit cube (12,582,912 tets, 2,146,689 nodes,
+31,802,497 CSR entries), interior vertices jittered +-0.2h (splitmix64 seed
+20261204), source f = sin(pi x) sin(pi y) sin(pi z), Dirichlet 0 on the
+boundary, degree-2 quadrature.
+
+* step   = one assembly of that system (zero + coloured element loop + rhs),
+           inputs resident in HBM; metric = elements assembled per second.
+* e2e    = the same assembly through the host-pointer C-ABI call
+           (fl_gpu_assemble_advdif_cg) with pinned host buffers: H2D of the
+           source field, D2H of val and rhs inside the timed region.
+* solve  = CG + Jacobi to rtol 1e-10 on the assembled system, plain FP64 and
+           mixed precision (FP32 inner CG inside FP64 refinement).
+
+``--impl reference`` times the CPU restatement of the reference algorithm
+(OpenMP over colours, full quadrature loops, bisection addto) on all host
+cores for the same metric.
+
+Multi-GPU: replicas only -- each rank assembles its own copy of the workload;
+``value`` is the elements of all ranks divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Melem/s assembly (P1 Poisson 128^3); Poisson time-to-1e-10"
+
+
+def algorithmic_bytes(E, N, nnz):
+    """Compulsory HBM bytes of one P1 assembly: connectivity, coordinates,
+    source, CSR pattern read once, values and rhs written once."""
+    return 16 * E + 24 * N + 8 * N + 4 * (N + 1) + 12 * nnz + 8 * N
+
+
+def cg_iteration_bytes(N, nnz):
+    """Compulsory bytes of one fused FP64 PCG iteration (matrix + vectors)."""
+    return 12 * nnz + 4 * (N + 1) + 104 * N
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(key):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        if args.impl != "reference":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def workload(n):
+    from fluidity_gb300 import meshgen as M
+    nd, X = M.cube_mesh(n)
+    return nd, X, M.poisson_source(X), M.boundary_nodes(X)
+
+
+def cpu_assembly_rate(nd, X, src, colours=None, findrm=None, colm=None, reps=1):
+    """Oracle assembly of the whole workload on all host cores; (Melem/s, threads, s)."""
+    from oracle import oracle as O
+    if findrm is None:
+        findrm, colm, _ = O.make_sparsity(nd)
+    if colours is None:
+        ocol, ncol = O.colour_cg1(nd)
+        colours = O.colour_sets(ocol, ncol)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _, _, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
+                                     findrm=findrm, colm=colm, diffusivity=1.0, source=src,
+                                     colours=colours)
+        dt = time.perf_counter() - t0
+        assert st == 0
+        best = dt if best is None else min(best, dt)
+    return nd.shape[0] / best / 1e6, O.num_threads(), best
+
+
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    nd, X, src, bn = workload(args.n)
+    t0 = time.perf_counter()
+    findrm, colm, _ = O.make_sparsity(nd)
+    ocol, ncol = O.colour_cg1(nd)
+    colours = O.colour_sets(ocol, ncol)
+    setup = time.perf_counter() - t0
+    times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, _, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
+                                     findrm=findrm, colm=colm, diffusivity=1.0, source=src,
+                                     colours=colours)
+        dt = time.perf_counter() - t0
+        assert st == 0
+        if k >= args.warmup:
+            times.append(dt)
+    t = float(np.mean(times))
+    E = nd.shape[0]
+    value = E / t / 1e6
+    thr = O.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Melem/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"P1 Poisson assembly, {args.n}^3 six-tet cube", "elements": E,
+                   "nodes": int(X.shape[0]), "nnz": int(colm.size), "cpu_setup_s": setup},
+        "cpu_baseline": {"value": value, "unit": "Melem/s", "cores": thr, "kind": "port",
+                         "sample": f"full {args.n}^3 assembly per step, OpenMP over "
+                                   f"{ncol} colours"},
+        "e2e": {"value": value, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, ws, dist):
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nd, X, src, bn = workload(args.n)
+    E, N = nd.shape[0], X.shape[0]
+    t0 = time.perf_counter()
+    m = ft.Mesh(nd, X)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    nnz = m.nnz
+    lib = m.lib
+    stream = torch.cuda.current_stream()
+    p = ft.advdif_params(diffusivity=1.0, have_source=True, quad_degree=2)
+    dsrc = torch.from_numpy(src).to(dev)
+    val = torch.empty(nnz, dtype=torch.float64, device=dev)
+    rhs = torch.empty(N, dtype=torch.float64, device=dev)
+
+    def step():
+        ft.assemble_advection_diffusion_cg(m, p, source=dsrc, val=val, rhs=rhs, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    l0 = ft.kernel_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = ft.kernel_launch_count() - l0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # element-loop device time (all colours) per assembly, CUDA events on the stream
+    import ctypes as C
+    lib.fl_set_kernel_timing(m.handle, 1)
+    kms = []
+    for _ in range(max(3, args.steps // 2)):
+        step()
+        f = C.c_float()
+        ft.check(lib.fl_last_assembly_kernel_ms(m.handle, C.byref(f)), "timing")
+        kms.append(f.value)
+    lib.fl_set_kernel_timing(m.handle, 0)
+    kernel_ms = float(np.median(kms))
+    alg = algorithmic_bytes(E, N, nnz)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+
+    # e2e through the host-pointer C-ABI with pinned buffers
+    hsrc = torch.from_numpy(src).pin_memory()
+    hval = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    hrhs = torch.empty(N, dtype=torch.float64).pin_memory()
+    hsrc_np, hval_np, hrhs_np = hsrc.numpy(), hval.numpy(), hrhs.numpy()
+    for _ in range(2):
+        ft.assemble_advection_diffusion_cg(m, p, source=hsrc_np, val=hval_np, rhs=hrhs_np)
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        ft.assemble_advection_diffusion_cg(m, p, source=hsrc_np, val=hval_np, rhs=hrhs_np)
+    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    assert np.array_equal(hval_np, val.cpu().numpy()), "host and device paths differ"
+
+    # solve: Dirichlet + CG to 1e-10 (fp64 and mixed)
+    solve = None
+    if not args.no_solve:
+        ina = torch.zeros(N, dtype=torch.uint8, device=dev)
+        dbn = torch.from_numpy(bn).to(dev)
+        dg = torch.zeros(bn.size, dtype=torch.float64, device=dev)
+        step()
+        ft.apply_dirichlet_conditions(m, rhs, ina, dbn, dg, dt=1.0, stream=stream)
+        out = {}
+        xs = {}
+        for prec in ("fp64", "mixed"):
+            x = torch.zeros(N, dtype=torch.float64, device=dev)
+            opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=20000, precision=prec,
+                                     start_from_zero=True)
+            ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)  # warm-up
+            x.zero_()
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            sms = s0.elapsed_time(s1)
+            xs[prec] = x
+            out[prec] = {"ms": sms, "iterations": rep["iterations"], "reason": rep["reason_name"],
+                         "outer": rep["outer_iterations"],
+                         "true_rel_residual": rep["true_rel_residual"],
+                         "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None}
+        it_bytes = cg_iteration_bytes(N, nnz)
+        f64 = out["fp64"]
+        f64["achieved_gbs"] = it_bytes * f64["iterations"] / (f64["ms"] * 1e-3) / 1e9
+        f64["frac_of_hbm"] = f64["achieved_gbs"] / peak
+        out["mixed"]["rel_diff_vs_fp64"] = float(
+            (xs["mixed"] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
+        xa = torch.from_numpy(src / (3 * np.pi ** 2)).to(dev)
+        out["fp64"]["max_err_vs_analytic"] = float((xs["fp64"] - xa).abs().max())
+        out["speedup_mixed_vs_fp64"] = f64["ms"] / out["mixed"]["ms"]
+        solve = out
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu and ws == 1:
+        s = m.sparsity()
+        col, ptr, el = m.colouring()
+        rate, thr, secs = cpu_assembly_rate(nd, X, src, colours=(ptr.astype(np.int64), el),
+                                            findrm=s.findrm.astype(np.int64), colm=s.colm)
+        cpu = {"value": rate, "unit": "Melem/s", "cores": thr, "kind": "port",
+               "sample": f"one full {args.n}^3 assembly ({secs:.2f} s), OpenMP over "
+                         f"{m.ncolours} colours, oracle restatement of the reference loop"}
+    value = E * ws / (ms * 1e-3) / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"P1 Poisson assembly, {args.n}^3 six-tet cube, jitter 0.2h",
+                   "elements": E, "nodes": N, "nnz": nnz, "colours": m.ncolours,
+                   "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (no flush)",
+                   "gpu_setup_s (sparsity+colouring)": setup_s},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": ncu_traffic("k_asm_p1_diffusion"),
+                     "peak_kind": peak_kind, "kernel": "k_asm_p1_diffusion (all colours)",
+                     "kernel_ms": kernel_ms, "algorithmic_bytes": alg},
+        "cpu_baseline": cpu,
+        "e2e": {"value": E * ws / (e2e_ms * 1e-3) / 1e6, "unit": "Melem/s",
+                "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * nnz + 8 * N,
+                "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "solve": solve,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="hexes per side")
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, ws, dist = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, ws, dist)
+        else:
+            run_ours(args, rank, ws, dist)
+    finally:
+        if dist:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

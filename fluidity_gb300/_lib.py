@@ -1,0 +1,114 @@
+"""ctypes binding of ``libfluidity_gb300.so`` (the C-ABI of include/fluidity_gb300.h).
+
+The structures below mirror the C declarations field for field.  Loading fails
+loudly when the library cannot be built or loaded: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+FL_OK = 0
+STATUS = {
+    0: "FL_OK", 1: "FL_ERR_ARG", 2: "FL_ERR_CUDA", 3: "FL_ERR_OUTSIDE_PATTERN",
+    4: "FL_ERR_TIMEOUT", 5: "FL_ERR_COLOURS", 6: "FL_ERR_NOMEM", 7: "FL_ERR_UNSUPPORTED",
+}
+REASONS = {
+    2: "KSP_CONVERGED_RTOL", 3: "KSP_CONVERGED_ATOL", -2: "KSP_DIVERGED_NULL",
+    -3: "KSP_DIVERGED_ITS", -4: "KSP_DIVERGED_DTOL", -5: "KSP_DIVERGED_BREAKDOWN",
+    -8: "KSP_DIVERGED_INDEFINITE_PC", -9: "KSP_DIVERGED_NANORINF",
+    -10: "KSP_DIVERGED_INDEFINITE_MAT",
+}
+
+
+class FlError(RuntimeError):
+    """A non-OK fl_status from the library (FLAbort/FLExit in the reference)."""
+
+    def __init__(self, status: int, where: str, message: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("nodes", C.c_int32), ("elements", C.c_int32), ("loc", C.c_int32),
+        ("index_base", C.c_int32), ("ndglno", C.c_void_p), ("x_nodes", C.c_int32),
+        ("x_ndglno", C.c_void_p), ("coords", C.c_void_p),
+    ]
+
+
+class AdvDifParams(C.Structure):
+    _fields_ = [
+        ("theta", C.c_double), ("dt", C.c_double), ("beta", C.c_double),
+        ("have_mass", C.c_int32), ("lump_mass", C.c_int32), ("have_advection", C.c_int32),
+        ("have_diffusivity", C.c_int32), ("isotropic_diffusivity", C.c_int32),
+        ("have_source", C.c_int32), ("have_absorption", C.c_int32), ("quad_degree", C.c_int32),
+        ("diffusivity", C.c_double * 9),
+    ]
+
+
+class Fields(C.Structure):
+    _fields_ = [("t", C.c_void_p), ("velocity", C.c_void_p), ("source", C.c_void_p),
+                ("absorption", C.c_void_p)]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [
+        ("ksp_type", C.c_int32), ("restart", C.c_int32), ("rtol", C.c_double),
+        ("atol", C.c_double), ("dtol", C.c_double), ("max_its", C.c_int32),
+        ("start_from_zero", C.c_int32), ("precision", C.c_int32), ("inner_rtol", C.c_double),
+    ]
+
+
+class SolveReport(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32), ("reason", C.c_int32), ("final_rnorm", C.c_double),
+        ("rnorm0", C.c_double), ("true_rel_residual", C.c_double),
+        ("outer_iterations", C.c_int32), ("pad", C.c_int32),
+    ]
+
+
+#: Every entry point declared in include/fluidity_gb300.h.
+EXPORTS = [
+    "fl_last_error", "fl_gpu_mesh_register", "fl_gpu_mesh_destroy", "fl_gpu_mesh_info",
+    "fl_gpu_sparsity_copy", "fl_gpu_colouring_copy", "fl_gpu_make_global_numbering_p2",
+    "fl_gpu_assemble_advdif_cg", "fl_dev_assemble_advdif_cg", "fl_gpu_apply_dirichlet",
+    "fl_dev_apply_dirichlet", "fl_gpu_petsc_solve", "fl_dev_petsc_solve", "fl_dev_csr_mult",
+    "fl_kernel_launch_count", "fl_set_kernel_timing", "fl_last_assembly_kernel_ms",
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def path() -> str:
+    return _build.LIB
+
+
+def load(build_if_needed: bool = True):
+    """Load the CUDA library (building it first when stale)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_needed and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError(f"{_build.LIB} is missing; run fluidity_gb300.build.build()")
+        lib = C.CDLL(_build.LIB)
+        lib.fl_last_error.restype = C.c_char_p
+        lib.fl_kernel_launch_count.restype = C.c_int64
+        for name in EXPORTS:
+            if name not in ("fl_last_error", "fl_kernel_launch_count"):
+                getattr(lib, name).restype = C.c_int
+        _lib = lib
+        return lib
+
+
+def check(status: int, where: str) -> None:
+    if status != FL_OK:
+        msg = load().fl_last_error().decode(errors="replace")
+        raise FlError(status, where, msg)

@@ -1,0 +1,581 @@
+// fl_assemble.cu -- CG advection-diffusion / Poisson element assembly into the
+// device csr_matrix, and strong Dirichlet conditions.
+//
+// The element loop replaces the coloured OpenMP region of
+// assemble_advection_diffusion_cg (assemble/Advection_Diffusion_CG.F90:560-598):
+// one launch per colour of the COLOURING_CG1 colouring; no two elements of a
+// colour share a node, so each CSR row receives at most one element's
+// contribution per launch and every entry is summed in (colour, element)
+// order -- the reference's own order -- without atomics.
+//
+// Element matrices follow the term routines of Advection_Diffusion_CG.F90
+// (:867 mass, :943 advection not by parts, :1143 absorption, :1164
+// diffusivity, :1129 source) with the quadrature sums regrouped: every
+// integral is a contraction of per-element geometric factors (|detJ|, invJ,
+// nodal coefficients) with reference-element tensors that hold the
+// quadrature sums over the same rule (femtools/Quadrature.F90:649-735) and the
+// same Lagrange basis (femtools/Shape_Functions.F90:128-329).  The regrouping
+// is exact in real arithmetic; results agree with the reference loops to
+// rounding.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "fl_internal.cuh"
+#include "fl_device.cuh"
+#include "fl_refelem.h"
+
+namespace fl {
+
+unsigned long long launches_assemble() { return unit_launches(); }
+
+// Reference tensors for one (field degree, quadrature degree) pair; velocity
+// and absorption coefficients are nodal on P1 (velocity) / the field mesh.
+struct RefTensors {
+  int loc, ngi;
+  double wsum;
+  double M[10][10];              // sum_g w N_i N_j
+  double R[10][10][3][3];        // sum_g w dN_i/dL_a dN_j/dL_b
+  double T[10][10][4][3];        // sum_g w N_i Nu_k dN_j/dL_a       (advection)
+  double D[10][10][4][3];        // sum_g w N_i N_j dNu_k/dL_a       (beta div u)
+  double W[10][10][10];          // sum_g w N_i N_j N_k              (absorption)
+};
+
+static void build_tensors(int degree, int qdeg, RefTensors& t) {
+  TetQuad q;
+  tet_quadrature(qdeg, q);
+  TetShape s, u;
+  tet_shape(degree, q, s);
+  tet_shape(1, q, u);
+  std::memset(&t, 0, sizeof(t));
+  t.loc = s.loc;
+  t.ngi = q.ngi;
+  for (int g = 0; g < q.ngi; ++g) t.wsum += q.w[g];
+  for (int i = 0; i < s.loc; ++i)
+    for (int j = 0; j < s.loc; ++j)
+      for (int g = 0; g < q.ngi; ++g) {
+        const double w = q.w[g];
+        t.M[i][j] += w * s.n[i][g] * s.n[j][g];
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) t.R[i][j][a][b] += w * s.dn[i][g][a] * s.dn[j][g][b];
+        for (int k = 0; k < 4; ++k)
+          for (int a = 0; a < 3; ++a) {
+            t.T[i][j][k][a] += w * s.n[i][g] * u.n[k][g] * s.dn[j][g][a];
+            t.D[i][j][k][a] += w * s.n[i][g] * s.n[j][g] * u.dn[k][g][a];
+          }
+        for (int k = 0; k < s.loc; ++k) t.W[i][j][k] += w * s.n[i][g] * s.n[j][g] * s.n[k][g];
+      }
+}
+
+// Geometry of a linear simplex element, as construct_cache computes it
+// (femtools/Transform_elements.F90:258-301): J_T(a,b) = x_b - x_4 (columns of
+// dn are unit vectors and -1 for the dependent coordinate), invJ by cofactors
+// over cyc3, detJ = J_T(:,1).invJ(:,1).  Returns the unscaled cofactors and
+// detJ; invJ = cof / detJ.
+struct Geo {
+  double cof[3][3];
+  double det;
+};
+
+__device__ __forceinline__ void element_geo(const double* __restrict__ X, const int32_t* __restrict__ xnd,
+                                            int64_t e, Geo& g) {
+  const int4 v = __ldg(reinterpret_cast<const int4*>(xnd) + e);
+  const int vi[4] = {v.x, v.y, v.z, v.w};
+  double x[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x[i][a] = __ldg(X + 3 * (int64_t)vi[i] + a);
+  double J[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[a][b] = x[b][a] - x[3][a];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+      g.cof[i][k] = J[i1][k1] * J[i2][k2] - J[i2][k1] * J[i1][k2];
+    }
+  g.det = J[0][0] * g.cof[0][0] + J[1][0] * g.cof[1][0] + J[2][0] * g.cof[2][0];
+}
+
+// csr addto of one entry (csr_addto, femtools/Sparse_Tools.F90:2631-2655):
+// exact zeros are skipped; a miss is an "outside sparsity pattern" error.
+__device__ __forceinline__ void addto(double* __restrict__ val, const int32_t* __restrict__ findrm,
+                                      const int32_t* __restrict__ colm, int i, int j, double v,
+                                      ErrWord* err, int e) {
+  if (v == 0.0) return;
+  const int p = csr_find(colm, __ldg(findrm + i), __ldg(findrm + i + 1), j);
+  if (p < 0) {
+    set_err(err, FL_ERR_OUTSIDE_PATTERN, e);
+    return;
+  }
+  val[p] += v;
+}
+
+struct AsmArgs {
+  const int32_t* elems;     // elements of this colour
+  int32_t count;
+  const int32_t* nd;        // field connectivity
+  const int32_t* xnd;       // coordinate connectivity (int4 per element)
+  const double* X;
+  const double* t;
+  const double* u;
+  const double* f;
+  const double* alpha;
+  const int32_t* findrm;
+  const int32_t* colm;
+  double* val;
+  double* rhs;
+  ErrWord* err;
+  const RefTensors* ref;
+  double theta_dt;
+  double beta;
+  double kappa[9];
+  int have_mass, lump, have_adv, have_beta, have_diff, iso, have_src, have_abs, use_dt;
+};
+
+// General element kernel: any term combination, P1 or P2 fields, P1
+// coordinates and velocity.  One thread per element; rows of the element
+// matrix are formed and inserted one at a time.
+template <int LOC>
+__global__ void __launch_bounds__(128) k_asm_general(AsmArgs A) {
+  note_launch();
+  const RefTensors& R = *A.ref;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < A.count; idx += gridDim.x * blockDim.x) {
+    const int e = __ldg(A.elems + idx);
+    Geo g;
+    element_geo(A.X, A.xnd, e, g);
+    const double rdet = 1.0 / g.det;
+    const double adet = fabs(g.det);
+    double invJ[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) invJ[a][b] = g.cof[a][b] * rdet;
+    int tn[LOC];
+#pragma unroll
+    for (int i = 0; i < LOC; ++i) tn[i] = __ldg(A.nd + (int64_t)e * LOC + i);
+    double Te[LOC];
+#pragma unroll
+    for (int i = 0; i < LOC; ++i) Te[i] = A.t ? __ldg(A.t + tn[i]) : 0.0;
+    // Diffusion factor Q(a,b) = |det| sum_cd invJ(c,a) kappa(c,d) invJ(d,b):
+    // dshape_dot_dshape / dshape_tensor_dshape (FETools.F90:391,668) with
+    // dshape = dn . invJ^T.
+    double Q[3][3];
+    if (A.have_diff) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          double s = 0.0;
+          if (A.iso) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) s += invJ[c][a] * invJ[c][b];
+            s *= A.kappa[0];
+          } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+              for (int d = 0; d < 3; ++d) s += invJ[c][a] * A.kappa[3 * c + d] * invJ[d][b];
+          }
+          Q[a][b] = s * adet;
+        }
+    }
+    // Advection factor V(k,a) = |det| u_k . invJ(:,a): u at quadrature points
+    // is the nodal P1 interpolant (ele_val_at_quad, Fields_Base.F90:2256).
+    double V[4][3];
+    if (A.have_adv) {
+      const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+      const int vi[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        double uk[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) uk[c] = __ldg(A.u + 3 * (int64_t)vi[k] + c);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) V[k][a] = (uk[0] * invJ[0][a] + uk[1] * invJ[1][a] + uk[2] * invJ[2][a]) * adet;
+      }
+    }
+    double al[LOC];
+    if (A.have_abs) {
+#pragma unroll
+      for (int k = 0; k < LOC; ++k) al[k] = __ldg(A.alpha + tn[k]) * adet;
+    }
+    double fe[LOC];
+    if (A.have_src) {
+#pragma unroll
+      for (int k = 0; k < LOC; ++k) fe[k] = __ldg(A.f + tn[k]) * adet;
+    }
+#pragma unroll 1
+    for (int i = 0; i < LOC; ++i) {
+      double m[LOC];     // matrix row
+      double op[LOC];    // operator row (advection + absorption + diffusion)
+      double r = 0.0;
+#pragma unroll
+      for (int j = 0; j < LOC; ++j) {
+        m[j] = 0.0;
+        op[j] = 0.0;
+      }
+      if (A.have_mass) {
+        if (A.lump) {
+          double s = 0.0;
+#pragma unroll
+          for (int j = 0; j < LOC; ++j) s += R.M[i][j] * adet;
+#pragma unroll
+          for (int j = 0; j < LOC; ++j) m[j] = (j == i) ? s : 0.0;
+        } else {
+#pragma unroll
+          for (int j = 0; j < LOC; ++j) m[j] = R.M[i][j] * adet;
+        }
+      }
+      if (A.have_adv) {
+#pragma unroll
+        for (int j = 0; j < LOC; ++j) {
+          double s = 0.0;
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) s += V[k][a] * R.T[i][j][k][a];
+          if (A.have_beta) {
+            double d = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+#pragma unroll
+              for (int a = 0; a < 3; ++a) d += V[k][a] * R.D[i][j][k][a];
+            s = s + A.beta * d;
+          }
+          op[j] += s;
+        }
+      }
+      if (A.have_abs) {
+#pragma unroll
+        for (int j = 0; j < LOC; ++j) {
+          double s = 0.0;
+#pragma unroll
+          for (int k = 0; k < LOC; ++k) s += al[k] * R.W[i][j][k];
+          op[j] += s;
+        }
+      }
+      if (A.have_diff) {
+#pragma unroll
+        for (int j = 0; j < LOC; ++j) {
+          double s = 0.0;
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) s += Q[a][b] * R.R[i][j][a][b];
+          op[j] += s;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < LOC; ++j) {
+        if (A.use_dt) m[j] += A.theta_dt * op[j];
+        r -= op[j] * Te[j];
+      }
+      if (A.have_src) {
+#pragma unroll
+        for (int j = 0; j < LOC; ++j) r += R.M[i][j] * fe[j];
+      }
+      const int row = tn[i];
+#pragma unroll
+      for (int j = 0; j < LOC; ++j) addto(A.val, A.findrm, A.colm, row, tn[j], m[j], A.err, e);
+      A.rhs[row] += r;
+    }
+  }
+}
+
+// P1 diffusion + source (+ consistent mass) in closed form: with P1
+// coordinates the gradients are the cofactor columns over detJ, so
+//   K_ij = (c_i . kappa c_j) * wsum / |detJ|,   c_4 = -(c_1 + c_2 + c_3)
+//   rhs_i = sum_j M_ij f_j,  M_ij = |detJ| * Mref_ij.
+// This is the pressure-Laplacian form of the Poisson workloads (exact
+// regrouping of dshape_dot_dshape over the rule).
+__global__ void __launch_bounds__(256) k_asm_p1_diffusion(AsmArgs A) {
+  note_launch();
+  const RefTensors& R = *A.ref;
+  const double wsum = R.wsum;
+  double M0 = R.M[0][0], M1 = R.M[0][1];
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < A.count; idx += gridDim.x * blockDim.x) {
+    const int e = __ldg(A.elems + idx);
+    Geo g;
+    element_geo(A.X, A.xnd, e, g);
+    const double adet = fabs(g.det);
+    const double s = wsum / adet;
+    double c[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) c[i][a] = g.cof[a][i];
+      c[3][a] = -(c[0][a] + c[1][a] + c[2][a]);
+    }
+    double kc[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (A.iso) kc[i][a] = c[i][a] * A.kappa[0];
+        else kc[i][a] = A.kappa[3 * a + 0] * c[i][0] + A.kappa[3 * a + 1] * c[i][1] + A.kappa[3 * a + 2] * c[i][2];
+      }
+    const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
+    const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
+    double K[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) K[i][j] = (c[i][0] * kc[j][0] + c[i][1] * kc[j][1] + c[i][2] * kc[j][2]) * s;
+    double Te[4], fe[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      Te[i] = A.t ? __ldg(A.t + tn[i]) : 0.0;
+      fe[i] = A.have_src ? __ldg(A.f + tn[i]) : 0.0;
+    }
+    double fsum = (fe[0] + fe[1]) + (fe[2] + fe[3]);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      double r = 0.0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) r -= K[i][j] * Te[j];
+      if (A.have_src) r += adet * (M1 * fsum + (M0 - M1) * fe[i]);
+      const int row = tn[i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        double m = A.use_dt ? A.theta_dt * K[i][j] : 0.0;
+        if (A.have_mass) m += adet * (i == j ? M0 : M1);
+        addto(A.val, A.findrm, A.colm, row, tn[j], m, A.err, e);
+      }
+      A.rhs[row] += r;
+    }
+  }
+}
+
+__global__ void k_zero(double* __restrict__ p, int64_t n) {
+  note_launch();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    p[k] = 0.0;
+}
+
+// Strong Dirichlet (Boundary_Conditions.F90:1983-2025).
+__global__ void k_dirichlet(int32_t nb, const int32_t* __restrict__ nodes, int32_t base,
+                            const double* __restrict__ gv, const double* __restrict__ t, double dt,
+                            int32_t n, double* __restrict__ rhs, uint8_t* __restrict__ inactive,
+                            ErrWord* err) {
+  note_launch();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nb; k += gridDim.x * blockDim.x) {
+    const int i = nodes[k] - base;
+    if (i < 0 || i >= n) {
+      set_err(err, FL_ERR_ARG, k);
+      continue;
+    }
+    inactive[i] = 1;
+    rhs[i] = dt > 0.0 ? (gv[k] - (t ? t[i] : 0.0)) / dt : gv[k];
+  }
+}
+
+// Per-mesh cache of reference tensors keyed by (field degree, quad degree).
+struct TensorCache {
+  std::mutex mu;
+  struct Entry {
+    int device, degree, qdeg;
+    RefTensors* d;
+  };
+  std::vector<Entry> entries;
+  const RefTensors* get(int device, int degree, int qdeg, cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& e : entries)
+      if (e.device == device && e.degree == degree && e.qdeg == qdeg) return e.d;
+    RefTensors h;
+    build_tensors(degree, qdeg, h);
+    RefTensors* d = nullptr;
+    if (cudaMalloc(&d, sizeof(RefTensors)) != cudaSuccess) return nullptr;
+    if (cudaMemcpyAsync(d, &h, sizeof(RefTensors), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      cudaFree(d);
+      return nullptr;
+    }
+    entries.push_back({device, degree, qdeg, d});
+    return d;
+  }
+};
+static TensorCache g_tensors;
+
+// Which kernel handles a parameter set: the closed-form P1 kernel covers the
+// Poisson/diffusion forms (no advection, no absorption, consistent mass).
+static bool use_p1_closed_form(const fl_mesh_t* m, const fl_advdif_params* p) {
+  return m->loc == 4 && !p->have_advection && !p->have_absorption && !(p->have_mass && p->lump_mass) &&
+         p->have_diffusivity;
+}
+
+int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
+             cudaStream_t s) {
+  FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
+  FL_CHECK_ARG(p->quad_degree >= 1 && p->quad_degree <= 4, "quadrature degree 1..4");
+  FL_CHECK_ARG(!p->have_advection || f->velocity, "advection needs a velocity field");
+  FL_CHECK_ARG(!p->have_source || f->source, "source field missing");
+  FL_CHECK_ARG(!p->have_absorption || f->absorption, "absorption field missing");
+  const int degree = m->loc == 4 ? 1 : 2;
+  const RefTensors* ref = g_tensors.get(m->device, degree, p->quad_degree, s);
+  if (!ref) {
+    set_error("reference tensor upload failed");
+    return FL_ERR_CUDA;
+  }
+  // zero(matrix); zero(rhs)  (Advection_Diffusion_CG.F90:560-561)
+  k_zero<<<grid_for(m->nnz, 256), 256, 0, s>>>(val, m->nnz);
+  k_zero<<<grid_for(m->N, 256), 256, 0, s>>>(rhs, m->N);
+  FL_TRY_CUDA(cudaGetLastError());
+  AsmArgs A{};
+  A.nd = m->ndglno.p;
+  A.xnd = m->xndglno.p;
+  A.X = m->coords.p;
+  A.t = f->t;
+  A.u = f->velocity;
+  A.f = f->source;
+  A.alpha = f->absorption;
+  A.findrm = m->findrm.p;
+  A.colm = m->colm.p;
+  A.val = val;
+  A.rhs = rhs;
+  A.err = m->err.p;
+  A.ref = ref;
+  A.theta_dt = p->dt * p->theta;
+  // epsilon(0.0) is the real(8) machine epsilon under -fdefault-real-8
+  const double eps = 2.220446049250313e-16;
+  A.use_dt = fabs(A.theta_dt) > eps;
+  A.beta = p->beta;
+  A.have_beta = p->have_advection && fabs(p->beta) > eps;
+  for (int k = 0; k < 9; ++k) A.kappa[k] = p->diffusivity[k];
+  A.have_mass = p->have_mass;
+  A.lump = p->have_mass && p->lump_mass;
+  A.have_adv = p->have_advection;
+  A.have_diff = p->have_diffusivity;
+  A.iso = p->isotropic_diffusivity;
+  A.have_src = p->have_source;
+  A.have_abs = p->have_absorption;
+  const bool closed = use_p1_closed_form(m, p);
+  if (m->timing) {
+    if (!m->ev0) {
+      FL_TRY_CUDA(cudaEventCreate(&m->ev0));
+      FL_TRY_CUDA(cudaEventCreate(&m->ev1));
+    }
+    FL_TRY_CUDA(cudaEventRecord(m->ev0, s));
+  }
+  for (int c = 0; c < m->ncolours; ++c) {
+    A.elems = m->colour_elems.p + m->colour_ptr[c];
+    A.count = m->colour_ptr[c + 1] - m->colour_ptr[c];
+    if (A.count == 0) continue;
+    if (closed) {
+      k_asm_p1_diffusion<<<grid_for(A.count, 256, 16), 256, 0, s>>>(A);
+    } else if (m->loc == 4) {
+      k_asm_general<4><<<grid_for(A.count, 128, 16), 128, 0, s>>>(A);
+    } else {
+      k_asm_general<10><<<grid_for(A.count, 128, 16), 128, 0, s>>>(A);
+    }
+    FL_TRY_CUDA(cudaGetLastError());
+  }
+  if (m->timing) {
+    FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
+    m->timed = true;
+  }
+  return FL_OK;
+}
+
+}  // namespace fl
+
+using namespace fl;
+
+static cudaStream_t pick_stream(fl_mesh m, void* stream) {
+  return stream ? (cudaStream_t)stream : m->stream;
+}
+
+extern "C" int fl_dev_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, const fl_fields* f,
+                                         double* val, double* rhs, void* stream) {
+  FL_CHECK_ARG(m, "null mesh");
+  cudaStream_t s = pick_stream(m, stream);
+  FL_TRY(assemble(m, p, f, val, rhs, s));
+  // pattern misses are reported synchronously, as FLAbort is in the reference
+  return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
+}
+
+extern "C" int fl_gpu_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, const fl_fields* f,
+                                         double* val, double* rhs) {
+  FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
+  cudaStream_t s = m->stream;
+  FL_TRY(m->st_val.reserve(m->nnz));
+  FL_TRY(m->st_rhs.reserve(m->N));
+  fl_fields df{nullptr, nullptr, nullptr, nullptr};
+  auto up = [&](const double* h, DevBuf<double>& d, size_t n, const double** out) -> int {
+    if (!h) return FL_OK;
+    FL_TRY(d.reserve(n));
+    FL_TRY_CUDA(cudaMemcpyAsync(d.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    *out = d.p;
+    return FL_OK;
+  };
+  FL_TRY(up(f->t, m->st_t, m->N, &df.t));
+  FL_TRY(up(p->have_advection ? f->velocity : nullptr, m->st_u, (size_t)3 * m->Nx, &df.velocity));
+  FL_TRY(up(p->have_source ? f->source : nullptr, m->st_src, m->N, &df.source));
+  FL_TRY(up(p->have_absorption ? f->absorption : nullptr, m->st_abs, m->N, &df.absorption));
+  FL_TRY(fl_dev_assemble_advdif_cg(m, p, &df, m->st_val.p, m->st_rhs.p, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(val, m->st_val.p, sizeof(double) * m->nnz, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(rhs, m->st_rhs.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  return FL_OK;
+}
+
+extern "C" int fl_set_kernel_timing(fl_mesh m, int32_t on) {
+  FL_CHECK_ARG(m, "null mesh");
+  m->timing = on != 0;
+  m->timed = false;
+  return FL_OK;
+}
+
+extern "C" int fl_last_assembly_kernel_ms(fl_mesh m, float* ms) {
+  FL_CHECK_ARG(m && ms, "null argument");
+  FL_CHECK_ARG(m->timed, "no timed assembly recorded (enable fl_set_kernel_timing first)");
+  FL_TRY_CUDA(cudaEventSynchronize(m->ev1));
+  FL_TRY_CUDA(cudaEventElapsedTime(ms, m->ev0, m->ev1));
+  return FL_OK;
+}
+
+extern "C" int fl_dev_apply_dirichlet(fl_mesh m, int32_t nb, const int32_t* nodes, int32_t base,
+                                      const double* g, const double* t, double dt, double* rhs,
+                                      uint8_t* inactive, void* stream) {
+  FL_CHECK_ARG(m && rhs && inactive, "null argument");
+  FL_CHECK_ARG(nb >= 0 && (nb == 0 || (nodes && g)), "boundary node list");
+  if (nb == 0) return FL_OK;
+  cudaStream_t s = pick_stream(m, stream);
+  k_dirichlet<<<grid_for(nb, 256), 256, 0, s>>>(nb, nodes, base, g, t, dt, m->N, rhs, inactive, m->err.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  return check_err(m->err.p, s, "Dirichlet node out of range");
+}
+
+extern "C" int fl_gpu_apply_dirichlet(fl_mesh m, int32_t nb, const int32_t* nodes, int32_t base,
+                                      const double* g, const double* t, double dt, double* rhs,
+                                      uint8_t* inactive) {
+  FL_CHECK_ARG(m && rhs && inactive, "null argument");
+  FL_CHECK_ARG(nb >= 0 && (nb == 0 || (nodes && g)), "boundary node list");
+  cudaStream_t s = m->stream;
+  FL_TRY(m->st_rhs.reserve(m->N));
+  FL_TRY(m->st_ina.reserve(m->N));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_rhs.p, rhs, sizeof(double) * m->N, cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_ina.p, inactive, m->N, cudaMemcpyHostToDevice, s));
+  if (nb > 0) {
+    FL_TRY(m->st_nodes.reserve(nb));
+    FL_TRY(m->st_g.reserve(nb));
+    FL_TRY_CUDA(cudaMemcpyAsync(m->st_nodes.p, nodes, sizeof(int32_t) * nb, cudaMemcpyHostToDevice, s));
+    FL_TRY_CUDA(cudaMemcpyAsync(m->st_g.p, g, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  }
+  const double* tp = nullptr;
+  if (t) {
+    FL_TRY(m->st_t.reserve(m->N));
+    FL_TRY_CUDA(cudaMemcpyAsync(m->st_t.p, t, sizeof(double) * m->N, cudaMemcpyHostToDevice, s));
+    tp = m->st_t.p;
+  }
+  FL_TRY(fl_dev_apply_dirichlet(m, nb, m->st_nodes.p, base, m->st_g.p, tp, dt, m->st_rhs.p, m->st_ina.p, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(rhs, m->st_rhs.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(inactive, m->st_ina.p, m->N, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  return FL_OK;
+}

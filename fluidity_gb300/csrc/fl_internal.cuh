@@ -1,0 +1,130 @@
+// fl_internal.cuh -- internal types and helpers of the GB300 CG hot-path
+// library.  Not part of the public C-ABI (see include/fluidity_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/fluidity_gb300.h"
+
+namespace fl {
+
+// Last error message of the calling host thread (fl_last_error()).
+void set_error(const char* fmt, ...);
+
+#define FL_TRY_CUDA(call)                                                          \
+  do {                                                                             \
+    cudaError_t _e = (call);                                                       \
+    if (_e != cudaSuccess) {                                                       \
+      ::fl::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #call,                   \
+                      cudaGetErrorString(_e));                                     \
+      return FL_ERR_CUDA;                                                          \
+    }                                                                              \
+  } while (0)
+
+#define FL_TRY(call)                                                               \
+  do {                                                                             \
+    int _s = (call);                                                               \
+    if (_s != FL_OK) return _s;                                                    \
+  } while (0)
+
+#define FL_CHECK_ARG(cond, msg)                                                    \
+  do {                                                                             \
+    if (!(cond)) {                                                                 \
+      ::fl::set_error("invalid argument: %s", msg);                                \
+      return FL_ERR_ARG;                                                           \
+    }                                                                              \
+  } while (0)
+
+// Grid sizes: a multiple of the SM count (152 on GB300) times resident CTAs.
+int num_sms();
+inline unsigned grid_for(int64_t n, int threads, int per_sm = 8) {
+  int64_t b = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)num_sms() * per_sm;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+// Plain device buffer (cudaMalloc/cudaFree) with grow-only resize.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  int reserve(size_t count) {
+    if (count <= n && p) return FL_OK;
+    release();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      set_error("cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+      return FL_ERR_NOMEM;
+    }
+    n = count;
+    return FL_OK;
+  }
+};
+
+// Device exclusive scan of int32 counts into int32 offsets (out[n] = total).
+// Returns FL_ERR_ARG when the total does not fit in int32.
+int exclusive_scan_i32(const int32_t* d_in, int32_t* d_out, int64_t n, cudaStream_t s);
+
+// Device-wide error word written by kernels (bounded waits, pattern misses).
+struct ErrWord {
+  int32_t code;      // FL_OK or an FL_ERR_* status
+  int32_t where;     // kernel-specific detail (element / row index)
+};
+
+// Per-translation-unit launch counters and workspace release hooks.
+unsigned long long launches_mesh();
+unsigned long long launches_assemble();
+unsigned long long launches_krylov();
+void release_krylov_work(struct ::fl_mesh_t* m);
+
+}  // namespace fl
+
+// Opaque mesh handle of the C-ABI: device mirrors of a field mesh and of its
+// coordinate (topology) mesh, plus the cached sparsity and colouring that the
+// reference caches in state / on the topology mesh.
+struct fl_mesh_t {
+  int device = 0;
+  int32_t N = 0;     // field-mesh nodes (matrix rows)
+  int32_t E = 0;     // elements
+  int32_t loc = 0;   // nodes per element of the field mesh (4 or 10)
+  int32_t Nx = 0;    // coordinate (P1 vertex) nodes
+  int64_t nnz = 0;
+  int32_t ncolours = 0;
+  cudaStream_t stream = nullptr;
+
+  fl::DevBuf<int32_t> ndglno;        // E*loc, 0-based, element-major
+  fl::DevBuf<int32_t> xndglno;       // E*4
+  fl::DevBuf<double> coords;         // 3*Nx
+  fl::DevBuf<int32_t> ne_ptr, ne;    // field node -> (element<<4 | local) ascending
+  fl::DevBuf<int32_t> vne_ptr, vne;  // vertex -> element ascending
+  fl::DevBuf<int32_t> findrm, colm, centrm;
+  fl::DevBuf<int32_t> colour;        // E, 1-based
+  fl::DevBuf<int32_t> colour_elems;  // E, sorted by (colour, element)
+  std::vector<int32_t> colour_ptr;   // ncolours+1 (host)
+  fl::DevBuf<fl::ErrWord> err;       // 1 word
+  // staging buffers of the host-pointer entry points (grow-only)
+  fl::DevBuf<double> st_val, st_rhs, st_t, st_u, st_src, st_abs, st_x, st_g;
+  fl::DevBuf<uint8_t> st_ina;
+  fl::DevBuf<int32_t> st_nodes;
+  // element-kernel timing of the last assembly (fl_set_kernel_timing)
+  bool timing = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool timed = false;
+};

@@ -1,0 +1,1144 @@
+// fl_krylov.cu -- device Krylov solves on the assembled csr_matrix, replacing
+// the PETSc KSPSolve that petsc_solve runs (femtools/Solvers.F90:1156-1302).
+//
+// Semantics of petsc_solve on a csr_matrix with inactive rows:
+//  * inactive rows are ghost rows masked out of the PETSc numbering
+//    (Petsc_Tools.F90:256-298); their columns are dropped and the rows carry
+//    only the diagonal ghost_pivot = sqrt((max|d|+min|d|)*max|d|/2) over all
+//    rows' |diagonal| (Petsc_Tools.F90:960-985, 1046-1056);
+//  * the rhs is lifted: b = rhs - A*(rhs on ghost nodes), b = 0 on ghost rows
+//    (Solvers.F90:1072-1104);
+//  * the initial guess is x on active rows and 0 on ghost rows, or 0 with
+//    start_from_zero (Solvers.F90:1648-1655);
+//  * after the solve ghost nodes take their rhs value (Petsc_Tools.F90:726-730).
+// Ghost entries of every Krylov vector stay exactly zero (b and the guess are
+// zero there and the ghost rows are diagonal), so the original CSR values are
+// used unchanged: ghost columns multiply zeros and ghost rows are replaced by
+// pivot * x.
+//
+// The Krylov methods restate PETSc's KSPCG (symmetric variant) and KSPGMRES
+// (left preconditioning, classical Gram-Schmidt without refinement, Givens
+// rotations, happy-breakdown tolerance 1e-30), with PCJACOBI and the default
+// convergence test KSPConvergedDefault on the preconditioned residual norm.
+// All scalars live on the device; reductions use a fixed block partition and
+// a fixed summation tree, so results are deterministic run to run.
+#include <cmath>
+#include <vector>
+
+#include "fl_internal.cuh"
+#include "fl_device.cuh"
+
+namespace fl {
+
+unsigned long long launches_krylov() { return unit_launches(); }
+
+constexpr int kThreads = 256;
+constexpr int kMaxRestart = 64;
+
+// Device-resident solver state (one per solve).
+struct KspState {
+  // convergence test (KSPConvergedDefault)
+  double rtol, atol, dtol, rnorm0, ttol, snorm_b;
+  double rnorm;          // last residual norm tested
+  int its, max_its, reason, done, guess_zero;
+  // CG scalars
+  double beta, betaold, dpi, dpiold, alpha, pcoef;
+  // ghost pivot reduction
+  double mind, maxd, pivot;
+  // GMRES
+  int it;                // inner index of the current cycle
+  int hapend;
+  double grs[kMaxRestart + 2];
+  double cc[kMaxRestart + 1], ss[kMaxRestart + 1];
+  double hh[(kMaxRestart + 1) * (kMaxRestart + 1)];   // column-major, ld = restart+1
+  double lhh[kMaxRestart + 1];                        // current Gram-Schmidt coefficients
+  double nrs[kMaxRestart + 1];
+  double tt;
+  // true residual report
+  double true_r2, b2;
+};
+
+// Workspace cached on a mesh handle (grow-only).
+struct KrylovWork {
+  DevBuf<double> b, y, r, z, p, w, w2, dinv, part;
+  DevBuf<double> V;     // (restart+1) * N for GMRES
+  DevBuf<float> val32;  // fp32 copy of the matrix (mixed precision)
+  DevBuf<float> r32, z32, p32, w32, d32, dinv32;
+  DevBuf<KspState> st;
+};
+
+static KrylovWork* work_of(fl_mesh_t* m);
+
+// ------------------------------------------------------------ utilities --
+template <int THREADS>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = lane < THREADS / 32 ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+// Sum of `n` partials in a fixed order by one block.
+__device__ double reduce_partials(const double* __restrict__ part, int n, double* red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) s += part[i];
+  return block_sum<kThreads>(s, red);
+}
+
+// KSPConvergedDefault for iteration `it` with residual norm rn.
+__device__ void converged_test(KspState& S, int it, double rn) {
+  if (it == 0) {
+    if (!S.guess_zero) {
+      double sn = S.snorm_b;
+      if (sn == 0.0) sn = rn;
+      S.rnorm0 = sn;
+    } else {
+      S.rnorm0 = rn;
+    }
+    S.ttol = fmax(S.rtol * S.rnorm0, S.atol);
+  }
+  S.rnorm = rn;
+  if (rn != rn) S.reason = FL_DIVERGED_NANORINF;
+  else if (rn <= S.ttol) S.reason = rn < S.atol ? FL_CONVERGED_ATOL : FL_CONVERGED_RTOL;
+  else if (rn >= S.dtol * S.rnorm0) S.reason = FL_DIVERGED_DTOL;
+  if (S.reason) S.done = 1;
+}
+
+// Rows handled by a group of G lanes; the group reduces with shuffles.  All
+// 32 lanes of the warp must call it together (rows past the end pass
+// valid = false and contribute nothing).
+template <int G>
+__device__ __forceinline__ double row_dot(const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
+                                          const double* __restrict__ val, const double* __restrict__ x,
+                                          int row, int sub, bool valid = true) {
+  int b = 0, e = 0;
+  if (valid) {
+    b = __ldg(findrm + row);
+    e = __ldg(findrm + row + 1);
+  }
+  double s = 0.0;
+  for (int k = b + sub; k < e; k += G) s += __ldg(val + k) * __ldg(x + __ldg(colm + k));
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+struct SpArgs {
+  int32_t n;
+  const int32_t* findrm;
+  const int32_t* colm;
+  const double* val;
+  const uint8_t* ghost;  // may be null
+  KspState* st;
+};
+
+// ---------------------------------------------------------------- setup --
+// diag / ghost pivot inputs: min and max of |diag| over all rows.
+__global__ void k_diag(SpArgs A, const int32_t* __restrict__ centrm, double* __restrict__ dinv,
+                       double* __restrict__ part_min, double* __restrict__ part_max) {
+  note_launch();
+  __shared__ double rmin[kThreads / 32], rmax[kThreads / 32];
+  double mn = HUGE_VAL, mx = -HUGE_VAL;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += gridDim.x * blockDim.x) {
+    const int c = centrm[i];
+    const double d = c >= 0 ? A.val[c] : 0.0;
+    dinv[i] = d;  // raw diagonal; inverted once the pivot is known
+    mn = fmin(mn, fabs(d));
+    mx = fmax(mx, fabs(d));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    rmin[w] = mn;
+    rmax[w] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < kThreads / 32; ++k) {
+      mn = fmin(mn, rmin[k]);
+      mx = fmax(mx, rmax[k]);
+    }
+    part_min[blockIdx.x] = fmin(rmin[0], mn);
+    part_max[blockIdx.x] = fmax(rmax[0], mx);
+  }
+}
+
+__global__ void k_pivot(KspState* st, const double* __restrict__ pmin, const double* __restrict__ pmax, int nb) {
+  note_launch();
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double mn = HUGE_VAL, mx = -HUGE_VAL;
+    for (int k = 0; k < nb; ++k) {
+      mn = fmin(mn, pmin[k]);
+      mx = fmax(mx, pmax[k]);
+    }
+    st->mind = mn;
+    st->maxd = mx;
+    st->pivot = sqrt((mx + mn) * mx / 2.0);
+  }
+}
+
+// PCJACOBI inverse diagonal (ghost rows: the pivot; a zero diagonal acts as 1,
+// as PCSetUp_Jacobi does).
+__global__ void k_dinv(int n, const uint8_t* __restrict__ ghost, const KspState* st, double* __restrict__ dinv,
+                       float* __restrict__ dinv32) {
+  note_launch();
+  const double piv = st->pivot;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = (ghost && ghost[i]) ? piv : dinv[i];
+    double v = d != 0.0 ? 1.0 / d : 1.0;
+    dinv[i] = v;
+    if (dinv32) dinv32[i] = (float)v;
+  }
+}
+
+// b = rhs - A*(rhs on ghosts) on active rows, 0 on ghost rows; y = guess.
+template <int G>
+__global__ void k_lift(SpArgs A, const double* __restrict__ rhs, const double* __restrict__ x0, int guess_zero,
+                       double* __restrict__ b, double* __restrict__ y) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    const bool valid = row < A.n;
+    const bool g = valid && A.ghost && A.ghost[row];
+    double s = 0.0;
+    if (A.ghost) {
+      int bb = 0, e = 0;
+      if (valid) {
+        bb = __ldg(A.findrm + row);
+        e = __ldg(A.findrm + row + 1);
+      }
+      for (int k = bb + sub; k < e; k += G) {
+        const int j = __ldg(A.colm + k);
+        if (A.ghost[j]) s += A.val[k] * rhs[j];
+      }
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    }
+    if (valid && sub == 0) {
+      b[row] = g ? 0.0 : rhs[row] - s;
+      y[row] = (guess_zero || g) ? 0.0 : x0[row];
+    }
+  }
+}
+
+// out = op(y) where op is the ghost-masked operator; optional fused epilogues.
+// mode 0: r = b - A y, z = dinv*r, partials of z.z and of (dinv b).(dinv b)
+template <int G>
+__global__ void k_init_resid(SpArgs A, const double* __restrict__ b, const double* __restrict__ y,
+                             const double* __restrict__ dinv, double* __restrict__ r, double* __restrict__ z,
+                             double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  double zz = 0.0, bb = 0.0, zr = 0.0;
+  const double piv = A.st->pivot;
+  const bool gz = A.st->guess_zero;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double ay = 0.0;
+    if (!gz) ay = row_dot<G>(A.findrm, A.colm, A.val, y, row, sub, row < A.n);
+    if (row < A.n && sub == 0) {
+      if (A.ghost && A.ghost[row]) ay = piv * y[row];
+      const double ri = b[row] - ay;
+      const double zi = ri * dinv[row];
+      const double bi = b[row] * dinv[row];
+      r[row] = ri;
+      z[row] = zi;
+      zz += zi * zi;
+      bb += bi * bi;
+      zr += zi * ri;
+    }
+  }
+  zz = block_sum<kThreads>(zz, red);
+  bb = block_sum<kThreads>(bb, red);
+  zr = block_sum<kThreads>(zr, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = zz;
+    part[nparts + blockIdx.x] = bb;
+    part[2 * nparts + blockIdx.x] = zr;
+  }
+}
+
+__global__ void k_cg_start(KspState* st, const double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double zz = reduce_partials(part, nparts, red);
+  const double bb = reduce_partials(part + nparts, nparts, red);
+  const double zr = reduce_partials(part + 2 * nparts, nparts, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    S.snorm_b = sqrt(bb);
+    S.its = 0;
+    S.reason = 0;
+    S.done = 0;
+    converged_test(S, 0, sqrt(zz));
+    S.beta = zr;
+    S.betaold = 0.0;
+    S.dpi = 0.0;
+  }
+}
+
+// ------------------------------------------------------------------- CG --
+// One CG iteration i (KSPSolve_CG):
+//   checks on beta; p = z (i == 0) or z + (beta/betaold) p;
+//   w = A p; dpi = p.w; a = beta/dpi; x += a p; r -= a w; z = B r;
+//   dp = ||z||; test; beta = z.r
+__global__ void k_cg_pcheck(KspState* st, int i) {
+  note_launch();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  KspState& S = *st;
+  if (S.done) return;
+  S.its = i + 1;
+  if (S.beta == 0.0) {
+    S.reason = FL_CONVERGED_ATOL;
+    S.done = 1;
+  } else if (i > 0 && S.beta * S.betaold < 0.0) {
+    S.reason = FL_DIVERGED_INDEFINITE_PC;
+    S.done = 1;
+  }
+}
+
+// p update fused into the SpMV: every gathered p_j is formed as
+// z_j + bcoef*p_j on the fly and the row's own p_i is written back.
+template <int G>
+__global__ void k_cg_spmv(SpArgs A, const double* __restrict__ z, double* __restrict__ p, const double* pold,
+                          double* __restrict__ w, double* __restrict__ part, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const KspState* S = A.st;
+  if (S->done) return;
+  const double bcoef = i == 0 ? 0.0 : S->beta / S->betaold;
+  const double piv = S->pivot;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  double pw = 0.0;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double s = 0.0;
+    if (row < A.n) {
+      const int b = __ldg(A.findrm + row), e = __ldg(A.findrm + row + 1);
+      for (int k = b + sub; k < e; k += G) {
+        const int j = __ldg(A.colm + k);
+        const double pj = i == 0 ? z[j] : z[j] + bcoef * pold[j];
+        s += __ldg(A.val + k) * pj;
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    if (row < A.n && sub == 0) {
+      const double pi = i == 0 ? z[row] : z[row] + bcoef * pold[row];
+      if (A.ghost && A.ghost[row]) s = piv * pi;
+      p[row] = pi;
+      w[row] = s;
+      pw += pi * s;
+    }
+  }
+  pw = block_sum<kThreads>(pw, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = pw;
+}
+
+__global__ void k_cg_alpha(KspState* st, const double* __restrict__ part, int nparts, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double dpi = reduce_partials(part, nparts, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    S.dpiold = S.dpi;
+    S.dpi = dpi;
+    S.betaold = S.beta;
+    if (dpi == 0.0 || (i > 0 && dpi * S.dpiold <= 0.0)) {
+      S.reason = FL_DIVERGED_INDEFINITE_MAT;
+      S.done = 1;
+    } else {
+      S.alpha = S.beta / dpi;
+    }
+  }
+}
+
+__global__ void k_cg_update(int n, KspState* st, const double* __restrict__ p, const double* __restrict__ w,
+                            const double* __restrict__ dinv, double* __restrict__ y, double* __restrict__ r,
+                            double* __restrict__ z, double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double a = st->alpha;
+  double zz = 0.0, zr = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    y[i] += a * p[i];
+    const double ri = r[i] - a * w[i];
+    const double zi = ri * dinv[i];
+    r[i] = ri;
+    z[i] = zi;
+    zz += zi * zi;
+    zr += zi * ri;
+  }
+  zz = block_sum<kThreads>(zz, red);
+  zr = block_sum<kThreads>(zr, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = zz;
+    part[nparts + blockIdx.x] = zr;
+  }
+}
+
+__global__ void k_cg_test(KspState* st, const double* __restrict__ part, int nparts, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double zz = reduce_partials(part, nparts, red);
+  const double zr = reduce_partials(part + nparts, nparts, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    converged_test(S, i + 1, sqrt(zz));
+    if (!S.done) {
+      S.beta = zr;
+      if (i + 1 >= S.max_its) {
+        S.reason = FL_DIVERGED_ITS;
+        S.done = 1;
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- GMRES --
+// v_out = B (A v_in) -- KSP_PCApplyBAorAB with left preconditioning.
+template <int G>
+__global__ void k_apply_BA(SpArgs A, const double* __restrict__ dinv, const double* __restrict__ vin,
+                           double* __restrict__ vout) {
+  note_launch();
+  if (A.st->done) return;
+  const double piv = A.st->pivot;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double s = 0.0;
+    s = row_dot<G>(A.findrm, A.colm, A.val, vin, row, sub, row < A.n);
+    if (row < A.n && sub == 0) {
+      if (A.ghost && A.ghost[row]) s = piv * vin[row];
+      vout[row] = s * dinv[row];
+    }
+  }
+}
+
+// Partials of v_new . v_j for j = 0..it (VecMDot in classical Gram-Schmidt).
+__global__ void k_mdot(int n, const KspState* st, const double* __restrict__ V, int64_t ld, int it,
+                       double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double* vn = V + (int64_t)(it + 1) * ld;
+  for (int j = 0; j <= it; ++j) {
+    const double* vj = V + (int64_t)j * ld;
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += vn[i] * vj[i];
+    s = block_sum<kThreads>(s, red);
+    if (threadIdx.x == 0) part[(int64_t)j * nparts + blockIdx.x] = s;
+  }
+}
+
+__global__ void k_gs_coeffs(KspState* st, const double* __restrict__ part, int nparts, int it) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  for (int j = 0; j <= it; ++j) {
+    const double h = reduce_partials(part + (int64_t)j * nparts, nparts, red);
+    if (threadIdx.x == 0) st->lhh[j] = h;
+  }
+}
+
+// v_new -= sum_j h_j v_j (VecMAXPY), partial of ||v_new||^2.
+__global__ void k_gs_update(int n, const KspState* st, double* __restrict__ V, int64_t ld, int it,
+                            double* __restrict__ part) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  double* vn = V + (int64_t)(it + 1) * ld;
+  double nn = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = vn[i];
+    for (int j = 0; j <= it; ++j) s -= st->lhh[j] * V[(int64_t)j * ld + i];
+    vn[i] = s;
+    nn += s * s;
+  }
+  nn = block_sum<kThreads>(nn, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = nn;
+}
+
+// VecNormalize, Hessenberg column, happy breakdown, KSPGMRESUpdateHessenberg,
+// convergence test (KSPGMRESCycle body after the orthogonalisation).
+__global__ void k_gmres_step(KspState* st, const double* __restrict__ part, int nparts, int it, int restart) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double nn = reduce_partials(part, nparts, red);
+  if (threadIdx.x != 0) return;
+  KspState& S = *st;
+  const int ld = restart + 1;
+  auto HH = [&](int i, int j) -> double& { return S.hh[j * ld + i]; };
+  const double tt = sqrt(nn);
+  S.tt = tt;
+  for (int j = 0; j <= it; ++j) HH(j, it) = S.lhh[j];
+  HH(it + 1, it) = tt;
+  double hapbnd = fabs(tt / S.grs[it]);
+  if (hapbnd > 1e-30) hapbnd = 1e-30;
+  const bool hapend = tt < hapbnd;
+  for (int j = 1; j <= it; ++j) {
+    const double h0 = HH(j - 1, it), h1 = HH(j, it);
+    HH(j - 1, it) = S.cc[j - 1] * h0 + S.ss[j - 1] * h1;
+    HH(j, it) = S.cc[j - 1] * h1 - S.ss[j - 1] * h0;
+  }
+  double res;
+  if (!hapend) {
+    const double h0 = HH(it, it), h1 = HH(it + 1, it);
+    const double rr = sqrt(h0 * h0 + h1 * h1);
+    if (rr == 0.0) {
+      S.reason = FL_DIVERGED_NULL;
+      S.done = 1;
+      S.it = it;  // this column is not used
+      return;
+    }
+    S.cc[it] = h0 / rr;
+    S.ss[it] = h1 / rr;
+    S.grs[it + 1] = -(S.ss[it] * S.grs[it]);
+    S.grs[it] = S.cc[it] * S.grs[it];
+    HH(it, it) = S.cc[it] * h0 + S.ss[it] * h1;
+    res = fabs(S.grs[it + 1]);
+  } else {
+    res = 0.0;
+  }
+  S.it = it + 1;
+  S.its += 1;
+  converged_test(S, S.its, res);
+  if (hapend && !S.reason) {
+    S.reason = FL_DIVERGED_BREAKDOWN;
+    S.done = 1;
+  }
+  if (!S.done && S.its >= S.max_its) {
+    S.reason = FL_DIVERGED_ITS;  // KSPSolve_GMRES: itcount >= max_it
+    S.done = 1;
+  }
+}
+
+__global__ void k_scale_vec(int n, const KspState* st, double* __restrict__ v) {
+  note_launch();
+  const double tt = st->tt;
+  if (tt == 0.0) return;
+  const double inv = 1.0 / tt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] *= inv;
+}
+
+// Cycle start: res = ||v0||, grs(0) = res, test; v0 normalised.
+__global__ void k_gmres_cycle_start(KspState* st, const double* __restrict__ part, int nparts, int first) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double nn = reduce_partials(part, nparts, red);
+  const double bb = reduce_partials(part + nparts, nparts, red);
+  if (threadIdx.x != 0) return;
+  KspState& S = *st;
+  const double res = sqrt(nn);
+  if (first) {
+    S.snorm_b = sqrt(bb);
+    S.its = 0;
+    S.reason = 0;
+    S.done = 0;
+  }
+  S.grs[0] = res;
+  S.it = 0;
+  S.hapend = 0;
+  S.tt = res;
+  if (res == 0.0) {
+    S.reason = FL_CONVERGED_ATOL;
+    S.done = 1;
+    S.rnorm = 0.0;
+    if (first) S.rnorm0 = 0.0;
+    return;
+  }
+  converged_test(S, S.its, res);
+}
+
+// Partials of ||v0||^2 and ||B b||^2 for the cycle start.
+__global__ void k_norm2_pair(int n, const double* __restrict__ v, const double* __restrict__ b,
+                             const double* __restrict__ dinv, double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  double a = 0.0, c = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    a += v[i] * v[i];
+    const double bi = b[i] * dinv[i];
+    c += bi * bi;
+  }
+  a = block_sum<kThreads>(a, red);
+  c = block_sum<kThreads>(c, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = a;
+    part[nparts + blockIdx.x] = c;
+  }
+}
+
+// KSPGMRESBuildSoln: back substitution on the rotated Hessenberg system.
+__global__ void k_gmres_backsolve(KspState* st, int restart) {
+  note_launch();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  KspState& S = *st;
+  const int ld = restart + 1;
+  auto HH = [&](int i, int j) -> double { return S.hh[j * ld + i]; };
+  const int last = S.it - 1;
+  if (last < 0) return;
+  S.nrs[last] = HH(last, last) != 0.0 ? S.grs[last] / HH(last, last) : 0.0;
+  for (int ii = 1; ii <= last; ++ii) {
+    const int k = last - ii;
+    double t = S.grs[k];
+    for (int j = k + 1; j <= last; ++j) t -= HH(k, j) * S.nrs[j];
+    S.nrs[k] = HH(k, k) != 0.0 ? t / HH(k, k) : 0.0;
+  }
+}
+
+__global__ void k_gmres_update_x(int n, const KspState* st, const double* __restrict__ V, int64_t ld,
+                                 double* __restrict__ y) {
+  note_launch();
+  const int last = st->it - 1;
+  if (last < 0) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j <= last; ++j) s += st->nrs[j] * V[(int64_t)j * ld + i];
+    y[i] += s;
+  }
+}
+
+// ------------------------------------------------------------- finalise --
+template <int G>
+__global__ void k_true_resid(SpArgs A, const double* __restrict__ b, const double* __restrict__ y,
+                             double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double piv = A.st->pivot;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  double rr = 0.0, bb = 0.0;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double s = 0.0;
+    s = row_dot<G>(A.findrm, A.colm, A.val, y, row, sub, row < A.n);
+    if (row < A.n && sub == 0) {
+      if (A.ghost && A.ghost[row]) s = piv * y[row];
+      const double ri = b[row] - s;
+      rr += ri * ri;
+      bb += b[row] * b[row];
+    }
+  }
+  rr = block_sum<kThreads>(rr, red);
+  bb = block_sum<kThreads>(bb, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = rr;
+    part[nparts + blockIdx.x] = bb;
+  }
+}
+
+__global__ void k_true_resid_final(KspState* st, const double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double rr = reduce_partials(part, nparts, red);
+  const double bb = reduce_partials(part + nparts, nparts, red);
+  if (threadIdx.x == 0) {
+    st->true_r2 = rr;
+    st->b2 = bb;
+  }
+}
+
+__global__ void k_copy_back(int n, const uint8_t* __restrict__ ghost, const double* __restrict__ rhs,
+                            const double* __restrict__ y, double* __restrict__ x) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = (ghost && ghost[i]) ? rhs[i] : y[i];
+}
+
+// ----------------------------------------------------------- mixed (fp32) --
+// Inner CG in fp32 storage (matrix, vectors) with fp64 dot products, driven
+// by an fp64 iterative-refinement loop on the true residual.
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  note_launch();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+struct SpArgs32 {
+  int32_t n;
+  const int32_t* findrm;
+  const int32_t* colm;
+  const float* val;
+  const uint8_t* ghost;
+};
+
+// Inner CG state lives in KspState fields reused: beta/betaold/dpi/alpha; the
+// inner convergence uses rnorm0 of the inner problem in `ttol`.
+template <int G>
+__global__ void k_cg32_spmv(SpArgs32 A, KspState* st, float piv, const float* __restrict__ z,
+                            float* __restrict__ p, float* __restrict__ w, double* __restrict__ part, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const float bcoef = i == 0 ? 0.0f : (float)(st->beta / st->betaold);
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  double pw = 0.0;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    float s = 0.0f;
+    if (row < A.n) {
+      const int b = __ldg(A.findrm + row), e = __ldg(A.findrm + row + 1);
+      for (int k = b + sub; k < e; k += G) {
+        const int j = __ldg(A.colm + k);
+        const float pj = i == 0 ? z[j] : fmaf(bcoef, p[j], z[j]);
+        s = fmaf(__ldg(A.val + k), pj, s);
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    // p is updated in place only after every gather of this launch: write to w's
+    // partner buffer first (w holds A p), p update happens in k_cg32_update.
+    if (row < A.n && sub == 0) {
+      const float pi = i == 0 ? z[row] : fmaf(bcoef, p[row], z[row]);
+      if (A.ghost && A.ghost[row]) s = piv * pi;
+      w[row] = s;
+      pw += (double)pi * (double)s;
+    }
+  }
+  pw = block_sum<kThreads>(pw, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = pw;
+}
+
+__global__ void k_cg32_update(int n, KspState* st, const float* __restrict__ z_in, float* __restrict__ p,
+                              const float* __restrict__ w, const float* __restrict__ dinv,
+                              float* __restrict__ d, float* __restrict__ r, float* __restrict__ z,
+                              double* __restrict__ part, int nparts, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const float bcoef = (float)st->pcoef;
+  const float a = (float)st->alpha;
+  double zz = 0.0, zr = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float pk = i == 0 ? z_in[k] : fmaf(bcoef, p[k], z_in[k]);
+    p[k] = pk;
+    d[k] = fmaf(a, pk, d[k]);
+    const float rk = fmaf(-a, w[k], r[k]);
+    const float zk = rk * dinv[k];
+    r[k] = rk;
+    z[k] = zk;
+    zz += (double)zk * zk;
+    zr += (double)zk * rk;
+  }
+  zz = block_sum<kThreads>(zz, red);
+  zr = block_sum<kThreads>(zr, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = zz;
+    part[nparts + blockIdx.x] = zr;
+  }
+}
+
+__global__ void k_cg32_alpha(KspState* st, const double* __restrict__ part, int nparts, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double dpi = reduce_partials(part, nparts, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    S.pcoef = i == 0 ? 0.0 : S.beta / S.betaold;
+    S.dpiold = S.dpi;
+    S.dpi = dpi;
+    S.betaold = S.beta;
+    if (dpi <= 0.0 || dpi != dpi) {
+      S.done = 1;  // inner breakdown: outer loop decides
+      S.reason = FL_DIVERGED_INDEFINITE_MAT;
+    } else {
+      S.alpha = S.beta / dpi;
+    }
+  }
+}
+
+__global__ void k_cg32_test(KspState* st, const double* __restrict__ part, int nparts, int i) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double zz = reduce_partials(part, nparts, red);
+  const double zr = reduce_partials(part + nparts, nparts, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    S.its = i + 1;
+    S.rnorm = sqrt(zz);
+    if (!(S.rnorm == S.rnorm)) {
+      S.reason = FL_DIVERGED_NANORINF;
+      S.done = 1;
+    } else if (S.rnorm <= S.ttol) {
+      S.reason = FL_CONVERGED_RTOL;
+      S.done = 1;
+    } else {
+      S.beta = zr;
+      if (i + 1 >= S.max_its) {
+        S.reason = FL_DIVERGED_ITS;
+        S.done = 1;
+      }
+    }
+  }
+}
+
+// Outer residual in fp64: r = b - A y; z = B r; and fp32 copies for the inner
+// solve (r32 = z-scaled residual, z32 = B r32).  Partials ||Br||^2, ||Bb||^2, (Br).r
+template <int G>
+__global__ void k_outer_resid(SpArgs A, const double* __restrict__ b, const double* __restrict__ y,
+                              const double* __restrict__ dinv, float* __restrict__ r32, float* __restrict__ z32,
+                              float* __restrict__ d32, double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double piv = A.st->pivot;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  double zz = 0.0, bb = 0.0, zr = 0.0;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double s = 0.0;
+    s = row_dot<G>(A.findrm, A.colm, A.val, y, row, sub, row < A.n);
+    if (row < A.n && sub == 0) {
+      if (A.ghost && A.ghost[row]) s = piv * y[row];
+      const double ri = b[row] - s;
+      const double zi = ri * dinv[row];
+      const double bi = b[row] * dinv[row];
+      r32[row] = (float)ri;
+      z32[row] = (float)zi;
+      d32[row] = 0.0f;
+      zz += zi * zi;
+      bb += bi * bi;
+      zr += zi * ri;
+    }
+  }
+  zz = block_sum<kThreads>(zz, red);
+  bb = block_sum<kThreads>(bb, red);
+  zr = block_sum<kThreads>(zr, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = zz;
+    part[nparts + blockIdx.x] = bb;
+    part[2 * nparts + blockIdx.x] = zr;
+  }
+}
+
+__global__ void k_add_correction(int n, const float* __restrict__ d, double* __restrict__ y) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] += (double)d[i];
+}
+
+// ------------------------------------------------------------------ host --
+struct Launch {
+  unsigned grid;
+  int nparts;
+};
+
+static int group_for(const fl_mesh_t* m) {
+  const double avg = (double)m->nnz / (double)(m->N > 0 ? m->N : 1);
+  if (avg > 24) return 8;
+  return 4;
+}
+
+#define FL_SPMV_DISPATCH(G, KERNEL, ...)                                            \
+  do {                                                                             \
+    if ((G) == 8) KERNEL<8><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                 \
+    else KERNEL<4><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
+  } while (0)
+
+int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost, const double* rhs,
+          double* x, fl_solve_report* rep, cudaStream_t s) {
+  FL_CHECK_ARG(m && o && val && rhs && x && rep, "null argument");
+  FL_CHECK_ARG(o->ksp_type == 0 || o->ksp_type == 1, "ksp_type must be 0 (cg) or 1 (gmres)");
+  FL_CHECK_ARG(o->max_its >= 0, "max_its");
+  const int restart = o->restart > 0 ? o->restart : 30;
+  FL_CHECK_ARG(restart <= kMaxRestart, "gmres restart above 64");
+  FL_CHECK_ARG(o->precision == 0 || o->ksp_type == 0, "mixed precision is a CG refinement");
+  KrylovWork* W = work_of(m);
+  if (!W) return FL_ERR_NOMEM;
+  const int n = m->N;
+  const int G = group_for(m);
+  const unsigned gsp = grid_for((int64_t)n * G, kThreads, 8);
+  const unsigned gv = grid_for(n, kThreads, 8);
+  const int np = (int)std::max(gsp, gv);
+  FL_TRY(W->b.reserve(n));
+  FL_TRY(W->y.reserve(n));
+  FL_TRY(W->r.reserve(n));
+  FL_TRY(W->z.reserve(n));
+  FL_TRY(W->p.reserve(n));
+  FL_TRY(W->w.reserve(n));
+  FL_TRY(W->dinv.reserve(n));
+  FL_TRY(W->part.reserve((size_t)np * (kMaxRestart + 2)));
+  FL_TRY(W->st.reserve(1));
+  KspState h{};
+  h.rtol = o->rtol;
+  h.atol = o->atol;
+  h.dtol = o->dtol > 0 ? o->dtol : 1e5;
+  h.max_its = o->max_its;
+  h.guess_zero = o->start_from_zero ? 1 : 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(W->st.p, &h, sizeof(KspState), cudaMemcpyHostToDevice, s));
+  KspState* st = W->st.p;
+  SpArgs A{n, m->findrm.p, m->colm.p, val, ghost, st};
+
+  // Jacobi diagonal and ghost pivot
+  k_diag<<<gv, kThreads, 0, s>>>(A, m->centrm.p, W->dinv.p, W->part.p, W->part.p + np);
+  k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + np, (int)gv);
+  const bool mixed = o->precision == 1;
+  if (mixed) FL_TRY(W->dinv32.reserve(n));
+  k_dinv<<<gv, kThreads, 0, s>>>(n, ghost, st, W->dinv.p, mixed ? W->dinv32.p : nullptr);
+  FL_SPMV_DISPATCH(G, k_lift, A, rhs, x, h.guess_zero, W->b.p, W->y.p);
+  FL_TRY_CUDA(cudaGetLastError());
+
+  int outer = 0;
+  const int chunk = 16;
+  if (!mixed && o->ksp_type == 0) {
+    FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
+    k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
+    FL_TRY_CUDA(cudaGetLastError());
+    // p and w double-buffer through (p, w) and (w, p): the fused SpMV reads the
+    // old p while writing the new one, so they alternate between two arrays.
+    double* pbuf[2] = {W->p.p, W->w.p};
+    FL_TRY(W->w2.reserve(n));
+    double* wv = W->w2.p;
+    for (int i = 0; i < o->max_its; ++i) {
+      double* pnew = pbuf[i & 1];
+      double* pold = pbuf[(i + 1) & 1];
+      k_cg_pcheck<<<1, 32, 0, s>>>(st, i);
+      FL_SPMV_DISPATCH(G, k_cg_spmv, A, W->z.p, pnew, pold, wv, W->part.p, i);
+      k_cg_alpha<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, i);
+      k_cg_update<<<gv, kThreads, 0, s>>>(n, st, pnew, wv, W->dinv.p, W->y.p, W->r.p, W->z.p, W->part.p, (int)gv);
+      k_cg_test<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, i);
+      if ((i + 1) % chunk == 0 || i + 1 == o->max_its) {
+        FL_TRY_CUDA(cudaGetLastError());
+        int done = 0;
+        FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FL_TRY_CUDA(cudaStreamSynchronize(s));
+        if (done) break;
+      }
+    }
+  } else if (!mixed) {
+    // GMRES(restart)
+    const int64_t ld = n;
+    FL_TRY(W->V.reserve((size_t)(restart + 1) * n));
+    double* V = W->V.p;
+    bool first = true;
+    while (true) {
+      // v0 = B (b - A y)   (KSPInitialResidual; zero guess: B b)
+      FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, V, W->part.p, (int)gsp);
+      k_gmres_cycle_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, first ? 1 : 0);
+      k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V);
+      FL_TRY_CUDA(cudaGetLastError());
+      for (int it = 0; it < restart; ++it) {
+        FL_SPMV_DISPATCH(G, k_apply_BA, A, W->dinv.p, V + it * ld, V + (it + 1) * ld);
+        k_mdot<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p, (int)gv);
+        k_gs_coeffs<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it);
+        k_gs_update<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p);
+        k_gmres_step<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it, restart);
+        k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V + (it + 1) * ld);
+        if ((it + 1) % 8 == 0 || it + 1 == restart) {
+          FL_TRY_CUDA(cudaGetLastError());
+          KspState hs;
+          FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+          FL_TRY_CUDA(cudaStreamSynchronize(s));
+          if (hs.done) break;
+        }
+      }
+      k_gmres_backsolve<<<1, 32, 0, s>>>(st, restart);
+      k_gmres_update_x<<<gv, kThreads, 0, s>>>(n, st, V, ld, W->y.p);
+      FL_TRY_CUDA(cudaGetLastError());
+      KspState hs;
+      FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+      FL_TRY_CUDA(cudaStreamSynchronize(s));
+      if (hs.done) break;
+      if (hs.its >= o->max_its) {
+        hs.reason = FL_DIVERGED_ITS;
+        FL_TRY_CUDA(cudaMemcpyAsync(&st->reason, &hs.reason, sizeof(int), cudaMemcpyHostToDevice, s));
+        break;
+      }
+      // restart: KSPInitialResidual with the updated guess
+      int gz = 0;
+      FL_TRY_CUDA(cudaMemcpyAsync(&st->guess_zero, &gz, sizeof(int), cudaMemcpyHostToDevice, s));
+      first = false;
+    }
+  } else {
+    // Mixed precision: fp32 inner CG (rtol inner_rtol) inside fp64 refinement
+    FL_TRY(W->val32.reserve(m->nnz));
+    FL_TRY(W->r32.reserve(n));
+    FL_TRY(W->z32.reserve(n));
+    FL_TRY(W->p32.reserve(n));
+    FL_TRY(W->w32.reserve(n));
+    FL_TRY(W->d32.reserve(n));
+    k_to_f32<<<grid_for(m->nnz, kThreads), kThreads, 0, s>>>(m->nnz, val, W->val32.p);
+    FL_TRY_CUDA(cudaGetLastError());
+    KspState hs;
+    FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+    FL_TRY_CUDA(cudaStreamSynchronize(s));
+    const float piv32 = (float)hs.pivot;
+    SpArgs32 A32{n, m->findrm.p, m->colm.p, W->val32.p, ghost};
+    const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-5;
+    double rnorm0 = 0.0, ttol = 0.0;
+    int total_inner = 0, reason = 0;
+    for (outer = 0; outer < 1000; ++outer) {
+      FL_SPMV_DISPATCH(G, k_outer_resid, A, W->b.p, W->y.p, W->dinv.p, W->r32.p, W->z32.p, W->d32.p, W->part.p,
+                       (int)gsp);
+      k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
+      FL_TRY_CUDA(cudaGetLastError());
+      FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+      FL_TRY_CUDA(cudaStreamSynchronize(s));
+      const double rn = hs.rnorm;
+      if (outer == 0) {
+        rnorm0 = hs.rnorm0;
+        ttol = hs.ttol;
+      }
+      if (rn != rn) { reason = FL_DIVERGED_NANORINF; break; }
+      if (rn <= ttol) { reason = rn < o->atol ? FL_CONVERGED_ATOL : FL_CONVERGED_RTOL; break; }
+      if (total_inner >= o->max_its) { reason = FL_DIVERGED_ITS; break; }
+      // inner solve B A d = B r in fp32 from d = 0 to inner_rtol * ||B r||
+      hs.ttol = inner_rtol * rn;
+      hs.done = 0;
+      hs.reason = 0;
+      hs.dpi = 0.0;
+      hs.its = 0;
+      hs.max_its = o->max_its - total_inner;
+      FL_TRY_CUDA(cudaMemcpyAsync(st, &hs, sizeof(KspState), cudaMemcpyHostToDevice, s));
+      int inner = 0;
+      for (int i = 0; i < hs.max_its; ++i) {
+        FL_SPMV_DISPATCH(G, k_cg32_spmv, A32, st, piv32, W->z32.p, W->p32.p, W->w32.p, W->part.p, i);
+        k_cg32_alpha<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, i);
+        k_cg32_update<<<gv, kThreads, 0, s>>>(n, st, W->z32.p, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p,
+                                               W->r32.p, W->z32.p, W->part.p, (int)gv, i);
+        k_cg32_test<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, i);
+        if ((i + 1) % chunk == 0 || i + 1 == hs.max_its) {
+          FL_TRY_CUDA(cudaGetLastError());
+          KspState h2;
+          FL_TRY_CUDA(cudaMemcpyAsync(&h2, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+          FL_TRY_CUDA(cudaStreamSynchronize(s));
+          inner = h2.its;
+          if (h2.done) break;
+        }
+      }
+      total_inner += inner;
+      k_add_correction<<<gv, kThreads, 0, s>>>(n, W->d32.p, W->y.p);
+      FL_TRY_CUDA(cudaGetLastError());
+    }
+    // report in the outer terms
+    hs.its = total_inner;
+    hs.reason = reason;
+    hs.rnorm0 = rnorm0;
+    FL_TRY_CUDA(cudaMemcpyAsync(&st->its, &hs.its, sizeof(int), cudaMemcpyHostToDevice, s));
+    FL_TRY_CUDA(cudaMemcpyAsync(&st->reason, &hs.reason, sizeof(int), cudaMemcpyHostToDevice, s));
+    FL_TRY_CUDA(cudaMemcpyAsync(&st->rnorm0, &hs.rnorm0, sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  FL_SPMV_DISPATCH(G, k_true_resid, A, W->b.p, W->y.p, W->part.p, (int)gsp);
+  k_true_resid_final<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
+  k_copy_back<<<gv, kThreads, 0, s>>>(n, ghost, rhs, W->y.p, x);
+  FL_TRY_CUDA(cudaGetLastError());
+  KspState hs;
+  FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  rep->iterations = hs.its;
+  rep->reason = hs.reason ? hs.reason : (o->max_its == 0 ? FL_DIVERGED_ITS : 0);
+  rep->final_rnorm = hs.rnorm;
+  rep->rnorm0 = hs.rnorm0;
+  rep->true_rel_residual = hs.b2 > 0 ? sqrt(hs.true_r2 / hs.b2) : sqrt(hs.true_r2);
+  rep->outer_iterations = outer;
+  rep->pad = 0;
+  return FL_OK;
+}
+
+// Cached workspace per mesh handle.
+struct WorkRegistry {
+  std::vector<std::pair<fl_mesh_t*, KrylovWork*>> v;
+} g_work;
+
+static KrylovWork* work_of(fl_mesh_t* m) {
+  for (auto& e : g_work.v)
+    if (e.first == m) return e.second;
+  KrylovWork* w = new KrylovWork();
+  g_work.v.push_back({m, w});
+  return w;
+}
+
+void release_krylov_work(fl_mesh_t* m) {
+  for (size_t i = 0; i < g_work.v.size(); ++i)
+    if (g_work.v[i].first == m) {
+      delete g_work.v[i].second;
+      g_work.v.erase(g_work.v.begin() + i);
+      return;
+    }
+}
+
+template <int G>
+__global__ void k_spmv_plain(SpArgs A, const double* __restrict__ x, double* __restrict__ y) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double s = 0.0;
+    s = row_dot<G>(A.findrm, A.colm, A.val, x, row, sub, row < A.n);
+    if (row < A.n && sub == 0) y[row] = s;
+  }
+}
+
+int csr_mult(fl_mesh_t* m, const double* val, const double* x, double* y, cudaStream_t s) {
+  const int G = group_for(m);
+  const unsigned gsp = grid_for((int64_t)m->N * G, kThreads, 8);
+  SpArgs A{m->N, m->findrm.p, m->colm.p, val, nullptr, nullptr};
+  FL_SPMV_DISPATCH(G, k_spmv_plain, A, x, y);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
+}  // namespace fl
+
+using namespace fl;
+
+extern "C" int fl_dev_petsc_solve(fl_mesh m, const fl_solver_opts* o, const double* val, const uint8_t* inactive,
+                                  const double* rhs, double* x, fl_solve_report* rep, void* stream) {
+  FL_CHECK_ARG(m, "null mesh");
+  cudaStream_t s = stream ? (cudaStream_t)stream : m->stream;
+  return solve(m, o, val, inactive, rhs, x, rep, s);
+}
+
+extern "C" int fl_gpu_petsc_solve(fl_mesh m, const fl_solver_opts* o, const double* val, const uint8_t* inactive,
+                                  const double* rhs, double* x, fl_solve_report* rep) {
+  FL_CHECK_ARG(m && o && val && rhs && x && rep, "null argument");
+  cudaStream_t s = m->stream;
+  FL_TRY(m->st_val.reserve(m->nnz));
+  FL_TRY(m->st_rhs.reserve(m->N));
+  FL_TRY(m->st_x.reserve(m->N));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_val.p, val, sizeof(double) * m->nnz, cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_rhs.p, rhs, sizeof(double) * m->N, cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_x.p, x, sizeof(double) * m->N, cudaMemcpyHostToDevice, s));
+  const uint8_t* ip = nullptr;
+  if (inactive) {
+    FL_TRY(m->st_ina.reserve(m->N));
+    FL_TRY_CUDA(cudaMemcpyAsync(m->st_ina.p, inactive, m->N, cudaMemcpyHostToDevice, s));
+    ip = m->st_ina.p;
+  }
+  FL_TRY(solve(m, o, m->st_val.p, ip, m->st_rhs.p, m->st_x.p, rep, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(x, m->st_x.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  return FL_OK;
+}
+
+extern "C" int fl_dev_csr_mult(fl_mesh m, const double* val, const double* x, double* y, void* stream) {
+  FL_CHECK_ARG(m && val && x && y, "null argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : m->stream;
+  return csr_mult(m, val, x, y, s);
+}

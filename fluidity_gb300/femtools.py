@@ -1,0 +1,278 @@
+"""Python mirror of Fluidity's CG hot-path interface, backed by the CUDA library.
+
+Names and argument meanings follow the reference routines they replace:
+
+==============================  ================================================
+this module                     reference
+==============================  ================================================
+``Mesh``                        ``mesh_type`` + coordinate ``vector_field``
+``make_sparsity``               ``get_csr_sparsity_firstorder`` ->
+                                ``make_sparsity`` (Sparsity_Patterns.F90:47)
+``get_mesh_colouring``          ``get_mesh_colouring(..., COLOURING_CG1, ...)``
+                                (Colouring.F90:85)
+``make_global_numbering_p2``    ``make_global_numbering`` (Global_Numbering.F90:291)
+``assemble_advection_diffusion_cg``  Advection_Diffusion_CG.F90:228
+``apply_dirichlet_conditions``  Boundary_Conditions.F90:1983
+``petsc_solve``                 Solvers.F90:111 (petsc_solve_scalar)
+``solve_field_equation_cg``     Advection_Diffusion_CG.F90:127
+==============================  ================================================
+
+Arrays are numpy (host, copied through the ``fl_gpu_*`` entry points) or torch
+CUDA tensors (device-resident, ``fl_dev_*`` entry points).  Indices are 0-based.
+Every call runs on the GPU; a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import AdvDifParams, Fields, MeshDesc, SolveReport, SolverOpts, check
+
+
+def _ptr(a):
+    """Data pointer of a numpy array or torch tensor (None passes through)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+def _is_device(a) -> bool:
+    return a is not None and not isinstance(a, np.ndarray)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return getattr(stream, "cuda_stream", stream)
+
+
+@dataclass
+class CsrSparsity:
+    """csr_sparsity (Sparse_Tools.F90:48-111), 0-based; centrm = -1 if no diagonal."""
+    findrm: np.ndarray
+    colm: np.ndarray
+    centrm: np.ndarray
+
+    @property
+    def nnz(self) -> int:
+        return int(self.colm.size)
+
+
+class Mesh:
+    """A field mesh registered on the GPU with its coordinate (P1) mesh.
+
+    ``ndglno`` (E, loc) and ``x_ndglno`` (E, 4) are element-major connectivities,
+    ``coords`` is (Nx, 3).  Registration builds the sparsity and the CG1
+    colouring on the device and caches them, as the reference caches them in
+    state / on the topology mesh.
+    """
+
+    def __init__(self, ndglno, coords, x_ndglno=None, nodes=None, index_base=0):
+        self.lib = _lib.load()
+        nd = np.ascontiguousarray(ndglno, dtype=np.int32)
+        self.E, self.loc = nd.shape
+        xnd = nd if x_ndglno is None else np.ascontiguousarray(x_ndglno, dtype=np.int32)
+        X = np.ascontiguousarray(coords, dtype=np.float64)
+        self.N = int(nodes if nodes is not None else nd.max() + 1 - index_base)
+        self.Nx = int(X.shape[0])
+        d = MeshDesc(self.N, self.E, self.loc, index_base, nd.ctypes.data, self.Nx,
+                     xnd.ctypes.data, X.ctypes.data)
+        h = C.c_void_p()
+        check(self.lib.fl_gpu_mesh_register(C.byref(d), C.byref(h)), "fl_gpu_mesh_register")
+        self.handle = h
+        nnz, ncol = C.c_int64(), C.c_int32()
+        check(self.lib.fl_gpu_mesh_info(h, C.byref(nnz), C.byref(ncol)), "fl_gpu_mesh_info")
+        self.nnz, self.ncolours = nnz.value, ncol.value
+        self._sparsity = None
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.fl_gpu_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sparsity(self) -> CsrSparsity:
+        if self._sparsity is None:
+            f = np.empty(self.N + 1, dtype=np.int32)
+            c = np.empty(self.nnz, dtype=np.int32)
+            d = np.empty(self.N, dtype=np.int32)
+            check(self.lib.fl_gpu_sparsity_copy(self.handle, _ptr(f), _ptr(c), _ptr(d), 0),
+                  "fl_gpu_sparsity_copy")
+            self._sparsity = CsrSparsity(f, c, d)
+        return self._sparsity
+
+    def colouring(self):
+        """(colour per element 1-based, colour_ptr (ncol+1), colour_elems)."""
+        col = np.empty(self.E, dtype=np.int32)
+        ptr = np.empty(self.ncolours + 1, dtype=np.int32)
+        el = np.empty(self.E, dtype=np.int32)
+        check(self.lib.fl_gpu_colouring_copy(self.handle, _ptr(col), _ptr(ptr), _ptr(el), 0),
+              "fl_gpu_colouring_copy")
+        return col, ptr, el
+
+
+def make_sparsity(mesh: Mesh) -> CsrSparsity:
+    """First-order sparsity of the mesh (get_csr_sparsity_firstorder)."""
+    return mesh.sparsity()
+
+
+def get_mesh_colouring(mesh: Mesh):
+    """COLOURING_CG1 colour sets: list of ascending element arrays."""
+    _, ptr, el = mesh.colouring()
+    return [el[ptr[c]:ptr[c + 1]] for c in range(mesh.ncolours)]
+
+
+def make_global_numbering_p2(ndglno_p1, nvert: int | None = None):
+    """P2 connectivity (E, 10) and node count derived from a P1 tet mesh."""
+    lib = _lib.load()
+    nd = np.ascontiguousarray(ndglno_p1, dtype=np.int32)
+    E = nd.shape[0]
+    nv = int(nvert if nvert is not None else nd.max() + 1)
+    out = np.empty((E, 10), dtype=np.int32)
+    n2 = C.c_int32()
+    check(lib.fl_gpu_make_global_numbering_p2(nv, E, _ptr(nd), 0, _ptr(out), C.byref(n2)),
+          "fl_gpu_make_global_numbering_p2")
+    return out, n2.value
+
+
+def advdif_params(*, theta=1.0, dt=1.0, beta=0.0, have_mass=False, lump_mass=False,
+                  have_advection=False, diffusivity=None, have_source=False,
+                  have_absorption=False, quad_degree=2) -> AdvDifParams:
+    """The options assemble_advection_diffusion_cg reads (Advection_Diffusion_CG.F90:384-465)."""
+    p = AdvDifParams()
+    p.theta, p.dt, p.beta = theta, dt, beta
+    p.have_mass, p.lump_mass = int(have_mass), int(have_mass and lump_mass)
+    p.have_advection = int(have_advection)
+    p.have_source, p.have_absorption = int(have_source), int(have_absorption)
+    p.quad_degree = quad_degree
+    if diffusivity is None:
+        p.have_diffusivity, p.isotropic_diffusivity = 0, 1
+    else:
+        K = np.asarray(diffusivity, dtype=np.float64)
+        if K.ndim == 0:
+            K = np.eye(3) * float(K)
+        p.have_diffusivity = 1
+        p.isotropic_diffusivity = int(np.array_equal(K, np.eye(3) * K[0, 0]))
+        for k in range(9):
+            p.diffusivity[k] = K.reshape(-1)[k]
+    return p
+
+
+def assemble_advection_diffusion_cg(mesh: Mesh, params: AdvDifParams, *, t=None, velocity=None,
+                                    source=None, absorption=None, val=None, rhs=None, stream=None):
+    """Matrix values (nnz) and rhs (N) of the CG advection-diffusion equation.
+
+    Host numpy fields -> host results through fl_gpu_assemble_advdif_cg; torch
+    CUDA fields -> device results through fl_dev_assemble_advdif_cg.
+    """
+    lib = mesh.lib
+    dev = any(_is_device(a) for a in (t, velocity, source, absorption, val, rhs))
+    if dev:
+        import torch
+        if val is None:
+            val = torch.empty(mesh.nnz, dtype=torch.float64, device="cuda")
+        if rhs is None:
+            rhs = torch.empty(mesh.N, dtype=torch.float64, device="cuda")
+        f = Fields(_ptr(t), _ptr(velocity), _ptr(source), _ptr(absorption))
+        check(lib.fl_dev_assemble_advdif_cg(mesh.handle, C.byref(params), C.byref(f), _ptr(val),
+                                            _ptr(rhs), _stream_ptr(stream)),
+              "fl_dev_assemble_advdif_cg")
+        return val, rhs
+    keep = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None
+            for a in (t, velocity, source, absorption)]
+    f = Fields(*[_ptr(a) for a in keep])
+    val = np.empty(mesh.nnz) if val is None else val
+    rhs = np.empty(mesh.N) if rhs is None else rhs
+    check(lib.fl_gpu_assemble_advdif_cg(mesh.handle, C.byref(params), C.byref(f), _ptr(val),
+                                        _ptr(rhs)), "fl_gpu_assemble_advdif_cg")
+    return val, rhs
+
+
+def apply_dirichlet_conditions(mesh: Mesh, rhs, inactive, nodes, values, t=None, dt=None,
+                               stream=None):
+    """Strong Dirichlet: rows inactive, rhs = (g - t)/dt (or g without dt)."""
+    lib = mesh.lib
+    dtv = float(dt) if dt is not None else 0.0
+    if _is_device(rhs):
+        check(lib.fl_dev_apply_dirichlet(mesh.handle, int(len(nodes)), _ptr(nodes), 0, _ptr(values),
+                                         _ptr(t), C.c_double(dtv), _ptr(rhs), _ptr(inactive),
+                                         _stream_ptr(stream)), "fl_dev_apply_dirichlet")
+        return
+    nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+    values = np.ascontiguousarray(values, dtype=np.float64)
+    tv = np.ascontiguousarray(t, dtype=np.float64) if t is not None else None
+    check(lib.fl_gpu_apply_dirichlet(mesh.handle, int(nodes.size), _ptr(nodes), 0, _ptr(values),
+                                     _ptr(tv), C.c_double(dtv), _ptr(rhs), _ptr(inactive)),
+          "fl_gpu_apply_dirichlet")
+
+
+def solver_options(*, ksp="cg", restart=30, rtol=1e-10, atol=0.0, dtol=1e5, max_its=10000,
+                   start_from_zero=False, precision="fp64", inner_rtol=1e-5) -> SolverOpts:
+    """solver/ options of the field (Solvers.F90:1566-1660); pc is always jacobi."""
+    o = SolverOpts()
+    o.ksp_type = {"cg": 0, "gmres": 1}[ksp]
+    o.restart, o.rtol, o.atol, o.dtol = restart, rtol, atol, dtol
+    o.max_its, o.start_from_zero = max_its, int(start_from_zero)
+    o.precision = {"fp64": 0, "mixed": 1}[precision]
+    o.inner_rtol = inner_rtol
+    return o
+
+
+def petsc_solve(mesh: Mesh, x, val, rhs, options: SolverOpts, inactive=None, stream=None) -> dict:
+    """Solve A x = rhs on the mesh pattern; x holds the guess and receives the solution."""
+    lib = mesh.lib
+    rep = SolveReport()
+    if _is_device(x):
+        check(lib.fl_dev_petsc_solve(mesh.handle, C.byref(options), _ptr(val), _ptr(inactive),
+                                     _ptr(rhs), _ptr(x), C.byref(rep), _stream_ptr(stream)),
+              "fl_dev_petsc_solve")
+    else:
+        v = np.ascontiguousarray(val, dtype=np.float64)
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        ina = np.ascontiguousarray(inactive, dtype=np.uint8) if inactive is not None else None
+        check(lib.fl_gpu_petsc_solve(mesh.handle, C.byref(options), _ptr(v), _ptr(ina), _ptr(b),
+                                     _ptr(x), C.byref(rep)), "fl_gpu_petsc_solve")
+    return {
+        "iterations": rep.iterations, "reason": rep.reason,
+        "reason_name": _lib.REASONS.get(rep.reason, str(rep.reason)),
+        "final_rnorm": rep.final_rnorm, "rnorm0": rep.rnorm0,
+        "true_rel_residual": rep.true_rel_residual, "outer_iterations": rep.outer_iterations,
+    }
+
+
+def csr_mult(mesh: Mesh, val, x, y, stream=None):
+    """y = A x (device tensors)."""
+    check(mesh.lib.fl_dev_csr_mult(mesh.handle, _ptr(val), _ptr(x), _ptr(y), _stream_ptr(stream)),
+          "fl_dev_csr_mult")
+
+
+def solve_field_equation_cg(mesh: Mesh, t, params: AdvDifParams, options: SolverOpts, *,
+                            bc_nodes, bc_values, velocity=None, source=None, absorption=None):
+    """One solve of a CG scalar field in acceleration form (Advection_Diffusion_CG.F90:127-174).
+
+    Assembles (M + theta dt (A + K)) delta_t = rhs, applies strong Dirichlet
+    conditions in rate-of-change form, solves for delta_t with zero initial
+    change and returns (t + dt * delta_t, solve report).  Host numpy arrays.
+    """
+    val, rhs = assemble_advection_diffusion_cg(mesh, params, t=t, velocity=velocity, source=source,
+                                               absorption=absorption)
+    inactive = np.zeros(mesh.N, dtype=np.uint8)
+    apply_dirichlet_conditions(mesh, rhs, inactive, bc_nodes, bc_values, t=t, dt=params.dt)
+    delta = np.zeros(mesh.N)
+    rep = petsc_solve(mesh, delta, val, rhs, options, inactive=inactive)
+    return t + params.dt * delta, rep
+
+
+def kernel_launch_count() -> int:
+    """Kernels this library launched in this process so far (all devices' counters)."""
+    return int(_lib.load().fl_kernel_launch_count())

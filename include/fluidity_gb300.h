@@ -1,0 +1,232 @@
+/* fluidity_gb300.h -- C-ABI of the GB300 (sm_103a) CG assembly + Krylov path.
+ *
+ * Drop-in boundary for Fluidity's continuous-Galerkin scalar hot path:
+ * the element loop of assemble/Advection_Diffusion_CG.F90 (and the P1/P2
+ * pressure Laplacians built by the same kernels), the csr_matrix sparsity and
+ * colouring it uses, strong Dirichlet conditions, and the petsc_solve Krylov
+ * solve on the assembled system.  A Fortran caller binds these entry points
+ * with ISO_C_BINDING (fluidity_gb300/fortran/fl_gpu_bindings.F90) and passes
+ * c_loc() pointers to the arrays it already owns:
+ *
+ *   csr_sparsity  findrm(N+1), colm(nnz), centrm(N)  1-based int32
+ *                 (femtools/Sparse_Tools.F90:48-111)
+ *   csr_matrix    val(nnz) real64, inactive%ptr(N) logical
+ *   scalar_field  val(N) real64
+ *   vector_field  val(3,N) real64, xyz interleaved per node
+ *   mesh_type     ndglno(loc*E) int32, element-major
+ *                 (femtools/Fields_Data_Types.F90:61-76,187-216)
+ *
+ * Conventions: plain pointers and sizes; no CUDA or torch types in the
+ * signatures (streams are passed as void*).  Functions named fl_gpu_* take
+ * HOST pointers and copy in/out; functions named fl_dev_* take DEVICE pointers
+ * and run on the given stream (NULL = the mesh handle's stream).  Every
+ * function returns an fl_status; fl_last_error() describes the last failure
+ * of the calling thread.  Indices follow `index_base` (1 = Fortran, 0 = C).
+ */
+#ifndef FLUIDITY_GB300_H
+#define FLUIDITY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Usage errors (>0) correspond to FLAbort/FLExit in the
+ * reference (include/fdebug.h:56-57); FL_ERR_OUTSIDE_PATTERN is csr_addto's
+ * "Attempting to set value in matrix outside sparsity pattern."
+ * (femtools/Sparse_Tools.F90:2646).  Solver divergence is not an error: it is
+ * reported as a negative KSPConvergedReason in fl_solve_report::reason. */
+enum fl_status {
+  FL_OK = 0,
+  FL_ERR_ARG = 1,
+  FL_ERR_CUDA = 2,
+  FL_ERR_OUTSIDE_PATTERN = 3,
+  FL_ERR_TIMEOUT = 4,
+  FL_ERR_COLOURS = 5,
+  FL_ERR_NOMEM = 6,
+  FL_ERR_UNSUPPORTED = 7
+};
+
+/* KSPConvergedReason values used by the device solvers (PETSc, the third-party
+ * library called at femtools/Solvers.F90:1251; checked by ConvergenceCheck,
+ * femtools/Solvers.F90:1369-1479). */
+enum fl_reason {
+  FL_CONVERGED_RTOL = 2,
+  FL_CONVERGED_ATOL = 3,
+  FL_DIVERGED_NULL = -2,
+  FL_DIVERGED_ITS = -3,
+  FL_DIVERGED_DTOL = -4,
+  FL_DIVERGED_BREAKDOWN = -5,
+  FL_DIVERGED_INDEFINITE_PC = -8,
+  FL_DIVERGED_NANORINF = -9,
+  FL_DIVERGED_INDEFINITE_MAT = -10
+};
+
+/* Message describing the last non-OK status returned on this thread. */
+const char* fl_last_error(void);
+
+/* ---------------------------------------------------------------- meshes -- */
+
+typedef struct fl_mesh_t* fl_mesh;
+
+typedef struct {
+  int32_t nodes;            /* node_count of the field mesh (matrix rows)   */
+  int32_t elements;         /* element_count                                */
+  int32_t loc;              /* nodes per element: 4 (P1) or 10 (P2)         */
+  int32_t index_base;       /* 1: Fortran ndglno; 0: C                      */
+  const int32_t* ndglno;    /* loc*elements field-mesh connectivity         */
+  int32_t x_nodes;          /* node_count of the coordinate (P1) mesh       */
+  const int32_t* x_ndglno;  /* 4*elements coordinate/topology connectivity  */
+  const double* coords;     /* 3*x_nodes, positions%val(3,N)                */
+} fl_mesh_desc;
+
+/* Registers a mesh: uploads connectivity and coordinates, builds on the GPU the
+ * first-order sparsity (replaces get_csr_sparsity_firstorder ->
+ * make_sparsity, femtools/Sparsity_Patterns_Meshes.F90:76,
+ * femtools/Sparsity_Patterns.F90:47) and the COLOURING_CG1 element colouring
+ * (replaces get_mesh_colouring, femtools/Colouring.F90:85), both bit-exact with
+ * the reference, and caches them on the handle as the reference caches them
+ * in state / on the topology mesh. */
+int fl_gpu_mesh_register(const fl_mesh_desc* desc, fl_mesh* out);
+int fl_gpu_mesh_destroy(fl_mesh mesh);
+/* Sizes of the cached structures: entries of the sparsity and colour count. */
+int fl_gpu_mesh_info(fl_mesh mesh, int64_t* nnz, int32_t* ncolours);
+
+/* Copies the cached csr_sparsity out (findrm(N+1), colm(nnz), centrm(N)) in
+ * the requested index base.  centrm of a row without diagonal is 0 in base 1
+ * (lists2csr_sparsity, femtools/Sparsity_Patterns.F90:414-426) and -1 in base 0. */
+int fl_gpu_sparsity_copy(fl_mesh mesh, int32_t* findrm, int32_t* colm, int32_t* centrm,
+                         int32_t index_base);
+
+/* Copies the colouring out: colour(E) 1-based colours per element, and the
+ * colour sets as colour_ptr(ncolours+1) offsets into colour_elems(E), elements
+ * ascending within a set (colour_sets, femtools/Colouring.F90:250-262). */
+int fl_gpu_colouring_copy(fl_mesh mesh, int32_t* colour, int32_t* colour_ptr,
+                          int32_t* colour_elems, int32_t index_base);
+
+/* Node numbering of the P2 mesh derived from a P1 tet connectivity (replaces
+ * make_global_numbering, femtools/Global_Numbering.F90:291-634, serial case),
+ * computed on the GPU and bit-exact: vertices in first-touch element order,
+ * then edges in (old node, neighbour ascending) order.  ndglno_p2 has
+ * 10*elements entries in number_tets_lagrange local order
+ * (femtools/Element_Numbering.F90:389-472); *n2 receives the node count. */
+int fl_gpu_make_global_numbering_p2(int32_t nvert, int32_t elements, const int32_t* ndglno_p1,
+                                    int32_t index_base, int32_t* ndglno_p2, int32_t* n2);
+
+/* ------------------------------------------------------------- assembly -- */
+
+/* Options of assemble_advection_diffusion_cg read from the options tree
+ * (assemble/Advection_Diffusion_CG.F90:384-465). */
+typedef struct {
+  double theta;              /* temporal_discretisation/theta               */
+  double dt;                 /* timestep                                    */
+  double beta;               /* conservative_advection                      */
+  int32_t have_mass;         /* .not. exclude_mass_terms                    */
+  int32_t lump_mass;         /* lump_mass_matrix                            */
+  int32_t have_advection;    /* .not. exclude_advection_terms               */
+  int32_t have_diffusivity;
+  int32_t isotropic_diffusivity;
+  int32_t have_source;
+  int32_t have_absorption;
+  int32_t quad_degree;       /* quadrature degree of the mesh (2 or 4)      */
+  double diffusivity[9];     /* constant diffusivity tensor, (i,j) row-major */
+} fl_advdif_params;
+
+/* Nodal fields.  t, source, absorption live on the field mesh; velocity lives
+ * on the coordinate mesh (3 values per node).  NULL = absent (t = 0). */
+typedef struct {
+  const double* t;
+  const double* velocity;
+  const double* source;
+  const double* absorption;
+} fl_fields;
+
+/* Element loop of assemble_advection_diffusion_cg
+ * (assemble/Advection_Diffusion_CG.F90:560-598 -> element kernel :702-865 ->
+ * addto, femtools/Sparse_Tools.F90:2680): zeroes val/rhs, then adds every
+ * element's matrix and right-hand side into the csr_matrix values (pattern of
+ * the handle) colour by colour, elements ascending within a colour, so the
+ * sums are deterministic.  Host pointers: val(nnz), rhs(N). */
+int fl_gpu_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
+                              const fl_fields* fields, double* val, double* rhs);
+/* Device-pointer form of the same call (all field pointers device). */
+int fl_dev_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
+                              const fl_fields* fields, double* val, double* rhs,
+                              void* stream);
+
+/* Strong Dirichlet (apply_dirichlet_conditions_scalar,
+ * femtools/Boundary_Conditions.F90:1983-2025): marks rows inactive
+ * (csr_set_inactive_rows, femtools/Sparse_Tools.F90:2136) and sets
+ * rhs(b) = (g - t(b))/dt, or rhs(b) = g when dt <= 0.  inactive(N) is one
+ * byte per row (0/1).  t may be NULL (zero). */
+int fl_gpu_apply_dirichlet(fl_mesh mesh, int32_t nb, const int32_t* nodes, int32_t index_base,
+                           const double* g, const double* t, double dt, double* rhs,
+                           uint8_t* inactive);
+int fl_dev_apply_dirichlet(fl_mesh mesh, int32_t nb, const int32_t* nodes, int32_t index_base,
+                           const double* g, const double* t, double dt, double* rhs,
+                           uint8_t* inactive, void* stream);
+
+/* ---------------------------------------------------------------- solve -- */
+
+/* Solver options read by petsc_solve_setup / setup_ksp_from_options
+ * (femtools/Solvers.F90:1566-1660). */
+typedef struct {
+  int32_t ksp_type;          /* 0 = cg, 1 = gmres                           */
+  int32_t restart;           /* gmres restart (schema default 30)           */
+  double rtol;               /* relative_error                              */
+  double atol;               /* absolute_error (default 0)                  */
+  double dtol;               /* divergence tolerance (PETSc default 1e5)    */
+  int32_t max_its;           /* max_iterations                              */
+  int32_t start_from_zero;   /* start_from_zero                             */
+  int32_t precision;         /* 0 = fp64; 1 = fp32 inner iterations inside
+                                fp64 iterative refinement                   */
+  double inner_rtol;         /* inner relative tolerance (precision = 1)    */
+} fl_solver_opts;
+
+typedef struct {
+  int32_t iterations;        /* KSPGetIterationNumber (inner total if mixed) */
+  int32_t reason;            /* KSPConvergedReason                          */
+  double final_rnorm;        /* last preconditioned residual norm           */
+  double rnorm0;             /* norm the relative tolerance scales          */
+  double true_rel_residual;  /* ||b - A x|| / ||b|| recomputed in fp64      */
+  int32_t outer_iterations;  /* refinement steps (precision = 1)            */
+  int32_t pad;
+} fl_solve_report;
+
+/* petsc_solve on the handle's csr_matrix (femtools/Solvers.F90:111-187):
+ * inactive rows become ghost rows (Petsc_Tools.F90:256-298) carrying the
+ * diagonal ghost_pivot (Petsc_Tools.F90:960-985), ghost columns are lifted
+ * into the rhs (Solvers.F90:1072-1104), CG or GMRES(restart) with Jacobi
+ * preconditioning runs on the device with PETSc's default convergence test,
+ * and ghost nodes take their rhs value afterwards (Petsc_Tools.F90:726-730).
+ * Host pointers: val(nnz), inactive(N) or NULL, rhs(N), x(N) (initial guess
+ * unless start_from_zero; solution on return). */
+int fl_gpu_petsc_solve(fl_mesh mesh, const fl_solver_opts* opts, const double* val,
+                       const uint8_t* inactive, const double* rhs, double* x,
+                       fl_solve_report* report);
+int fl_dev_petsc_solve(fl_mesh mesh, const fl_solver_opts* opts, const double* val,
+                       const uint8_t* inactive, const double* rhs, double* x,
+                       fl_solve_report* report, void* stream);
+
+/* y = A x on the handle's pattern (csr_mult, femtools/Sparse_Tools.F90:3822);
+ * device pointers. */
+int fl_dev_csr_mult(fl_mesh mesh, const double* val, const double* x, double* y, void* stream);
+
+/* Number of kernels this library launched on the calling process so far
+ * (launch accounting for benchmarks). */
+int64_t fl_kernel_launch_count(void);
+
+/* Profiling hooks in the spirit of the reference's profiler keys
+ * ("advection_diffusion_loop", Advection_Diffusion_CG.F90:574-600): when
+ * enabled, the element loop of each assembly call on the handle is bracketed
+ * by CUDA events on its stream, and fl_last_assembly_kernel_ms returns the
+ * device time of that loop (all colours) for the last call. */
+int fl_set_kernel_timing(fl_mesh mesh, int32_t on);
+int fl_last_assembly_kernel_ms(fl_mesh mesh, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUIDITY_GB300_H */

@@ -1,0 +1,239 @@
+"""ctypes wrapper of the CPU oracle (``fl_oracle.cpp``).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` -- never by the product package.
+Indices are 0-based numpy arrays; CSR row pointers are int64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libfl_oracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++ -O3 -fopenmp)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "fl_oracle.cpp"))
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(_LIB_PATH)
+        _lib.orc_make_sparsity.restype = C.c_int64
+        _lib.orc_triangle_detwei_sum.restype = C.c_double
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+def tet_quadrature(degree: int):
+    """(l (ngi,4), w (ngi,), actual degree) -- Quadrature.F90:649-735."""
+    l = np.zeros((16, 4))
+    w = np.zeros(16)
+    ngi, deg = C.c_int(), C.c_int()
+    rc = lib().orc_tet_quadrature(degree, C.byref(ngi), C.byref(deg), _p(l), _p(w))
+    if rc:
+        raise ValueError(f"no tet quadrature of degree {degree}")
+    return l[: ngi.value].copy(), w[: ngi.value].copy(), deg.value
+
+
+def tet_shape(degree: int, quad_degree: int):
+    """(n (loc,ngi), dn (loc,ngi,3)) -- Shape_Functions.F90:128-329."""
+    n = np.zeros(10 * 16)
+    dn = np.zeros(10 * 16 * 3)
+    loc, ngi = C.c_int(), C.c_int()
+    rc = lib().orc_tet_shape(degree, quad_degree, C.byref(loc), C.byref(ngi), _p(n), _p(dn))
+    if rc:
+        raise ValueError("bad shape request")
+    L, G = loc.value, ngi.value
+    return n[: L * G].reshape(L, G).copy(), dn[: L * G * 3].reshape(L, G, 3).copy()
+
+
+def tet_counts(degree: int) -> np.ndarray:
+    c = np.zeros(40, dtype=np.int32)
+    loc = lib().orc_tet_counts(degree, _p(c))
+    return c[: 4 * loc].reshape(loc, 4).copy()
+
+
+def triangle_detwei_sum(X: np.ndarray) -> float:
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    return lib().orc_triangle_detwei_sum(_p(X))
+
+
+def transform_cache(ndglno_x: np.ndarray, coords: np.ndarray):
+    E = ndglno_x.shape[0]
+    nx = np.ascontiguousarray(ndglno_x, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    JT = np.zeros((E, 3, 3))
+    invJ = np.zeros((E, 3, 3))
+    det = np.zeros(E)
+    lib().orc_transform_cache(E, _p(nx), _p(X), _p(JT), _p(invJ), _p(det))
+    return JT, invJ, det
+
+
+def make_sparsity(ndglno: np.ndarray, nrows: int | None = None):
+    """(findrm int64 (N+1), colm int32, centrm int64) -- Sparsity_Patterns.F90:47."""
+    nd = np.ascontiguousarray(ndglno, dtype=np.int32)
+    E, loc = nd.shape
+    if nrows is None:
+        nrows = int(nd.max()) + 1
+    findrm = np.zeros(nrows + 1, dtype=np.int64)
+    centrm = np.zeros(nrows, dtype=np.int64)
+    nnz = lib().orc_make_sparsity(nrows, E, loc, _p(nd), _p(findrm), None, 0, _p(centrm))
+    colm = np.zeros(nnz, dtype=np.int32)
+    lib().orc_make_sparsity(nrows, E, loc, _p(nd), _p(findrm), _p(colm), nnz, _p(centrm))
+    return findrm, colm, centrm
+
+
+def colour_cg1(ndglno_vertices: np.ndarray, nvert: int | None = None):
+    """(colour per element, 1-based; ncolours) -- Colouring.F90:85-199."""
+    nd = np.ascontiguousarray(ndglno_vertices, dtype=np.int32)
+    E, nvl = nd.shape
+    if nvert is None:
+        nvert = int(nd.max()) + 1
+    colour = np.zeros(E, dtype=np.int32)
+    ncol = lib().orc_colour_cg1(E, nvl, _p(nd), nvert, _p(colour))
+    return colour, ncol
+
+
+def colour_sets(colour: np.ndarray, ncol: int):
+    """(colour_ptr int64 (ncol+1), elements ascending within each colour)."""
+    order = np.lexsort((np.arange(colour.size), colour))
+    counts = np.bincount(colour, minlength=ncol + 1)[1:]
+    ptr = np.zeros(ncol + 1, dtype=np.int64)
+    np.cumsum(counts, out=ptr[1:])
+    return ptr, order.astype(np.int32)
+
+
+def make_global_numbering_p2(ndglno1: np.ndarray, nvert: int | None = None):
+    """(ndglno2 (E,10) int32 0-based, N2) -- Global_Numbering.F90:291-634."""
+    nd = np.ascontiguousarray(ndglno1, dtype=np.int32)
+    E = nd.shape[0]
+    if nvert is None:
+        nvert = int(nd.max()) + 1
+    out = np.zeros((E, 10), dtype=np.int32)
+    n2 = lib().orc_make_global_numbering_p2(nvert, E, _p(nd), _p(out))
+    return out, n2
+
+
+class _Params(C.Structure):
+    _fields_ = [
+        ("theta", C.c_double), ("dt", C.c_double), ("beta", C.c_double),
+        ("have_mass", C.c_int), ("lump_mass", C.c_int), ("have_advection", C.c_int),
+        ("have_diffusivity", C.c_int), ("isotropic", C.c_int), ("have_source", C.c_int),
+        ("have_absorption", C.c_int), ("quad_degree", C.c_int), ("t_degree", C.c_int),
+        ("u_degree", C.c_int), ("diffusivity", C.c_double * 9),
+    ]
+
+
+def assemble_advdif(*, ndglno_t, nt, ndglno_x, coords, findrm, colm,
+                    theta=1.0, dt=1.0, beta=0.0, have_mass=False, lump_mass=False,
+                    velocity=None, ndglno_u=None, u_degree=1, T=None, source=None,
+                    absorption=None, diffusivity=None, quad_degree=2, t_degree=1,
+                    colours=None, nthreads=0):
+    """(val, rhs, status) of the element loop -- Advection_Diffusion_CG.F90:228-659.
+
+    ``diffusivity`` is a 3x3 constant tensor (isotropic if it is a multiple of
+    the identity), a scalar, or None.  ``colours`` = (colour_ptr, elements) or
+    None for element order (serial build).
+    """
+    P = _Params()
+    P.theta, P.dt, P.beta = theta, dt, beta
+    P.have_mass, P.lump_mass = int(have_mass), int(lump_mass)
+    P.have_advection = int(velocity is not None)
+    P.have_source = int(source is not None)
+    P.have_absorption = int(absorption is not None)
+    P.quad_degree, P.t_degree, P.u_degree = quad_degree, t_degree, u_degree
+    if diffusivity is None:
+        P.have_diffusivity = 0
+        P.isotropic = 1
+    else:
+        K = np.asarray(diffusivity, dtype=np.float64)
+        if K.ndim == 0:
+            K = np.eye(3) * float(K)
+        P.have_diffusivity = 1
+        P.isotropic = int(np.allclose(K, np.eye(3) * K[0, 0], rtol=0, atol=0))
+        for a in range(9):
+            P.diffusivity[a] = K.reshape(-1)[a]
+    nd_t = np.ascontiguousarray(ndglno_t, dtype=np.int32)
+    nd_x = np.ascontiguousarray(ndglno_x, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    E = nd_t.shape[0]
+    nd_u = np.ascontiguousarray(ndglno_u if ndglno_u is not None else nd_x, dtype=np.int32)
+    U = np.ascontiguousarray(velocity, dtype=np.float64) if velocity is not None else None
+    Tv = np.ascontiguousarray(T, dtype=np.float64) if T is not None else None
+    S = np.ascontiguousarray(source, dtype=np.float64) if source is not None else None
+    A = np.ascontiguousarray(absorption, dtype=np.float64) if absorption is not None else None
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    val = np.zeros(c.size)
+    rhs = np.zeros(nt)
+    if colours is None:
+        ncol, cptr, celems = 0, None, None
+    else:
+        cptr = np.ascontiguousarray(colours[0], dtype=np.int64)
+        celems = np.ascontiguousarray(colours[1], dtype=np.int32)
+        ncol = cptr.size - 1
+    st = lib().orc_assemble_advdif(
+        C.byref(P), E, _p(nd_t), nt, _p(nd_x), _p(X), _p(nd_u), _p(U), _p(Tv), _p(S), _p(A),
+        _p(f), _p(c), _p(val), _p(rhs), ncol, _p(cptr), _p(celems), int(nthreads))
+    return val, rhs, st
+
+
+def apply_dirichlet(nodes, g, T, dt, rhs, inactive):
+    nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    Tv = np.ascontiguousarray(T, dtype=np.float64) if T is not None else None
+    lib().orc_apply_dirichlet(nodes.size, _p(nodes), _p(g), _p(Tv), C.c_double(float(dt or 0.0)), _p(rhs),
+                              _p(inactive))
+
+
+def petsc_solve(findrm, colm, val, inactive, rhs, x0=None, *, ksp="cg", restart=30,
+                rtol=1e-10, atol=0.0, dtol=1e5, max_its=10000, start_from_zero=True,
+                nthreads=0, history=False):
+    """(x, its, reason, final_rnorm[, history]) -- Solvers.F90:111-1302 + PETSc KSP."""
+    n = findrm.size - 1
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    v = np.ascontiguousarray(val, dtype=np.float64)
+    ina = np.ascontiguousarray(inactive, dtype=np.uint8) if inactive is not None else None
+    b = np.ascontiguousarray(rhs, dtype=np.float64)
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    its, reason, rn = C.c_int(), C.c_int(), C.c_double()
+    cap = max_its + 64 if history else 0
+    hist = np.zeros(cap) if history else None
+    nh = lib().orc_petsc_solve(
+        n, _p(f), _p(c), _p(v), _p(ina), _p(b), _p(x), 0 if ksp == "cg" else 1, int(restart),
+        C.c_double(rtol), C.c_double(atol), C.c_double(dtol), int(max_its), int(bool(start_from_zero)),
+        C.byref(its), C.byref(reason), C.byref(rn), _p(hist), cap, int(nthreads))
+    if history:
+        return x, its.value, reason.value, rn.value, hist[: min(nh, cap)]
+    return x, its.value, reason.value, rn.value
+
+
+def csr_mult(findrm, colm, val, x):
+    n = findrm.size - 1
+    y = np.zeros(n)
+    lib().orc_csr_mult(n, _p(np.ascontiguousarray(findrm, dtype=np.int64)),
+                       _p(np.ascontiguousarray(colm, dtype=np.int32)),
+                       _p(np.ascontiguousarray(val, dtype=np.float64)),
+                       _p(np.ascontiguousarray(x, dtype=np.float64)), _p(y))
+    return y

@@ -1,0 +1,148 @@
+"""GPU element assembly against the oracle's restatement of
+assemble_advection_diffusion_cg, entry by entry.
+
+Tolerance (floating point): |a - a_ref| <= 1e-12 * max_j |a_ref(i, j)| per row
+for the matrix, and the same row scale for the right-hand side.
+"""
+import numpy as np
+import pytest
+
+from conftest import row_scaled_error
+from fluidity_gb300 import femtools as ft
+from fluidity_gb300 import meshgen as M
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def _oracle(O, nd, X, ndt, nt, f, c, colours=None, **kw):
+    val, rhs, st = O.assemble_advdif(ndglno_t=ndt, nt=nt, ndglno_x=nd, coords=X, findrm=f, colm=c,
+                                     colours=colours, **kw)
+    assert st == 0
+    return val, rhs
+
+
+def _compare(val, rhs, oval, orhs, f, tol=TOL):
+    assert row_scaled_error(val, oval, f) <= tol
+    # rhs scaled by the largest |rhs| of the row's neighbourhood
+    scale = max(np.abs(orhs).max(), 1e-300)
+    assert np.abs(rhs - orhs).max() <= tol * scale
+
+
+CASES = {
+    "poisson": dict(diffusivity=1.0, source=True),
+    "anisotropic": dict(diffusivity=np.diag([1.0, 1.0, 1e-3]), source=True),
+    "advdif": dict(theta=0.5, dt=0.01, have_mass=True, velocity=True, T=True, diffusivity=1e-3),
+    "advdif_beta1": dict(theta=0.5, dt=0.01, have_mass=True, velocity=True, T=True,
+                         diffusivity=1e-3, beta=1.0),
+    "lumped_absorption": dict(theta=1.0, dt=0.1, have_mass=True, lump_mass=True, absorption=True,
+                              T=True, diffusivity=0.5, source=True),
+    "mass_only": dict(have_mass=True, source=True),
+}
+
+
+def _fields(X, case):
+    out = {}
+    for k, v in case.items():
+        if v is True:
+            out[k] = {"source": M.poisson_source(X), "velocity": M.advdif_velocity(X),
+                      "T": M.gaussian_tracer(X), "absorption": 1.0 + X[:, 0]}[k]
+        else:
+            out[k] = v
+    return out
+
+
+def _params(case, quad_degree):
+    return ft.advdif_params(theta=case.get("theta", 1.0), dt=case.get("dt", 1.0),
+                            beta=case.get("beta", 0.0), have_mass=case.get("have_mass", False),
+                            lump_mass=case.get("lump_mass", False),
+                            have_advection="velocity" in case,
+                            diffusivity=case.get("diffusivity"), have_source="source" in case,
+                            have_absorption="absorption" in case, quad_degree=quad_degree)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("mesh", ["cube4", "aniso"])
+def test_p1_assembly_matches_oracle(O, aniso_mesh, name, mesh):
+    nd, X = M.cube_mesh(4) if mesh == "cube4" else aniso_mesh
+    case = CASES[name]
+    fl = _fields(X, case)
+    m = ft.Mesh(nd, X)
+    f, c, _ = O.make_sparsity(nd)
+    ocol, ncol = O.colour_cg1(nd)
+    colours = O.colour_sets(ocol, ncol)
+    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass")}
+    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass") if k in case})
+    oval, orhs = _oracle(O, nd, X, nd, X.shape[0], f, c, colours=colours, **kw)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, _params(case, 2), t=fl.get("T"),
+                                                  velocity=fl.get("velocity"),
+                                                  source=fl.get("source"),
+                                                  absorption=fl.get("absorption"))
+    _compare(val, rhs, oval, orhs, f)
+
+
+@pytest.mark.parametrize("name", ["poisson", "anisotropic", "advdif", "lumped_absorption"])
+def test_p2_assembly_matches_oracle(O, name):
+    nd, X = M.cube_mesh(3)
+    nd2, n2 = O.make_global_numbering_p2(nd)
+    X2 = M.p2_coordinates(nd, nd2, X, O.tet_counts(2))
+    case = CASES[name]
+    fl = _fields(X2, case)
+    if "velocity" in fl:
+        fl["velocity"] = M.advdif_velocity(X)  # velocity lives on the P1 coordinate mesh
+    m = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    f, c, _ = O.make_sparsity(nd2)
+    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass")}
+    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass") if k in case})
+    oval, orhs = _oracle(O, nd, X, nd2, n2, f, c, quad_degree=4, t_degree=2, **kw)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, _params(case, 4), t=fl.get("T"),
+                                                  velocity=fl.get("velocity"),
+                                                  source=fl.get("source"),
+                                                  absorption=fl.get("absorption"))
+    _compare(val, rhs, oval, orhs, f)
+
+
+def test_assembly_deterministic_and_device_path(O):
+    import torch
+    nd, X = M.cube_mesh(16)
+    m = ft.Mesh(nd, X)
+    p = _params(CASES["poisson"], 2)
+    src = M.poisson_source(X)
+    v1, r1 = ft.assemble_advection_diffusion_cg(m, p, source=src)
+    v2, r2 = ft.assemble_advection_diffusion_cg(m, p, source=src)
+    assert v1.tobytes() == v2.tobytes() and r1.tobytes() == r2.tobytes()
+    dsrc = torch.from_numpy(src).cuda()
+    dv, dr = ft.assemble_advection_diffusion_cg(m, p, source=dsrc)
+    torch.cuda.synchronize()
+    assert dv.cpu().numpy().tobytes() == v1.tobytes()
+    assert dr.cpu().numpy().tobytes() == r1.tobytes()
+
+
+def test_large_mesh_properties():
+    """64^3 (1.57M tets): symmetric Laplacian with zero row sums and rhs summing
+    to the integral of the interpolated source -- size-independent checks."""
+    import scipy.sparse as sp
+    n = 64
+    nd, X = M.cube_mesh(n)
+    m = ft.Mesh(nd, X)
+    assert m.nnz == M.cube_counts(n)["nnz1"]
+    s = m.sparsity()
+    ones = np.ones(X.shape[0])
+    val, rhs = ft.assemble_advection_diffusion_cg(m, _params(CASES["poisson"], 2), source=ones)
+    A = sp.csr_matrix((val, s.colm, s.findrm))
+    assert abs(A - A.T).max() <= 1e-15 * np.abs(val).max()
+    assert np.abs(A @ ones).max() <= 1e-12 * np.abs(val).max()
+    assert abs(rhs.sum() - 1.0) <= 1e-12
+
+
+def test_invalid_options_are_errors():
+    """Bad options raise FlError (FLAbort/FLExit in the reference) and leave the handle usable."""
+    nd, X = M.cube_mesh(2)
+    m = ft.Mesh(nd, X)
+    with pytest.raises(ft._lib.FlError):
+        ft.assemble_advection_diffusion_cg(m, ft.advdif_params(diffusivity=1.0, quad_degree=7))
+    with pytest.raises(ft._lib.FlError):  # advection without a velocity field
+        ft.assemble_advection_diffusion_cg(m, ft.advdif_params(have_advection=True))
+    val, rhs = ft.assemble_advection_diffusion_cg(m, _params(CASES["poisson"], 2),
+                                                  source=np.ones(X.shape[0]))
+    assert np.isfinite(val).all()

@@ -1,0 +1,167 @@
+"""Device CG / GMRES / mixed-precision solves against the oracle's restatement
+of petsc_solve (ghost rows, rhs lifting, PETSc KSP + Jacobi, default
+convergence test) and against direct solves."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from fluidity_gb300 import femtools as ft
+from fluidity_gb300 import meshgen as M
+
+pytestmark = pytest.mark.gpu
+
+
+def poisson(O, n, degree=1, kappa=1.0):
+    nd, X = M.cube_mesh(n)
+    if degree == 2:
+        nd2, n2 = O.make_global_numbering_p2(nd)
+        Xf = M.p2_coordinates(nd, nd2, X, O.tet_counts(2))
+        m = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+        q = 4
+    else:
+        Xf, m, q = X, ft.Mesh(nd, X), 2
+    p = ft.advdif_params(diffusivity=kappa, have_source=True, quad_degree=q)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, p, source=M.poisson_source(Xf))
+    ina = np.zeros(m.N, dtype=np.uint8)
+    bn = M.boundary_nodes(Xf)
+    ft.apply_dirichlet_conditions(m, rhs, ina, bn, np.zeros(bn.size), dt=1.0)
+    return m, Xf, val, rhs, ina
+
+
+def direct(m, val, rhs, ina):
+    s = m.sparsity()
+    A = sp.csr_matrix((val, s.colm, s.findrm), shape=(m.N, m.N))
+    act, gh = np.nonzero(ina == 0)[0], np.nonzero(ina)[0]
+    x = rhs.copy()
+    x[act] = spla.spsolve(A[act][:, act].tocsc(), rhs[act] - A[act][:, gh] @ rhs[gh])
+    return x
+
+
+def oracle_solve(O, m, val, rhs, ina, **kw):
+    s = m.sparsity()
+    return O.petsc_solve(s.findrm.astype(np.int64), s.colm, val, ina, rhs, **kw)
+
+
+@pytest.mark.parametrize("degree,n", [(1, 8), (2, 3)])
+def test_cg_matches_oracle_and_direct(O, degree, n):
+    m, X, val, rhs, ina = poisson(O, n, degree)
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(ksp="cg", rtol=1e-10), inactive=ina)
+    ox, oits, oreason, orn = oracle_solve(O, m, val, rhs, ina, ksp="cg", rtol=1e-10)
+    assert rep["reason"] == 2 and oreason == 2
+    assert abs(rep["iterations"] - oits) <= 1
+    xd = direct(m, val, rhs, ina)
+    scale = np.abs(xd).max()
+    assert np.abs(x - xd).max() <= 1e-7 * scale
+    assert np.abs(x - ox).max() <= 1e-7 * scale
+    # ghost nodes take their rhs value
+    assert np.array_equal(x[ina == 1], rhs[ina == 1])
+
+
+def test_gmres_advdif_matches_oracle(O):
+    nd, X = M.cube_mesh(8)
+    m = ft.Mesh(nd, X)
+    T0 = M.gaussian_tracer(X)
+    p = ft.advdif_params(theta=0.5, dt=0.01, have_mass=True, have_advection=True, diffusivity=1e-3)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, p, t=T0, velocity=M.advdif_velocity(X))
+    ina = np.zeros(m.N, dtype=np.uint8)
+    bn = M.boundary_nodes(X)
+    ft.apply_dirichlet_conditions(m, rhs, ina, bn, np.zeros(bn.size), t=T0, dt=0.01)
+    for restart in (30, 4):
+        x = np.zeros(m.N)
+        rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(ksp="gmres", restart=restart,
+                                                               rtol=1e-10), inactive=ina)
+        ox, oits, oreason, _ = oracle_solve(O, m, val, rhs, ina, ksp="gmres", restart=restart,
+                                            rtol=1e-10)
+        assert rep["reason"] == oreason == 2
+        assert abs(rep["iterations"] - oits) <= 1
+        xd = direct(m, val, rhs, ina)
+        assert np.abs(x - xd).max() <= 1e-7 * np.abs(xd).max()
+
+
+def test_nonzero_initial_guess(O):
+    m, X, val, rhs, ina = poisson(O, 6)
+    x0 = np.random.default_rng(0).standard_normal(m.N) * 1e-3
+    x = x0.copy()
+    rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(rtol=1e-10, start_from_zero=False),
+                         inactive=ina)
+    ox, oits, oreason, _ = oracle_solve(O, m, val, rhs, ina, x0=x0, rtol=1e-10,
+                                        start_from_zero=False)
+    assert rep["reason"] == oreason == 2
+    assert abs(rep["iterations"] - oits) <= 1
+    assert abs(rep["rnorm0"] - 0) > 0
+
+
+def test_failure_reasons(O):
+    m, X, val, rhs, ina = poisson(O, 6)
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(rtol=1e-12, max_its=2), inactive=ina)
+    assert rep["reason"] == -3 and rep["iterations"] == 2
+    bad = rhs.copy()
+    bad[np.nonzero(ina == 0)[0][0]] = np.nan
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, bad, ft.solver_options(rtol=1e-12), inactive=ina)
+    assert rep["reason"] == -9
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(ksp="gmres", rtol=1e-12, max_its=3),
+                         inactive=ina)
+    assert rep["reason"] == -3 and rep["iterations"] == 3
+
+
+@pytest.mark.parametrize("kappa", [1.0, np.diag([1.0, 1.0, 1e-3])])
+def test_mixed_precision_reaches_fp64_tolerance(O, kappa):
+    m, X, val, rhs, ina = poisson(O, 16, kappa=kappa)
+    x64 = np.zeros(m.N)
+    r64 = ft.petsc_solve(m, x64, val, rhs, ft.solver_options(rtol=1e-10), inactive=ina)
+    xm = np.zeros(m.N)
+    rm = ft.petsc_solve(m, xm, val, rhs, ft.solver_options(rtol=1e-10, precision="mixed"),
+                        inactive=ina)
+    assert r64["reason"] == 2 and rm["reason"] == 2
+    assert rm["outer_iterations"] >= 2
+    assert rm["final_rnorm"] <= 1e-10 * r64["rnorm0"] * (1 + 1e-12)
+    assert np.abs(xm - x64).max() <= 1e-7 * np.abs(x64).max()
+
+
+def test_device_resident_solve(O):
+    import torch
+    m, X, val, rhs, ina = poisson(O, 8)
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(rtol=1e-10), inactive=ina)
+    dx = torch.zeros(m.N, dtype=torch.float64, device="cuda")
+    drep = ft.petsc_solve(m, dx, torch.from_numpy(val).cuda(), torch.from_numpy(rhs).cuda(),
+                          ft.solver_options(rtol=1e-10), inactive=torch.from_numpy(ina).cuda())
+    torch.cuda.synchronize()
+    assert drep["iterations"] == rep["iterations"]
+    assert dx.cpu().numpy().tobytes() == x.tobytes()  # deterministic reductions
+
+
+def test_advdif_ten_steps_matches_oracle(O):
+    """The CPU workload (advection-diffusion, theta=0.5, dt=0.01, GMRES+Jacobi, 10
+    steps) at 8^3: the GPU driver and the oracle agree after every step."""
+    nd, X = M.cube_mesh(8)
+    m = ft.Mesh(nd, X)
+    s = m.sparsity()
+    u = M.advdif_velocity(X)
+    bn = M.boundary_nodes(X)
+    T = M.gaussian_tracer(X)
+    T[bn] = 0.0
+    To = T.copy()
+    p = ft.advdif_params(theta=0.5, dt=0.01, have_mass=True, have_advection=True, diffusivity=1e-3)
+    opts = ft.solver_options(ksp="gmres", restart=30, rtol=1e-10, start_from_zero=True)
+    ocol, ncol = O.colour_cg1(nd)
+    cs = O.colour_sets(ocol, ncol)
+    for step in range(10):
+        T, rep = ft.solve_field_equation_cg(m, T, p, opts, bc_nodes=bn, bc_values=np.zeros(bn.size),
+                                            velocity=u)
+        assert rep["reason"] == 2
+        val, rhs, st = O.assemble_advdif(ndglno_t=nd, nt=m.N, ndglno_x=nd, coords=X,
+                                         findrm=s.findrm, colm=s.colm, theta=0.5, dt=0.01,
+                                         have_mass=True, velocity=u, T=To, diffusivity=1e-3,
+                                         colours=cs)
+        ina = np.zeros(m.N, dtype=np.uint8)
+        O.apply_dirichlet(bn, np.zeros(bn.size), To, 0.01, rhs, ina)
+        dx, its, reason, _ = O.petsc_solve(s.findrm.astype(np.int64), s.colm, val, ina, rhs,
+                                           ksp="gmres", restart=30, rtol=1e-10)
+        To = To + 0.01 * dx
+        assert np.abs(T - To).max() <= 1e-9 * np.abs(To).max()

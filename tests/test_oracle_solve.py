@@ -1,0 +1,124 @@
+"""The oracle's assembled systems and Krylov solves against analytic facts and scipy.
+
+No reference test pins matrix entries or iteration counts; these checks pin
+what the reference's regression suite asserts: solvers converge to the stated
+tolerance, P1 Poisson converges at second order (the MMS order > 1.9 asserts of
+tests/Helmholtz-anisotropic-scalar-mms-p1p1cg-*), and the solution of the
+assembled system matches a direct solve.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from fluidity_gb300 import meshgen as M
+
+
+def poisson_system(O, n, jitter=0.2, degree=1):
+    nd, X = M.cube_mesh(n, jitter=jitter)
+    if degree == 2:
+        nd2, n2 = O.make_global_numbering_p2(nd)
+        Xf = M.p2_coordinates(nd, nd2, X, O.tet_counts(2))
+        ndt, nt, q = nd2, n2, 4
+    else:
+        ndt, nt, Xf, q = nd, X.shape[0], X, 2
+    f, c, ce = O.make_sparsity(ndt)
+    src = M.poisson_source(Xf)
+    val, rhs, st = O.assemble_advdif(ndglno_t=ndt, nt=nt, ndglno_x=nd, coords=X, findrm=f, colm=c,
+                                     diffusivity=1.0, source=src, quad_degree=q, t_degree=degree)
+    assert st == 0
+    bn = M.boundary_nodes(Xf)
+    inactive = np.zeros(nt, dtype=np.uint8)
+    O.apply_dirichlet(bn, np.zeros(bn.size), None, 1.0, rhs, inactive)
+    return nd, X, Xf, f, c, val, rhs, inactive, bn
+
+
+def reduced_direct(f, c, val, rhs, inactive):
+    n = f.size - 1
+    A = sp.csr_matrix((val, c, f), shape=(n, n))
+    act = np.nonzero(inactive == 0)[0]
+    gh = np.nonzero(inactive)[0]
+    b = rhs[act] - A[act][:, gh] @ rhs[gh]
+    x = np.array(rhs, dtype=np.float64)
+    x[act] = spla.spsolve(A[act][:, act].tocsc(), b)
+    return x
+
+
+def test_laplacian_symmetric_rowsum_zero(O):
+    nd, X = M.cube_mesh(3)
+    f, c, _ = O.make_sparsity(nd)
+    val, rhs, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
+                                     findrm=f, colm=c, diffusivity=1.0)
+    A = sp.csr_matrix((val, c, f))
+    assert abs(A - A.T).max() < 1e-15
+    assert np.abs(A @ np.ones(A.shape[0])).max() < 1e-14
+
+
+def test_source_integral(O):
+    """sum_i rhs_i = integral of the P1 interpolant of f over the cube."""
+    nd, X = M.cube_mesh(4)
+    f, c, _ = O.make_sparsity(nd)
+    src = np.ones(X.shape[0])
+    val, rhs, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
+                                     findrm=f, colm=c, diffusivity=1.0, source=src)
+    assert abs(rhs.sum() - 1.0) < 1e-13
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+def test_cg_matches_direct(O, degree):
+    nd, X, Xf, f, c, val, rhs, ina, bn = poisson_system(O, 4, degree=degree)
+    x, its, reason, rn = O.petsc_solve(f, c, val, ina, rhs, ksp="cg", rtol=1e-12)
+    assert reason == 2 and its > 0
+    xd = reduced_direct(f, c, val, rhs, ina)
+    assert np.abs(x - xd).max() <= 1e-9 * np.abs(xd).max()
+
+
+def test_gmres_matches_direct_advdif(O):
+    nd, X = M.cube_mesh(4)
+    f, c, _ = O.make_sparsity(nd)
+    u = M.advdif_velocity(X)
+    T0 = M.gaussian_tracer(X)
+    val, rhs, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X, findrm=f,
+                                     colm=c, theta=0.5, dt=0.01, have_mass=True, velocity=u, T=T0,
+                                     diffusivity=1e-3)
+    assert st == 0
+    A = sp.csr_matrix((val, c, f))
+    assert abs(A - A.T).max() > 1e-8  # advection makes it non-symmetric
+    bn = M.boundary_nodes(X)
+    ina = np.zeros(X.shape[0], dtype=np.uint8)
+    O.apply_dirichlet(bn, np.zeros(bn.size), T0, 0.01, rhs, ina)
+    x, its, reason, rn = O.petsc_solve(f, c, val, ina, rhs, ksp="gmres", restart=30, rtol=1e-12)
+    assert reason == 2
+    xd = reduced_direct(f, c, val, rhs, ina)
+    assert np.abs(x - xd).max() <= 1e-9 * np.abs(xd).max()
+
+
+def test_gmres_restart_and_history(O):
+    nd, X, Xf, f, c, val, rhs, ina, bn = poisson_system(O, 5)
+    x, its, reason, rn, hist = O.petsc_solve(f, c, val, ina, rhs, ksp="gmres", restart=5,
+                                             rtol=1e-10, history=True)
+    assert reason == 2 and its > 5
+    assert hist[-1] <= 1e-10 * hist[0] * 1.0000001
+
+
+def test_poisson_mms_order(O):
+    """P1 Poisson, u = f/(3 pi^2): nodal L2-type error falls at order ~2."""
+    errs = []
+    for n in (8, 16, 32):
+        nd, X, Xf, f, c, val, rhs, ina, bn = poisson_system(O, n, jitter=0.0)
+        x, its, reason, rn = O.petsc_solve(f, c, val, ina, rhs, ksp="cg", rtol=1e-12)
+        assert reason == 2
+        u = M.poisson_source(X) / (3 * np.pi ** 2)
+        errs.append(np.sqrt(np.mean((x - u) ** 2)))
+    orders = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(orders) > 1.7 and orders[-1] > 1.9, orders
+
+
+def test_failure_reasons(O):
+    nd, X, Xf, f, c, val, rhs, ina, bn = poisson_system(O, 4)
+    x, its, reason, rn = O.petsc_solve(f, c, val, ina, rhs, ksp="cg", rtol=1e-12, max_its=2)
+    assert reason == -3 and its == 2  # KSP_DIVERGED_ITS
+    bad = rhs.copy()
+    bad[np.nonzero(ina == 0)[0][0]] = np.nan
+    x, its, reason, rn = O.petsc_solve(f, c, val, ina, bad, ksp="cg")
+    assert reason == -9  # KSP_DIVERGED_NANORINF
