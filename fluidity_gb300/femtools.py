@@ -46,8 +46,11 @@ def _is_device(a) -> bool:
 
 
 def _stream_ptr(stream):
+    """CUDA stream handle for device-path calls: the given stream, or torch's
+    current stream so the library's work is ordered with the caller's tensors."""
     if stream is None:
-        return None
+        import torch
+        stream = torch.cuda.current_stream()
     return getattr(stream, "cuda_stream", stream)
 
 
