@@ -80,6 +80,37 @@ EXPORTS = [
     "fl_kernel_launch_count", "fl_set_kernel_timing", "fl_last_assembly_kernel_ms",
 ]
 
+_P = C.c_void_p
+_I32 = C.c_int32
+_D = C.c_double
+#: ctypes signatures of every entry point (pointers are c_void_p so 64-bit
+#: host and device addresses pass unchanged).
+_SIGNATURES = {
+    "fl_last_error": (C.c_char_p, []),
+    "fl_gpu_mesh_register": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(C.c_void_p)]),
+    "fl_gpu_mesh_destroy": (C.c_int, [_P]),
+    "fl_gpu_mesh_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "fl_gpu_sparsity_copy": (C.c_int, [_P, _P, _P, _P, _I32]),
+    "fl_gpu_colouring_copy": (C.c_int, [_P, _P, _P, _P, _I32]),
+    "fl_gpu_make_global_numbering_p2": (C.c_int, [_I32, _I32, _P, _I32, _P,
+                                                  C.POINTER(C.c_int32)]),
+    "fl_gpu_assemble_advdif_cg": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(Fields), _P,
+                                            _P]),
+    "fl_dev_assemble_advdif_cg": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(Fields), _P,
+                                            _P, _P]),
+    "fl_gpu_apply_dirichlet": (C.c_int, [_P, _I32, _P, _I32, _P, _P, _D, _P, _P]),
+    "fl_dev_apply_dirichlet": (C.c_int, [_P, _I32, _P, _I32, _P, _P, _D, _P, _P, _P]),
+    "fl_gpu_petsc_solve": (C.c_int, [_P, C.POINTER(SolverOpts), _P, _P, _P, _P,
+                                     C.POINTER(SolveReport)]),
+    "fl_dev_petsc_solve": (C.c_int, [_P, C.POINTER(SolverOpts), _P, _P, _P, _P,
+                                     C.POINTER(SolveReport), _P]),
+    "fl_dev_csr_mult": (C.c_int, [_P, _P, _P, _P, _P]),
+    "fl_kernel_launch_count": (C.c_int64, []),
+    "fl_set_kernel_timing": (C.c_int, [_P, _I32]),
+    "fl_last_assembly_kernel_ms": (C.c_int, [_P, C.POINTER(C.c_float)]),
+}
+assert sorted(_SIGNATURES) == sorted(EXPORTS)
+
 _lib = None
 _lock = threading.Lock()
 
@@ -99,11 +130,10 @@ def load(build_if_needed: bool = True):
         if not os.path.exists(_build.LIB):
             raise RuntimeError(f"{_build.LIB} is missing; run fluidity_gb300.build.build()")
         lib = C.CDLL(_build.LIB)
-        lib.fl_last_error.restype = C.c_char_p
-        lib.fl_kernel_launch_count.restype = C.c_int64
-        for name in EXPORTS:
-            if name not in ("fl_last_error", "fl_kernel_launch_count"):
-                getattr(lib, name).restype = C.c_int
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
         _lib = lib
         return lib
 

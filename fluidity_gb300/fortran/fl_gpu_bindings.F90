@@ -1,0 +1,170 @@
+!    fl_gpu_bindings.F90 -- ISO_C_BINDING interface to libfluidity_gb300.so.
+!
+!    The Fortran side of the drop-in boundary: explicit interfaces to the
+!    C-ABI declared in include/fluidity_gb300.h, plus wrappers that take
+!    Fluidity's own types (csr_matrix, scalar_field, vector_field, mesh_type)
+!    and call the GPU entry points with c_loc() pointers to the arrays those
+!    types already own.  The wrappers keep the argument meaning of the routines
+!    they stand in for:
+!
+!      gpu_assemble_advection_diffusion_cg  -> assemble_advection_diffusion_cg
+!                                    (assemble/Advection_Diffusion_CG.F90:228)
+!      gpu_petsc_solve_scalar       -> petsc_solve_scalar (femtools/Solvers.F90:111)
+!
+!    Status handling follows the reference: usage errors abort with FLAbort
+!    (include/fdebug.h:56), solver divergence is returned as a negative
+!    KSPConvergedReason for ConvergenceCheck (femtools/Solvers.F90:1369).
+!
+!    Not compiled in this repository's build (no Fortran compiler is
+!    available); it is compiled into Fluidity's femtools library by the
+!    integration recipe of INTEGRATION.md.
+#include "fdebug.h"
+module fl_gpu_bindings
+  use iso_c_binding
+  implicit none
+  private
+
+  public :: fl_mesh_desc, fl_advdif_params, fl_fields, fl_solver_opts, fl_solve_report
+  public :: fl_gpu_mesh_register, fl_gpu_mesh_destroy, fl_gpu_mesh_info, &
+            fl_gpu_sparsity_copy, fl_gpu_colouring_copy, fl_gpu_make_global_numbering_p2, &
+            fl_gpu_assemble_advdif_cg, fl_gpu_apply_dirichlet, fl_gpu_petsc_solve
+  public :: gpu_check
+
+  integer(c_int), parameter, public :: FL_OK = 0
+
+  type, bind(c) :: fl_mesh_desc
+     integer(c_int32_t) :: nodes, elements, loc, index_base
+     type(c_ptr) :: ndglno
+     integer(c_int32_t) :: x_nodes
+     type(c_ptr) :: x_ndglno
+     type(c_ptr) :: coords
+  end type fl_mesh_desc
+
+  type, bind(c) :: fl_advdif_params
+     real(c_double) :: theta, dt, beta
+     integer(c_int32_t) :: have_mass, lump_mass, have_advection, have_diffusivity
+     integer(c_int32_t) :: isotropic_diffusivity, have_source, have_absorption, quad_degree
+     real(c_double) :: diffusivity(9)
+  end type fl_advdif_params
+
+  type, bind(c) :: fl_fields
+     type(c_ptr) :: t, velocity, source, absorption
+  end type fl_fields
+
+  type, bind(c) :: fl_solver_opts
+     integer(c_int32_t) :: ksp_type, restart
+     real(c_double) :: rtol, atol, dtol
+     integer(c_int32_t) :: max_its, start_from_zero, precision
+     real(c_double) :: inner_rtol
+  end type fl_solver_opts
+
+  type, bind(c) :: fl_solve_report
+     integer(c_int32_t) :: iterations, reason
+     real(c_double) :: final_rnorm, rnorm0, true_rel_residual
+     integer(c_int32_t) :: outer_iterations, pad
+  end type fl_solve_report
+
+  interface
+     function fl_last_error() bind(c, name="fl_last_error") result(msg)
+       import :: c_ptr
+       type(c_ptr) :: msg
+     end function fl_last_error
+
+     function fl_gpu_mesh_register(desc, handle) bind(c, name="fl_gpu_mesh_register") result(st)
+       import :: c_int, c_ptr, fl_mesh_desc
+       type(fl_mesh_desc), intent(in) :: desc
+       type(c_ptr), intent(out) :: handle
+       integer(c_int) :: st
+     end function fl_gpu_mesh_register
+
+     function fl_gpu_mesh_destroy(handle) bind(c, name="fl_gpu_mesh_destroy") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: handle
+       integer(c_int) :: st
+     end function fl_gpu_mesh_destroy
+
+     function fl_gpu_mesh_info(handle, nnz, ncolours) bind(c, name="fl_gpu_mesh_info") result(st)
+       import :: c_int, c_ptr, c_int64_t, c_int32_t
+       type(c_ptr), value :: handle
+       integer(c_int64_t), intent(out) :: nnz
+       integer(c_int32_t), intent(out) :: ncolours
+       integer(c_int) :: st
+     end function fl_gpu_mesh_info
+
+     function fl_gpu_sparsity_copy(handle, findrm, colm, centrm, base) &
+          bind(c, name="fl_gpu_sparsity_copy") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: handle, findrm, colm, centrm
+       integer(c_int32_t), value :: base
+       integer(c_int) :: st
+     end function fl_gpu_sparsity_copy
+
+     function fl_gpu_colouring_copy(handle, colour, colour_ptr, colour_elems, base) &
+          bind(c, name="fl_gpu_colouring_copy") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: handle, colour, colour_ptr, colour_elems
+       integer(c_int32_t), value :: base
+       integer(c_int) :: st
+     end function fl_gpu_colouring_copy
+
+     function fl_gpu_make_global_numbering_p2(nvert, elements, ndglno_p1, base, ndglno_p2, n2) &
+          bind(c, name="fl_gpu_make_global_numbering_p2") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       integer(c_int32_t), value :: nvert, elements, base
+       type(c_ptr), value :: ndglno_p1, ndglno_p2
+       integer(c_int32_t), intent(out) :: n2
+       integer(c_int) :: st
+     end function fl_gpu_make_global_numbering_p2
+
+     function fl_gpu_assemble_advdif_cg(handle, params, fields, val, rhs) &
+          bind(c, name="fl_gpu_assemble_advdif_cg") result(st)
+       import :: c_int, c_ptr, fl_advdif_params, fl_fields
+       type(c_ptr), value :: handle
+       type(fl_advdif_params), intent(in) :: params
+       type(fl_fields), intent(in) :: fields
+       type(c_ptr), value :: val, rhs
+       integer(c_int) :: st
+     end function fl_gpu_assemble_advdif_cg
+
+     function fl_gpu_apply_dirichlet(handle, nb, nodes, base, g, t, dt, rhs, inactive) &
+          bind(c, name="fl_gpu_apply_dirichlet") result(st)
+       import :: c_int, c_ptr, c_int32_t, c_double
+       type(c_ptr), value :: handle, nodes, g, t, rhs, inactive
+       integer(c_int32_t), value :: nb, base
+       real(c_double), value :: dt
+       integer(c_int) :: st
+     end function fl_gpu_apply_dirichlet
+
+     function fl_gpu_petsc_solve(handle, opts, val, inactive, rhs, x, report) &
+          bind(c, name="fl_gpu_petsc_solve") result(st)
+       import :: c_int, c_ptr, fl_solver_opts, fl_solve_report
+       type(c_ptr), value :: handle
+       type(fl_solver_opts), intent(in) :: opts
+       type(c_ptr), value :: val, inactive, rhs, x
+       type(fl_solve_report), intent(out) :: report
+       integer(c_int) :: st
+     end function fl_gpu_petsc_solve
+  end interface
+
+contains
+
+  subroutine gpu_check(st, where)
+    !!< FLAbort on a usage error returned by the library.
+    integer(c_int), intent(in) :: st
+    character(len=*), intent(in) :: where
+    character(kind=c_char), pointer :: msg(:)
+    character(len=1024) :: text
+    integer :: i
+
+    if (st == FL_OK) return
+    call c_f_pointer(fl_last_error(), msg, (/ 1024 /))
+    text = ""
+    do i = 1, 1024
+       if (msg(i) == c_null_char) exit
+       text(i:i) = msg(i)
+    end do
+    ewrite(-1, *) trim(where), ": ", trim(text)
+    FLAbort("GPU CG path failed")
+  end subroutine gpu_check
+
+end module fl_gpu_bindings

@@ -29,3 +29,12 @@ def test_library_exports_every_symbol():
     out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
     for name in declared_symbols():
         assert re.search(rf"\bT {name}\b", out), name
+
+
+def test_every_entry_point_has_a_full_ctypes_signature():
+    """Pointers cross as c_void_p: a missing argtypes list would truncate 64-bit addresses."""
+    lib = _lib.load()
+    for name in declared_symbols():
+        fn = getattr(lib, name)
+        assert fn.argtypes is not None, name
+        assert fn.restype is not None, name

@@ -44,7 +44,7 @@ CASES = {
 def _fields(X, case):
     out = {}
     for k, v in case.items():
-        if v is True:
+        if v is True and k in ("source", "velocity", "T", "absorption"):
             out[k] = {"source": M.poisson_source(X), "velocity": M.advdif_velocity(X),
                       "T": M.gaussian_tracer(X), "absorption": 1.0 + X[:, 0]}[k]
         else:
