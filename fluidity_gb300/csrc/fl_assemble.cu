@@ -2,11 +2,17 @@
 // device csr_matrix, and strong Dirichlet conditions.
 //
 // The element loop replaces the coloured OpenMP region of
-// assemble_advection_diffusion_cg (assemble/Advection_Diffusion_CG.F90:560-598):
-// one launch per colour of the COLOURING_CG1 colouring; no two elements of a
-// colour share a node, so each CSR row receives at most one element's
-// contribution per launch and every entry is summed in (colour, element)
-// order -- the reference's own order -- without atomics.
+// assemble_advection_diffusion_cg (assemble/Advection_Diffusion_CG.F90:560-598)
+// in two passes:
+//  1. an element pass computes every element's matrix and right-hand side once
+//     (coalesced, one thread per element) into a coefficient-major scratch
+//     buffer;
+//  2. a row pass gives each CSR row to one thread, which adds the
+//     contributions of the row's elements in the order of their colour in the
+//     COLOURING_CG1 colouring -- the order in which the reference's coloured
+//     loop adds them -- and writes the row once.
+// No atomics; every entry is summed in the reference's (colour, element)
+// order, so results are deterministic.
 //
 // Element matrices follow the term routines of Advection_Diffusion_CG.F90
 // (:867 mass, :943 advection not by parts, :1143 absorption, :1164
@@ -102,23 +108,8 @@ __device__ __forceinline__ void element_geo(const double* __restrict__ X, const 
   g.det = J[0][0] * g.cof[0][0] + J[1][0] * g.cof[1][0] + J[2][0] * g.cof[2][0];
 }
 
-// csr addto of one entry (csr_addto, femtools/Sparse_Tools.F90:2631-2655):
-// exact zeros are skipped; a miss is an "outside sparsity pattern" error.
-__device__ __forceinline__ void addto(double* __restrict__ val, const int32_t* __restrict__ findrm,
-                                      const int32_t* __restrict__ colm, int i, int j, double v,
-                                      ErrWord* err, int e) {
-  if (v == 0.0) return;
-  const int p = csr_find(colm, __ldg(findrm + i), __ldg(findrm + i + 1), j);
-  if (p < 0) {
-    set_err(err, FL_ERR_OUTSIDE_PATTERN, e);
-    return;
-  }
-  val[p] += v;
-}
-
 struct AsmArgs {
-  const int32_t* elems;     // elements of this colour
-  int32_t count;
+  int32_t E;
   const int32_t* nd;        // field connectivity
   const int32_t* xnd;       // coordinate connectivity (int4 per element)
   const double* X;
@@ -126,11 +117,7 @@ struct AsmArgs {
   const double* u;
   const double* f;
   const double* alpha;
-  const int32_t* findrm;
-  const int32_t* colm;
-  double* val;
-  double* rhs;
-  ErrWord* err;
+  double* em;               // element matrices: em[k * E + e]
   const RefTensors* ref;
   double theta_dt;
   double beta;
@@ -139,14 +126,15 @@ struct AsmArgs {
 };
 
 // General element kernel: any term combination, P1 or P2 fields, P1
-// coordinates and velocity.  One thread per element; rows of the element
-// matrix are formed and inserted one at a time.
+// coordinates and velocity.  One thread per element; writes the full LOC x LOC
+// matrix (row-major, coefficient k = i*LOC + j) and the LOC rhs entries
+// (k = LOC*LOC + i).
 template <int LOC>
 __global__ void __launch_bounds__(128) k_asm_general(AsmArgs A) {
   note_launch();
   const RefTensors& R = *A.ref;
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < A.count; idx += gridDim.x * blockDim.x) {
-    const int e = __ldg(A.elems + idx);
+  const int64_t E = A.E;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
     Geo g;
     element_geo(A.X, A.xnd, e, g);
     const double rdet = 1.0 / g.det;
@@ -280,31 +268,39 @@ __global__ void __launch_bounds__(128) k_asm_general(AsmArgs A) {
 #pragma unroll
         for (int j = 0; j < LOC; ++j) r += R.M[i][j] * fe[j];
       }
-      const int row = tn[i];
 #pragma unroll
-      for (int j = 0; j < LOC; ++j) addto(A.val, A.findrm, A.colm, row, tn[j], m[j], A.err, e);
-      A.rhs[row] += r;
+      for (int j = 0; j < LOC; ++j) A.em[(int64_t)(i * LOC + j) * E + e] = m[j];
+      A.em[(int64_t)(LOC * LOC + i) * E + e] = r;
     }
   }
+}
+
+// Symmetric storage index of (i, j) in a 4x4 matrix: 0..9.
+__host__ __device__ constexpr int sym4(int i, int j) {
+  return i <= j ? i * 4 - (i * (i - 1)) / 2 + (j - i) : j * 4 - (j * (j - 1)) / 2 + (i - j);
 }
 
 // P1 diffusion + source (+ consistent mass) in closed form: with P1
 // coordinates the gradients are the cofactor columns over detJ, so
 //   K_ij = (c_i . kappa c_j) * wsum / |detJ|,   c_4 = -(c_1 + c_2 + c_3)
-//   rhs_i = sum_j M_ij f_j,  M_ij = |detJ| * Mref_ij.
-// This is the pressure-Laplacian form of the Poisson workloads (exact
-// regrouping of dshape_dot_dshape over the rule).
+//   rhs_i = sum_j M_ij f_j - sum_j K_ij t_j,  M_ij = |detJ| * Mref_ij.
+// This is the pressure-Laplacian form of the Poisson workloads (an exact
+// regrouping of dshape_dot_dshape over the rule).  Writes the 10 unique matrix
+// entries (k = sym4(i, j)) and 4 rhs entries (k = 10 + i).
 __global__ void __launch_bounds__(256) k_asm_p1_diffusion(AsmArgs A) {
   note_launch();
   const RefTensors& R = *A.ref;
-  const double wsum = R.wsum;
-  double M0 = R.M[0][0], M1 = R.M[0][1];
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < A.count; idx += gridDim.x * blockDim.x) {
-    const int e = __ldg(A.elems + idx);
+  const double M0 = R.M[0][0], M1 = R.M[0][1];
+  // theta*dt folds into the stiffness scale (the reference multiplies the
+  // element matrix by dt_theta when |dt_theta| > epsilon)
+  const double kscale = R.wsum * (A.use_dt ? A.theta_dt : 0.0) * (A.iso ? A.kappa[0] : 1.0);
+  const double rscale = R.wsum * (A.iso ? A.kappa[0] : 1.0);
+  const int64_t E = A.E;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
     Geo g;
     element_geo(A.X, A.xnd, e, g);
     const double adet = fabs(g.det);
-    const double s = wsum / adet;
+    const double rdet = __drcp_rn(adet);
     double c[4][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -317,45 +313,137 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion(AsmArgs A) {
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        if (A.iso) kc[i][a] = c[i][a] * A.kappa[0];
+        if (A.iso) kc[i][a] = c[i][a];
         else kc[i][a] = A.kappa[3 * a + 0] * c[i][0] + A.kappa[3 * a + 1] * c[i][1] + A.kappa[3 * a + 2] * c[i][2];
       }
     const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
     const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
-    double K[4][4];
+    double G[4][4];  // c_i . kappa c_j (symmetric for symmetric kappa)
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) K[i][j] = (c[i][0] * kc[j][0] + c[i][1] * kc[j][1] + c[i][2] * kc[j][2]) * s;
-    double Te[4], fe[4];
+      for (int j = i; j < 4; ++j) {
+        G[i][j] = c[i][0] * kc[j][0] + c[i][1] * kc[j][1] + c[i][2] * kc[j][2];
+        G[j][i] = G[i][j];
+      }
+    const double ks = kscale * rdet;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      Te[i] = A.t ? __ldg(A.t + tn[i]) : 0.0;
-      fe[i] = A.have_src ? __ldg(A.f + tn[i]) : 0.0;
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = i; j < 4; ++j) {
+        double m = G[i][j] * ks;
+        if (A.have_mass) m += adet * (i == j ? M0 : M1);
+        A.em[(int64_t)sym4(i, j) * E + e] = m;
+      }
+    double fsum = 0.0, fe[4] = {0.0, 0.0, 0.0, 0.0};
+    if (A.have_src) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) fe[i] = __ldg(A.f + tn[i]);
+      fsum = (fe[0] + fe[1]) + (fe[2] + fe[3]);
     }
-    double fsum = (fe[0] + fe[1]) + (fe[2] + fe[3]);
+    double Te[4] = {0.0, 0.0, 0.0, 0.0};
+    if (A.t) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) Te[i] = __ldg(A.t + tn[i]);
+    }
+    const double rs = rscale * rdet;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       double r = 0.0;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) r -= K[i][j] * Te[j];
-      if (A.have_src) r += adet * (M1 * fsum + (M0 - M1) * fe[i]);
-      const int row = tn[i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        double m = A.use_dt ? A.theta_dt * K[i][j] : 0.0;
-        if (A.have_mass) m += adet * (i == j ? M0 : M1);
-        addto(A.val, A.findrm, A.colm, row, tn[j], m, A.err, e);
-      }
-      A.rhs[row] += r;
+      if (A.have_src) r = adet * (M1 * fsum + (M0 - M1) * fe[i]);
+      if (A.t) r -= (G[i][0] * Te[0] + G[i][1] * Te[1] + G[i][2] * Te[2] + G[i][3] * Te[3]) * rs;
+      A.em[(int64_t)(10 + i) * E + e] = r;
     }
   }
 }
 
-__global__ void k_zero(double* __restrict__ p, int64_t n) {
+// Row pass: thread per CSR row; contributions of the row's elements are added
+// in the colour order of ne_col and the row is written once.  Accumulators
+// and the row's column indices live in shared memory for rows up to RMAX
+// entries; longer rows accumulate in place in val (the row belongs to this
+// thread alone).  A column missing from the pattern is csr_addto's
+// "outside sparsity pattern" error.
+struct PullArgs {
+  int32_t N, E;
+  const int32_t* ne_ptr;
+  const int32_t* ne_col;
+  const int32_t* nd;
+  const int32_t* findrm;
+  const int32_t* colm;
+  const double* em;
+  double* val;
+  double* rhs;
+  ErrWord* err;
+};
+
+template <int LOC, bool SYM, int THREADS, int RMAX>
+__global__ void __launch_bounds__(THREADS) k_rows_pull(PullArgs P) {
   note_launch();
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    p[k] = 0.0;
+  extern __shared__ unsigned char smem_raw[];
+  double* acc = reinterpret_cast<double*>(smem_raw);                       // [RMAX][THREADS]
+  int32_t* col = reinterpret_cast<int32_t*>(acc + (size_t)RMAX * THREADS);  // [RMAX][THREADS]
+  const int t = threadIdx.x;
+  const int64_t E = P.E;
+  constexpr int NK = SYM ? LOC * (LOC + 1) / 2 : LOC * LOC;
+  for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
+    const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
+    const bool in_smem = L <= RMAX;
+    if (in_smem) {
+      for (int k = 0; k < L; ++k) {
+        acc[k * THREADS + t] = 0.0;
+        col[k * THREADS + t] = __ldg(P.colm + base + k);
+      }
+    } else {
+      for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
+    }
+    double r = 0.0;
+    const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
+    for (int q = ib; q < ie; ++q) {
+      const int inc = __ldg(P.ne_col + q);
+      const int e = inc >> 4, a = inc & 15;
+#pragma unroll
+      for (int b = 0; b < LOC; ++b) {
+        const int j = __ldg(P.nd + (int64_t)e * LOC + b);
+        int k;
+        if (SYM) k = a <= b ? a * LOC - (a * (a - 1)) / 2 + (b - a) : b * LOC - (b * (b - 1)) / 2 + (a - b);
+        else k = a * LOC + b;
+        const double v = __ldg(P.em + (int64_t)k * E + e);
+        // bisection in the row (csr_sparsity_pos, Sparse_Tools.F90:2411)
+        int lo = 0, hi = L - 1, pos = -1;
+        while (lo <= hi) {
+          const int mid = (lo + hi) >> 1;
+          const int c = in_smem ? col[mid * THREADS + t] : __ldg(P.colm + base + mid);
+          if (c == j) { pos = mid; break; }
+          if (c < j) lo = mid + 1;
+          else hi = mid - 1;
+        }
+        if (pos < 0) {
+          if (v != 0.0) set_err(P.err, FL_ERR_OUTSIDE_PATTERN, row);
+          continue;
+        }
+        if (in_smem) acc[pos * THREADS + t] += v;
+        else P.val[base + pos] += v;
+      }
+      r += __ldg(P.em + (int64_t)(NK + a) * E + e);
+    }
+    if (in_smem)
+      for (int k = 0; k < L; ++k) P.val[base + k] = acc[k * THREADS + t];
+    P.rhs[row] = r;
+  }
+}
+
+template <int LOC, bool SYM, int THREADS, int RMAX>
+static int launch_pull(const PullArgs& P, cudaStream_t s) {
+  const size_t smem = (size_t)RMAX * THREADS * (sizeof(double) + sizeof(int32_t));
+  static bool configured = false;
+  if (!configured) {
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull<LOC, SYM, THREADS, RMAX>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  k_rows_pull<LOC, SYM, THREADS, RMAX><<<grid_for(P.N, THREADS, 16), THREADS, smem, s>>>(P);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
 }
 
 // Strong Dirichlet (Boundary_Conditions.F90:1983-2025).
@@ -422,11 +510,10 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     set_error("reference tensor upload failed");
     return FL_ERR_CUDA;
   }
-  // zero(matrix); zero(rhs)  (Advection_Diffusion_CG.F90:560-561)
-  k_zero<<<grid_for(m->nnz, 256), 256, 0, s>>>(val, m->nnz);
-  k_zero<<<grid_for(m->N, 256), 256, 0, s>>>(rhs, m->N);
-  FL_TRY_CUDA(cudaGetLastError());
+  // zero(matrix); zero(rhs) (Advection_Diffusion_CG.F90:560-561) happen in the
+  // row pass, which writes every entry of val and rhs.
   AsmArgs A{};
+  A.E = m->E;
   A.nd = m->ndglno.p;
   A.xnd = m->xndglno.p;
   A.X = m->coords.p;
@@ -434,11 +521,6 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   A.u = f->velocity;
   A.f = f->source;
   A.alpha = f->absorption;
-  A.findrm = m->findrm.p;
-  A.colm = m->colm.p;
-  A.val = val;
-  A.rhs = rhs;
-  A.err = m->err.p;
   A.ref = ref;
   A.theta_dt = p->dt * p->theta;
   // epsilon(0.0) is the real(8) machine epsilon under -fdefault-real-8
@@ -455,6 +537,10 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   A.have_src = p->have_source;
   A.have_abs = p->have_absorption;
   const bool closed = use_p1_closed_form(m, p);
+  const int loc = m->loc;
+  const int ncoef = closed ? 14 : loc * loc + loc;
+  FL_TRY(m->em.reserve((size_t)ncoef * m->E));
+  A.em = m->em.p;
   if (m->timing) {
     if (!m->ev0) {
       FL_TRY_CUDA(cudaEventCreate(&m->ev0));
@@ -462,18 +548,21 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     }
     FL_TRY_CUDA(cudaEventRecord(m->ev0, s));
   }
-  for (int c = 0; c < m->ncolours; ++c) {
-    A.elems = m->colour_elems.p + m->colour_ptr[c];
-    A.count = m->colour_ptr[c + 1] - m->colour_ptr[c];
-    if (A.count == 0) continue;
-    if (closed) {
-      k_asm_p1_diffusion<<<grid_for(A.count, 256, 16), 256, 0, s>>>(A);
-    } else if (m->loc == 4) {
-      k_asm_general<4><<<grid_for(A.count, 128, 16), 128, 0, s>>>(A);
-    } else {
-      k_asm_general<10><<<grid_for(A.count, 128, 16), 128, 0, s>>>(A);
-    }
-    FL_TRY_CUDA(cudaGetLastError());
+  if (closed) {
+    k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
+  } else if (loc == 4) {
+    k_asm_general<4><<<grid_for(m->E, 128, 16), 128, 0, s>>>(A);
+  } else {
+    k_asm_general<10><<<grid_for(m->E, 128, 16), 128, 0, s>>>(A);
+  }
+  FL_TRY_CUDA(cudaGetLastError());
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ndglno.p, m->findrm.p, m->colm.p, m->em.p,
+             val, rhs, m->err.p};
+  if (loc == 4) {
+    if (closed) FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
+    else FL_TRY((launch_pull<4, false, 128, 32>(P, s)));
+  } else {
+    FL_TRY((launch_pull<10, false, 64, 96>(P, s)));
   }
   if (m->timing) {
     FL_TRY_CUDA(cudaEventRecord(m->ev1, s));

@@ -113,12 +113,14 @@ struct fl_mesh_t {
   fl::DevBuf<int32_t> xndglno;       // E*4
   fl::DevBuf<double> coords;         // 3*Nx
   fl::DevBuf<int32_t> ne_ptr, ne;    // field node -> (element<<4 | local) ascending
+  fl::DevBuf<int32_t> ne_col;        // same incidences per node, ordered by element colour
   fl::DevBuf<int32_t> vne_ptr, vne;  // vertex -> element ascending
   fl::DevBuf<int32_t> findrm, colm, centrm;
   fl::DevBuf<int32_t> colour;        // E, 1-based
   fl::DevBuf<int32_t> colour_elems;  // E, sorted by (colour, element)
   std::vector<int32_t> colour_ptr;   // ncolours+1 (host)
   fl::DevBuf<fl::ErrWord> err;       // 1 word
+  fl::DevBuf<double> em;             // element matrices + rhs (coefficient-major scratch)
   // staging buffers of the host-pointer entry points (grow-only)
   fl::DevBuf<double> st_val, st_rhs, st_t, st_u, st_src, st_abs, st_x, st_g;
   fl::DevBuf<uint8_t> st_ina;

@@ -42,7 +42,7 @@ struct KspState {
   double rnorm;          // last residual norm tested
   int its, max_its, reason, done, guess_zero;
   // CG scalars
-  double beta, betaold, dpi, dpiold, alpha, pcoef;
+  double beta, betaold, dpi, dpiold, alpha, pcoef, dpi_next, beta_n, betaold_n;
   // ghost pivot reduction
   double mind, maxd, pivot;
   // GMRES
@@ -290,60 +290,137 @@ __global__ void k_cg_start(KspState* st, const double* __restrict__ part, int np
     S.beta = zr;
     S.betaold = 0.0;
     S.dpi = 0.0;
+    S.dpi_next = 0.0;
   }
 }
 
-// ------------------------------------------------------------------- CG --
-// One CG iteration i (KSPSolve_CG):
-//   checks on beta; p = z (i == 0) or z + (beta/betaold) p;
-//   w = A p; dpi = p.w; a = beta/dpi; x += a p; r -= a w; z = B r;
-//   dp = ||z||; test; beta = z.r
-__global__ void k_cg_pcheck(KspState* st, int i) {
-  note_launch();
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  KspState& S = *st;
-  if (S.done) return;
-  S.its = i + 1;
-  if (S.beta == 0.0) {
-    S.reason = FL_CONVERGED_ATOL;
-    S.done = 1;
-  } else if (i > 0 && S.beta * S.betaold < 0.0) {
-    S.reason = FL_DIVERGED_INDEFINITE_PC;
-    S.done = 1;
-  }
+// ------------------------------------------------------- CG (3 kernels) --
+// Scalars are formed redundantly by every block from the previous kernel's
+// per-block partials, summed in one fixed order, so every block sees the same
+// bits; block 0 records them in the state.  One iteration i is
+//   k_cg_p:    beta/test of iteration i-1 (from the update partials); p = z + b p
+//   k_cg_ap:   w = A p, partials of p.w
+//   k_cg_xr:   dpi, a = beta/dpi; x += a p; r -= a w; z = B r; partials z.z, z.r
+__device__ __forceinline__ double sum_fixed(const double* __restrict__ part, int n, double* red) {
+  return block_sum<kThreads>(([&] {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += kThreads) s += part[i];
+    return s;
+  })(), red);
 }
 
-// p update fused into the SpMV: every gathered p_j is formed as
-// z_j + bcoef*p_j on the fly and the row's own p_i is written back.
-template <int G>
-__global__ void k_cg_spmv(SpArgs A, const double* __restrict__ z, double* __restrict__ p, const double* pold,
-                          double* __restrict__ w, double* __restrict__ part, int i) {
+// Broadcast of a value held by thread 0 to the block.
+__device__ __forceinline__ double bcast0(double v, double* slot) {
+  if (threadIdx.x == 0) *slot = v;
+  __syncthreads();
+  const double r = *slot;
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_cg_p(int n, KspState* st, const double* __restrict__ part, int nparts, int i,
+                       const double* __restrict__ z, double* __restrict__ p) {
   note_launch();
   __shared__ double red[kThreads / 32];
-  const KspState* S = A.st;
-  if (S->done) return;
-  const double bcoef = i == 0 ? 0.0 : S->beta / S->betaold;
-  const double piv = S->pivot;
+  __shared__ double slot;
+  __shared__ int stop;
+  if (threadIdx.x == 0) stop = st->done;
+  __syncthreads();
+  if (stop) return;
+  double coef = 0.0;
+  if (i > 0) {
+    // end of iteration i-1: dp = ||z||, test, beta = z.r; then the checks that
+    // open iteration i (KSPSolve_CG).  Every block decides from the committed
+    // state; block 0 publishes the new beta only through the pending fields.
+    const double zz = sum_fixed(part, nparts, red);
+    const double zr = sum_fixed(part + nparts, nparts, red);
+    if (threadIdx.x == 0) {
+      KspState S = *st;
+      converged_test(S, i, sqrt(zz));
+      int its = i;
+      if (!S.done) {
+        S.betaold = S.beta;
+        S.beta = zr;
+        if (i >= S.max_its) {
+          S.reason = FL_DIVERGED_ITS;
+          S.done = 1;
+        }
+      }
+      if (!S.done) {
+        its = i + 1;
+        if (S.beta == 0.0) {
+          S.reason = FL_CONVERGED_ATOL;
+          S.done = 1;
+        } else if (S.beta * S.betaold < 0.0) {
+          S.reason = FL_DIVERGED_INDEFINITE_PC;
+          S.done = 1;
+        }
+      }
+      if (blockIdx.x == 0) {
+        st->rnorm = S.rnorm;
+        st->its = its;
+        st->beta_n = S.beta;
+        st->betaold_n = S.betaold;
+        if (S.done) {
+          st->reason = S.reason;
+          st->done = 1;
+        }
+      }
+      coef = S.beta / S.betaold;
+      stop = S.done;
+    }
+    __syncthreads();
+    if (stop) return;
+    coef = bcast0(coef, &slot);
+  } else {
+    // iteration 0: beta of the initial residual (k_cg_start)
+    if (threadIdx.x == 0) {
+      const int d = st->beta == 0.0;
+      if (blockIdx.x == 0) {
+        st->its = 1;
+        st->beta_n = st->beta;
+        st->betaold_n = st->betaold;
+        if (d) {
+          st->reason = FL_CONVERGED_ATOL;
+          st->done = 1;
+        }
+      }
+      stop = d;
+    }
+    __syncthreads();
+    if (stop) return;
+  }
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    p[k] = i == 0 ? z[k] : z[k] + coef * p[k];
+}
+
+// Publishes the scalars of k_cg_p (beta, betaold) and of the previous k_cg_xr
+// (dpi) once no block of those launches reads them any more.
+__global__ void k_cg_commit(KspState* st) {
+  note_launch();
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    st->beta = st->beta_n;
+    st->betaold = st->betaold_n;
+    st->dpi = st->dpi_next;
+  }
+}
+
+template <int G>
+__global__ void k_cg_ap(SpArgs A, const double* __restrict__ p, double* __restrict__ w,
+                        double* __restrict__ part) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (A.st->done) return;
+  const double piv = A.st->pivot;
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
   double pw = 0.0;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
-    double s = 0.0;
-    if (row < A.n) {
-      const int b = __ldg(A.findrm + row), e = __ldg(A.findrm + row + 1);
-      for (int k = b + sub; k < e; k += G) {
-        const int j = __ldg(A.colm + k);
-        const double pj = i == 0 ? z[j] : z[j] + bcoef * pold[j];
-        s += __ldg(A.val + k) * pj;
-      }
-    }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    double s = row_dot<G>(A.findrm, A.colm, A.val, p, row, sub, row < A.n);
     if (row < A.n && sub == 0) {
-      const double pi = i == 0 ? z[row] : z[row] + bcoef * pold[row];
+      const double pi = p[row];
       if (A.ghost && A.ghost[row]) s = piv * pi;
-      p[row] = pi;
       w[row] = s;
       pw += pi * s;
     }
@@ -352,66 +429,54 @@ __global__ void k_cg_spmv(SpArgs A, const double* __restrict__ z, double* __rest
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
 }
 
-__global__ void k_cg_alpha(KspState* st, const double* __restrict__ part, int nparts, int i) {
+__global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ pin, int npin, int i,
+                        const double* __restrict__ p, const double* __restrict__ w,
+                        const double* __restrict__ dinv, double* __restrict__ y, double* __restrict__ r,
+                        double* __restrict__ z, double* __restrict__ part, int nparts) {
   note_launch();
   __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  const double dpi = reduce_partials(part, nparts, red);
+  __shared__ double slot;
+  __shared__ int stop;
+  if (threadIdx.x == 0) stop = st->done;
+  __syncthreads();
+  if (stop) return;
+  const double dpi = sum_fixed(pin, npin, red);
+  double a = 0.0;
   if (threadIdx.x == 0) {
-    KspState& S = *st;
-    S.dpiold = S.dpi;
-    S.dpi = dpi;
-    S.betaold = S.beta;
-    if (dpi == 0.0 || (i > 0 && dpi * S.dpiold <= 0.0)) {
-      S.reason = FL_DIVERGED_INDEFINITE_MAT;
-      S.done = 1;
-    } else {
-      S.alpha = S.beta / dpi;
+    const double dpiold = st->dpi;
+    const double beta = st->beta;
+    int d = 0;
+    if (dpi == 0.0 || (i > 0 && dpi * dpiold <= 0.0)) d = 1;
+    a = beta / dpi;
+    stop = d;
+    // every block reads dpiold before block 0 overwrites it: the write is
+    // deferred to k_cg_p of the next iteration via dpi_next
+    if (blockIdx.x == 0) {
+      st->dpi_next = dpi;
+      if (d) {
+        st->reason = FL_DIVERGED_INDEFINITE_MAT;
+        st->done = 1;
+      }
     }
   }
-}
-
-__global__ void k_cg_update(int n, KspState* st, const double* __restrict__ p, const double* __restrict__ w,
-                            const double* __restrict__ dinv, double* __restrict__ y, double* __restrict__ r,
-                            double* __restrict__ z, double* __restrict__ part, int nparts) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  const double a = st->alpha;
+  __syncthreads();
+  if (stop) return;
+  a = bcast0(a, &slot);
   double zz = 0.0, zr = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    y[i] += a * p[i];
-    const double ri = r[i] - a * w[i];
-    const double zi = ri * dinv[i];
-    r[i] = ri;
-    z[i] = zi;
-    zz += zi * zi;
-    zr += zi * ri;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    y[k] += a * p[k];
+    const double rk = r[k] - a * w[k];
+    const double zk = rk * dinv[k];
+    r[k] = rk;
+    z[k] = zk;
+    zz += zk * zk;
+    zr += zk * rk;
   }
   zz = block_sum<kThreads>(zz, red);
   zr = block_sum<kThreads>(zr, red);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[nparts + blockIdx.x] = zr;
-  }
-}
-
-__global__ void k_cg_test(KspState* st, const double* __restrict__ part, int nparts, int i) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  const double zz = reduce_partials(part, nparts, red);
-  const double zr = reduce_partials(part + nparts, nparts, red);
-  if (threadIdx.x == 0) {
-    KspState& S = *st;
-    converged_test(S, i + 1, sqrt(zz));
-    if (!S.done) {
-      S.beta = zr;
-      if (i + 1 >= S.max_its) {
-        S.reason = FL_DIVERGED_ITS;
-        S.done = 1;
-      }
-    }
   }
 }
 
@@ -909,20 +974,18 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
     k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
     FL_TRY_CUDA(cudaGetLastError());
-    // p and w double-buffer through (p, w) and (w, p): the fused SpMV reads the
-    // old p while writing the new one, so they alternate between two arrays.
-    double* pbuf[2] = {W->p.p, W->w.p};
     FL_TRY(W->w2.reserve(n));
-    double* wv = W->w2.p;
-    for (int i = 0; i < o->max_its; ++i) {
-      double* pnew = pbuf[i & 1];
-      double* pold = pbuf[(i + 1) & 1];
-      k_cg_pcheck<<<1, 32, 0, s>>>(st, i);
-      FL_SPMV_DISPATCH(G, k_cg_spmv, A, W->z.p, pnew, pold, wv, W->part.p, i);
-      k_cg_alpha<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, i);
-      k_cg_update<<<gv, kThreads, 0, s>>>(n, st, pnew, wv, W->dinv.p, W->y.p, W->r.p, W->z.p, W->part.p, (int)gv);
-      k_cg_test<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, i);
-      if ((i + 1) % chunk == 0 || i + 1 == o->max_its) {
+    // partial buffers: [0, gsp) p.w ; [2*np, 2*np + 2*gv) z.z and z.r
+    double* part_pw = W->part.p;
+    double* part_zz = W->part.p + 2 * np;
+    for (int i = 0; i < o->max_its + 1; ++i) {
+      k_cg_p<<<gv, kThreads, 0, s>>>(n, st, part_zz, (int)gv, i, W->z.p, W->p.p);
+      k_cg_commit<<<1, 32, 0, s>>>(st);
+      if (i == o->max_its) break;  // final test only
+      FL_SPMV_DISPATCH(G, k_cg_ap, A, W->p.p, W->w2.p, part_pw);
+      k_cg_xr<<<gv, kThreads, 0, s>>>(n, st, part_pw, (int)gsp, i, W->p.p, W->w2.p, W->dinv.p, W->y.p,
+                                       W->r.p, W->z.p, part_zz, (int)gv);
+      if ((i + 1) % chunk == 0) {
         FL_TRY_CUDA(cudaGetLastError());
         int done = 0;
         FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -930,6 +993,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
         if (done) break;
       }
     }
+    FL_TRY_CUDA(cudaGetLastError());
   } else if (!mixed) {
     // GMRES(restart)
     const int64_t ld = n;

@@ -424,6 +424,29 @@ __global__ void k_scatter_colour(const int32_t* __restrict__ colour, int32_t E, 
     if (colour[e] == c) out[base + pos[e]] = e;
 }
 
+// Each node's incidences reordered by the colour of their element.  A node
+// meets at most one element of each colour, so the order is total; it is the
+// order in which the reference's coloured loop (Advection_Diffusion_CG.F90:582-598)
+// adds the elements' contributions to that node's row.
+__global__ void k_sort_by_colour(const int32_t* __restrict__ ptr, const int32_t* __restrict__ ne,
+                                 const int32_t* __restrict__ colour, int32_t* __restrict__ out, int32_t n) {
+  note_launch();
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int b = ptr[v], e = ptr[v + 1];
+    for (int i = b; i < e; ++i) out[i] = ne[i];
+    for (int i = b + 1; i < e; ++i) {
+      const int x = out[i];
+      const int cx = colour[x >> 4];
+      int j = i - 1;
+      while (j >= b && colour[out[j] >> 4] > cx) {
+        out[j + 1] = out[j];
+        --j;
+      }
+      out[j + 1] = x;
+    }
+  }
+}
+
 static int build_colouring(fl_mesh_t* m, cudaStream_t s) {
   const int32_t E = m->E;
   FL_TRY(m->vne_ptr.reserve(m->Nx + 1));
@@ -585,6 +608,13 @@ extern "C" int fl_gpu_mesh_register(const fl_mesh_desc* d, fl_mesh* out) {
     if ((st = build_sparsity(m->ndglno.p, m->loc, m->N, m->ne_ptr, m->ne, m->findrm, m->colm, m->centrm,
                              &m->nnz, m->err.p, s)) != FL_OK) break;
     if ((st = build_colouring(m, s)) != FL_OK) break;
+    if ((st = m->ne_col.reserve((size_t)m->E * m->loc)) != FL_OK) break;
+    k_sort_by_colour<<<grid_for(m->N, 128), 128, 0, s>>>(m->ne_ptr.p, m->ne.p, m->colour.p, m->ne_col.p, m->N);
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+      set_error("colour ordering of incidences failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
   } while (0);
   if (st != FL_OK) {
     if (m->stream) cudaStreamDestroy(m->stream);
