@@ -335,7 +335,22 @@ __global__ void k_cg_p(int n, KspState* st, const double* __restrict__ part, int
     const double zz = sum_fixed(part, nparts, red);
     const double zr = sum_fixed(part + nparts, nparts, red);
     if (threadIdx.x == 0) {
-      KspState S = *st;
+      // copy only the scalars the decision needs (the GMRES arrays of the
+      // state stay in global memory)
+      KspState& G = *st;
+      KspState S;
+      S.rtol = G.rtol;
+      S.atol = G.atol;
+      S.dtol = G.dtol;
+      S.rnorm0 = G.rnorm0;
+      S.ttol = G.ttol;
+      S.snorm_b = G.snorm_b;
+      S.guess_zero = G.guess_zero;
+      S.max_its = G.max_its;
+      S.reason = 0;
+      S.done = 0;
+      S.beta = G.beta;
+      S.betaold = G.betaold;
       converged_test(S, i, sqrt(zz));
       int its = i;
       if (!S.done) {
