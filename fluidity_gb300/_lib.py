@@ -78,6 +78,7 @@ EXPORTS = [
     "fl_gpu_assemble_advdif_cg", "fl_dev_assemble_advdif_cg", "fl_gpu_apply_dirichlet",
     "fl_dev_apply_dirichlet", "fl_gpu_petsc_solve", "fl_dev_petsc_solve", "fl_dev_csr_mult",
     "fl_kernel_launch_count", "fl_set_kernel_timing", "fl_last_assembly_kernel_ms",
+    "fl_dev_assemble_p1_diffusion_noalloc",
 ]
 
 _P = C.c_void_p
@@ -98,6 +99,8 @@ _SIGNATURES = {
                                             _P]),
     "fl_dev_assemble_advdif_cg": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(Fields), _P,
                                             _P, _P]),
+    "fl_dev_assemble_p1_diffusion_noalloc": (C.c_int, [_P, C.POINTER(AdvDifParams),
+                                                       C.POINTER(Fields), _P, _P, _P]),
     "fl_gpu_apply_dirichlet": (C.c_int, [_P, _I32, _P, _I32, _P, _P, _D, _P, _P]),
     "fl_dev_apply_dirichlet": (C.c_int, [_P, _I32, _P, _I32, _P, _P, _D, _P, _P, _P]),
     "fl_gpu_petsc_solve": (C.c_int, [_P, C.POINTER(SolverOpts), _P, _P, _P, _P,

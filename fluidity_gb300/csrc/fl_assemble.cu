@@ -628,6 +628,104 @@ extern "C" int fl_last_assembly_kernel_ms(fl_mesh m, float* ms) {
   return FL_OK;
 }
 
+namespace fl {
+
+// ------------------------------------------------- allocation-free variant --
+// Some callers cannot allocate device memory at the point where they assemble:
+// a host application whose memory manager has reserved the device's memory
+// up front, or a time-stepping loop that must not call cudaMalloc (which can
+// synchronise the whole device).  For them, the P1 diffusion assembly (the
+// pressure-Poisson form) runs with its element-matrix scratch in a fixed,
+// file-scope device array instead of the handle's grow-only buffer.
+//
+// Limit: meshes of at most kNoAllocMaxElements elements (14 doubles of scratch
+// per element, 14.7 MB held by every GPU that loads the library until exit).
+// The array is shared by every call: the element pass writes every value the
+// row pass reads, so nothing needs clearing between calls, but calls whose
+// work overlaps on the GPU (different streams or threads) race on it.
+constexpr int kNoAllocMaxElements = 131072;
+constexpr int kNoAllocCoef = 14;  // 10 symmetric matrix entries + 4 rhs entries
+static __device__ __align__(256) double g_noalloc_em[(size_t)kNoAllocCoef * kNoAllocMaxElements];
+static __device__ __align__(256) RefTensors g_noalloc_ref[4];  // quadrature degrees 1..4
+
+// Host-side device addresses of the arrays above, resolved once per device by
+// cudaGetSymbolAddress (the array's name in host code is not a device address).
+struct NoAllocDevice {
+  bool ready = false;
+  double* em = nullptr;
+  RefTensors* ref = nullptr;
+};
+static std::mutex g_noalloc_mu;
+static NoAllocDevice g_noalloc_dev[64];
+
+static int noalloc_setup(int dev, NoAllocDevice** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  FL_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal");
+  NoAllocDevice& d = g_noalloc_dev[dev];
+  if (!d.ready) {
+    void* p = nullptr;
+    FL_TRY_CUDA(cudaGetSymbolAddress(&p, g_noalloc_em));
+    d.em = static_cast<double*>(p);
+    FL_TRY_CUDA(cudaGetSymbolAddress(&p, g_noalloc_ref));
+    d.ref = static_cast<RefTensors*>(p);
+    for (int q = 1; q <= 4; ++q) {
+      RefTensors h;
+      build_tensors(1, q, h);
+      FL_TRY_CUDA(cudaMemcpyToSymbol(g_noalloc_ref, &h, sizeof(RefTensors), sizeof(RefTensors) * (q - 1),
+                                     cudaMemcpyHostToDevice));
+    }
+    d.ready = true;
+  }
+  *out = &d;
+  return FL_OK;
+}
+
+}  // namespace fl
+
+extern "C" int fl_dev_assemble_p1_diffusion_noalloc(fl_mesh m, const fl_advdif_params* p, const fl_fields* f,
+                                                    double* val, double* rhs, void* stream) {
+  using namespace fl;
+  FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
+  FL_CHECK_ARG(m->loc == 4, "allocation-free assembly supports P1 field meshes only");
+  FL_CHECK_ARG(use_p1_closed_form(m, p), "allocation-free assembly supports the diffusion form only "
+               "(diffusivity, optional source and consistent mass; no advection or absorption)");
+  FL_CHECK_ARG(p->quad_degree >= 1 && p->quad_degree <= 4, "quadrature degree 1..4");
+  FL_CHECK_ARG(!p->have_source || f->source, "source field missing");
+  if (m->E > kNoAllocMaxElements) {
+    set_error("invalid argument: %d elements exceed the allocation-free limit of %d", m->E,
+              kNoAllocMaxElements);
+    return FL_ERR_ARG;
+  }
+  int dev = 0;
+  FL_TRY_CUDA(cudaGetDevice(&dev));
+  NoAllocDevice* d = nullptr;
+  FL_TRY(noalloc_setup(dev, &d));
+  cudaStream_t s = stream ? (cudaStream_t)stream : m->stream;
+  AsmArgs A{};
+  A.E = m->E;
+  A.nd = m->ndglno.p;
+  A.xnd = m->xndglno.p;
+  A.X = m->coords.p;
+  A.t = f->t;
+  A.f = f->source;
+  A.em = d->em;
+  A.ref = d->ref + (p->quad_degree - 1);
+  A.theta_dt = p->dt * p->theta;
+  const double eps = 2.220446049250313e-16;
+  A.use_dt = fabs(A.theta_dt) > eps;
+  for (int k = 0; k < 9; ++k) A.kappa[k] = p->diffusivity[k];
+  A.have_mass = p->have_mass;
+  A.have_diff = p->have_diffusivity;
+  A.iso = p->isotropic_diffusivity;
+  A.have_src = p->have_source;
+  k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
+  FL_TRY_CUDA(cudaGetLastError());
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ndglno.p, m->findrm.p, m->colm.p, d->em,
+             val, rhs, m->err.p};
+  FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
+  return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
+}
+
 extern "C" int fl_dev_apply_dirichlet(fl_mesh m, int32_t nb, const int32_t* nodes, int32_t base,
                                       const double* g, const double* t, double dt, double* rhs,
                                       uint8_t* inactive, void* stream) {

@@ -155,6 +155,24 @@ int fl_dev_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
                               const fl_fields* fields, double* val, double* rhs,
                               void* stream);
 
+/* Allocation-free form of fl_dev_assemble_advdif_cg for the P1 diffusion
+ * (pressure-Poisson) case: diffusivity with optional source and consistent
+ * mass, no advection or absorption, on a P1 field mesh.  No counterpart in the
+ * reference.  It exists for callers that cannot allocate device memory when
+ * they assemble -- an application whose memory manager has already reserved
+ * the device, or a loop that must not call cudaMalloc because it can
+ * synchronise the device.  The call allocates nothing: its element-matrix
+ * scratch is a fixed array inside the library sized for at most 131072
+ * elements (14.7 MB held on every GPU that loads the library); larger meshes
+ * are rejected with FL_ERR_ARG.  The first call on a device also looks up
+ * that array's device address and uploads the reference-element tables, so
+ * make the first call on each device before any stream capture.  Every call
+ * shares the array, so calls whose GPU work overlaps (other streams or
+ * threads) race.  Device pointers; results equal fl_dev_assemble_advdif_cg's. */
+int fl_dev_assemble_p1_diffusion_noalloc(fl_mesh mesh, const fl_advdif_params* params,
+                                         const fl_fields* fields, double* val, double* rhs,
+                                         void* stream);
+
 /* Strong Dirichlet (apply_dirichlet_conditions_scalar,
  * femtools/Boundary_Conditions.F90:1983-2025): marks rows inactive
  * (csr_set_inactive_rows, femtools/Sparse_Tools.F90:2136) and sets
