@@ -65,6 +65,7 @@ struct KrylovWork {
   DevBuf<float> val32;  // fp32 copy of the matrix (mixed precision)
   DevBuf<float> r32, z32, p32, w32, d32, dinv32;
   DevBuf<KspState> st;
+  DevBuf<unsigned> ticket;  // retire counters of the last-block reductions
 };
 
 static KrylovWork* work_of(fl_mesh_t* m);
@@ -86,10 +87,12 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return v;  // valid in thread 0
 }
 
-// Sum of `n` partials in a fixed order by one block.
+// Sum of `n` partials in a fixed order by one block.  The partials were
+// written by other blocks (possibly of the same launch), so they are read at
+// L2 (__ldcg), never from this SM's L1.
 __device__ double reduce_partials(const double* __restrict__ part, int n, double* red) {
   double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += kThreads) s += part[i];
+  for (int i = threadIdx.x; i < n; i += kThreads) s += __ldcg(part + i);
   return block_sum<kThreads>(s, red);
 }
 
@@ -295,138 +298,48 @@ __global__ void k_cg_start(KspState* st, const double* __restrict__ part, int np
 }
 
 // ------------------------------------------------------- CG (3 kernels) --
-// Scalars are formed redundantly by every block from the previous kernel's
-// per-block partials, summed in one fixed order, so every block sees the same
-// bits; block 0 records them in the state.  One iteration i is
-//   k_cg_p:    beta/test of iteration i-1 (from the update partials); p = z + b p
-//   k_cg_ap:   w = A p, partials of p.w
-//   k_cg_xr:   dpi, a = beta/dpi; x += a p; r -= a w; z = B r; partials z.z, z.r
-__device__ __forceinline__ double sum_fixed(const double* __restrict__ part, int n, double* red) {
-  return block_sum<kThreads>(([&] {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < n; i += kThreads) s += part[i];
-    return s;
-  })(), red);
-}
+// One iteration i of KSPSolve_CG in three launches; each global reduction is
+// finished by the last block of its launch to retire (a ticket counter), which
+// sums the per-block partials in block order -- one fixed order, so results
+// are deterministic -- and publishes the scalars for the next launch:
+//   k_cg_p:   p = z (i == 0) or z + (beta/betaold) p
+//   k_cg_ap:  w = A p; partials of p.w; last block: dpi, checks, a = beta/dpi
+//   k_cg_xr:  x += a p; r -= a w; z = B r; partials of z.z and z.r;
+//             last block: dp = ||z||, test, beta = z.r, checks of iteration i+1
+// A launch whose state is `done` returns at once (the host polls `done`).
 
-// Broadcast of a value held by thread 0 to the block.
-__device__ __forceinline__ double bcast0(double v, double* slot) {
-  if (threadIdx.x == 0) *slot = v;
+// True in the block that retires last; its threads then see every block's
+// partials.  The counter is reset for the next launch.
+__device__ __forceinline__ bool last_block(unsigned* ticket) {
+  __shared__ bool last;
+  __threadfence();
   __syncthreads();
-  const double r = *slot;
-  __syncthreads();
-  return r;
-}
-
-__global__ void k_cg_p(int n, KspState* st, const double* __restrict__ part, int nparts, int i,
-                       const double* __restrict__ z, double* __restrict__ p) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  __shared__ double slot;
-  __shared__ int stop;
-  if (threadIdx.x == 0) stop = st->done;
-  __syncthreads();
-  if (stop) return;
-  double coef = 0.0;
-  if (i > 0) {
-    // end of iteration i-1: dp = ||z||, test, beta = z.r; then the checks that
-    // open iteration i (KSPSolve_CG).  Every block decides from the committed
-    // state; block 0 publishes the new beta only through the pending fields.
-    const double zz = sum_fixed(part, nparts, red);
-    const double zr = sum_fixed(part + nparts, nparts, red);
-    if (threadIdx.x == 0) {
-      // copy only the scalars the decision needs (the GMRES arrays of the
-      // state stay in global memory)
-      KspState& G = *st;
-      KspState S;
-      S.rtol = G.rtol;
-      S.atol = G.atol;
-      S.dtol = G.dtol;
-      S.rnorm0 = G.rnorm0;
-      S.ttol = G.ttol;
-      S.snorm_b = G.snorm_b;
-      S.guess_zero = G.guess_zero;
-      S.max_its = G.max_its;
-      S.reason = 0;
-      S.done = 0;
-      S.beta = G.beta;
-      S.betaold = G.betaold;
-      converged_test(S, i, sqrt(zz));
-      int its = i;
-      if (!S.done) {
-        S.betaold = S.beta;
-        S.beta = zr;
-        if (i >= S.max_its) {
-          S.reason = FL_DIVERGED_ITS;
-          S.done = 1;
-        }
-      }
-      if (!S.done) {
-        its = i + 1;
-        if (S.beta == 0.0) {
-          S.reason = FL_CONVERGED_ATOL;
-          S.done = 1;
-        } else if (S.beta * S.betaold < 0.0) {
-          S.reason = FL_DIVERGED_INDEFINITE_PC;
-          S.done = 1;
-        }
-      }
-      if (blockIdx.x == 0) {
-        st->rnorm = S.rnorm;
-        st->its = its;
-        st->beta_n = S.beta;
-        st->betaold_n = S.betaold;
-        if (S.done) {
-          st->reason = S.reason;
-          st->done = 1;
-        }
-      }
-      coef = S.beta / S.betaold;
-      stop = S.done;
-    }
-    __syncthreads();
-    if (stop) return;
-    coef = bcast0(coef, &slot);
-  } else {
-    // iteration 0: beta of the initial residual (k_cg_start)
-    if (threadIdx.x == 0) {
-      const int d = st->beta == 0.0;
-      if (blockIdx.x == 0) {
-        st->its = 1;
-        st->beta_n = st->beta;
-        st->betaold_n = st->betaold;
-        if (d) {
-          st->reason = FL_CONVERGED_ATOL;
-          st->done = 1;
-        }
-      }
-      stop = d;
-    }
-    __syncthreads();
-    if (stop) return;
+  if (threadIdx.x == 0) {
+    const unsigned t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+    if (last) *ticket = 0u;
   }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+__global__ void k_cg_p(int n, const KspState* st, int i, const double* __restrict__ z, double* __restrict__ p) {
+  note_launch();
+  if (st->done) return;
+  const double coef = st->pcoef;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     p[k] = i == 0 ? z[k] : z[k] + coef * p[k];
 }
 
-// Publishes the scalars of k_cg_p (beta, betaold) and of the previous k_cg_xr
-// (dpi) once no block of those launches reads them any more.
-__global__ void k_cg_commit(KspState* st) {
-  note_launch();
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    st->beta = st->beta_n;
-    st->betaold = st->betaold_n;
-    st->dpi = st->dpi_next;
-  }
-}
-
 template <int G>
 __global__ void k_cg_ap(SpArgs A, const double* __restrict__ p, double* __restrict__ w,
-                        double* __restrict__ part) {
+                        double* __restrict__ part, unsigned* ticket, int i) {
   note_launch();
   __shared__ double red[kThreads / 32];
-  if (A.st->done) return;
-  const double piv = A.st->pivot;
+  KspState* st = A.st;
+  if (st->done) return;
+  const double piv = st->pivot;
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
   double pw = 0.0;
@@ -442,41 +355,29 @@ __global__ void k_cg_ap(SpArgs A, const double* __restrict__ p, double* __restri
   }
   pw = block_sum<kThreads>(pw, red);
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
-}
-
-__global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ pin, int npin, int i,
-                        const double* __restrict__ p, const double* __restrict__ w,
-                        const double* __restrict__ dinv, double* __restrict__ y, double* __restrict__ r,
-                        double* __restrict__ z, double* __restrict__ part, int nparts) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  __shared__ double slot;
-  __shared__ int stop;
-  if (threadIdx.x == 0) stop = st->done;
-  __syncthreads();
-  if (stop) return;
-  const double dpi = sum_fixed(pin, npin, red);
-  double a = 0.0;
+  if (!last_block(ticket)) return;
+  const double dpi = reduce_partials(part, gridDim.x, red);
   if (threadIdx.x == 0) {
-    const double dpiold = st->dpi;
-    const double beta = st->beta;
-    int d = 0;
-    if (dpi == 0.0 || (i > 0 && dpi * dpiold <= 0.0)) d = 1;
-    a = beta / dpi;
-    stop = d;
-    // every block reads dpiold before block 0 overwrites it: the write is
-    // deferred to k_cg_p of the next iteration via dpi_next
-    if (blockIdx.x == 0) {
-      st->dpi_next = dpi;
-      if (d) {
-        st->reason = FL_DIVERGED_INDEFINITE_MAT;
-        st->done = 1;
-      }
+    KspState& S = *st;
+    S.dpiold = S.dpi;
+    S.dpi = dpi;
+    S.betaold = S.beta;
+    if (dpi == 0.0 || (i > 0 && dpi * S.dpiold <= 0.0)) {
+      S.reason = FL_DIVERGED_INDEFINITE_MAT;
+      S.done = 1;
+    } else {
+      S.alpha = S.beta / dpi;
     }
   }
-  __syncthreads();
-  if (stop) return;
-  a = bcast0(a, &slot);
+}
+
+__global__ void k_cg_xr(int n, KspState* st, int i, const double* __restrict__ p, const double* __restrict__ w,
+                        const double* __restrict__ dinv, double* __restrict__ y, double* __restrict__ r,
+                        double* __restrict__ z, double* __restrict__ part, unsigned* ticket) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  if (st->done) return;
+  const double a = st->alpha;
   double zz = 0.0, zr = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     y[k] += a * p[k];
@@ -491,7 +392,50 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ pin, int
   zr = block_sum<kThreads>(zr, red);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
-    part[nparts + blockIdx.x] = zr;
+    part[gridDim.x + blockIdx.x] = zr;
+  }
+  if (!last_block(ticket)) return;
+  const double zzs = reduce_partials(part, gridDim.x, red);
+  const double zrs = reduce_partials(part + gridDim.x, gridDim.x, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    converged_test(S, i + 1, sqrt(zzs));  // KSPConvergedDefault at iteration i+1
+    if (!S.done) {
+      S.beta = zrs;
+      if (i + 1 >= S.max_its) {
+        S.reason = FL_DIVERGED_ITS;
+        S.done = 1;
+      }
+    }
+    if (!S.done) {
+      // opening checks of iteration i+1
+      S.its = i + 2;
+      if (S.beta == 0.0) {
+        S.reason = FL_CONVERGED_ATOL;
+        S.done = 1;
+        S.its = i + 2;
+      } else if (S.beta * S.betaold < 0.0) {
+        S.reason = FL_DIVERGED_INDEFINITE_PC;
+        S.done = 1;
+      }
+      S.pcoef = S.beta / S.betaold;
+    } else {
+      S.its = i + 1;
+    }
+  }
+}
+
+// Opening checks of iteration 0 (beta of the initial residual).
+__global__ void k_cg_open(KspState* st) {
+  note_launch();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  KspState& S = *st;
+  if (S.done) return;
+  S.its = 1;
+  S.pcoef = 0.0;
+  if (S.beta == 0.0) {
+    S.reason = FL_CONVERGED_ATOL;
+    S.done = 1;
   }
 }
 
@@ -765,15 +709,23 @@ struct SpArgs32 {
   const uint8_t* ghost;
 };
 
-// Inner CG state lives in KspState fields reused: beta/betaold/dpi/alpha; the
-// inner convergence uses rnorm0 of the inner problem in `ttol`.
+// Inner CG of the refinement, same three-launch structure as the FP64 CG:
+// fp32 matrix and vectors, fp64 dot products and scalars.  The inner problem
+// starts from d = 0 and stops when ||B r|| <= ttol (set by the outer loop).
+__global__ void k_cg32_p(int n, const KspState* st, int i, const float* __restrict__ z, float* __restrict__ p) {
+  note_launch();
+  if (st->done) return;
+  const float coef = (float)st->pcoef;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    p[k] = i == 0 ? z[k] : fmaf(coef, p[k], z[k]);
+}
+
 template <int G>
-__global__ void k_cg32_spmv(SpArgs32 A, KspState* st, float piv, const float* __restrict__ z,
-                            float* __restrict__ p, float* __restrict__ w, double* __restrict__ part, int i) {
+__global__ void k_cg32_ap(SpArgs32 A, KspState* st, float piv, const float* __restrict__ p,
+                          float* __restrict__ w, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   if (st->done) return;
-  const float bcoef = i == 0 ? 0.0f : (float)(st->beta / st->betaold);
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
   double pw = 0.0;
@@ -782,18 +734,12 @@ __global__ void k_cg32_spmv(SpArgs32 A, KspState* st, float piv, const float* __
     float s = 0.0f;
     if (row < A.n) {
       const int b = __ldg(A.findrm + row), e = __ldg(A.findrm + row + 1);
-      for (int k = b + sub; k < e; k += G) {
-        const int j = __ldg(A.colm + k);
-        const float pj = i == 0 ? z[j] : fmaf(bcoef, p[j], z[j]);
-        s = fmaf(__ldg(A.val + k), pj, s);
-      }
+      for (int k = b + sub; k < e; k += G) s = fmaf(__ldg(A.val + k), p[__ldg(A.colm + k)], s);
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
-    // p is updated in place only after every gather of this launch: write to w's
-    // partner buffer first (w holds A p), p update happens in k_cg32_update.
     if (row < A.n && sub == 0) {
-      const float pi = i == 0 ? z[row] : fmaf(bcoef, p[row], z[row]);
+      const float pi = p[row];
       if (A.ghost && A.ghost[row]) s = piv * pi;
       w[row] = s;
       pw += (double)pi * (double)s;
@@ -801,22 +747,30 @@ __global__ void k_cg32_spmv(SpArgs32 A, KspState* st, float piv, const float* __
   }
   pw = block_sum<kThreads>(pw, red);
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
+  if (!last_block(ticket)) return;
+  const double dpi = reduce_partials(part, gridDim.x, red);
+  if (threadIdx.x == 0) {
+    KspState& S = *st;
+    S.betaold = S.beta;
+    if (dpi <= 0.0 || dpi != dpi) {
+      S.reason = FL_DIVERGED_INDEFINITE_MAT;  // inner breakdown: the outer loop decides
+      S.done = 1;
+    } else {
+      S.alpha = S.beta / dpi;
+    }
+  }
 }
 
-__global__ void k_cg32_update(int n, KspState* st, const float* __restrict__ z_in, float* __restrict__ p,
-                              const float* __restrict__ w, const float* __restrict__ dinv,
-                              float* __restrict__ d, float* __restrict__ r, float* __restrict__ z,
-                              double* __restrict__ part, int nparts, int i) {
+__global__ void k_cg32_xr(int n, KspState* st, int i, const float* __restrict__ p, const float* __restrict__ w,
+                          const float* __restrict__ dinv, float* __restrict__ d, float* __restrict__ r,
+                          float* __restrict__ z, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   if (st->done) return;
-  const float bcoef = (float)st->pcoef;
   const float a = (float)st->alpha;
   double zz = 0.0, zr = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const float pk = i == 0 ? z_in[k] : fmaf(bcoef, p[k], z_in[k]);
-    p[k] = pk;
-    d[k] = fmaf(a, pk, d[k]);
+    d[k] = fmaf(a, p[k], d[k]);
     const float rk = fmaf(-a, w[k], r[k]);
     const float zk = rk * dinv[k];
     r[k] = rk;
@@ -828,52 +782,27 @@ __global__ void k_cg32_update(int n, KspState* st, const float* __restrict__ z_i
   zr = block_sum<kThreads>(zr, red);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
-    part[nparts + blockIdx.x] = zr;
+    part[gridDim.x + blockIdx.x] = zr;
   }
-}
-
-__global__ void k_cg32_alpha(KspState* st, const double* __restrict__ part, int nparts, int i) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  const double dpi = reduce_partials(part, nparts, red);
-  if (threadIdx.x == 0) {
-    KspState& S = *st;
-    S.pcoef = i == 0 ? 0.0 : S.beta / S.betaold;
-    S.dpiold = S.dpi;
-    S.dpi = dpi;
-    S.betaold = S.beta;
-    if (dpi <= 0.0 || dpi != dpi) {
-      S.done = 1;  // inner breakdown: outer loop decides
-      S.reason = FL_DIVERGED_INDEFINITE_MAT;
-    } else {
-      S.alpha = S.beta / dpi;
-    }
-  }
-}
-
-__global__ void k_cg32_test(KspState* st, const double* __restrict__ part, int nparts, int i) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  const double zz = reduce_partials(part, nparts, red);
-  const double zr = reduce_partials(part + nparts, nparts, red);
+  if (!last_block(ticket)) return;
+  const double zzs = reduce_partials(part, gridDim.x, red);
+  const double zrs = reduce_partials(part + gridDim.x, gridDim.x, red);
   if (threadIdx.x == 0) {
     KspState& S = *st;
     S.its = i + 1;
-    S.rnorm = sqrt(zz);
+    S.rnorm = sqrt(zzs);
     if (!(S.rnorm == S.rnorm)) {
       S.reason = FL_DIVERGED_NANORINF;
       S.done = 1;
     } else if (S.rnorm <= S.ttol) {
       S.reason = FL_CONVERGED_RTOL;
       S.done = 1;
+    } else if (i + 1 >= S.max_its) {
+      S.reason = FL_DIVERGED_ITS;
+      S.done = 1;
     } else {
-      S.beta = zr;
-      if (i + 1 >= S.max_its) {
-        S.reason = FL_DIVERGED_ITS;
-        S.done = 1;
-      }
+      S.beta = zrs;
+      S.pcoef = S.beta / S.betaold;
     }
   }
 }
@@ -928,16 +857,25 @@ struct Launch {
   int nparts;
 };
 
+// Lanes per CSR row in the FP64 SpMV kernels.  FP64 throughput is scarce on
+// this part, and each level of the in-group shuffle reduction costs a DADD on
+// every lane, so short rows use two lanes.
 static int group_for(const fl_mesh_t* m) {
   const double avg = (double)m->nnz / (double)(m->N > 0 ? m->N : 1);
-  if (avg > 24) return 8;
-  return 4;
+  if (avg > 24) return 4;
+  return 2;
 }
+
+#define FL_SPMV32_DISPATCH(G, KERNEL, ...)                                          \
+  do {                                                                             \
+    if ((G) == 8) KERNEL<8><<<gsp32, kThreads, 0, s>>>(__VA_ARGS__);               \
+    else KERNEL<4><<<gsp32, kThreads, 0, s>>>(__VA_ARGS__);                        \
+  } while (0)
 
 #define FL_SPMV_DISPATCH(G, KERNEL, ...)                                            \
   do {                                                                             \
-    if ((G) == 8) KERNEL<8><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                 \
-    else KERNEL<4><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
+    if ((G) == 4) KERNEL<4><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                 \
+    else KERNEL<2><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
   } while (0)
 
 int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost, const double* rhs,
@@ -990,17 +928,15 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
     FL_TRY_CUDA(cudaGetLastError());
     FL_TRY(W->w2.reserve(n));
-    // partial buffers: [0, gsp) p.w ; [2*np, 2*np + 2*gv) z.z and z.r
-    double* part_pw = W->part.p;
-    double* part_zz = W->part.p + 2 * np;
-    for (int i = 0; i < o->max_its + 1; ++i) {
-      k_cg_p<<<gv, kThreads, 0, s>>>(n, st, part_zz, (int)gv, i, W->z.p, W->p.p);
-      k_cg_commit<<<1, 32, 0, s>>>(st);
-      if (i == o->max_its) break;  // final test only
-      FL_SPMV_DISPATCH(G, k_cg_ap, A, W->p.p, W->w2.p, part_pw);
-      k_cg_xr<<<gv, kThreads, 0, s>>>(n, st, part_pw, (int)gsp, i, W->p.p, W->w2.p, W->dinv.p, W->y.p,
-                                       W->r.p, W->z.p, part_zz, (int)gv);
-      if ((i + 1) % chunk == 0) {
+    FL_TRY(W->ticket.reserve(4));
+    FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s));
+    k_cg_open<<<1, 32, 0, s>>>(st);
+    for (int i = 0; i < o->max_its; ++i) {
+      k_cg_p<<<gv, kThreads, 0, s>>>(n, st, i, W->z.p, W->p.p);
+      FL_SPMV_DISPATCH(G, k_cg_ap, A, W->p.p, W->w2.p, W->part.p, W->ticket.p, i);
+      k_cg_xr<<<gv, kThreads, 0, s>>>(n, st, i, W->p.p, W->w2.p, W->dinv.p, W->y.p, W->r.p, W->z.p,
+                                       W->part.p + 2 * np, W->ticket.p + 1);
+      if ((i + 1) % chunk == 0 || i + 1 == o->max_its) {
         FL_TRY_CUDA(cudaGetLastError());
         int done = 0;
         FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1061,7 +997,11 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     FL_TRY(W->p32.reserve(n));
     FL_TRY(W->w32.reserve(n));
     FL_TRY(W->d32.reserve(n));
+    FL_TRY(W->ticket.reserve(4));
+    FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s));
     k_to_f32<<<grid_for(m->nnz, kThreads), kThreads, 0, s>>>(m->nnz, val, W->val32.p);
+    const int G32 = G == 2 ? 4 : 8;
+    const unsigned gsp32 = grid_for((int64_t)n * G32, kThreads, 8);
     FL_TRY_CUDA(cudaGetLastError());
     KspState hs;
     FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
@@ -1092,19 +1032,19 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
       hs.reason = 0;
       hs.dpi = 0.0;
       hs.its = 0;
+      hs.pcoef = 0.0;
       hs.max_its = o->max_its - total_inner;
       FL_TRY_CUDA(cudaMemcpyAsync(st, &hs, sizeof(KspState), cudaMemcpyHostToDevice, s));
       int inner = 0;
       for (int i = 0; i < hs.max_its; ++i) {
-        FL_SPMV_DISPATCH(G, k_cg32_spmv, A32, st, piv32, W->z32.p, W->p32.p, W->w32.p, W->part.p, i);
-        k_cg32_alpha<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, i);
-        k_cg32_update<<<gv, kThreads, 0, s>>>(n, st, W->z32.p, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p,
-                                               W->r32.p, W->z32.p, W->part.p, (int)gv, i);
-        k_cg32_test<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, i);
+        k_cg32_p<<<gv, kThreads, 0, s>>>(n, st, i, W->z32.p, W->p32.p);
+        FL_SPMV32_DISPATCH(G32, k_cg32_ap, A32, st, piv32, W->p32.p, W->w32.p, W->part.p, W->ticket.p);
+        k_cg32_xr<<<gv, kThreads, 0, s>>>(n, st, i, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
+                                           W->z32.p, W->part.p + 2 * np, W->ticket.p + 1);
         if ((i + 1) % chunk == 0 || i + 1 == hs.max_its) {
           FL_TRY_CUDA(cudaGetLastError());
           KspState h2;
-          FL_TRY_CUDA(cudaMemcpyAsync(&h2, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+          FL_TRY_CUDA(cudaMemcpyAsync(&h2.its, &st->its, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
           FL_TRY_CUDA(cudaStreamSynchronize(s));
           inner = h2.its;
           if (h2.done) break;
