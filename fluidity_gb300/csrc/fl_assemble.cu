@@ -31,6 +31,7 @@
 #include "fl_internal.cuh"
 #include "fl_device.cuh"
 #include "fl_refelem.h"
+#include "fl_df64.cuh"
 
 namespace fl {
 
@@ -357,6 +358,121 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion(AsmArgs A) {
   }
 }
 
+// P1 diffusion + source (+ consistent mass) in double-float arithmetic: the
+// same closed form as k_asm_p1_diffusion with the FP64 pipe used only for the
+// nine coordinate differences J(a,b) = x_b - x_4 (one rounding, as the
+// reference's matmul with the 0/+-1 entries of dn).  Each difference is split
+// exactly into two floats, and cofactors, determinant, reciprocal, the Gram
+// products c_i . kappa c_j (isotropic or diagonal kappa), the mass and the
+// source integral run on the FP32 pipes with error-free transformations.  The
+// rows of the Gram matrix of c_1..c_4 sum to zero (c_4 = -(c_1+c_2+c_3)), so
+// only six products are formed.  Output: the 10 unique matrix entries and 4
+// rhs entries per element as (hi, lo) float pairs.
+struct DfArgs {
+  int32_t E;
+  const int32_t* nd;
+  const int32_t* xnd;
+  const double* X;
+  const double* t;
+  const double* f;
+  float2* em;
+  df kscale;     // wsum * theta*dt (* kappa if isotropic)
+  df rscale;     // wsum (* kappa if isotropic): operator scale of the rhs t-term
+  df kdiag[3];   // diagonal kappa (ones if isotropic)
+  df m0, m1;     // reference mass entries (diagonal, off-diagonal)
+  int have_mass, have_src, aniso;
+};
+
+__global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
+  note_launch();
+  const int64_t E = A.E;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+    const int vi[4] = {v.x, v.y, v.z, v.w};
+    double x[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + 3 * (int64_t)vi[i] + a);
+    df J[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
+    df cof[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+        cof[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
+      }
+    const df det = df_dot3(J[0][0], cof[0][0], J[1][0], cof[1][0], J[2][0], cof[2][0]);
+    const df adet = df_abs(det);
+    const df rdet = df_rcp(adet);
+    // gradient directions c_i = column i of cof; kappa applied to the second factor
+    df kc[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) kc[i][a] = A.aniso ? df_mul(A.kdiag[a], cof[a][i]) : cof[a][i];
+    df G[4][4];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = i; j < 3; ++j) {
+        G[i][j] = df_dot3(cof[0][i], kc[j][0], cof[1][i], kc[j][1], cof[2][i], kc[j][2]);
+        G[j][i] = G[i][j];
+      }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      G[i][3] = df_neg(df_add(df_add(G[i][0], G[i][1]), G[i][2]));
+      G[3][i] = G[i][3];
+    }
+    G[3][3] = df_neg(df_add(df_add(G[0][3], G[1][3]), G[2][3]));
+    const df ks = df_mul(A.kscale, rdet);
+    df madet0 = {0.0f, 0.0f}, madet1 = {0.0f, 0.0f};
+    if (A.have_mass) {
+      madet0 = df_mul(adet, A.m0);
+      madet1 = df_mul(adet, A.m1);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = i; j < 4; ++j) {
+        df m = df_mul(G[i][j], ks);
+        if (A.have_mass) m = df_add(m, i == j ? madet0 : madet1);
+        A.em[(int64_t)sym4(i, j) * E + e] = make_float2(m.hi, m.lo);
+      }
+    const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
+    const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
+    df r[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    if (A.have_src) {
+      df fe[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) fe[i] = df_from_double(__ldg(A.f + tn[i]));
+      const df fsum = df_add(df_add(fe[0], fe[1]), df_add(fe[2], fe[3]));
+      const df q1 = df_mul(df_mul(adet, A.m1), fsum);
+      const df q2 = df_mul(adet, df_sub(A.m0, A.m1));
+#pragma unroll
+      for (int i = 0; i < 4; ++i) r[i] = df_add(q1, df_mul(q2, fe[i]));
+    }
+    if (A.t) {
+      df te[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) te[i] = df_from_double(__ldg(A.t + tn[i]));
+      const df rs = df_mul(A.rscale, rdet);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        df s = df_add(df_dot3(G[i][0], te[0], G[i][1], te[1], G[i][2], te[2]), df_mul(G[i][3], te[3]));
+        r[i] = df_sub(r[i], df_mul(s, rs));
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) A.em[(int64_t)(10 + i) * E + e] = make_float2(r[i].hi, r[i].lo);
+  }
+}
+
 // Row pass: thread per CSR row; contributions of the row's elements are added
 // in the colour order of ne_col and the row is written once.  Accumulators
 // and the row's column indices live in shared memory for rows up to RMAX
@@ -375,6 +491,82 @@ struct PullArgs {
   double* rhs;
   ErrWord* err;
 };
+
+// Double-float version of the row pass: element values are (hi, lo) float
+// pairs; each row accumulates in double-float (shared memory, or in val for
+// rows longer than RMAX) and converts every entry to double once.
+template <int THREADS, int RMAX>
+__global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
+  note_launch();
+  extern __shared__ unsigned char smem_raw[];
+  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
+  const float2* em = reinterpret_cast<const float2*>(P.em);
+  const int t = threadIdx.x;
+  const int64_t E = P.E;
+  for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
+    const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
+    const bool in_smem = L <= RMAX;
+    if (in_smem) {
+      for (int k = 0; k < L; ++k) acc[k * THREADS + t] = make_float2(0.0f, 0.0f);
+    } else {
+      for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
+    }
+    df r = {0.0f, 0.0f};
+    const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
+    for (int q = ib; q < ie; ++q) {
+      const int inc = __ldg(P.ne_col + q);
+      const int e = inc >> 4, a = inc & 15;
+      const int4 nv = __ldg(reinterpret_cast<const int4*>(P.nd) + e);
+      const int nodes[4] = {nv.x, nv.y, nv.z, nv.w};
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int j = nodes[b];
+        const float2 v2 = __ldg(em + (int64_t)sym4(a, b) * E + e);
+        int lo = 0, hi = L - 1, pos = -1;
+        while (lo <= hi) {
+          const int mid = (lo + hi) >> 1;
+          const int c = __ldg(P.colm + base + mid);
+          if (c == j) { pos = mid; break; }
+          if (c < j) lo = mid + 1;
+          else hi = mid - 1;
+        }
+        if (pos < 0) {
+          if (v2.x != 0.0f || v2.y != 0.0f) set_err(P.err, FL_ERR_OUTSIDE_PATTERN, row);
+          continue;
+        }
+        if (in_smem) {
+          const float2 c = acc[pos * THREADS + t];
+          const df s = df_add({c.x, c.y}, {v2.x, v2.y});
+          acc[pos * THREADS + t] = make_float2(s.hi, s.lo);
+        } else {
+          P.val[base + pos] += (double)v2.x + (double)v2.y;
+        }
+      }
+      const float2 rv = __ldg(em + (int64_t)(10 + a) * E + e);
+      r = df_add(r, {rv.x, rv.y});
+    }
+    if (in_smem)
+      for (int k = 0; k < L; ++k) {
+        const float2 c = acc[k * THREADS + t];
+        P.val[base + k] = (double)c.x + (double)c.y;
+      }
+    P.rhs[row] = df_to_double(r);
+  }
+}
+
+template <int THREADS, int RMAX>
+static int launch_pull_df(const PullArgs& P, cudaStream_t s) {
+  const size_t smem = (size_t)RMAX * THREADS * sizeof(float2);
+  static bool configured = false;
+  if (!configured) {
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df<THREADS, RMAX>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  k_rows_pull_df<THREADS, RMAX><<<grid_for(P.N, THREADS, 16), THREADS, smem, s>>>(P);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
 
 template <int LOC, bool SYM, int THREADS, int RMAX>
 __global__ void __launch_bounds__(THREADS) k_rows_pull(PullArgs P) {
@@ -548,7 +740,35 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     }
     FL_TRY_CUDA(cudaEventRecord(m->ev0, s));
   }
-  if (closed) {
+  // Diagonal (or isotropic) kappa: the double-float element pass; a full
+  // tensor keeps the FP64 closed form.
+  bool diag_kappa = true;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      if (a != b && p->diffusivity[3 * a + b] != 0.0) diag_kappa = false;
+  const bool use_df = closed && (p->isotropic_diffusivity || diag_kappa);
+  if (use_df) {
+    RefTensors h;
+    build_tensors(1, p->quad_degree, h);
+    DfArgs D{};
+    D.E = m->E;
+    D.nd = m->ndglno.p;
+    D.xnd = m->xndglno.p;
+    D.X = m->coords.p;
+    D.t = f->t;
+    D.f = f->source;
+    D.em = reinterpret_cast<float2*>(m->em.p);
+    const double kap = p->isotropic_diffusivity ? p->diffusivity[0] : 1.0;
+    D.kscale = df_host(h.wsum * (A.use_dt ? A.theta_dt : 0.0) * kap);
+    D.rscale = df_host(h.wsum * kap);
+    D.aniso = p->isotropic_diffusivity ? 0 : 1;
+    for (int a = 0; a < 3; ++a) D.kdiag[a] = df_host(p->isotropic_diffusivity ? 1.0 : p->diffusivity[4 * a]);
+    D.m0 = df_host(h.M[0][0]);
+    D.m1 = df_host(h.M[0][1]);
+    D.have_mass = p->have_mass;
+    D.have_src = p->have_source;
+    k_asm_p1_diffusion_df<<<grid_for(m->E, 256, 16), 256, 0, s>>>(D);
+  } else if (closed) {
     k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
   } else if (loc == 4) {
     k_asm_general<4><<<grid_for(m->E, 128, 16), 128, 0, s>>>(A);
@@ -559,7 +779,8 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ndglno.p, m->findrm.p, m->colm.p, m->em.p,
              val, rhs, m->err.p};
   if (loc == 4) {
-    if (closed) FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
+    if (use_df) FL_TRY((launch_pull_df<128, 32>(P, s)));
+    else if (closed) FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
     else FL_TRY((launch_pull<4, false, 128, 32>(P, s)));
   } else {
     FL_TRY((launch_pull<10, false, 64, 96>(P, s)));

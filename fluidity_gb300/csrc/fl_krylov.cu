@@ -23,10 +23,12 @@
 // All scalars live on the device; reductions use a fixed block partition and
 // a fixed summation tree, so results are deterministic run to run.
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "fl_internal.cuh"
 #include "fl_device.cuh"
+#include "fl_df64.cuh"
 
 namespace fl {
 
@@ -85,6 +87,47 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   }
   __syncthreads();
   return v;  // valid in thread 0
+}
+
+// Block sum in double-float: each thread's FP64 partial is split exactly
+// enough into two floats and the shuffle/shared-memory tree runs on the FP32
+// pipes (a warp-wide FP64 add costs ~16 SM cycles on GB300, a double-float
+// add about 3).  Result valid in thread 0, as a double.
+__device__ __forceinline__ df warp_sum_df(df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    df u;
+    u.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    u.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = df_add(v, u);
+  }
+  return v;
+}
+
+template <int THREADS>
+__device__ __forceinline__ double block_sum_df(df v, float2* red) {
+  v = warp_sum_df(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = make_float2(v.hi, v.lo);
+  __syncthreads();
+  if (w == 0) {
+    const float2 q = lane < THREADS / 32 ? red[lane] : make_float2(0.0f, 0.0f);
+    v = warp_sum_df({q.x, q.y});
+  }
+  __syncthreads();
+  return df_to_double(v);
+}
+
+template <int THREADS>
+__device__ __forceinline__ double block_sum_df(double v, float2* red) {
+  return block_sum_df<THREADS>(df_from_double(v), red);
+}
+
+// Exact product of two floats accumulated in double-float.
+__device__ __forceinline__ df df_fma_ff(float a, float b, df acc) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  return df_add(acc, {p, e});
 }
 
 // Sum of `n` partials in a fixed order by one block.  The partials were
@@ -337,6 +380,7 @@ __global__ void k_cg_ap(SpArgs A, const double* __restrict__ p, double* __restri
                         double* __restrict__ part, unsigned* ticket, int i) {
   note_launch();
   __shared__ double red[kThreads / 32];
+  __shared__ float2 redf[kThreads / 32];
   KspState* st = A.st;
   if (st->done) return;
   const double piv = st->pivot;
@@ -353,7 +397,7 @@ __global__ void k_cg_ap(SpArgs A, const double* __restrict__ p, double* __restri
       pw += pi * s;
     }
   }
-  pw = block_sum<kThreads>(pw, red);
+  pw = block_sum_df<kThreads>(pw, redf);
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
   if (!last_block(ticket)) return;
   const double dpi = reduce_partials(part, gridDim.x, red);
@@ -376,6 +420,7 @@ __global__ void k_cg_xr(int n, KspState* st, int i, const double* __restrict__ p
                         double* __restrict__ z, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
+  __shared__ float2 redf[kThreads / 32];
   if (st->done) return;
   const double a = st->alpha;
   double zz = 0.0, zr = 0.0;
@@ -388,8 +433,8 @@ __global__ void k_cg_xr(int n, KspState* st, int i, const double* __restrict__ p
     zz += zk * zk;
     zr += zk * rk;
   }
-  zz = block_sum<kThreads>(zz, red);
-  zr = block_sum<kThreads>(zr, red);
+  zz = block_sum_df<kThreads>(zz, redf);
+  zr = block_sum_df<kThreads>(zr, redf);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[gridDim.x + blockIdx.x] = zr;
@@ -726,9 +771,10 @@ __global__ void k_cg32_ap(SpArgs32 A, KspState* st, float piv, const float* __re
   note_launch();
   __shared__ double red[kThreads / 32];
   if (st->done) return;
+  __shared__ float2 redf[kThreads / 32];
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
-  double pw = 0.0;
+  df pwd = {0.0f, 0.0f};
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
     float s = 0.0f;
@@ -742,10 +788,10 @@ __global__ void k_cg32_ap(SpArgs32 A, KspState* st, float piv, const float* __re
       const float pi = p[row];
       if (A.ghost && A.ghost[row]) s = piv * pi;
       w[row] = s;
-      pw += (double)pi * (double)s;
+      pwd = df_fma_ff(pi, s, pwd);
     }
   }
-  pw = block_sum<kThreads>(pw, red);
+  const double pw = block_sum_df<kThreads>(pwd, redf);
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
   if (!last_block(ticket)) return;
   const double dpi = reduce_partials(part, gridDim.x, red);
@@ -767,19 +813,20 @@ __global__ void k_cg32_xr(int n, KspState* st, int i, const float* __restrict__ 
   note_launch();
   __shared__ double red[kThreads / 32];
   if (st->done) return;
+  __shared__ float2 redf[kThreads / 32];
   const float a = (float)st->alpha;
-  double zz = 0.0, zr = 0.0;
+  df zzd = {0.0f, 0.0f}, zrd = {0.0f, 0.0f};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     d[k] = fmaf(a, p[k], d[k]);
     const float rk = fmaf(-a, w[k], r[k]);
     const float zk = rk * dinv[k];
     r[k] = rk;
     z[k] = zk;
-    zz += (double)zk * zk;
-    zr += (double)zk * rk;
+    zzd = df_fma_ff(zk, zk, zzd);
+    zrd = df_fma_ff(zk, rk, zrd);
   }
-  zz = block_sum<kThreads>(zz, red);
-  zr = block_sum<kThreads>(zr, red);
+  const double zz = block_sum_df<kThreads>(zzd, redf);
+  const double zr = block_sum_df<kThreads>(zrd, redf);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[gridDim.x + blockIdx.x] = zr;
@@ -861,6 +908,11 @@ struct Launch {
 // this part, and each level of the in-group shuffle reduction costs a DADD on
 // every lane, so short rows use two lanes.
 static int group_for(const fl_mesh_t* m) {
+  static int forced = [] {
+    const char* e = getenv("FL_SPMV_LANES");
+    return e ? atoi(e) : 0;
+  }();
+  if (forced == 1 || forced == 2 || forced == 4) return forced;
   const double avg = (double)m->nnz / (double)(m->N > 0 ? m->N : 1);
   if (avg > 24) return 4;
   return 2;
@@ -875,7 +927,8 @@ static int group_for(const fl_mesh_t* m) {
 #define FL_SPMV_DISPATCH(G, KERNEL, ...)                                            \
   do {                                                                             \
     if ((G) == 4) KERNEL<4><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                 \
-    else KERNEL<2><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
+    else if ((G) == 2) KERNEL<2><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);            \
+    else KERNEL<1><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
   } while (0)
 
 int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost, const double* rhs,
