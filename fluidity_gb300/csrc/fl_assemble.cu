@@ -483,6 +483,7 @@ struct PullArgs {
   int32_t N, E;
   const int32_t* ne_ptr;
   const int32_t* ne_col;
+  const uint32_t* ne_pos;
   const int32_t* nd;
   const int32_t* findrm;
   const int32_t* colm;
@@ -515,34 +516,23 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
     const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
     for (int q = ib; q < ie; ++q) {
       const int inc = __ldg(P.ne_col + q);
+      const uint32_t pw = __ldg(P.ne_pos + q);
       const int e = inc >> 4, a = inc & 15;
-      const int4 nv = __ldg(reinterpret_cast<const int4*>(P.nd) + e);
-      const int nodes[4] = {nv.x, nv.y, nv.z, nv.w};
+      float2 v2[4];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) v2[b] = __ldg(em + (int64_t)sym4(a, b) * E + e);
+      const float2 rv = __ldg(em + (int64_t)(10 + a) * E + e);
 #pragma unroll
       for (int b = 0; b < 4; ++b) {
-        const int j = nodes[b];
-        const float2 v2 = __ldg(em + (int64_t)sym4(a, b) * E + e);
-        int lo = 0, hi = L - 1, pos = -1;
-        while (lo <= hi) {
-          const int mid = (lo + hi) >> 1;
-          const int c = __ldg(P.colm + base + mid);
-          if (c == j) { pos = mid; break; }
-          if (c < j) lo = mid + 1;
-          else hi = mid - 1;
-        }
-        if (pos < 0) {
-          if (v2.x != 0.0f || v2.y != 0.0f) set_err(P.err, FL_ERR_OUTSIDE_PATTERN, row);
-          continue;
-        }
+        const int pos = (pw >> (8 * b)) & 0xffu;
         if (in_smem) {
           const float2 c = acc[pos * THREADS + t];
-          const df s = df_add({c.x, c.y}, {v2.x, v2.y});
-          acc[pos * THREADS + t] = make_float2(s.hi, s.lo);
+          const df sum = df_add({c.x, c.y}, {v2[b].x, v2[b].y});
+          acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
         } else {
-          P.val[base + pos] += (double)v2.x + (double)v2.y;
+          P.val[base + pos] += (double)v2[b].x + (double)v2[b].y;
         }
       }
-      const float2 rv = __ldg(em + (int64_t)(10 + a) * E + e);
       r = df_add(r, {rv.x, rv.y});
     }
     if (in_smem)
@@ -572,19 +562,16 @@ template <int LOC, bool SYM, int THREADS, int RMAX>
 __global__ void __launch_bounds__(THREADS) k_rows_pull(PullArgs P) {
   note_launch();
   extern __shared__ unsigned char smem_raw[];
-  double* acc = reinterpret_cast<double*>(smem_raw);                       // [RMAX][THREADS]
-  int32_t* col = reinterpret_cast<int32_t*>(acc + (size_t)RMAX * THREADS);  // [RMAX][THREADS]
+  double* acc = reinterpret_cast<double*>(smem_raw);  // [RMAX][THREADS]
   const int t = threadIdx.x;
   const int64_t E = P.E;
   constexpr int NK = SYM ? LOC * (LOC + 1) / 2 : LOC * LOC;
+  constexpr int PW = (LOC + 3) / 4;
   for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
     const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
     const bool in_smem = L <= RMAX;
     if (in_smem) {
-      for (int k = 0; k < L; ++k) {
-        acc[k * THREADS + t] = 0.0;
-        col[k * THREADS + t] = __ldg(P.colm + base + k);
-      }
+      for (int k = 0; k < L; ++k) acc[k * THREADS + t] = 0.0;
     } else {
       for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
     }
@@ -593,26 +580,16 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull(PullArgs P) {
     for (int q = ib; q < ie; ++q) {
       const int inc = __ldg(P.ne_col + q);
       const int e = inc >> 4, a = inc & 15;
+      uint32_t pw[PW];
+#pragma unroll
+      for (int w = 0; w < PW; ++w) pw[w] = __ldg(P.ne_pos + (int64_t)q * PW + w);
 #pragma unroll
       for (int b = 0; b < LOC; ++b) {
-        const int j = __ldg(P.nd + (int64_t)e * LOC + b);
         int k;
         if (SYM) k = a <= b ? a * LOC - (a * (a - 1)) / 2 + (b - a) : b * LOC - (b * (b - 1)) / 2 + (a - b);
         else k = a * LOC + b;
         const double v = __ldg(P.em + (int64_t)k * E + e);
-        // bisection in the row (csr_sparsity_pos, Sparse_Tools.F90:2411)
-        int lo = 0, hi = L - 1, pos = -1;
-        while (lo <= hi) {
-          const int mid = (lo + hi) >> 1;
-          const int c = in_smem ? col[mid * THREADS + t] : __ldg(P.colm + base + mid);
-          if (c == j) { pos = mid; break; }
-          if (c < j) lo = mid + 1;
-          else hi = mid - 1;
-        }
-        if (pos < 0) {
-          if (v != 0.0) set_err(P.err, FL_ERR_OUTSIDE_PATTERN, row);
-          continue;
-        }
+        const int pos = (pw[b >> 2] >> (8 * (b & 3))) & 0xffu;
         if (in_smem) acc[pos * THREADS + t] += v;
         else P.val[base + pos] += v;
       }
@@ -626,7 +603,7 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull(PullArgs P) {
 
 template <int LOC, bool SYM, int THREADS, int RMAX>
 static int launch_pull(const PullArgs& P, cudaStream_t s) {
-  const size_t smem = (size_t)RMAX * THREADS * (sizeof(double) + sizeof(int32_t));
+  const size_t smem = (size_t)RMAX * THREADS * sizeof(double);
   static bool configured = false;
   if (!configured) {
     FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull<LOC, SYM, THREADS, RMAX>,
@@ -776,8 +753,8 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     k_asm_general<10><<<grid_for(m->E, 128, 16), 128, 0, s>>>(A);
   }
   FL_TRY_CUDA(cudaGetLastError());
-  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ndglno.p, m->findrm.p, m->colm.p, m->em.p,
-             val, rhs, m->err.p};
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
+             m->em.p, val, rhs, m->err.p};
   if (loc == 4) {
     if (use_df) FL_TRY((launch_pull_df<128, 32>(P, s)));
     else if (closed) FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
@@ -941,8 +918,8 @@ extern "C" int fl_dev_assemble_p1_diffusion_noalloc(fl_mesh m, const fl_advdif_p
   A.have_src = p->have_source;
   k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
   FL_TRY_CUDA(cudaGetLastError());
-  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ndglno.p, m->findrm.p, m->colm.p, d->em,
-             val, rhs, m->err.p};
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
+             d->em, val, rhs, m->err.p};
   FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
   return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
 }

@@ -114,12 +114,15 @@ __device__ __forceinline__ df df_from_double(double d) {
   const uint32_t sign = hw & 0x80000000u;
   const uint32_t fb = sign | ((uint32_t)(exp - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
   const float hi = __uint_as_float(fb);
+  // lo = rem * 2^(exp - 1075) for the 29 remaining bits, built from bits too
+  // (integer pipe only): normalise rem, keep its leading 24 bits.
   const uint32_t rem = lw & 0x1fffffffu;
-  // rem * 2^(exp - 1075); the power of two is built from exponent bits
-  const float scale = __uint_as_float((uint32_t)(exp - 1075 + 127) << 23);
-  float lo = (float)rem * scale;
-  if (sign) lo = -lo;
-  return {hi, lo};
+  if (rem == 0u) return {hi, 0.0f};
+  const int lz = __clz(rem);                        // >= 3
+  const uint32_t nrm = rem << lz;                   // leading one at bit 31
+  const uint32_t mant = (nrm << 1) >> 9;            // 23 bits after the leading one
+  const uint32_t lexp = (uint32_t)(exp - 1075 + (31 - lz) + 127);
+  return {hi, __uint_as_float(sign | (lexp << 23) | mant)};
 }
 
 // Host-side split of a double constant.

@@ -114,6 +114,8 @@ struct fl_mesh_t {
   fl::DevBuf<double> coords;         // 3*Nx
   fl::DevBuf<int32_t> ne_ptr, ne;    // field node -> (element<<4 | local) ascending
   fl::DevBuf<int32_t> ne_col;        // same incidences per node, ordered by element colour
+  fl::DevBuf<uint32_t> ne_pos;       // per ne_col incidence: row position of each element node,
+                                     // one byte per node, ceil(loc/4) words per incidence
   fl::DevBuf<int32_t> vne_ptr, vne;  // vertex -> element ascending
   fl::DevBuf<int32_t> findrm, colm, centrm;
   fl::DevBuf<int32_t> colour;        // E, 1-based

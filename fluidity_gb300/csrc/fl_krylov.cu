@@ -68,6 +68,15 @@ struct KrylovWork {
   DevBuf<float> r32, z32, p32, w32, d32, dinv32;
   DevBuf<KspState> st;
   DevBuf<unsigned> ticket;  // retire counters of the last-block reductions
+  // Sliced ELL copy of the pattern for the CG SpMV: slices of 32 rows, each
+  // padded to its longest row and stored column-major (entry j of the slice's
+  // rows contiguous), so one thread per row reads coalesced values.
+  bool sell_ready = false;
+  int32_t nslices = 0;
+  int64_t sell_len = 0;
+  DevBuf<int32_t> swidth, sptr, scol, smap;
+  DevBuf<double> sval;
+  DevBuf<float> sval32;
 };
 
 static KrylovWork* work_of(fl_mesh_t* m);
@@ -340,6 +349,73 @@ __global__ void k_cg_start(KspState* st, const double* __restrict__ part, int np
   }
 }
 
+// ----------------------------------------------------------- sliced ELL --
+constexpr int kSlice = 32;
+
+__global__ void k_sell_width(const int32_t* __restrict__ findrm, int n, int nslices, int32_t* __restrict__ width) {
+  note_launch();
+  for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < nslices; sl += gridDim.x * blockDim.x) {
+    int w = 0;
+    for (int r = sl * kSlice; r < min(n, (sl + 1) * kSlice); ++r) w = max(w, findrm[r + 1] - findrm[r]);
+    width[sl] = w * kSlice;  // entries of the slice
+  }
+}
+
+// Column indices and CSR positions of the padded layout (padding: the row's
+// own column and no CSR position).
+__global__ void k_sell_fill(const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm, int n,
+                            const int32_t* __restrict__ sptr, int32_t* __restrict__ scol, int32_t* __restrict__ smap) {
+  note_launch();
+  const int nsl = (n + kSlice - 1) / kSlice;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nsl * kSlice; r += gridDim.x * blockDim.x) {
+    const int sl = r / kSlice, lane = r % kSlice;
+    const int w = (sptr[sl + 1] - sptr[sl]) / kSlice;
+    const bool real = r < n;
+    const int b = real ? findrm[r] : 0, len = real ? findrm[r + 1] - b : 0;
+    for (int j = 0; j < w; ++j) {
+      const int64_t idx = (int64_t)sptr[sl] + (int64_t)j * kSlice + lane;
+      if (j < len) {
+        scol[idx] = colm[b + j];
+        smap[idx] = b + j;
+      } else {
+        scol[idx] = real ? r : 0;
+        smap[idx] = -1;
+      }
+    }
+  }
+}
+
+__global__ void k_sell_values(int64_t len, const int32_t* __restrict__ smap, const double* __restrict__ val,
+                              double* __restrict__ sval, float* __restrict__ sval32) {
+  note_launch();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < len; k += (int64_t)gridDim.x * blockDim.x) {
+    const int m = smap[k];
+    const double v = m >= 0 ? val[m] : 0.0;
+    if (sval) sval[k] = v;
+    if (sval32) sval32[k] = (float)v;
+  }
+}
+
+struct SellArgs {
+  int32_t n;
+  const int32_t* sptr;
+  const int32_t* scol;
+  const uint8_t* ghost;
+  KspState* st;
+};
+
+// Row r of the sliced layout: sum over the row's entries in CSR order (the
+// same order as a sequential CSR row product, so results are deterministic).
+template <class V, class X>
+__device__ __forceinline__ double sell_row_dot(const SellArgs& A, const V* __restrict__ sval, const X* __restrict__ x,
+                                               int r) {
+  const int sl = r / kSlice, lane = r % kSlice;
+  const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
+  double s = 0.0;
+  for (int k = b; k < e; k += kSlice) s += (double)__ldg(sval + k) * (double)x[__ldg(A.scol + k)];
+  return s;
+}
+
 // ------------------------------------------------------- CG (3 kernels) --
 // One iteration i of KSPSolve_CG in three launches; each global reduction is
 // finished by the last block of its launch to retire (a ticket counter), which
@@ -375,27 +451,21 @@ __global__ void k_cg_p(int n, const KspState* st, int i, const double* __restric
     p[k] = i == 0 ? z[k] : z[k] + coef * p[k];
 }
 
-template <int G>
-__global__ void k_cg_ap(SpArgs A, const double* __restrict__ p, double* __restrict__ w,
-                        double* __restrict__ part, unsigned* ticket, int i) {
+__global__ void k_cg_ap(SellArgs A, const double* __restrict__ sval, const double* __restrict__ p,
+                        double* __restrict__ w, double* __restrict__ part, unsigned* ticket, int i) {
   note_launch();
   __shared__ double red[kThreads / 32];
   __shared__ float2 redf[kThreads / 32];
   KspState* st = A.st;
   if (st->done) return;
   const double piv = st->pivot;
-  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
-  const int gpb = blockDim.x / G;
   double pw = 0.0;
-  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
-    const int row = base + threadIdx.x / G;
-    double s = row_dot<G>(A.findrm, A.colm, A.val, p, row, sub, row < A.n);
-    if (row < A.n && sub == 0) {
-      const double pi = p[row];
-      if (A.ghost && A.ghost[row]) s = piv * pi;
-      w[row] = s;
-      pw += pi * s;
-    }
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+    double s = sell_row_dot(A, sval, p, row);
+    const double pi = p[row];
+    if (A.ghost && A.ghost[row]) s = piv * pi;
+    w[row] = s;
+    pw += pi * s;
   }
   pw = block_sum_df<kThreads>(pw, redf);
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
@@ -765,31 +835,23 @@ __global__ void k_cg32_p(int n, const KspState* st, int i, const float* __restri
     p[k] = i == 0 ? z[k] : fmaf(coef, p[k], z[k]);
 }
 
-template <int G>
-__global__ void k_cg32_ap(SpArgs32 A, KspState* st, float piv, const float* __restrict__ p,
+__global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv, const float* __restrict__ p,
                           float* __restrict__ w, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
-  if (st->done) return;
   __shared__ float2 redf[kThreads / 32];
-  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
-  const int gpb = blockDim.x / G;
+  KspState* st = A.st;
+  if (st->done) return;
   df pwd = {0.0f, 0.0f};
-  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
-    const int row = base + threadIdx.x / G;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+    const int sl = row / kSlice, lane = row % kSlice;
+    const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
     float s = 0.0f;
-    if (row < A.n) {
-      const int b = __ldg(A.findrm + row), e = __ldg(A.findrm + row + 1);
-      for (int k = b + sub; k < e; k += G) s = fmaf(__ldg(A.val + k), p[__ldg(A.colm + k)], s);
-    }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
-    if (row < A.n && sub == 0) {
-      const float pi = p[row];
-      if (A.ghost && A.ghost[row]) s = piv * pi;
-      w[row] = s;
-      pwd = df_fma_ff(pi, s, pwd);
-    }
+    for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[__ldg(A.scol + k)], s);
+    const float pi = p[row];
+    if (A.ghost && A.ghost[row]) s = piv * pi;
+    w[row] = s;
+    pwd = df_fma_ff(pi, s, pwd);
   }
   const double pw = block_sum_df<kThreads>(pwd, redf);
   if (threadIdx.x == 0) part[blockIdx.x] = pw;
@@ -976,17 +1038,41 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
 
   int outer = 0;
   const int chunk = 16;
+  if (!W->sell_ready) {
+    const int nsl = (n + kSlice - 1) / kSlice;
+    FL_TRY(W->swidth.reserve(nsl + 1));
+    FL_TRY(W->sptr.reserve(nsl + 1));
+    k_sell_width<<<grid_for(nsl, kThreads), kThreads, 0, s>>>(m->findrm.p, n, nsl, W->swidth.p);
+    FL_TRY_CUDA(cudaGetLastError());
+    FL_TRY(exclusive_scan_i32(W->swidth.p, W->sptr.p, nsl, s));
+    int32_t len = 0;
+    FL_TRY_CUDA(cudaMemcpyAsync(&len, W->sptr.p + nsl, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    FL_TRY_CUDA(cudaStreamSynchronize(s));
+    FL_TRY(W->scol.reserve(len));
+    FL_TRY(W->smap.reserve(len));
+    k_sell_fill<<<grid_for((int64_t)nsl * kSlice, kThreads), kThreads, 0, s>>>(m->findrm.p, m->colm.p, n, W->sptr.p,
+                                                                               W->scol.p, W->smap.p);
+    FL_TRY_CUDA(cudaGetLastError());
+    W->nslices = nsl;
+    W->sell_len = len;
+    W->sell_ready = true;
+  }
+  SellArgs SA{n, W->sptr.p, W->scol.p, ghost, st};
+  const unsigned gsl = grid_for(n, kThreads, 8);
   if (!mixed && o->ksp_type == 0) {
     FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
     k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
     FL_TRY_CUDA(cudaGetLastError());
     FL_TRY(W->w2.reserve(n));
     FL_TRY(W->ticket.reserve(4));
+    FL_TRY(W->sval.reserve(W->sell_len));
     FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s));
+    k_sell_values<<<grid_for(W->sell_len, kThreads), kThreads, 0, s>>>(W->sell_len, W->smap.p, val, W->sval.p,
+                                                                         nullptr);
     k_cg_open<<<1, 32, 0, s>>>(st);
     for (int i = 0; i < o->max_its; ++i) {
       k_cg_p<<<gv, kThreads, 0, s>>>(n, st, i, W->z.p, W->p.p);
-      FL_SPMV_DISPATCH(G, k_cg_ap, A, W->p.p, W->w2.p, W->part.p, W->ticket.p, i);
+      k_cg_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval.p, W->p.p, W->w2.p, W->part.p, W->ticket.p, i);
       k_cg_xr<<<gv, kThreads, 0, s>>>(n, st, i, W->p.p, W->w2.p, W->dinv.p, W->y.p, W->r.p, W->z.p,
                                        W->part.p + 2 * np, W->ticket.p + 1);
       if ((i + 1) % chunk == 0 || i + 1 == o->max_its) {
@@ -1044,7 +1130,6 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     }
   } else {
     // Mixed precision: fp32 inner CG (rtol inner_rtol) inside fp64 refinement
-    FL_TRY(W->val32.reserve(m->nnz));
     FL_TRY(W->r32.reserve(n));
     FL_TRY(W->z32.reserve(n));
     FL_TRY(W->p32.reserve(n));
@@ -1052,15 +1137,14 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     FL_TRY(W->d32.reserve(n));
     FL_TRY(W->ticket.reserve(4));
     FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s));
-    k_to_f32<<<grid_for(m->nnz, kThreads), kThreads, 0, s>>>(m->nnz, val, W->val32.p);
-    const int G32 = G == 2 ? 4 : 8;
-    const unsigned gsp32 = grid_for((int64_t)n * G32, kThreads, 8);
+    FL_TRY(W->sval32.reserve(W->sell_len));
+    k_sell_values<<<grid_for(W->sell_len, kThreads), kThreads, 0, s>>>(W->sell_len, W->smap.p, val, nullptr,
+                                                                         W->sval32.p);
     FL_TRY_CUDA(cudaGetLastError());
     KspState hs;
     FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
     FL_TRY_CUDA(cudaStreamSynchronize(s));
     const float piv32 = (float)hs.pivot;
-    SpArgs32 A32{n, m->findrm.p, m->colm.p, W->val32.p, ghost};
     const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-5;
     double rnorm0 = 0.0, ttol = 0.0;
     int total_inner = 0, reason = 0;
@@ -1091,7 +1175,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
       int inner = 0;
       for (int i = 0; i < hs.max_its; ++i) {
         k_cg32_p<<<gv, kThreads, 0, s>>>(n, st, i, W->z32.p, W->p32.p);
-        FL_SPMV32_DISPATCH(G32, k_cg32_ap, A32, st, piv32, W->p32.p, W->w32.p, W->part.p, W->ticket.p);
+        k_cg32_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval32.p, piv32, W->p32.p, W->w32.p, W->part.p, W->ticket.p);
         k_cg32_xr<<<gv, kThreads, 0, s>>>(n, st, i, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
                                            W->z32.p, W->part.p + 2 * np, W->ticket.p + 1);
         if ((i + 1) % chunk == 0 || i + 1 == hs.max_its) {

@@ -447,6 +447,34 @@ __global__ void k_sort_by_colour(const int32_t* __restrict__ ptr, const int32_t*
   }
 }
 
+// For every incidence (row i, element e) of ne_col, the positions of e's nodes
+// inside row i (offsets from findrm[i]), one byte each -- the bisection of
+// csr_sparsity_pos (Sparse_Tools.F90:2411) done once per mesh instead of once
+// per entry per assembly.  255 marks a position that does not fit a byte.
+__global__ void k_incidence_positions(const int32_t* __restrict__ ne_ptr, const int32_t* __restrict__ ne_col,
+                                      const int32_t* __restrict__ nd, int loc, const int32_t* __restrict__ findrm,
+                                      const int32_t* __restrict__ colm, int32_t n, uint32_t* __restrict__ pos,
+                                      ErrWord* err) {
+  note_launch();
+  const int pw = (loc + 3) / 4;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+    const int b0 = findrm[row], b1 = findrm[row + 1];
+    for (int q = ne_ptr[row]; q < ne_ptr[row + 1]; ++q) {
+      const int e = ne_col[q] >> 4;
+      uint32_t words[3] = {0u, 0u, 0u};
+      for (int b = 0; b < loc; ++b) {
+        const int j = nd[(int64_t)e * loc + b];
+        const int p = csr_find(colm, b0, b1, j);
+        if (p < 0) set_err(err, FL_ERR_OUTSIDE_PATTERN, row);
+        if (p - b0 > 254) set_err(err, FL_ERR_UNSUPPORTED, row);  // rows longer than 255 entries
+        const uint32_t off = p < 0 ? 255u : (uint32_t)min(p - b0, 255);
+        words[b >> 2] |= off << (8 * (b & 3));
+      }
+      for (int w = 0; w < pw; ++w) pos[(int64_t)q * pw + w] = words[w];
+    }
+  }
+}
+
 static int build_colouring(fl_mesh_t* m, cudaStream_t s) {
   const int32_t E = m->E;
   FL_TRY(m->vne_ptr.reserve(m->Nx + 1));
@@ -615,6 +643,10 @@ extern "C" int fl_gpu_mesh_register(const fl_mesh_desc* d, fl_mesh* out) {
       st = FL_ERR_CUDA;
       break;
     }
+    if ((st = m->ne_pos.reserve((size_t)m->E * m->loc * ((m->loc + 3) / 4))) != FL_OK) break;
+    k_incidence_positions<<<grid_for(m->N, 128), 128, 0, s>>>(m->ne_ptr.p, m->ne_col.p, m->ndglno.p, m->loc,
+                                                              m->findrm.p, m->colm.p, m->N, m->ne_pos.p, m->err.p);
+    if ((st = check_err(m->err.p, s, "incidence positions")) != FL_OK) break;
   } while (0);
   if (st != FL_OK) {
     if (m->stream) cudaStreamDestroy(m->stream);
