@@ -553,7 +553,8 @@ static int launch_pull_df(const PullArgs& P, cudaStream_t s) {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = true;
   }
-  k_rows_pull_df<THREADS, RMAX><<<grid_for(P.N, THREADS, 16), THREADS, smem, s>>>(P);
+  const unsigned grid = (unsigned)((P.N + THREADS - 1) / THREADS);
+  k_rows_pull_df<THREADS, RMAX><<<grid, THREADS, smem, s>>>(P);
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
@@ -610,7 +611,10 @@ static int launch_pull(const PullArgs& P, cudaStream_t s) {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = true;
   }
-  k_rows_pull<LOC, SYM, THREADS, RMAX><<<grid_for(P.N, THREADS, 16), THREADS, smem, s>>>(P);
+  // one block per chunk of THREADS consecutive rows, issued in row order: the
+  // rows in flight form a contiguous band whose elements' values stay in L2
+  const unsigned grid = (unsigned)((P.N + THREADS - 1) / THREADS);
+  k_rows_pull<LOC, SYM, THREADS, RMAX><<<grid, THREADS, smem, s>>>(P);
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
@@ -756,7 +760,10 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
              m->em.p, val, rhs, m->err.p};
   if (loc == 4) {
-    if (use_df) FL_TRY((launch_pull_df<128, 32>(P, s)));
+    // shared accumulators sized to the mesh's longest row (longer rows, if any,
+    // accumulate in place in val)
+    if (use_df && m->max_row <= 16) FL_TRY((launch_pull_df<128, 16>(P, s)));
+    else if (use_df) FL_TRY((launch_pull_df<128, 32>(P, s)));
     else if (closed) FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
     else FL_TRY((launch_pull<4, false, 128, 32>(P, s)));
   } else {

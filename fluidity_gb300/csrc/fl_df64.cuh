@@ -114,15 +114,14 @@ __device__ __forceinline__ df df_from_double(double d) {
   const uint32_t sign = hw & 0x80000000u;
   const uint32_t fb = sign | ((uint32_t)(exp - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
   const float hi = __uint_as_float(fb);
-  // lo = rem * 2^(exp - 1075) for the 29 remaining bits, built from bits too
-  // (integer pipe only): normalise rem, keep its leading 24 bits.
+  // lo = rem * 2^(exp - 1075) for the 29 remaining bits, rounded down to 23:
+  // a float 2^E0 * (1 + m 2^-23) with m = rem >> 6 minus 2^E0 is exactly
+  // m 2^(E0-23) (Sterbenz), so no normalisation instruction is needed.
   const uint32_t rem = lw & 0x1fffffffu;
-  if (rem == 0u) return {hi, 0.0f};
-  const int lz = __clz(rem);                        // >= 3
-  const uint32_t nrm = rem << lz;                   // leading one at bit 31
-  const uint32_t mant = (nrm << 1) >> 9;            // 23 bits after the leading one
-  const uint32_t lexp = (uint32_t)(exp - 1075 + (31 - lz) + 127);
-  return {hi, __uint_as_float(sign | (lexp << 23) | mant)};
+  const uint32_t e0 = (uint32_t)(exp - 1046 + 127) << 23;
+  float lo = __uint_as_float(e0 | (rem >> 6)) - __uint_as_float(e0);
+  if (sign) lo = -lo;
+  return {hi, lo};
 }
 
 // Host-side split of a double constant.

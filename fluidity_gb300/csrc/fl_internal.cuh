@@ -107,6 +107,7 @@ struct fl_mesh_t {
   int32_t Nx = 0;    // coordinate (P1 vertex) nodes
   int64_t nnz = 0;
   int32_t ncolours = 0;
+  int32_t max_row = 0;  // longest CSR row
   cudaStream_t stream = nullptr;
 
   fl::DevBuf<int32_t> ndglno;        // E*loc, 0-based, element-major

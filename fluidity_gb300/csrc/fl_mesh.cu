@@ -586,6 +586,14 @@ using namespace fl;
 
 extern "C" const char* fl_last_error(void) { return g_err; }
 
+__global__ void k_max_row(const int32_t* __restrict__ findrm, int32_t n, int32_t* __restrict__ out) {
+  note_launch();
+  int m = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    m = max(m, findrm[i + 1] - findrm[i]);
+  atomicMax(out, m);
+}
+
 static int upload_conn(const int32_t* host, int64_t n, int32_t base, int32_t nodes, DevBuf<int32_t>& dst,
                        ErrWord* d_err, cudaStream_t s) {
   FL_TRY(dst.reserve(n));
@@ -635,6 +643,18 @@ extern "C" int fl_gpu_mesh_register(const fl_mesh_desc* d, fl_mesh* out) {
     if ((st = build_incidence(m->ndglno.p, m->E, m->loc, m->N, m->ne_ptr, m->ne, s)) != FL_OK) break;
     if ((st = build_sparsity(m->ndglno.p, m->loc, m->N, m->ne_ptr, m->ne, m->findrm, m->colm, m->centrm,
                              &m->nnz, m->err.p, s)) != FL_OK) break;
+    {
+      DevBuf<int32_t> mr;
+      if ((st = mr.reserve(1)) != FL_OK) break;
+      cudaMemsetAsync(mr.p, 0, sizeof(int32_t), s);
+      k_max_row<<<grid_for(m->N, 256), 256, 0, s>>>(m->findrm.p, m->N, mr.p);
+      if (cudaMemcpyAsync(&m->max_row, mr.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess) {
+        set_error("row length reduction failed");
+        st = FL_ERR_CUDA;
+        break;
+      }
+    }
     if ((st = build_colouring(m, s)) != FL_OK) break;
     if ((st = m->ne_col.reserve((size_t)m->E * m->loc)) != FL_OK) break;
     k_sort_by_colour<<<grid_for(m->N, 128), 128, 0, s>>>(m->ne_ptr.p, m->ne.p, m->colour.p, m->ne_col.p, m->N);
