@@ -385,7 +385,6 @@ struct DfArgs {
 
 __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   note_launch();
-  const int64_t E = A.E;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
     const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
     const int vi[4] = {v.x, v.y, v.z, v.w};
@@ -393,7 +392,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + 3 * (int64_t)vi[i] + a);
+      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
     df J[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -436,13 +435,15 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
       madet0 = df_mul(adet, A.m0);
       madet1 = df_mul(adet, A.m1);
     }
+    df K[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int j = i; j < 4; ++j) {
         df m = df_mul(G[i][j], ks);
         if (A.have_mass) m = df_add(m, i == j ? madet0 : madet1);
-        A.em[(int64_t)sym4(i, j) * E + e] = make_float2(m.hi, m.lo);
+        K[i][j] = m;
+        K[j][i] = m;
       }
     const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
     const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
@@ -468,8 +469,14 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
         r[i] = df_sub(r[i], df_mul(s, rs));
       }
     }
+    // row-slice records: element e, local row i -> {K_i0, K_i1, K_i2, K_i3, r_i, 0}
+    float4* rec = reinterpret_cast<float4*>(A.em) + (uint32_t)e * 12u;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) A.em[(int64_t)(10 + i) * E + e] = make_float2(r[i].hi, r[i].lo);
+    for (int i = 0; i < 4; ++i) {
+      rec[3 * i + 0] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
+      rec[3 * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, K[i][3].hi, K[i][3].lo);
+      rec[3 * i + 2] = make_float4(r[i].hi, r[i].lo, 0.0f, 0.0f);
+    }
   }
 }
 
@@ -501,9 +508,8 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
   note_launch();
   extern __shared__ unsigned char smem_raw[];
   float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
-  const float2* em = reinterpret_cast<const float2*>(P.em);
+  const float4* rec = reinterpret_cast<const float4*>(P.em);
   const int t = threadIdx.x;
-  const int64_t E = P.E;
   for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
     const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
     const bool in_smem = L <= RMAX;
@@ -517,11 +523,11 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
     for (int q = ib; q < ie; ++q) {
       const int inc = __ldg(P.ne_col + q);
       const uint32_t pw = __ldg(P.ne_pos + q);
-      const int e = inc >> 4, a = inc & 15;
-      float2 v2[4];
-#pragma unroll
-      for (int b = 0; b < 4; ++b) v2[b] = __ldg(em + (int64_t)sym4(a, b) * E + e);
-      const float2 rv = __ldg(em + (int64_t)(10 + a) * E + e);
+      // record of (element, local row) = inc>>4, inc&15: index 3*(4e + a)
+      const uint32_t ri = 3u * (uint32_t)(((inc >> 4) << 2) | (inc & 15));
+      const float4 q0 = __ldg(rec + ri), q1 = __ldg(rec + ri + 1), q2 = __ldg(rec + ri + 2);
+      const float2 v2[4] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
+                            make_float2(q1.z, q1.w)};
 #pragma unroll
       for (int b = 0; b < 4; ++b) {
         const int pos = (pw >> (8 * b)) & 0xffu;
@@ -533,7 +539,7 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
           P.val[base + pos] += (double)v2[b].x + (double)v2[b].y;
         }
       }
-      r = df_add(r, {rv.x, rv.y});
+      r = df_add(r, {q2.x, q2.y});
     }
     if (in_smem)
       for (int k = 0; k < L; ++k) {
@@ -711,7 +717,9 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   A.have_abs = p->have_absorption;
   const bool closed = use_p1_closed_form(m, p);
   const int loc = m->loc;
-  const int ncoef = closed ? 14 : loc * loc + loc;
+  // coefficient storage per element (doubles): 14 for the FP64 closed form,
+  // 24 for the double-float row-slice records, LOC*(LOC+1) for the general form
+  const int ncoef = closed ? 24 : loc * loc + loc;
   FL_TRY(m->em.reserve((size_t)ncoef * m->E));
   A.em = m->em.p;
   if (m->timing) {
