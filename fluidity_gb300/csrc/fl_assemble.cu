@@ -24,6 +24,7 @@
 // is exact in real arithmetic; results agree with the reference loops to
 // rounding.
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -520,31 +521,54 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
     }
     df r = {0.0f, 0.0f};
     const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
-    for (int q = ib; q < ie; ++q) {
-      const int inc = __ldg(P.ne_col + q);
-      const uint32_t pw = __ldg(P.ne_pos + q);
-      // record of (element, local row) = inc>>4, inc&15: index 3*(4e + a)
-      const uint32_t ri = 3u * (uint32_t)(((inc >> 4) << 2) | (inc & 15));
-      const float4 q0 = __ldg(rec + ri), q1 = __ldg(rec + ri + 1), q2 = __ldg(rec + ri + 2);
-      const float2 v2[4] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
-                            make_float2(q1.z, q1.w)};
+    // incidences in groups of four: all index and record loads of a group are
+    // issued before any accumulation (memory-level parallelism); the adds run
+    // in the group's order, so the colour order of the sum is kept
+    for (int q0 = ib; q0 < ie; q0 += 4) {
+      int inc[4];
+      uint32_t pw[4];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int pos = (pw >> (8 * b)) & 0xffu;
-        if (in_smem) {
-          const float2 c = acc[pos * THREADS + t];
-          const df sum = df_add({c.x, c.y}, {v2[b].x, v2[b].y});
-          acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
+      for (int u = 0; u < 4; ++u) {
+        const bool ok = q0 + u < ie;
+        inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
+        pw[u] = ok ? __ldg(P.ne_pos + q0 + u) : 0u;
+      }
+      float4 q[4][3];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        // record of (element, local row) = inc>>4, inc&15: index 3*(4e + a)
+        const uint32_t ri = 3u * (uint32_t)(((inc[u] >> 4) << 2) | (inc[u] & 15));
+        if (q0 + u < ie) {
+          q[u][0] = __ldg(rec + ri);
+          q[u][1] = __ldg(rec + ri + 1);
+          q[u][2] = __ldg(rec + ri + 2);
         } else {
-          P.val[base + pos] += (double)v2[b].x + (double)v2[b].y;
+          q[u][0] = q[u][1] = q[u][2] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
       }
-      r = df_add(r, {q2.x, q2.y});
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (q0 + u >= ie) break;
+        const float2 v2[4] = {make_float2(q[u][0].x, q[u][0].y), make_float2(q[u][0].z, q[u][0].w),
+                              make_float2(q[u][1].x, q[u][1].y), make_float2(q[u][1].z, q[u][1].w)};
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int pos = (pw[u] >> (8 * b)) & 0xffu;
+          if (in_smem) {
+            const float2 c = acc[pos * THREADS + t];
+            const df sum = df_add({c.x, c.y}, {v2[b].x, v2[b].y});
+            acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
+          } else {
+            P.val[base + pos] += df_to_double({v2[b].x, v2[b].y});
+          }
+        }
+        r = df_add(r, {q[u][2].x, q[u][2].y});
+      }
     }
     if (in_smem)
       for (int k = 0; k < L; ++k) {
         const float2 c = acc[k * THREADS + t];
-        P.val[base + k] = (double)c.x + (double)c.y;
+        P.val[base + k] = df_to_double({c.x, c.y});
       }
     P.rhs[row] = df_to_double(r);
   }
@@ -642,6 +666,37 @@ __global__ void k_dirichlet(int32_t nb, const int32_t* __restrict__ nodes, int32
   }
 }
 
+// Row pass with the row-tile index chosen for the mesh: 0, 1, 2 select 64,
+// 128, 256 rows per block for P1 (32, 64, 128 for P2).  Shared accumulators
+// are sized to the mesh's longest row; longer rows, if any, accumulate in
+// place in val.  Every row is summed by one thread in incidence order, so the
+// tile changes no result.
+static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int max_row, int tile, cudaStream_t s) {
+  if (loc == 4 && use_df) {
+    if (max_row <= 16) {
+      if (tile == 0) return launch_pull_df<64, 16>(P, s);
+      if (tile == 2) return launch_pull_df<256, 16>(P, s);
+      return launch_pull_df<128, 16>(P, s);
+    }
+    if (tile == 0) return launch_pull_df<64, 32>(P, s);
+    if (tile == 2) return launch_pull_df<256, 32>(P, s);
+    return launch_pull_df<128, 32>(P, s);
+  }
+  if (loc == 4 && closed) {
+    if (tile == 0) return launch_pull<4, true, 64, 32>(P, s);
+    if (tile == 2) return launch_pull<4, true, 256, 32>(P, s);
+    return launch_pull<4, true, 128, 32>(P, s);
+  }
+  if (loc == 4) {
+    if (tile == 0) return launch_pull<4, false, 64, 32>(P, s);
+    if (tile == 2) return launch_pull<4, false, 256, 32>(P, s);
+    return launch_pull<4, false, 128, 32>(P, s);
+  }
+  if (tile == 0) return launch_pull<10, false, 32, 96>(P, s);
+  if (tile == 2) return launch_pull<10, false, 128, 96>(P, s);
+  return launch_pull<10, false, 64, 96>(P, s);
+}
+
 // Per-mesh cache of reference tensors keyed by (field degree, quad degree).
 struct TensorCache {
   std::mutex mu;
@@ -676,8 +731,22 @@ static bool use_p1_closed_form(const fl_mesh_t* m, const fl_advdif_params* p) {
          p->have_diffusivity;
 }
 
+size_t assembly_scratch_doubles(const fl_mesh_t* m, const fl_advdif_params* p) {
+  const bool closed = use_p1_closed_form(m, p);
+  const int ncoef = closed ? 24 : m->loc * m->loc + m->loc;
+  return (size_t)ncoef * m->E;
+}
+
+int dirichlet_launch(fl_mesh_t* m, int32_t nb, const int32_t* nodes, int32_t base, const double* g, const double* t,
+                     double dt, double* rhs, uint8_t* inactive, cudaStream_t s) {
+  if (nb <= 0) return FL_OK;
+  k_dirichlet<<<grid_for(nb, 256), 256, 0, s>>>(nb, nodes, base, g, t, dt, m->N, rhs, inactive, m->err.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
 int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
-             cudaStream_t s) {
+             cudaStream_t s, double* em_override) {
   FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
   FL_CHECK_ARG(p->quad_degree >= 1 && p->quad_degree <= 4, "quadrature degree 1..4");
   FL_CHECK_ARG(!p->have_advection || f->velocity, "advection needs a velocity field");
@@ -720,8 +789,14 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   // coefficient storage per element (doubles): 14 for the FP64 closed form,
   // 24 for the double-float row-slice records, LOC*(LOC+1) for the general form
   const int ncoef = closed ? 24 : loc * loc + loc;
-  FL_TRY(m->em.reserve((size_t)ncoef * m->E));
-  A.em = m->em.p;
+  double* em = em_override;
+  if (!em) {
+    FL_TRY(m->em.reserve((size_t)ncoef * m->E));
+    em = m->em.p;
+  }
+  A.em = em;
+  // element-pass tiles (the autotuner's choice; results do not depend on it)
+  const int eb = m->tile_elem_block, esm = m->tile_elem_per_sm;
   if (m->timing) {
     if (!m->ev0) {
       FL_TRY_CUDA(cudaEventCreate(&m->ev0));
@@ -746,7 +821,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     D.X = m->coords.p;
     D.t = f->t;
     D.f = f->source;
-    D.em = reinterpret_cast<float2*>(m->em.p);
+    D.em = reinterpret_cast<float2*>(em);
     const double kap = p->isotropic_diffusivity ? p->diffusivity[0] : 1.0;
     D.kscale = df_host(h.wsum * (A.use_dt ? A.theta_dt : 0.0) * kap);
     D.rscale = df_host(h.wsum * kap);
@@ -756,32 +831,93 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     D.m1 = df_host(h.M[0][1]);
     D.have_mass = p->have_mass;
     D.have_src = p->have_source;
-    k_asm_p1_diffusion_df<<<grid_for(m->E, 256, 16), 256, 0, s>>>(D);
+    k_asm_p1_diffusion_df<<<grid_for(m->E, eb, esm), eb, 0, s>>>(D);
   } else if (closed) {
-    k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
+    k_asm_p1_diffusion<<<grid_for(m->E, eb, esm), eb, 0, s>>>(A);
   } else if (loc == 4) {
-    k_asm_general<4><<<grid_for(m->E, 128, 16), 128, 0, s>>>(A);
+    k_asm_general<4><<<grid_for(m->E, 128, esm), 128, 0, s>>>(A);
   } else {
-    k_asm_general<10><<<grid_for(m->E, 128, 16), 128, 0, s>>>(A);
+    k_asm_general<10><<<grid_for(m->E, 128, esm), 128, 0, s>>>(A);
   }
   FL_TRY_CUDA(cudaGetLastError());
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
-             m->em.p, val, rhs, m->err.p};
-  if (loc == 4) {
-    // shared accumulators sized to the mesh's longest row (longer rows, if any,
-    // accumulate in place in val)
-    if (use_df && m->max_row <= 16) FL_TRY((launch_pull_df<128, 16>(P, s)));
-    else if (use_df) FL_TRY((launch_pull_df<128, 32>(P, s)));
-    else if (closed) FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
-    else FL_TRY((launch_pull<4, false, 128, 32>(P, s)));
-  } else {
-    FL_TRY((launch_pull<10, false, 64, 96>(P, s)));
-  }
+             em, val, rhs, m->err.p};
+  FL_TRY(launch_rows(P, loc, use_df, closed, m->max_row, m->tile_rows, s));
   if (m->timing) {
     FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
     m->timed = true;
   }
   return FL_OK;
+}
+
+// Tile autotuner: times the assembly of this mesh and parameter set under
+// each element-pass tile (threads per block x blocks per SM) and then each
+// row-pass tile, keeping the fastest of each (median of three timed runs
+// after one warm-up).  The candidates only regroup independent elements and
+// rows, so val and rhs are the same under every choice; they hold the
+// assembled system on return.
+int autotune_assembly(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
+                      cudaStream_t s) {
+  static const int kBlocks[] = {128, 256};
+  static const int kPerSm[] = {4, 8, 16, 32};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FL_TRY_CUDA(cudaEventCreate(&e0));
+  FL_TRY_CUDA(cudaEventCreate(&e1));
+  const bool timing = m->timing;
+  m->timing = false;
+  auto time_one = [&](float* ms) -> int {
+    float t[3];
+    FL_TRY(assemble(m, p, f, val, rhs, s, nullptr));
+    for (int k = 0; k < 3; ++k) {
+      FL_TRY_CUDA(cudaEventRecord(e0, s));
+      FL_TRY(assemble(m, p, f, val, rhs, s, nullptr));
+      FL_TRY_CUDA(cudaEventRecord(e1, s));
+      FL_TRY_CUDA(cudaEventSynchronize(e1));
+      FL_TRY_CUDA(cudaEventElapsedTime(&t[k], e0, e1));
+    }
+    std::sort(t, t + 3);
+    *ms = t[1];
+    return FL_OK;
+  };
+  int st = FL_OK;
+  do {
+    float best = 1e30f;
+    int bb = m->tile_elem_block, bs = m->tile_elem_per_sm;
+    for (int b : kBlocks)
+      for (int ps : kPerSm) {
+        m->tile_elem_block = b;
+        m->tile_elem_per_sm = ps;
+        float ms = 0.f;
+        if ((st = time_one(&ms)) != FL_OK) break;
+        if (ms < best) {
+          best = ms;
+          bb = b;
+          bs = ps;
+        }
+      }
+    m->tile_elem_block = bb;
+    m->tile_elem_per_sm = bs;
+    if (st != FL_OK) break;
+    best = 1e30f;
+    int br = m->tile_rows;
+    for (int r = 0; r < 3; ++r) {
+      m->tile_rows = r;
+      float ms = 0.f;
+      if ((st = time_one(&ms)) != FL_OK) break;
+      if (ms < best) {
+        best = ms;
+        br = r;
+      }
+    }
+    m->tile_rows = br;
+    if (st != FL_OK) break;
+    st = assemble(m, p, f, val, rhs, s, nullptr);
+    m->tuned = true;
+  } while (0);
+  m->timing = timing;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
 }
 
 }  // namespace fl
@@ -796,7 +932,7 @@ extern "C" int fl_dev_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, c
                                          double* val, double* rhs, void* stream) {
   FL_CHECK_ARG(m, "null mesh");
   cudaStream_t s = pick_stream(m, stream);
-  FL_TRY(assemble(m, p, f, val, rhs, s));
+  FL_TRY(assemble(m, p, f, val, rhs, s, nullptr));
   // pattern misses are reported synchronously, as FLAbort is in the reference
   return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
 }
@@ -823,6 +959,30 @@ extern "C" int fl_gpu_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, c
   FL_TRY_CUDA(cudaMemcpyAsync(val, m->st_val.p, sizeof(double) * m->nnz, cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaMemcpyAsync(rhs, m->st_rhs.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
+  return FL_OK;
+}
+
+extern "C" int fl_dev_autotune_assembly(fl_mesh m, const fl_advdif_params* p, const fl_fields* f, double* val,
+                                        double* rhs, void* stream, int32_t* tiles) {
+  FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
+  cudaStream_t s = pick_stream(m, stream);
+  FL_TRY(autotune_assembly(m, p, f, val, rhs, s));
+  if (tiles) {
+    tiles[0] = m->tile_elem_block;
+    tiles[1] = m->tile_elem_per_sm;
+    tiles[2] = m->tile_rows;
+  }
+  return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
+}
+
+extern "C" int fl_set_assembly_tiles(fl_mesh m, int32_t elem_block, int32_t elem_blocks_per_sm, int32_t row_tile) {
+  FL_CHECK_ARG(m, "null mesh");
+  FL_CHECK_ARG(elem_block == 128 || elem_block == 256, "element block 128 or 256");
+  FL_CHECK_ARG(elem_blocks_per_sm >= 1 && elem_blocks_per_sm <= 64, "element blocks per SM 1..64");
+  FL_CHECK_ARG(row_tile >= 0 && row_tile <= 2, "row tile 0..2");
+  m->tile_elem_block = elem_block;
+  m->tile_elem_per_sm = elem_blocks_per_sm;
+  m->tile_rows = row_tile;
   return FL_OK;
 }
 

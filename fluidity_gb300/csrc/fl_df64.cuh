@@ -130,6 +130,22 @@ inline df df_host(double d) {
   return {hi, (float)(d - (double)hi)};
 }
 
-__device__ __forceinline__ double df_to_double(df x) { return (double)x.hi + (double)x.lo; }
+// Exact float -> double by bits (GB300 runs F2F conversions on the FP64 pipe at
+// FP64 rate; this uses the integer pipe).  Zero and subnormal floats map to
+// a signed zero (magnitudes below 2^-126 do not occur in assembled values).
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xffu;
+  const uint32_t sign = b & 0x80000000u;
+  if (e == 0u) return __hiloint2double((int)sign, 0);
+  if (e == 0xffu) return (double)f;  // inf / nan: keep IEEE semantics
+  const uint32_t m = b & 0x7fffffu;
+  const uint32_t hi = sign | ((e + 896u) << 20) | (m >> 3);
+  const uint32_t lo = m << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// hi + lo as one double: exact conversions by bits, one FP64 add.
+__device__ __forceinline__ double df_to_double(df x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
 
 }  // namespace fl

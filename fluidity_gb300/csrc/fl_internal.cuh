@@ -88,6 +88,63 @@ struct ErrWord {
   int32_t where;     // kernel-specific detail (element / row index)
 };
 
+// Graph-capturable FP64 CG on one system (batched solves).  cg_prepare may
+// synchronise (first use of a mesh builds its sliced layout); the *_launch and
+// cg_iterate calls only enqueue device work.
+struct KrylovWork;
+struct KspState;
+struct SpArgs {
+  int32_t n;
+  const int32_t* findrm;
+  const int32_t* colm;
+  const double* val;
+  const uint8_t* ghost;  // may be null
+  KspState* st;
+};
+
+struct SellArgs {
+  int32_t n;
+  const int32_t* sptr;
+  const int32_t* scol;
+  const uint8_t* ghost;
+  KspState* st;
+};
+
+struct CgPlan {
+  struct ::fl_mesh_t* m = nullptr;
+  KrylovWork* W = nullptr;
+  fl_solver_opts o{};
+  const double* val = nullptr;
+  const uint8_t* ghost = nullptr;
+  const double* rhs = nullptr;
+  double* x = nullptr;
+  int n = 0, G = 2, np = 0;
+  int ksp = 0, restart = 30;  // 0: CG (one iteration per cg_iterate), 1: GMRES (one cycle)
+  unsigned gsp = 0, gv = 0, gsl = 0;
+  int64_t sell_len = 0;
+  const int32_t* smap = nullptr;
+  SellArgs SA{};
+  SpArgs A{};
+};
+int cg_prepare(CgPlan& P, struct ::fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost,
+               const double* rhs, double* x, cudaStream_t s);
+void cg_setup_launch(CgPlan& P, cudaStream_t s);
+void cg_iterate(CgPlan& P, cudaStream_t s);
+void cg_finish_launch(CgPlan& P, cudaStream_t s);
+int cg_report(CgPlan& P, fl_solve_report* rep, cudaStream_t s);
+void cg_release(CgPlan& P);
+KspState* cg_state(CgPlan& P);
+void gather_done(KspState* const* d_states, int n, int* d_out, cudaStream_t s);
+
+// Assembly pieces used by batches (no synchronisation, no allocation).
+size_t assembly_scratch_doubles(const struct ::fl_mesh_t* m, const fl_advdif_params* p);
+int assemble(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
+             cudaStream_t s, double* em_override);
+int dirichlet_launch(struct ::fl_mesh_t* m, int32_t nb, const int32_t* nodes, int32_t base, const double* g,
+                     const double* t, double dt, double* rhs, uint8_t* inactive, cudaStream_t s);
+int autotune_assembly(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val,
+                      double* rhs, cudaStream_t s);
+
 // Per-translation-unit launch counters and workspace release hooks.
 unsigned long long launches_mesh();
 unsigned long long launches_assemble();
@@ -108,6 +165,11 @@ struct fl_mesh_t {
   int64_t nnz = 0;
   int32_t ncolours = 0;
   int32_t max_row = 0;  // longest CSR row
+  // assembly tiles (set by the autotuner; results do not depend on them)
+  int tile_elem_block = 256;  // threads per element-pass block
+  int tile_elem_per_sm = 16;  // element-pass blocks per SM of the grid-stride grid
+  int tile_rows = 1;          // row-pass tile index (see launch_rows)
+  bool tuned = false;
   cudaStream_t stream = nullptr;
 
   fl::DevBuf<int32_t> ndglno;        // E*loc, 0-based, element-major

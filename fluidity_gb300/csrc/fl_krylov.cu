@@ -43,6 +43,7 @@ struct KspState {
   double rtol, atol, dtol, rnorm0, ttol, snorm_b;
   double rnorm;          // last residual norm tested
   int its, max_its, reason, done, guess_zero;
+  int cg_i;              // CG iteration index (advanced on the device)
   // CG scalars
   double beta, betaold, dpi, dpiold, alpha, pcoef, dpi_next, beta_n, betaold_n;
   // ghost pivot reduction
@@ -50,6 +51,8 @@ struct KspState {
   // GMRES
   int it;                // inner index of the current cycle
   int hapend;
+  int live;              // the current cycle started unconverged (its correction is applied)
+  int gm_first;          // next cycle is the first (device-driven restarts)
   double grs[kMaxRestart + 2];
   double cc[kMaxRestart + 1], ss[kMaxRestart + 1];
   double hh[(kMaxRestart + 1) * (kMaxRestart + 1)];   // column-major, ld = restart+1
@@ -186,14 +189,6 @@ __device__ __forceinline__ double row_dot(const int32_t* __restrict__ findrm, co
   return s;
 }
 
-struct SpArgs {
-  int32_t n;
-  const int32_t* findrm;
-  const int32_t* colm;
-  const double* val;
-  const uint8_t* ghost;  // may be null
-  KspState* st;
-};
 
 // ---------------------------------------------------------------- setup --
 // diag / ghost pivot inputs: min and max of |diag| over all rows.
@@ -300,6 +295,7 @@ __global__ void k_init_resid(SpArgs A, const double* __restrict__ b, const doubl
   __shared__ double red[kThreads / 32];
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
+  if (A.st->done) return;  // a restart after convergence (device-driven GMRES)
   double zz = 0.0, bb = 0.0, zr = 0.0;
   const double piv = A.st->pivot;
   const bool gz = A.st->guess_zero;
@@ -396,13 +392,6 @@ __global__ void k_sell_values(int64_t len, const int32_t* __restrict__ smap, con
   }
 }
 
-struct SellArgs {
-  int32_t n;
-  const int32_t* sptr;
-  const int32_t* scol;
-  const uint8_t* ghost;
-  KspState* st;
-};
 
 // Row r of the sliced layout: sum over the row's entries in CSR order (the
 // same order as a sequential CSR row product, so results are deterministic).
@@ -443,21 +432,23 @@ __device__ __forceinline__ bool last_block(unsigned* ticket) {
   return last;
 }
 
-__global__ void k_cg_p(int n, const KspState* st, int i, const double* __restrict__ z, double* __restrict__ p) {
+__global__ void k_cg_p(int n, const KspState* st, const double* __restrict__ z, double* __restrict__ p) {
   note_launch();
   if (st->done) return;
+  const int i = st->cg_i;
   const double coef = st->pcoef;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     p[k] = i == 0 ? z[k] : z[k] + coef * p[k];
 }
 
 __global__ void k_cg_ap(SellArgs A, const double* __restrict__ sval, const double* __restrict__ p,
-                        double* __restrict__ w, double* __restrict__ part, unsigned* ticket, int i) {
+                        double* __restrict__ w, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   __shared__ float2 redf[kThreads / 32];
   KspState* st = A.st;
   if (st->done) return;
+  const int i = st->cg_i;
   const double piv = st->pivot;
   double pw = 0.0;
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
@@ -485,13 +476,14 @@ __global__ void k_cg_ap(SellArgs A, const double* __restrict__ sval, const doubl
   }
 }
 
-__global__ void k_cg_xr(int n, KspState* st, int i, const double* __restrict__ p, const double* __restrict__ w,
+__global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const double* __restrict__ w,
                         const double* __restrict__ dinv, double* __restrict__ y, double* __restrict__ r,
                         double* __restrict__ z, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   __shared__ float2 redf[kThreads / 32];
   if (st->done) return;
+  const int i = st->cg_i;
   const double a = st->alpha;
   double zz = 0.0, zr = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -537,6 +529,7 @@ __global__ void k_cg_xr(int n, KspState* st, int i, const double* __restrict__ p
     } else {
       S.its = i + 1;
     }
+    if (!S.done) S.cg_i = i + 1;
   }
 }
 
@@ -545,6 +538,7 @@ __global__ void k_cg_open(KspState* st) {
   note_launch();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   KspState& S = *st;
+  S.cg_i = 0;
   if (S.done) return;
   S.its = 1;
   S.pcoef = 0.0;
@@ -682,14 +676,26 @@ __global__ void k_scale_vec(int n, const KspState* st, double* __restrict__ v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] *= inv;
 }
 
-// Cycle start: res = ||v0||, grs(0) = res, test; v0 normalised.
+// Cycle start: res = ||v0||, grs(0) = res, test; v0 normalised.  first < 0
+// takes the first-cycle flag from the state (restarts decided on the device);
+// a solve that has already converged leaves the state as it is.
 __global__ void k_gmres_cycle_start(KspState* st, const double* __restrict__ part, int nparts, int first) {
   note_launch();
   __shared__ double red[kThreads / 32];
+  if (st->done) {
+    __syncthreads();
+    if (threadIdx.x == 0) st->live = 0;
+    return;
+  }
   const double nn = reduce_partials(part, nparts, red);
   const double bb = reduce_partials(part + nparts, nparts, red);
   if (threadIdx.x != 0) return;
   KspState& S = *st;
+  if (first < 0) {
+    first = S.gm_first;
+    S.gm_first = 0;
+  }
+  S.live = 1;
   const double res = sqrt(nn);
   if (first) {
     S.snorm_b = sqrt(bb);
@@ -735,6 +741,7 @@ __global__ void k_gmres_backsolve(KspState* st, int restart) {
   note_launch();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   KspState& S = *st;
+  if (!S.live) return;
   const int ld = restart + 1;
   auto HH = [&](int i, int j) -> double { return S.hh[j * ld + i]; };
   const int last = S.it - 1;
@@ -751,6 +758,7 @@ __global__ void k_gmres_backsolve(KspState* st, int restart) {
 __global__ void k_gmres_update_x(int n, const KspState* st, const double* __restrict__ V, int64_t ld,
                                  double* __restrict__ y) {
   note_launch();
+  if (!st->live) return;
   const int last = st->it - 1;
   if (last < 0) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -758,6 +766,21 @@ __global__ void k_gmres_update_x(int n, const KspState* st, const double* __rest
     for (int j = 0; j <= last; ++j) s += st->nrs[j] * V[(int64_t)j * ld + i];
     y[i] += s;
   }
+}
+
+// End of a device-driven cycle: the iteration limit (KSPSolve_GMRES's
+// itcount >= max_it test) and the nonzero guess of the restart.
+__global__ void k_gmres_cycle_end(KspState* st) {
+  note_launch();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  KspState& S = *st;
+  if (!S.live) return;
+  S.live = 0;
+  if (!S.done && S.its >= S.max_its) {
+    S.reason = FL_DIVERGED_ITS;
+    S.done = 1;
+  }
+  S.guess_zero = 0;
 }
 
 // ------------------------------------------------------------- finalise --
@@ -827,9 +850,10 @@ struct SpArgs32 {
 // Inner CG of the refinement, same three-launch structure as the FP64 CG:
 // fp32 matrix and vectors, fp64 dot products and scalars.  The inner problem
 // starts from d = 0 and stops when ||B r|| <= ttol (set by the outer loop).
-__global__ void k_cg32_p(int n, const KspState* st, int i, const float* __restrict__ z, float* __restrict__ p) {
+__global__ void k_cg32_p(int n, const KspState* st, const float* __restrict__ z, float* __restrict__ p) {
   note_launch();
   if (st->done) return;
+  const int i = st->cg_i;
   const float coef = (float)st->pcoef;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
     p[k] = i == 0 ? z[k] : fmaf(coef, p[k], z[k]);
@@ -869,13 +893,14 @@ __global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv,
   }
 }
 
-__global__ void k_cg32_xr(int n, KspState* st, int i, const float* __restrict__ p, const float* __restrict__ w,
+__global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, const float* __restrict__ w,
                           const float* __restrict__ dinv, float* __restrict__ d, float* __restrict__ r,
                           float* __restrict__ z, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   if (st->done) return;
   __shared__ float2 redf[kThreads / 32];
+  const int i = st->cg_i;
   const float a = (float)st->alpha;
   df zzd = {0.0f, 0.0f}, zrd = {0.0f, 0.0f};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -912,6 +937,7 @@ __global__ void k_cg32_xr(int n, KspState* st, int i, const float* __restrict__ 
     } else {
       S.beta = zrs;
       S.pcoef = S.beta / S.betaold;
+      S.cg_i = i + 1;
     }
   }
 }
@@ -993,6 +1019,39 @@ static int group_for(const fl_mesh_t* m) {
     else KERNEL<1><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
   } while (0)
 
+// Sliced-ELL pattern of the mesh, built once and cached on the workspace.
+static int ensure_sell(fl_mesh_t* m, KrylovWork* W, cudaStream_t s) {
+  if (W->sell_ready) return FL_OK;
+  const int n = m->N;
+  const int nsl = (n + kSlice - 1) / kSlice;
+  FL_TRY(W->swidth.reserve(nsl + 1));
+  FL_TRY(W->sptr.reserve(nsl + 1));
+  k_sell_width<<<grid_for(nsl, kThreads), kThreads, 0, s>>>(m->findrm.p, n, nsl, W->swidth.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY(exclusive_scan_i32(W->swidth.p, W->sptr.p, nsl, s));
+  int32_t len = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&len, W->sptr.p + nsl, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  FL_TRY(W->scol.reserve(len));
+  FL_TRY(W->smap.reserve(len));
+  k_sell_fill<<<grid_for((int64_t)nsl * kSlice, kThreads), kThreads, 0, s>>>(m->findrm.p, m->colm.p, n, W->sptr.p,
+                                                                             W->scol.p, W->smap.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  W->nslices = nsl;
+  W->sell_len = len;
+  W->sell_ready = true;
+  return FL_OK;
+}
+
+// One FP64 CG iteration: three launches, no host interaction (capturable).
+static void cg_iteration(int n, KspState* st, const SellArgs& SA, KrylovWork* W, unsigned gv, unsigned gsl, int np,
+                         cudaStream_t s) {
+  k_cg_p<<<gv, kThreads, 0, s>>>(n, st, W->z.p, W->p.p);
+  k_cg_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval.p, W->p.p, W->w2.p, W->part.p, W->ticket.p);
+  k_cg_xr<<<gv, kThreads, 0, s>>>(n, st, W->p.p, W->w2.p, W->dinv.p, W->y.p, W->r.p, W->z.p, W->part.p + 2 * np,
+                                   W->ticket.p + 1);
+}
+
 int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost, const double* rhs,
           double* x, fl_solve_report* rep, cudaStream_t s) {
   FL_CHECK_ARG(m && o && val && rhs && x && rep, "null argument");
@@ -1038,25 +1097,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
 
   int outer = 0;
   const int chunk = 16;
-  if (!W->sell_ready) {
-    const int nsl = (n + kSlice - 1) / kSlice;
-    FL_TRY(W->swidth.reserve(nsl + 1));
-    FL_TRY(W->sptr.reserve(nsl + 1));
-    k_sell_width<<<grid_for(nsl, kThreads), kThreads, 0, s>>>(m->findrm.p, n, nsl, W->swidth.p);
-    FL_TRY_CUDA(cudaGetLastError());
-    FL_TRY(exclusive_scan_i32(W->swidth.p, W->sptr.p, nsl, s));
-    int32_t len = 0;
-    FL_TRY_CUDA(cudaMemcpyAsync(&len, W->sptr.p + nsl, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    FL_TRY_CUDA(cudaStreamSynchronize(s));
-    FL_TRY(W->scol.reserve(len));
-    FL_TRY(W->smap.reserve(len));
-    k_sell_fill<<<grid_for((int64_t)nsl * kSlice, kThreads), kThreads, 0, s>>>(m->findrm.p, m->colm.p, n, W->sptr.p,
-                                                                               W->scol.p, W->smap.p);
-    FL_TRY_CUDA(cudaGetLastError());
-    W->nslices = nsl;
-    W->sell_len = len;
-    W->sell_ready = true;
-  }
+  FL_TRY(ensure_sell(m, W, s));
   SellArgs SA{n, W->sptr.p, W->scol.p, ghost, st};
   const unsigned gsl = grid_for(n, kThreads, 8);
   if (!mixed && o->ksp_type == 0) {
@@ -1071,10 +1112,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
                                                                          nullptr);
     k_cg_open<<<1, 32, 0, s>>>(st);
     for (int i = 0; i < o->max_its; ++i) {
-      k_cg_p<<<gv, kThreads, 0, s>>>(n, st, i, W->z.p, W->p.p);
-      k_cg_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval.p, W->p.p, W->w2.p, W->part.p, W->ticket.p, i);
-      k_cg_xr<<<gv, kThreads, 0, s>>>(n, st, i, W->p.p, W->w2.p, W->dinv.p, W->y.p, W->r.p, W->z.p,
-                                       W->part.p + 2 * np, W->ticket.p + 1);
+      cg_iteration(n, st, SA, W, gv, gsl, np, s);
       if ((i + 1) % chunk == 0 || i + 1 == o->max_its) {
         FL_TRY_CUDA(cudaGetLastError());
         int done = 0;
@@ -1170,13 +1208,14 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
       hs.dpi = 0.0;
       hs.its = 0;
       hs.pcoef = 0.0;
+      hs.cg_i = 0;
       hs.max_its = o->max_its - total_inner;
       FL_TRY_CUDA(cudaMemcpyAsync(st, &hs, sizeof(KspState), cudaMemcpyHostToDevice, s));
       int inner = 0;
       for (int i = 0; i < hs.max_its; ++i) {
-        k_cg32_p<<<gv, kThreads, 0, s>>>(n, st, i, W->z32.p, W->p32.p);
+        k_cg32_p<<<gv, kThreads, 0, s>>>(n, st, W->z32.p, W->p32.p);
         k_cg32_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval32.p, piv32, W->p32.p, W->w32.p, W->part.p, W->ticket.p);
-        k_cg32_xr<<<gv, kThreads, 0, s>>>(n, st, i, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
+        k_cg32_xr<<<gv, kThreads, 0, s>>>(n, st, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
                                            W->z32.p, W->part.p + 2 * np, W->ticket.p + 1);
         if ((i + 1) % chunk == 0 || i + 1 == hs.max_its) {
           FL_TRY_CUDA(cudaGetLastError());
@@ -1214,6 +1253,165 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   rep->outer_iterations = outer;
   rep->pad = 0;
   return FL_OK;
+}
+
+// ------------------------------------------------- batched / graph CG --
+__global__ void k_state_init(KspState* st, double rtol, double atol, double dtol, int max_its, int guess_zero) {
+  note_launch();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  KspState& S = *st;
+  S.rtol = rtol;
+  S.atol = atol;
+  S.dtol = dtol;
+  S.max_its = max_its;
+  S.guess_zero = guess_zero;
+  S.rnorm0 = S.ttol = S.snorm_b = S.rnorm = 0.0;
+  S.its = S.reason = S.done = 0;
+  S.cg_i = 0;
+  S.beta = S.betaold = S.dpi = S.dpiold = S.alpha = S.pcoef = S.dpi_next = 0.0;
+  S.true_r2 = S.b2 = 0.0;
+  S.it = S.hapend = S.live = 0;
+  S.gm_first = 1;
+  S.tt = 0.0;
+}
+
+// done flags of several solves gathered into one array (polled by the host)
+__global__ void k_gather_done(KspState* const* sts, int n, int* out) {
+  note_launch();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = sts[i]->done;
+}
+
+int cg_prepare(CgPlan& P, fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost,
+               const double* rhs, double* x, cudaStream_t s) {
+  FL_CHECK_ARG(m && o && val && rhs && x, "null argument");
+  FL_CHECK_ARG((o->ksp_type == 0 || o->ksp_type == 1) && o->precision == 0,
+               "graph-batched solves are FP64 CG or GMRES");
+  FL_CHECK_ARG(o->max_its >= 0, "max_its");
+  const int restart = o->restart > 0 ? o->restart : 30;
+  FL_CHECK_ARG(restart <= kMaxRestart, "gmres restart above 64");
+  KrylovWork* M = work_of(m);  // pattern owner
+  if (!M) return FL_ERR_NOMEM;
+  FL_TRY(ensure_sell(m, M, s));
+  if (!P.W) P.W = new KrylovWork();
+  KrylovWork* W = P.W;
+  const int n = m->N;
+  P.m = m;
+  P.o = *o;
+  P.val = val;
+  P.ghost = ghost;
+  P.rhs = rhs;
+  P.x = x;
+  P.n = n;
+  P.G = group_for(m);
+  P.gsp = grid_for((int64_t)n * P.G, kThreads, 8);
+  P.gv = grid_for(n, kThreads, 8);
+  P.gsl = grid_for(n, kThreads, 8);
+  P.np = (int)std::max(P.gsp, P.gv);
+  P.ksp = o->ksp_type;
+  P.restart = restart;
+  if (P.ksp == 1) FL_TRY(W->V.reserve((size_t)(restart + 1) * n));
+  FL_TRY(W->b.reserve(n));
+  FL_TRY(W->y.reserve(n));
+  FL_TRY(W->r.reserve(n));
+  FL_TRY(W->z.reserve(n));
+  FL_TRY(W->p.reserve(n));
+  FL_TRY(W->w2.reserve(n));
+  FL_TRY(W->dinv.reserve(n));
+  FL_TRY(W->part.reserve((size_t)P.np * (kMaxRestart + 2)));
+  FL_TRY(W->st.reserve(1));
+  FL_TRY(W->ticket.reserve(4));
+  FL_TRY(W->sval.reserve(M->sell_len));
+  P.sell_len = M->sell_len;
+  P.smap = M->smap.p;
+  P.SA = SellArgs{n, M->sptr.p, M->scol.p, ghost, W->st.p};
+  P.A = SpArgs{n, m->findrm.p, m->colm.p, val, ghost, W->st.p};
+  return FL_OK;
+}
+
+// Everything before the first iteration, as device work only (capturable).
+void cg_setup_launch(CgPlan& P, cudaStream_t s) {
+  KrylovWork* W = P.W;
+  KspState* st = W->st.p;
+  const int G = P.G;
+  const unsigned gsp = P.gsp;
+  k_state_init<<<1, 32, 0, s>>>(st, P.o.rtol, P.o.atol, P.o.dtol > 0 ? P.o.dtol : 1e5, P.o.max_its,
+                                 P.o.start_from_zero ? 1 : 0);
+  k_diag<<<P.gv, kThreads, 0, s>>>(P.A, P.m->centrm.p, W->dinv.p, W->part.p, W->part.p + P.np);
+  k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + P.np, (int)P.gv);
+  k_dinv<<<P.gv, kThreads, 0, s>>>(P.n, P.ghost, st, W->dinv.p, nullptr);
+  FL_SPMV_DISPATCH(G, k_lift, P.A, P.rhs, P.x, P.o.start_from_zero ? 1 : 0, W->b.p, W->y.p);
+  if (P.ksp == 1) return;  // GMRES: the first cycle computes the initial residual
+  FL_SPMV_DISPATCH(G, k_init_resid, P.A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
+  k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
+  cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s);
+  cudaMemsetAsync(W->p.p, 0, sizeof(double) * P.n, s);
+  k_sell_values<<<grid_for(P.sell_len, kThreads), kThreads, 0, s>>>(P.sell_len, P.smap, P.val, W->sval.p, nullptr);
+  k_cg_open<<<1, 32, 0, s>>>(st);
+}
+
+// One GMRES(restart) cycle with the restart decisions on the device: the same
+// launches as solve()'s host-driven cycle; every launch returns at once when
+// the solve has converged, so cycles may be replayed past convergence.
+static void gmres_cycle(CgPlan& P, cudaStream_t s) {
+  KrylovWork* W = P.W;
+  KspState* st = W->st.p;
+  const int G = P.G, n = P.n, restart = P.restart;
+  const unsigned gsp = P.gsp, gv = P.gv;
+  const int64_t ld = n;
+  double* V = W->V.p;
+  FL_SPMV_DISPATCH(G, k_init_resid, P.A, W->b.p, W->y.p, W->dinv.p, W->r.p, V, W->part.p, (int)gsp);
+  k_gmres_cycle_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, -1);
+  k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V);
+  for (int it = 0; it < restart; ++it) {
+    FL_SPMV_DISPATCH(G, k_apply_BA, P.A, W->dinv.p, V + it * ld, V + (it + 1) * ld);
+    k_mdot<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p, (int)gv);
+    k_gs_coeffs<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it);
+    k_gs_update<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p);
+    k_gmres_step<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it, restart);
+    k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V + (it + 1) * ld);
+  }
+  k_gmres_backsolve<<<1, 32, 0, s>>>(st, restart);
+  k_gmres_update_x<<<gv, kThreads, 0, s>>>(n, st, V, ld, W->y.p);
+  k_gmres_cycle_end<<<1, 32, 0, s>>>(st);
+}
+
+void cg_iterate(CgPlan& P, cudaStream_t s) {
+  if (P.ksp == 1) gmres_cycle(P, s);
+  else cg_iteration(P.n, P.W->st.p, P.SA, P.W, P.gv, P.gsl, P.np, s);
+}
+
+void cg_finish_launch(CgPlan& P, cudaStream_t s) {
+  KrylovWork* W = P.W;
+  const int G = P.G;
+  const unsigned gsp = P.gsp;
+  FL_SPMV_DISPATCH(G, k_true_resid, P.A, W->b.p, W->y.p, W->part.p, (int)gsp);
+  k_true_resid_final<<<1, kThreads, 0, s>>>(W->st.p, W->part.p, (int)gsp);
+  k_copy_back<<<P.gv, kThreads, 0, s>>>(P.n, P.ghost, P.rhs, W->y.p, P.x);
+}
+
+int cg_report(CgPlan& P, fl_solve_report* rep, cudaStream_t s) {
+  KspState hs;
+  FL_TRY_CUDA(cudaMemcpyAsync(&hs, P.W->st.p, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  rep->iterations = hs.its;
+  rep->reason = hs.reason ? hs.reason : FL_DIVERGED_ITS;
+  rep->final_rnorm = hs.rnorm;
+  rep->rnorm0 = hs.rnorm0;
+  rep->true_rel_residual = hs.b2 > 0 ? sqrt(hs.true_r2 / hs.b2) : sqrt(hs.true_r2);
+  rep->outer_iterations = 0;
+  rep->pad = 0;
+  return FL_OK;
+}
+
+void cg_release(CgPlan& P) {
+  delete P.W;
+  P.W = nullptr;
+}
+
+KspState* cg_state(CgPlan& P) { return P.W->st.p; }
+
+void gather_done(KspState* const* d_states, int n, int* d_out, cudaStream_t s) {
+  k_gather_done<<<1, 128, 0, s>>>(d_states, n, d_out);
 }
 
 // Cached workspace per mesh handle.

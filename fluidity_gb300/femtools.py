@@ -15,6 +15,8 @@ this module                     reference
 ``apply_dirichlet_conditions``  Boundary_Conditions.F90:1983
 ``petsc_solve``                 Solvers.F90:111 (petsc_solve_scalar)
 ``solve_field_equation_cg``     Advection_Diffusion_CG.F90:127
+``Batch``                       many ``solve_field_equation_cg`` steps at once
+``autotune_assembly``           (no counterpart: assembly tile choice)
 ==============================  ================================================
 
 Arrays are numpy (host, copied through the ``fl_gpu_*`` entry points) or torch
@@ -245,12 +247,7 @@ def petsc_solve(mesh: Mesh, x, val, rhs, options: SolverOpts, inactive=None, str
         ina = np.ascontiguousarray(inactive, dtype=np.uint8) if inactive is not None else None
         check(lib.fl_gpu_petsc_solve(mesh.handle, C.byref(options), _ptr(v), _ptr(ina), _ptr(b),
                                      _ptr(x), C.byref(rep)), "fl_gpu_petsc_solve")
-    return {
-        "iterations": rep.iterations, "reason": rep.reason,
-        "reason_name": _lib.REASONS.get(rep.reason, str(rep.reason)),
-        "final_rnorm": rep.final_rnorm, "rnorm0": rep.rnorm0,
-        "true_rel_residual": rep.true_rel_residual, "outer_iterations": rep.outer_iterations,
-    }
+    return _report_dict(rep)
 
 
 def csr_mult(mesh: Mesh, val, x, y, stream=None):
@@ -274,6 +271,99 @@ def solve_field_equation_cg(mesh: Mesh, t, params: AdvDifParams, options: Solver
     delta = np.zeros(mesh.N)
     rep = petsc_solve(mesh, delta, val, rhs, options, inactive=inactive)
     return t + params.dt * delta, rep
+
+
+def _report_dict(rep: SolveReport) -> dict:
+    return {
+        "iterations": rep.iterations, "reason": rep.reason,
+        "reason_name": _lib.REASONS.get(rep.reason, str(rep.reason)),
+        "final_rnorm": rep.final_rnorm, "rnorm0": rep.rnorm0,
+        "true_rel_residual": rep.true_rel_residual, "outer_iterations": rep.outer_iterations,
+    }
+
+
+def autotune_assembly(mesh: Mesh, params: AdvDifParams, *, t=None, velocity=None, source=None,
+                      absorption=None, val=None, rhs=None, stream=None):
+    """Pick the fastest assembly tiles for this mesh (device tensors).
+
+    Returns (val, rhs, tiles) with the assembled system and the chosen
+    (element block, element blocks per SM, row tile); later assemblies on the
+    mesh use the tiles.  Results do not depend on them.
+    """
+    import torch
+    if val is None:
+        val = torch.empty(mesh.nnz, dtype=torch.float64, device="cuda")
+    if rhs is None:
+        rhs = torch.empty(mesh.N, dtype=torch.float64, device="cuda")
+    f = Fields(_ptr(t), _ptr(velocity), _ptr(source), _ptr(absorption))
+    tiles = (C.c_int32 * 3)()
+    check(mesh.lib.fl_dev_autotune_assembly(mesh.handle, C.byref(params), C.byref(f), _ptr(val),
+                                            _ptr(rhs), _stream_ptr(stream), tiles),
+          "fl_dev_autotune_assembly")
+    return val, rhs, tuple(int(v) for v in tiles)
+
+
+def set_assembly_tiles(mesh: Mesh, elem_block: int, elem_blocks_per_sm: int, row_tile: int):
+    check(mesh.lib.fl_set_assembly_tiles(mesh.handle, elem_block, elem_blocks_per_sm, row_tile),
+          "fl_set_assembly_tiles")
+
+
+class Batch:
+    """Many solve_field_equation_cg steps run as CUDA graphs (fl_batch_*).
+
+    Each ``add`` registers one step on device tensors: assembly of ``params``
+    with the given fields, strong Dirichlet conditions on ``bc_nodes`` in
+    rate-of-change form, and a solve with ``options`` into ``x`` (the initial
+    guess unless start_from_zero).  ``run`` executes every member and returns
+    their solve reports; the tensors are read at run time, so a later ``run``
+    sees their new contents.  The batch keeps references to every tensor.
+    """
+
+    def __init__(self):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.fl_batch_create(C.byref(h)), "fl_batch_create")
+        self.handle = h.value
+        self._keep = []
+        self.members = []
+
+    def add(self, mesh: Mesh, params: AdvDifParams, options: SolverOpts, *, bc_nodes, bc_values,
+            t=None, velocity=None, source=None, absorption=None, x=None):
+        import torch
+        dev = torch.device("cuda")
+        val = torch.empty(mesh.nnz, dtype=torch.float64, device=dev)
+        rhs = torch.empty(mesh.N, dtype=torch.float64, device=dev)
+        inactive = torch.zeros(mesh.N, dtype=torch.uint8, device=dev)
+        if x is None:
+            x = torch.zeros(mesh.N, dtype=torch.float64, device=dev)
+        nodes = torch.as_tensor(bc_nodes, dtype=torch.int32, device=dev).contiguous()
+        values = torch.as_tensor(bc_values, dtype=torch.float64, device=dev).contiguous()
+        f = Fields(_ptr(t), _ptr(velocity), _ptr(source), _ptr(absorption))
+        check(self.lib.fl_batch_add(self.handle, mesh.handle, C.byref(params), C.byref(f),
+                                    int(nodes.numel()), _ptr(nodes), 0, _ptr(values),
+                                    C.byref(options), _ptr(val), _ptr(rhs), _ptr(inactive), _ptr(x)),
+              "fl_batch_add")
+        m = {"mesh": mesh, "val": val, "rhs": rhs, "inactive": inactive, "x": x}
+        self._keep.append((params, options, nodes, values, t, velocity, source, absorption))
+        self.members.append(m)
+        return m
+
+    def run(self, stream=None) -> list[dict]:
+        n = len(self.members)
+        reps = (SolveReport * max(n, 1))()
+        check(self.lib.fl_batch_run(self.handle, _stream_ptr(stream), reps), "fl_batch_run")
+        return [_report_dict(reps[i]) for i in range(n)]
+
+    def close(self):
+        if self.handle:
+            self.lib.fl_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def kernel_launch_count() -> int:

@@ -145,3 +145,24 @@ def cube_counts(n: int) -> dict:
         "N2": (2 * n + 1) ** 3,
         "nnz2": 230 * n ** 3 + 138 * n ** 2 + 24 * n + 1,
     }
+
+
+def batch_tracer_params(nfields: int = 32, seed: int = SEED_FIELDS):
+    """Per-field ``(kappa, s)`` of the batched tracers: kappa log-uniform in
+    [1e-4, 1e-1] and velocity scale s uniform in [0.5, 2], two uniforms per
+    field drawn in field order (kappa first)."""
+    u = uniform01(seed, 2 * nfields).reshape(nfields, 2)
+    kappa = 10.0 ** (-4.0 + 3.0 * u[:, 0])
+    scale = 0.5 + 1.5 * u[:, 1]
+    return kappa, scale
+
+
+#: Sides of the unevenly sized meshes solved alongside the batched tracers.
+BATCH_MESH_SIDES = (24, 32, 40, 48, 64, 72, 88, 96)
+
+
+def batch_mesh(index: int, n: int | None = None):
+    """Jittered six-tet cube number ``index`` of the uneven-mesh batch (seed
+    SEED_MESHES + index); ``n`` overrides its side for small tests."""
+    side = BATCH_MESH_SIDES[index] if n is None else n
+    return cube_mesh(side, seed=SEED_MESHES + index)

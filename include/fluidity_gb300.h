@@ -231,6 +231,44 @@ int fl_dev_petsc_solve(fl_mesh mesh, const fl_solver_opts* opts, const double* v
  * device pointers. */
 int fl_dev_csr_mult(fl_mesh mesh, const double* val, const double* x, double* y, void* stream);
 
+/* ------------------------------------------------------ tiles / batches -- */
+
+/* Assembly tile autotuner (no counterpart in the reference, whose element
+ * loop has no tiles).  Times the assembly of `params`/`fields` on the mesh
+ * under each element-pass tile (128 or 256 threads per block x 4..32 blocks
+ * per SM) and each row-pass tile (index 0..2: 64/128/256 rows per block for
+ * P1, 32/64/128 for P2), keeps the fastest on the handle for later calls and
+ * writes it to tiles[3] (may be NULL).  The tiles regroup independent work
+ * only: val and rhs are identical under every choice and hold the assembled
+ * system on return.  Device pointers, as fl_dev_assemble_advdif_cg. */
+int fl_dev_autotune_assembly(fl_mesh mesh, const fl_advdif_params* params, const fl_fields* fields,
+                             double* val, double* rhs, void* stream, int32_t* tiles);
+int fl_set_assembly_tiles(fl_mesh mesh, int32_t elem_block, int32_t elem_blocks_per_sm, int32_t row_tile);
+
+/* Batched steps (no single counterpart in the reference: they stand for many
+ * solve_field_equation_cg calls, Advection_Diffusion_CG.F90:127-174, on
+ * fields sharing one mesh or on several meshes).  A member is one step:
+ * assembly as fl_dev_assemble_advdif_cg, strong Dirichlet conditions as
+ * fl_dev_apply_dirichlet (inactive is cleared first), and an FP64 CG or
+ * GMRES(restart) + Jacobi solve as fl_dev_petsc_solve into x.  All pointers
+ * are DEVICE pointers owned by the caller and must stay valid while the batch
+ * exists.  fl_batch_run executes every member as one branch of a CUDA graph
+ * (assembly, conditions, set-up and the first iterations), then replays a
+ * second graph of further iterations until every member has converged or
+ * reached max_its, and fills reports[member] in the order of fl_batch_add.
+ * The first run (and the first after an fl_batch_add) autotunes the tiles of
+ * each mesh not tuned yet, builds the graphs and may allocate; later runs
+ * re-execute the same graphs on the arrays' current contents.  Results are
+ * identical to the unbatched entry points called member by member. */
+typedef struct fl_batch_t* fl_batch;
+int fl_batch_create(fl_batch* batch);
+int fl_batch_add(fl_batch batch, fl_mesh mesh, const fl_advdif_params* params, const fl_fields* fields,
+                 int32_t nb, const int32_t* bc_nodes, int32_t index_base, const double* bc_values,
+                 const fl_solver_opts* opts, double* val, double* rhs, uint8_t* inactive, double* x);
+int fl_batch_run(fl_batch batch, void* stream, fl_solve_report* reports);
+int fl_batch_size(fl_batch batch);
+int fl_batch_destroy(fl_batch batch);
+
 /* Number of kernels this library launched on the calling process so far
  * (launch accounting for benchmarks). */
 int64_t fl_kernel_launch_count(void);
