@@ -79,6 +79,7 @@ EXPORTS = [
     "fl_dev_apply_dirichlet", "fl_gpu_petsc_solve", "fl_dev_petsc_solve", "fl_dev_csr_mult",
     "fl_kernel_launch_count", "fl_set_kernel_timing", "fl_last_assembly_kernel_ms",
     "fl_dev_assemble_p1_diffusion_noalloc", "fl_dev_autotune_assembly", "fl_set_assembly_tiles",
+    "fl_get_assembly_tiles",
     "fl_batch_create", "fl_batch_add", "fl_batch_run", "fl_batch_size", "fl_batch_destroy",
 ]
 
@@ -115,6 +116,7 @@ _SIGNATURES = {
     "fl_dev_autotune_assembly": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(Fields), _P, _P,
                                            _P, C.POINTER(C.c_int32)]),
     "fl_set_assembly_tiles": (C.c_int, [_P, _I32, _I32, _I32]),
+    "fl_get_assembly_tiles": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "fl_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
     "fl_batch_add": (C.c_int, [_P, _P, C.POINTER(AdvDifParams), C.POINTER(Fields), _I32, _P, _I32,
                                _P, C.POINTER(SolverOpts), _P, _P, _P, _P]),

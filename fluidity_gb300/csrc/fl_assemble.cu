@@ -986,6 +986,14 @@ extern "C" int fl_set_assembly_tiles(fl_mesh m, int32_t elem_block, int32_t elem
   return FL_OK;
 }
 
+extern "C" int fl_get_assembly_tiles(fl_mesh m, int32_t* tiles) {
+  FL_CHECK_ARG(m && tiles, "null argument");
+  tiles[0] = m->tile_elem_block;
+  tiles[1] = m->tile_elem_per_sm;
+  tiles[2] = m->tile_rows;
+  return FL_OK;
+}
+
 extern "C" int fl_set_kernel_timing(fl_mesh m, int32_t on) {
   FL_CHECK_ARG(m, "null mesh");
   m->timing = on != 0;

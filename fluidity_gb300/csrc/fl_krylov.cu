@@ -53,6 +53,9 @@ struct KspState {
   int hapend;
   int live;              // the current cycle started unconverged (its correction is applied)
   int gm_first;          // next cycle is the first (device-driven restarts)
+  // fp32 CG with reliable updates
+  int rel, hold, outer;  // reliable mode; an update is pending; updates done
+  double rmax, rdelta;   // largest recurrence residual since the last update; trigger ratio
   double grs[kMaxRestart + 2];
   double cc[kMaxRestart + 1], ss[kMaxRestart + 1];
   double hh[(kMaxRestart + 1) * (kMaxRestart + 1)];   // column-major, ld = restart+1
@@ -852,7 +855,7 @@ struct SpArgs32 {
 // starts from d = 0 and stops when ||B r|| <= ttol (set by the outer loop).
 __global__ void k_cg32_p(int n, const KspState* st, const float* __restrict__ z, float* __restrict__ p) {
   note_launch();
-  if (st->done) return;
+  if (st->done || st->hold) return;
   const int i = st->cg_i;
   const float coef = (float)st->pcoef;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
@@ -865,7 +868,7 @@ __global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv,
   __shared__ double red[kThreads / 32];
   __shared__ float2 redf[kThreads / 32];
   KspState* st = A.st;
-  if (st->done) return;
+  if (st->done || st->hold) return;
   df pwd = {0.0f, 0.0f};
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
     const int sl = row / kSlice, lane = row % kSlice;
@@ -898,7 +901,7 @@ __global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, cons
                           float* __restrict__ z, double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
-  if (st->done) return;
+  if (st->done || st->hold) return;
   __shared__ float2 redf[kThreads / 32];
   const int i = st->cg_i;
   const float a = (float)st->alpha;
@@ -928,6 +931,17 @@ __global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, cons
     if (!(S.rnorm == S.rnorm)) {
       S.reason = FL_DIVERGED_NANORINF;
       S.done = 1;
+    } else if (S.rel) {
+      // reliable updates: the recurrence residual is only a trigger; the
+      // convergence test runs on the fp64 residual after the update
+      if (S.rnorm <= S.ttol || S.rnorm < S.rdelta * S.rmax || i + 1 >= S.max_its) {
+        S.hold = 1;
+      } else {
+        S.rmax = fmax(S.rmax, S.rnorm);
+        S.beta = zrs;
+        S.pcoef = S.beta / S.betaold;
+        S.cg_i = i + 1;
+      }
     } else if (S.rnorm <= S.ttol) {
       S.reason = FL_CONVERGED_RTOL;
       S.done = 1;
@@ -979,6 +993,46 @@ __global__ void k_outer_resid(SpArgs A, const double* __restrict__ b, const doub
     part[nparts + blockIdx.x] = bb;
     part[2 * nparts + blockIdx.x] = zr;
   }
+}
+
+// Reliable update, after y += d and the fp64 residual (k_outer_resid): the
+// PETSc convergence test on the true preconditioned residual, then CG goes on
+// from the same search direction with beta from the true residual.  The
+// first call opens the solve (KSPConvergedDefault at iteration 0).
+__global__ void k_rel_commit(KspState* st, const double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double zz = reduce_partials(part, nparts, red);
+  const double bb = reduce_partials(part + nparts, nparts, red);
+  const double zr = reduce_partials(part + 2 * nparts, nparts, red);
+  if (threadIdx.x != 0) return;
+  KspState& S = *st;
+  const double rn = sqrt(zz);
+  if (S.cg_i == 0 && S.outer == 0 && !S.hold) {
+    S.snorm_b = sqrt(bb);
+    S.its = 0;
+    S.reason = 0;
+    S.done = 0;
+    converged_test(S, 0, rn);
+    S.beta = zr;
+    S.rmax = rn;
+    return;
+  }
+  S.outer += 1;
+  S.hold = 0;
+  S.rnorm = rn;
+  if (rn != rn) S.reason = FL_DIVERGED_NANORINF;
+  else if (rn <= S.ttol) S.reason = rn < S.atol ? FL_CONVERGED_ATOL : FL_CONVERGED_RTOL;
+  else if (rn >= S.dtol * S.rnorm0) S.reason = FL_DIVERGED_DTOL;
+  else if (S.its >= S.max_its) S.reason = FL_DIVERGED_ITS;
+  if (S.reason) {
+    S.done = 1;
+    return;
+  }
+  S.beta = zr;
+  S.pcoef = zr / S.betaold;
+  S.cg_i = S.its;
+  S.rmax = rn;
 }
 
 __global__ void k_add_correction(int n, const float* __restrict__ d, double* __restrict__ y) {
@@ -1060,6 +1114,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   const int restart = o->restart > 0 ? o->restart : 30;
   FL_CHECK_ARG(restart <= kMaxRestart, "gmres restart above 64");
   FL_CHECK_ARG(o->precision == 0 || o->ksp_type == 0, "mixed precision is a CG refinement");
+  FL_CHECK_ARG(o->precision >= 0 && o->precision <= 2, "precision 0 (fp64), 1 or 2 (mixed)");
   KrylovWork* W = work_of(m);
   if (!W) return FL_ERR_NOMEM;
   const int n = m->N;
@@ -1089,7 +1144,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   // Jacobi diagonal and ghost pivot
   k_diag<<<gv, kThreads, 0, s>>>(A, m->centrm.p, W->dinv.p, W->part.p, W->part.p + np);
   k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + np, (int)gv);
-  const bool mixed = o->precision == 1;
+  const bool mixed = o->precision != 0;
   if (mixed) FL_TRY(W->dinv32.reserve(n));
   k_dinv<<<gv, kThreads, 0, s>>>(n, ghost, st, W->dinv.p, mixed ? W->dinv32.p : nullptr);
   FL_SPMV_DISPATCH(G, k_lift, A, rhs, x, h.guess_zero, W->b.p, W->y.p);
@@ -1186,7 +1241,54 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     const double inner_rtol = o->inner_rtol > 0 ? o->inner_rtol : 1e-5;
     double rnorm0 = 0.0, ttol = 0.0;
     int total_inner = 0, reason = 0;
-    for (outer = 0; outer < 1000; ++outer) {
+    if (o->precision == 2) {
+      // fp32 CG with reliable updates (Sleijpen and van der Vorst, 1996): the
+      // fp32 recurrence runs without restarts; whenever its residual has
+      // dropped by rdelta since the last update, or claims convergence, the
+      // correction is added to the fp64 solution, the fp64 residual replaces
+      // the recurrence residual and the convergence test runs on it.
+      hs.rel = 1;
+      hs.hold = 0;
+      hs.outer = 0;
+      hs.cg_i = 0;
+      hs.rdelta = 0.1;
+      hs.rmax = 0.0;
+      FL_TRY_CUDA(cudaMemcpyAsync(st, &hs, sizeof(KspState), cudaMemcpyHostToDevice, s));
+      auto update = [&]() {
+        FL_SPMV_DISPATCH(G, k_outer_resid, A, W->b.p, W->y.p, W->dinv.p, W->r32.p, W->z32.p, W->d32.p,
+                         W->part.p, (int)gsp);
+        k_rel_commit<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
+      };
+      update();
+      for (int i = 0; i < 1000000; i += chunk) {
+        for (int k = 0; k < chunk; ++k) {
+          k_cg32_p<<<gv, kThreads, 0, s>>>(n, st, W->z32.p, W->p32.p);
+          k_cg32_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval32.p, piv32, W->p32.p, W->w32.p, W->part.p,
+                                              W->ticket.p);
+          k_cg32_xr<<<gv, kThreads, 0, s>>>(n, st, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
+                                             W->z32.p, W->part.p + 2 * np, W->ticket.p + 1);
+        }
+        FL_TRY_CUDA(cudaGetLastError());
+        KspState h2;
+        FL_TRY_CUDA(cudaMemcpyAsync(&h2.its, &st->its, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+        FL_TRY_CUDA(cudaMemcpyAsync(&h2.hold, &st->hold, sizeof(int), cudaMemcpyDeviceToHost, s));
+        FL_TRY_CUDA(cudaStreamSynchronize(s));
+        if (h2.done) break;
+        if (h2.hold) {
+          k_add_correction<<<gv, kThreads, 0, s>>>(n, W->d32.p, W->y.p);
+          update();
+          FL_TRY_CUDA(cudaGetLastError());
+        }
+      }
+      // a solve stopped inside the fp32 recurrence keeps its last correction
+      k_add_correction<<<gv, kThreads, 0, s>>>(n, W->d32.p, W->y.p);
+      FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+      FL_TRY_CUDA(cudaStreamSynchronize(s));
+      hs.rel = 0;
+      FL_TRY_CUDA(cudaMemcpyAsync(&st->rel, &hs.rel, sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    const int rel_updates = hs.outer;
+    for (outer = 0; o->precision == 1 && outer < 1000; ++outer) {
       FL_SPMV_DISPATCH(G, k_outer_resid, A, W->b.p, W->y.p, W->dinv.p, W->r32.p, W->z32.p, W->d32.p, W->part.p,
                        (int)gsp);
       k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
@@ -1230,13 +1332,16 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
       k_add_correction<<<gv, kThreads, 0, s>>>(n, W->d32.p, W->y.p);
       FL_TRY_CUDA(cudaGetLastError());
     }
-    // report in the outer terms
-    hs.its = total_inner;
-    hs.reason = reason;
-    hs.rnorm0 = rnorm0;
-    FL_TRY_CUDA(cudaMemcpyAsync(&st->its, &hs.its, sizeof(int), cudaMemcpyHostToDevice, s));
-    FL_TRY_CUDA(cudaMemcpyAsync(&st->reason, &hs.reason, sizeof(int), cudaMemcpyHostToDevice, s));
-    FL_TRY_CUDA(cudaMemcpyAsync(&st->rnorm0, &hs.rnorm0, sizeof(double), cudaMemcpyHostToDevice, s));
+    if (o->precision == 2) outer = rel_updates;
+    if (o->precision == 1) {
+      // report in the outer terms
+      hs.its = total_inner;
+      hs.reason = reason;
+      hs.rnorm0 = rnorm0;
+      FL_TRY_CUDA(cudaMemcpyAsync(&st->its, &hs.its, sizeof(int), cudaMemcpyHostToDevice, s));
+      FL_TRY_CUDA(cudaMemcpyAsync(&st->reason, &hs.reason, sizeof(int), cudaMemcpyHostToDevice, s));
+      FL_TRY_CUDA(cudaMemcpyAsync(&st->rnorm0, &hs.rnorm0, sizeof(double), cudaMemcpyHostToDevice, s));
+    }
   }
   FL_SPMV_DISPATCH(G, k_true_resid, A, W->b.p, W->y.p, W->part.p, (int)gsp);
   k_true_resid_final<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);

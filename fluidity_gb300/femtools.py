@@ -106,6 +106,12 @@ class Mesh:
         except Exception:
             pass
 
+    def tiles(self) -> tuple:
+        """Assembly tiles in use: (element block, element blocks per SM, row tile)."""
+        t = (C.c_int32 * 3)()
+        check(self.lib.fl_get_assembly_tiles(self.handle, t), "fl_get_assembly_tiles")
+        return tuple(int(v) for v in t)
+
     def sparsity(self) -> CsrSparsity:
         if self._sparsity is None:
             f = np.empty(self.N + 1, dtype=np.int32)
@@ -228,7 +234,7 @@ def solver_options(*, ksp="cg", restart=30, rtol=1e-10, atol=0.0, dtol=1e5, max_
     o.ksp_type = {"cg": 0, "gmres": 1}[ksp]
     o.restart, o.rtol, o.atol, o.dtol = restart, rtol, atol, dtol
     o.max_its, o.start_from_zero = max_its, int(start_from_zero)
-    o.precision = {"fp64": 0, "mixed": 1}[precision]
+    o.precision = {"fp64": 0, "mixed": 1, "reliable": 2}[precision]
     o.inner_rtol = inner_rtol
     return o
 

@@ -197,8 +197,14 @@ typedef struct {
   double dtol;               /* divergence tolerance (PETSc default 1e5)    */
   int32_t max_its;           /* max_iterations                              */
   int32_t start_from_zero;   /* start_from_zero                             */
-  int32_t precision;         /* 0 = fp64; 1 = fp32 inner iterations inside
-                                fp64 iterative refinement                   */
+  int32_t precision;         /* 0 = fp64; 1 = fp32 inner CG solves inside
+                                fp64 iterative refinement (restarted);
+                                2 = fp32 CG with reliable updates: fp64
+                                refinement of the solution and residual
+                                whenever the fp32 residual has dropped
+                                tenfold, without restarting the fp32
+                                Krylov space; the convergence test runs on
+                                the fp64 residual (CG only)                  */
   double inner_rtol;         /* inner relative tolerance (precision = 1)    */
 } fl_solver_opts;
 
@@ -208,7 +214,7 @@ typedef struct {
   double final_rnorm;        /* last preconditioned residual norm           */
   double rnorm0;             /* norm the relative tolerance scales          */
   double true_rel_residual;  /* ||b - A x|| / ||b|| recomputed in fp64      */
-  int32_t outer_iterations;  /* refinement steps (precision = 1)            */
+  int32_t outer_iterations;  /* refinement steps (precision = 1 or 2)       */
   int32_t pad;
 } fl_solve_report;
 
@@ -244,6 +250,7 @@ int fl_dev_csr_mult(fl_mesh mesh, const double* val, const double* x, double* y,
 int fl_dev_autotune_assembly(fl_mesh mesh, const fl_advdif_params* params, const fl_fields* fields,
                              double* val, double* rhs, void* stream, int32_t* tiles);
 int fl_set_assembly_tiles(fl_mesh mesh, int32_t elem_block, int32_t elem_blocks_per_sm, int32_t row_tile);
+int fl_get_assembly_tiles(fl_mesh mesh, int32_t* tiles);
 
 /* Batched steps (no single counterpart in the reference: they stand for many
  * solve_field_equation_cg calls, Advection_Diffusion_CG.F90:127-174, on

@@ -109,18 +109,42 @@ def test_failure_reasons(O):
     assert rep["reason"] == -3 and rep["iterations"] == 3
 
 
+@pytest.mark.parametrize("precision", ["mixed", "reliable"])
 @pytest.mark.parametrize("kappa", [1.0, np.diag([1.0, 1.0, 1e-3])])
-def test_mixed_precision_reaches_fp64_tolerance(O, kappa):
+def test_mixed_precision_reaches_fp64_tolerance(O, kappa, precision):
     m, X, val, rhs, ina = poisson(O, 16, kappa=kappa)
     x64 = np.zeros(m.N)
     r64 = ft.petsc_solve(m, x64, val, rhs, ft.solver_options(rtol=1e-10), inactive=ina)
     xm = np.zeros(m.N)
-    rm = ft.petsc_solve(m, xm, val, rhs, ft.solver_options(rtol=1e-10, precision="mixed"),
+    rm = ft.petsc_solve(m, xm, val, rhs, ft.solver_options(rtol=1e-10, precision=precision),
                         inactive=ina)
     assert r64["reason"] == 2 and rm["reason"] == 2
     assert rm["outer_iterations"] >= 2
+    # the convergence test ran on the fp64 residual, against the fp64 solve's scale
+    assert rm["rnorm0"] == pytest.approx(r64["rnorm0"], rel=1e-12)
     assert rm["final_rnorm"] <= 1e-10 * r64["rnorm0"] * (1 + 1e-12)
+    assert rm["true_rel_residual"] <= 2 * r64["true_rel_residual"] + 1e-11
     assert np.abs(xm - x64).max() <= 1e-7 * np.abs(x64).max()
+    if precision == "reliable":
+        # no restarts of the Krylov space: close to the fp64 iteration count
+        assert rm["iterations"] <= 1.25 * r64["iterations"] + 5
+
+
+def test_reliable_updates_from_a_guess_and_iteration_limit(O):
+    m, X, val, rhs, ina = poisson(O, 12)
+    xd = direct(m, val, rhs, ina)
+    x = xd * (1 + 1e-3 * np.sin(7 * X[:, 0]))
+    r = ft.petsc_solve(m, x, val, rhs, ft.solver_options(rtol=1e-10, precision="reliable"),
+                       inactive=ina)
+    x0 = np.zeros(m.N)
+    r0 = ft.petsc_solve(m, x0, val, rhs, ft.solver_options(rtol=1e-10, precision="reliable"),
+                        inactive=ina)
+    assert r["reason"] == r0["reason"] == 2 and r["iterations"] < r0["iterations"]
+    assert np.abs(x - xd).max() <= 1e-7 * np.abs(xd).max()
+    xl = np.zeros(m.N)
+    rl = ft.petsc_solve(m, xl, val, rhs, ft.solver_options(rtol=1e-14, max_its=9,
+                                                           precision="reliable"), inactive=ina)
+    assert rl["reason"] == -3 and rl["iterations"] == 9
 
 
 def test_device_resident_solve(O):
