@@ -81,6 +81,8 @@ EXPORTS = [
     "fl_dev_assemble_p1_diffusion_noalloc", "fl_dev_autotune_assembly", "fl_set_assembly_tiles",
     "fl_get_assembly_tiles",
     "fl_batch_create", "fl_batch_add", "fl_batch_run", "fl_batch_size", "fl_batch_destroy",
+    "fl_gnn_num_params", "fl_gnn_create", "fl_gnn_destroy", "fl_gnn_set_weights",
+    "fl_gnn_get_weights", "fl_gnn_predict", "fl_gnn_gradients", "fl_gnn_train_step",
 ]
 
 _P = C.c_void_p
@@ -123,6 +125,14 @@ _SIGNATURES = {
     "fl_batch_run": (C.c_int, [_P, _P, C.POINTER(SolveReport)]),
     "fl_batch_size": (C.c_int, [_P]),
     "fl_batch_destroy": (C.c_int, [_P]),
+    "fl_gnn_num_params": (C.c_int, []),
+    "fl_gnn_create": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "fl_gnn_destroy": (C.c_int, [_P]),
+    "fl_gnn_set_weights": (C.c_int, [_P, _P, _I32]),
+    "fl_gnn_get_weights": (C.c_int, [_P, _P, _I32]),
+    "fl_gnn_predict": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+    "fl_gnn_gradients": (C.c_int, [_P, _P, _P, _P, _P, _P, _I32, _P, C.POINTER(C.c_float), _P]),
+    "fl_gnn_train_step": (C.c_int, [_P, _P, _P, _P, _P, _P, _I32, C.c_float, _P, _P]),
 }
 assert sorted(_SIGNATURES) == sorted(EXPORTS)
 

@@ -49,7 +49,8 @@ struct fl_batch_t {
   fl::DevBuf<fl::KspState*> states;     // device array of member states
   fl::DevBuf<int> done;                 // gathered convergence flags
   int* h_done = nullptr;                // pinned host copy
-  cudaEvent_t fork = nullptr;
+  cudaStream_t s0 = nullptr;            // the batch's own stream (graphs are captured on it)
+  cudaEvent_t fork = nullptr, join = nullptr;
   bool built = false;
 };
 
@@ -65,9 +66,13 @@ static void destroy_graphs(fl_batch_t* b) {
 extern "C" int fl_batch_create(fl_batch* out) {
   FL_CHECK_ARG(out, "null handle");
   fl_batch_t* b = new fl_batch_t();
-  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->s0, cudaStreamNonBlocking) != cudaSuccess) {
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
     delete b;
-    set_error("cudaEventCreate failed");
+    set_error("stream/event creation failed");
     return FL_ERR_CUDA;
   }
   *out = b;
@@ -86,6 +91,8 @@ extern "C" int fl_batch_destroy(fl_batch b) {
   }
   if (b->h_done) cudaFreeHost(b->h_done);
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->s0) cudaStreamDestroy(b->s0);
   delete b;
   return FL_OK;
 }
@@ -204,11 +211,13 @@ static int build(fl_batch_t* b, cudaStream_t s0) {
 
 extern "C" int fl_batch_run(fl_batch b, void* stream, fl_solve_report* reports) {
   FL_CHECK_ARG(b && reports, "null argument");
-  cudaStream_t s0 = (cudaStream_t)stream;
-  bool own = false;
-  if (!s0) {
-    FL_TRY_CUDA(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
-    own = true;
+  // the batch runs on its own stream (which can be captured), after the
+  // caller's stream has reached this call and before it continues
+  cudaStream_t caller = (cudaStream_t)stream;
+  cudaStream_t s0 = b->s0;
+  if (caller) {
+    FL_TRY_CUDA(cudaEventRecord(b->join, caller));
+    FL_TRY_CUDA(cudaStreamWaitEvent(s0, b->join, 0));
   }
   int st = FL_OK;
   do {
@@ -241,10 +250,7 @@ extern "C" int fl_batch_run(fl_batch b, void* stream, fl_solve_report* reports) 
       if ((st = check_err(m->m->err.p, s0, "batched assembly")) != FL_OK) break;
   } while (0);
   if (st == FL_ERR_CUDA && fl_last_error()[0] == 0) set_error("%s", cudaGetErrorString(cudaGetLastError()));
-  if (own) {
-    cudaStreamSynchronize(s0);
-    cudaStreamDestroy(s0);
-  }
+  if (caller && cudaEventRecord(b->join, s0) == cudaSuccess) cudaStreamWaitEvent(caller, b->join, 0);
   return st;
 }
 

@@ -149,6 +149,7 @@ int autotune_assembly(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl
 unsigned long long launches_mesh();
 unsigned long long launches_assemble();
 unsigned long long launches_krylov();
+unsigned long long launches_gnn();
 void release_krylov_work(struct ::fl_mesh_t* m);
 
 }  // namespace fl

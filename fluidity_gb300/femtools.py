@@ -49,11 +49,14 @@ def _is_device(a) -> bool:
 
 def _stream_ptr(stream):
     """CUDA stream handle for device-path calls: the given stream, or torch's
-    current stream so the library's work is ordered with the caller's tensors."""
+    current stream so the library's work is ordered with the caller's tensors.
+    Torch's default stream is the legacy default stream (handle 0), which the
+    C-ABI reads as "the mesh's own stream": it is passed as cudaStreamLegacy."""
     if stream is None:
         import torch
         stream = torch.cuda.current_stream()
-    return getattr(stream, "cuda_stream", stream)
+    h = getattr(stream, "cuda_stream", stream)
+    return h if h else 1  # cudaStreamLegacy
 
 
 @dataclass

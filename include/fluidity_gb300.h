@@ -19,7 +19,8 @@
  * Conventions: plain pointers and sizes; no CUDA or torch types in the
  * signatures (streams are passed as void*).  Functions named fl_gpu_* take
  * HOST pointers and copy in/out; functions named fl_dev_* take DEVICE pointers
- * and run on the given stream (NULL = the mesh handle's stream).  Every
+ * and run on the given stream (NULL = the mesh handle's stream; the legacy
+ * default stream is passed as cudaStreamLegacy).  Every
  * function returns an fl_status; fl_last_error() describes the last failure
  * of the calling thread.  Indices follow `index_base` (1 = Fortran, 0 = C).
  */
@@ -275,6 +276,40 @@ int fl_batch_add(fl_batch batch, fl_mesh mesh, const fl_advdif_params* params, c
 int fl_batch_run(fl_batch batch, void* stream, fl_solve_report* reports);
 int fl_batch_size(fl_batch batch);
 int fl_batch_destroy(fl_batch batch);
+
+/* ------------------------------------------------- learned warm start -- */
+
+/* Message-passing network that predicts the next pressure of a sequence of
+ * Poisson solves, used as the initial guess of fl_dev_petsc_solve (no
+ * counterpart in the reference).  Node features: previous two pressures p1,
+ * p2, the right-hand side b and the coordinates; three message-passing layers
+ * of width 64 over the mesh's sparsity graph; BF16 weights and activations
+ * with FP32 accumulation on the tensor cores; prediction
+ * 2 p1 - p2 + max|p1| * output.  Parameters are one flat FP32 vector of
+ * fl_gnn_num_params() entries:
+ *   We[64][16] be[64] | 3 x (Wl[64][128] bl[64]) | wd[64] bd[1]
+ * (Wl columns 0..63 act on the node's own state, 64..127 on the mean of its
+ * neighbours').  All field pointers are DEVICE pointers of N doubles on a P1
+ * mesh.  mask (N bytes, 1 = node counts in the loss; NULL = all) and nact
+ * (its number of ones) select the nodes of the loss: the mean squared error
+ * of the prediction normalised by max|p1|.  fl_gnn_gradients returns that
+ * loss and its gradient (host arrays); fl_gnn_train_step applies one Adam
+ * step (beta 0.9, 0.999) with learning rate lr and, if loss_dev is not NULL,
+ * writes the step's sum of squared errors to that device float. */
+typedef struct fl_gnn_t* fl_gnn;
+int fl_gnn_num_params(void);
+int fl_gnn_create(fl_mesh mesh, fl_gnn* net);
+int fl_gnn_destroy(fl_gnn net);
+int fl_gnn_set_weights(fl_gnn net, const float* weights, int32_t count);
+int fl_gnn_get_weights(fl_gnn net, float* weights, int32_t count);
+int fl_gnn_predict(fl_gnn net, const double* p1, const double* p2, const double* b, double* pred,
+                   void* stream);
+int fl_gnn_gradients(fl_gnn net, const double* p1, const double* p2, const double* b,
+                     const double* target, const uint8_t* mask, int32_t nact, float* grad,
+                     float* loss, void* stream);
+int fl_gnn_train_step(fl_gnn net, const double* p1, const double* p2, const double* b,
+                      const double* target, const uint8_t* mask, int32_t nact, float lr,
+                      float* loss_dev, void* stream);
 
 /* Number of kernels this library launched on the calling process so far
  * (launch accounting for benchmarks). */
