@@ -314,6 +314,99 @@ def bench_batch(args, dev, stream):
     return out
 
 
+def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
+    """Learned warm start on the rotating-source Poisson sequence: generate the
+    plain solves, train the network on steps 2..ntrain-1 on the GPU, then time
+    the held-out steps' solves to rtol 1e-10 from the zero, previous-step and
+    learned guesses (FP64 CG and reliable-update mixed CG), each timed from the
+    guess construction (the network's prediction included) to the solution."""
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+    from fluidity_gb300 import meshgen as M
+    from fluidity_gb300 import warmstart as WS
+
+    nd, X = M.cube_mesh(n)
+    m = ft.Mesh(nd, X)
+    seq = WS.PoissonSequence(m, X, M.boundary_nodes(X), stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ps, bs = WS.pressure_sequence(seq, nsteps)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    net = WS.PressureGuessNet(m)
+    t0 = time.perf_counter()
+    kval = seq.val if getattr(args, "energy_loss", True) else None
+    losses = WS.train(net, ps, bs, seq.mask, seq.nact, range(2, ntrain), epochs=epochs, stream=stream,
+                      kval=kval)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    ntrain_steps = epochs * (ntrain - 2)
+    # network forward time alone
+    out = torch.empty_like(ps[0])
+    for _ in range(3):
+        net.predict(ps[ntrain - 1], ps[ntrain - 2], bs[ntrain], out=out, stream=stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(20):
+        net.predict(ps[ntrain - 1], ps[ntrain - 2], bs[ntrain], out=out, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    predict_ms = e0.elapsed_time(e1) / 20
+
+    variants = {
+        "fp64_zero": ("fp64", "zero"), "fp64_previous": ("fp64", "previous"),
+        "fp64_learned": ("fp64", "learned"), "mixed_previous": ("reliable", "previous"),
+        "mixed_learned": ("reliable", "learned"), "mixed_zero": ("reliable", "zero"),
+    }
+    res = {k: {"ms": [], "iterations": [], "err": [], "true_rel_residual": []} for k in variants}
+    tight = ft.solver_options(ksp="cg", rtol=1e-13, max_its=50000)
+    x = torch.empty_like(ps[0])
+    for t in range(ntrain, nsteps):
+        val, rhs, ina = seq.system(t)
+        ref = ps[t].clone()
+        ft.petsc_solve(m, ref, val, rhs, tight, inactive=ina, stream=stream)
+        scale = ref.abs().max()
+        for k, (prec, guess) in variants.items():
+            opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000, precision=prec)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            if guess == "zero":
+                x.zero_()
+            elif guess == "previous":
+                x.copy_(ps[t - 1])
+            else:
+                net.predict(ps[t - 1], ps[t - 2], bs[t], out=x, stream=stream)
+            rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            r = res[k]
+            r["ms"].append(e0.elapsed_time(e1))
+            r["iterations"].append(rep["iterations"])
+            r["true_rel_residual"].append(rep["true_rel_residual"])
+            r["err"].append(float((x - ref).abs().max() / scale))
+            assert rep["reason"] > 0, (k, t, rep)
+    summary = {}
+    for k, r in res.items():
+        summary[k] = {"mean_ms": float(np.mean(r["ms"])), "mean_iterations": float(np.mean(r["iterations"])),
+                      "max_err_vs_fp64_tight": float(np.max(r["err"])),
+                      "max_true_rel_residual": float(np.max(r["true_rel_residual"]))}
+    base = summary["fp64_zero"]["mean_ms"]
+    return {
+        "workload": f"{nsteps}-step rotating-source Poisson sequence on the {n}^3 P1 mesh; "
+                    f"train on steps 2..{ntrain - 1}, CG to rtol 1e-10 on the {nsteps - ntrain} held-out steps",
+        "nodes": m.N, "epochs": epochs, "train_steps": ntrain_steps, "train_s": train_s,
+        "train_ms_per_step": train_s / ntrain_steps * 1e3, "loss_first_epoch": float(losses[0]),
+        "loss_last_epoch": float(losses[-1]), "generate_s": gen_s, "predict_ms": predict_ms,
+        "variants": summary,
+        "speedup_mixed_learned_vs_fp64_zero": base / summary["mixed_learned"]["mean_ms"],
+        "speedup_mixed_learned_vs_fp64_previous": summary["fp64_previous"]["mean_ms"]
+        / summary["mixed_learned"]["mean_ms"],
+        "speedup_fp64_learned_vs_fp64_previous": summary["fp64_previous"]["mean_ms"]
+        / summary["fp64_learned"]["mean_ms"],
+    }
+
+
 def run_ours(args, rank, ws, dist):
     import torch
 
@@ -434,6 +527,10 @@ def run_ours(args, rank, ws, dist):
     batch = None
     if not args.no_batch:
         batch = bench_batch(args, dev, stream)
+    learned = None
+    if not args.no_learned:
+        learned = {f"n{k}": bench_learned(args, dev, stream, k, epochs=e)
+                   for k, e in ((64, args.epochs), (args.n, max(4, args.epochs // 3)))}
 
     if rank != 0:
         return
@@ -468,6 +565,7 @@ def run_ours(args, rank, ws, dist):
         "clocks": clk.summary(),
         "solve": solve,
         "batch": batch,
+        "learned": learned,
     }
     print(json.dumps(line), flush=True)
 
@@ -482,6 +580,8 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--batch-fields", type=int, default=32)
     args = ap.parse_args()
     rank, ws, dist = dist_setup(args)

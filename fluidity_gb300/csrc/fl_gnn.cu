@@ -142,7 +142,7 @@ __global__ void k_gnn_inv_deg(int n, const int32_t* __restrict__ findrm, float* 
   }
 }
 
-// h0 = relu(We f + be); Z0 = We f + be (bf16)
+// h0 = relu(We f + be); Z0 = We f + be (bf16, stored when Z is not null)
 __global__ void __launch_bounds__(kTh) k_gnn_encode(Inputs in, const bf16* __restrict__ We,
                                                     const float* __restrict__ be, bf16* __restrict__ Z,
                                                     bf16* __restrict__ H) {
@@ -173,54 +173,25 @@ __global__ void __launch_bounds__(kTh) k_gnn_encode(Inputs in, const bf16* __res
         const int row = base + w * 16 + g + 8 * h, c = nt * 8 + t * 2;
         if (row >= in.n) continue;
         const float z0 = acc[nt][2 * h] + be[c], z1 = acc[nt][2 * h + 1] + be[c + 1];
-        *reinterpret_cast<__nv_bfloat162*>(Z + (int64_t)row * kW + c) = __floats2bfloat162_rn(z0, z1);
+        if (Z) *reinterpret_cast<__nv_bfloat162*>(Z + (int64_t)row * kW + c) = __floats2bfloat162_rn(z0, z1);
         *reinterpret_cast<__nv_bfloat162*>(H + (int64_t)row * kW + c) =
             __floats2bfloat162_rn(fmaxf(z0, 0.0f), fmaxf(z1, 0.0f));
       }
   }
 }
 
-// a_i = inv_deg_i * sum_{j in row i, j != i} h_j  (one warp per node)
-__global__ void k_gnn_aggregate(int n, const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
-                                const float* __restrict__ inv_deg, const bf16* __restrict__ H,
-                                bf16* __restrict__ A) {
-  note_launch();
-  const int lane = threadIdx.x & 31;
-  const int nw = gridDim.x * (blockDim.x >> 5);
-  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nw) {
-    float2 s = {0.0f, 0.0f};
-    const int e = findrm[i + 1];
-    for (int k = findrm[i]; k < e; ++k) {
-      const int j = colm[k];
-      if (j == i) continue;
-      const float2 h = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(H + (int64_t)j * kW)[lane]);
-      s.x += h.x;
-      s.y += h.y;
-    }
-    const float d = inv_deg[i];
-    reinterpret_cast<__nv_bfloat162*>(A + (int64_t)i * kW)[lane] = __floats2bfloat162_rn(s.x * d, s.y * d);
-  }
-}
-
-// Copy a 64-node tile of [H | A] (bf16, 64 + 64 columns) into shared memory.
-__device__ __forceinline__ void load_x_tile(const bf16* H, const bf16* A, int n, int base, bf16* Xs) {
-  for (int k = threadIdx.x; k < kTM * 16; k += kTh) {
-    const int r = k >> 4, q = k & 15;  // 16 chunks of 8 bf16 per row
-    const int i = base + r;
-    uint4 v = {0u, 0u, 0u, 0u};
-    if (i < n) {
-      const bf16* src = q < 8 ? H + (int64_t)i * kW + q * 8 : A + (int64_t)i * kW + (q - 8) * 8;
-      v = *reinterpret_cast<const uint4*>(src);
-    }
-    *reinterpret_cast<uint4*>(Xs + r * kLd128 + q * 8) = v;
-  }
-}
-
-// z = Wl [h ; a] + bl;  Z = bf16(z);  h' = h + relu(z)
-__global__ void __launch_bounds__(kTh) k_gnn_layer_fwd(int n, const bf16* __restrict__ Hin,
-                                                       const bf16* __restrict__ A, const bf16* __restrict__ Wl,
-                                                       const float* __restrict__ bl, bf16* __restrict__ Z,
-                                                       bf16* __restrict__ Hout) {
+// One message-passing layer on a tile of 64 nodes: the tile's own states h
+// and the means a of their neighbours' states (gathered by the four warps,
+// one node at a time, FP32 sums of the bf16 rows in pattern order) are
+// staged in shared memory as [h | a], then on the tensor cores
+// z = Wl [h ; a] + bl and h' = h + relu(z).  A and Z (the values the
+// backward pass needs) are stored only when their pointers are not null.
+__global__ void __launch_bounds__(kTh) k_gnn_layer_fwd(int n, const int32_t* __restrict__ findrm,
+                                                       const int32_t* __restrict__ colm,
+                                                       const float* __restrict__ inv_deg,
+                                                       const bf16* __restrict__ Hin, const bf16* __restrict__ Wl,
+                                                       const float* __restrict__ bl, bf16* __restrict__ A,
+                                                       bf16* __restrict__ Z, bf16* __restrict__ Hout) {
   note_launch();
   __shared__ __align__(16) bf16 Xs[kTM * kLd128];
   __shared__ __align__(16) bf16 Ws[kW * kLd128];
@@ -233,7 +204,45 @@ __global__ void __launch_bounds__(kTh) k_gnn_layer_fwd(int n, const bf16* __rest
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int base = tile * kTM;
     __syncthreads();
-    load_x_tile(Hin, A, n, base, Xs);
+    for (int k = threadIdx.x; k < kTM * 8; k += kTh) {
+      const int r = k >> 3, q = k & 7, i = base + r;
+      uint4 v = {0u, 0u, 0u, 0u};
+      if (i < n) v = *reinterpret_cast<const uint4*>(Hin + (int64_t)i * kW + q * 8);
+      *reinterpret_cast<uint4*>(Xs + r * kLd128 + q * 8) = v;
+    }
+    {
+      // four nodes per warp at a time, eight lanes per node, eight features
+      // (one 16-byte load) per lane
+      const int sub = lane >> 3, q = lane & 7;
+      for (int r = w * 4 + sub; r < kTM; r += kTh / 8) {
+        const int i = base + r;
+        float s[8] = {};
+        if (i < n) {
+          const int e = findrm[i + 1];
+          for (int k = findrm[i]; k < e; ++k) {
+            const int j = colm[k];
+            if (j == i) continue;
+            const uint4 v = *reinterpret_cast<const uint4*>(Hin + (int64_t)j * kW + q * 8);
+            const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float2 h = __bfloat1622float2(h2[u]);
+              s[2 * u] += h.x;
+              s[2 * u + 1] += h.y;
+            }
+          }
+          const float d = inv_deg[i];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) s[u] *= d;
+        }
+        uint4 out;
+        __nv_bfloat162* o2 = reinterpret_cast<__nv_bfloat162*>(&out);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) o2[u] = __floats2bfloat162_rn(s[2 * u], s[2 * u + 1]);
+        *reinterpret_cast<uint4*>(Xs + r * kLd128 + kW + q * 8) = out;
+        if (A && i < n) *reinterpret_cast<uint4*>(A + (int64_t)i * kW + q * 8) = out;
+      }
+    }
     __syncthreads();
     float acc[8][4] = {};
     warp_gemm<2 * kW, 8, kLd128, kLd128>(Xs + w * 16 * kLd128, Ws, acc);
@@ -245,7 +254,7 @@ __global__ void __launch_bounds__(kTh) k_gnn_layer_fwd(int n, const bf16* __rest
         if (row >= n) continue;
         const float z0 = acc[nt][2 * h] + bl[c], z1 = acc[nt][2 * h + 1] + bl[c + 1];
         const float2 hin = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(Xs + r * kLd128 + c));
-        *reinterpret_cast<__nv_bfloat162*>(Z + (int64_t)row * kW + c) = __floats2bfloat162_rn(z0, z1);
+        if (Z) *reinterpret_cast<__nv_bfloat162*>(Z + (int64_t)row * kW + c) = __floats2bfloat162_rn(z0, z1);
         *reinterpret_cast<__nv_bfloat162*>(Hout + (int64_t)row * kW + c) =
             __floats2bfloat162_rn(hin.x + fmaxf(z0, 0.0f), hin.y + fmaxf(z1, 0.0f));
       }
@@ -263,9 +272,14 @@ struct DecodeArgs {
   float inv_nact;       // 1 / number of active nodes
   float* dH;            // [n][64] gradient w.r.t. h3 (training)
   float* part;          // [gridDim][66]: dwd, dbd, loss
+  int energy;           // loss in the energy norm of the matrix
+  double* e;            // energy loss: normalised error (first pass writes it)
+  const double* Ke;     // energy loss: K e (second pass reads it)
 };
 
 // o = wd . h3 + bd; prediction; training: e, dL/do, dh3, decoder partials.
+// Loss in the energy norm (e^T K e over the active nodes) takes two passes:
+// the first writes e (Ke is null), the second, after K e, the gradients.
 __global__ void __launch_bounds__(kTh) k_gnn_decode(DecodeArgs D) {
   note_launch();
   __shared__ float red[kTh / 32][kW + 2];
@@ -286,16 +300,26 @@ __global__ void __launch_bounds__(kTh) k_gnn_decode(DecodeArgs D) {
     if (D.pred && lane == 0) D.pred[i] = ext + s * (double)o;
     if (D.target) {
       const bool act = !D.mask || D.mask[i];
-      const float e = act ? (float)((ext - D.target[i]) / s) + o : 0.0f;
-      const float go = 2.0f * e * D.inv_nact;
-      loss += lane == 0 ? e * e : 0.0f;
+      float go;
+      if (D.energy && !D.Ke) {
+        if (lane == 0) D.e[i] = act ? (ext - D.target[i]) / s + (double)o : 0.0;
+        continue;
+      } else if (D.energy) {
+        const double ke = act ? D.Ke[i] : 0.0;
+        go = (float)(2.0 * ke) * D.inv_nact;
+        loss += lane == 0 ? (float)(D.e[i] * ke) : 0.0f;
+      } else {
+        const float e = act ? (float)((ext - D.target[i]) / s) + o : 0.0f;
+        go = 2.0f * e * D.inv_nact;
+        loss += lane == 0 ? e * e : 0.0f;
+      }
       gb += lane == 0 ? go : 0.0f;
       gw.x += go * h.x;
       gw.y += go * h.y;
       reinterpret_cast<float2*>(D.dH + (int64_t)i * kW)[lane] = make_float2(go * wd.x, go * wd.y);
     }
   }
-  if (!D.target) return;
+  if (!D.target || (D.energy && !D.Ke)) return;
   red[w][2 * lane] = gw.x;
   red[w][2 * lane + 1] = gw.y;
   if (lane == 0) {
@@ -522,6 +546,8 @@ struct fl_gnn_t {
   DevBuf<bf16> wb, H, Z, A;  // H, Z: 4 x n x 64; A: 3 x n x 64
   int steps = 0;
   float nact_inv = 0.0f;
+  const double* kval = nullptr;  // matrix of the energy-norm loss (null: squared error)
+  DevBuf<double> e, Ke;
 };
 
 namespace {
@@ -547,17 +573,26 @@ int forward(fl_gnn_t* G, const double* p1, const double* p2, const double* b, do
   FL_TRY_CUDA(cudaMemsetAsync(G->scal.p, 0, sizeof(float) * 4, s));
   k_gnn_scales<<<grid_for(n, 256, 4), 256, 0, s>>>(n, p1, b, G->scal.p);
   Inputs in{n, p1, p2, b, m->coords.p, G->scal.p};
-  k_gnn_encode<<<tile_grid(n), kTh, 0, s>>>(in, G->wb.p + kOffWe, G->w.p + kOffBe, Zbuf(G, 0), Hbuf(G, 0));
+  const bool train = target != nullptr;
+  k_gnn_encode<<<tile_grid(n), kTh, 0, s>>>(in, G->wb.p + kOffWe, G->w.p + kOffBe, train ? Zbuf(G, 0) : nullptr,
+                                            Hbuf(G, 0));
   for (int l = 1; l <= kLayers; ++l) {
     const int off = kOffL + (l - 1) * kLayerSize;
-    k_gnn_aggregate<<<warp_grid(n), 256, 0, s>>>(n, m->findrm.p, m->colm.p, G->inv_deg.p, Hbuf(G, l - 1),
-                                                  Abuf(G, l - 1));
-    k_gnn_layer_fwd<<<tile_grid(n), kTh, 0, s>>>(n, Hbuf(G, l - 1), Abuf(G, l - 1), G->wb.p + off,
-                                                  G->w.p + off + 2 * kW * kW, Zbuf(G, l), Hbuf(G, l));
+    k_gnn_layer_fwd<<<tile_grid(n), kTh, 0, s>>>(n, m->findrm.p, m->colm.p, G->inv_deg.p, Hbuf(G, l - 1),
+                                                  G->wb.p + off, G->w.p + off + 2 * kW * kW,
+                                                  train ? Abuf(G, l - 1) : nullptr, train ? Zbuf(G, l) : nullptr,
+                                                  Hbuf(G, l));
   }
+  const bool energy = train && G->kval;
   DecodeArgs D{in, Hbuf(G, kLayers), G->wb.p + kOffWd, G->w.p + kOffBd, pred, target, mask, G->nact_inv,
-               G->dH.p, G->part.p};
+               G->dH.p, G->part.p, energy ? 1 : 0, G->e.p, nullptr};
   k_gnn_decode<<<persist_grid(n), kTh, 0, s>>>(D);
+  if (energy) {
+    FL_TRY(csr_mult(m, G->kval, G->e.p, G->Ke.p, s));
+    D.pred = nullptr;
+    D.Ke = G->Ke.p;
+    k_gnn_decode<<<persist_grid(n), kTh, 0, s>>>(D);
+  }
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
@@ -641,6 +676,16 @@ extern "C" int fl_gnn_destroy(fl_gnn G) {
     cudaDeviceSynchronize();
     delete G;
   }
+  return FL_OK;
+}
+
+extern "C" int fl_gnn_set_loss(fl_gnn G, const double* val) {
+  FL_CHECK_ARG(G, "null network");
+  if (val) {
+    FL_TRY(G->e.reserve(G->n));
+    FL_TRY(G->Ke.reserve(G->n));
+  }
+  G->kval = val;
   return FL_OK;
 }
 

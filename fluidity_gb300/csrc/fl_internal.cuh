@@ -135,6 +135,7 @@ int cg_report(CgPlan& P, fl_solve_report* rep, cudaStream_t s);
 void cg_release(CgPlan& P);
 KspState* cg_state(CgPlan& P);
 void gather_done(KspState* const* d_states, int n, int* d_out, cudaStream_t s);
+int csr_mult(struct ::fl_mesh_t* m, const double* val, const double* x, double* y, cudaStream_t s);
 
 // Assembly pieces used by batches (no synchronisation, no allocation).
 size_t assembly_scratch_doubles(const struct ::fl_mesh_t* m, const fl_advdif_params* p);

@@ -50,6 +50,12 @@ class PressureGuessNet:
         check(self.lib.fl_gnn_get_weights(self.handle, w.ctypes.data, self.nparams), "fl_gnn_get_weights")
         return w
 
+    def set_loss(self, val=None):
+        """None: mean squared error; a device tensor of matrix values: the
+        energy norm of the error in that matrix (kept referenced)."""
+        self._kval = val
+        check(self.lib.fl_gnn_set_loss(self.handle, _ptr(val)), "fl_gnn_set_loss")
+
     # compute ---------------------------------------------------------------
     def predict(self, p1, p2, b, out=None, stream=None):
         import torch
@@ -172,11 +178,13 @@ def pressure_sequence(seq: PoissonSequence, nsteps: int, rtol=1e-10):
 
 
 def train(net: PressureGuessNet, ps, bs, mask, nact, steps, *, epochs=20, lr=2e-3,
-          lr_final=1e-4, stream=None, seed=SEED_NET):
+          lr_final=1e-4, stream=None, seed=SEED_NET, kval=None):
     """Adam over the samples (p[t-1], p[t-2], b[t]) -> p[t] for t in `steps`,
-    in a seeded shuffled order per epoch, cosine learning-rate decay.  Returns
-    the mean loss of each epoch."""
+    in a seeded shuffled order per epoch, cosine learning-rate decay; the loss
+    is the energy norm of the error in the matrix `kval` when given, else the
+    mean squared error.  Returns the mean loss of each epoch."""
     import torch
+    net.set_loss(kval)
     steps = list(steps)
     total = epochs * len(steps)
     loss_dev = torch.zeros(total, dtype=torch.float32, device=ps[0].device)

@@ -301,6 +301,12 @@ int fl_gnn_num_params(void);
 int fl_gnn_create(fl_mesh mesh, fl_gnn* net);
 int fl_gnn_destroy(fl_gnn net);
 int fl_gnn_set_weights(fl_gnn net, const float* weights, int32_t count);
+/* Loss of the following gradient and training calls: val = NULL (default)
+ * selects the mean squared error; a device pointer to the assembled matrix
+ * values on the mesh's pattern selects the energy norm e^T K e / nact of the
+ * normalised error over the active nodes, the quantity CG minimises.  The
+ * matrix is read at each call. */
+int fl_gnn_set_loss(fl_gnn net, const double* val);
 int fl_gnn_get_weights(fl_gnn net, float* weights, int32_t count);
 int fl_gnn_predict(fl_gnn net, const double* p1, const double* p2, const double* b, double* pred,
                    void* stream);

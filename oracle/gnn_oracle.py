@@ -10,7 +10,9 @@ reference has no learned component); the formulas below restate it:
     h0   = relu(We f + be)
     h_l  = h_{l-1} + relu(Wl [h_{l-1} ; mean_{j in N(i), j != i} h_{l-1,j}] + bl)
     pred = 2 p1 - p2 + s (wd . h_3 + bd)
-    loss = mean over active nodes of ((pred - target) / s)^2
+    loss = mean over active nodes of ((pred - target) / s)^2, or, given the
+           matrix K, e^T K e / (number of active nodes) with e the normalised
+           error on the active nodes (zero elsewhere)
 
 ``rounded=True`` reproduces the GPU's storage precision: weights, features,
 activations (h, a, z) and the layer gradients fed to the tensor cores (dz) are
@@ -79,7 +81,7 @@ def graph(findrm, colm):
     return P
 
 
-def forward(params, p1, p2, b, X, P, target=None, mask=None, rounded=True):
+def forward(params, p1, p2, b, X, P, target=None, mask=None, rounded=True, K=None):
     R = bf16 if rounded else (lambda v: np.asarray(v, dtype=np.float64))
     q = unpack(params)
     if rounded:
@@ -120,17 +122,23 @@ def forward(params, p1, p2, b, X, P, target=None, mask=None, rounded=True):
         e = np.where(act, (ext - target) / s + o, 0.0)
         c["e"] = e
         c["nact"] = int(act.sum())
-        c["loss"] = float(np.sum(e * e) / c["nact"])
+        if K is None:
+            c["ge"] = 2.0 * e
+            c["loss"] = float(np.sum(e * e) / c["nact"])
+        else:
+            Ke = np.where(act, K @ e, 0.0)
+            c["ge"] = 2.0 * Ke
+            c["loss"] = float(e @ Ke / c["nact"])
     return c
 
 
-def gradients(params, p1, p2, b, X, P, target, mask=None, rounded=True):
+def gradients(params, p1, p2, b, X, P, target, mask=None, rounded=True, K=None):
     """(loss, flat gradient) of the loss with respect to the FP32 parameters."""
     R = bf16 if rounded else (lambda v: np.asarray(v, dtype=np.float64))
     q = unpack(params)
-    c = forward(params, p1, p2, b, X, P, target, mask, rounded)
+    c = forward(params, p1, p2, b, X, P, target, mask, rounded, K)
     g = {}
-    go = 2.0 * c["e"] / c["nact"]
+    go = c["ge"] / c["nact"]
     H3 = c["H"][LAYERS]
     wd = R(q["wd"])
     g["wd"] = H3.T @ go

@@ -2,6 +2,7 @@
 against central finite differences (plain FP64 mode), and its BF16 storage
 mode against the FP64 mode."""
 import numpy as np
+import pytest
 
 from fluidity_gb300 import meshgen as M
 from fluidity_gb300.warmstart import init_weights, rotating_source
@@ -31,9 +32,25 @@ def _case(n=3, seed=5):
     return w, p1, p2, b, X, P, target, mask
 
 
-def test_gradient_matches_finite_differences():
+def _laplacian(n):
+    """A symmetric positive definite matrix on the mesh graph (graph Laplacian
+    plus identity) standing in for the assembled stiffness matrix."""
+    import scipy.sparse as sp
+    nd, X = M.cube_mesh(n)
+    N = X.shape[0]
+    r = np.repeat(nd, 4, axis=1).reshape(-1)
+    c = np.tile(nd, (1, 4)).reshape(-1)
+    A = sp.csr_matrix((np.ones(r.size), (r, c)), shape=(N, N))
+    A.data[:] = -1.0
+    A = A + sp.diags(-np.asarray(A.sum(axis=1)).ravel() + 1.0)
+    return A.tocsr()
+
+
+@pytest.mark.parametrize("energy", [False, True])
+def test_gradient_matches_finite_differences(energy):
     w, p1, p2, b, X, P, target, mask = _case()
-    loss, g = G.gradients(w, p1, p2, b, X, P, target, mask, rounded=False)
+    K = _laplacian(3) if energy else None
+    loss, g = G.gradients(w, p1, p2, b, X, P, target, mask, rounded=False, K=K)
     rng = np.random.default_rng(3)
     blocks = [(G.OFF_WE, G.OFF_BE), (G.OFF_BE, G.OFF_L), (G.OFF_L, G.OFF_L + 8192),
               (G.OFF_L + G.LAYER_SIZE - 64, G.OFF_L + G.LAYER_SIZE),
@@ -47,8 +64,8 @@ def test_gradient_matches_finite_differences():
             wp, wm = w.copy(), w.copy()
             wp[k] += h
             wm[k] -= h
-            lp = G.forward(wp, p1, p2, b, X, P, target, mask, rounded=False)["loss"]
-            lm = G.forward(wm, p1, p2, b, X, P, target, mask, rounded=False)["loss"]
+            lp = G.forward(wp, p1, p2, b, X, P, target, mask, rounded=False, K=K)["loss"]
+            lm = G.forward(wm, p1, p2, b, X, P, target, mask, rounded=False, K=K)["loss"]
             fd = (lp - lm) / (2 * h)
             assert abs(fd - g[k]) <= 1e-5 * abs(g[k]) + 1e-9 * np.abs(g).max(), (k, fd, g[k])
 

@@ -45,10 +45,22 @@ def test_forward_matches_oracle():
     assert err < 1e-2, err
 
 
-def test_gradients_match_oracle():
+@pytest.mark.parametrize("energy", [False, True])
+def test_gradients_match_oracle(energy):
+    import scipy.sparse as sp
+    import torch
     m, X, P, net, w, (p1, p2, b, t, mk), (dp1, dp2, db, dt, dm) = _setup()
+    K = None
+    if energy:
+        # the loss in the energy norm of the assembled Poisson matrix
+        src = torch.from_numpy(M.poisson_source(X)).cuda()
+        val, _ = ft.assemble_advection_diffusion_cg(
+            m, ft.advdif_params(diffusivity=1.0, have_source=True, quad_degree=2), source=src)
+        net.set_loss(val)
+        s = m.sparsity()
+        K = sp.csr_matrix((val.cpu().numpy(), s.colm, s.findrm), shape=(m.N, m.N))
     loss, g = net.gradients(dp1, dp2, db, dt, dm)
-    lo, go = G.gradients(w, p1, p2, b, X, P, t, mk, rounded=True)
+    lo, go = G.gradients(w, p1, p2, b, X, P, t, mk, rounded=True, K=K)
     assert abs(loss - lo) <= 1e-3 * lo
     blocks = {"We": (G.OFF_WE, G.OFF_BE), "be": (G.OFF_BE, G.OFF_L), "wd": (G.OFF_WD, G.OFF_BD),
               "bd": (G.OFF_BD, G.NPARAMS)}
