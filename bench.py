@@ -529,8 +529,10 @@ def run_ours(args, rank, ws, dist):
         batch = bench_batch(args, dev, stream)
     learned = None
     if not args.no_learned:
-        learned = {f"n{k}": bench_learned(args, dev, stream, k, epochs=e)
-                   for k, e in ((64, args.epochs), (args.n, max(4, args.epochs // 3)))}
+        sizes = [int(v) for v in args.learned_sizes.split(",") if v]
+        learned = {f"n{k}": bench_learned(args, dev, stream, k,
+                                          epochs=args.epochs if k <= 64 else max(4, args.epochs // 3))
+                   for k in sizes}
 
     if rank != 0:
         return
@@ -582,6 +584,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--learned-sizes", default="64,128",
+                    help="mesh sides of the learned-warm-start sequences")
     ap.add_argument("--batch-fields", type=int, default=32)
     args = ap.parse_args()
     rank, ws, dist = dist_setup(args)

@@ -98,18 +98,26 @@ __device__ __forceinline__ df df_rcp(df x) {
   return df_fast_two_sum(r0, r0 * res);
 }
 
+// Conversion path of df_from_double, kept out of line so that the common
+// path carries no FP64 instruction (an inlined branch this short would be
+// predicated and executed by every thread).
+static __device__ __noinline__ df df_from_double_rare(double d) {
+  const float hi = __double2float_rn(d);
+  return {hi, __double2float_rn(d - (double)hi)};
+}
+
 // Exact-or-nearly split of a double into hi + lo by slicing its bits (no FP64
 // or conversion-pipe instruction on the common path): hi keeps the leading 24
 // significand bits, lo the remaining 29 rounded to 24 (exact when the double
-// has at most 48 significant bits).  Magnitudes outside [2^-70, 2^100], zeros,
-// infinities and NaNs take the conversion path.
+// has at most 48 significant bits).  Zeros are split by bits too; magnitudes
+// outside [2^-70, 2^100], infinities and NaNs take the conversion path.
 __device__ __forceinline__ df df_from_double(double d) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(d);
   const uint32_t hw = (uint32_t)(b >> 32), lw = (uint32_t)b;
   const int exp = (int)((hw >> 20) & 0x7ffu);
   if (exp < 1023 - 70 || exp > 1023 + 100) {
-    const float hi = __double2float_rn(d);
-    return {hi, __double2float_rn(d - (double)hi)};
+    if ((b << 1) == 0ull) return {__uint_as_float(hw & 0x80000000u), 0.0f};  // signed zero
+    return df_from_double_rare(d);
   }
   const uint32_t sign = hw & 0x80000000u;
   const uint32_t fb = sign | ((uint32_t)(exp - 1023 + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);

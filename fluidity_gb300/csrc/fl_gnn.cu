@@ -42,7 +42,7 @@ constexpr int kF = 16;        // input features (6 used), one mma K step
 constexpr int kLayers = 3;
 constexpr int kTM = 64;       // nodes per tile
 constexpr int kTh = 128;      // threads of the tile kernels (4 warps x 16 nodes)
-constexpr int kPersist = 304; // blocks of the reduction-over-nodes kernels
+constexpr int kPersist = 456; // blocks (3 per SM) of the reduction-over-nodes kernels
 
 // flat FP32 parameter vector
 constexpr int kOffWe = 0;                    // [64][16]
@@ -384,45 +384,60 @@ __global__ void __launch_bounds__(kTh) k_gnn_bwd_dx(int n, const float* __restri
 }
 
 // Layer backward, weight gradients: dWl = dZ^T [h ; a], dbl = sum dZ, summed
-// over the node tiles of this block; one partial per block.
-__global__ void __launch_bounds__(kTh) k_gnn_bwd_dw(int n, const float* __restrict__ dHn,
-                                                    const bf16* __restrict__ Z, const bf16* __restrict__ Hin,
-                                                    const bf16* __restrict__ A, float* __restrict__ part) {
+// over the node tiles of this block; one partial per block.  Eight warps:
+// warp w owns output rows 16 (w % 4) .. +16 and input columns 64 (w / 4) ..
+// +64.  Tiles are loaded eight channels (16 bytes of bf16, 32 of fp32) at a
+// time and transposed into shared memory ([channel][node]).
+constexpr int kThW = 256;
+__global__ void __launch_bounds__(kThW) k_gnn_bwd_dw(int n, const float* __restrict__ dHn,
+                                                     const bf16* __restrict__ Z, const bf16* __restrict__ Hin,
+                                                     const bf16* __restrict__ A, float* __restrict__ part) {
   note_launch();
   __shared__ __align__(16) bf16 dZt[kW * kLd64];      // [out][node]
   __shared__ __align__(16) bf16 Xt[2 * kW * kLd64];   // [in][node]
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  float acc[16][4] = {};
+  const int wm = w & 3, wn = w >> 2;
+  float acc[8][4] = {};
   float db = 0.0f;  // thread c < 64: bias gradient of output channel c
   const int ntiles = (n + kTM - 1) / kTM;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int base = tile * kTM;
     __syncthreads();
-    for (int k = threadIdx.x; k < kTM * kW; k += kTh) {
-      const int r = k / kW, c = k % kW, i = base + r;
-      float d = 0.0f;
-      bf16 hv = __float2bfloat16_rn(0.0f), av = hv;
+    for (int k = threadIdx.x; k < kTM * (kW / 8); k += kThW) {
+      const int r = k >> 3, c0 = (k & 7) * 8, i = base + r;
+      float d[8] = {};
+      uint4 hv = {0u, 0u, 0u, 0u}, av = hv;
       if (i < n) {
-        const float z = __bfloat162float(Z[(int64_t)i * kW + c]);
-        d = z > 0.0f ? dHn[(int64_t)i * kW + c] : 0.0f;
-        hv = Hin[(int64_t)i * kW + c];
-        av = A[(int64_t)i * kW + c];
+        const uint4 zv = *reinterpret_cast<const uint4*>(Z + (int64_t)i * kW + c0);
+        const float4 g0 = *reinterpret_cast<const float4*>(dHn + (int64_t)i * kW + c0);
+        const float4 g1 = *reinterpret_cast<const float4*>(dHn + (int64_t)i * kW + c0 + 4);
+        hv = *reinterpret_cast<const uint4*>(Hin + (int64_t)i * kW + c0);
+        av = *reinterpret_cast<const uint4*>(A + (int64_t)i * kW + c0);
+        const bf16* z8 = reinterpret_cast<const bf16*>(&zv);
+        const float gg[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+#pragma unroll
+        for (int u = 0; u < 8; ++u) d[u] = __bfloat162float(z8[u]) > 0.0f ? gg[u] : 0.0f;
       }
-      dZt[c * kLd64 + r] = __float2bfloat16_rn(d);
-      Xt[c * kLd64 + r] = hv;
-      Xt[(c + kW) * kLd64 + r] = av;
+      const bf16* h8 = reinterpret_cast<const bf16*>(&hv);
+      const bf16* a8 = reinterpret_cast<const bf16*>(&av);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        dZt[(c0 + u) * kLd64 + r] = __float2bfloat16_rn(d[u]);
+        Xt[(c0 + u) * kLd64 + r] = h8[u];
+        Xt[(kW + c0 + u) * kLd64 + r] = a8[u];
+      }
     }
     __syncthreads();
-    warp_gemm<kTM, 16, kLd64, kLd64>(dZt + w * 16 * kLd64, Xt, acc);
+    warp_gemm<kTM, 8, kLd64, kLd64>(dZt + wm * 16 * kLd64, Xt + wn * kW * kLd64, acc);
     if (threadIdx.x < kW)
       for (int r = 0; r < kTM; ++r) db += __bfloat162float(dZt[threadIdx.x * kLd64 + r]);
   }
   float* out = part + (int64_t)blockIdx.x * kPartStride;
 #pragma unroll
-  for (int nt = 0; nt < 16; ++nt)
+  for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int o = w * 16 + g + 8 * h, c = nt * 8 + t * 2;
+      const int o = wm * 16 + g + 8 * h, c = wn * kW + nt * 8 + t * 2;
       out[o * 2 * kW + c] = acc[nt][2 * h];
       out[o * 2 * kW + c + 1] = acc[nt][2 * h + 1];
     }
@@ -467,14 +482,20 @@ __global__ void __launch_bounds__(kTh) k_gnn_bwd_enc(Inputs in, const float* __r
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int base = tile * kTM;
     __syncthreads();
-    for (int k = threadIdx.x; k < kTM * kW; k += kTh) {
-      const int r = k / kW, c = k % kW, i = base + r;
-      float d = 0.0f;
+    for (int k = threadIdx.x; k < kTM * (kW / 8); k += kTh) {
+      const int r = k >> 3, c0 = (k & 7) * 8, i = base + r;
+      float d[8] = {};
       if (i < in.n) {
-        const float z = __bfloat162float(Z0[(int64_t)i * kW + c]);
-        d = z > 0.0f ? dH0[(int64_t)i * kW + c] : 0.0f;
+        const uint4 zv = *reinterpret_cast<const uint4*>(Z0 + (int64_t)i * kW + c0);
+        const float4 g0 = *reinterpret_cast<const float4*>(dH0 + (int64_t)i * kW + c0);
+        const float4 g1 = *reinterpret_cast<const float4*>(dH0 + (int64_t)i * kW + c0 + 4);
+        const bf16* z8 = reinterpret_cast<const bf16*>(&zv);
+        const float gg[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+#pragma unroll
+        for (int u = 0; u < 8; ++u) d[u] = __bfloat162float(z8[u]) > 0.0f ? gg[u] : 0.0f;
       }
-      dZt[c * kLd64 + r] = __float2bfloat16_rn(d);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) dZt[(c0 + u) * kLd64 + r] = __float2bfloat16_rn(d[u]);
     }
     if (threadIdx.x < kTM) {
       const int i = base + threadIdx.x;
@@ -610,7 +631,7 @@ int backward(fl_gnn_t* G, const double* p1, const double* p2, const double* b, c
   for (int l = kLayers; l >= 1; --l) {
     const int off = kOffL + (l - 1) * kLayerSize;
     k_gnn_bwd_dx<<<tile_grid(n), kTh, 0, s>>>(n, cur, Zbuf(G, l), G->wb.p + off, nxt, G->dA.p);
-    k_gnn_bwd_dw<<<pg, kTh, 0, s>>>(n, cur, Zbuf(G, l), Hbuf(G, l - 1), Abuf(G, l - 1), G->part.p);
+    k_gnn_bwd_dw<<<pg, kThW, 0, s>>>(n, cur, Zbuf(G, l), Hbuf(G, l - 1), Abuf(G, l - 1), G->part.p);
     k_gnn_reduce<<<grid_for(kLayerSize, 256, 4), 256, 0, s>>>(G->part.p, (int)pg, kPartStride, kLayerSize,
                                                                G->g.p + off);
     k_gnn_agg_bwd<<<warp_grid(n), 256, 0, s>>>(n, m->findrm.p, m->colm.p, G->inv_deg.p, G->dA.p, nxt);
