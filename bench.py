@@ -61,12 +61,17 @@ def measured_peak_hbm():
 
 
 def ncu_traffic(key):
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    """DRAM bytes per launch recorded from an ncu capture (profiles/ncu_traffic.txt)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     try:
         with open(p) as fh:
-            return json.load(fh).get(key)
+            for line in fh:
+                f = line.split()
+                if f and not f[0].startswith("#") and f[0] == key:
+                    return float(f[1])
     except Exception:
         return None
+    return None
 
 
 class ClockSampler:
@@ -555,7 +560,7 @@ def run_ours(args, rank, ws, dist):
                    "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (no flush)",
                    "gpu_setup_s (sparsity+colouring)": setup_s},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": ncu_traffic("k_asm_p1_diffusion"),
+                     "frac": achieved / peak, "traffic": ncu_traffic(f"assembly_p1_poisson_{args.n}"),
                      "peak_kind": peak_kind,
                      "kernel": "assembly: k_asm_p1_diffusion_df + k_rows_pull_df",
                      "kernel_ms": kernel_ms, "algorithmic_bytes": alg},
