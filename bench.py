@@ -154,7 +154,7 @@ def workload(n):
     return nd, X, M.poisson_source(X), M.boundary_nodes(X)
 
 
-def cpu_assembly_rate(nd, X, src, colours=None, findrm=None, colm=None, reps=1):
+def cpu_assembly_rate(nd, X, src, colours=None, findrm=None, colm=None, reps=1, nthreads=0):
     """Oracle assembly of the whole workload on all host cores; (Melem/s, threads, s)."""
     from oracle import oracle as O
     if findrm is None:
@@ -167,11 +167,40 @@ def cpu_assembly_rate(nd, X, src, colours=None, findrm=None, colm=None, reps=1):
         t0 = time.perf_counter()
         _, _, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
                                      findrm=findrm, colm=colm, diffusivity=1.0, source=src,
-                                     colours=colours)
+                                     colours=colours, nthreads=nthreads)
         dt = time.perf_counter() - t0
         assert st == 0
         best = dt if best is None else min(best, dt)
-    return nd.shape[0] / best / 1e6, O.num_threads(), best
+    return nd.shape[0] / best / 1e6, nthreads or O.num_threads(), best
+
+
+def cpu_advdif_steps(n=16, nsteps=10, nthreads=0):
+    """The oracle's restatement of the 10-step advection-diffusion workload on
+    the host cores (assembly, Dirichlet, GMRES(30) + Jacobi); ms per step."""
+    from fluidity_gb300 import meshgen as M
+    from oracle import oracle as O
+    nd, X = M.cube_mesh(n)
+    findrm, colm, _ = O.make_sparsity(nd)
+    ocol, ncol = O.colour_cg1(nd)
+    cs = O.colour_sets(ocol, ncol)
+    u = M.advdif_velocity(X)
+    bn = M.boundary_nodes(X)
+    T = M.gaussian_tracer(X)
+    t0 = time.perf_counter()
+    its = []
+    for _ in range(nsteps):
+        val, rhs, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
+                                         findrm=findrm, colm=colm, theta=0.5, dt=0.01,
+                                         have_mass=True, velocity=u, T=T, diffusivity=1e-3,
+                                         colours=cs, nthreads=nthreads)
+        assert st == 0
+        ina = np.zeros(X.shape[0], dtype=np.uint8)
+        O.apply_dirichlet(bn, np.zeros(bn.size), T, 0.01, rhs, ina)
+        dx, it, reason, _ = O.petsc_solve(findrm.astype(np.int64), colm, val, ina, rhs,
+                                          ksp="gmres", restart=30, rtol=1e-10)
+        its.append(int(it))
+        T = T + 0.01 * dx
+    return (time.perf_counter() - t0) / nsteps * 1e3, its
 
 
 def run_reference(args, rank, ws, dist):
@@ -317,6 +346,133 @@ def bench_batch(args, dev, stream):
     }
     b.close()
     return out
+
+
+def p2_algorithmic_bytes(E, N1, N2, nnz):
+    """Compulsory HBM bytes of one P2 assembly (P2 and P1 connectivity,
+    coordinates, source, pattern read once, values and rhs written once)."""
+    return 40 * E + 16 * E + 24 * N1 + 8 * N2 + 4 * (N2 + 1) + 12 * nnz + 8 * N2
+
+
+def bench_p2(args, dev, stream, n=64):
+    """P2 Poisson on the n^3 six-tet cube (degree-4 quadrature): assembly
+    throughput against its algorithmic bytes, then CG + Jacobi to 1e-10."""
+    import ctypes as C
+
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+    from fluidity_gb300 import meshgen as M
+
+    nd, X = M.cube_mesh(n)
+    nd2, n2 = ft.make_global_numbering_p2(nd)
+    X2 = M.p2_coordinates(nd, nd2, X, M.P2_COUNTS)
+    m = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    p = ft.advdif_params(diffusivity=1.0, have_source=True, quad_degree=4)
+    src = torch.from_numpy(M.poisson_source(X2)).to(dev)
+    val = torch.empty(m.nnz, dtype=torch.float64, device=dev)
+    rhs = torch.empty(m.N, dtype=torch.float64, device=dev)
+    step = lambda: ft.assemble_advection_diffusion_cg(m, p, source=src, val=val, rhs=rhs, stream=stream)
+    for _ in range(3):
+        step()
+    reps = max(3, min(20, args.steps))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    m.lib.fl_set_kernel_timing(m.handle, 1)
+    kms = []
+    for _ in range(reps):
+        step()
+        f = C.c_float()
+        ft.check(m.lib.fl_last_assembly_kernel_ms(m.handle, C.byref(f)), "timing")
+        kms.append(f.value)
+    m.lib.fl_set_kernel_timing(m.handle, 0)
+    kernel_ms = float(np.median(kms))
+    alg = p2_algorithmic_bytes(m.E, X.shape[0], m.N, m.nnz)
+    peak, _ = measured_peak_hbm()
+    achieved = alg / (kernel_ms * 1e-3) / 1e9
+    ina = torch.zeros(m.N, dtype=torch.uint8, device=dev)
+    bn = M.boundary_nodes(X2)
+    step()
+    ft.apply_dirichlet_conditions(m, rhs, ina, torch.from_numpy(bn).to(dev),
+                                  torch.zeros(bn.size, dtype=torch.float64, device=dev), dt=1.0,
+                                  stream=stream)
+    solve = {}
+    for prec in ("fp64", "reliable"):
+        x = torch.zeros(m.N, dtype=torch.float64, device=dev)
+        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000, precision=prec)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        solve[prec] = {"ms": e0.elapsed_time(e1), "iterations": rep["iterations"],
+                       "reason": rep["reason_name"], "true_rel_residual": rep["true_rel_residual"]}
+    it_bytes = cg_iteration_bytes(m.N, m.nnz)
+    f64 = solve["fp64"]
+    f64["achieved_gbs"] = it_bytes * f64["iterations"] / (f64["ms"] * 1e-3) / 1e9
+    f64["frac_of_hbm"] = f64["achieved_gbs"] / peak
+    xa = torch.from_numpy(M.poisson_source(X2) / (3 * np.pi ** 2)).to(dev)
+    return {
+        "workload": f"P2 Poisson, {n}^3 six-tet cube, degree-4 quadrature (11 points)",
+        "elements": m.E, "nodes": m.N, "nnz": m.nnz, "ms_per_assembly": ms,
+        "melem_per_s": m.E / (ms * 1e-3) / 1e6, "kernel_ms": kernel_ms,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "algorithmic_bytes": alg},
+        "solve": solve, "max_err_vs_analytic": float((x - xa).abs().max()),
+    }
+
+
+def bench_advdif_steps(args, dev, stream, n=16, nsteps=10):
+    """The CPU-runnable workload: 10 advection-diffusion steps (theta 0.5,
+    dt 0.01, GMRES(30) + Jacobi to 1e-10) on the 16^3 mesh, through
+    solve_field_equation_cg's device path, timed per step."""
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+    from fluidity_gb300 import meshgen as M
+
+    nd, X = M.cube_mesh(n)
+    m = ft.Mesh(nd, X)
+    p = ft.advdif_params(theta=0.5, dt=0.01, have_mass=True, have_advection=True, diffusivity=1e-3)
+    u = torch.from_numpy(M.advdif_velocity(X)).to(dev)
+    bn = M.boundary_nodes(X)
+    nodes = torch.from_numpy(bn).to(dev)
+    g = torch.zeros(bn.size, dtype=torch.float64, device=dev)
+    opts = ft.solver_options(ksp="gmres", restart=30, rtol=1e-10, max_its=10000)
+    val = torch.empty(m.nnz, dtype=torch.float64, device=dev)
+    rhs = torch.empty(m.N, dtype=torch.float64, device=dev)
+    ina = torch.zeros(m.N, dtype=torch.uint8, device=dev)
+    dT = torch.zeros(m.N, dtype=torch.float64, device=dev)
+
+    def run():
+        t = torch.from_numpy(M.gaussian_tracer(X)).to(dev)
+        its = []
+        for _ in range(nsteps):
+            ft.assemble_advection_diffusion_cg(m, p, t=t, velocity=u, val=val, rhs=rhs, stream=stream)
+            ina.zero_()
+            ft.apply_dirichlet_conditions(m, rhs, ina, nodes, g, t=t, dt=p.dt, stream=stream)
+            dT.zero_()
+            rep = ft.petsc_solve(m, dT, val, rhs, opts, inactive=ina, stream=stream)
+            its.append(rep["iterations"])
+            t = t + p.dt * dT
+        return t, its
+
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t, its = run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"workload": f"advection-diffusion, {n}^3 six-tet cube, {nsteps} steps, GMRES(30)+Jacobi rtol 1e-10",
+            "ms_per_step": ms / nsteps, "iterations": its, "tracer_max_final": float(t.max())}
 
 
 def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
@@ -529,6 +685,8 @@ def run_ours(args, rank, ws, dist):
             out[f"speedup_{prec}_vs_fp64"] = f64["ms"] / out[prec]["ms"]
         solve = out
 
+    p2 = None if args.no_p2 else bench_p2(args, dev, stream)
+    steps16 = bench_advdif_steps(args, dev, stream)
     batch = None
     if not args.no_batch:
         batch = bench_batch(args, dev, stream)
@@ -545,11 +703,19 @@ def run_ours(args, rank, ws, dist):
     if not args.no_cpu and ws == 1:
         s = m.sparsity()
         col, ptr, el = m.colouring()
+        ncores = len(os.sched_getaffinity(0))
         rate, thr, secs = cpu_assembly_rate(nd, X, src, colours=(ptr.astype(np.int64), el),
-                                            findrm=s.findrm.astype(np.int64), colm=s.colm)
+                                            findrm=s.findrm.astype(np.int64), colm=s.colm,
+                                            nthreads=ncores)
+        adv_ms, adv_its = cpu_advdif_steps(nthreads=ncores)
+        rate1, _, secs1 = cpu_assembly_rate(nd, X, src, colours=(ptr.astype(np.int64), el),
+                                            findrm=s.findrm.astype(np.int64), colm=s.colm,
+                                            nthreads=1)
         cpu = {"value": rate, "unit": "Melem/s", "cores": thr, "kind": "port",
                "sample": f"one full {args.n}^3 assembly ({secs:.2f} s), OpenMP over "
-                         f"{m.ncolours} colours, oracle restatement of the reference loop"}
+                         f"{m.ncolours} colours, oracle restatement of the reference loop",
+               "value_1_core": rate1, "sample_1_core": f"one full {args.n}^3 assembly ({secs1:.2f} s)",
+               "advdif_16_ten_steps_ms_per_step": adv_ms, "advdif_16_ten_steps_iterations": adv_its}
     value = E * ws / (ms * 1e-3) / 1e6
     line = {
         "metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": ws, "steps": args.steps,
@@ -571,6 +737,8 @@ def run_ours(args, rank, ws, dist):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "solve": solve,
+        "p2": p2,
+        "advdif_16_ten_steps": steps16,
         "batch": batch,
         "learned": learned,
     }
@@ -587,6 +755,7 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-p2", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--learned-sizes", default="64,128",

@@ -166,3 +166,11 @@ def batch_mesh(index: int, n: int | None = None):
     SEED_MESHES + index); ``n`` overrides its side for small tests."""
     side = BATCH_MESH_SIDES[index] if n is None else n
     return cube_mesh(side, seed=SEED_MESHES + index)
+
+
+#: Barycentric counts (x2) of the ten local P2 nodes in the local node order of
+#: femtools/Element_Numbering.F90:389-472 (vertex 1, edge 12, vertex 2, edge 13,
+#: edge 23, vertex 3, edge 14, edge 24, edge 34, vertex 4).
+P2_COUNTS = np.array([[2, 0, 0, 0], [1, 1, 0, 0], [0, 2, 0, 0], [1, 0, 1, 0], [0, 1, 1, 0],
+                      [0, 0, 2, 0], [1, 0, 0, 1], [0, 1, 0, 1], [0, 0, 1, 1], [0, 0, 0, 2]],
+                     dtype=np.int32)
