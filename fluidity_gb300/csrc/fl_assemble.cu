@@ -481,6 +481,144 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   }
 }
 
+// P2 diffusion + source (+ consistent mass) in double-float.  With P1
+// coordinates the reference gradients are constant per element, so
+//   K_ij = theta dt / |detJ| * sum_k Q_k S_ij,k (+ |detJ| Mref_ij),
+//   Q = cof^T kappa cof (6 symmetric components),
+//   S_ij,k = sum_g w dN_i/dL_a dN_j/dL_b over the rule, symmetrised in (a, b),
+//   rhs_i = |detJ| sum_j Mref_ij f_j - 1/|detJ| sum_j (sum_k Q_k S_ij,k) t_j,
+// an exact regrouping of dshape_dot_dshape / dshape_tensor_dshape
+// (FETools.F90:391,668) over the quadrature rule, as for P1.  The tables
+// (55 symmetric pairs) travel as kernel parameters.  Each element writes ten
+// row slices {K_i0..K_i9, r_i, 0} of double-float pairs (96 B each).
+struct DfP2Args {
+  int32_t E;
+  const int32_t* nd;   // P2 connectivity, 10 per element
+  const int32_t* xnd;  // P1 coordinate connectivity
+  const double* X;
+  const double* t;
+  const double* f;
+  float4* em;
+  df S[55][6];
+  df M[55];
+  df qs;        // theta*dt (zero when the dt factor is not applied)
+  df kdiag[3];  // diagonal kappa (isotropic: kappa in every entry)
+  int have_mass, have_src;
+};
+
+__host__ __device__ constexpr int sym10(int i, int j) {
+  return i <= j ? i * 10 - (i * (i - 1)) / 2 + (j - i) : j * 10 - (j * (j - 1)) / 2 + (i - j);
+}
+
+// sum_k a_k b_k of double-float values: exact leading products (FMA
+// TwoProduct) summed by TwoSum, all error terms in one float, one
+// renormalisation.
+template <int K>
+__device__ __forceinline__ df df_dot(const df* a, const df* b) {
+  float s = a[0].hi * b[0].hi;
+  float e = fmaf(a[0].hi, b[0].hi, -s);
+  e = fmaf(a[0].hi, b[0].lo, e);
+  e = fmaf(a[0].lo, b[0].hi, e);
+#pragma unroll
+  for (int k = 1; k < K; ++k) {
+    const float p = a[k].hi * b[k].hi;
+    float ep = fmaf(a[k].hi, b[k].hi, -p);
+    ep = fmaf(a[k].hi, b[k].lo, ep);
+    ep = fmaf(a[k].lo, b[k].hi, ep);
+    const df t = df_two_sum(s, p);
+    s = t.hi;
+    e += t.lo + ep;
+  }
+  return df_fast_two_sum(s, e);
+}
+
+__global__ void __launch_bounds__(128) k_asm_p2_diffusion_df(DfP2Args A) {
+  note_launch();
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+    const int vi[4] = {v.x, v.y, v.z, v.w};
+    double x[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+    df J[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
+    df cof[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+        cof[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
+      }
+    const df det = df_dot3(J[0][0], cof[0][0], J[1][0], cof[1][0], J[2][0], cof[2][0]);
+    const df adet = df_abs(det);
+    const df rdet = df_rcp(adet);
+    // Q_ab = sum_c cof_ca kappa_c cof_cb in the order 00, 11, 22, 01, 02, 12
+    const int qa[6] = {0, 1, 2, 0, 0, 1}, qb[6] = {0, 1, 2, 1, 2, 2};
+    df qo[6], qk[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const int a = qa[k], b = qb[k];
+      const df q = df_dot3(cof[0][a], df_mul(A.kdiag[0], cof[0][b]), cof[1][a], df_mul(A.kdiag[1], cof[1][b]),
+                           cof[2][a], df_mul(A.kdiag[2], cof[2][b]));
+      qo[k] = df_mul(q, rdet);    // operator: 1/|detJ| Q
+      qk[k] = df_mul(qo[k], A.qs);  // matrix: theta dt/|detJ| Q
+    }
+    int tn[10];
+    {
+      // 10 ints per element: element e starts at 40 e bytes, 8-byte aligned
+      const int2* nd2 = reinterpret_cast<const int2*>(A.nd + (uint32_t)e * 10u);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const int2 w = __ldg(nd2 + k);
+        tn[2 * k] = w.x;
+        tn[2 * k + 1] = w.y;
+      }
+    }
+    df fe[10], te[10];
+#pragma unroll
+    for (int j = 0; j < 10; ++j) {
+      fe[j] = A.have_src ? df_mul(adet, df_from_double(__ldg(A.f + tn[j]))) : df{0.0f, 0.0f};
+      te[j] = A.t ? df_from_double(__ldg(A.t + tn[j])) : df{0.0f, 0.0f};
+    }
+    float4* rec = A.em + (uint32_t)e * 60u;
+#pragma unroll 1
+    for (int i = 0; i < 10; ++i) {
+      df K[10];
+      df tsum = {0.0f, 0.0f};
+#pragma unroll
+      for (int j = 0; j < 10; ++j) {
+        const df* Sp = A.S[sym10(i, j)];
+        if (A.t) {
+          const df op = df_dot<6>(qo, Sp);
+          K[j] = df_mul(op, A.qs);
+          tsum = df_add(tsum, df_mul(op, te[j]));
+        } else {
+          K[j] = df_dot<6>(qk, Sp);
+        }
+        if (A.have_mass) K[j] = df_add(K[j], df_mul(adet, A.M[sym10(i, j)]));
+      }
+      df r = {0.0f, 0.0f};
+      if (A.have_src) {
+        df mrow[10];
+#pragma unroll
+        for (int j = 0; j < 10; ++j) mrow[j] = A.M[sym10(i, j)];
+        r = df_dot<10>(mrow, fe);
+      }
+      if (A.t) r = df_sub(r, tsum);
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        rec[6 * i + k] = make_float4(K[2 * k].hi, K[2 * k].lo, K[2 * k + 1].hi, K[2 * k + 1].lo);
+      rec[6 * i + 5] = make_float4(r.hi, r.lo, 0.0f, 0.0f);
+    }
+  }
+}
+
 // Row pass: thread per CSR row; contributions of the row's elements are added
 // in the colour order of ne_col and the row is written once.  Accumulators
 // and the row's column indices live in shared memory for rows up to RMAX
@@ -572,6 +710,84 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
       }
     P.rhs[row] = df_to_double(r);
   }
+}
+
+// Row pass of the P2 double-float records: slice (element, local row) =
+// 6 float4 {K_a0..K_a9, r_a, 0}; the row positions of the ten element nodes
+// come from three ne_pos words per incidence.  Incidences are taken two at a
+// time (loads first, then the adds in colour order).
+template <int THREADS, int RMAX>
+__global__ void __launch_bounds__(THREADS) k_rows_pull_df10(PullArgs P) {
+  note_launch();
+  extern __shared__ unsigned char smem_raw[];
+  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
+  const float4* rec = reinterpret_cast<const float4*>(P.em);
+  const int t = threadIdx.x;
+  for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
+    const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
+    const bool in_smem = L <= RMAX;
+    if (in_smem) {
+      for (int k = 0; k < L; ++k) acc[k * THREADS + t] = make_float2(0.0f, 0.0f);
+    } else {
+      for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
+    }
+    df r = {0.0f, 0.0f};
+    const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
+    for (int q0 = ib; q0 < ie; q0 += 2) {
+      int inc[2];
+      uint32_t pw[2][3];
+      float4 q[2][6];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const bool ok = q0 + u < ie;
+        inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
+#pragma unroll
+        for (int w = 0; w < 3; ++w) pw[u][w] = ok ? __ldg(P.ne_pos + (int64_t)(q0 + u) * 3 + w) : 0u;
+        const uint32_t ri = 6u * (uint32_t)((inc[u] >> 4) * 10 + (inc[u] & 15));
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[u][k] = ok ? __ldg(rec + ri + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (q0 + u >= ie) break;
+#pragma unroll
+        for (int b = 0; b < 10; ++b) {
+          const float4 c4 = q[u][b >> 1];
+          const df v = (b & 1) ? df{c4.z, c4.w} : df{c4.x, c4.y};
+          const int pos = (pw[u][b >> 2] >> (8 * (b & 3))) & 0xffu;
+          if (in_smem) {
+            const float2 c = acc[pos * THREADS + t];
+            const df sum = df_add({c.x, c.y}, v);
+            acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
+          } else {
+            P.val[base + pos] += df_to_double(v);
+          }
+        }
+        r = df_add(r, {q[u][5].x, q[u][5].y});
+      }
+    }
+    if (in_smem)
+      for (int k = 0; k < L; ++k) {
+        const float2 c = acc[k * THREADS + t];
+        P.val[base + k] = df_to_double({c.x, c.y});
+      }
+    P.rhs[row] = df_to_double(r);
+  }
+}
+
+template <int THREADS, int RMAX>
+static int launch_pull_df10(const PullArgs& P, cudaStream_t s) {
+  const size_t smem = (size_t)RMAX * THREADS * sizeof(float2);
+  static bool configured = false;
+  if (!configured) {
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df10<THREADS, RMAX>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  const unsigned grid = (unsigned)((P.N + THREADS - 1) / THREADS);
+  k_rows_pull_df10<THREADS, RMAX><<<grid, THREADS, smem, s>>>(P);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
 }
 
 template <int THREADS, int RMAX>
@@ -672,6 +888,12 @@ __global__ void k_dirichlet(int32_t nb, const int32_t* __restrict__ nodes, int32
 // place in val.  Every row is summed by one thread in incidence order, so the
 // tile changes no result.
 static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int max_row, int tile, cudaStream_t s) {
+  if (loc == 10 && use_df) {
+    if (max_row > 72) return launch_pull_df10<32, 128>(P, s);
+    if (tile == 0) return launch_pull_df10<32, 72>(P, s);
+    if (tile == 2) return launch_pull_df10<128, 72>(P, s);
+    return launch_pull_df10<64, 72>(P, s);
+  }
   if (loc == 4 && use_df) {
     if (max_row <= 16) {
       if (tile == 0) return launch_pull_df<64, 16>(P, s);
@@ -726,14 +948,32 @@ static TensorCache g_tensors;
 
 // Which kernel handles a parameter set: the closed-form P1 kernel covers the
 // Poisson/diffusion forms (no advection, no absorption, consistent mass).
-static bool use_p1_closed_form(const fl_mesh_t* m, const fl_advdif_params* p) {
-  return m->loc == 4 && !p->have_advection && !p->have_absorption && !(p->have_mass && p->lump_mass) &&
-         p->have_diffusivity;
+static bool diffusion_form(const fl_advdif_params* p) {
+  return !p->have_advection && !p->have_absorption && !(p->have_mass && p->lump_mass) && p->have_diffusivity;
 }
 
+static bool use_p1_closed_form(const fl_mesh_t* m, const fl_advdif_params* p) {
+  return m->loc == 4 && diffusion_form(p);
+}
+
+static bool diagonal_kappa(const fl_advdif_params* p) {
+  if (p->isotropic_diffusivity) return true;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b)
+      if (a != b && p->diffusivity[3 * a + b] != 0.0) return false;
+  return true;
+}
+
+// The double-float P2 kernel: the diffusion form with a diagonal kappa.
+static bool use_p2_df(const fl_mesh_t* m, const fl_advdif_params* p) {
+  return m->loc == 10 && diffusion_form(p) && diagonal_kappa(p);
+}
+
+// Element-record storage per element, in doubles (a double-float pair counts
+// as one): P1 closed form 24 (row slices of 6 pairs), P2 double-float 120 (row
+// slices of 12 pairs), general forms LOC*(LOC+1) coefficient-major.
 size_t assembly_scratch_doubles(const fl_mesh_t* m, const fl_advdif_params* p) {
-  const bool closed = use_p1_closed_form(m, p);
-  const int ncoef = closed ? 24 : m->loc * m->loc + m->loc;
+  const int ncoef = use_p1_closed_form(m, p) ? 24 : use_p2_df(m, p) ? 120 : m->loc * m->loc + m->loc;
   return (size_t)ncoef * m->E;
 }
 
@@ -785,13 +1025,11 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   A.have_src = p->have_source;
   A.have_abs = p->have_absorption;
   const bool closed = use_p1_closed_form(m, p);
+  const bool p2df = use_p2_df(m, p);
   const int loc = m->loc;
-  // coefficient storage per element (doubles): 14 for the FP64 closed form,
-  // 24 for the double-float row-slice records, LOC*(LOC+1) for the general form
-  const int ncoef = closed ? 24 : loc * loc + loc;
   double* em = em_override;
   if (!em) {
-    FL_TRY(m->em.reserve((size_t)ncoef * m->E));
+    FL_TRY(m->em.reserve(assembly_scratch_doubles(m, p)));
     em = m->em.p;
   }
   A.em = em;
@@ -804,14 +1042,39 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     }
     FL_TRY_CUDA(cudaEventRecord(m->ev0, s));
   }
-  // Diagonal (or isotropic) kappa: the double-float element pass; a full
-  // tensor keeps the FP64 closed form.
-  bool diag_kappa = true;
-  for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 3; ++b)
-      if (a != b && p->diffusivity[3 * a + b] != 0.0) diag_kappa = false;
-  const bool use_df = closed && (p->isotropic_diffusivity || diag_kappa);
-  if (use_df) {
+  // Diagonal (or isotropic) kappa: the double-float element passes; a full
+  // tensor keeps the FP64 forms.
+  const bool use_df = (closed && diagonal_kappa(p)) || p2df;
+  if (p2df) {
+    RefTensors h;
+    build_tensors(2, p->quad_degree, h);
+    DfP2Args D{};
+    D.E = m->E;
+    D.nd = m->ndglno.p;
+    D.xnd = m->xndglno.p;
+    D.X = m->coords.p;
+    D.t = f->t;
+    D.f = f->source;
+    D.em = reinterpret_cast<float4*>(em);
+    for (int i = 0; i < 10; ++i)
+      for (int j = i; j < 10; ++j) {
+        const int q = sym10(i, j);
+        const double (*R)[3] = h.R[i][j];
+        D.S[q][0] = df_host(R[0][0]);
+        D.S[q][1] = df_host(R[1][1]);
+        D.S[q][2] = df_host(R[2][2]);
+        D.S[q][3] = df_host(R[0][1] + R[1][0]);
+        D.S[q][4] = df_host(R[0][2] + R[2][0]);
+        D.S[q][5] = df_host(R[1][2] + R[2][1]);
+        D.M[q] = df_host(h.M[i][j]);
+      }
+    D.qs = df_host(A.use_dt ? A.theta_dt : 0.0);
+    for (int a = 0; a < 3; ++a)
+      D.kdiag[a] = df_host(p->isotropic_diffusivity ? p->diffusivity[0] : p->diffusivity[4 * a]);
+    D.have_mass = p->have_mass;
+    D.have_src = p->have_source;
+    k_asm_p2_diffusion_df<<<grid_for(m->E, 128, esm), 128, 0, s>>>(D);
+  } else if (use_df) {
     RefTensors h;
     build_tensors(1, p->quad_degree, h);
     DfArgs D{};
