@@ -108,6 +108,7 @@ struct SellArgs {
   const int32_t* scol;
   const uint8_t* ghost;
   KspState* st;
+  const int16_t* soff;  // column - row (2-byte indices) when not null; else scol
 };
 
 struct CgPlan {

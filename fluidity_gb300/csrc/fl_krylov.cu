@@ -81,6 +81,8 @@ struct KrylovWork {
   int32_t nslices = 0;
   int64_t sell_len = 0;
   DevBuf<int32_t> swidth, sptr, scol, smap;
+  DevBuf<int16_t> soff;  // column - row as int16 when every entry fits (else unused)
+  bool sell16 = false;
   DevBuf<double> sval;
   DevBuf<float> sval32;
 };
@@ -363,7 +365,8 @@ __global__ void k_sell_width(const int32_t* __restrict__ findrm, int n, int nsli
 // Column indices and CSR positions of the padded layout (padding: the row's
 // own column and no CSR position).
 __global__ void k_sell_fill(const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm, int n,
-                            const int32_t* __restrict__ sptr, int32_t* __restrict__ scol, int32_t* __restrict__ smap) {
+                            const int32_t* __restrict__ sptr, int32_t* __restrict__ scol, int32_t* __restrict__ smap,
+                            int16_t* __restrict__ soff, int* __restrict__ wide) {
   note_launch();
   const int nsl = (n + kSlice - 1) / kSlice;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nsl * kSlice; r += gridDim.x * blockDim.x) {
@@ -373,13 +376,18 @@ __global__ void k_sell_fill(const int32_t* __restrict__ findrm, const int32_t* _
     const int b = real ? findrm[r] : 0, len = real ? findrm[r + 1] - b : 0;
     for (int j = 0; j < w; ++j) {
       const int64_t idx = (int64_t)sptr[sl] + (int64_t)j * kSlice + lane;
+      int c;
       if (j < len) {
-        scol[idx] = colm[b + j];
+        c = colm[b + j];
         smap[idx] = b + j;
       } else {
-        scol[idx] = real ? r : 0;
+        c = real ? r : 0;
         smap[idx] = -1;
       }
+      scol[idx] = c;
+      const int d = real ? c - r : 0;
+      if (d < -32768 || d > 32767) atomicOr(wide, 1);
+      soff[idx] = (int16_t)d;
     }
   }
 }
@@ -404,7 +412,11 @@ __device__ __forceinline__ double sell_row_dot(const SellArgs& A, const V* __res
   const int sl = r / kSlice, lane = r % kSlice;
   const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
   double s = 0.0;
-  for (int k = b; k < e; k += kSlice) s += (double)__ldg(sval + k) * (double)x[__ldg(A.scol + k)];
+  if (A.soff) {
+    for (int k = b; k < e; k += kSlice) s += (double)__ldg(sval + k) * (double)x[r + __ldg(A.soff + k)];
+  } else {
+    for (int k = b; k < e; k += kSlice) s += (double)__ldg(sval + k) * (double)x[__ldg(A.scol + k)];
+  }
   return s;
 }
 
@@ -874,7 +886,11 @@ __global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv,
     const int sl = row / kSlice, lane = row % kSlice;
     const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
     float s = 0.0f;
-    for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[__ldg(A.scol + k)], s);
+    if (A.soff) {
+      for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[row + __ldg(A.soff + k)], s);
+    } else {
+      for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[__ldg(A.scol + k)], s);
+    }
     const float pi = p[row];
     if (A.ghost && A.ghost[row]) s = piv * pi;
     w[row] = s;
@@ -1088,9 +1104,18 @@ static int ensure_sell(fl_mesh_t* m, KrylovWork* W, cudaStream_t s) {
   FL_TRY_CUDA(cudaStreamSynchronize(s));
   FL_TRY(W->scol.reserve(len));
   FL_TRY(W->smap.reserve(len));
+  FL_TRY(W->soff.reserve(len));
+  DevBuf<int> wide;
+  FL_TRY(wide.reserve(1));
+  FL_TRY_CUDA(cudaMemsetAsync(wide.p, 0, sizeof(int), s));
   k_sell_fill<<<grid_for((int64_t)nsl * kSlice, kThreads), kThreads, 0, s>>>(m->findrm.p, m->colm.p, n, W->sptr.p,
-                                                                             W->scol.p, W->smap.p);
+                                                                             W->scol.p, W->smap.p, W->soff.p,
+                                                                             wide.p);
   FL_TRY_CUDA(cudaGetLastError());
+  int h_wide = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&h_wide, wide.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  W->sell16 = h_wide == 0;  // every column within 32767 of its row: 2-byte indices
   W->nslices = nsl;
   W->sell_len = len;
   W->sell_ready = true;
@@ -1153,7 +1178,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   int outer = 0;
   const int chunk = 16;
   FL_TRY(ensure_sell(m, W, s));
-  SellArgs SA{n, W->sptr.p, W->scol.p, ghost, st};
+  SellArgs SA{n, W->sptr.p, W->scol.p, ghost, st, W->sell16 ? W->soff.p : nullptr};
   const unsigned gsl = grid_for(n, kThreads, 8);
   if (!mixed && o->ksp_type == 0) {
     FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
@@ -1428,7 +1453,7 @@ int cg_prepare(CgPlan& P, fl_mesh_t* m, const fl_solver_opts* o, const double* v
   FL_TRY(W->sval.reserve(M->sell_len));
   P.sell_len = M->sell_len;
   P.smap = M->smap.p;
-  P.SA = SellArgs{n, M->sptr.p, M->scol.p, ghost, W->st.p};
+  P.SA = SellArgs{n, M->sptr.p, M->scol.p, ghost, W->st.p, M->sell16 ? M->soff.p : nullptr};
   P.A = SpArgs{n, m->findrm.p, m->colm.p, val, ghost, W->st.p};
   return FL_OK;
 }
