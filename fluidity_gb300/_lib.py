@@ -83,7 +83,7 @@ EXPORTS = [
     "fl_batch_create", "fl_batch_add", "fl_batch_run", "fl_batch_size", "fl_batch_destroy",
     "fl_gnn_num_params", "fl_gnn_create", "fl_gnn_destroy", "fl_gnn_set_weights",
     "fl_gnn_get_weights", "fl_gnn_predict", "fl_gnn_gradients", "fl_gnn_train_step",
-    "fl_gnn_set_loss",
+    "fl_gnn_set_loss", "fl_gpu_pattern_register",
 ]
 
 _P = C.c_void_p
@@ -128,6 +128,7 @@ _SIGNATURES = {
     "fl_batch_destroy": (C.c_int, [_P]),
     "fl_gnn_num_params": (C.c_int, []),
     "fl_gnn_set_loss": (C.c_int, [_P, _P]),
+    "fl_gpu_pattern_register": (C.c_int, [_I32, _P, _P, _I32, C.POINTER(C.c_void_p)]),
     "fl_gnn_create": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "fl_gnn_destroy": (C.c_int, [_P]),
     "fl_gnn_set_weights": (C.c_int, [_P, _P, _I32]),

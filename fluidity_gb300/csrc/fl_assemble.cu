@@ -988,6 +988,7 @@ int dirichlet_launch(fl_mesh_t* m, int32_t nb, const int32_t* nodes, int32_t bas
 int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
              cudaStream_t s, double* em_override) {
   FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
+  FL_CHECK_ARG(m->E > 0 && (m->loc == 4 || m->loc == 10), "the handle has no elements (pattern-only handle)");
   FL_CHECK_ARG(p->quad_degree >= 1 && p->quad_degree <= 4, "quadrature degree 1..4");
   FL_CHECK_ARG(!p->have_advection || f->velocity, "advection needs a velocity field");
   FL_CHECK_ARG(!p->have_source || f->source, "source field missing");

@@ -607,6 +607,72 @@ static int upload_conn(const int32_t* host, int64_t n, int32_t base, int32_t nod
   return check_err(d_err, s, "connectivity out of range");
 }
 
+// Pattern check of a caller's CSR: rows strictly ascending and in range,
+// the diagonal's position (-1 when the row has none).
+__global__ void k_pattern_check(const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm, int32_t n,
+                                int32_t* __restrict__ centrm, ErrWord* err) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int b = findrm[i], e = findrm[i + 1];
+    int d = -1;
+    if (e < b) set_err(err, FL_ERR_ARG, i);
+    for (int k = b; k < e; ++k) {
+      const int c = colm[k];
+      if (c < 0 || c >= n || (k > b && colm[k - 1] >= c)) set_err(err, FL_ERR_ARG, i);
+      if (c == i) d = k;
+    }
+    centrm[i] = d;
+  }
+}
+
+// A handle that carries only a square CSR pattern (no elements): enough for
+// fl_gpu/dev_petsc_solve and fl_dev_csr_mult on a matrix read from a file.
+extern "C" int fl_gpu_pattern_register(int32_t n, const int32_t* findrm, const int32_t* colm, int32_t index_base,
+                                       fl_mesh* out) {
+  FL_CHECK_ARG(out && findrm && colm, "null argument");
+  FL_CHECK_ARG(n > 0, "row count");
+  FL_CHECK_ARG(index_base == 0 || index_base == 1, "index_base");
+  const int64_t nnz = (int64_t)findrm[n] - findrm[0];
+  FL_CHECK_ARG(findrm[0] == index_base && nnz > 0 && nnz < ((int64_t)1 << 31), "row pointers");
+  fl_mesh_t* m = new fl_mesh_t();
+  int st = FL_OK;
+  do {
+    cudaGetDevice(&m->device);
+    if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      set_error("cudaStreamCreate failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    cudaStream_t s = m->stream;
+    m->N = n;
+    m->nnz = nnz;
+    std::vector<int32_t> f(n + 1), c((size_t)nnz);
+    for (int i = 0; i <= n; ++i) f[i] = findrm[i] - index_base;
+    for (int64_t k = 0; k < nnz; ++k) c[k] = colm[k] - index_base;
+    int32_t mr = 0;
+    for (int i = 0; i < n; ++i) mr = std::max(mr, f[i + 1] - f[i]);
+    m->max_row = mr;
+    if ((st = m->err.reserve(1)) || (st = m->findrm.reserve(n + 1)) || (st = m->colm.reserve(nnz)) ||
+        (st = m->centrm.reserve(n)))
+      break;
+    if (cudaMemsetAsync(m->err.p, 0, sizeof(ErrWord), s) != cudaSuccess ||
+        cudaMemcpyAsync(m->findrm.p, f.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(m->colm.p, c.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      set_error("pattern upload failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    k_pattern_check<<<grid_for(n, 256), 256, 0, s>>>(m->findrm.p, m->colm.p, n, m->centrm.p, m->err.p);
+    if ((st = check_err(m->err.p, s, "CSR rows must hold ascending column indices in range")) != FL_OK) break;
+  } while (0);
+  if (st != FL_OK) {
+    fl_gpu_mesh_destroy(m);
+    return st;
+  }
+  *out = m;
+  return FL_OK;
+}
+
 extern "C" int fl_gpu_mesh_register(const fl_mesh_desc* d, fl_mesh* out) {
   FL_CHECK_ARG(d && out, "null descriptor/handle");
   FL_CHECK_ARG(d->loc == 4 || d->loc == 10, "loc must be 4 (P1) or 10 (P2)");

@@ -91,6 +91,15 @@ typedef struct {
  * in state / on the topology mesh. */
 int fl_gpu_mesh_register(const fl_mesh_desc* desc, fl_mesh* out);
 int fl_gpu_mesh_destroy(fl_mesh mesh);
+
+/* A handle holding only a square CSR pattern (n rows, findrm(n+1), colm, each
+ * row's columns strictly ascending; index_base as elsewhere) and no elements:
+ * for solving a system read from a file (the matrixdump that
+ * DumpMatrixEquation writes, femtools/Petsc_Tools.F90:1487-1504, and that
+ * tools/petsc_readnsolve.F90 reads) with fl_gpu/dev_petsc_solve and
+ * fl_dev_csr_mult.  Assembly on such a handle returns FL_ERR_ARG. */
+int fl_gpu_pattern_register(int32_t n, const int32_t* findrm, const int32_t* colm, int32_t index_base,
+                            fl_mesh* out);
 /* Sizes of the cached structures: entries of the sparsity and colour count. */
 int fl_gpu_mesh_info(fl_mesh mesh, int64_t* nnz, int32_t* ncolours);
 

@@ -189,3 +189,22 @@ def test_advdif_ten_steps_matches_oracle(O):
                                            ksp="gmres", restart=30, rtol=1e-10)
         To = To + 0.01 * dx
         assert np.abs(T - To).max() <= 1e-9 * np.abs(To).max()
+
+
+def test_readnsolve_of_a_dump_matches_petsc_solve(O, tmp_path):
+    """A matrixdump of the Dirichlet Poisson system, solved through a
+    pattern-only handle, gives the solve of the original csr_matrix."""
+    from fluidity_gb300 import petsc_io as P
+    m, X, val, rhs, ina = poisson(O, 8)
+    s = m.sparsity()
+    x = np.zeros(m.N)
+    opts = ft.solver_options(ksp="cg", rtol=1e-10)
+    rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina)
+    nf, nc, nv, b, x0 = P.petsc_matrix(s.findrm, s.colm, val, ina, rhs)
+    f = tmp_path / "matrixdump"
+    P.write_matrixdump(f, nf, nc, nv, b, x0)
+    y, drep = P.petsc_readnsolve(f, opts)
+    act = ina == 0
+    assert drep["reason"] == 2 and abs(drep["iterations"] - rep["iterations"]) <= 1
+    assert np.abs(y[act] - x[act]).max() <= 1e-8 * np.abs(x).max()
+    assert np.abs(y[~act]).max() == 0.0
