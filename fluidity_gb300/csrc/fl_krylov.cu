@@ -85,6 +85,63 @@ struct KrylovWork {
   bool sell16 = false;
   DevBuf<double> sval;
   DevBuf<float> sval32;
+  // stream on which iteration chunks are captured and replayed as graphs
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  ~KrylovWork() {
+    if (cs) cudaStreamDestroy(cs);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+  }
+};
+
+// A chunk of solver iterations as one CUDA graph: captured on the
+// workspace's own stream (the caller's stream may be the legacy default
+// stream, which cannot be captured) and replayed there, ordered after the
+// caller's stream by an event; end_graphs() orders the caller after it.
+struct IterGraph {
+  KrylovWork* W;
+  cudaStream_t caller;
+  cudaGraphExec_t exec = nullptr;
+  ~IterGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  template <class Body>
+  int build(Body body) {
+    if (!W->cs) {
+      FL_TRY_CUDA(cudaStreamCreateWithFlags(&W->cs, cudaStreamNonBlocking));
+      FL_TRY_CUDA(cudaEventCreateWithFlags(&W->ev_in, cudaEventDisableTiming));
+      FL_TRY_CUDA(cudaEventCreateWithFlags(&W->ev_out, cudaEventDisableTiming));
+    }
+    FL_TRY_CUDA(cudaEventRecord(W->ev_in, caller));
+    FL_TRY_CUDA(cudaStreamWaitEvent(W->cs, W->ev_in, 0));
+    cudaGraph_t g = nullptr;
+    FL_TRY_CUDA(cudaStreamBeginCapture(W->cs, cudaStreamCaptureModeThreadLocal));
+    body(W->cs);
+    const cudaError_t e = cudaStreamEndCapture(W->cs, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      set_error("iteration graph capture: %s", cudaGetErrorString(e));
+      return FL_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      set_error("iteration graph instantiation: %s", cudaGetErrorString(ei));
+      return FL_ERR_CUDA;
+    }
+    return FL_OK;
+  }
+  int launch() {
+    FL_TRY_CUDA(cudaGraphLaunch(exec, W->cs));
+    return FL_OK;
+  }
+  // caller's stream continues after everything enqueued on the graph stream
+  int join() {
+    FL_TRY_CUDA(cudaEventRecord(W->ev_out, W->cs));
+    FL_TRY_CUDA(cudaStreamWaitEvent(caller, W->ev_out, 0));
+    return FL_OK;
+  }
 };
 
 static KrylovWork* work_of(fl_mesh_t* m);
@@ -452,8 +509,20 @@ __global__ void k_cg_p(int n, const KspState* st, const double* __restrict__ z, 
   if (st->done) return;
   const int i = st->cg_i;
   const double coef = st->pcoef;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-    p[k] = i == 0 ? z[k] : z[k] + coef * p[k];
+  // two rows per thread (16-byte accesses); the last odd row separately
+  const int n2 = n >> 1;
+  const double2* z2 = reinterpret_cast<const double2*>(z);
+  double2* p2 = reinterpret_cast<double2*>(p);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
+    const double2 zv = z2[k];
+    if (i == 0) {
+      p2[k] = zv;
+    } else {
+      const double2 pv = p2[k];
+      p2[k] = make_double2(zv.x + coef * pv.x, zv.y + coef * pv.y);
+    }
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) p[n - 1] = i == 0 ? z[n - 1] : z[n - 1] + coef * p[n - 1];
 }
 
 __global__ void k_cg_ap(SellArgs A, const double* __restrict__ sval, const double* __restrict__ p,
@@ -501,7 +570,28 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
   const int i = st->cg_i;
   const double a = st->alpha;
   double zz = 0.0, zr = 0.0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+  // two rows per thread (16-byte accesses); the last odd row by the last thread
+  const int n2 = n >> 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
+    const double2 pv = reinterpret_cast<const double2*>(p)[k];
+    const double2 wv = reinterpret_cast<const double2*>(w)[k];
+    const double2 dv = reinterpret_cast<const double2*>(dinv)[k];
+    const double2 rv = reinterpret_cast<const double2*>(r)[k];
+    double2 yv = reinterpret_cast<double2*>(y)[k];
+    yv.x += a * pv.x;
+    yv.y += a * pv.y;
+    const double r0 = rv.x - a * wv.x, r1 = rv.y - a * wv.y;
+    const double z0 = r0 * dv.x, z1 = r1 * dv.y;
+    reinterpret_cast<double2*>(y)[k] = yv;
+    reinterpret_cast<double2*>(r)[k] = make_double2(r0, r1);
+    reinterpret_cast<double2*>(z)[k] = make_double2(z0, z1);
+    zz += z0 * z0;
+    zz += z1 * z1;
+    zr += z0 * r0;
+    zr += z1 * r1;
+  }
+  if ((n & 1) && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {
+    const int k = n - 1;
     y[k] += a * p[k];
     const double rk = r[k] - a * w[k];
     const double zk = rk * dinv[k];
@@ -870,8 +960,20 @@ __global__ void k_cg32_p(int n, const KspState* st, const float* __restrict__ z,
   if (st->done || st->hold) return;
   const int i = st->cg_i;
   const float coef = (float)st->pcoef;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-    p[k] = i == 0 ? z[k] : fmaf(coef, p[k], z[k]);
+  // four rows per thread (16-byte accesses); the last n % 4 rows by thread 0
+  const int n4 = n >> 2;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += gridDim.x * blockDim.x) {
+    const float4 zv = reinterpret_cast<const float4*>(z)[k];
+    if (i == 0) {
+      reinterpret_cast<float4*>(p)[k] = zv;
+    } else {
+      const float4 pv = reinterpret_cast<const float4*>(p)[k];
+      reinterpret_cast<float4*>(p)[k] = make_float4(fmaf(coef, pv.x, zv.x), fmaf(coef, pv.y, zv.y),
+                                                    fmaf(coef, pv.z, zv.z), fmaf(coef, pv.w, zv.w));
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    for (int k = n4 * 4; k < n; ++k) p[k] = i == 0 ? z[k] : fmaf(coef, p[k], z[k]);
 }
 
 __global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv, const float* __restrict__ p,
@@ -922,15 +1024,40 @@ __global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, cons
   const int i = st->cg_i;
   const float a = (float)st->alpha;
   df zzd = {0.0f, 0.0f}, zrd = {0.0f, 0.0f};
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    d[k] = fmaf(a, p[k], d[k]);
-    const float rk = fmaf(-a, w[k], r[k]);
-    const float zk = rk * dinv[k];
-    r[k] = rk;
-    z[k] = zk;
-    zzd = df_fma_ff(zk, zk, zzd);
-    zrd = df_fma_ff(zk, rk, zrd);
+  // four rows per thread (16-byte accesses); the last n % 4 rows by the last thread
+  const int n4 = n >> 2;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += gridDim.x * blockDim.x) {
+    const float4 pv = reinterpret_cast<const float4*>(p)[k];
+    const float4 wv = reinterpret_cast<const float4*>(w)[k];
+    const float4 dv = reinterpret_cast<const float4*>(dinv)[k];
+    const float4 rv = reinterpret_cast<const float4*>(r)[k];
+    const float4 cv = reinterpret_cast<const float4*>(d)[k];
+    const float pa[4] = {pv.x, pv.y, pv.z, pv.w}, wa[4] = {wv.x, wv.y, wv.z, wv.w};
+    const float da[4] = {dv.x, dv.y, dv.z, dv.w}, ra[4] = {rv.x, rv.y, rv.z, rv.w};
+    const float ca[4] = {cv.x, cv.y, cv.z, cv.w};
+    float ro[4], zo[4], co[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      co[u] = fmaf(a, pa[u], ca[u]);
+      ro[u] = fmaf(-a, wa[u], ra[u]);
+      zo[u] = ro[u] * da[u];
+      zzd = df_fma_ff(zo[u], zo[u], zzd);
+      zrd = df_fma_ff(zo[u], ro[u], zrd);
+    }
+    reinterpret_cast<float4*>(d)[k] = make_float4(co[0], co[1], co[2], co[3]);
+    reinterpret_cast<float4*>(r)[k] = make_float4(ro[0], ro[1], ro[2], ro[3]);
+    reinterpret_cast<float4*>(z)[k] = make_float4(zo[0], zo[1], zo[2], zo[3]);
   }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1)
+    for (int k = n4 * 4; k < n; ++k) {
+      d[k] = fmaf(a, p[k], d[k]);
+      const float rk = fmaf(-a, w[k], r[k]);
+      const float zk = rk * dinv[k];
+      r[k] = rk;
+      z[k] = zk;
+      zzd = df_fma_ff(zk, zk, zzd);
+      zrd = df_fma_ff(zk, rk, zrd);
+    }
   const double zz = block_sum_df<kThreads>(zzd, redf);
   const double zr = block_sum_df<kThreads>(zrd, redf);
   if (threadIdx.x == 0) {
@@ -1082,12 +1209,13 @@ static int group_for(const fl_mesh_t* m) {
     else KERNEL<4><<<gsp32, kThreads, 0, s>>>(__VA_ARGS__);                        \
   } while (0)
 
-#define FL_SPMV_DISPATCH(G, KERNEL, ...)                                            \
+#define FL_SPMV_DISPATCH_S(G, STREAM, KERNEL, ...)                                  \
   do {                                                                             \
-    if ((G) == 4) KERNEL<4><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                 \
-    else if ((G) == 2) KERNEL<2><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);            \
-    else KERNEL<1><<<gsp, kThreads, 0, s>>>(__VA_ARGS__);                          \
+    if ((G) == 4) KERNEL<4><<<gsp, kThreads, 0, STREAM>>>(__VA_ARGS__);            \
+    else if ((G) == 2) KERNEL<2><<<gsp, kThreads, 0, STREAM>>>(__VA_ARGS__);       \
+    else KERNEL<1><<<gsp, kThreads, 0, STREAM>>>(__VA_ARGS__);                     \
   } while (0)
+#define FL_SPMV_DISPATCH(G, KERNEL, ...) FL_SPMV_DISPATCH_S(G, s, KERNEL, __VA_ARGS__)
 
 // Sliced-ELL pattern of the mesh, built once and cached on the workspace.
 static int ensure_sell(fl_mesh_t* m, KrylovWork* W, cudaStream_t s) {
@@ -1145,7 +1273,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   const int n = m->N;
   const int G = group_for(m);
   const unsigned gsp = grid_for((int64_t)n * G, kThreads, 8);
-  const unsigned gv = grid_for(n, kThreads, 8);
+  const unsigned gv = grid_for(n, kThreads, 4);
   const int np = (int)std::max(gsp, gv);
   FL_TRY(W->b.reserve(n));
   FL_TRY(W->y.reserve(n));
@@ -1191,16 +1319,22 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     k_sell_values<<<grid_for(W->sell_len, kThreads), kThreads, 0, s>>>(W->sell_len, W->smap.p, val, W->sval.p,
                                                                          nullptr);
     k_cg_open<<<1, 32, 0, s>>>(st);
-    for (int i = 0; i < o->max_its; ++i) {
-      cg_iteration(n, st, SA, W, gv, gsl, np, s);
-      if ((i + 1) % chunk == 0 || i + 1 == o->max_its) {
-        FL_TRY_CUDA(cudaGetLastError());
-        int done = 0;
-        FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
-        FL_TRY_CUDA(cudaStreamSynchronize(s));
-        if (done) break;
-      }
+    FL_TRY_CUDA(cudaGetLastError());
+    // chunks of `chunk` iterations replayed as one graph until the device
+    // reports convergence or the iteration limit (iterations past the end
+    // of the solve return at once)
+    IterGraph gr{W, s};
+    FL_TRY(gr.build([&](cudaStream_t c) {
+      for (int k = 0; k < chunk; ++k) cg_iteration(n, st, SA, W, gv, gsl, np, c);
+    }));
+    for (int i = 0; i < o->max_its; i += chunk) {
+      FL_TRY(gr.launch());
+      int done = 0;
+      FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, W->cs));
+      FL_TRY_CUDA(cudaStreamSynchronize(W->cs));
+      if (done) break;
     }
+    FL_TRY(gr.join());
     FL_TRY_CUDA(cudaGetLastError());
   } else if (!mixed) {
     // GMRES(restart)
@@ -1285,26 +1419,37 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
         k_rel_commit<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
       };
       update();
-      for (int i = 0; i < 1000000; i += chunk) {
+      FL_TRY_CUDA(cudaGetLastError());
+      IterGraph gr{W, s};
+      FL_TRY(gr.build([&](cudaStream_t c) {
         for (int k = 0; k < chunk; ++k) {
-          k_cg32_p<<<gv, kThreads, 0, s>>>(n, st, W->z32.p, W->p32.p);
-          k_cg32_ap<<<gsl, kThreads, 0, s>>>(SA, W->sval32.p, piv32, W->p32.p, W->w32.p, W->part.p,
+          k_cg32_p<<<gv, kThreads, 0, c>>>(n, st, W->z32.p, W->p32.p);
+          k_cg32_ap<<<gsl, kThreads, 0, c>>>(SA, W->sval32.p, piv32, W->p32.p, W->w32.p, W->part.p,
                                               W->ticket.p);
-          k_cg32_xr<<<gv, kThreads, 0, s>>>(n, st, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
+          k_cg32_xr<<<gv, kThreads, 0, c>>>(n, st, W->p32.p, W->w32.p, W->dinv32.p, W->d32.p, W->r32.p,
                                              W->z32.p, W->part.p + 2 * np, W->ticket.p + 1);
         }
-        FL_TRY_CUDA(cudaGetLastError());
+      }));
+      const cudaStream_t c = W->cs;
+      auto update_c = [&]() {
+        FL_SPMV_DISPATCH_S(G, c, k_outer_resid, A, W->b.p, W->y.p, W->dinv.p, W->r32.p, W->z32.p, W->d32.p,
+                           W->part.p, (int)gsp);
+        k_rel_commit<<<1, kThreads, 0, c>>>(st, W->part.p, (int)gsp);
+      };
+      for (int i = 0; i < 1000000; i += chunk) {
+        FL_TRY(gr.launch());
         KspState h2;
-        FL_TRY_CUDA(cudaMemcpyAsync(&h2.its, &st->its, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
-        FL_TRY_CUDA(cudaMemcpyAsync(&h2.hold, &st->hold, sizeof(int), cudaMemcpyDeviceToHost, s));
-        FL_TRY_CUDA(cudaStreamSynchronize(s));
+        FL_TRY_CUDA(cudaMemcpyAsync(&h2.its, &st->its, sizeof(int) * 4, cudaMemcpyDeviceToHost, c));
+        FL_TRY_CUDA(cudaMemcpyAsync(&h2.hold, &st->hold, sizeof(int), cudaMemcpyDeviceToHost, c));
+        FL_TRY_CUDA(cudaStreamSynchronize(c));
         if (h2.done) break;
         if (h2.hold) {
-          k_add_correction<<<gv, kThreads, 0, s>>>(n, W->d32.p, W->y.p);
-          update();
+          k_add_correction<<<gv, kThreads, 0, c>>>(n, W->d32.p, W->y.p);
+          update_c();
           FL_TRY_CUDA(cudaGetLastError());
         }
       }
+      FL_TRY(gr.join());
       // a solve stopped inside the fp32 recurrence keeps its last correction
       k_add_correction<<<gv, kThreads, 0, s>>>(n, W->d32.p, W->y.p);
       FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
@@ -1434,7 +1579,7 @@ int cg_prepare(CgPlan& P, fl_mesh_t* m, const fl_solver_opts* o, const double* v
   P.n = n;
   P.G = group_for(m);
   P.gsp = grid_for((int64_t)n * P.G, kThreads, 8);
-  P.gv = grid_for(n, kThreads, 8);
+  P.gv = grid_for(n, kThreads, 4);
   P.gsl = grid_for(n, kThreads, 8);
   P.np = (int)std::max(P.gsp, P.gv);
   P.ksp = o->ksp_type;
