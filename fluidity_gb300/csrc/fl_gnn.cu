@@ -102,11 +102,13 @@ struct Inputs {
 
 __device__ __forceinline__ float scale_of(float v) { return v > 0.0f ? v : 1.0f; }
 
+// Features in FP32: the pressures and rhs rounded to float, times the float
+// reciprocal of their scale (no FP64 divide).
 __device__ __forceinline__ void features(const Inputs& in, int i, float* f) {
-  const double s = scale_of(in.scal[0]), sb = scale_of(in.scal[1]);
-  f[0] = (float)(in.p1[i] / s);
-  f[1] = (float)(in.p2[i] / s);
-  f[2] = (float)(in.b[i] / sb);
+  const float is = 1.0f / scale_of(in.scal[0]), isb = 1.0f / scale_of(in.scal[1]);
+  f[0] = __double2float_rn(in.p1[i]) * is;
+  f[1] = __double2float_rn(in.p2[i]) * is;
+  f[2] = __double2float_rn(in.b[i]) * isb;
   f[3] = (float)(2.0 * in.X[3 * i] - 1.0);
   f[4] = (float)(2.0 * in.X[3 * i + 1] - 1.0);
   f[5] = (float)(2.0 * in.X[3 * i + 2] - 1.0);
@@ -212,25 +214,39 @@ __global__ void __launch_bounds__(kTh) k_gnn_layer_fwd(int n, const int32_t* __r
     }
     {
       // four nodes per warp at a time, eight lanes per node, eight features
-      // (one 16-byte load) per lane
+      // (one 16-byte load) per lane.  The eight lanes of a node first load
+      // eight of its column indices, then every row load of those eight
+      // neighbours is issued before the sums (pattern order is kept).
       const int sub = lane >> 3, q = lane & 7;
       for (int r = w * 4 + sub; r < kTM; r += kTh / 8) {
         const int i = base + r;
         float s[8] = {};
-        if (i < n) {
-          const int e = findrm[i + 1];
-          for (int k = findrm[i]; k < e; ++k) {
-            const int j = colm[k];
-            if (j == i) continue;
-            const uint4 v = *reinterpret_cast<const uint4*>(Hin + (int64_t)j * kW + q * 8);
-            const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&v);
+        const int b = i < n ? findrm[i] : 0, e = i < n ? findrm[i + 1] : 0;
+        const int len = __reduce_max_sync(0xffffffffu, e - b);  // longest row of the warp's nodes
+        for (int k0 = 0; k0 < len; k0 += 8) {
+          const int kk = b + k0 + q;
+          const int jl = kk < e ? colm[kk] : -1;
+          uint4 v[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const float2 h = __bfloat1622float2(h2[u]);
-              s[2 * u] += h.x;
-              s[2 * u + 1] += h.y;
+          for (int u = 0; u < 8; ++u) {
+            const int j = __shfl_sync(0xffffffffu, jl, u, 8);
+            v[u] = (j >= 0 && j != i) ? *reinterpret_cast<const uint4*>(Hin + (int64_t)j * kW + q * 8)
+                                      : make_uint4(0u, 0u, 0u, 0u);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int j = __shfl_sync(0xffffffffu, jl, u, 8);
+            if (j < 0 || j == i) continue;
+            const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&v[u]);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const float2 h = __bfloat1622float2(h2[c]);
+              s[2 * c] += h.x;
+              s[2 * c + 1] += h.y;
             }
           }
+        }
+        if (i < n) {
           const float d = inv_deg[i];
 #pragma unroll
           for (int u = 0; u < 8; ++u) s[u] *= d;
@@ -454,14 +470,30 @@ __global__ void k_gnn_agg_bwd(int n, const int32_t* __restrict__ findrm, const i
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < n; j += nw) {
     float2 s = {0.0f, 0.0f};
-    const int e = findrm[j + 1];
-    for (int k = findrm[j]; k < e; ++k) {
-      const int i = colm[k];
-      if (i == j) continue;
-      const float d = inv_deg[i];
-      const float2 v = reinterpret_cast<const float2*>(dA + (int64_t)i * kW)[lane];
-      s.x = fmaf(d, v.x, s.x);
-      s.y = fmaf(d, v.y, s.y);
+    const int b = findrm[j], e = findrm[j + 1];
+    // the lanes load 32 column indices (and their inverse degrees) at a time,
+    // then the rows of up to eight neighbours are loaded before they are summed
+    for (int k0 = b; k0 < e; k0 += 32) {
+      const int il = k0 + lane < e ? colm[k0 + lane] : -1;
+      const float dl = il >= 0 ? inv_deg[il] : 0.0f;
+      const int cnt = min(32, e - k0);
+      for (int u0 = 0; u0 < cnt; u0 += 8) {
+        float2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = __shfl_sync(0xffffffffu, il, (u0 + u) & 31);
+          v[u] = (u0 + u < cnt && i != j) ? reinterpret_cast<const float2*>(dA + (int64_t)i * kW)[lane]
+                                           : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = __shfl_sync(0xffffffffu, il, (u0 + u) & 31);
+          const float d = __shfl_sync(0xffffffffu, dl, (u0 + u) & 31);
+          if (u0 + u >= cnt || i == j) continue;
+          s.x = fmaf(d, v[u].x, s.x);
+          s.y = fmaf(d, v[u].y, s.y);
+        }
+      }
     }
     float2* o = reinterpret_cast<float2*>(dHin + (int64_t)j * kW) + lane;
     const float2 c = *o;

@@ -84,19 +84,24 @@ def graph(findrm, colm):
 def forward(params, p1, p2, b, X, P, target=None, mask=None, rounded=True, K=None):
     R = bf16 if rounded else (lambda v: np.asarray(v, dtype=np.float64))
     q = unpack(params)
+    n = p1.size
+    feat = np.zeros((n, F))
     if rounded:
+        # FP32: the values rounded to float times the float reciprocal of the scale
         s = float(np.float32(np.max(np.abs(p1)))) or 1.0
         sb = float(np.float32(np.max(np.abs(b)))) or 1.0
         f32 = lambda v: np.asarray(v, dtype=np.float32).astype(np.float64)
+        i_s, i_sb = np.float32(1.0) / np.float32(s), np.float32(1.0) / np.float32(sb)
+        feat[:, 0] = (np.asarray(p1, np.float32) * i_s).astype(np.float64)
+        feat[:, 1] = (np.asarray(p2, np.float32) * i_s).astype(np.float64)
+        feat[:, 2] = (np.asarray(b, np.float32) * i_sb).astype(np.float64)
     else:
         s = float(np.max(np.abs(p1))) or 1.0
         sb = float(np.max(np.abs(b))) or 1.0
         f32 = lambda v: np.asarray(v, dtype=np.float64)
-    n = p1.size
-    feat = np.zeros((n, F))
-    feat[:, 0] = f32(p1 / s)
-    feat[:, 1] = f32(p2 / s)
-    feat[:, 2] = f32(b / sb)
+        feat[:, 0] = p1 / s
+        feat[:, 1] = p2 / s
+        feat[:, 2] = b / sb
     feat[:, 3:6] = f32(2.0 * X - 1.0)
     Fm = R(feat)
     c = {"s": s, "F": Fm, "H": [], "Z": [], "A": [], "X": []}
