@@ -84,6 +84,7 @@ EXPORTS = [
     "fl_gnn_num_params", "fl_gnn_create", "fl_gnn_destroy", "fl_gnn_set_weights",
     "fl_gnn_get_weights", "fl_gnn_predict", "fl_gnn_gradients", "fl_gnn_train_step",
     "fl_gnn_set_loss", "fl_gpu_pattern_register",
+    "fl_amg_create", "fl_amg_solve", "fl_amg_levels", "fl_amg_destroy",
 ]
 
 _P = C.c_void_p
@@ -129,6 +130,10 @@ _SIGNATURES = {
     "fl_gnn_num_params": (C.c_int, []),
     "fl_gnn_set_loss": (C.c_int, [_P, _P]),
     "fl_gpu_pattern_register": (C.c_int, [_I32, _P, _P, _I32, C.POINTER(C.c_void_p)]),
+    "fl_amg_create": (C.c_int, [_P, _P, _P, _P, C.POINTER(C.c_void_p)]),
+    "fl_amg_solve": (C.c_int, [_P, C.POINTER(SolverOpts), _P, _P, C.POINTER(SolveReport), _P]),
+    "fl_amg_levels": (C.c_int, [_P, C.POINTER(C.c_int32), _P, _P, _I32]),
+    "fl_amg_destroy": (C.c_int, [_P]),
     "fl_gnn_create": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "fl_gnn_destroy": (C.c_int, [_P]),
     "fl_gnn_set_weights": (C.c_int, [_P, _P, _I32]),

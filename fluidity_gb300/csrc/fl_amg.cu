@@ -1,0 +1,1408 @@
+// fl_amg.cu -- smoothed-aggregation algebraic multigrid preconditioner for
+// the CG solve of the pressure (Poisson) systems.
+//
+// The stronger preconditioner of petsc_solve's options (femtools/Solvers.F90:
+// 1827-1969, PCGAMG), restated on the GPU with the structure of PETSc's GAMG
+// defaults:
+//   * aggregation by a distance-2 maximal independent set of the matrix graph
+//     (Luby's algorithm with hashed priorities, Bell, Dalton and Olson 2012),
+//     rows without off-diagonal couplings (Dirichlet ghost rows) left out;
+//   * one Jacobi smoothing step of the piecewise-constant prolongator,
+//     P = (I - omega D^-1 A) P0, omega = 4 / (3 rho), rho a Gershgorin bound
+//     on the spectrum of D^-1 A;
+//   * Galerkin coarse operators A_c = P^T A P;
+//   * Chebyshev(2)-Jacobi smoothing on [0.1 rho, 1.1 rho] before and after the
+//     coarse correction (a symmetric V-cycle), and a dense direct solve on the
+//     coarsest level.
+// Every sparse product sums its terms in a fixed order (candidates sorted by
+// column and then by their position), so the hierarchy and the solve are
+// deterministic.  The solve is PCG with PETSc's default convergence test on
+// the preconditioned residual norm, petsc_solve's ghost semantics and rhs
+// lifting, as the Jacobi solve of fl_krylov.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "fl_internal.cuh"
+#include "fl_device.cuh"
+
+namespace fl {
+
+unsigned long long launches_amg() { return unit_launches(); }
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kCap = 8192;         // candidate entries of one row of a sparse product
+constexpr int kMaxCoarse = 512;    // rows of the coarsest level (dense inverse)
+constexpr int kMaxLevels = 12;
+
+struct Csr {
+  int32_t n = 0, m = 0;  // rows, columns
+  int64_t nnz = 0;
+  DevBuf<int32_t> ptr, col;
+  DevBuf<double> val;
+};
+
+// ------------------------------------------------------------ helpers --
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+template <int NT>
+__device__ double block_sum_d(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  v = 0.0;
+  if (w == 0) {
+    v = lane < NT / 32 ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;
+}
+
+// y = A x for one row by G lanes (rows sorted; terms in pattern order per lane)
+template <int G>
+__device__ __forceinline__ double csr_row(const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                          const double* __restrict__ val, const double* __restrict__ x, int row,
+                                          int sub, bool valid) {
+  int b = 0, e = 0;
+  if (valid) {
+    b = __ldg(ptr + row);
+    e = __ldg(ptr + row + 1);
+  }
+  double s = 0.0;
+  for (int k = b + sub; k < e; k += G) s += __ldg(val + k) * __ldg(x + __ldg(col + k));
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+// ------------------------------------------------------ level-0 matrix --
+// min / max of |a_ii| over every row (ghost pivot, Petsc_Tools.F90:972-983),
+// as ordered bits of non-negative doubles
+__global__ void k_diag_range(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, unsigned long long* mm) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
+      if (col[k] == i) d = fabs(val[k]);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    atomicMin(mm, b);
+    atomicMax(mm + 1, b);
+  }
+}
+
+// The matrix PETSc is given: ghost rows hold only the ghost pivot on the
+// diagonal, ghost columns are dropped (zero) in active rows.
+__global__ void k_mask(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                       const double* __restrict__ val, const uint8_t* __restrict__ ghost,
+                       const unsigned long long* __restrict__ mm, double* __restrict__ out) {
+  note_launch();
+  const double mind = __longlong_as_double((long long)mm[0]), maxd = __longlong_as_double((long long)mm[1]);
+  const double piv = sqrt((maxd + mind) * maxd / 2.0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const bool gi = ghost && ghost[i];
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      double v;
+      if (gi) v = j == i ? piv : 0.0;
+      else v = (ghost && ghost[j]) ? 0.0 : val[k];
+      out[k] = v;
+    }
+  }
+}
+
+// 1/a_ii (0 when the row has no diagonal) and the Gershgorin bound of the
+// row of D^-1 A: sum_j |a_ij| / |a_ii|
+__global__ void k_dinv_gersh(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, double* __restrict__ dinv,
+                             unsigned long long* __restrict__ gmax) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double d = 0.0, s = 0.0;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      s += fabs(val[k]);
+      if (col[k] == i) d = val[k];
+    }
+    dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
+    const double g = d != 0.0 ? s / fabs(d) : 0.0;
+    atomicMax(gmax, (unsigned long long)__double_as_longlong(g));
+  }
+}
+
+// ------------------------------------------------------- aggregation --
+// tuple = state (2 bits: 2 in the set, 1 undecided, 0 out) | hash (30) | index
+__device__ __forceinline__ unsigned long long tup(uint32_t st, uint32_t h, uint32_t i) {
+  return ((unsigned long long)st << 62) | ((unsigned long long)(h & 0x3fffffffu) << 32) | i;
+}
+
+__device__ __forceinline__ bool coupled(const double* __restrict__ val, int k) { return val[k] != 0.0; }
+
+__global__ void k_mis_init(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                           const double* __restrict__ val, uint32_t seed, unsigned long long* __restrict__ t,
+                           int32_t* __restrict__ agg) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    bool any = false;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) any = any || (col[k] != i && coupled(val, k));
+    t[i] = tup(any ? 1u : 0u, hash32((uint32_t)i * 2654435761u + seed), (uint32_t)i);
+    agg[i] = -1;
+  }
+}
+
+// tout_i = max of tin over i and its coupled neighbours
+__global__ void k_mis_max(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                          const double* __restrict__ val, const unsigned long long* __restrict__ tin,
+                          unsigned long long* __restrict__ tout) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned long long m = tin[i];
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
+      if (col[k] != i && coupled(val, k)) m = max(m, tin[col[k]]);
+    tout[i] = m;
+  }
+}
+
+__global__ void k_mis_update(int n, unsigned long long* __restrict__ t, const unsigned long long* __restrict__ t2,
+                             int* __restrict__ left) {
+  note_launch();
+  int c = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long v = t[i];
+    if ((v >> 62) != 1ull) continue;
+    if (t2[i] == v) t[i] = (v & ~(3ull << 62)) | (2ull << 62);  // into the set
+    else if ((t2[i] >> 62) == 2ull) t[i] = v & ~(3ull << 62);   // within distance 2 of the set
+    else ++c;
+  }
+  if (c) atomicAdd(left, c);
+}
+
+__global__ void k_mis_flag(int n, const unsigned long long* __restrict__ t, int32_t* __restrict__ flag) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    flag[i] = (t[i] >> 62) == 2ull ? 1 : 0;
+}
+
+// distance 1: the highest set member among i and its neighbours
+__global__ void k_agg1(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                       const double* __restrict__ val, const unsigned long long* __restrict__ t,
+                       const int32_t* __restrict__ rank, int32_t* __restrict__ agg,
+                       unsigned long long* __restrict__ pick) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned long long best = (t[i] >> 62) == 2ull ? t[i] : 0ull;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      if (j != i && coupled(val, k) && (t[j] >> 62) == 2ull) best = max(best, t[j]);
+    }
+    pick[i] = best;
+    if (best) agg[i] = rank[(uint32_t)best];
+  }
+}
+
+// distance 2: the highest pick among the neighbours
+__global__ void k_agg2(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                       const double* __restrict__ val, const unsigned long long* __restrict__ pick,
+                       const int32_t* __restrict__ rank, int32_t* __restrict__ agg, ErrWord* err) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (agg[i] >= 0) continue;
+    bool any = false;
+    unsigned long long best = 0ull;
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      if (j != i && coupled(val, k)) {
+        any = true;
+        best = max(best, pick[j]);
+      }
+    }
+    if (!any) continue;  // uncoupled row: no aggregate
+    if (!best) {
+      set_err(err, FL_ERR_UNSUPPORTED, i);  // not reachable after a maximal set
+      continue;
+    }
+    agg[i] = rank[(uint32_t)best];
+  }
+}
+
+// P0: one entry (agg(i), 1) per aggregated row
+__global__ void k_p0_count(int n, const int32_t* __restrict__ agg, int32_t* __restrict__ cnt) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) cnt[i] = agg[i] >= 0;
+}
+__global__ void k_p0_fill(int n, const int32_t* __restrict__ agg, const int32_t* __restrict__ ptr,
+                          int32_t* __restrict__ col, double* __restrict__ val) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (agg[i] >= 0) {
+      col[ptr[i]] = agg[i];
+      val[ptr[i]] = 1.0;
+    }
+}
+
+// ------------------------------------------- deterministic sparse product --
+// Row i of C = L B: candidates (col_B(q), l_ik b_kq) for k in row i of L and q
+// in row k of B, sorted by (column, candidate position), summed per column in
+// that order.  One block per row; pass 0 counts the columns, pass 1 fills.
+struct ProdArgs {
+  int32_t n;
+  const int32_t *lp, *lc;
+  const double* lv;
+  const int32_t *bp, *bc;
+  const double* bv;
+  int32_t* cnt;       // pass 0
+  const int32_t* cp;  // pass 1
+  int32_t* cc;
+  double* cv;
+  ErrWord* err;
+};
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_spgemm(ProdArgs A, int pass) {
+  note_launch();
+  extern __shared__ unsigned char sm[];
+  unsigned long long* key = reinterpret_cast<unsigned long long*>(sm);  // [kCap]
+  double* v = reinterpret_cast<double*>(key + kCap);                     // [kCap]
+  __shared__ int s_n, s_tot;
+  __shared__ int s_scan[NT];
+  for (int row = blockIdx.x; row < A.n; row += gridDim.x) {
+    // candidate offsets: lane-parallel prefix over the row of L
+    const int lb = A.lp[row], le = A.lp[row + 1];
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    for (int k0 = lb; k0 < le; k0 += NT) {
+      const int k = k0 + threadIdx.x;
+      const int len = k < le ? A.bp[A.lc[k] + 1] - A.bp[A.lc[k]] : 0;
+      s_scan[threadIdx.x] = len;
+      __syncthreads();
+      for (int o = 1; o < NT; o <<= 1) {
+        const int x = threadIdx.x >= o ? s_scan[threadIdx.x - o] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += x;
+        __syncthreads();
+      }
+      const int base = s_n, excl = s_scan[threadIdx.x] - len;
+      if (k < le) {
+        const int kk = A.lc[k];
+        const double l = A.lv[k];
+        const int qb = A.bp[kk];
+        for (int q = 0; q < len; ++q) {
+          const int pos = base + excl + q;
+          if (pos < kCap) {
+            key[pos] = ((unsigned long long)(uint32_t)A.bc[qb + q] << 32) | (uint32_t)pos;
+            v[pos] = l * A.bv[qb + q];
+          }
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == NT - 1) s_n = base + s_scan[NT - 1];
+      __syncthreads();
+    }
+    const int nc = s_n;
+    if (nc > kCap) {  // left to k_spgemm_long
+      if (pass == 0 && threadIdx.x == 0) A.cnt[row] = -1;
+      __syncthreads();
+      continue;
+    }
+    int pw = 1;
+    while (pw < nc) pw <<= 1;
+    for (int k = nc + threadIdx.x; k < pw; k += NT) key[k] = ~0ull;
+    __syncthreads();
+    // bitonic sort of the keys
+    for (int size = 2; size <= pw; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int k = threadIdx.x; k < pw; k += NT) {
+          const int l = k ^ stride;
+          if (l > k) {
+            const unsigned long long a = key[k], b = key[l];
+            const bool up = (k & size) == 0;
+            if ((a > b) == up) {
+              key[k] = b;
+              key[l] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    // segment heads
+    if (threadIdx.x == 0) s_tot = 0;
+    __syncthreads();
+    int mine = 0;
+    for (int k = threadIdx.x; k < nc; k += NT) mine += (k == 0 || (key[k] >> 32) != (key[k - 1] >> 32));
+    if (mine) atomicAdd(&s_tot, mine);
+    __syncthreads();
+    if (pass == 0) {
+      if (threadIdx.x == 0) A.cnt[row] = s_tot;
+      __syncthreads();
+      continue;
+    }
+    // pass 1: output slot of each head = number of heads before it
+    const int out0 = A.cp[row];
+    for (int k0 = 0; k0 < nc; k0 += NT) {
+      const int k = k0 + threadIdx.x;
+      const int head = k < nc && (k == 0 || (key[k] >> 32) != (key[k - 1] >> 32));
+      s_scan[threadIdx.x] = head;
+      __syncthreads();
+      for (int o = 1; o < NT; o <<= 1) {
+        const int x = threadIdx.x >= o ? s_scan[threadIdx.x - o] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += x;
+        __syncthreads();
+      }
+      if (head) {
+        const int slot = (k0 == 0 ? 0 : s_tot) + s_scan[threadIdx.x] - 1;
+        const uint32_t c = (uint32_t)(key[k] >> 32);
+        double sum = 0.0;
+        for (int q = k; q < nc && (uint32_t)(key[q] >> 32) == c; ++q) sum += v[(uint32_t)key[q]];
+        A.cc[out0 + slot] = (int32_t)c;
+        A.cv[out0 + slot] = sum;
+      }
+      __syncthreads();
+      if (threadIdx.x == NT - 1) s_tot = (k0 == 0 ? 0 : s_tot) + s_scan[NT - 1];
+      __syncthreads();
+    }
+  }
+}
+
+// Rows with more candidates than one block's shared memory holds: one thread
+// per row inserts the candidates, in their generation order, into a sorted
+// list of distinct columns (at most kLongCols) in global scratch, adding
+// values of equal columns in that order.  pass 0 writes the counts, pass 1
+// the row.
+constexpr int kLongCols = 4096;
+__global__ void k_spgemm_long(ProdArgs A, const int32_t* __restrict__ rows, int nrows, int pass,
+                              int32_t* __restrict__ scol, double* __restrict__ sval) {
+  note_launch();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nrows; t += gridDim.x * blockDim.x) {
+    const int row = rows[t];
+    int32_t* uc = scol + (int64_t)t * kLongCols;
+    double* uv = sval + (int64_t)t * kLongCols;
+    int nu = 0;
+    bool over = false;
+    for (int k = A.lp[row]; k < A.lp[row + 1] && !over; ++k) {
+      const int kk = A.lc[k];
+      const double l = A.lv[k];
+      for (int q = A.bp[kk]; q < A.bp[kk + 1]; ++q) {
+        const int c = A.bc[q];
+        const double v = l * A.bv[q];
+        int lo = 0, hi = nu;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (uc[mid] < c) lo = mid + 1;
+          else hi = mid;
+        }
+        if (lo < nu && uc[lo] == c) {
+          uv[lo] += v;
+        } else {
+          if (nu == kLongCols) {
+            over = true;
+            break;
+          }
+          for (int z = nu; z > lo; --z) {
+            uc[z] = uc[z - 1];
+            uv[z] = uv[z - 1];
+          }
+          uc[lo] = c;
+          uv[lo] = v;
+          ++nu;
+        }
+      }
+    }
+    if (over) {
+      set_err(A.err, FL_ERR_UNSUPPORTED, row);
+      nu = 0;
+    }
+    if (pass == 0) {
+      A.cnt[row] = nu;
+    } else {
+      const int o = A.cp[row];
+      for (int z = 0; z < nu; ++z) {
+        A.cc[o + z] = uc[z];
+        A.cv[o + z] = uv[z];
+      }
+    }
+  }
+}
+
+__global__ void k_long_rows(int n, const int32_t* __restrict__ cnt, int32_t* __restrict__ list, int* __restrict__ nl) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (cnt[i] < 0) list[atomicAdd(nl, 1)] = i;
+}
+
+// Transpose (rows of C = columns of B): slots by atomics, then each column's
+// entries sorted by row (insertion sort; columns are short).
+__global__ void k_t_count(int64_t nnz, const int32_t* __restrict__ col, int32_t* __restrict__ cnt) {
+  note_launch();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(cnt + col[k], 1);
+}
+__global__ void k_t_fill(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                         const double* __restrict__ val, const int32_t* __restrict__ tp, int32_t* __restrict__ fill,
+                         int32_t* __restrict__ tc, double* __restrict__ tv) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+      const int j = col[k];
+      const int s = tp[j] + atomicAdd(fill + j, 1);
+      tc[s] = i;
+      tv[s] = val[k];
+    }
+}
+__global__ void k_t_sort(int m, const int32_t* __restrict__ tp, int32_t* __restrict__ tc, double* __restrict__ tv) {
+  note_launch();
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+    const int b = tp[j], e = tp[j + 1];
+    for (int k = b + 1; k < e; ++k) {
+      const int c = tc[k];
+      const double x = tv[k];
+      int q = k - 1;
+      while (q >= b && tc[q] > c) {
+        tc[q + 1] = tc[q];
+        tv[q + 1] = tv[q];
+        --q;
+      }
+      tc[q + 1] = c;
+      tv[q + 1] = x;
+    }
+  }
+}
+
+// P = P0 - omega D^-1 (A P0) on the pattern of A P0
+__global__ void k_smooth_p(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                           double* __restrict__ val, const int32_t* __restrict__ agg,
+                           const double* __restrict__ dinv, double omega) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k)
+      val[k] = (col[k] == agg[i] ? 1.0 : 0.0) - omega * dinv[i] * val[k];
+}
+
+// --------------------------------------------------------- sliced ELL --
+// The finest operator in slices of 32 rows, each padded to its longest row
+// and stored column-major (entry j of the slice's rows contiguous), so that
+// one thread per row reads coalesced values; padding has the row's own column
+// and value 0.  Terms are summed in the row's CSR order.
+struct SellOp {
+  int32_t n;
+  const int32_t* sptr;
+  const int32_t* col;
+  const double* val;
+};
+
+__global__ void k_sl_width(int n, const int32_t* __restrict__ ptr, int32_t* __restrict__ w) {
+  note_launch();
+  const int nsl = (n + 31) / 32;
+  for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < nsl; sl += gridDim.x * blockDim.x) {
+    int m = 0;
+    for (int r = sl * 32; r < min(n, sl * 32 + 32); ++r) m = max(m, ptr[r + 1] - ptr[r]);
+    w[sl] = m * 32;
+  }
+}
+
+__global__ void k_sl_fill(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                          const double* __restrict__ val, const int32_t* __restrict__ sptr, int32_t* __restrict__ scol,
+                          double* __restrict__ sval) {
+  note_launch();
+  const int nsl = (n + 31) / 32;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nsl * 32; r += gridDim.x * blockDim.x) {
+    const int sl = r / 32, lane = r % 32;
+    const int w = (sptr[sl + 1] - sptr[sl]) / 32;
+    const bool real = r < n;
+    const int b = real ? ptr[r] : 0, len = real ? ptr[r + 1] - b : 0;
+    for (int j = 0; j < w; ++j) {
+      const int64_t idx = (int64_t)sptr[sl] + (int64_t)j * 32 + lane;
+      scol[idx] = j < len ? col[b + j] : (real ? r : 0);
+      sval[idx] = j < len ? val[b + j] : 0.0;
+    }
+  }
+}
+
+__device__ __forceinline__ double sell_dot(const SellOp& S, const double* __restrict__ x, int r) {
+  const int sl = r >> 5;
+  const int b = __ldg(S.sptr + sl) + (r & 31), e = __ldg(S.sptr + sl + 1);
+  double s = 0.0;
+  for (int k = b; k < e; k += 32) s += __ldg(S.val + k) * __ldg(x + __ldg(S.col + k));
+  return s;
+}
+
+__global__ void k_cheb_sl(SellOp A, const double* __restrict__ dinv, const double* __restrict__ b,
+                          const double* __restrict__ x, double* __restrict__ d, double c1, double c2,
+                          double* __restrict__ xo) {
+  note_launch();
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+    const double r = b[row] - sell_dot(A, x, row);
+    const double dn = (c1 != 0.0 ? c1 * d[row] : 0.0) + c2 * dinv[row] * r;
+    d[row] = dn;
+    xo[row] = x[row] + dn;
+  }
+}
+
+__global__ void k_resid_sl(SellOp A, const double* __restrict__ b, const double* __restrict__ x,
+                           double* __restrict__ r) {
+  note_launch();
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x)
+    r[row] = b[row] - sell_dot(A, x, row);
+}
+
+// ----------------------------------------------------------- V-cycle --
+struct Op {  // a CSR operator and its row grouping
+  int32_t n;
+  const int32_t* ptr;
+  const int32_t* col;
+  const double* val;
+};
+
+// x = d = (D^-1 b) / theta   (first Chebyshev step from a zero guess)
+__global__ void k_cheb0(int n, const double* __restrict__ dinv, const double* __restrict__ b, double ith,
+                        double* __restrict__ x, double* __restrict__ d) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = dinv[i] * b[i] * ith;
+    d[i] = v;
+    x[i] = v;
+  }
+}
+
+// r = b - A x;  d = c1 d + c2 D^-1 r;  xo = x + d   (xo != x)
+template <int G>
+__global__ void k_cheb(Op A, const double* __restrict__ dinv, const double* __restrict__ b,
+                       const double* __restrict__ x, double* __restrict__ d, double c1, double c2,
+                       double* __restrict__ xo) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    const double ax = csr_row<G>(A.ptr, A.col, A.val, x, row, sub, row < A.n);
+    if (row < A.n && sub == 0) {
+      const double r = b[row] - ax;
+      const double dn = (c1 != 0.0 ? c1 * d[row] : 0.0) + c2 * dinv[row] * r;
+      d[row] = dn;
+      xo[row] = x[row] + dn;
+    }
+  }
+}
+
+// r = b - A x
+template <int G>
+__global__ void k_resid(Op A, const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ r) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    const double ax = csr_row<G>(A.ptr, A.col, A.val, x, row, sub, row < A.n);
+    if (row < A.n && sub == 0) r[row] = b[row] - ax;
+  }
+}
+
+// y = A x (+ z when z is not null)
+template <int G>
+__global__ void k_spmv_add(Op A, const double* __restrict__ x, const double* z, double* y) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    const double ax = csr_row<G>(A.ptr, A.col, A.val, x, row, sub, row < A.n);
+    if (row < A.n && sub == 0) y[row] = (z ? z[row] : 0.0) + ax;
+  }
+}
+
+// coarsest level: x = Ainv b, one warp per row, terms in column order
+__global__ void k_dense(int n, const double* __restrict__ inv, const double* __restrict__ b, double* __restrict__ x) {
+  note_launch();
+  const int lane = threadIdx.x & 31;
+  for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += gridDim.x * (blockDim.x >> 5)) {
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s += inv[(int64_t)row * n + j] * b[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[row] = s;
+  }
+}
+
+// ------------------------------------------------------------ PCG --
+struct AmgState {
+  double rtol, atol, dtol, rnorm0, ttol, rnorm;
+  double alpha, beta, betaold, dpi, dpiold, pcoef;
+  double true_r2, b2;
+  int its, max_its, reason, done, guess_zero, i;
+};
+
+__device__ void amg_converged(AmgState& S, int it, double rn, double bn) {
+  if (it == 0) {
+    S.rnorm0 = S.guess_zero ? rn : (bn > 0.0 ? bn : rn);
+    S.ttol = fmax(S.rtol * S.rnorm0, S.atol);
+  }
+  S.rnorm = rn;
+  if (rn != rn) S.reason = FL_DIVERGED_NANORINF;
+  else if (rn <= S.ttol) S.reason = rn < S.atol ? FL_CONVERGED_ATOL : FL_CONVERGED_RTOL;
+  else if (rn >= S.dtol * S.rnorm0) S.reason = FL_DIVERGED_DTOL;
+  if (S.reason) S.done = 1;
+}
+
+// b = rhs - A (rhs on ghosts) on active rows, 0 on ghosts; y = guess (0 on ghosts)
+template <int G>
+__global__ void k_amg_lift(Op A, const uint8_t* __restrict__ ghost, const double* __restrict__ rhs,
+                           const double* __restrict__ x0, int guess_zero, double* __restrict__ b,
+                           double* __restrict__ y) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    double s = 0.0;
+    if (row < A.n && ghost) {
+      for (int k = __ldg(A.ptr + row) + sub; k < __ldg(A.ptr + row + 1); k += G) {
+        const int j = A.col[k];
+        if (ghost[j]) s += A.val[k] * rhs[j];
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    if (row < A.n && sub == 0) {
+      const bool g = ghost && ghost[row];
+      b[row] = g ? 0.0 : rhs[row] - s;
+      y[row] = (guess_zero || g) ? 0.0 : x0[row];
+    }
+  }
+}
+
+// partials of a.b and c.d over blocks (two dots in one pass; c may be null)
+__global__ void k_dots(int n, const double* __restrict__ a, const double* __restrict__ b,
+                       const double* __restrict__ c, const double* __restrict__ d, double* __restrict__ part) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  double s = 0.0, t = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    s += a[i] * b[i];
+    if (c) t += c[i] * d[i];
+  }
+  s = block_sum_d<kT>(s, red);
+  t = block_sum_d<kT>(t, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s;
+    part[gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// w = A p and partials of p.w
+template <int G>
+__global__ void k_amg_ap(Op A, const AmgState* st, const double* __restrict__ p, double* __restrict__ w,
+                         double* __restrict__ part) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  if (st->done) return;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
+  double pw = 0.0;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    const double s = csr_row<G>(A.ptr, A.col, A.val, p, row, sub, row < A.n);
+    if (row < A.n && sub == 0) {
+      w[row] = s;
+      pw += p[row] * s;
+    }
+  }
+  pw = block_sum_d<kT>(pw, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = pw;
+}
+
+// w = A p and partials of p.w on the sliced-ELL finest operator
+__global__ void k_amg_ap_sl(SellOp A, const AmgState* st, const double* __restrict__ p, double* __restrict__ w,
+                            double* __restrict__ part) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  if (st->done) return;
+  double pw = 0.0;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
+    const double s = sell_dot(A, p, row);
+    w[row] = s;
+    pw += p[row] * s;
+  }
+  pw = block_sum_d<kT>(pw, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = pw;
+}
+
+__device__ double sum_parts(const double* __restrict__ part, int n, double* red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += kT) s += part[i];
+  return block_sum_d<kT>(s, red);
+}
+
+// alpha = beta / p.w (KSPSolve_CG)
+__global__ void k_amg_alpha(AmgState* st, const double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  if (st->done) return;
+  const double dpi = sum_parts(part, nparts, red);
+  if (threadIdx.x) return;
+  AmgState& S = *st;
+  S.dpiold = S.dpi;
+  S.dpi = dpi;
+  S.betaold = S.beta;
+  if (dpi == 0.0 || (S.i > 0 && dpi * S.dpiold <= 0.0)) {
+    S.reason = FL_DIVERGED_INDEFINITE_MAT;
+    S.done = 1;
+  } else {
+    S.alpha = S.beta / dpi;
+  }
+}
+
+__global__ void k_amg_xr(int n, const AmgState* st, const double* __restrict__ p, const double* __restrict__ w,
+                         double* __restrict__ y, double* __restrict__ r) {
+  note_launch();
+  if (st->done) return;
+  const double a = st->alpha;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    y[i] += a * p[i];
+    r[i] -= a * w[i];
+  }
+}
+
+// after z = B r: convergence test on ||z|| at iteration i+1, beta = z.r
+__global__ void k_amg_beta(AmgState* st, const double* __restrict__ part, int nparts, int first,
+                           const double* __restrict__ bnorm) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  if (st->done) return;
+  const double zz = sum_parts(part, nparts, red);
+  const double zr = sum_parts(part + nparts, nparts, red);
+  if (threadIdx.x) return;
+  AmgState& S = *st;
+  if (first) {
+    S.its = 0;
+    amg_converged(S, 0, sqrt(zz), bnorm ? *bnorm : 0.0);
+    S.beta = zr;
+    S.pcoef = 0.0;
+    S.i = 0;
+    if (!S.done && zr == 0.0) {
+      S.reason = FL_CONVERGED_ATOL;
+      S.done = 1;
+    }
+    return;
+  }
+  const int it = S.i + 1;
+  S.its = it;
+  amg_converged(S, it, sqrt(zz), 0.0);
+  if (S.done) return;
+  if (it >= S.max_its) {
+    S.reason = FL_DIVERGED_ITS;
+    S.done = 1;
+    return;
+  }
+  S.beta = zr;
+  if (zr * S.betaold < 0.0) {
+    S.reason = FL_DIVERGED_INDEFINITE_PC;
+    S.done = 1;
+    return;
+  }
+  S.pcoef = zr / S.betaold;
+  S.i = it;
+}
+
+__global__ void k_amg_p(int n, const AmgState* st, const double* __restrict__ z, double* __restrict__ p) {
+  note_launch();
+  if (st->done) return;
+  const double c = st->pcoef;
+  const bool first = st->i == 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = first ? z[i] : z[i] + c * p[i];
+}
+
+__global__ void k_amg_norm_b(const double* __restrict__ part, int nparts, double* out) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  const double s = sum_parts(part, nparts, red);
+  if (threadIdx.x == 0) *out = sqrt(s);
+}
+
+__global__ void k_amg_true(AmgState* st, const double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kT / 32];
+  const double rr = sum_parts(part, nparts, red);
+  const double bb = sum_parts(part + nparts, nparts, red);
+  if (threadIdx.x == 0) {
+    st->true_r2 = rr;
+    st->b2 = bb;
+  }
+}
+
+__global__ void k_amg_copy_back(int n, const uint8_t* __restrict__ ghost, const double* __restrict__ rhs,
+                                const double* __restrict__ y, double* __restrict__ x) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = (ghost && ghost[i]) ? rhs[i] : y[i];
+}
+
+// lanes per row of a CSR product: about four entries per lane, 2..32 lanes
+int lanes_for(const Csr& A) {
+  const double avg = A.n ? (double)A.nnz / A.n : 0.0;
+  int g = 2;
+  while (g < 32 && g * 4 < avg) g <<= 1;
+  return g;
+}
+
+}  // namespace
+}  // namespace fl
+
+using namespace fl;
+
+struct AmgLevel {
+  Csr A, P, R;
+  DevBuf<int32_t> sptr, scol;  // sliced-ELL copy of A (finest level)
+  DevBuf<double> sval;
+  bool sell = false;
+  DevBuf<double> dinv, x0, x1, d, b, r, xc;  // xc: the V-cycle's result on this level
+  double rho = 2.0;  // Gershgorin bound of the spectrum of D^-1 A
+  int G = 2, GP = 2, GR = 2;  // lanes per row of A, P and R
+};
+
+struct fl_amg_t {
+  fl_mesh_t* m = nullptr;
+  const double* val = nullptr;    // caller's matrix (rhs lifting)
+  const uint8_t* ghost = nullptr;  // caller's inactive mask
+  std::vector<std::unique_ptr<AmgLevel>> L;
+  int nc = 0;  // rows of the coarsest level
+  DevBuf<double> cinv;
+  // solve work
+  DevBuf<double> bb, y, r, z, p, w, part, bnorm;
+  DevBuf<AmgState> st;
+  cudaStream_t cs = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  ~fl_amg_t() {
+    if (cs) cudaStreamDestroy(cs);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+  }
+};
+
+namespace {
+
+int spgemm(const Csr& Lm, const Csr& B, Csr& C, ErrWord* err, cudaStream_t s) {
+  C.n = Lm.n;
+  C.m = B.m;
+  DevBuf<int32_t> cnt;
+  FL_TRY(cnt.reserve((size_t)Lm.n + 1));
+  FL_TRY(C.ptr.reserve((size_t)Lm.n + 1));
+  ProdArgs A{Lm.n, Lm.ptr.p, Lm.col.p, Lm.val.p, B.ptr.p, B.col.p, B.val.p, cnt.p, nullptr, nullptr, nullptr, err};
+  const size_t smem = (size_t)kCap * (sizeof(unsigned long long) + sizeof(double));
+  static bool configured = false;
+  if (!configured) {
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_spgemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  const unsigned grid = (unsigned)std::max(1, std::min(Lm.n, num_sms() * 8));
+  k_spgemm<256><<<grid, 256, smem, s>>>(A, 0);
+  FL_TRY_CUDA(cudaGetLastError());
+  // rows above the shared-memory capacity
+  DevBuf<int32_t> list;
+  DevBuf<int> nl;
+  FL_TRY(list.reserve((size_t)Lm.n));
+  FL_TRY(nl.reserve(1));
+  FL_TRY_CUDA(cudaMemsetAsync(nl.p, 0, sizeof(int), s));
+  k_long_rows<<<grid_for(Lm.n, kT), kT, 0, s>>>(Lm.n, cnt.p, list.p, nl.p);
+  int nlong = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&nlong, nl.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  DevBuf<int32_t> lcol;
+  DevBuf<double> lval;
+  if (nlong > 0) {
+    if (nlong > (1 << 16)) {
+      set_error("sparse product: %d rows above the candidate capacity", nlong);
+      return FL_ERR_UNSUPPORTED;
+    }
+    FL_TRY(lcol.reserve((size_t)nlong * kLongCols));
+    FL_TRY(lval.reserve((size_t)nlong * kLongCols));
+    k_spgemm_long<<<grid_for(nlong, 64), 64, 0, s>>>(A, list.p, nlong, 0, lcol.p, lval.p);
+    FL_TRY_CUDA(cudaGetLastError());
+  }
+  FL_TRY(check_err(err, s, "sparse product row with more distinct columns than the scratch holds"));
+  FL_TRY(exclusive_scan_i32(cnt.p, C.ptr.p, Lm.n, s));
+  int32_t nnz = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&nnz, C.ptr.p + Lm.n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  C.nnz = nnz;
+  FL_TRY(C.col.reserve((size_t)std::max(nnz, 1)));
+  FL_TRY(C.val.reserve((size_t)std::max(nnz, 1)));
+  A.cp = C.ptr.p;
+  A.cc = C.col.p;
+  A.cv = C.val.p;
+  k_spgemm<256><<<grid, 256, smem, s>>>(A, 1);
+  if (nlong > 0) k_spgemm_long<<<grid_for(nlong, 64), 64, 0, s>>>(A, list.p, nlong, 1, lcol.p, lval.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY_CUDA(cudaStreamSynchronize(s));  // scratch buffers are released on return
+  return FL_OK;
+}
+
+int transpose(const Csr& B, Csr& T, cudaStream_t s) {
+  T.n = B.m;
+  T.m = B.n;
+  T.nnz = B.nnz;
+  DevBuf<int32_t> cnt, fill;
+  FL_TRY(cnt.reserve((size_t)B.m + 1));
+  FL_TRY(fill.reserve((size_t)B.m + 1));
+  FL_TRY(T.ptr.reserve((size_t)B.m + 1));
+  FL_TRY(T.col.reserve((size_t)std::max<int64_t>(B.nnz, 1)));
+  FL_TRY(T.val.reserve((size_t)std::max<int64_t>(B.nnz, 1)));
+  FL_TRY_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (B.m + 1), s));
+  FL_TRY_CUDA(cudaMemsetAsync(fill.p, 0, sizeof(int32_t) * (B.m + 1), s));
+  k_t_count<<<grid_for(B.nnz, kT), kT, 0, s>>>(B.nnz, B.col.p, cnt.p);
+  FL_TRY(exclusive_scan_i32(cnt.p, T.ptr.p, B.m, s));
+  k_t_fill<<<grid_for(B.n, kT), kT, 0, s>>>(B.n, B.ptr.p, B.col.p, B.val.p, T.ptr.p, fill.p, T.col.p, T.val.p);
+  k_t_sort<<<grid_for(B.m, kT), kT, 0, s>>>(B.m, T.ptr.p, T.col.p, T.val.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
+// Dense inverse of a small SPD matrix by Cholesky (host, once per hierarchy).
+int dense_inverse(const std::vector<double>& a, int n, std::vector<double>& inv) {
+  std::vector<double> l(a);
+  for (int j = 0; j < n; ++j) {
+    double d = l[(size_t)j * n + j];
+    for (int k = 0; k < j; ++k) d -= l[(size_t)j * n + k] * l[(size_t)j * n + k];
+    if (!(d > 0.0)) {
+      set_error("coarsest AMG operator is not positive definite");
+      return FL_ERR_UNSUPPORTED;
+    }
+    d = std::sqrt(d);
+    l[(size_t)j * n + j] = d;
+    for (int i = j + 1; i < n; ++i) {
+      double s = l[(size_t)i * n + j];
+      for (int k = 0; k < j; ++k) s -= l[(size_t)i * n + k] * l[(size_t)j * n + k];
+      l[(size_t)i * n + j] = s / d;
+    }
+  }
+  inv.assign((size_t)n * n, 0.0);
+  std::vector<double> y(n);
+  for (int c = 0; c < n; ++c) {
+    for (int i = 0; i < n; ++i) {  // L y = e_c
+      double s = i == c ? 1.0 : 0.0;
+      for (int k = 0; k < i; ++k) s -= l[(size_t)i * n + k] * y[k];
+      y[i] = s / l[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {  // L^T x = y
+      double s = y[i];
+      for (int k = i + 1; k < n; ++k) s -= l[(size_t)k * n + i] * inv[(size_t)k * n + c];
+      inv[(size_t)i * n + c] = s / l[(size_t)i * n + i];
+    }
+  }
+  return FL_OK;
+}
+
+int level_setup(AmgLevel& Lv, cudaStream_t s) {
+  const int n = Lv.A.n;
+  FL_TRY(Lv.dinv.reserve(n));
+  DevBuf<unsigned long long> g;
+  FL_TRY(g.reserve(1));
+  FL_TRY_CUDA(cudaMemsetAsync(g.p, 0, sizeof(unsigned long long), s));
+  k_dinv_gersh<<<grid_for(n, kT), kT, 0, s>>>(n, Lv.A.ptr.p, Lv.A.col.p, Lv.A.val.p, Lv.dinv.p, g.p);
+  unsigned long long hb = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&hb, g.p, sizeof(hb), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  double rho;
+  std::memcpy(&rho, &hb, sizeof(rho));
+  Lv.rho = rho > 0.0 ? rho : 1.0;
+  Lv.G = lanes_for(Lv.A);
+  FL_TRY(Lv.x0.reserve(n));
+  FL_TRY(Lv.x1.reserve(n));
+  FL_TRY(Lv.d.reserve(n));
+  FL_TRY(Lv.b.reserve(n));
+  FL_TRY(Lv.r.reserve(n));
+  FL_TRY(Lv.xc.reserve(n));
+  return FL_OK;
+}
+
+// Aggregates of level Lv and its prolongator; returns the coarse size.
+int coarsen(AmgLevel& Lv, int level, ErrWord* err, cudaStream_t s, int* nc_out) {
+  const int n = Lv.A.n;
+  const Csr& A = Lv.A;
+  DevBuf<unsigned long long> t, t1, t2, pick;
+  DevBuf<int32_t> agg, flag, rank;
+  DevBuf<int> left;
+  FL_TRY(t.reserve(n));
+  FL_TRY(t1.reserve(n));
+  FL_TRY(t2.reserve(n));
+  FL_TRY(pick.reserve(n));
+  FL_TRY(agg.reserve(n));
+  FL_TRY(flag.reserve(n));
+  FL_TRY(rank.reserve((size_t)n + 1));
+  FL_TRY(left.reserve(1));
+  const unsigned gr = grid_for(n, kT);
+  k_mis_init<<<gr, kT, 0, s>>>(n, A.ptr.p, A.col.p, A.val.p, 0x9e3779b9u * (uint32_t)(level + 1), t.p, agg.p);
+  for (int round = 0; round < 200; ++round) {
+    k_mis_max<<<gr, kT, 0, s>>>(n, A.ptr.p, A.col.p, A.val.p, t.p, t1.p);
+    k_mis_max<<<gr, kT, 0, s>>>(n, A.ptr.p, A.col.p, A.val.p, t1.p, t2.p);
+    FL_TRY_CUDA(cudaMemsetAsync(left.p, 0, sizeof(int), s));
+    k_mis_update<<<gr, kT, 0, s>>>(n, t.p, t2.p, left.p);
+    int h = 0;
+    FL_TRY_CUDA(cudaMemcpyAsync(&h, left.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FL_TRY_CUDA(cudaStreamSynchronize(s));
+    if (h == 0) break;
+    if (round == 199) {
+      set_error("aggregation did not converge");
+      return FL_ERR_UNSUPPORTED;
+    }
+  }
+  k_mis_flag<<<gr, kT, 0, s>>>(n, t.p, flag.p);
+  FL_TRY(exclusive_scan_i32(flag.p, rank.p, n, s));
+  int32_t nc = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&nc, rank.p + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  *nc_out = nc;
+  if (nc == 0) return FL_OK;
+  k_agg1<<<gr, kT, 0, s>>>(n, A.ptr.p, A.col.p, A.val.p, t.p, rank.p, agg.p, pick.p);
+  k_agg2<<<gr, kT, 0, s>>>(n, A.ptr.p, A.col.p, A.val.p, pick.p, rank.p, agg.p, err);
+  FL_TRY(check_err(err, s, "aggregation left a coupled row without an aggregate"));
+  // P0 and the smoothed prolongator
+  Csr P0;
+  P0.n = n;
+  P0.m = nc;
+  FL_TRY(P0.ptr.reserve((size_t)n + 1));
+  k_p0_count<<<gr, kT, 0, s>>>(n, agg.p, flag.p);
+  FL_TRY(exclusive_scan_i32(flag.p, P0.ptr.p, n, s));
+  int32_t nnz0 = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&nnz0, P0.ptr.p + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  P0.nnz = nnz0;
+  FL_TRY(P0.col.reserve((size_t)std::max(nnz0, 1)));
+  FL_TRY(P0.val.reserve((size_t)std::max(nnz0, 1)));
+  k_p0_fill<<<gr, kT, 0, s>>>(n, agg.p, P0.ptr.p, P0.col.p, P0.val.p);
+  FL_TRY(spgemm(A, P0, Lv.P, err, s));  // A P0
+  const double omega = 4.0 / (3.0 * Lv.rho);
+  k_smooth_p<<<gr, kT, 0, s>>>(n, Lv.P.ptr.p, Lv.P.col.p, Lv.P.val.p, agg.p, Lv.dinv.p, omega);
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY(transpose(Lv.P, Lv.R, s));
+  Lv.GP = lanes_for(Lv.P);
+  Lv.GR = lanes_for(Lv.R);
+  return FL_OK;
+}
+
+// ------------------------------------------------------- V-cycle launch --
+#define FL_AMG_G(G, KERNEL, GRID, S, ...)                                           \
+  do {                                                                              \
+    switch (G) {                                                                    \
+      case 32: KERNEL<32><<<GRID, kT, 0, S>>>(__VA_ARGS__); break;                   \
+      case 16: KERNEL<16><<<GRID, kT, 0, S>>>(__VA_ARGS__); break;                   \
+      case 8: KERNEL<8><<<GRID, kT, 0, S>>>(__VA_ARGS__); break;                     \
+      case 4: KERNEL<4><<<GRID, kT, 0, S>>>(__VA_ARGS__); break;                     \
+      default: KERNEL<2><<<GRID, kT, 0, S>>>(__VA_ARGS__); break;                    \
+    }                                                                               \
+  } while (0)
+
+Op op_of(const Csr& A) { return Op{A.n, A.ptr.p, A.col.p, A.val.p}; }
+
+// Chebyshev(2) coefficients on [0.1 rho, 1.1 rho]
+struct Cheb {
+  double ith, c1, c2;
+};
+Cheb cheb_of(double rho) {
+  const double lo = 0.1 * rho, hi = 1.1 * rho;
+  const double th = 0.5 * (hi + lo), de = 0.5 * (hi - lo), sg = th / de;
+  const double r0 = 1.0 / sg, r1 = 1.0 / (2.0 * sg - r0);
+  return Cheb{1.0 / th, r1 * r0, 2.0 * r1 / de};
+}
+
+// x_l = V(b_l), all on stream s (capturable)
+void vcycle(fl_amg_t* H, int l, const double* b, double* x, cudaStream_t s) {
+  if (l == (int)H->L.size() - 1) {
+    k_dense<<<grid_for((int64_t)H->nc * 32, kT, 4), kT, 0, s>>>(H->nc, H->cinv.p, b, x);
+    return;
+  }
+  AmgLevel& Lv = *H->L[l];
+  AmgLevel& Ln = *H->L[l + 1];
+  const int n = Lv.A.n, G = Lv.G;
+  const Op A = op_of(Lv.A);
+  const Cheb c = cheb_of(Lv.rho);
+  const unsigned gv = grid_for(n, kT, 4), gs = grid_for((int64_t)n * G, kT, 8);
+  const SellOp S{n, Lv.sptr.p, Lv.scol.p, Lv.sval.p};
+  const unsigned gl = grid_for(n, kT, 8);
+  // pre-smoothing from zero: two Chebyshev steps (one product)
+  k_cheb0<<<gv, kT, 0, s>>>(n, Lv.dinv.p, b, c.ith, Lv.x0.p, Lv.d.p);
+  if (Lv.sell) k_cheb_sl<<<gl, kT, 0, s>>>(S, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, c.c1, c.c2, Lv.x1.p);
+  else FL_AMG_G(G, k_cheb, gs, s, A, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, c.c1, c.c2, Lv.x1.p);
+  // restriction of the residual, coarse correction, prolongation
+  if (Lv.sell) k_resid_sl<<<gl, kT, 0, s>>>(S, b, Lv.x1.p, Lv.r.p);
+  else FL_AMG_G(G, k_resid, gs, s, A, b, Lv.x1.p, Lv.r.p);
+  const unsigned gr = grid_for((int64_t)Ln.A.n * Lv.GR, kT, 8);
+  FL_AMG_G(Lv.GR, k_spmv_add, gr, s, op_of(Lv.R), Lv.r.p, nullptr, Ln.b.p);
+  vcycle(H, l + 1, Ln.b.p, Ln.xc.p, s);
+  FL_AMG_G(Lv.GP, k_spmv_add, grid_for((int64_t)n * Lv.GP, kT, 8), s, op_of(Lv.P), Ln.xc.p, Lv.x1.p, Lv.x0.p);
+  // post-smoothing: two Chebyshev steps from the corrected guess
+  if (Lv.sell) {
+    k_cheb_sl<<<gl, kT, 0, s>>>(S, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, 0.0, c.ith, Lv.x1.p);
+    k_cheb_sl<<<gl, kT, 0, s>>>(S, Lv.dinv.p, b, Lv.x1.p, Lv.d.p, c.c1, c.c2, x);
+  } else {
+    FL_AMG_G(G, k_cheb, gs, s, A, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, 0.0, c.ith, Lv.x1.p);
+    FL_AMG_G(G, k_cheb, gs, s, A, Lv.dinv.p, b, Lv.x1.p, Lv.d.p, c.c1, c.c2, x);
+  }
+}
+
+}  // namespace
+
+namespace {
+
+int make_sell(AmgLevel& Lv, cudaStream_t s) {
+  const int n = Lv.A.n, nsl = (n + 31) / 32;
+  DevBuf<int32_t> w;
+  FL_TRY(w.reserve((size_t)nsl + 1));
+  FL_TRY(Lv.sptr.reserve((size_t)nsl + 1));
+  k_sl_width<<<grid_for(nsl, kT), kT, 0, s>>>(n, Lv.A.ptr.p, w.p);
+  FL_TRY(exclusive_scan_i32(w.p, Lv.sptr.p, nsl, s));
+  int32_t len = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&len, Lv.sptr.p + nsl, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  FL_TRY(Lv.scol.reserve((size_t)len));
+  FL_TRY(Lv.sval.reserve((size_t)len));
+  k_sl_fill<<<grid_for((int64_t)nsl * 32, kT), kT, 0, s>>>(n, Lv.A.ptr.p, Lv.A.col.p, Lv.A.val.p, Lv.sptr.p,
+                                                           Lv.scol.p, Lv.sval.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  Lv.sell = true;
+  return FL_OK;
+}
+
+int build_hierarchy(fl_amg_t* H, cudaStream_t s) {
+  fl_mesh_t* m = H->m;
+  const int n = m->N;
+  DevBuf<ErrWord> err;
+  FL_TRY(err.reserve(1));
+  FL_TRY_CUDA(cudaMemsetAsync(err.p, 0, sizeof(ErrWord), s));
+  // level 0: the ghost-masked matrix on the mesh pattern
+  H->L.emplace_back(new AmgLevel());
+  AmgLevel& L0 = *H->L[0];
+  L0.A.n = L0.A.m = n;
+  L0.A.nnz = m->nnz;
+  FL_TRY(L0.A.ptr.reserve((size_t)n + 1));
+  FL_TRY(L0.A.col.reserve((size_t)m->nnz));
+  FL_TRY(L0.A.val.reserve((size_t)m->nnz));
+  FL_TRY_CUDA(cudaMemcpyAsync(L0.A.ptr.p, m->findrm.p, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToDevice, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(L0.A.col.p, m->colm.p, sizeof(int32_t) * m->nnz, cudaMemcpyDeviceToDevice, s));
+  DevBuf<unsigned long long> mm;
+  FL_TRY(mm.reserve(2));
+  const unsigned long long init[2] = {~0ull >> 1, 0ull};  // +max finite bits, 0
+  FL_TRY_CUDA(cudaMemcpyAsync(mm.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  k_diag_range<<<grid_for(n, kT), kT, 0, s>>>(n, m->findrm.p, m->colm.p, H->val, mm.p);
+  k_mask<<<grid_for(n, kT), kT, 0, s>>>(n, m->findrm.p, m->colm.p, H->val, H->ghost, mm.p, L0.A.val.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY(level_setup(L0, s));
+  FL_TRY(make_sell(L0, s));
+  for (int l = 0; l + 1 < kMaxLevels && H->L[l]->A.n > kMaxCoarse; ++l) {
+    AmgLevel& Lv = *H->L[l];
+    int nc = 0;
+    FL_TRY(coarsen(Lv, l, err.p, s, &nc));
+    if (nc == 0 || nc * 10 > Lv.A.n * 9) break;  // no useful coarsening left
+    Csr AP;
+    FL_TRY(spgemm(Lv.A, Lv.P, AP, err.p, s));
+    H->L.emplace_back(new AmgLevel());
+    AmgLevel& Lc = *H->L[l + 1];
+    FL_TRY(spgemm(Lv.R, AP, Lc.A, err.p, s));
+    FL_TRY(check_err(err.p, s, "Galerkin product row above the candidate capacity"));
+    FL_TRY(level_setup(Lc, s));
+  }
+  // coarsest level: dense inverse
+  AmgLevel& Lz = *H->L.back();
+  const int nz = Lz.A.n;
+  if (nz > kMaxCoarse) {
+    set_error("AMG coarsening stopped at %d rows (dense coarse solve limit %d)", nz, kMaxCoarse);
+    return FL_ERR_UNSUPPORTED;
+  }
+  std::vector<int32_t> hp(nz + 1), hc((size_t)Lz.A.nnz);
+  std::vector<double> hv((size_t)Lz.A.nnz), dense((size_t)nz * nz, 0.0), inv;
+  FL_TRY_CUDA(cudaMemcpyAsync(hp.data(), Lz.A.ptr.p, sizeof(int32_t) * (nz + 1), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(hc.data(), Lz.A.col.p, sizeof(int32_t) * Lz.A.nnz, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(hv.data(), Lz.A.val.p, sizeof(double) * Lz.A.nnz, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < nz; ++i)
+    for (int k = hp[i]; k < hp[i + 1]; ++k) dense[(size_t)i * nz + hc[k]] += hv[k];
+  // rows without any coupling (possible only when level 0 is the coarsest:
+  // ghost rows) keep their diagonal, which is the ghost pivot
+  FL_TRY(dense_inverse(dense, nz, inv));
+  FL_TRY(H->cinv.reserve((size_t)nz * nz));
+  FL_TRY_CUDA(cudaMemcpyAsync(H->cinv.p, inv.data(), sizeof(double) * nz * nz, cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  H->nc = nz;
+  return FL_OK;
+}
+
+// K iterations of AMG-preconditioned CG (capturable; no host interaction)
+void amg_iterations(fl_amg_t* H, int K, cudaStream_t c) {
+  AmgLevel& L0 = *H->L[0];
+  const int n = L0.A.n, G = L0.G;
+  const Op A = op_of(L0.A);
+  const unsigned gv = grid_for(n, kT, 4), gl = grid_for(n, kT, 8);
+  const SellOp S{n, L0.sptr.p, L0.scol.p, L0.sval.p};
+  AmgState* st = H->st.p;
+  (void)A;
+  (void)G;
+  for (int k = 0; k < K; ++k) {
+    k_amg_ap_sl<<<gl, kT, 0, c>>>(S, st, H->p.p, H->w.p, H->part.p);
+    k_amg_alpha<<<1, kT, 0, c>>>(st, H->part.p, (int)gl);
+    k_amg_xr<<<gv, kT, 0, c>>>(n, st, H->p.p, H->w.p, H->y.p, H->r.p);
+    vcycle(H, 0, H->r.p, H->z.p, c);
+    k_dots<<<gv, kT, 0, c>>>(n, H->z.p, H->z.p, H->z.p, H->r.p, H->part.p);
+    k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 0, nullptr);
+    k_amg_p<<<gv, kT, 0, c>>>(n, st, H->z.p, H->p.p);
+  }
+}
+
+}  // namespace
+
+extern "C" int fl_amg_create(fl_mesh m, const double* val, const uint8_t* inactive, void* stream, fl_amg* out) {
+  FL_CHECK_ARG(m && val && out, "null argument");
+  FL_CHECK_ARG(m->N > 0 && m->nnz > 0, "empty matrix");
+  fl_amg_t* H = new fl_amg_t();
+  H->m = m;
+  H->val = val;
+  H->ghost = inactive;
+  cudaStream_t caller = stream ? (cudaStream_t)stream : m->stream;
+  int st = FL_OK;
+  do {
+    if (cudaStreamCreateWithFlags(&H->cs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&H->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&H->ev_out, cudaEventDisableTiming) != cudaSuccess) {
+      set_error("stream/event creation failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    if (cudaEventRecord(H->ev_in, caller) != cudaSuccess || cudaStreamWaitEvent(H->cs, H->ev_in, 0) != cudaSuccess) {
+      st = FL_ERR_CUDA;
+      break;
+    }
+    st = build_hierarchy(H, H->cs);
+  } while (0);
+  if (st != FL_OK) {
+    if (st == FL_ERR_CUDA && fl_last_error()[0] == 0) set_error("%s", cudaGetErrorString(cudaGetLastError()));
+    cudaStreamSynchronize(H->cs);
+    delete H;
+    return st;
+  }
+  *out = H;
+  return FL_OK;
+}
+
+extern "C" int fl_amg_destroy(fl_amg H) {
+  if (H) {
+    cudaDeviceSynchronize();
+    delete H;
+  }
+  return FL_OK;
+}
+
+extern "C" int fl_amg_levels(fl_amg H, int32_t* levels, int64_t* rows, int64_t* nnz, int32_t cap) {
+  FL_CHECK_ARG(H && levels, "null argument");
+  *levels = (int32_t)H->L.size();
+  for (int l = 0; l < (int)H->L.size() && l < cap; ++l) {
+    if (rows) rows[l] = H->L[l]->A.n;
+    if (nnz) nnz[l] = H->L[l]->A.nnz;
+  }
+  return FL_OK;
+}
+
+extern "C" int fl_amg_solve(fl_amg H, const fl_solver_opts* o, const double* rhs, double* x, fl_solve_report* rep,
+                            void* stream) {
+  FL_CHECK_ARG(H && o && rhs && x && rep, "null argument");
+  FL_CHECK_ARG(o->ksp_type == 0, "the AMG preconditioner is used with CG");
+  FL_CHECK_ARG(o->precision == 0, "the AMG-preconditioned solve runs in FP64");
+  FL_CHECK_ARG(o->max_its >= 0, "max_its");
+  fl_mesh_t* m = H->m;
+  AmgLevel& L0 = *H->L[0];
+  const int n = L0.A.n, G = L0.G;
+  const unsigned gs = grid_for((int64_t)n * G, kT, 8), gv = grid_for(n, kT, 4);
+  const unsigned np = std::max(std::max(gs, gv), grid_for(n, kT, 8));
+  FL_TRY(H->bb.reserve(n));
+  FL_TRY(H->y.reserve(n));
+  FL_TRY(H->r.reserve(n));
+  FL_TRY(H->z.reserve(n));
+  FL_TRY(H->p.reserve(n));
+  FL_TRY(H->w.reserve(n));
+  FL_TRY(H->part.reserve((size_t)2 * np));
+  FL_TRY(H->st.reserve(1));
+  FL_TRY(H->bnorm.reserve(1));
+  cudaStream_t caller = stream ? (cudaStream_t)stream : m->stream;
+  cudaStream_t c = H->cs;
+  FL_TRY_CUDA(cudaEventRecord(H->ev_in, caller));
+  FL_TRY_CUDA(cudaStreamWaitEvent(c, H->ev_in, 0));
+  AmgState h{};
+  h.rtol = o->rtol;
+  h.atol = o->atol;
+  h.dtol = o->dtol > 0 ? o->dtol : 1e5;
+  h.max_its = o->max_its;
+  h.guess_zero = o->start_from_zero ? 1 : 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(H->st.p, &h, sizeof(h), cudaMemcpyHostToDevice, c));
+  AmgState* st = H->st.p;
+  const Op A = op_of(L0.A);
+  const Op Aorig{n, m->findrm.p, m->colm.p, H->val};
+  FL_AMG_G(G, k_amg_lift, gs, c, Aorig, H->ghost, rhs, x, h.guess_zero, H->bb.p, H->y.p);
+  FL_AMG_G(G, k_resid, gs, c, A, H->bb.p, H->y.p, H->r.p);
+  const double* bn = nullptr;
+  if (!h.guess_zero) {  // rnorm0 = ||B b|| (KSPConvergedDefault with a nonzero guess)
+    vcycle(H, 0, H->bb.p, H->z.p, c);
+    k_dots<<<gv, kT, 0, c>>>(n, H->z.p, H->z.p, nullptr, nullptr, H->part.p);
+    k_amg_norm_b<<<1, kT, 0, c>>>(H->part.p, (int)gv, H->bnorm.p);
+    bn = H->bnorm.p;
+  }
+  vcycle(H, 0, H->r.p, H->z.p, c);
+  k_dots<<<gv, kT, 0, c>>>(n, H->z.p, H->z.p, H->z.p, H->r.p, H->part.p);
+  k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 1, bn);
+  k_amg_p<<<gv, kT, 0, c>>>(n, st, H->z.p, H->p.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  // iterations: chunks of four as one graph, replayed until done
+  const int K = 4;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  FL_TRY_CUDA(cudaStreamBeginCapture(c, cudaStreamCaptureModeThreadLocal));
+  amg_iterations(H, K, c);
+  cudaError_t e = cudaStreamEndCapture(c, &g);
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    set_error("AMG iteration graph: %s", cudaGetErrorString(e));
+    return FL_ERR_CUDA;
+  }
+  int st_code = FL_OK;
+  for (int i = 0; i <= o->max_its; i += K) {
+    if (cudaGraphLaunch(ex, c) != cudaSuccess) {
+      st_code = FL_ERR_CUDA;
+      break;
+    }
+    int done = 0;
+    if (cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, c) != cudaSuccess ||
+        cudaStreamSynchronize(c) != cudaSuccess) {
+      st_code = FL_ERR_CUDA;
+      break;
+    }
+    if (done) break;
+  }
+  cudaGraphExecDestroy(ex);
+  FL_TRY(st_code);
+  // true residual and the solution (ghost rows take their rhs)
+  FL_AMG_G(G, k_resid, gs, c, A, H->bb.p, H->y.p, H->r.p);
+  k_dots<<<gv, kT, 0, c>>>(n, H->r.p, H->r.p, H->bb.p, H->bb.p, H->part.p);
+  k_amg_true<<<1, kT, 0, c>>>(st, H->part.p, (int)gv);
+  k_amg_copy_back<<<gv, kT, 0, c>>>(n, H->ghost, rhs, H->y.p, x);
+  FL_TRY_CUDA(cudaGetLastError());
+  AmgState hs;
+  FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, c));
+  FL_TRY_CUDA(cudaStreamSynchronize(c));
+  FL_TRY_CUDA(cudaEventRecord(H->ev_out, c));
+  FL_TRY_CUDA(cudaStreamWaitEvent(caller, H->ev_out, 0));
+  rep->iterations = hs.its;
+  rep->reason = hs.reason ? hs.reason : FL_DIVERGED_ITS;
+  rep->final_rnorm = hs.rnorm;
+  rep->rnorm0 = hs.rnorm0;
+  rep->true_rel_residual = hs.b2 > 0 ? sqrt(hs.true_r2 / hs.b2) : sqrt(hs.true_r2);
+  rep->outer_iterations = (int32_t)H->L.size();
+  rep->pad = 0;
+  return FL_OK;
+}

@@ -152,6 +152,7 @@ unsigned long long launches_mesh();
 unsigned long long launches_assemble();
 unsigned long long launches_krylov();
 unsigned long long launches_gnn();
+unsigned long long launches_amg();
 void release_krylov_work(struct ::fl_mesh_t* m);
 
 }  // namespace fl

@@ -259,6 +259,48 @@ def petsc_solve(mesh: Mesh, x, val, rhs, options: SolverOpts, inactive=None, str
     return _report_dict(rep)
 
 
+class AmgPreconditioner:
+    """Smoothed-aggregation AMG hierarchy of one assembled matrix (fl_amg_*),
+    the counterpart of petsc_solve's gamg preconditioner.  `val` and
+    `inactive` are device tensors that must not change while it is used."""
+
+    def __init__(self, mesh: Mesh, val, inactive=None, stream=None):
+        self.lib = mesh.lib
+        self.mesh = mesh
+        self._keep = (val, inactive)
+        h = C.c_void_p()
+        check(self.lib.fl_amg_create(mesh.handle, _ptr(val), _ptr(inactive), _stream_ptr(stream),
+                                     C.byref(h)), "fl_amg_create")
+        self.handle = h.value
+
+    def levels(self):
+        """[(rows, nonzeros)] of every level, finest first."""
+        cap = 16
+        nl = C.c_int32()
+        rows = (C.c_int64 * cap)()
+        nnz = (C.c_int64 * cap)()
+        check(self.lib.fl_amg_levels(self.handle, C.byref(nl), rows, nnz, cap), "fl_amg_levels")
+        return [(int(rows[i]), int(nnz[i])) for i in range(nl.value)]
+
+    def solve(self, x, rhs, options: SolverOpts, stream=None) -> dict:
+        """CG preconditioned by the hierarchy: x holds the guess, receives the solution."""
+        rep = SolveReport()
+        check(self.lib.fl_amg_solve(self.handle, C.byref(options), _ptr(rhs), _ptr(x), C.byref(rep),
+                                    _stream_ptr(stream)), "fl_amg_solve")
+        return _report_dict(rep)
+
+    def close(self):
+        if self.handle:
+            self.lib.fl_amg_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def csr_mult(mesh: Mesh, val, x, y, stream=None):
     """y = A x (device tensors)."""
     check(mesh.lib.fl_dev_csr_mult(mesh.handle, _ptr(val), _ptr(x), _ptr(y), _stream_ptr(stream)),

@@ -286,6 +286,33 @@ int fl_batch_run(fl_batch batch, void* stream, fl_solve_report* reports);
 int fl_batch_size(fl_batch batch);
 int fl_batch_destroy(fl_batch batch);
 
+/* ----------------------------------------------- AMG preconditioner -- */
+
+/* Smoothed-aggregation algebraic multigrid for CG, the GPU counterpart of
+ * the gamg preconditioner of petsc_solve's options (femtools/Solvers.F90:
+ * 1827-1969, PETSc PCGAMG with its default structure):
+ *   - aggregates from a distance-2 maximal independent set of the matrix graph;
+ *   - one Jacobi smoothing of the piecewise-constant prolongator;
+ *   - Galerkin coarse operators;
+ *   - Chebyshev(2)-Jacobi smoothing;
+ *   - a dense solve on the coarsest level (at most 512 rows).
+ * fl_amg_create builds the hierarchy for the matrix val (device, on the
+ * mesh's pattern) with the inactive (Dirichlet) rows of `inactive` (device,
+ * may be NULL) treated as petsc_solve treats them.  Both arrays must stay
+ * valid and unchanged while the handle is used; like cache_solver_context,
+ * one hierarchy serves many right-hand sides.  fl_amg_solve runs CG on that
+ * system with the hierarchy as preconditioner: ghost rows, rhs lifting and
+ * PETSc's default convergence test on the preconditioned residual norm as
+ * fl_dev_petsc_solve (opts: ksp_type 0, precision 0; report->outer_iterations
+ * returns the number of levels).  Device pointers; the hierarchy and the
+ * solve are deterministic. */
+typedef struct fl_amg_t* fl_amg;
+int fl_amg_create(fl_mesh mesh, const double* val, const uint8_t* inactive, void* stream, fl_amg* amg);
+int fl_amg_solve(fl_amg amg, const fl_solver_opts* opts, const double* rhs, double* x,
+                 fl_solve_report* report, void* stream);
+int fl_amg_levels(fl_amg amg, int32_t* levels, int64_t* rows, int64_t* nnz, int32_t capacity);
+int fl_amg_destroy(fl_amg amg);
+
 /* ------------------------------------------------- learned warm start -- */
 
 /* Message-passing network that predicts the next pressure of a sequence of
