@@ -260,6 +260,7 @@ __global__ void k_p0_fill(int n, const int32_t* __restrict__ agg, const int32_t*
 // that order.  One block per row; pass 0 counts the columns, pass 1 fills.
 struct ProdArgs {
   int32_t n;
+  const int32_t* rows;  // rows to process (null: all n rows)
   const int32_t *lp, *lc;
   const double* lv;
   const int32_t *bp, *bc;
@@ -279,7 +280,8 @@ __global__ void __launch_bounds__(NT) k_spgemm(ProdArgs A, int pass) {
   double* v = reinterpret_cast<double*>(key + kCap);                     // [kCap]
   __shared__ int s_n, s_tot;
   __shared__ int s_scan[NT];
-  for (int row = blockIdx.x; row < A.n; row += gridDim.x) {
+  for (int it = blockIdx.x; it < A.n; it += gridDim.x) {
+    const int row = A.rows ? A.rows[it] : it;
     // candidate offsets: lane-parallel prefix over the row of L
     const int lb = A.lp[row], le = A.lp[row + 1];
     if (threadIdx.x == 0) s_n = 0;
@@ -378,6 +380,105 @@ __global__ void __launch_bounds__(NT) k_spgemm(ProdArgs A, int pass) {
   }
 }
 
+// The same product, one warp per row, for rows of at most kWarpCap
+// candidates (the common case on the finer levels); longer rows are marked
+// with count -2 for the block kernel.  Same candidate order, same sort key,
+// same sums: identical results to the block kernel.
+constexpr int kWarpCap = 256;
+constexpr int kWarpsW = 8;
+__global__ void __launch_bounds__(kWarpsW * 32) k_spgemm_warp(ProdArgs A, int pass) {
+  note_launch();
+  __shared__ unsigned long long key_all[kWarpsW][kWarpCap];
+  __shared__ double v_all[kWarpsW][kWarpCap];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned long long* key = key_all[w];
+  double* v = v_all[w];
+  const int nw = gridDim.x * kWarpsW;
+  for (int row = blockIdx.x * kWarpsW + w; row < A.n; row += nw) {
+    const int lb = A.lp[row], le = A.lp[row + 1];
+    int total = 0;
+    bool over = false;
+    for (int k0 = lb; k0 < le; k0 += 32) {
+      const int k = k0 + lane;
+      const int len = k < le ? A.bp[A.lc[k] + 1] - A.bp[A.lc[k]] : 0;
+      int incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += x;
+      }
+      const int excl = total + incl - len;
+      const int chunk = __shfl_sync(0xffffffffu, incl, 31);
+      if (total + chunk > kWarpCap) {
+        over = true;
+        break;
+      }
+      if (k < le) {
+        const int kk = A.lc[k];
+        const double l = A.lv[k];
+        const int qb = A.bp[kk];
+        for (int q = 0; q < len; ++q) {
+          const int pos = excl + q;
+          key[pos] = ((unsigned long long)(uint32_t)A.bc[qb + q] << 32) | (uint32_t)pos;
+          v[pos] = l * A.bv[qb + q];
+        }
+      }
+      total += chunk;
+    }
+    __syncwarp();
+    if (over) {
+      if (pass == 0 && lane == 0) A.cnt[row] = -2;
+      continue;
+    }
+    const int nc = total;
+    int pw = 1;
+    while (pw < nc) pw <<= 1;
+    for (int k = nc + lane; k < pw; k += 32) key[k] = ~0ull;
+    __syncwarp();
+    for (int size = 2; size <= pw; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int k = lane; k < pw; k += 32) {
+          const int l = k ^ stride;
+          if (l > k) {
+            const unsigned long long a = key[k], b = key[l];
+            const bool up = (k & size) == 0;
+            if ((a > b) == up) {
+              key[k] = b;
+              key[l] = a;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    // heads, their ranks (ballot prefix) and per-column sums in sorted order
+    int base = 0;
+    const int out0 = pass == 1 ? A.cp[row] : 0;
+    for (int k0 = 0; k0 < nc; k0 += 32) {
+      const int k = k0 + lane;
+      const bool head = k < nc && (k == 0 || (key[k] >> 32) != (key[k - 1] >> 32));
+      const unsigned m = __ballot_sync(0xffffffffu, head);
+      if (pass == 1 && head) {
+        const int slot = base + __popc(m & ((1u << lane) - 1u));
+        const uint32_t c = (uint32_t)(key[k] >> 32);
+        double sum = 0.0;
+        for (int q = k; q < nc && (uint32_t)(key[q] >> 32) == c; ++q) sum += v[(uint32_t)key[q]];
+        A.cc[out0 + slot] = (int32_t)c;
+        A.cv[out0 + slot] = sum;
+      }
+      base += __popc(m);
+    }
+    if (pass == 0 && lane == 0) A.cnt[row] = base;
+    __syncwarp();
+  }
+}
+
+__global__ void k_rows_marked(int n, const int32_t* __restrict__ cnt, int mark, int32_t* __restrict__ list,
+                              int* __restrict__ nl) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (cnt[i] == mark) list[atomicAdd(nl, 1)] = i;
+}
+
 // Rows with more candidates than one block's shared memory holds: one thread
 // per row inserts the candidates, in their generation order, into a sorted
 // list of distinct columns (at most kLongCols) in global scratch, adding
@@ -438,11 +539,6 @@ __global__ void k_spgemm_long(ProdArgs A, const int32_t* __restrict__ rows, int 
   }
 }
 
-__global__ void k_long_rows(int n, const int32_t* __restrict__ cnt, int32_t* __restrict__ list, int* __restrict__ nl) {
-  note_launch();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    if (cnt[i] < 0) list[atomicAdd(nl, 1)] = i;
-}
 
 // Transpose (rows of C = columns of B): slots by atomics, then each column's
 // entries sorted by row (insertion sort; columns are short).
@@ -463,9 +559,58 @@ __global__ void k_t_fill(int n, const int32_t* __restrict__ ptr, const int32_t* 
       tv[s] = val[k];
     }
 }
-__global__ void k_t_sort(int m, const int32_t* __restrict__ tp, int32_t* __restrict__ tc, double* __restrict__ tv) {
+// Columns of up to kSortCap entries: one block per column, bitonic sort of
+// (row, position) keys in shared memory.  Longer columns are marked (-1 in
+// `longc`) for the thread-per-column insertion sort below.
+constexpr int kSortCap = 2048;
+__global__ void __launch_bounds__(256) k_t_sort_blk(int m, const int32_t* __restrict__ tp, int32_t* __restrict__ tc,
+                                                    double* __restrict__ tv, int32_t* __restrict__ longc) {
+  note_launch();
+  __shared__ unsigned long long key[kSortCap];
+  __shared__ double v[kSortCap];
+  for (int j = blockIdx.x; j < m; j += gridDim.x) {
+    const int b = tp[j], len = tp[j + 1] - b;
+    longc[j] = len > kSortCap ? -1 : 0;
+    if (len > kSortCap || len < 2) continue;
+    int pw = 1;
+    while (pw < len) pw <<= 1;
+    for (int k = threadIdx.x; k < pw; k += 256) {
+      if (k < len) {
+        key[k] = ((unsigned long long)(uint32_t)tc[b + k] << 32) | (uint32_t)k;
+        v[k] = tv[b + k];
+      } else {
+        key[k] = ~0ull;
+      }
+    }
+    __syncthreads();
+    for (int size = 2; size <= pw; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int k = threadIdx.x; k < pw; k += 256) {
+          const int l = k ^ stride;
+          if (l > k) {
+            const unsigned long long x = key[k], y = key[l];
+            const bool up = (k & size) == 0;
+            if ((x > y) == up) {
+              key[k] = y;
+              key[l] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int k = threadIdx.x; k < len; k += 256) {
+      tc[b + k] = (int32_t)(key[k] >> 32);
+      tv[b + k] = v[(uint32_t)key[k]];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_t_sort(int m, const int32_t* __restrict__ tp, int32_t* __restrict__ tc, double* __restrict__ tv,
+                         const int32_t* __restrict__ longc) {
   note_launch();
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+    if (longc[j] == 0) continue;
     const int b = tp[j], e = tp[j + 1];
     for (int k = b + 1; k < e; ++k) {
       const int c = tc[k];
@@ -891,31 +1036,44 @@ struct fl_amg_t {
 namespace {
 
 int spgemm(const Csr& Lm, const Csr& B, Csr& C, ErrWord* err, cudaStream_t s) {
+  // rows go to the warp kernel (up to kWarpCap candidates), the block kernel
+  // (up to kCap) or the one-thread-per-row kernel (longer)
   C.n = Lm.n;
   C.m = B.m;
-  DevBuf<int32_t> cnt;
+  DevBuf<int32_t> cnt, list2, list1;
+  DevBuf<int> nl;
   FL_TRY(cnt.reserve((size_t)Lm.n + 1));
   FL_TRY(C.ptr.reserve((size_t)Lm.n + 1));
-  ProdArgs A{Lm.n, Lm.ptr.p, Lm.col.p, Lm.val.p, B.ptr.p, B.col.p, B.val.p, cnt.p, nullptr, nullptr, nullptr, err};
+  FL_TRY(list2.reserve((size_t)Lm.n));
+  FL_TRY(list1.reserve((size_t)Lm.n));
+  FL_TRY(nl.reserve(2));
+  ProdArgs A{Lm.n, nullptr, Lm.ptr.p, Lm.col.p, Lm.val.p, B.ptr.p, B.col.p, B.val.p, cnt.p, nullptr, nullptr,
+             nullptr, err};
   const size_t smem = (size_t)kCap * (sizeof(unsigned long long) + sizeof(double));
   static bool configured = false;
   if (!configured) {
     FL_TRY_CUDA(cudaFuncSetAttribute(k_spgemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = true;
   }
-  const unsigned grid = (unsigned)std::max(1, std::min(Lm.n, num_sms() * 8));
-  k_spgemm<256><<<grid, 256, smem, s>>>(A, 0);
-  FL_TRY_CUDA(cudaGetLastError());
-  // rows above the shared-memory capacity
-  DevBuf<int32_t> list;
-  DevBuf<int> nl;
-  FL_TRY(list.reserve((size_t)Lm.n));
-  FL_TRY(nl.reserve(1));
-  FL_TRY_CUDA(cudaMemsetAsync(nl.p, 0, sizeof(int), s));
-  k_long_rows<<<grid_for(Lm.n, kT), kT, 0, s>>>(Lm.n, cnt.p, list.p, nl.p);
-  int nlong = 0;
-  FL_TRY_CUDA(cudaMemcpyAsync(&nlong, nl.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  const unsigned gw = (unsigned)std::max(1, std::min((Lm.n + kWarpsW - 1) / kWarpsW, num_sms() * 8));
+  k_spgemm_warp<<<gw, kWarpsW * 32, 0, s>>>(A, 0);
+  FL_TRY_CUDA(cudaMemsetAsync(nl.p, 0, sizeof(int) * 2, s));
+  k_rows_marked<<<grid_for(Lm.n, kT), kT, 0, s>>>(Lm.n, cnt.p, -2, list2.p, nl.p);
+  int hn[2] = {0, 0};
+  FL_TRY_CUDA(cudaMemcpyAsync(hn, nl.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
+  const int nblock = hn[0];
+  ProdArgs Ab = A;
+  Ab.n = nblock;
+  Ab.rows = list2.p;
+  const unsigned gb = (unsigned)std::max(1, std::min(nblock, num_sms() * 8));
+  int nlong = 0;
+  if (nblock > 0) {
+    k_spgemm<256><<<gb, 256, smem, s>>>(Ab, 0);
+    k_rows_marked<<<grid_for(Lm.n, kT), kT, 0, s>>>(Lm.n, cnt.p, -1, list1.p, nl.p + 1);
+    FL_TRY_CUDA(cudaMemcpyAsync(&nlong, nl.p + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FL_TRY_CUDA(cudaStreamSynchronize(s));
+  }
   DevBuf<int32_t> lcol;
   DevBuf<double> lval;
   if (nlong > 0) {
@@ -925,9 +1083,9 @@ int spgemm(const Csr& Lm, const Csr& B, Csr& C, ErrWord* err, cudaStream_t s) {
     }
     FL_TRY(lcol.reserve((size_t)nlong * kLongCols));
     FL_TRY(lval.reserve((size_t)nlong * kLongCols));
-    k_spgemm_long<<<grid_for(nlong, 64), 64, 0, s>>>(A, list.p, nlong, 0, lcol.p, lval.p);
-    FL_TRY_CUDA(cudaGetLastError());
+    k_spgemm_long<<<grid_for(nlong, 64), 64, 0, s>>>(A, list1.p, nlong, 0, lcol.p, lval.p);
   }
+  FL_TRY_CUDA(cudaGetLastError());
   FL_TRY(check_err(err, s, "sparse product row with more distinct columns than the scratch holds"));
   FL_TRY(exclusive_scan_i32(cnt.p, C.ptr.p, Lm.n, s));
   int32_t nnz = 0;
@@ -936,11 +1094,12 @@ int spgemm(const Csr& Lm, const Csr& B, Csr& C, ErrWord* err, cudaStream_t s) {
   C.nnz = nnz;
   FL_TRY(C.col.reserve((size_t)std::max(nnz, 1)));
   FL_TRY(C.val.reserve((size_t)std::max(nnz, 1)));
-  A.cp = C.ptr.p;
-  A.cc = C.col.p;
-  A.cv = C.val.p;
-  k_spgemm<256><<<grid, 256, smem, s>>>(A, 1);
-  if (nlong > 0) k_spgemm_long<<<grid_for(nlong, 64), 64, 0, s>>>(A, list.p, nlong, 1, lcol.p, lval.p);
+  A.cp = Ab.cp = C.ptr.p;
+  A.cc = Ab.cc = C.col.p;
+  A.cv = Ab.cv = C.val.p;
+  k_spgemm_warp<<<gw, kWarpsW * 32, 0, s>>>(A, 1);
+  if (nblock > 0) k_spgemm<256><<<gb, 256, smem, s>>>(Ab, 1);
+  if (nlong > 0) k_spgemm_long<<<grid_for(nlong, 64), 64, 0, s>>>(A, list1.p, nlong, 1, lcol.p, lval.p);
   FL_TRY_CUDA(cudaGetLastError());
   FL_TRY_CUDA(cudaStreamSynchronize(s));  // scratch buffers are released on return
   return FL_OK;
@@ -961,7 +1120,12 @@ int transpose(const Csr& B, Csr& T, cudaStream_t s) {
   k_t_count<<<grid_for(B.nnz, kT), kT, 0, s>>>(B.nnz, B.col.p, cnt.p);
   FL_TRY(exclusive_scan_i32(cnt.p, T.ptr.p, B.m, s));
   k_t_fill<<<grid_for(B.n, kT), kT, 0, s>>>(B.n, B.ptr.p, B.col.p, B.val.p, T.ptr.p, fill.p, T.col.p, T.val.p);
-  k_t_sort<<<grid_for(B.m, kT), kT, 0, s>>>(B.m, T.ptr.p, T.col.p, T.val.p);
+  DevBuf<int32_t> longc;
+  FL_TRY(longc.reserve((size_t)B.m + 1));
+  k_t_sort_blk<<<(unsigned)std::max(1, std::min(B.m, num_sms() * 8)), 256, 0, s>>>(B.m, T.ptr.p, T.col.p, T.val.p,
+                                                                                   longc.p);
+  k_t_sort<<<grid_for(B.m, kT), kT, 0, s>>>(B.m, T.ptr.p, T.col.p, T.val.p, longc.p);
+  FL_TRY_CUDA(cudaStreamSynchronize(s));  // longc is released on return
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
