@@ -519,7 +519,15 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
         "fp64_zero": ("fp64", "zero"), "fp64_previous": ("fp64", "previous"),
         "fp64_learned": ("fp64", "learned"), "mixed_previous": ("reliable", "previous"),
         "mixed_learned": ("reliable", "learned"), "mixed_zero": ("reliable", "zero"),
+        "amg_zero": ("amg", "zero"), "amg_previous": ("amg", "previous"), "amg_learned": ("amg", "learned"),
     }
+    # one AMG hierarchy serves the whole sequence (the matrix does not change)
+    seq.system(ntrain)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    amg = ft.AmgPreconditioner(m, seq.val, seq.ina, stream=stream, unpreconditioned_norm=True)
+    torch.cuda.synchronize()
+    amg_setup_ms = (time.perf_counter() - t0) * 1e3
     res = {k: {"ms": [], "iterations": [], "err": [], "true_rel_residual": []} for k in variants}
     tight = ft.solver_options(ksp="cg", rtol=1e-13, max_its=50000)
     x = torch.empty_like(ps[0])
@@ -529,7 +537,8 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
         ft.petsc_solve(m, ref, val, rhs, tight, inactive=ina, stream=stream)
         scale = ref.abs().max()
         for k, (prec, guess) in variants.items():
-            opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000, precision=prec)
+            opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000,
+                                     precision="fp64" if prec == "amg" else prec)
             torch.cuda.synchronize()
             e0.record(stream)
             if guess == "zero":
@@ -538,7 +547,10 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
                 x.copy_(ps[t - 1])
             else:
                 net.predict(ps[t - 1], ps[t - 2], bs[t], out=x, stream=stream)
-            rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
+            if prec == "amg":
+                rep = amg.solve(x, rhs, ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000), stream=stream)
+            else:
+                rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
             e1.record(stream)
             torch.cuda.synchronize()
             r = res[k]
@@ -552,8 +564,10 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
         summary[k] = {"mean_ms": float(np.mean(r["ms"])), "mean_iterations": float(np.mean(r["iterations"])),
                       "max_err_vs_fp64_tight": float(np.max(r["err"])),
                       "max_true_rel_residual": float(np.max(r["true_rel_residual"]))}
+    amg.close()
     base = summary["fp64_zero"]["mean_ms"]
     return {
+        "amg_setup_ms": amg_setup_ms,
         "workload": f"{nsteps}-step rotating-source Poisson sequence on the {n}^3 P1 mesh; "
                     f"train on steps 2..{ntrain - 1}, CG to rtol 1e-10 on the {nsteps - ntrain} held-out steps",
         "nodes": m.N, "epochs": epochs, "train_steps": ntrain_steps, "train_s": train_s,
@@ -673,13 +687,37 @@ def run_ours(args, rank, ws, dist):
                          "outer": rep["outer_iterations"],
                          "true_rel_residual": rep["true_rel_residual"],
                          "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None}
+        # smoothed-aggregation AMG preconditioner: hierarchy once, then CG
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        amg = ft.AmgPreconditioner(m, val, ina, stream=stream, unpreconditioned_norm=True)
+        torch.cuda.synchronize()
+        amg_setup = time.perf_counter() - t0
+        xg = torch.zeros(N, dtype=torch.float64, device=dev)
+        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=20000, start_from_zero=True)
+        amg.solve(xg, rhs, opts, stream=stream)
+        xg.zero_()
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        rep = amg.solve(xg, rhs, opts, stream=stream)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        out["amg"] = {"ms": s0.elapsed_time(s1), "setup_ms": amg_setup * 1e3, "iterations": rep["iterations"],
+                      "reason": rep["reason_name"], "levels": amg.levels(),
+                      "norm": "unpreconditioned ||r|| / ||b|| (true residual target 1e-10)",
+                      "true_rel_residual": rep["true_rel_residual"],
+                      "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None,
+                      "rel_diff_vs_fp64": None}
+        xs["amg"] = xg
+        amg.close()
         it_bytes = cg_iteration_bytes(N, nnz)
         f64 = out["fp64"]
         f64["achieved_gbs"] = it_bytes * f64["iterations"] / (f64["ms"] * 1e-3) / 1e9
         f64["frac_of_hbm"] = f64["achieved_gbs"] / peak
         xa = torch.from_numpy(src / (3 * np.pi ** 2)).to(dev)
         out["fp64"]["max_err_vs_analytic"] = float((xs["fp64"] - xa).abs().max())
-        for prec in ("mixed", "reliable"):
+        for prec in ("mixed", "reliable", "amg"):
             out[prec]["rel_diff_vs_fp64"] = float(
                 (xs[prec] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
             out[f"speedup_{prec}_vs_fp64"] = f64["ms"] / out[prec]["ms"]

@@ -1024,6 +1024,7 @@ struct fl_amg_t {
   // solve work
   DevBuf<double> bb, y, r, z, p, w, part, bnorm;
   DevBuf<AmgState> st;
+  int unprec = 0;  // 1: convergence test on ||r|| (KSP_NORM_UNPRECONDITIONED)
   cudaStream_t cs = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   ~fl_amg_t() {
@@ -1414,7 +1415,8 @@ void amg_iterations(fl_amg_t* H, int K, cudaStream_t c) {
     k_amg_alpha<<<1, kT, 0, c>>>(st, H->part.p, (int)gl);
     k_amg_xr<<<gv, kT, 0, c>>>(n, st, H->p.p, H->w.p, H->y.p, H->r.p);
     vcycle(H, 0, H->r.p, H->z.p, c);
-    k_dots<<<gv, kT, 0, c>>>(n, H->z.p, H->z.p, H->z.p, H->r.p, H->part.p);
+    const double* nv = H->unprec ? H->r.p : H->z.p;  // the norm of the convergence test
+    k_dots<<<gv, kT, 0, c>>>(n, nv, nv, H->z.p, H->r.p, H->part.p);
     k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 0, nullptr);
     k_amg_p<<<gv, kT, 0, c>>>(n, st, H->z.p, H->p.p);
   }
@@ -1452,6 +1454,12 @@ extern "C" int fl_amg_create(fl_mesh m, const double* val, const uint8_t* inacti
     return st;
   }
   *out = H;
+  return FL_OK;
+}
+
+extern "C" int fl_amg_set_norm(fl_amg H, int32_t unpreconditioned) {
+  FL_CHECK_ARG(H, "null handle");
+  H->unprec = unpreconditioned ? 1 : 0;
   return FL_OK;
 }
 
@@ -1510,14 +1518,16 @@ extern "C" int fl_amg_solve(fl_amg H, const fl_solver_opts* o, const double* rhs
   FL_AMG_G(G, k_amg_lift, gs, c, Aorig, H->ghost, rhs, x, h.guess_zero, H->bb.p, H->y.p);
   FL_AMG_G(G, k_resid, gs, c, A, H->bb.p, H->y.p, H->r.p);
   const double* bn = nullptr;
-  if (!h.guess_zero) {  // rnorm0 = ||B b|| (KSPConvergedDefault with a nonzero guess)
-    vcycle(H, 0, H->bb.p, H->z.p, c);
-    k_dots<<<gv, kT, 0, c>>>(n, H->z.p, H->z.p, nullptr, nullptr, H->part.p);
+  if (!h.guess_zero) {  // rnorm0 = ||B b|| (or ||b||) with a nonzero guess (KSPConvergedDefault)
+    if (!H->unprec) vcycle(H, 0, H->bb.p, H->z.p, c);
+    const double* v = H->unprec ? H->bb.p : H->z.p;
+    k_dots<<<gv, kT, 0, c>>>(n, v, v, nullptr, nullptr, H->part.p);
     k_amg_norm_b<<<1, kT, 0, c>>>(H->part.p, (int)gv, H->bnorm.p);
     bn = H->bnorm.p;
   }
   vcycle(H, 0, H->r.p, H->z.p, c);
-  k_dots<<<gv, kT, 0, c>>>(n, H->z.p, H->z.p, H->z.p, H->r.p, H->part.p);
+  const double* nv = H->unprec ? H->r.p : H->z.p;
+  k_dots<<<gv, kT, 0, c>>>(n, nv, nv, H->z.p, H->r.p, H->part.p);
   k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 1, bn);
   k_amg_p<<<gv, kT, 0, c>>>(n, st, H->z.p, H->p.p);
   FL_TRY_CUDA(cudaGetLastError());

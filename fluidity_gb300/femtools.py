@@ -264,7 +264,7 @@ class AmgPreconditioner:
     the counterpart of petsc_solve's gamg preconditioner.  `val` and
     `inactive` are device tensors that must not change while it is used."""
 
-    def __init__(self, mesh: Mesh, val, inactive=None, stream=None):
+    def __init__(self, mesh: Mesh, val, inactive=None, stream=None, unpreconditioned_norm=False):
         self.lib = mesh.lib
         self.mesh = mesh
         self._keep = (val, inactive)
@@ -272,6 +272,8 @@ class AmgPreconditioner:
         check(self.lib.fl_amg_create(mesh.handle, _ptr(val), _ptr(inactive), _stream_ptr(stream),
                                      C.byref(h)), "fl_amg_create")
         self.handle = h.value
+        if unpreconditioned_norm:
+            check(self.lib.fl_amg_set_norm(self.handle, 1), "fl_amg_set_norm")
 
     def levels(self):
         """[(rows, nonzeros)] of every level, finest first."""

@@ -27,7 +27,9 @@ module fl_gpu_bindings
   public :: fl_mesh_desc, fl_advdif_params, fl_fields, fl_solver_opts, fl_solve_report
   public :: fl_gpu_mesh_register, fl_gpu_mesh_destroy, fl_gpu_mesh_info, &
             fl_gpu_sparsity_copy, fl_gpu_colouring_copy, fl_gpu_make_global_numbering_p2, &
-            fl_gpu_assemble_advdif_cg, fl_gpu_apply_dirichlet, fl_gpu_petsc_solve
+            fl_gpu_assemble_advdif_cg, fl_gpu_apply_dirichlet, fl_gpu_petsc_solve, &
+            fl_gpu_pattern_register, fl_dev_petsc_solve, fl_amg_create, fl_amg_solve, fl_amg_destroy, &
+            fl_batch_create, fl_batch_add, fl_batch_run, fl_batch_destroy, fl_set_assembly_tiles
   public :: gpu_check
 
   integer(c_int), parameter, public :: FL_OK = 0
@@ -144,6 +146,91 @@ module fl_gpu_bindings
        type(fl_solve_report), intent(out) :: report
        integer(c_int) :: st
      end function fl_gpu_petsc_solve
+
+     ! device-pointer solve (arrays already on the GPU, e.g. from
+     ! fl_dev_assemble_advdif_cg); stream may be c_null_ptr
+     function fl_dev_petsc_solve(handle, opts, val, inactive, rhs, x, report, stream) &
+          bind(c, name="fl_dev_petsc_solve") result(st)
+       import :: c_int, c_ptr, fl_solver_opts, fl_solve_report
+       type(c_ptr), value :: handle
+       type(fl_solver_opts), intent(in) :: opts
+       type(c_ptr), value :: val, inactive, rhs, x, stream
+       type(fl_solve_report), intent(out) :: report
+       integer(c_int) :: st
+     end function fl_dev_petsc_solve
+
+     ! a handle for a matrix read from a matrixdump (tools/petsc_readnsolve.F90)
+     function fl_gpu_pattern_register(n, findrm, colm, base, handle) &
+          bind(c, name="fl_gpu_pattern_register") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       integer(c_int32_t), value :: n, base
+       type(c_ptr), value :: findrm, colm
+       type(c_ptr), intent(out) :: handle
+       integer(c_int) :: st
+     end function fl_gpu_pattern_register
+
+     ! smoothed-aggregation AMG for CG (the gamg preconditioner option);
+     ! device pointers, the hierarchy is reused while the matrix is unchanged
+     ! (cache_solver_context)
+     function fl_amg_create(handle, val, inactive, stream, amg) bind(c, name="fl_amg_create") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: handle, val, inactive, stream
+       type(c_ptr), intent(out) :: amg
+       integer(c_int) :: st
+     end function fl_amg_create
+
+     function fl_amg_solve(amg, opts, rhs, x, report, stream) bind(c, name="fl_amg_solve") result(st)
+       import :: c_int, c_ptr, fl_solver_opts, fl_solve_report
+       type(c_ptr), value :: amg, rhs, x, stream
+       type(fl_solver_opts), intent(in) :: opts
+       type(fl_solve_report), intent(out) :: report
+       integer(c_int) :: st
+     end function fl_amg_solve
+
+     function fl_amg_destroy(amg) bind(c, name="fl_amg_destroy") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: amg
+       integer(c_int) :: st
+     end function fl_amg_destroy
+
+     ! several solve_field_equation_cg steps (fields or meshes) as CUDA graphs
+     function fl_batch_create(batch) bind(c, name="fl_batch_create") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), intent(out) :: batch
+       integer(c_int) :: st
+     end function fl_batch_create
+
+     function fl_batch_add(batch, handle, params, fields, nb, bc_nodes, base, bc_values, opts, &
+          val, rhs, inactive, x) bind(c, name="fl_batch_add") result(st)
+       import :: c_int, c_ptr, c_int32_t, fl_advdif_params, fl_fields, fl_solver_opts
+       type(c_ptr), value :: batch, handle, bc_nodes, bc_values, val, rhs, inactive, x
+       type(fl_advdif_params), intent(in) :: params
+       type(fl_fields), intent(in) :: fields
+       type(fl_solver_opts), intent(in) :: opts
+       integer(c_int32_t), value :: nb, base
+       integer(c_int) :: st
+     end function fl_batch_add
+
+     function fl_batch_run(batch, stream, reports) bind(c, name="fl_batch_run") result(st)
+       import :: c_int, c_ptr, fl_solve_report
+       type(c_ptr), value :: batch, stream
+       type(fl_solve_report), intent(out) :: reports(*)
+       integer(c_int) :: st
+     end function fl_batch_run
+
+     function fl_batch_destroy(batch) bind(c, name="fl_batch_destroy") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: batch
+       integer(c_int) :: st
+     end function fl_batch_destroy
+
+     function fl_set_assembly_tiles(handle, elem_block, elem_blocks_per_sm, row_tile) &
+          bind(c, name="fl_set_assembly_tiles") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: handle
+       integer(c_int32_t), value :: elem_block, elem_blocks_per_sm, row_tile
+       integer(c_int) :: st
+     end function fl_set_assembly_tiles
   end interface
 
 contains

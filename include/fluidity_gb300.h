@@ -311,6 +311,10 @@ int fl_amg_create(fl_mesh mesh, const double* val, const uint8_t* inactive, void
 int fl_amg_solve(fl_amg amg, const fl_solver_opts* opts, const double* rhs, double* x,
                  fl_solve_report* report, void* stream);
 int fl_amg_levels(fl_amg amg, int32_t* levels, int64_t* rows, int64_t* nnz, int32_t capacity);
+/* Norm of the convergence test: 0 (default) the preconditioned residual
+ * ||B r||, PETSc's default for CG; 1 the residual ||r|| itself
+ * (KSP_NORM_UNPRECONDITIONED), so that rtol bounds ||b - A x|| / ||b||. */
+int fl_amg_set_norm(fl_amg amg, int32_t unpreconditioned);
 int fl_amg_destroy(fl_amg amg);
 
 /* ------------------------------------------------- learned warm start -- */

@@ -87,3 +87,17 @@ def test_amg_is_deterministic_and_reusable():
     assert r4["reason"] == -3 and r4["iterations"] == 3
     a1.close()
     a2.close()
+
+
+def test_amg_unpreconditioned_norm_bounds_the_true_residual():
+    import torch
+    m, val, rhs, ina = _system(14)
+    amg = ft.AmgPreconditioner(m, val, ina, unpreconditioned_norm=True)
+    for guess in ("zero", "nonzero"):
+        x = torch.zeros(m.N, dtype=torch.float64, device="cuda")
+        if guess == "nonzero":
+            x += 0.01
+        r = amg.solve(x, rhs, ft.solver_options(ksp="cg", rtol=1e-10))
+        assert r["reason"] == 2
+        assert r["true_rel_residual"] <= 1.5e-10, r
+    amg.close()
