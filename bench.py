@@ -526,6 +526,7 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     amg = ft.AmgPreconditioner(m, seq.val, seq.ina, stream=stream, unpreconditioned_norm=True)
+    amg.set_precision(True)  # FP32 V-cycle inside the FP64 CG
     torch.cuda.synchronize()
     amg_setup_ms = (time.perf_counter() - t0) * 1e3
     res = {k: {"ms": [], "iterations": [], "err": [], "true_rel_residual": []} for k in variants}
@@ -693,23 +694,26 @@ def run_ours(args, rank, ws, dist):
         amg = ft.AmgPreconditioner(m, val, ina, stream=stream, unpreconditioned_norm=True)
         torch.cuda.synchronize()
         amg_setup = time.perf_counter() - t0
-        xg = torch.zeros(N, dtype=torch.float64, device=dev)
         opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=20000, start_from_zero=True)
-        amg.solve(xg, rhs, opts, stream=stream)
-        xg.zero_()
-        torch.cuda.synchronize()
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        rep = amg.solve(xg, rhs, opts, stream=stream)
-        s1.record(stream)
-        torch.cuda.synchronize()
-        out["amg"] = {"ms": s0.elapsed_time(s1), "setup_ms": amg_setup * 1e3, "iterations": rep["iterations"],
-                      "reason": rep["reason_name"], "levels": amg.levels(),
-                      "norm": "unpreconditioned ||r|| / ||b|| (true residual target 1e-10)",
-                      "true_rel_residual": rep["true_rel_residual"],
-                      "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None,
-                      "rel_diff_vs_fp64": None}
-        xs["amg"] = xg
+        for key, fp32 in (("amg", False), ("amg_fp32_cycle", True)):
+            amg.set_precision(fp32)
+            xg = torch.zeros(N, dtype=torch.float64, device=dev)
+            amg.solve(xg, rhs, opts, stream=stream)
+            xg.zero_()
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            rep = amg.solve(xg, rhs, opts, stream=stream)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            out[key] = {"ms": s0.elapsed_time(s1), "setup_ms": amg_setup * 1e3, "iterations": rep["iterations"],
+                        "reason": rep["reason_name"], "levels": amg.levels(),
+                        "norm": "unpreconditioned ||r|| / ||b|| (true residual target 1e-10)",
+                        "cycle": "fp32" if fp32 else "fp64",
+                        "true_rel_residual": rep["true_rel_residual"],
+                        "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None,
+                        "rel_diff_vs_fp64": None}
+            xs[key] = xg
         amg.close()
         it_bytes = cg_iteration_bytes(N, nnz)
         f64 = out["fp64"]
@@ -717,7 +721,7 @@ def run_ours(args, rank, ws, dist):
         f64["frac_of_hbm"] = f64["achieved_gbs"] / peak
         xa = torch.from_numpy(src / (3 * np.pi ** 2)).to(dev)
         out["fp64"]["max_err_vs_analytic"] = float((xs["fp64"] - xa).abs().max())
-        for prec in ("mixed", "reliable", "amg"):
+        for prec in ("mixed", "reliable", "amg", "amg_fp32_cycle"):
             out[prec]["rel_diff_vs_fp64"] = float(
                 (xs[prec] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
             out[f"speedup_{prec}_vs_fp64"] = f64["ms"] / out[prec]["ms"]

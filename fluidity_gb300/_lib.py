@@ -84,7 +84,7 @@ EXPORTS = [
     "fl_gnn_num_params", "fl_gnn_create", "fl_gnn_destroy", "fl_gnn_set_weights",
     "fl_gnn_get_weights", "fl_gnn_predict", "fl_gnn_gradients", "fl_gnn_train_step",
     "fl_gnn_set_loss", "fl_gpu_pattern_register",
-    "fl_amg_create", "fl_amg_solve", "fl_amg_levels", "fl_amg_destroy", "fl_amg_set_norm",
+    "fl_amg_create", "fl_amg_solve", "fl_amg_levels", "fl_amg_destroy", "fl_amg_set_norm", "fl_amg_set_precision",
 ]
 
 _P = C.c_void_p
@@ -135,6 +135,7 @@ _SIGNATURES = {
     "fl_amg_levels": (C.c_int, [_P, C.POINTER(C.c_int32), _P, _P, _I32]),
     "fl_amg_destroy": (C.c_int, [_P]),
     "fl_amg_set_norm": (C.c_int, [_P, _I32]),
+    "fl_amg_set_precision": (C.c_int, [_P, _I32]),
     "fl_gnn_create": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "fl_gnn_destroy": (C.c_int, [_P]),
     "fl_gnn_set_weights": (C.c_int, [_P, _P, _I32]),

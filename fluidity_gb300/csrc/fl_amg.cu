@@ -642,12 +642,14 @@ __global__ void k_smooth_p(int n, const int32_t* __restrict__ ptr, const int32_t
 // and stored column-major (entry j of the slice's rows contiguous), so that
 // one thread per row reads coalesced values; padding has the row's own column
 // and value 0.  Terms are summed in the row's CSR order.
-struct SellOp {
+template <class T>
+struct SellOpT {
   int32_t n;
   const int32_t* sptr;
   const int32_t* col;
-  const double* val;
+  const T* val;
 };
+typedef SellOpT<double> SellOp;
 
 __global__ void k_sl_width(int n, const int32_t* __restrict__ ptr, int32_t* __restrict__ w) {
   note_launch();
@@ -677,106 +679,143 @@ __global__ void k_sl_fill(int n, const int32_t* __restrict__ ptr, const int32_t*
   }
 }
 
-__device__ __forceinline__ double sell_dot(const SellOp& S, const double* __restrict__ x, int r) {
+template <class T>
+__device__ __forceinline__ T sell_dot(const SellOpT<T>& S, const T* __restrict__ x, int r) {
   const int sl = r >> 5;
   const int b = __ldg(S.sptr + sl) + (r & 31), e = __ldg(S.sptr + sl + 1);
-  double s = 0.0;
+  T s = 0;
   for (int k = b; k < e; k += 32) s += __ldg(S.val + k) * __ldg(x + __ldg(S.col + k));
   return s;
 }
 
-__global__ void k_cheb_sl(SellOp A, const double* __restrict__ dinv, const double* __restrict__ b,
-                          const double* __restrict__ x, double* __restrict__ d, double c1, double c2,
-                          double* __restrict__ xo) {
+// The V-cycle kernels compute in T (double, or float for the FP32 cycle);
+// the finest level reads its rhs (TB) and writes its result (TO) in FP64.
+// r = b - A x;  d = c1 d + c2 D^-1 r;  xo = x + d   (xo != x)
+template <class T, class TB, class TO>
+__global__ void k_cheb_sl(SellOpT<T> A, const T* __restrict__ dinv, const TB* __restrict__ b,
+                          const T* __restrict__ x, T* __restrict__ d, T c1, T c2, TO* __restrict__ xo) {
   note_launch();
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
-    const double r = b[row] - sell_dot(A, x, row);
-    const double dn = (c1 != 0.0 ? c1 * d[row] : 0.0) + c2 * dinv[row] * r;
+    const T r = (T)b[row] - sell_dot(A, x, row);
+    const T dn = (c1 != (T)0 ? c1 * d[row] : (T)0) + c2 * dinv[row] * r;
     d[row] = dn;
-    xo[row] = x[row] + dn;
+    xo[row] = (TO)(x[row] + dn);
   }
 }
 
-__global__ void k_resid_sl(SellOp A, const double* __restrict__ b, const double* __restrict__ x,
-                           double* __restrict__ r) {
+template <class T, class TB>
+__global__ void k_resid_sl(SellOpT<T> A, const TB* __restrict__ b, const T* __restrict__ x, T* __restrict__ r) {
   note_launch();
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x)
-    r[row] = b[row] - sell_dot(A, x, row);
+    r[row] = (T)b[row] - sell_dot(A, x, row);
 }
 
 // ----------------------------------------------------------- V-cycle --
-struct Op {  // a CSR operator and its row grouping
+template <class T>
+struct OpT {  // a CSR operator
   int32_t n;
   const int32_t* ptr;
   const int32_t* col;
-  const double* val;
+  const T* val;
 };
+typedef OpT<double> Op;
+
+template <int G, class T>
+__device__ __forceinline__ T csr_rowT(const OpT<T>& A, const T* __restrict__ x, int row, int sub, bool valid) {
+  int b = 0, e = 0;
+  if (valid) {
+    b = __ldg(A.ptr + row);
+    e = __ldg(A.ptr + row + 1);
+  }
+  T s = 0;
+  for (int k = b + sub; k < e; k += G) s += __ldg(A.val + k) * __ldg(x + __ldg(A.col + k));
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+  return s;
+}
 
 // x = d = (D^-1 b) / theta   (first Chebyshev step from a zero guess)
-__global__ void k_cheb0(int n, const double* __restrict__ dinv, const double* __restrict__ b, double ith,
-                        double* __restrict__ x, double* __restrict__ d) {
+template <class T, class TB>
+__global__ void k_cheb0(int n, const T* __restrict__ dinv, const TB* __restrict__ b, T ith, T* __restrict__ x,
+                        T* __restrict__ d) {
   note_launch();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double v = dinv[i] * b[i] * ith;
+    const T v = dinv[i] * (T)b[i] * ith;
     d[i] = v;
     x[i] = v;
   }
 }
 
-// r = b - A x;  d = c1 d + c2 D^-1 r;  xo = x + d   (xo != x)
-template <int G>
-__global__ void k_cheb(Op A, const double* __restrict__ dinv, const double* __restrict__ b,
-                       const double* __restrict__ x, double* __restrict__ d, double c1, double c2,
-                       double* __restrict__ xo) {
+template <int G, class T, class TB, class TO>
+__global__ void k_cheb(OpT<T> A, const T* __restrict__ dinv, const TB* __restrict__ b, const T* __restrict__ x,
+                       T* __restrict__ d, T c1, T c2, TO* __restrict__ xo) {
   note_launch();
   const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
-    const double ax = csr_row<G>(A.ptr, A.col, A.val, x, row, sub, row < A.n);
+    const T ax = csr_rowT<G>(A, x, row, sub, row < A.n);
     if (row < A.n && sub == 0) {
-      const double r = b[row] - ax;
-      const double dn = (c1 != 0.0 ? c1 * d[row] : 0.0) + c2 * dinv[row] * r;
+      const T r = (T)b[row] - ax;
+      const T dn = (c1 != (T)0 ? c1 * d[row] : (T)0) + c2 * dinv[row] * r;
       d[row] = dn;
-      xo[row] = x[row] + dn;
+      xo[row] = (TO)(x[row] + dn);
     }
   }
 }
 
-// r = b - A x
+// r = b - A x (FP64; the solve's own residuals)
 template <int G>
 __global__ void k_resid(Op A, const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ r) {
   note_launch();
   const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
-    const double ax = csr_row<G>(A.ptr, A.col, A.val, x, row, sub, row < A.n);
+    const double ax = csr_rowT<G>(A, x, row, sub, row < A.n);
     if (row < A.n && sub == 0) r[row] = b[row] - ax;
   }
 }
 
-// y = A x (+ z when z is not null)
-template <int G>
-__global__ void k_spmv_add(Op A, const double* __restrict__ x, const double* z, double* y) {
+template <int G, class T, class TB>
+__global__ void k_residT(OpT<T> A, const TB* __restrict__ b, const T* __restrict__ x, T* __restrict__ r) {
   note_launch();
   const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
-    const double ax = csr_row<G>(A.ptr, A.col, A.val, x, row, sub, row < A.n);
-    if (row < A.n && sub == 0) y[row] = (z ? z[row] : 0.0) + ax;
+    const T ax = csr_rowT<G>(A, x, row, sub, row < A.n);
+    if (row < A.n && sub == 0) r[row] = (T)b[row] - ax;
+  }
+}
+
+// y = A x (+ z when z is not null)
+template <int G, class T>
+__global__ void k_spmv_add(OpT<T> A, const T* __restrict__ x, const T* z, T* y) {
+  note_launch();
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), gpb = blockDim.x / G;
+  for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
+    const int row = base + threadIdx.x / G;
+    const T ax = csr_rowT<G>(A, x, row, sub, row < A.n);
+    if (row < A.n && sub == 0) y[row] = (z ? z[row] : (T)0) + ax;
   }
 }
 
 // coarsest level: x = Ainv b, one warp per row, terms in column order
-__global__ void k_dense(int n, const double* __restrict__ inv, const double* __restrict__ b, double* __restrict__ x) {
+template <class T, class TB, class TO>
+__global__ void k_dense(int n, const T* __restrict__ inv, const TB* __restrict__ b, TO* __restrict__ x) {
   note_launch();
   const int lane = threadIdx.x & 31;
   for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < n; row += gridDim.x * (blockDim.x >> 5)) {
-    double s = 0.0;
-    for (int j = lane; j < n; j += 32) s += inv[(int64_t)row * n + j] * b[j];
+    T s = 0;
+    for (int j = lane; j < n; j += 32) s += inv[(int64_t)row * n + j] * (T)b[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) x[row] = s;
+    if (lane == 0) x[row] = (TO)s;
   }
+}
+
+__global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  note_launch();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
 }
 
 // ------------------------------------------------------------ PCG --
@@ -1010,6 +1049,8 @@ struct AmgLevel {
   DevBuf<double> sval;
   bool sell = false;
   DevBuf<double> dinv, x0, x1, d, b, r, xc;  // xc: the V-cycle's result on this level
+  // single-precision copies of the operators and work vectors (FP32 cycle)
+  DevBuf<float> Af, Pf, Rf, sf, dinvf, x0f, x1f, df, bf, rf, xcf;
   double rho = 2.0;  // Gershgorin bound of the spectrum of D^-1 A
   int G = 2, GP = 2, GR = 2;  // lanes per row of A, P and R
 };
@@ -1025,6 +1066,8 @@ struct fl_amg_t {
   DevBuf<double> bb, y, r, z, p, w, part, bnorm;
   DevBuf<AmgState> st;
   int unprec = 0;  // 1: convergence test on ||r|| (KSP_NORM_UNPRECONDITIONED)
+  int fp32 = 0;    // 1: the V-cycle runs in FP32 (operators and vectors)
+  DevBuf<float> cinvf;
   cudaStream_t cs = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   ~fl_amg_t() {
@@ -1279,39 +1322,106 @@ Cheb cheb_of(double rho) {
   return Cheb{1.0 / th, r1 * r0, 2.0 * r1 / de};
 }
 
-// x_l = V(b_l), all on stream s (capturable)
-void vcycle(fl_amg_t* H, int l, const double* b, double* x, cudaStream_t s) {
+// the operators and vectors of a level in the cycle's precision
+template <class T>
+struct View {
+  const T *Av, *Pv, *Rv, *sv, *dinv;
+  T *x0, *x1, *d, *b, *r, *xc;
+};
+View<double> view(AmgLevel& L, double*) {
+  return View<double>{L.A.val.p, L.P.val.p, L.R.val.p, L.sval.p, L.dinv.p,
+                      L.x0.p,    L.x1.p,    L.d.p,     L.b.p,    L.r.p,    L.xc.p};
+}
+View<float> view(AmgLevel& L, float*) {
+  return View<float>{L.Af.p, L.Pf.p, L.Rf.p, L.sf.p, L.dinvf.p, L.x0f.p, L.x1f.p, L.df.p, L.bf.p, L.rf.p, L.xcf.p};
+}
+
+#define FL_AMG_SWITCH(G, CALL)            \
+  switch (G) {                            \
+    case 32: { constexpr int GG = 32; CALL; } break; \
+    case 16: { constexpr int GG = 16; CALL; } break; \
+    case 8: { constexpr int GG = 8; CALL; } break;   \
+    case 4: { constexpr int GG = 4; CALL; } break;   \
+    default: { constexpr int GG = 2; CALL; } break;  \
+  }
+
+// x_l = V(b_l), all on stream s (capturable); T the arithmetic of the cycle,
+// TB / TO the types of its rhs and result (FP64 on the finest level)
+template <class T, class TB, class TO>
+void vcycle(fl_amg_t* H, int l, const TB* b, TO* x, cudaStream_t s) {
   if (l == (int)H->L.size() - 1) {
-    k_dense<<<grid_for((int64_t)H->nc * 32, kT, 4), kT, 0, s>>>(H->nc, H->cinv.p, b, x);
+    const T* inv = nullptr;
+    if constexpr (sizeof(T) == 8) inv = reinterpret_cast<const T*>(H->cinv.p);
+    else inv = reinterpret_cast<const T*>(H->cinvf.p);
+    k_dense<T, TB, TO><<<grid_for((int64_t)H->nc * 32, kT, 4), kT, 0, s>>>(H->nc, inv, b, x);
     return;
   }
   AmgLevel& Lv = *H->L[l];
   AmgLevel& Ln = *H->L[l + 1];
+  const View<T> V = view(Lv, (T*)nullptr), W = view(Ln, (T*)nullptr);
   const int n = Lv.A.n, G = Lv.G;
-  const Op A = op_of(Lv.A);
+  const OpT<T> A{n, Lv.A.ptr.p, Lv.A.col.p, V.Av};
+  const SellOpT<T> S{n, Lv.sptr.p, Lv.scol.p, V.sv};
   const Cheb c = cheb_of(Lv.rho);
-  const unsigned gv = grid_for(n, kT, 4), gs = grid_for((int64_t)n * G, kT, 8);
-  const SellOp S{n, Lv.sptr.p, Lv.scol.p, Lv.sval.p};
-  const unsigned gl = grid_for(n, kT, 8);
+  const T ith = (T)c.ith, c1 = (T)c.c1, c2 = (T)c.c2;
+  const unsigned gv = grid_for(n, kT, 4), gs = grid_for((int64_t)n * G, kT, 8), gl = grid_for(n, kT, 8);
   // pre-smoothing from zero: two Chebyshev steps (one product)
-  k_cheb0<<<gv, kT, 0, s>>>(n, Lv.dinv.p, b, c.ith, Lv.x0.p, Lv.d.p);
-  if (Lv.sell) k_cheb_sl<<<gl, kT, 0, s>>>(S, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, c.c1, c.c2, Lv.x1.p);
-  else FL_AMG_G(G, k_cheb, gs, s, A, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, c.c1, c.c2, Lv.x1.p);
+  k_cheb0<T, TB><<<gv, kT, 0, s>>>(n, V.dinv, b, ith, V.x0, V.d);
+  if (Lv.sell) k_cheb_sl<T, TB, T><<<gl, kT, 0, s>>>(S, V.dinv, b, V.x0, V.d, c1, c2, V.x1);
+  else FL_AMG_SWITCH(G, (k_cheb<GG, T, TB, T><<<gs, kT, 0, s>>>(A, V.dinv, b, V.x0, V.d, c1, c2, V.x1)));
   // restriction of the residual, coarse correction, prolongation
-  if (Lv.sell) k_resid_sl<<<gl, kT, 0, s>>>(S, b, Lv.x1.p, Lv.r.p);
-  else FL_AMG_G(G, k_resid, gs, s, A, b, Lv.x1.p, Lv.r.p);
-  const unsigned gr = grid_for((int64_t)Ln.A.n * Lv.GR, kT, 8);
-  FL_AMG_G(Lv.GR, k_spmv_add, gr, s, op_of(Lv.R), Lv.r.p, nullptr, Ln.b.p);
-  vcycle(H, l + 1, Ln.b.p, Ln.xc.p, s);
-  FL_AMG_G(Lv.GP, k_spmv_add, grid_for((int64_t)n * Lv.GP, kT, 8), s, op_of(Lv.P), Ln.xc.p, Lv.x1.p, Lv.x0.p);
+  if (Lv.sell) k_resid_sl<T, TB><<<gl, kT, 0, s>>>(S, b, V.x1, V.r);
+  else FL_AMG_SWITCH(G, (k_residT<GG, T, TB><<<gs, kT, 0, s>>>(A, b, V.x1, V.r)));
+  const OpT<T> R{Ln.A.n, Lv.R.ptr.p, Lv.R.col.p, V.Rv};
+  const OpT<T> P{n, Lv.P.ptr.p, Lv.P.col.p, V.Pv};
+  const unsigned gr = grid_for((int64_t)Ln.A.n * Lv.GR, kT, 8), gp = grid_for((int64_t)n * Lv.GP, kT, 8);
+  FL_AMG_SWITCH(Lv.GR, (k_spmv_add<GG, T><<<gr, kT, 0, s>>>(R, V.r, (const T*)nullptr, W.b)));
+  vcycle<T, T, T>(H, l + 1, W.b, W.xc, s);
+  FL_AMG_SWITCH(Lv.GP, (k_spmv_add<GG, T><<<gp, kT, 0, s>>>(P, W.xc, V.x1, V.x0)));
   // post-smoothing: two Chebyshev steps from the corrected guess
   if (Lv.sell) {
-    k_cheb_sl<<<gl, kT, 0, s>>>(S, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, 0.0, c.ith, Lv.x1.p);
-    k_cheb_sl<<<gl, kT, 0, s>>>(S, Lv.dinv.p, b, Lv.x1.p, Lv.d.p, c.c1, c.c2, x);
+    k_cheb_sl<T, TB, T><<<gl, kT, 0, s>>>(S, V.dinv, b, V.x0, V.d, (T)0, ith, V.x1);
+    k_cheb_sl<T, TB, TO><<<gl, kT, 0, s>>>(S, V.dinv, b, V.x1, V.d, c1, c2, x);
   } else {
-    FL_AMG_G(G, k_cheb, gs, s, A, Lv.dinv.p, b, Lv.x0.p, Lv.d.p, 0.0, c.ith, Lv.x1.p);
-    FL_AMG_G(G, k_cheb, gs, s, A, Lv.dinv.p, b, Lv.x1.p, Lv.d.p, c.c1, c.c2, x);
+    FL_AMG_SWITCH(G, (k_cheb<GG, T, TB, T><<<gs, kT, 0, s>>>(A, V.dinv, b, V.x0, V.d, (T)0, ith, V.x1)));
+    FL_AMG_SWITCH(G, (k_cheb<GG, T, TB, TO><<<gs, kT, 0, s>>>(A, V.dinv, b, V.x1, V.d, c1, c2, x)));
   }
+}
+
+// the preconditioner z = B r in the handle's precision
+void precondition(fl_amg_t* H, const double* r, double* z, cudaStream_t s) {
+  if (H->fp32) vcycle<float, double, double>(H, 0, r, z, s);
+  else vcycle<double, double, double>(H, 0, r, z, s);
+}
+
+// single-precision copies of every level's operators and vectors
+int make_fp32(fl_amg_t* H, cudaStream_t s) {
+  auto conv = [&](const double* a, DevBuf<float>& b, int64_t n) -> int {
+    FL_TRY(b.reserve((size_t)std::max<int64_t>(n, 1)));
+    if (n > 0) k_to_float<<<grid_for(n, kT), kT, 0, s>>>(n, a, b.p);
+    return FL_OK;
+  };
+  for (size_t l = 0; l < H->L.size(); ++l) {
+    AmgLevel& L = *H->L[l];
+    const int n = L.A.n;
+    FL_TRY(conv(L.A.val.p, L.Af, L.A.nnz));
+    FL_TRY(conv(L.dinv.p, L.dinvf, n));
+    if (L.sell) FL_TRY(conv(L.sval.p, L.sf, (int64_t)L.sval.n));
+    if (l + 1 < H->L.size()) {
+      FL_TRY(conv(L.P.val.p, L.Pf, L.P.nnz));
+      FL_TRY(conv(L.R.val.p, L.Rf, L.R.nnz));
+    }
+    FL_TRY(L.x0f.reserve(n));
+    FL_TRY(L.x1f.reserve(n));
+    FL_TRY(L.df.reserve(n));
+    FL_TRY(L.bf.reserve(n));
+    FL_TRY(L.rf.reserve(n));
+    FL_TRY(L.xcf.reserve(n));
+  }
+  FL_TRY(conv(H->cinv.p, H->cinvf, (int64_t)H->nc * H->nc));
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  return FL_OK;
 }
 
 }  // namespace
@@ -1414,7 +1524,7 @@ void amg_iterations(fl_amg_t* H, int K, cudaStream_t c) {
     k_amg_ap_sl<<<gl, kT, 0, c>>>(S, st, H->p.p, H->w.p, H->part.p);
     k_amg_alpha<<<1, kT, 0, c>>>(st, H->part.p, (int)gl);
     k_amg_xr<<<gv, kT, 0, c>>>(n, st, H->p.p, H->w.p, H->y.p, H->r.p);
-    vcycle(H, 0, H->r.p, H->z.p, c);
+    precondition(H, H->r.p, H->z.p, c);
     const double* nv = H->unprec ? H->r.p : H->z.p;  // the norm of the convergence test
     k_dots<<<gv, kT, 0, c>>>(n, nv, nv, H->z.p, H->r.p, H->part.p);
     k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 0, nullptr);
@@ -1460,6 +1570,13 @@ extern "C" int fl_amg_create(fl_mesh m, const double* val, const uint8_t* inacti
 extern "C" int fl_amg_set_norm(fl_amg H, int32_t unpreconditioned) {
   FL_CHECK_ARG(H, "null handle");
   H->unprec = unpreconditioned ? 1 : 0;
+  return FL_OK;
+}
+
+extern "C" int fl_amg_set_precision(fl_amg H, int32_t fp32) {
+  FL_CHECK_ARG(H, "null handle");
+  if (fp32 && !H->cinvf.p) FL_TRY(make_fp32(H, H->cs));
+  H->fp32 = fp32 ? 1 : 0;
   return FL_OK;
 }
 
@@ -1519,13 +1636,13 @@ extern "C" int fl_amg_solve(fl_amg H, const fl_solver_opts* o, const double* rhs
   FL_AMG_G(G, k_resid, gs, c, A, H->bb.p, H->y.p, H->r.p);
   const double* bn = nullptr;
   if (!h.guess_zero) {  // rnorm0 = ||B b|| (or ||b||) with a nonzero guess (KSPConvergedDefault)
-    if (!H->unprec) vcycle(H, 0, H->bb.p, H->z.p, c);
+    if (!H->unprec) precondition(H, H->bb.p, H->z.p, c);
     const double* v = H->unprec ? H->bb.p : H->z.p;
     k_dots<<<gv, kT, 0, c>>>(n, v, v, nullptr, nullptr, H->part.p);
     k_amg_norm_b<<<1, kT, 0, c>>>(H->part.p, (int)gv, H->bnorm.p);
     bn = H->bnorm.p;
   }
-  vcycle(H, 0, H->r.p, H->z.p, c);
+  precondition(H, H->r.p, H->z.p, c);
   const double* nv = H->unprec ? H->r.p : H->z.p;
   k_dots<<<gv, kT, 0, c>>>(n, nv, nv, H->z.p, H->r.p, H->part.p);
   k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 1, bn);

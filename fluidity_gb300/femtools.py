@@ -275,6 +275,10 @@ class AmgPreconditioner:
         if unpreconditioned_norm:
             check(self.lib.fl_amg_set_norm(self.handle, 1), "fl_amg_set_norm")
 
+    def set_precision(self, fp32: bool):
+        """FP32 (True) or FP64 (False) arithmetic inside the V-cycle."""
+        check(self.lib.fl_amg_set_precision(self.handle, int(fp32)), "fl_amg_set_precision")
+
     def levels(self):
         """[(rows, nonzeros)] of every level, finest first."""
         cap = 16

@@ -315,6 +315,10 @@ int fl_amg_levels(fl_amg amg, int32_t* levels, int64_t* rows, int64_t* nnz, int3
  * ||B r||, PETSc's default for CG; 1 the residual ||r|| itself
  * (KSP_NORM_UNPRECONDITIONED), so that rtol bounds ||b - A x|| / ||b||. */
 int fl_amg_set_norm(fl_amg amg, int32_t unpreconditioned);
+/* Arithmetic of the V-cycle: 0 (default) FP64; 1 FP32 operators and vectors
+ * inside the cycle (a single-precision preconditioner for the FP64 CG, whose
+ * residuals, dot products and convergence test stay in FP64). */
+int fl_amg_set_precision(fl_amg amg, int32_t fp32);
 int fl_amg_destroy(fl_amg amg);
 
 /* ------------------------------------------------- learned warm start -- */

@@ -101,3 +101,26 @@ def test_amg_unpreconditioned_norm_bounds_the_true_residual():
         assert r["reason"] == 2
         assert r["true_rel_residual"] <= 1.5e-10, r
     amg.close()
+
+
+def test_amg_fp32_cycle():
+    """A single-precision V-cycle inside the FP64 CG reaches the same FP64
+    tolerance and solution."""
+    import torch
+    m, val, rhs, ina = _system(14)
+    opts = ft.solver_options(ksp="cg", rtol=1e-10)
+    amg = ft.AmgPreconditioner(m, val, ina, unpreconditioned_norm=True)
+    x64 = torch.zeros(m.N, dtype=torch.float64, device="cuda")
+    r64 = amg.solve(x64, rhs, opts)
+    amg.set_precision(True)
+    x32 = torch.zeros_like(x64)
+    r32 = amg.solve(x32, rhs, opts)
+    assert r32["reason"] == 2 and r32["true_rel_residual"] <= 1.5e-10
+    assert r32["iterations"] <= 1.3 * r64["iterations"] + 2
+    assert torch.allclose(x32, x64, rtol=0, atol=1e-8 * x64.abs().max().item())
+    # and back to FP64: the same bits as before
+    amg.set_precision(False)
+    x = torch.zeros_like(x64)
+    amg.solve(x, rhs, opts)
+    assert torch.equal(x, x64)
+    amg.close()
