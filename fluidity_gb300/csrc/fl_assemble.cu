@@ -384,6 +384,9 @@ struct DfArgs {
   int have_mass, have_src, aniso;
 };
 
+// Specialised on the term set (consistent mass, source, old field t,
+// diagonal kappa) so that each instance carries only its own work.
+template <bool MASS, bool SRC, bool TF, bool ANISO>
 __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   note_launch();
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
@@ -415,7 +418,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int a = 0; a < 3; ++a) kc[i][a] = A.aniso ? df_mul(A.kdiag[a], cof[a][i]) : cof[a][i];
+      for (int a = 0; a < 3; ++a) kc[i][a] = ANISO ? df_mul(A.kdiag[a], cof[a][i]) : cof[a][i];
     df G[4][4];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -432,7 +435,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
     G[3][3] = df_neg(df_add(df_add(G[0][3], G[1][3]), G[2][3]));
     const df ks = df_mul(A.kscale, rdet);
     df madet0 = {0.0f, 0.0f}, madet1 = {0.0f, 0.0f};
-    if (A.have_mass) {
+    if (MASS) {
       madet0 = df_mul(adet, A.m0);
       madet1 = df_mul(adet, A.m1);
     }
@@ -442,14 +445,14 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
 #pragma unroll
       for (int j = i; j < 4; ++j) {
         df m = df_mul(G[i][j], ks);
-        if (A.have_mass) m = df_add(m, i == j ? madet0 : madet1);
+        if (MASS) m = df_add(m, i == j ? madet0 : madet1);
         K[i][j] = m;
         K[j][i] = m;
       }
     const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
     const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
     df r[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-    if (A.have_src) {
+    if (SRC) {
       df fe[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) fe[i] = df_from_double(__ldg(A.f + tn[i]));
@@ -459,7 +462,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
 #pragma unroll
       for (int i = 0; i < 4; ++i) r[i] = df_add(q1, df_mul(q2, fe[i]));
     }
-    if (A.t) {
+    if (TF) {
       df te[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) te[i] = df_from_double(__ldg(A.t + tn[i]));
@@ -1095,7 +1098,21 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     D.m1 = df_host(h.M[0][1]);
     D.have_mass = p->have_mass;
     D.have_src = p->have_source;
-    k_asm_p1_diffusion_df<<<grid_for(m->E, eb, esm), eb, 0, s>>>(D);
+    const unsigned g = grid_for(m->E, eb, esm);
+    const int key = (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
+    switch (key) {
+#define FL_DF_CASE(K, M, S, T, AN) \
+  case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, 0, s>>>(D); break;
+      FL_DF_CASE(0, false, false, false, false) FL_DF_CASE(1, false, false, false, true)
+      FL_DF_CASE(2, false, false, true, false) FL_DF_CASE(3, false, false, true, true)
+      FL_DF_CASE(4, false, true, false, false) FL_DF_CASE(5, false, true, false, true)
+      FL_DF_CASE(6, false, true, true, false) FL_DF_CASE(7, false, true, true, true)
+      FL_DF_CASE(8, true, false, false, false) FL_DF_CASE(9, true, false, false, true)
+      FL_DF_CASE(10, true, false, true, false) FL_DF_CASE(11, true, false, true, true)
+      FL_DF_CASE(12, true, true, false, false) FL_DF_CASE(13, true, true, false, true)
+      FL_DF_CASE(14, true, true, true, false) FL_DF_CASE(15, true, true, true, true)
+#undef FL_DF_CASE
+    }
   } else if (closed) {
     k_asm_p1_diffusion<<<grid_for(m->E, eb, esm), eb, 0, s>>>(A);
   } else if (loc == 4) {
