@@ -386,10 +386,19 @@ struct DfArgs {
 
 // Specialised on the term set (consistent mass, source, old field t,
 // diagonal kappa) so that each instance carries only its own work.
+// The records of a warp's 32 consecutive elements are one contiguous 6 kB
+// chunk: each thread stages its 12 float4 in shared memory and the warp
+// writes the chunk with coalesced 16-byte stores (blockDim/32 x 6 kB of
+// dynamic shared memory).
 template <bool MASS, bool SRC, bool TF, bool ANISO>
 __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   note_launch();
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
+  extern __shared__ float4 stage_all[];
+  const int lane = threadIdx.x & 31;
+  float4* stage = stage_all + (threadIdx.x >> 5) * 384;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
+    const int e = base + lane;
+    if (e < A.E) {
     const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
     const int vi[4] = {v.x, v.y, v.z, v.w};
     double x[4][3];
@@ -474,13 +483,23 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
       }
     }
     // row-slice records: element e, local row i -> {K_i0, K_i1, K_i2, K_i3, r_i, 0}
-    float4* rec = reinterpret_cast<float4*>(A.em) + (uint32_t)e * 12u;
+    float4* rec = stage + lane * 12;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       rec[3 * i + 0] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
       rec[3 * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, K[i][3].hi, K[i][3].lo);
       rec[3 * i + 2] = make_float4(r[i].hi, r[i].lo, 0.0f, 0.0f);
     }
+    }
+    __syncwarp();
+    float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * 12u;
+    const int nvalid = min(32, A.E - base) * 12;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const int idx = k * 32 + lane;
+      if (idx < nvalid) out[idx] = stage[idx];
+    }
+    __syncwarp();
   }
 }
 
@@ -1099,10 +1118,11 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     D.have_mass = p->have_mass;
     D.have_src = p->have_source;
     const unsigned g = grid_for(m->E, eb, esm);
+    const size_t smem = (size_t)(eb / 32) * 384 * sizeof(float4);  // 6 kB per warp
     const int key = (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
     switch (key) {
 #define FL_DF_CASE(K, M, S, T, AN) \
-  case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, 0, s>>>(D); break;
+  case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, smem, s>>>(D); break;
       FL_DF_CASE(0, false, false, false, false) FL_DF_CASE(1, false, false, false, true)
       FL_DF_CASE(2, false, false, true, false) FL_DF_CASE(3, false, false, true, true)
       FL_DF_CASE(4, false, true, false, false) FL_DF_CASE(5, false, true, false, true)
