@@ -428,6 +428,126 @@ def bench_p2(args, dev, stream, n=64):
     }
 
 
+def bench_projection(args, dev, stream, m, X, n):
+    """P1-P1 pressure projection on the mesh of the headline workload: the
+    divergence matrix C^T, the second-order pattern, C M_l^-1 C^T, the KMK
+    stabilisation, the projection rhs, CG + Jacobi on CMC + KMK to 1e-10 and
+    the velocity correction; kernel times by CUDA events on the stream, and
+    the oracle's serial restatement timed on a 32^3 sample."""
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+    from fluidity_gb300 import meshgen as M
+    from fluidity_gb300 import projection as PR
+
+    E, N, nnz = m.E, m.N, m.nnz
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    so = PR.get_csr_sparsity_secondorder(m)
+    torch.cuda.synchronize()
+    so_setup = time.perf_counter() - t0
+    nnz2 = so.nnz
+    ct = torch.empty((3, nnz), dtype=torch.float64, device=dev)
+    outs = {k: torch.empty(N, dtype=torch.float64, device=dev) for k in ("ct_rhs", "dml", "gml")}
+    cmc = torch.empty(nnz2, dtype=torch.float64, device=dev)
+    kmk = torch.empty(nnz2, dtype=torch.float64, device=dev)
+    kt = torch.empty(nnz, dtype=torch.float64, device=dev)
+    bn = M.boundary_nodes(X)
+
+    def div():
+        PR.assemble_divergence_matrix_cg(m, ct=ct, ct_rhs=outs["ct_rhs"], div_mass_lumped=outs["dml"],
+                                         grad_mass_lumped=outs["gml"], stream=stream)
+
+    div()
+    inv = PR.inverse_lumped_mass(outs["gml"], bn)
+    pml = outs["dml"]
+
+    def prod():
+        PR.assemble_masslumped_cmc(so, ct, inv, ct, out=cmc, stream=stream)
+
+    def kmkf():
+        PR.assemble_kmk_matrix(m, so, pml, theta_pg=1.0, kmk=kmk, kt=kt, stream=stream)
+
+    reps = max(3, min(10, args.steps))
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    div_ms, prod_ms, kmk_ms = timed(div), timed(prod), timed(kmkf)
+    peak, _ = measured_peak_hbm()
+    div_bytes = 16 * E + 24 * N + 4 * (N + 1) + 4 * nnz + 24 * nnz + 16 * N
+    prod_bytes = 12 * nnz2 + 4 * (N + 1) + 24 * nnz + 8 * nnz + 4 * (N + 1) + 24 * N
+    # the projection: rhs = -C u*, CG on CMC + KMK (one reference node), correction
+    bubble = 64.0 * np.prod(X * (1.0 - X), axis=1)
+    u = torch.from_numpy(M.advdif_velocity(X) * bubble[:, None]).to(dev).contiguous()
+    prod()
+    kmkf()
+    PR.add_kmk_matrix(so, cmc, kmk, stream=stream)
+    rhs = PR.assemble_masslumped_poisson_rhs(m, ct, None, None, None, u, dt=1.0, theta_pg=1.0, stream=stream)
+    ina = torch.zeros(N, dtype=torch.uint8, device=dev)
+    ina[N // 2] = 1
+    rhs[N // 2] = 0.0
+    dp = torch.zeros(N, dtype=torch.float64, device=dev)
+    opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rep = ft.petsc_solve(so, dp, cmc, rhs, opts, inactive=ina, stream=stream)
+    PR.correct_masslumped_velocity(m, ct, inv, dp, u, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    solve_ms = e0.elapsed_time(e1)
+    it_bytes = cg_iteration_bytes(N, nnz2)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        nd32, X32 = M.cube_mesh(32)
+        f32, c32, _ = O.make_sparsity(nd32)
+        t0 = time.perf_counter()
+        ct32, _, _, gml32 = O.assemble_divergence_p1(nd32, X32, f32, c32)
+        t_div = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        sf, sc = O.sparsity_secondorder(f32, c32)
+        t_so = time.perf_counter() - t0
+        w32 = np.repeat((1.0 / gml32)[:, None], 3, axis=1)
+        t0 = time.perf_counter()
+        O.mult_div_vector_div_T(f32, c32, ct32, w32, ct32, sf, sc)
+        t_prod = time.perf_counter() - t0
+        cpu = {"kind": "port", "cores": 1, "sample": "32^3 six-tet cube (196,608 elements), serial oracle",
+               "divergence_melem_per_s": nd32.shape[0] / t_div / 1e6, "secondorder_pattern_s": t_so,
+               "cmc_product_mentries_per_s": len(sc) / t_prod / 1e6}
+    so.close()
+    return {
+        "workload": f"P1-P1 pressure projection, {n}^3 six-tet cube",
+        "elements": E, "nodes": N, "nnz_first_order": nnz, "nnz_second_order": nnz2,
+        "secondorder_pattern_setup_s": so_setup,
+        "divergence": {"ms": div_ms, "melem_per_s": E / (div_ms * 1e-3) / 1e6,
+                       "roofline": {"bound": "hbm", "achieved": div_bytes / (div_ms * 1e-3) / 1e9,
+                                    "peak": peak, "unit": "GB/s",
+                                    "frac": div_bytes / (div_ms * 1e-3) / 1e9 / peak,
+                                    "algorithmic_bytes": div_bytes}},
+        "cmc_product": {"ms": prod_ms, "mentries_per_s": nnz2 / (prod_ms * 1e-3) / 1e6,
+                        "roofline": {"bound": "hbm", "achieved": prod_bytes / (prod_ms * 1e-3) / 1e9,
+                                     "peak": peak, "unit": "GB/s",
+                                     "frac": prod_bytes / (prod_ms * 1e-3) / 1e9 / peak,
+                                     "algorithmic_bytes": prod_bytes}},
+        "kmk_ms": kmk_ms,
+        "projection_solve": {"ms": solve_ms, "iterations": rep["iterations"], "reason": rep["reason_name"],
+                             "true_rel_residual": rep["true_rel_residual"],
+                             "cg_iteration_gbs": it_bytes * rep["iterations"] / (solve_ms * 1e-3) / 1e9},
+        "cpu_baseline": cpu,
+    }
+
+
 def bench_advdif_steps(args, dev, stream, n=16, nsteps=10):
     """The CPU-runnable workload: 10 advection-diffusion steps (theta 0.5,
     dt 0.01, GMRES(30) + Jacobi to 1e-10) on the 16^3 mesh, through
@@ -730,6 +850,7 @@ def run_ours(args, rank, ws, dist):
         solve = out
 
     p2 = None if args.no_p2 else bench_p2(args, dev, stream)
+    projection = None if args.no_projection else bench_projection(args, dev, stream, m, X, args.n)
     steps16 = bench_advdif_steps(args, dev, stream)
     batch = None
     if not args.no_batch:
@@ -783,6 +904,7 @@ def run_ours(args, rank, ws, dist):
         "clocks": clk.summary(),
         "solve": solve,
         "p2": p2,
+        "projection": projection,
         "advdif_16_ten_steps": steps16,
         "batch": batch,
         "learned": learned,
@@ -802,6 +924,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-p2", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-projection", action="store_true")
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--learned-sizes", default="64,128",
                     help="mesh sides of the learned-warm-start sequences")

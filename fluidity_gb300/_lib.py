@@ -63,6 +63,14 @@ class SolverOpts(C.Structure):
     ]
 
 
+class DivergenceParams(C.Structure):
+    _fields_ = [
+        ("integrate_by_parts", C.c_int32), ("nfaces", C.c_int32), ("index_base", C.c_int32),
+        ("pad", C.c_int32), ("faces", C.c_void_p), ("face_ele", C.c_void_p), ("bc_type", C.c_void_p),
+        ("bc_val", C.c_void_p),
+    ]
+
+
 class SolveReport(C.Structure):
     _fields_ = [
         ("iterations", C.c_int32), ("reason", C.c_int32), ("final_rnorm", C.c_double),
@@ -85,6 +93,9 @@ EXPORTS = [
     "fl_gnn_get_weights", "fl_gnn_predict", "fl_gnn_gradients", "fl_gnn_train_step",
     "fl_gnn_set_loss", "fl_gpu_pattern_register",
     "fl_amg_create", "fl_amg_solve", "fl_amg_levels", "fl_amg_destroy", "fl_amg_set_norm", "fl_amg_set_precision",
+    "fl_gpu_secondorder_register", "fl_dev_assemble_divergence_cg", "fl_dev_lumped_mass",
+    "fl_dev_mult_div_vector_div_T", "fl_dev_mult_div_invscalar_div_T", "fl_dev_assemble_kmk",
+    "fl_dev_masslumped_poisson_rhs", "fl_dev_correct_masslumped_velocity", "fl_dev_csr_addto",
 ]
 
 _P = C.c_void_p
@@ -143,6 +154,15 @@ _SIGNATURES = {
     "fl_gnn_predict": (C.c_int, [_P, _P, _P, _P, _P, _P]),
     "fl_gnn_gradients": (C.c_int, [_P, _P, _P, _P, _P, _P, _I32, _P, C.POINTER(C.c_float), _P]),
     "fl_gnn_train_step": (C.c_int, [_P, _P, _P, _P, _P, _P, _I32, C.c_float, _P, _P]),
+    "fl_gpu_secondorder_register": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "fl_dev_assemble_divergence_cg": (C.c_int, [_P, C.POINTER(DivergenceParams), _P, _P, _P, _P, _P]),
+    "fl_dev_lumped_mass": (C.c_int, [_P, _P, _P]),
+    "fl_dev_mult_div_vector_div_T": (C.c_int, [_P, _I32, _P, _P, _P, _P, _P]),
+    "fl_dev_mult_div_invscalar_div_T": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+    "fl_dev_assemble_kmk": (C.c_int, [_P, _P, _D, _P, _P, _P, _P]),
+    "fl_dev_masslumped_poisson_rhs": (C.c_int, [_P, _P, _P, _P, _P, _P, _D, _D, _P, _P]),
+    "fl_dev_correct_masslumped_velocity": (C.c_int, [_P, _P, _P, _P, _P, _P]),
+    "fl_dev_csr_addto": (C.c_int, [_P, _P, _P, _D, _P]),
 }
 assert sorted(_SIGNATURES) == sorted(EXPORTS)
 

@@ -17,7 +17,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfluidity_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"]
-SOURCES = ["fl_mesh.cu", "fl_assemble.cu", "fl_krylov.cu", "fl_batch.cu", "fl_gnn.cu", "fl_amg.cu"]
+SOURCES = ["fl_mesh.cu", "fl_assemble.cu", "fl_krylov.cu", "fl_batch.cu", "fl_gnn.cu", "fl_amg.cu",
+           "fl_projection.cu"]
 
 
 def _nvcc() -> str:

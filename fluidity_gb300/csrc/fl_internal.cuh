@@ -146,6 +146,9 @@ int dirichlet_launch(struct ::fl_mesh_t* m, int32_t nb, const int32_t* nodes, in
                      const double* t, double dt, double* rhs, uint8_t* inactive, cudaStream_t s);
 int autotune_assembly(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val,
                       double* rhs, cudaStream_t s);
+// Row pass of P1 FP64 element values in the symmetric coefficient-major layout
+// em[k*E + e] (ten matrix entries, then four rhs entries per element).
+int rows_p1_closed(struct ::fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s);
 
 // Per-translation-unit launch counters and workspace release hooks.
 unsigned long long launches_mesh();
@@ -153,6 +156,7 @@ unsigned long long launches_assemble();
 unsigned long long launches_krylov();
 unsigned long long launches_gnn();
 unsigned long long launches_amg();
+unsigned long long launches_projection();
 void release_krylov_work(struct ::fl_mesh_t* m);
 
 }  // namespace fl
@@ -189,6 +193,9 @@ struct fl_mesh_t {
   fl::DevBuf<int32_t> colour_elems;  // E, sorted by (colour, element)
   std::vector<int32_t> colour_ptr;   // ncolours+1 (host)
   fl::DevBuf<fl::ErrWord> err;       // 1 word
+  fl::DevBuf<int32_t> tpos;          // per entry (k, j): position of (j, k) (built on first use)
+  struct fl_mesh_t* so_parent = nullptr;  // second-order pattern handles: the mesh they square
+  fl::DevBuf<int32_t> face_cnt, face_ptr, face_list;  // node -> surface faces (divergence surface terms)
   fl::DevBuf<double> em;             // element matrices + rhs (coefficient-major scratch)
   // staging buffers of the host-pointer entry points (grow-only)
   fl::DevBuf<double> st_val, st_rhs, st_t, st_u, st_src, st_abs, st_x, st_g;

@@ -756,7 +756,7 @@ extern "C" int fl_gpu_mesh_destroy(fl_mesh m) {
 
 extern "C" int64_t fl_kernel_launch_count(void) {
   return (int64_t)(launches_mesh() + launches_assemble() + launches_krylov() + launches_gnn() +
-                   launches_amg());
+                   launches_amg() + launches_projection());
 }
 
 extern "C" int fl_gpu_mesh_info(fl_mesh m, int64_t* nnz, int32_t* ncolours) {

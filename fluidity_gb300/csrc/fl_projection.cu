@@ -1,0 +1,978 @@
+// fl_projection.cu -- the pressure-projection matrices of a P1 velocity /
+// P1 pressure discretisation on one mesh:
+//   * the divergence matrix C^T and the lumped masses of
+//     assemble_divergence_matrix_cg (assemble/Divergence_Matrix_CG.F90:67-375),
+//     including the surface terms of the integrated-by-parts form;
+//   * the lumped mass of compute_lumped_mass (femtools/FEFields.F90:161-214);
+//   * the second-order sparsity of get_csr_sparsity_secondorder
+//     (femtools/Sparsity_Patterns_Meshes.F90:122-148 -> make_sparsity_transpose,
+//     femtools/Sparsity_Patterns.F90:87-148), bit-exact;
+//   * the weighted row products mult_div_vector_div_T and
+//     mult_div_invscalar_div_T (femtools/Sparse_Matrices_Fields.F90:590-748)
+//     that form C M_l^-1 C^T (assemble_masslumped_cmc,
+//     assemble/Assemble_CMC.F90:119-135) and the P1-P1 stabilisation
+//     K M^-1 K (assemble_kmk_matrix, assemble/Momentum_CG.F90:2707-2766);
+//   * the mass-lumped projection right-hand side and velocity correction
+//     (assemble_masslumped_poisson_rhs, correct_masslumped_velocity,
+//     assemble/Momentum_CG.F90:2544-2575,2670-2705).
+//
+// Layout.  C^T is the reference's block_csr_matrix with blocks (1, dim): three
+// FP64 value arrays over the mesh's first-order pattern.  Vector fields are
+// vector_field%val(3, N): x, y, z of a node adjacent.  The second-order
+// pattern is a pattern-only handle whose parent is the mesh; the products
+// read the parent's pattern and its transpose map tpos (tpos[p] = position of
+// (colm[p], row) for the entry p of a row: the pattern is structurally
+// symmetric).
+//
+// Kernels.
+//   k_div_elem   element pass: per element the nine signed cofactors / 24 and
+//                |det| / 24 (the whole P1 element matrix: row a of
+//                shape_dshape is sign(det) cof(:, b) / 24 for every b), as
+//                double-float pairs, 80 B, written through shared memory
+//                with coalesced stores.
+//   k_div_rows   row pass: one thread per row sums its incidences in colour
+//                order (deterministic) into double-float shared accumulators.
+//   k_div_faces  surface terms, one thread per boundary node, faces in
+//                ascending order after the element terms.
+//   k_so_rows    second-order pattern: one warp per row gathers the rows of
+//                its neighbours, sorts them bitonically in shared memory and
+//                keeps the distinct columns.
+//   k_rowprod    out(i,j) = sum_k sum_d a_d(i,k) w_d(k) b_d(j,k): one warp per
+//                output row, the row's columns and FP64 accumulators in shared
+//                memory; the two half-warps take two k at a time and add in
+//                a fixed order, so every sum is deterministic.
+//   k_kmk_elem   FP64 P1 pressure-diffusion element matrix
+//                0.5 V grad N^T h_bar grad N with h_bar the element's edge-
+//                length tensor (closed form below); summed by the assembly's
+//                FP64 row pass.
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <vector>
+
+#include "fl_internal.cuh"
+#include "fl_device.cuh"
+#include "fl_df64.cuh"
+
+namespace fl {
+
+unsigned long long launches_projection() { return unit_launches(); }
+
+namespace {
+
+constexpr int kT = 256;
+
+cudaStream_t pick(fl_mesh_t* m, void* stream) { return stream ? (cudaStream_t)stream : m->stream; }
+
+// ------------------------------------------------------------- divergence --
+struct DivElemArgs {
+  int32_t E;
+  const int32_t* xnd;
+  const double* X;
+  float4* rec;  // 5 float4 per element
+  df k24;       // 1/24
+};
+
+__global__ void __launch_bounds__(256) k_div_elem(DivElemArgs A) {
+  note_launch();
+  extern __shared__ float4 stage_all[];
+  const int lane = threadIdx.x & 31;
+  float4* stage = stage_all + (threadIdx.x >> 5) * 160;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
+    const int e = base + lane;
+    if (e < A.E) {
+      const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+      const int vi[4] = {v.x, v.y, v.z, v.w};
+      double x[4][3];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+      df J[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
+      df c[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+          c[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
+        }
+      const df det = df_dot3(J[0][0], c[0][0], J[1][0], c[1][0], J[2][0], c[2][0]);
+      const df s = det.hi < 0.0f ? df_neg(A.k24) : A.k24;
+      df r[10];
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) r[3 * d + b] = df_mul(c[d][b], s);
+      r[9] = df_mul(df_abs(det), A.k24);
+      float4* o = stage + lane * 5;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) o[k] = make_float4(r[2 * k].hi, r[2 * k].lo, r[2 * k + 1].hi, r[2 * k + 1].lo);
+    }
+    __syncwarp();
+    float4* out = A.rec + (uint32_t)base * 5u;
+    const int nvalid = min(32, A.E - base) * 5;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const int idx = k * 32 + lane;
+      if (idx < nvalid) out[idx] = stage[idx];
+    }
+    __syncwarp();
+  }
+}
+
+struct DivRowArgs {
+  int32_t N;
+  const int32_t* ne_ptr;
+  const int32_t* ne_col;
+  const uint32_t* ne_pos;
+  const int32_t* findrm;
+  const float4* rec;
+  double* ct0;
+  double* ct1;
+  double* ct2;
+  double* ct_rhs;  // zeroed when given
+  double* dml;
+  double* gml;
+};
+
+__device__ __forceinline__ df f2(float x, float y) { return {x, y}; }
+
+// CT: assemble the three blocks; BYPARTS: -dshape_shape instead of shape_dshape.
+template <int THREADS, int RMAX, bool CT, bool BYPARTS>
+__global__ void __launch_bounds__(THREADS) k_div_rows(DivRowArgs P) {
+  note_launch();
+  extern __shared__ unsigned char smem_raw[];
+  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [3][RMAX][THREADS]
+  const int t = threadIdx.x;
+  double* ct[3] = {P.ct0, P.ct1, P.ct2};
+  for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
+    const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
+    const bool in_smem = L <= RMAX;
+    if (CT) {
+      if (in_smem) {
+        for (int d = 0; d < 3; ++d)
+          for (int k = 0; k < L; ++k) acc[(d * RMAX + k) * THREADS + t] = make_float2(0.0f, 0.0f);
+      } else {
+        for (int d = 0; d < 3; ++d)
+          for (int k = 0; k < L; ++k) ct[d][base + k] = 0.0;
+      }
+    }
+    df mass = {0.0f, 0.0f};
+    const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
+    for (int q = ib; q < ie; ++q) {
+      const int inc = __ldg(P.ne_col + q);
+      const int e = inc >> 4, a = inc & 15;
+      const float4* r = P.rec + (uint32_t)e * 5u;
+      const float4 r4 = __ldg(r + 4);
+      mass = df_add(mass, f2(r4.z, r4.w));
+      if (!CT) continue;
+      const uint32_t pw = __ldg(P.ne_pos + q);
+      const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+      df c[3][4];
+      c[0][0] = f2(r0.x, r0.y); c[0][1] = f2(r0.z, r0.w); c[0][2] = f2(r1.x, r1.y);
+      c[1][0] = f2(r1.z, r1.w); c[1][1] = f2(r2.x, r2.y); c[1][2] = f2(r2.z, r2.w);
+      c[2][0] = f2(r3.x, r3.y); c[2][1] = f2(r3.z, r3.w); c[2][2] = f2(r4.x, r4.y);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) c[d][3] = df_neg(df_add(df_add(c[d][0], c[d][1]), c[d][2]));
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        df own = c[d][0];
+        if (BYPARTS) {
+          own = a == 1 ? c[d][1] : own;
+          own = a == 2 ? c[d][2] : own;
+          own = a == 3 ? c[d][3] : own;
+          own = df_neg(own);
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const df v = BYPARTS ? own : c[d][b];
+          const int pos = (pw >> (8 * b)) & 0xffu;
+          if (in_smem) {
+            float2* p = &acc[(d * RMAX + pos) * THREADS + t];
+            const df sum = df_add(f2(p->x, p->y), v);
+            *p = make_float2(sum.hi, sum.lo);
+          } else {
+            ct[d][base + pos] += df_to_double(v);
+          }
+        }
+      }
+    }
+    if (CT && in_smem)
+      for (int d = 0; d < 3; ++d)
+        for (int k = 0; k < L; ++k) {
+          const float2 v = acc[(d * RMAX + k) * THREADS + t];
+          ct[d][base + k] = df_to_double(f2(v.x, v.y));
+        }
+    const double ms = df_to_double(mass);
+    if (P.dml) P.dml[row] = ms;
+    if (P.gml) P.gml[row] = ms;
+    if (P.ct_rhs) P.ct_rhs[row] = 0.0;
+  }
+}
+
+// node -> surface faces incidence (counting sort, lists sorted ascending)
+__global__ void k_face_count(int32_t nf, const int32_t* __restrict__ faces, int32_t base, int32_t N,
+                             int32_t* __restrict__ cnt, ErrWord* err) {
+  note_launch();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * nf; k += gridDim.x * blockDim.x) {
+    const int v = faces[k] - base;
+    if (v < 0 || v >= N) {
+      set_err(err, FL_ERR_ARG, k / 3);
+      continue;
+    }
+    atomicAdd(cnt + v, 1);
+  }
+}
+
+__global__ void k_face_fill(int32_t nf, const int32_t* __restrict__ faces, int32_t base, int32_t N,
+                            const int32_t* __restrict__ fptr, int32_t* __restrict__ fill,
+                            int32_t* __restrict__ flist) {
+  note_launch();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * nf; k += gridDim.x * blockDim.x) {
+    const int v = faces[k] - base;
+    if (v < 0 || v >= N) continue;
+    const int slot = atomicAdd(fill + v, 1);
+    flist[fptr[v] + slot] = k / 3;
+  }
+}
+
+__global__ void k_face_sort(int32_t N, const int32_t* __restrict__ fptr, int32_t* __restrict__ flist) {
+  note_launch();
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x) {
+    const int b = fptr[v], e = fptr[v + 1];
+    for (int i = b + 1; i < e; ++i) {
+      const int x = flist[i];
+      int j = i - 1;
+      while (j >= b && flist[j] > x) {
+        flist[j + 1] = flist[j];
+        --j;
+      }
+      flist[j + 1] = x;
+    }
+  }
+}
+
+struct FaceArgs {
+  int32_t N;
+  int32_t base;
+  const int32_t* fptr;
+  const int32_t* flist;
+  const int32_t* faces;
+  const int32_t* face_ele;
+  const int32_t* bc_type;
+  const double* bc_val;
+  const int32_t* xnd;
+  const double* X;
+  const int32_t* findrm;
+  const int32_t* colm;
+  double* ct0;
+  double* ct1;
+  double* ct2;
+  double* ct_rhs;
+  int32_t E;
+  ErrWord* err;
+};
+
+// Surface terms of the integrated-by-parts divergence (Divergence_Matrix_CG.F90
+// :312-366).  Face mass of a P1 triangle: detJ/12 on the diagonal and detJ/24
+// off it (the three-point rule is exact for it); normal = facet_normal
+// (Transform_elements.F90:1527-1553).
+__global__ void k_div_faces(FaceArgs F) {
+  note_launch();
+  double* ct[3] = {F.ct0, F.ct1, F.ct2};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F.N; i += gridDim.x * blockDim.x) {
+    const int qb = F.fptr[i], qe = F.fptr[i + 1];
+    for (int q = qb; q < qe; ++q) {
+      const int f = F.flist[q];
+      int ty[3];
+      bool skip = false;
+      for (int d = 0; d < 3; ++d) {
+        ty[d] = F.bc_type ? F.bc_type[3 * f + d] : 0;
+        skip = skip || ty[d] == 2 || ty[d] == 3 || ty[d] == 4;
+      }
+      if (skip) continue;
+      int fn[3], li = -1;
+      for (int j = 0; j < 3; ++j) {
+        fn[j] = F.faces[3 * f + j] - F.base;
+        if (fn[j] == i) li = j;
+      }
+      const int el = F.face_ele[f] - F.base;
+      if (li < 0 || el < 0 || el >= F.E) {
+        set_err(F.err, FL_ERR_ARG, f);
+        continue;
+      }
+      double Xf[3][3], cf[3] = {0.0, 0.0, 0.0}, ce[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < 3; ++j)
+        for (int a = 0; a < 3; ++a) {
+          Xf[j][a] = F.X[3 * fn[j] + a];
+          cf[a] += Xf[j][a];
+        }
+      for (int j = 0; j < 4; ++j) {
+        const int v = F.xnd[4 * el + j];
+        for (int a = 0; a < 3; ++a) ce[a] += F.X[3 * v + a];
+      }
+      double J0[3], J1[3], ow[3];
+      for (int a = 0; a < 3; ++a) {
+        J0[a] = Xf[0][a] - Xf[2][a];
+        J1[a] = Xf[1][a] - Xf[2][a];
+        ow[a] = cf[a] / 3.0 - ce[a] / 4.0;
+      }
+      double n[3] = {J0[1] * J1[2] - J0[2] * J1[1], J0[2] * J1[0] - J0[0] * J1[2], J0[0] * J1[1] - J0[1] * J1[0]};
+      const double detJ = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      const double o = n[0] * ow[0] + n[1] * ow[1] + n[2] * ow[2];
+      for (int a = 0; a < 3; ++a) n[a] *= o;
+      const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      for (int a = 0; a < 3; ++a) n[a] /= len;
+      double mrow[3];
+      for (int j = 0; j < 3; ++j) mrow[j] = detJ * (j == li ? 1.0 / 12.0 : 1.0 / 24.0);
+      const double* bv = F.bc_val ? F.bc_val + 9 * f : nullptr;
+      if (ty[0] == 5 && F.ct_rhs) {
+        if (!bv) {
+          set_err(F.err, FL_ERR_ARG, f);
+          continue;
+        }
+        double r = 0.0;
+        for (int j = 0; j < 3; ++j) r += mrow[j] * bv[3 * j];
+        F.ct_rhs[i] -= r;
+        continue;
+      }
+      const int rb = F.findrm[i], re = F.findrm[i + 1];
+      for (int d = 0; d < 3; ++d) {
+        if (ty[d] == 1 && F.ct_rhs) {
+          if (!bv) {
+            set_err(F.err, FL_ERR_ARG, f);
+            continue;
+          }
+          double r = 0.0;
+          for (int j = 0; j < 3; ++j) r += n[d] * mrow[j] * bv[3 * j + d];
+          F.ct_rhs[i] -= r;
+        } else {
+          for (int j = 0; j < 3; ++j) {
+            const int p = csr_find(F.colm, rb, re, fn[j]);
+            if (p < 0) {
+              set_err(F.err, FL_ERR_OUTSIDE_PATTERN, i);
+              continue;
+            }
+            ct[d][p] += n[d] * mrow[j];
+          }
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- pattern products --
+// tpos[p] for the entry p = (k, j) of row k: the position of (j, k) in row j.
+__global__ void k_tpos(int32_t N, const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
+                       int32_t* __restrict__ tpos, ErrWord* err) {
+  note_launch();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x)
+    for (int p = findrm[k]; p < findrm[k + 1]; ++p) {
+      const int j = colm[p];
+      const int t = csr_find(colm, findrm[j], findrm[j + 1], k);
+      if (t < 0) set_err(err, FL_ERR_ARG, k);
+      tpos[p] = t < 0 ? p : t;
+    }
+}
+
+constexpr int kSoWarps = 4;
+constexpr int kSoCap = 1024;  // gathered candidates of one row
+
+// pass 0: distinct-column count of every row (and the longest row);
+// pass 1: the columns, ascending, and the diagonal position.
+__global__ void __launch_bounds__(kSoWarps * 32) k_so_rows(int32_t N, const int32_t* __restrict__ fr,
+                                                          const int32_t* __restrict__ cm,
+                                                          const int32_t* __restrict__ optr,
+                                                          int32_t* __restrict__ cnt, int32_t* __restrict__ ocol,
+                                                          int32_t* __restrict__ ocentre, int32_t* maxrow,
+                                                          ErrWord* err, int pass) {
+  note_launch();
+  __shared__ int32_t keys_all[kSoWarps][kSoCap];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t* keys = keys_all[w];
+  for (int row = blockIdx.x * kSoWarps + w; row < N; row += gridDim.x * kSoWarps) {
+    int nc = 0;
+    const int qb = fr[row], qe = fr[row + 1];
+    for (int q = qb; q < qe; ++q) {
+      const int k = cm[q];
+      const int kb = fr[k], len = fr[k + 1] - kb;
+      for (int t = lane; t < len; t += 32)
+        if (nc + t < kSoCap) keys[nc + t] = cm[kb + t];
+      nc += len;
+    }
+    if (nc > kSoCap) {
+      if (lane == 0) set_err(err, FL_ERR_UNSUPPORTED, row);
+      __syncwarp();
+      continue;
+    }
+    int pw = 1;
+    while (pw < nc) pw <<= 1;
+    for (int t = nc + lane; t < pw; t += 32) keys[t] = INT_MAX;
+    __syncwarp();
+    for (int size = 2; size <= pw; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int t = lane; t < pw; t += 32) {
+          const int l = t ^ stride;
+          if (l > t) {
+            const int a = keys[t], b = keys[l];
+            const bool up = (t & size) == 0;
+            if ((a > b) == up) {
+              keys[t] = b;
+              keys[l] = a;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    int total = 0;
+    const int o0 = pass ? optr[row] : 0;
+    for (int t0 = 0; t0 < nc; t0 += 32) {
+      const int t = t0 + lane;
+      const bool head = t < nc && (t == 0 || keys[t] != keys[t - 1]);
+      const unsigned hm = __ballot_sync(0xffffffffu, head);
+      if (pass && head) {
+        const int slot = total + __popc(hm & ((1u << lane) - 1u));
+        ocol[o0 + slot] = keys[t];
+        if (keys[t] == row) ocentre[row] = o0 + slot;
+      }
+      total += __popc(hm);
+    }
+    if (pass == 0 && lane == 0) {
+      cnt[row] = total;
+      atomicMax(maxrow, total);
+    }
+    __syncwarp();
+  }
+}
+
+constexpr int kPW = 8;      // warps per block of the product kernel
+constexpr int kPCap = 256;  // longest output row held in shared memory
+
+struct RowProdArgs {
+  int32_t n;
+  const int32_t* aptr;
+  const int32_t* acol;
+  const int32_t* tpos;
+  const int32_t* optr;
+  const int32_t* ocol;
+  const double* a[3];
+  const double* b[3];
+  const double* w;  // NDIM values per node; the divisor s when DIV
+  double theta;     // DIV: the divisor is theta * s unless scale == 0
+  int scale;
+  double* out;
+  ErrWord* err;
+};
+
+template <int NDIM, bool DIV>
+__global__ void __launch_bounds__(kPW * 32) k_rowprod(RowProdArgs P) {
+  note_launch();
+  __shared__ int32_t s_col_all[kPW][kPCap];
+  __shared__ double s_acc_all[kPW][kPCap];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+  int32_t* s_col = s_col_all[w];
+  double* s_acc = s_acc_all[w];
+  for (int row = blockIdx.x * kPW + w; row < P.n; row += gridDim.x * kPW) {
+    const int ob = __ldg(P.optr + row), L = __ldg(P.optr + row + 1) - ob;
+    if (L > kPCap) {
+      if (lane == 0) set_err(P.err, FL_ERR_UNSUPPORTED, row);
+      __syncwarp();
+      continue;
+    }
+    for (int t = lane; t < L; t += 32) {
+      s_col[t] = __ldg(P.ocol + ob + t);
+      s_acc[t] = 0.0;
+    }
+    __syncwarp();
+    const int qb = __ldg(P.aptr + row), qe = __ldg(P.aptr + row + 1);
+    for (int q0 = qb; q0 < qe; q0 += 2) {
+      const int q = q0 + half;
+      const bool act = q < qe;
+      int kb = 0, ke = 0;
+      double c[NDIM];
+#pragma unroll
+      for (int d = 0; d < NDIM; ++d) c[d] = 0.0;
+      if (act) {
+        const int k = __ldg(P.acol + q);
+        kb = __ldg(P.aptr + k);
+        ke = __ldg(P.aptr + k + 1);
+        if (DIV) {
+          double sk = __ldg(P.w + k);
+          if (P.scale) sk = sk * P.theta;
+          c[0] = __ldg(P.a[0] + q) / sk;
+        } else {
+#pragma unroll
+          for (int d = 0; d < NDIM; ++d) c[d] = __ldg(P.a[d] + q) * __ldg(P.w + NDIM * k + d);
+        }
+      }
+      const int len = ke - kb;
+      const int mlen = max(len, __shfl_xor_sync(0xffffffffu, len, 16));
+      for (int c0 = 0; c0 < mlen; c0 += 16) {
+        const int r = kb + c0 + hl;
+        bool has = act && r < ke;
+        double v = 0.0;
+        int slot = 0;
+        if (has) {
+          const int j = __ldg(P.acol + r);
+          const int tp = __ldg(P.tpos + r);
+          v = c[0] * __ldg(P.b[0] + tp);
+#pragma unroll
+          for (int d = 1; d < NDIM; ++d) v = fma(c[d], __ldg(P.b[d] + tp), v);
+          int lo = 0, hi = L;
+          while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (s_col[mid] < j) lo = mid + 1;
+            else hi = mid;
+          }
+          slot = lo;
+          if (slot >= L || s_col[slot] != j) {
+            set_err(P.err, FL_ERR_OUTSIDE_PATTERN, row);
+            has = false;
+          }
+        }
+        if (half == 0 && has) s_acc[slot] += v;
+        __syncwarp();
+        if (half == 1 && has) s_acc[slot] += v;
+        __syncwarp();
+      }
+    }
+    for (int t = lane; t < L; t += 32) P.out[ob + t] = s_acc[t];
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------- KMK --
+// Largest eigenvalue of a symmetric 3x3 matrix (m00, m01, m02, m11, m12, m22)
+// by the trigonometric solution of its characteristic cubic.
+__device__ __forceinline__ double lmax_sym3(const double* m) {
+  const double q = (m[0] + m[3] + m[5]) / 3.0;
+  const double p1 = m[1] * m[1] + m[2] * m[2] + m[4] * m[4];
+  const double d0 = m[0] - q, d1 = m[3] - q, d2 = m[5] - q;
+  const double p2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1;
+  if (!(p2 > 0.0)) return q;
+  const double p = sqrt(p2 / 6.0);
+  const double ip = 1.0 / p;
+  const double b0 = d0 * ip, b1 = m[1] * ip, b2 = m[2] * ip, b3 = d1 * ip, b4 = m[4] * ip, b5 = d2 * ip;
+  double r = 0.5 * (b0 * (b3 * b5 - b4 * b4) - b1 * (b1 * b5 - b4 * b2) + b2 * (b1 * b4 - b3 * b2));
+  r = fmin(1.0, fmax(-1.0, r));
+  return q + 2.0 * p * cos(acos(r) / 3.0);
+}
+
+struct KmkArgs {
+  int32_t E;
+  const int32_t* xnd;
+  const double* X;
+  double* em;  // [10][E] symmetric element entries (row pass layout)
+};
+
+// h_bar = edge_length_from_eigenvalue_metric(simplex_tensor(ele)) is
+// m^(-1/2) for the element metric m.  Every edge e_ab satisfies
+// e_ab^T m e_ab = 1 for m = 1/2 sum_b g_b g_b^T (g_b the barycentric
+// gradients, sum g_b = 0, g_c . e_ab = delta_cb - delta_ca), the unique
+// solution of simplex_tensor's system, so W = m^-1 = 2 J J^T - 1/2 (J 1)(J 1)^T
+// (Sherman-Morrison on I + 1 1^T) with J the edge matrix, det W = 2 det(J)^2.
+// h_bar = W^(1/2) = (-W^2 + (i1^2 - i2) W + i1 i3 I) / (i1 i2 - i3) from the
+// invariants of the square roots of W's eigenvalues (Cayley-Hamilton); the
+// largest eigenvalue comes from W, the smallest as 1/lambda_max(m), the middle
+// one from det W, so none is a small difference of large ones.
+__global__ void __launch_bounds__(128) k_kmk_elem(KmkArgs A) {
+  note_launch();
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+    const int vi[4] = {v.x, v.y, v.z, v.w};
+    double x[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+    double J[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) J[a][b] = x[b][a] - x[3][a];
+    double c[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+        c[i][k] = J[i1][k1] * J[i2][k2] - J[i2][k1] * J[i1][k2];
+      }
+    const double det = J[0][0] * c[0][0] + J[1][0] * c[1][0] + J[2][0] * c[2][0];
+    // g_b * det = column b of c; the fourth is minus their sum
+    double g[4][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      g[0][a] = c[a][0];
+      g[1][a] = c[a][1];
+      g[2][a] = c[a][2];
+      g[3][a] = -(c[a][0] + c[a][1] + c[a][2]);
+    }
+    const int ix[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+    double W[6], M[6];
+    double j1[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) j1[a] = J[a][0] + J[a][1] + J[a][2];
+    const double im = 0.5 / (det * det);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const int r = ix[k][0], s = ix[k][1];
+      W[k] = 2.0 * (J[r][0] * J[s][0] + J[r][1] * J[s][1] + J[r][2] * J[s][2]) - 0.5 * j1[r] * j1[s];
+      M[k] = im * (g[0][r] * g[0][s] + g[1][r] * g[1][s] + g[2][r] * g[2][s] + g[3][r] * g[3][s]);
+    }
+    const double l1 = lmax_sym3(W), l3 = 1.0 / lmax_sym3(M);
+    const double l2 = 2.0 * det * det / (l1 * l3);
+    const double s1 = sqrt(l1), s2 = sqrt(l2), s3 = sqrt(l3);
+    const double i1 = s1 + s2 + s3, i2 = s1 * s2 + s2 * s3 + s1 * s3, i3 = s1 * s2 * s3;
+    const double cw = i1 * i1 - i2, ci = i1 * i3, den = 1.0 / (i1 * i2 - i3);
+    // W^2 (symmetric)
+    const double w00 = W[0], w01 = W[1], w02 = W[2], w11 = W[3], w12 = W[4], w22 = W[5];
+    double H[3][3];
+    H[0][0] = (-(w00 * w00 + w01 * w01 + w02 * w02) + cw * w00 + ci) * den;
+    H[0][1] = (-(w00 * w01 + w01 * w11 + w02 * w12) + cw * w01) * den;
+    H[0][2] = (-(w00 * w02 + w01 * w12 + w02 * w22) + cw * w02) * den;
+    H[1][1] = (-(w01 * w01 + w11 * w11 + w12 * w12) + cw * w11 + ci) * den;
+    H[1][2] = (-(w01 * w02 + w11 * w12 + w12 * w22) + cw * w12) * den;
+    H[2][2] = (-(w02 * w02 + w12 * w12 + w22 * w22) + cw * w22 + ci) * den;
+    H[1][0] = H[0][1];
+    H[2][0] = H[0][2];
+    H[2][1] = H[1][2];
+    // 0.5 * V * g_a^T H g_b with g = c / det, V = |det| / 6
+    const double ks = 1.0 / (12.0 * fabs(det));
+    double hg[4][3];
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) hg[b][r] = H[r][0] * g[b][0] + H[r][1] * g[b][1] + H[r][2] * g[b][2];
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = a; b < 4; ++b) {
+        A.em[(int64_t)k * A.E + e] = ks * (g[a][0] * hg[b][0] + g[a][1] * hg[b][1] + g[a][2] * hg[b][2]);
+        ++k;
+      }
+  }
+}
+
+// ------------------------------------------------------ projection vectors --
+__global__ void k_poisson_rhs(int32_t N, const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
+                              const double* __restrict__ c0, const double* __restrict__ c1,
+                              const double* __restrict__ c2, const double* __restrict__ mom,
+                              const double* __restrict__ ct_rhs, const double* __restrict__ iml,
+                              const double* __restrict__ u, double s, double* __restrict__ out) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double y = 0.0;
+    for (int p = findrm[i]; p < findrm[i + 1]; ++p) {
+      const int k = colm[p];
+      const double l0 = (mom ? mom[3 * k] * iml[3 * k] : 0.0) + u[3 * k] * s;
+      const double l1 = (mom ? mom[3 * k + 1] * iml[3 * k + 1] : 0.0) + u[3 * k + 1] * s;
+      const double l2 = (mom ? mom[3 * k + 2] * iml[3 * k + 2] : 0.0) + u[3 * k + 2] * s;
+      y += c0[p] * l0 + c1[p] * l1 + c2[p] * l2;
+    }
+    out[i] = -y + (ct_rhs ? ct_rhs[i] * s : 0.0);
+  }
+}
+
+__global__ void k_correct_velocity(int32_t N, const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
+                                   const int32_t* __restrict__ tpos, const double* __restrict__ c0,
+                                   const double* __restrict__ c1, const double* __restrict__ c2,
+                                   const double* __restrict__ iml, const double* __restrict__ dp,
+                                   double* __restrict__ u) {
+  note_launch();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < N; k += gridDim.x * blockDim.x) {
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0;
+    for (int r = findrm[k]; r < findrm[k + 1]; ++r) {
+      const int i = colm[r], t = tpos[r];
+      const double x = dp[i];
+      d0 += c0[t] * x;
+      d1 += c1[t] * x;
+      d2 += c2[t] * x;
+    }
+    u[3 * k] += d0 * iml[3 * k];
+    u[3 * k + 1] += d1 * iml[3 * k + 1];
+    u[3 * k + 2] += d2 * iml[3 * k + 2];
+  }
+}
+
+__global__ void k_axpy(int64_t n, double a, const double* __restrict__ x, double* __restrict__ y) {
+  note_launch();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    y[k] += a * x[k];
+}
+
+// ----------------------------------------------------------- host helpers --
+int ensure_tpos(fl_mesh_t* m, cudaStream_t s) {
+  if (m->tpos.p) return FL_OK;
+  FL_TRY(m->tpos.reserve((size_t)m->nnz));
+  k_tpos<<<grid_for(m->N, kT), kT, 0, s>>>(m->N, m->findrm.p, m->colm.p, m->tpos.p, m->err.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  const int st = check_err(m->err.p, s, "the pattern is not structurally symmetric");
+  if (st != FL_OK) m->tpos.release();
+  return st;
+}
+
+bool p1_mesh(const fl_mesh_t* m) { return m && m->E > 0 && m->loc == 4; }
+
+template <int THREADS, int RMAX, bool CT, bool BP>
+int launch_div_rows(const DivRowArgs& R, cudaStream_t s) {
+  const size_t smem = CT ? (size_t)3 * RMAX * THREADS * sizeof(float2) : 0;
+  static bool configured = false;
+  if (!configured && smem > 48 * 1024) {
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_div_rows<THREADS, RMAX, CT, BP>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  const unsigned grid = (unsigned)((R.N + THREADS - 1) / THREADS);
+  k_div_rows<THREADS, RMAX, CT, BP><<<grid, THREADS, smem, s>>>(R);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
+// Element and row passes: CT blocks (when ct0 is given) and lumped masses.
+int divergence_passes(fl_mesh_t* m, bool by_parts, double* ct0, double* ct1, double* ct2, double* ct_rhs,
+                      double* dml, double* gml, cudaStream_t s) {
+  FL_TRY(m->em.reserve((size_t)m->E * 10));  // 80 B per element
+  DivElemArgs A{m->E, m->xndglno.p, m->coords.p, reinterpret_cast<float4*>(m->em.p), df_host(1.0 / 24.0)};
+  const unsigned g = grid_for(m->E, 256, 16);
+  k_div_elem<<<g, 256, (256 / 32) * 160 * sizeof(float4), s>>>(A);
+  FL_TRY_CUDA(cudaGetLastError());
+  DivRowArgs R{m->N, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->findrm.p, reinterpret_cast<const float4*>(m->em.p),
+               ct0, ct1, ct2, ct_rhs, dml, gml};
+  if (!ct0) return launch_div_rows<128, 16, false, false>(R, s);
+  if (m->max_row <= 16)
+    return by_parts ? launch_div_rows<128, 16, true, true>(R, s) : launch_div_rows<128, 16, true, false>(R, s);
+  return by_parts ? launch_div_rows<64, 32, true, true>(R, s) : launch_div_rows<64, 32, true, false>(R, s);
+}
+
+}  // namespace
+}  // namespace fl
+
+using namespace fl;
+
+// The second-order pattern of a P1 mesh as a pattern-only handle.
+extern "C" int fl_gpu_secondorder_register(fl_mesh mesh, fl_mesh* out) {
+  FL_CHECK_ARG(mesh && out, "null argument");
+  FL_CHECK_ARG(mesh->N > 0 && mesh->findrm.p && mesh->colm.p, "the mesh has no pattern");
+  cudaStream_t s = mesh->stream;
+  FL_TRY(ensure_tpos(mesh, s));
+  fl_mesh_t* h = new fl_mesh_t();
+  int st = FL_OK;
+  do {
+    cudaGetDevice(&h->device);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      set_error("cudaStreamCreate failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    const int N = mesh->N;
+    h->N = N;
+    h->so_parent = mesh;
+    DevBuf<int32_t> cnt, mr;
+    if ((st = h->err.reserve(1)) || (st = cnt.reserve(N + 1)) || (st = mr.reserve(1)) ||
+        (st = h->findrm.reserve(N + 1)) || (st = h->centrm.reserve(N)))
+      break;
+    if (cudaMemsetAsync(h->err.p, 0, sizeof(ErrWord), s) != cudaSuccess ||
+        cudaMemsetAsync(mr.p, 0, sizeof(int32_t), s) != cudaSuccess) {
+      set_error("memset failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    const unsigned g = (unsigned)std::max(1, std::min((N + kSoWarps - 1) / kSoWarps, num_sms() * 16));
+    k_so_rows<<<g, kSoWarps * 32, 0, s>>>(N, mesh->findrm.p, mesh->colm.p, nullptr, cnt.p, nullptr, nullptr, mr.p,
+                                          h->err.p, 0);
+    if ((st = check_err(h->err.p, s, "second-order row with more candidates than the row scratch holds")) != FL_OK)
+      break;
+    if ((st = exclusive_scan_i32(cnt.p, h->findrm.p, N, s)) != FL_OK) break;
+    int32_t nnz = 0, maxrow = 0;
+    if (cudaMemcpyAsync(&nnz, h->findrm.p + N, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&maxrow, mr.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      set_error("pattern size read-back failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    h->nnz = nnz;
+    h->max_row = maxrow;
+    if ((st = h->colm.reserve((size_t)std::max(nnz, 1)))) break;
+    k_fill_i32<<<grid_for(N, kT), kT, 0, s>>>(h->centrm.p, N, -1);
+    k_so_rows<<<g, kSoWarps * 32, 0, s>>>(N, mesh->findrm.p, mesh->colm.p, h->findrm.p, nullptr, h->colm.p,
+                                          h->centrm.p, mr.p, h->err.p, 1);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+      set_error("second-order pattern fill failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+  } while (0);
+  if (st != FL_OK) {
+    fl_gpu_mesh_destroy(h);
+    return st;
+  }
+  *out = h;
+  return FL_OK;
+}
+
+extern "C" int fl_dev_assemble_divergence_cg(fl_mesh m, const fl_divergence_params* p, double* const ct_val[3],
+                                             double* ct_rhs, double* div_mass_lumped, double* grad_mass_lumped,
+                                             void* stream) {
+  FL_CHECK_ARG(p1_mesh(m), "a P1 mesh handle (P1 pressure and velocity on one mesh)");
+  FL_CHECK_ARG(p && ct_val && ct_val[0] && ct_val[1] && ct_val[2], "null argument");
+  FL_CHECK_ARG(p->index_base == 0 || p->index_base == 1, "index_base");
+  const bool bp = p->integrate_by_parts != 0;
+  FL_CHECK_ARG(!bp || p->nfaces == 0 || (p->faces && p->face_ele), "faces and face_ele");
+  cudaStream_t s = pick(m, stream);
+  FL_TRY(divergence_passes(m, bp, ct_val[0], ct_val[1], ct_val[2], ct_rhs, div_mass_lumped, grad_mass_lumped, s));
+  if (bp && p->nfaces > 0) {
+    const int N = m->N, nf = p->nfaces;
+    FL_TRY(m->face_cnt.reserve(N + 1));
+    FL_TRY(m->face_ptr.reserve(N + 1));
+    FL_TRY(m->face_list.reserve((size_t)3 * nf));
+    FL_TRY_CUDA(cudaMemsetAsync(m->face_cnt.p, 0, sizeof(int32_t) * (N + 1), s));
+    k_face_count<<<grid_for(3 * (int64_t)nf, kT), kT, 0, s>>>(nf, p->faces, p->index_base, N, m->face_cnt.p,
+                                                             m->err.p);
+    FL_TRY(check_err(m->err.p, s, "surface face node out of range"));
+    FL_TRY(exclusive_scan_i32(m->face_cnt.p, m->face_ptr.p, N, s));
+    FL_TRY_CUDA(cudaMemsetAsync(m->face_cnt.p, 0, sizeof(int32_t) * (N + 1), s));
+    k_face_fill<<<grid_for(3 * (int64_t)nf, kT), kT, 0, s>>>(nf, p->faces, p->index_base, N, m->face_ptr.p,
+                                                            m->face_cnt.p, m->face_list.p);
+    k_face_sort<<<grid_for(N, kT), kT, 0, s>>>(N, m->face_ptr.p, m->face_list.p);
+    FaceArgs F{N, p->index_base, m->face_ptr.p, m->face_list.p, p->faces, p->face_ele, p->bc_type, p->bc_val,
+               m->xndglno.p, m->coords.p, m->findrm.p, m->colm.p, ct_val[0], ct_val[1], ct_val[2], ct_rhs,
+               m->E, m->err.p};
+    k_div_faces<<<grid_for(N, 128), 128, 0, s>>>(F);
+    FL_TRY_CUDA(cudaGetLastError());
+  }
+  return check_err(m->err.p, s, "divergence assembly");
+}
+
+extern "C" int fl_dev_lumped_mass(fl_mesh m, double* lumped_mass, void* stream) {
+  FL_CHECK_ARG(p1_mesh(m), "a P1 mesh handle");
+  FL_CHECK_ARG(lumped_mass, "null argument");
+  cudaStream_t s = pick(m, stream);
+  FL_TRY(divergence_passes(m, false, nullptr, nullptr, nullptr, nullptr, lumped_mass, nullptr, s));
+  return FL_OK;
+}
+
+static int rowprod_launch(fl_mesh prod, int ndim, bool div, const double* const a[3], const double* w,
+                          const double* const b[3], double theta, int scale, double* out, cudaStream_t s) {
+  fl_mesh_t* par = prod->so_parent;
+  RowProdArgs P{};
+  P.n = prod->N;
+  P.aptr = par->findrm.p;
+  P.acol = par->colm.p;
+  P.tpos = par->tpos.p;
+  P.optr = prod->findrm.p;
+  P.ocol = prod->colm.p;
+  for (int d = 0; d < 3; ++d) {
+    P.a[d] = d < ndim ? a[d] : nullptr;
+    P.b[d] = d < ndim ? b[d] : nullptr;
+  }
+  P.w = w;
+  P.theta = theta;
+  P.scale = scale;
+  P.out = out;
+  P.err = prod->err.p;
+  const unsigned g = (unsigned)std::max(1, std::min((P.n + kPW - 1) / kPW, num_sms() * 8));
+  if (div) k_rowprod<1, true><<<g, kPW * 32, 0, s>>>(P);
+  else if (ndim == 1) k_rowprod<1, false><<<g, kPW * 32, 0, s>>>(P);
+  else if (ndim == 2) k_rowprod<2, false><<<g, kPW * 32, 0, s>>>(P);
+  else k_rowprod<3, false><<<g, kPW * 32, 0, s>>>(P);
+  FL_TRY_CUDA(cudaGetLastError());
+  return check_err(prod->err.p, s, "row product: output row longer than the shared-memory row or outside the pattern");
+}
+
+static int check_product(fl_mesh prod) {
+  FL_CHECK_ARG(prod && prod->so_parent, "a second-order pattern handle (fl_gpu_secondorder_register)");
+  FL_CHECK_ARG(prod->so_parent->tpos.p, "the parent mesh has no transpose map");
+  return FL_OK;
+}
+
+extern "C" int fl_dev_mult_div_vector_div_T(fl_mesh prod, int32_t ndim, const double* const a_val[3],
+                                            const double* w, const double* const b_val[3], double* out,
+                                            void* stream) {
+  FL_TRY(check_product(prod));
+  FL_CHECK_ARG(ndim >= 1 && ndim <= 3, "ndim 1..3");
+  FL_CHECK_ARG(a_val && b_val && w && out, "null argument");
+  for (int d = 0; d < ndim; ++d) FL_CHECK_ARG(a_val[d] && b_val[d], "null block");
+  return rowprod_launch(prod, ndim, false, a_val, w, b_val, 1.0, 0, out, pick(prod, stream));
+}
+
+extern "C" int fl_dev_mult_div_invscalar_div_T(fl_mesh prod, const double* a_val, const double* s_val,
+                                               const double* b_val, double* out, void* stream) {
+  FL_TRY(check_product(prod));
+  FL_CHECK_ARG(a_val && b_val && s_val && out, "null argument");
+  const double* a[3] = {a_val, nullptr, nullptr};
+  const double* b[3] = {b_val, nullptr, nullptr};
+  return rowprod_launch(prod, 1, true, a, s_val, b, 1.0, 0, out, pick(prod, stream));
+}
+
+extern "C" int fl_dev_assemble_kmk(fl_mesh m, fl_mesh prod, double theta_pg, const double* p_masslump,
+                                   double* kt_val, double* kmk_val, void* stream) {
+  FL_CHECK_ARG(p1_mesh(m), "a P1 mesh handle");
+  FL_TRY(check_product(prod));
+  FL_CHECK_ARG(prod->so_parent == m, "the product pattern of this mesh");
+  FL_CHECK_ARG(p_masslump && kmk_val, "null argument");
+  cudaStream_t s = pick(m, stream);
+  double* kt = kt_val;
+  if (!kt) {
+    FL_TRY(m->st_val.reserve((size_t)m->nnz));
+    kt = m->st_val.p;
+  }
+  FL_TRY(m->em.reserve((size_t)m->E * 14));
+  // the row pass also sums four rhs slots per element: keep them zero
+  FL_TRY_CUDA(cudaMemsetAsync(m->em.p + (size_t)10 * m->E, 0, sizeof(double) * 4 * m->E, s));
+  KmkArgs K{m->E, m->xndglno.p, m->coords.p, m->em.p};
+  k_kmk_elem<<<grid_for(m->E, 128, 16), 128, 0, s>>>(K);
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY(m->st_rhs.reserve((size_t)m->N));
+  FL_TRY(rows_p1_closed(m, m->em.p, kt, m->st_rhs.p, s));
+  // by scaling masslump with theta, kmk is divided by theta (Momentum_CG.F90:2750-2762)
+  const int scale = fabs(theta_pg - 1.0) < DBL_EPSILON ? 0 : 1;
+  const double* a[3] = {kt, nullptr, nullptr};
+  return rowprod_launch(prod, 1, true, a, p_masslump, a, theta_pg, scale, kmk_val, s);
+}
+
+extern "C" int fl_dev_masslumped_poisson_rhs(fl_mesh m, const double* const ctp_val[3], const double* mom_rhs,
+                                             const double* ct_rhs, const double* inverse_masslump,
+                                             const double* velocity, double dt, double theta_pg,
+                                             double* poisson_rhs, void* stream) {
+  FL_CHECK_ARG(m && m->N > 0 && m->findrm.p, "mesh");
+  FL_CHECK_ARG(ctp_val && ctp_val[0] && ctp_val[1] && ctp_val[2] && velocity && poisson_rhs, "null argument");
+  FL_CHECK_ARG(!mom_rhs || inverse_masslump, "mom_rhs needs inverse_masslump");
+  FL_CHECK_ARG(dt != 0.0 && theta_pg != 0.0, "dt and theta_pg nonzero");
+  cudaStream_t s = pick(m, stream);
+  k_poisson_rhs<<<grid_for(m->N, kT), kT, 0, s>>>(m->N, m->findrm.p, m->colm.p, ctp_val[0], ctp_val[1], ctp_val[2],
+                                                   mom_rhs, ct_rhs, inverse_masslump, velocity, 1.0 / dt / theta_pg,
+                                                   poisson_rhs);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
+extern "C" int fl_dev_correct_masslumped_velocity(fl_mesh m, const double* const ct_val[3],
+                                                  const double* inverse_masslump, const double* delta_p,
+                                                  double* velocity, void* stream) {
+  FL_CHECK_ARG(m && m->N > 0 && m->findrm.p, "mesh");
+  FL_CHECK_ARG(ct_val && ct_val[0] && ct_val[1] && ct_val[2] && inverse_masslump && delta_p && velocity,
+               "null argument");
+  cudaStream_t s = pick(m, stream);
+  FL_TRY(ensure_tpos(m, s));
+  k_correct_velocity<<<grid_for(m->N, kT), kT, 0, s>>>(m->N, m->findrm.p, m->colm.p, m->tpos.p, ct_val[0],
+                                                        ct_val[1], ct_val[2], inverse_masslump, delta_p, velocity);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
+extern "C" int fl_dev_csr_addto(fl_mesh pattern, double* val, const double* other, double scale, void* stream) {
+  FL_CHECK_ARG(pattern && pattern->nnz > 0 && val && other, "null argument");
+  cudaStream_t s = pick(pattern, stream);
+  k_axpy<<<grid_for(pattern->nnz, kT), kT, 0, s>>>(pattern->nnz, scale, other, val);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}

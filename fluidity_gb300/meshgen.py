@@ -96,6 +96,25 @@ def boundary_nodes(coords: np.ndarray, tol: float = 1e-14) -> np.ndarray:
     return np.nonzero(on)[0].astype(np.int32)
 
 
+def boundary_faces(ndglno: np.ndarray):
+    """Surface mesh of a tet mesh: ``(faces (nf, 3) int32, face_ele (nf,) int32)``.
+
+    The faces that belong to one element only, in (element, local face)
+    order; local face ``f`` holds the element's vertices other than ``f`` in
+    ascending local order.  ``face_ele`` is the owning element (the
+    reference's ``face_ele``).
+    """
+    nd = np.asarray(ndglno, dtype=np.int64)
+    E = nd.shape[0]
+    drop = [[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]]
+    tri = np.stack([nd[:, d] for d in drop], axis=1).reshape(-1, 3)   # (4E, 3)
+    key = np.sort(tri, axis=1)
+    _, inv, cnt = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    once = cnt[inv.reshape(-1)] == 1
+    idx = np.nonzero(once)[0]
+    return tri[idx].astype(np.int32), (idx // 4).astype(np.int32)
+
+
 def p2_coordinates(ndglno1: np.ndarray, ndglno2: np.ndarray, coords1: np.ndarray,
                    counts: np.ndarray) -> np.ndarray:
     """Positions of P2 nodes of an affine mesh: ``sum_j (count_j / 2) X_j``.

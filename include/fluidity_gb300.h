@@ -361,6 +361,89 @@ int fl_gnn_train_step(fl_gnn net, const double* p1, const double* p2, const doub
                       const double* target, const uint8_t* mask, int32_t nact, float lr,
                       float* loss_dev, void* stream);
 
+/* ------------------------------------------------ pressure projection -- */
+/* P1 pressure and P1 velocity on one mesh handle (the P1-P1 configuration of
+ * the projection method).  The divergence matrix ct_m is a block_csr_matrix
+ * with blocks (1, dim): three device arrays of mesh-pattern values.  Vector
+ * fields are vector_field%val(3, N) (x, y, z of a node adjacent). */
+
+/* Second-order sparsity of the mesh's first-order pattern
+ * (get_csr_sparsity_secondorder, femtools/Sparsity_Patterns_Meshes.F90:122-148
+ * -> make_sparsity_transpose, femtools/Sparsity_Patterns.F90:87-148), built on
+ * the GPU and bit-exact, as a pattern-only handle usable by fl_dev_petsc_solve,
+ * fl_dev_csr_mult, fl_dev_apply_dirichlet and fl_gpu_sparsity_copy, and by the
+ * row products below.  The mesh must outlive the returned handle. */
+int fl_gpu_secondorder_register(fl_mesh mesh, fl_mesh* out);
+
+/* Options of assemble_divergence_matrix_cg (assemble/Divergence_Matrix_CG.F90:
+ * 67-375).  By parts, the surface loop (:312-366) runs over the nfaces surface
+ * triangles: faces(3, nfaces) = face_global_nodes, face_ele(nfaces) = the
+ * volume element of each face, bc_type(3, nfaces) = field_bc_type(dim, sele)
+ * (0 none or strong Dirichlet, 1 weakdirichlet, 2 no_normal_flow, 3 internal,
+ * 4 free_surface, 5 prescribed_normal_flow), bc_val(3, 3, nfaces) =
+ * ele_val(field_bc, dim, sele) per face node (types 1 and 5 only; may be null
+ * otherwise). */
+typedef struct {
+  int32_t integrate_by_parts;
+  int32_t nfaces;
+  int32_t index_base;
+  int32_t pad;
+  const int32_t* faces;
+  const int32_t* face_ele;
+  const int32_t* bc_type;
+  const double* bc_val;
+} fl_divergence_params;
+
+/* Replaces assemble_divergence_matrix_cg for P1P1, single phase: ct_val[dim]
+ * (mesh nnz each), ct_rhs (N, zeroed then the weak-Dirichlet / normal-flow
+ * surface terms; may be null), div_mass_lumped and grad_mass_lumped (N; may
+ * be null).  Device pointers; element contributions are summed in colour
+ * order and are deterministic. */
+int fl_dev_assemble_divergence_cg(fl_mesh mesh, const fl_divergence_params* params, double* const ct_val[3],
+                                  double* ct_rhs, double* div_mass_lumped, double* grad_mass_lumped,
+                                  void* stream);
+
+/* compute_lumped_mass (femtools/FEFields.F90:161-214) of a P1 mesh with unit
+ * density, as get_lumped_mass (femtools/State_Fields.F90:124-152) caches it. */
+int fl_dev_lumped_mass(fl_mesh mesh, double* lumped_mass, void* stream);
+
+/* mult_div_vector_div_T (femtools/Sparse_Matrices_Fields.F90:590-671):
+ * out(i,j) = sum_k sum_dim a_dim(i,k) w(dim,k) b_dim(j,k) over the
+ * second-order pattern `product`; a and b are ndim blocks on the parent
+ * mesh's pattern, w is vector_field%val(ndim, N).  With a = ctp_m, b = ct_m
+ * and w the inverse lumped mass it is assemble_masslumped_cmc
+ * (assemble/Assemble_CMC.F90:119-135). */
+int fl_dev_mult_div_vector_div_T(fl_mesh product, int32_t ndim, const double* const a_val[3], const double* w,
+                                 const double* const b_val[3], double* out, void* stream);
+/* mult_div_invscalar_div_T (femtools/Sparse_Matrices_Fields.F90:673-748):
+ * out(i,j) = sum_k a(i,k) b(j,k) / s(k).  Every entry of a second-order
+ * pattern has a common column, so every output entry is written at its own
+ * position. */
+int fl_dev_mult_div_invscalar_div_T(fl_mesh product, const double* a_val, const double* s_val,
+                                    const double* b_val, double* out, void* stream);
+
+/* assemble_kmk_matrix (assemble/Momentum_CG.F90:2707-2766): the P1-P1 pressure
+ * stabilisation K^T M_l^-1 K / theta_pg over the second-order pattern, K the
+ * pressure diffusion matrix with the elements' edge-length tensors
+ * (0.5 dshape_tensor_dshape with h_bar = get_edge_lengths).  kt_val receives K
+ * (mesh nnz; may be null). */
+int fl_dev_assemble_kmk(fl_mesh mesh, fl_mesh product, double theta_pg, const double* p_masslump, double* kt_val,
+                        double* kmk_val, void* stream);
+
+/* assemble_masslumped_poisson_rhs (assemble/Momentum_CG.F90:2670-2705):
+ * poisson_rhs = -C_P (M_l^-1 mom_rhs + u / (dt theta_pg)) + ct_rhs / (dt theta_pg);
+ * mom_rhs and ct_rhs may be null (zero). */
+int fl_dev_masslumped_poisson_rhs(fl_mesh mesh, const double* const ctp_val[3], const double* mom_rhs,
+                                  const double* ct_rhs, const double* inverse_masslump, const double* velocity,
+                                  double dt, double theta_pg, double* poisson_rhs, void* stream);
+/* correct_masslumped_velocity (assemble/Momentum_CG.F90:2544-2575):
+ * u += M_l^-1 C^T delta_p. */
+int fl_dev_correct_masslumped_velocity(fl_mesh mesh, const double* const ct_val[3], const double* inverse_masslump,
+                                       const double* delta_p, double* velocity, void* stream);
+/* addto(matrix, other, scale) for two matrices on one pattern (add_kmk_matrix,
+ * assemble/Momentum_CG.F90:2768-2777, is scale 1). */
+int fl_dev_csr_addto(fl_mesh pattern, double* val, const double* other, double scale, void* stream);
+
 /* Number of kernels this library launched on the calling process so far
  * (launch accounting for benchmarks). */
 int64_t fl_kernel_launch_count(void);

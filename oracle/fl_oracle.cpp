@@ -1042,3 +1042,479 @@ void orc_csr_mult(int n, const int64_t* findrm, const int* colm, const double* v
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Pressure projection pieces on a P1 mesh (P1 velocity, P1 pressure).
+// ===========================================================================
+namespace {
+
+// Triangle rule of degree 2 (Quadrature.F90:936-949, construct_tri_quadratures:
+// Str71 three points, permutation 5 (Quadrature.F90:1821-1826) of the
+// coordinates (1/6, 1 - 2/6), weight 1/6 each).  Face node i has shape
+// function L_i; the P1 face element's dn is d(L1, L2, L3)/d(L1, L2).
+struct TriQuad {
+  int ngi = 3;
+  double l[3][3];
+  double w[3];
+};
+TriQuad tri_quad2() {
+  TriQuad t;
+  const double c1 = 0.166666666666666666666666666666666, c2 = 1.0 - 2.0 * c1;
+  const int perm[3][3] = {{1, 1, 2}, {1, 2, 1}, {2, 1, 1}};
+  const double c[2] = {c1, c2};
+  for (int k = 0; k < 3; ++k) {
+    for (int j = 0; j < 3; ++j) t.l[k][j] = c[perm[k][j] - 1];
+    t.w[k] = 0.166666666666666666666666666666666;
+  }
+  return t;
+}
+
+void element_dshape(const double* coords, const int* xn, const Shape& s, int ngi, const Quad& q,
+                    double (*dt)[16][3], double* detwei, double* detJ) {
+  double X[12];
+  for (int i = 0; i < 4; ++i)
+    for (int a = 0; a < 3; ++a) X[3 * i + a] = coords[3 * (int64_t)xn[i] + a];
+  Geo g;
+  element_geometry(X, s, g);
+  for (int gi = 0; gi < ngi; ++gi) detwei[gi] = std::fabs(g.detJ) * q.w[gi];
+  for (int gi = 0; gi < ngi; ++gi)
+    for (int i = 0; i < s.loc; ++i)
+      for (int a = 0; a < 3; ++a) {
+        double v = 0.0;
+        for (int b = 0; b < 3; ++b) v += s.dn[i][gi][b] * g.invJ[a][b];
+        dt[i][gi][a] = v;
+      }
+  if (detJ) *detJ = g.detJ;
+}
+
+// solve (femtools/Vector_tools.F90, LAPACK dgesv): Gaussian elimination with
+// partial pivoting on the largest magnitude in the column.
+void solve_dense(int n, double* A /*row-major n x n*/, double* x) {
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(A[r * n + c]) > std::fabs(A[piv * n + c])) piv = r;
+    if (piv != c) {
+      for (int k = 0; k < n; ++k) std::swap(A[c * n + k], A[piv * n + k]);
+      std::swap(x[c], x[piv]);
+    }
+    for (int r = c + 1; r < n; ++r) {
+      const double f = A[r * n + c] / A[c * n + c];
+      for (int k = c; k < n; ++k) A[r * n + k] -= f * A[c * n + k];
+      x[r] -= f * x[c];
+    }
+  }
+  for (int r = n - 1; r >= 0; --r) {
+    double v = x[r];
+    for (int k = r + 1; k < n; ++k) v -= A[r * n + k] * x[k];
+    x[r] = v / A[r * n + r];
+  }
+}
+
+// simplex_tensor (femtools/Metric_tools.F90:852-941): the metric m whose
+// unit ball has every edge of the simplex at unit length, from the dof(dim)
+// linear system A(edge, idx(k,l)) = diff(k) diff(l) coeff(k,l), A x = 1.
+void simplex_tensor(int dim, const double* X /*dim x (dim+1), column = vertex*/, double* m) {
+  const int loc = dim + 1, d = dim * (dim + 1) / 2;
+  auto idx = [dim](int i, int j) {  // 1-based as in the reference
+    const int k = std::min(i, j), l = std::max(i, j);
+    if (k == 1) return l;
+    return dim == 3 ? l + k : l + k - 1;
+  };
+  double A[36] = {}, x[6];
+  int n = 0;
+  for (int i = 0; i < loc; ++i)
+    for (int j = i + 1; j < loc; ++j) {
+      double diff[3];
+      for (int a = 0; a < dim; ++a) diff[a] = X[dim * j + a] - X[dim * i + a];
+      for (int k = 1; k <= dim; ++k)
+        for (int l = 1; l <= dim; ++l)
+          A[n * d + idx(k, l) - 1] = diff[k - 1] * diff[l - 1] * (k == l ? 1.0 : 2.0);
+      ++n;
+    }
+  for (int k = 0; k < d; ++k) x[k] = 1.0;
+  solve_dense(d, A, x);
+  for (int i = 1; i <= dim; ++i)
+    for (int j = 1; j <= dim; ++j) m[(i - 1) * dim + (j - 1)] = x[idx(i, j) - 1];
+}
+
+// eigendecomposition_symmetric (femtools/Vector_tools.F90, LAPACK dsyev),
+// restated as the cyclic Jacobi method: m = V diag(e) V^T.
+void eigen_sym(int n, const double* m, double* V, double* e) {
+  double a[9];
+  std::memcpy(a, m, sizeof(double) * n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) V[i * n + j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += a[p * n + q] * a[p * n + q];
+    if (off == 0.0) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a[p * n + q];
+        if (apq == 0.0) continue;
+        const double th = (a[q * n + q] - a[p * n + p]) / (2.0 * apq);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {
+          const double akp = a[k * n + p], akq = a[k * n + q];
+          a[k * n + p] = c * akp - s * akq;
+          a[k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = a[p * n + k], aqk = a[q * n + k];
+          a[p * n + k] = c * apk - s * aqk;
+          a[q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[k * n + p], vkq = V[k * n + q];
+          V[k * n + p] = c * vkp - s * vkq;
+          V[k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < n; ++i) e[i] = a[i * n + i];
+}
+
+// edge_length_from_eigenvalue_metric (femtools/Metric_tools.F90:157-164):
+// eigenvalues replaced by 1/sqrt(|lambda|) (:145-155) and recomposed.
+void edge_length_metric(int n, const double* m, double* out) {
+  double V[9], e[3];
+  eigen_sym(n, m, V, e);
+  for (int i = 0; i < n; ++i) e[i] = 1.0 / std::sqrt(std::fabs(e[i]));
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < n; ++k) v += V[i * n + k] * e[k] * V[j * n + k];
+      out[i * n + j] = v;
+    }
+}
+
+// mult_div_invscalar_div_T (femtools/Sparse_Matrices_Fields.F90:673-748):
+// product(i,j) = sum_k A(i,k) B(j,k) / s(k) by a merge walk of the sorted
+// rows; the output position only advances for entries with a common column.
+void mult_div_invscalar(int n, const int64_t* af, const int* ac, const double* av, const double* s,
+                        const int64_t* bf, const int* bc, const double* bv, const int64_t* pf,
+                        const int* pc, double* out) {
+  int64_t nentry0 = 0;
+  for (int i = 0; i < n; ++i) {
+    const int64_t rb = af[i], re = af[i + 1];
+    if (re - rb <= 0) continue;
+    for (int64_t jc = pf[i]; jc < pf[i + 1]; ++jc) {
+      const int j = pc[jc];
+      const int64_t cb = bf[j], ce = bf[j + 1];
+      if (ce - cb <= 0) continue;
+      double entry0 = 0.0;
+      bool addflag = false;
+      int64_t k1 = rb, k2 = cb;
+      while (k1 < re && k2 < ce) {
+        if (ac[k1] < bc[k2]) {
+          ++k1;
+        } else if (ac[k1] == bc[k2]) {
+          entry0 = entry0 + av[k1] * bv[k2] / s[ac[k1]];
+          addflag = true;
+          ++k1;
+          ++k2;
+        } else {
+          ++k2;
+        }
+      }
+      if (addflag) out[nentry0++] = entry0;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// compute_lumped_mass (femtools/FEFields.F90:161-214) with unit density:
+// row sums of shape_shape(N, N, detwei) added per element.
+int orc_lumped_mass(int E, int degree, const int* ndglno, const int* ndglno_x, const double* coords,
+                    int quad_degree, int N, double* out) {
+  Quad q;
+  if (!make_tet_quad(quad_degree, q) || degree < 1 || degree > 2) return ORC_ERR_ARG;
+  Shape s, xs;
+  make_shape(degree, q, s);
+  make_shape(1, q, xs);
+  std::memset(out, 0, sizeof(double) * N);
+  for (int e = 0; e < E; ++e) {
+    double X[12];
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) X[3 * i + a] = coords[3 * (int64_t)ndglno_x[4 * (int64_t)e + i] + a];
+    Geo g;
+    element_geometry(X, xs, g);
+    double detwei[16];
+    for (int gi = 0; gi < q.ngi; ++gi) detwei[gi] = std::fabs(g.detJ) * q.w[gi];
+    const int* nd = ndglno + (int64_t)s.loc * e;
+    for (int i = 0; i < s.loc; ++i) {
+      double row = 0.0;
+      for (int j = 0; j < s.loc; ++j) {
+        double m = 0.0;
+        for (int gi = 0; gi < q.ngi; ++gi) m += s.n[i][gi] * s.n[j][gi] * detwei[gi];
+        row += m;
+      }
+      out[nd[i]] += row;
+    }
+  }
+  return ORC_OK;
+}
+
+// assemble_divergence_matrix_cg (assemble/Divergence_Matrix_CG.F90:67-375)
+// for P1 pressure and P1 velocity on one mesh, single phase:
+//   not by parts: ele_mat = shape_dshape(N_p, dN_u, detwei)  (FETools.F90:332)
+//   by parts:     ele_mat = -dshape_shape(dN_p, N_u, detwei) (FETools.F90:364)
+// added per dimension into the blocks ct(dim) over the first-order pattern,
+// with the lumped div/grad masses (row sums of shape_shape).  By parts, the
+// surface loop (:312-366) adds shape_shape_vector(N, N, detwei_f, normal)
+// (FETools.F90:228) into ct(dim) for faces without a boundary condition in
+// that dimension (type 0), into ct_rhs against the weak-Dirichlet values
+// (type 1) or, for prescribed normal flow (type 5 in dimension 1), subtracts
+// shape_rhs(N, detwei_f * g) from ct_rhs; faces of types 2-4 are skipped.
+// The face normal is facet_normal (Transform_elements.F90:1527-1553): the
+// cross product of the face Jacobian's columns oriented along (face centroid
+// - element centroid) and normalised.  bc_type is [face][dim], bc_val is
+// [face][face node][dim].  ct holds the three blocks one after the other.
+int orc_assemble_divergence_p1(int E, const int* ndglno, const double* coords, int N, const int64_t* findrm,
+                               const int* colm, int quad_degree, int by_parts, int nf, const int* faces,
+                               const int* face_ele, const int* bc_type, const double* bc_val, double* ct,
+                               double* ct_rhs, double* div_ml, double* grad_ml) {
+  Quad q;
+  if (!make_tet_quad(quad_degree, q)) return ORC_ERR_ARG;
+  Shape s;
+  make_shape(1, q, s);
+  const int64_t nnz = findrm[N] - findrm[0];
+  std::memset(ct, 0, sizeof(double) * 3 * nnz);
+  if (ct_rhs) std::memset(ct_rhs, 0, sizeof(double) * N);
+  if (div_ml) std::memset(div_ml, 0, sizeof(double) * N);
+  if (grad_ml) std::memset(grad_ml, 0, sizeof(double) * N);
+  for (int e = 0; e < E; ++e) {
+    const int* nd = ndglno + 4 * (int64_t)e;
+    double dt[10][16][3], detwei[16];
+    element_dshape(coords, nd, s, q.ngi, q, dt, detwei, nullptr);
+    for (int d = 0; d < 3; ++d)
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+          double v = 0.0;
+          for (int gi = 0; gi < q.ngi; ++gi)
+            v += detwei[gi] * (by_parts ? dt[i][gi][d] * s.n[j][gi] : s.n[i][gi] * dt[j][gi][d]);
+          if (by_parts) v = -v;
+          const int64_t p = csr_pos(findrm, colm, nd[i], nd[j]);
+          if (p < 0) return ORC_ERR_OUTSIDE_PATTERN;
+          ct[d * nnz + p] += v;
+        }
+    for (int i = 0; i < 4; ++i) {
+      double row = 0.0;
+      for (int j = 0; j < 4; ++j) {
+        double m = 0.0;
+        for (int gi = 0; gi < q.ngi; ++gi) m += s.n[i][gi] * s.n[j][gi] * detwei[gi];
+        row += m;
+      }
+      if (div_ml) div_ml[nd[i]] += row;
+      if (grad_ml) grad_ml[nd[i]] += row;
+    }
+  }
+  if (!by_parts) return ORC_OK;
+  const TriQuad t = tri_quad2();
+  for (int f = 0; f < nf; ++f) {
+    const int* ty = bc_type + 3 * f;
+    bool skip = false;
+    for (int d = 0; d < 3; ++d) skip = skip || ty[d] == 2 || ty[d] == 3 || ty[d] == 4;
+    if (skip) continue;
+    const int* fn = faces + 3 * f;
+    const int* en = ndglno + 4 * (int64_t)face_ele[f];
+    double Xf[3][3], cf[3] = {0, 0, 0}, ce[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int a = 0; a < 3; ++a) {
+        Xf[i][a] = coords[3 * (int64_t)fn[i] + a];
+        cf[a] += Xf[i][a];
+      }
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) ce[a] += coords[3 * (int64_t)en[i] + a];
+    double J[3][2], outward[3];
+    for (int a = 0; a < 3; ++a) {
+      J[a][0] = Xf[0][a] - Xf[2][a];
+      J[a][1] = Xf[1][a] - Xf[2][a];
+      outward[a] = cf[a] / 3.0 - ce[a] / 4.0;
+    }
+    double detJ = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double c = J[cyc3[i + 2]][0] * J[cyc3[i + 1]][1] - J[cyc3[i + 2]][1] * J[cyc3[i + 1]][0];
+      detJ += c * c;
+    }
+    detJ = std::sqrt(detJ);
+    double nrm[3] = {J[1][0] * J[2][1] - J[2][0] * J[1][1], J[2][0] * J[0][1] - J[0][0] * J[2][1],
+                     J[0][0] * J[1][1] - J[1][0] * J[0][1]};
+    const double o = nrm[0] * outward[0] + nrm[1] * outward[1] + nrm[2] * outward[2];
+    for (int a = 0; a < 3; ++a) nrm[a] *= o;
+    const double len = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+    for (int a = 0; a < 3; ++a) nrm[a] /= len;
+    double dw[3];
+    for (int gi = 0; gi < 3; ++gi) dw[gi] = detJ * t.w[gi];
+    const double* bv = bc_val ? bc_val + 9 * f : nullptr;
+    if (ty[0] == 5 && ct_rhs) {
+      for (int i = 0; i < 3; ++i) {
+        double r = 0.0;
+        for (int gi = 0; gi < 3; ++gi) {
+          double gq = 0.0;
+          for (int j = 0; j < 3; ++j) gq += bv[3 * j + 0] * t.l[gi][j];
+          r += t.l[gi][i] * (dw[gi] * gq);
+        }
+        ct_rhs[fn[i]] -= r;
+      }
+      continue;
+    }
+    for (int d = 0; d < 3; ++d)
+      for (int i = 0; i < 3; ++i) {
+        double mrow[3];
+        for (int j = 0; j < 3; ++j) {
+          double v = 0.0;
+          for (int gi = 0; gi < 3; ++gi) v += nrm[d] * (t.l[gi][i] * t.l[gi][j]) * dw[gi];
+          mrow[j] = v;
+        }
+        if (ty[d] == 1 && ct_rhs) {
+          double r = 0.0;
+          for (int j = 0; j < 3; ++j) r += mrow[j] * bv[3 * j + d];
+          ct_rhs[fn[i]] -= r;
+        } else {
+          for (int j = 0; j < 3; ++j) {
+            const int64_t p = csr_pos(findrm, colm, fn[i], fn[j]);
+            if (p < 0) return ORC_ERR_OUTSIDE_PATTERN;
+            ct[d * nnz + p] += mrow[j];
+          }
+        }
+      }
+  }
+  return ORC_OK;
+}
+
+// make_sparsity_transpose (femtools/Sparsity_Patterns.F90:87-148) for one
+// mesh: for every node i, every pair (j, k) of the nodes sharing an element
+// with i (row i of the first-order pattern) puts k in row j, ascending
+// (insert_ascending).  Two-call protocol: with out_colm == nullptr only the
+// entry count is returned.
+int64_t orc_sparsity_secondorder(int n, const int64_t* findrm, const int* colm, int64_t* out_findrm,
+                                 int* out_colm, int64_t cap) {
+  std::vector<std::vector<int>> rows(n);
+  for (int i = 0; i < n; ++i)
+    for (int64_t a = findrm[i]; a < findrm[i + 1]; ++a) {
+      std::vector<int>& r = rows[colm[a]];
+      for (int64_t b = findrm[i]; b < findrm[i + 1]; ++b) {
+        const int k = colm[b];
+        auto it = std::lower_bound(r.begin(), r.end(), k);
+        if (it == r.end() || *it != k) r.insert(it, k);
+      }
+    }
+  int64_t nnz = 0;
+  out_findrm[0] = 0;
+  for (int i = 0; i < n; ++i) {
+    if (out_colm)
+      for (size_t k = 0; k < rows[i].size(); ++k)
+        if (nnz + (int64_t)k < cap) out_colm[nnz + k] = rows[i][k];
+    nnz += (int64_t)rows[i].size();
+    out_findrm[i + 1] = nnz;
+  }
+  return nnz;
+}
+
+// mult_div_vector_div_T (femtools/Sparse_Matrices_Fields.F90:590-671):
+// product(i,j) = sum_k sum_dim A_dim(i,k) B_dim(j,k) w(dim,k) by a merge walk
+// of the sorted rows, every product entry written in order.  a and b hold
+// ndim blocks of values one after the other, both on the pattern (af, ac)
+// (ctp_m and ct_m share the divergence sparsity); w is
+// vector_field%val(ndim, ncols).
+void orc_mult_div_vector_div_T(int n, int ndim, const int64_t* af, const int* ac, const double* a,
+                               const double* w, const double* b, const int64_t* pf, const int* pc,
+                               double* out) {
+  const int64_t* bf = af;
+  const int* bc = ac;
+  const int64_t annz = af[n] - af[0];
+  int64_t nentry0 = 0;
+  for (int i = 0; i < n; ++i)
+    for (int64_t jc = pf[i]; jc < pf[i + 1]; ++jc) {
+      const int j = pc[jc];
+      double entry0 = 0.0;
+      int64_t k1 = af[i], k2 = bf[j];
+      while (k1 < af[i + 1] && k2 < bf[j + 1]) {
+        if (ac[k1] < bc[k2]) {
+          ++k1;
+        } else if (ac[k1] == bc[k2]) {
+          for (int d = 0; d < ndim; ++d)
+            entry0 = entry0 + a[d * annz + k1] * b[d * annz + k2] * w[(int64_t)ndim * ac[k1] + d];
+          ++k1;
+          ++k2;
+        } else {
+          ++k2;
+        }
+      }
+      out[nentry0++] = entry0;
+    }
+}
+
+void orc_mult_div_invscalar_div_T(int n, const int64_t* af, const int* ac, const double* a, const double* s,
+                                  const int64_t* bf, const int* bc, const double* b, const int64_t* pf,
+                                  const int* pc, double* out) {
+  mult_div_invscalar(n, af, ac, a, s, bf, bc, b, pf, pc, out);
+}
+
+// simplex_tensor and its edge-length form for one simplex (the known answers
+// of error_measures/tests/test_simplex_tensor.F90 and
+// test_simplex_tensor_edgelens.F90 pin them).
+void orc_simplex_tensor(int dim, const double* X, double* m) { simplex_tensor(dim, X, m); }
+void orc_edge_length_metric(int dim, const double* m, double* out) { edge_length_metric(dim, m, out); }
+
+// assemble_kmk_matrix (assemble/Momentum_CG.F90:2707-2766) on a P1 pressure
+// mesh: kt = sum_e 0.5 dshape_tensor_dshape(dp, h_bar, dp, detwei)
+// (FETools.F90:668-698) with h_bar = get_edge_lengths of the element
+// (error_measures/Edge_lengths.F90:68-79: edge_length_from_eigenvalue of
+// simplex_tensor) at every quadrature point, then
+// kmk = mult_div_invscalar_div_T(kt, masslump (times theta_pg unless
+// |theta_pg - 1| < epsilon), kt) over the second-order pattern.
+int orc_assemble_kmk(int E, const int* ndglno, const double* coords, int N, const int64_t* findrm,
+                     const int* colm, int quad_degree, double theta_pg, const double* p_masslump,
+                     const int64_t* sof, const int* soc, double* kt, double* kmk) {
+  Quad q;
+  if (!make_tet_quad(quad_degree, q)) return ORC_ERR_ARG;
+  Shape s;
+  make_shape(1, q, s);
+  const int64_t nnz = findrm[N] - findrm[0];
+  std::memset(kt, 0, sizeof(double) * nnz);
+  for (int e = 0; e < E; ++e) {
+    const int* nd = ndglno + 4 * (int64_t)e;
+    double dt[10][16][3], detwei[16];
+    element_dshape(coords, nd, s, q.ngi, q, dt, detwei, nullptr);
+    double X[12], M[9], H[9];
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) X[3 * i + a] = coords[3 * (int64_t)nd[i] + a];
+    simplex_tensor(3, X, M);
+    edge_length_metric(3, M, H);
+    double R[4][4] = {};
+    for (int gi = 0; gi < q.ngi; ++gi)
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+          double v[3];
+          for (int b = 0; b < 3; ++b) {
+            double t = 0.0;
+            for (int a = 0; a < 3; ++a) t += dt[i][gi][a] * H[a * 3 + b];
+            v[b] = t;
+          }
+          double dd = 0.0;
+          for (int b = 0; b < 3; ++b) dd += v[b] * dt[j][gi][b];
+          R[i][j] = R[i][j] + dd * detwei[gi];
+        }
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        const int64_t p = csr_pos(findrm, colm, nd[i], nd[j]);
+        if (p < 0) return ORC_ERR_OUTSIDE_PATTERN;
+        kt[p] += 0.5 * R[i][j];
+      }
+  }
+  std::vector<double> sc(p_masslump, p_masslump + N);
+  if (!(std::fabs(theta_pg - 1.0) < 2.220446049250313e-16))
+    for (int i = 0; i < N; ++i) sc[i] = p_masslump[i] * theta_pg;
+  mult_div_invscalar(N, findrm, colm, kt, sc.data(), findrm, colm, kt, sof, soc, kmk);
+  return ORC_OK;
+}
+
+}  // extern "C"

@@ -237,3 +237,136 @@ def csr_mult(findrm, colm, val, x):
                        _p(np.ascontiguousarray(val, dtype=np.float64)),
                        _p(np.ascontiguousarray(x, dtype=np.float64)), _p(y))
     return y
+
+
+# ------------------------------------------------ pressure projection (P1P1) --
+def lumped_mass(ndglno, ndglno_x, coords, n, degree=1, quad_degree=2):
+    """compute_lumped_mass (FEFields.F90:161-214), unit density."""
+    nd = np.ascontiguousarray(ndglno, dtype=np.int32)
+    ndx = np.ascontiguousarray(ndglno_x, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    out = np.zeros(n)
+    st = lib().orc_lumped_mass(nd.shape[0], degree, _p(nd), _p(ndx), _p(X), quad_degree, n, _p(out))
+    assert st == 0, st
+    return out
+
+
+def assemble_divergence_p1(ndglno, coords, findrm, colm, *, by_parts=False, faces=None, face_ele=None,
+                           bc_type=None, bc_val=None, quad_degree=2):
+    """(ct (3, nnz), ct_rhs, div_mass_lumped, grad_mass_lumped) --
+    assemble_divergence_matrix_cg (Divergence_Matrix_CG.F90:67-375), P1P1."""
+    nd = np.ascontiguousarray(ndglno, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    n = f.size - 1
+    nf = 0 if faces is None else len(faces)
+    fa = np.ascontiguousarray(faces, dtype=np.int32) if nf else None
+    fe = np.ascontiguousarray(face_ele, dtype=np.int32) if nf else None
+    ty = (np.ascontiguousarray(bc_type, dtype=np.int32) if bc_type is not None
+          else np.zeros((nf, 3), np.int32)) if nf else None
+    bv = (np.ascontiguousarray(bc_val, dtype=np.float64) if bc_val is not None
+          else np.zeros((nf, 3, 3))) if nf else None
+    ct = np.zeros((3, c.size))
+    ct_rhs, dml, gml = np.zeros(n), np.zeros(n), np.zeros(n)
+    st = lib().orc_assemble_divergence_p1(nd.shape[0], _p(nd), _p(X), n, _p(f), _p(c), quad_degree,
+                                          int(bool(by_parts)), nf, _p(fa), _p(fe), _p(ty), _p(bv), _p(ct),
+                                          _p(ct_rhs), _p(dml), _p(gml))
+    assert st == 0, st
+    return ct, ct_rhs, dml, gml
+
+
+def sparsity_secondorder(findrm, colm):
+    """(findrm int64, colm int32) of make_sparsity_transpose (Sparsity_Patterns.F90:87-148)."""
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    n = f.size - 1
+    lib().orc_sparsity_secondorder.restype = C.c_int64
+    of = np.zeros(n + 1, dtype=np.int64)
+    nnz = lib().orc_sparsity_secondorder(n, _p(f), _p(c), _p(of), None, 0)
+    oc = np.zeros(nnz, dtype=np.int32)
+    lib().orc_sparsity_secondorder(n, _p(f), _p(c), _p(of), _p(oc), nnz)
+    return of, oc
+
+
+def mult_div_vector_div_T(findrm, colm, a, w, b, pf, pc):
+    """mult_div_vector_div_T (Sparse_Matrices_Fields.F90:590-671); a, b: (ndim, nnz); w: (ncols, ndim)."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    ndim = a.shape[0]
+    out = np.zeros(len(pc))
+    lib().orc_mult_div_vector_div_T(len(findrm) - 1, ndim, _p(np.ascontiguousarray(findrm, dtype=np.int64)),
+                                    _p(np.ascontiguousarray(colm, dtype=np.int32)), _p(a),
+                                    _p(np.ascontiguousarray(w, dtype=np.float64)),
+                                    _p(np.ascontiguousarray(b, dtype=np.float64)),
+                                    _p(np.ascontiguousarray(pf, dtype=np.int64)),
+                                    _p(np.ascontiguousarray(pc, dtype=np.int32)), _p(out))
+    return out
+
+
+def mult_div_invscalar_div_T(findrm, colm, a, s, b, pf, pc):
+    """mult_div_invscalar_div_T (Sparse_Matrices_Fields.F90:673-748), a and b on one pattern."""
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    out = np.zeros(len(pc))
+    lib().orc_mult_div_invscalar_div_T(len(f) - 1, _p(f), _p(c), _p(np.ascontiguousarray(a, dtype=np.float64)),
+                                       _p(np.ascontiguousarray(s, dtype=np.float64)), _p(f), _p(c),
+                                       _p(np.ascontiguousarray(b, dtype=np.float64)),
+                                       _p(np.ascontiguousarray(pf, dtype=np.int64)),
+                                       _p(np.ascontiguousarray(pc, dtype=np.int32)), _p(out))
+    return out
+
+
+def simplex_tensor(X):
+    """simplex_tensor (Metric_tools.F90:852-941) of one simplex; X is (dim+1, dim)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    dim = X.shape[1]
+    m = np.zeros((dim, dim))
+    lib().orc_simplex_tensor(dim, _p(X), _p(m))
+    return m
+
+
+def edge_length_metric(m):
+    """edge_length_from_eigenvalue_metric (Metric_tools.F90:157-164)."""
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    out = np.zeros_like(m)
+    lib().orc_edge_length_metric(m.shape[0], _p(m), _p(out))
+    return out
+
+
+def assemble_kmk(ndglno, coords, findrm, colm, p_masslump, so_findrm, so_colm, theta_pg=1.0, quad_degree=2):
+    """(kt, kmk) -- assemble_kmk_matrix (Momentum_CG.F90:2707-2766)."""
+    nd = np.ascontiguousarray(ndglno, dtype=np.int32)
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    kt = np.zeros(c.size)
+    kmk = np.zeros(len(so_colm))
+    st = lib().orc_assemble_kmk(nd.shape[0], _p(nd), _p(np.ascontiguousarray(coords, dtype=np.float64)),
+                                f.size - 1, _p(f), _p(c), quad_degree, C.c_double(theta_pg),
+                                _p(np.ascontiguousarray(p_masslump, dtype=np.float64)),
+                                _p(np.ascontiguousarray(so_findrm, dtype=np.int64)),
+                                _p(np.ascontiguousarray(so_colm, dtype=np.int32)), _p(kt), _p(kmk))
+    assert st == 0, st
+    return kt, kmk
+
+
+def _block(findrm, colm, v):
+    import scipy.sparse as sp
+    n = len(findrm) - 1
+    return sp.csr_matrix((v, np.asarray(colm), np.asarray(findrm)), shape=(n, n))
+
+
+def masslumped_poisson_rhs(findrm, colm, ctp, mom_rhs, ct_rhs, inverse_masslump, velocity, dt, theta_pg):
+    """assemble_masslumped_poisson_rhs (Momentum_CG.F90:2670-2705); vector fields are (N, 3)."""
+    lm = mom_rhs * inverse_masslump + velocity * (1.0 / dt / theta_pg)
+    y = np.zeros(len(findrm) - 1)
+    for d in range(3):
+        y += _block(findrm, colm, ctp[d]) @ lm[:, d]
+    return -y + ct_rhs * (1.0 / dt / theta_pg)
+
+
+def correct_masslumped_velocity(findrm, colm, ct, inverse_masslump, delta_p, velocity):
+    """correct_masslumped_velocity (Momentum_CG.F90:2544-2575): u += M_l^-1 C^T dp."""
+    u = np.array(velocity, dtype=np.float64)
+    for d in range(3):
+        u[:, d] += (_block(findrm, colm, ct[d]).T @ delta_p) * inverse_masslump[:, d]
+    return u

@@ -14,7 +14,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared_symbols():
     txt = open(HEADER).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(fl_[a-z0-9_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(fl_[A-Za-z0-9_]+)\s*\(", txt)))
 
 
 def test_header_and_binding_agree():

@@ -1,0 +1,109 @@
+"""CPU oracle of the pressure-projection pieces, pinned against the
+reference's known answers and exact identities (no GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from fluidity_gb300 import meshgen as M
+from oracle import oracle as O
+
+
+@pytest.fixture(scope="module")
+def mesh4():
+    nd, X = M.cube_mesh(4)
+    f, c, _ = O.make_sparsity(nd)
+    return nd, X, f, c
+
+
+def test_simplex_tensor_known_answer():
+    # error_measures/tests/test_simplex_tensor.F90: tests/data/triangle.1 has
+    # vertices (0, 0.5), (0, -0.5), (1, 0) and the metric diag(0.75, 1)
+    m = O.simplex_tensor(np.array([[0.0, 0.5], [0.0, -0.5], [1.0, 0.0]]))
+    assert np.allclose(m, [[0.75, 0.0], [0.0, 1.0]], rtol=0, atol=4 * np.finfo(float).eps)
+
+
+def test_simplex_tensor_unit_edges(mesh4):
+    # error_measures/tests/test_simplex_tensor_edgelens.F90: in the metric every
+    # edge has unit length (tolerance 201 epsilon)
+    nd, X, _, _ = mesh4
+    for e in range(0, len(nd), 7):
+        P = X[nd[e]]
+        m = O.simplex_tensor(P)
+        h = O.edge_length_metric(m)
+        for i in range(4):
+            for j in range(i + 1, 4):
+                d = P[j] - P[i]
+                assert abs(np.sqrt(d @ m @ d) - 1.0) < 201 * np.finfo(float).eps
+        assert np.abs(h @ m @ h - np.eye(3)).max() < 1e-13
+
+
+def test_lumped_mass_is_the_volume(mesh4):
+    nd, X, f, c = mesh4
+    ml = O.lumped_mass(nd, nd, X, len(X))
+    assert abs(ml.sum() - 1.0) < 1e-14
+    assert (ml > 0).all()
+
+
+def test_divergence_by_parts_identity(mesh4):
+    # integral(N_i dN_j/dx) = -integral(dN_i/dx N_j) + surface integral(N_i N_j n)
+    nd, X, f, c = mesh4
+    ct, _, dml, gml = O.assemble_divergence_p1(nd, X, f, c)
+    faces, fe = M.boundary_faces(nd)
+    ct2, rhs2, _, _ = O.assemble_divergence_p1(nd, X, f, c, by_parts=True, faces=faces, face_ele=fe)
+    assert np.abs(ct - ct2).max() < 1e-15 * 1e3 * np.abs(ct).max()
+    assert np.array_equal(dml, gml)
+    assert not rhs2.any()
+    # divergence of a constant field is zero away from the boundary
+    bn = M.boundary_nodes(X)
+    inner = np.setdiff1d(np.arange(len(X)), bn)
+    for d in range(3):
+        A = sp.csr_matrix((ct[d], c, f), shape=(len(X),) * 2)
+        assert np.abs((A @ np.ones(len(X)))[inner]).max() < 1e-16
+
+
+def test_divergence_surface_types(mesh4):
+    # weak Dirichlet moves the face term to ct_rhs; types 2-4 drop the face
+    nd, X, f, c = mesh4
+    faces, fe = M.boundary_faces(nd)
+    nf = len(faces)
+    ty0 = np.zeros((nf, 3), np.int32)
+    ct0, _, _, _ = O.assemble_divergence_p1(nd, X, f, c, by_parts=True, faces=faces, face_ele=fe, bc_type=ty0)
+    ty = ty0.copy()
+    ty[:, 0] = 1
+    g = np.random.default_rng(3).random((nf, 3, 3))
+    ct1, rhs1, _, _ = O.assemble_divergence_p1(nd, X, f, c, by_parts=True, faces=faces, face_ele=fe, bc_type=ty,
+                                               bc_val=g)
+    ctn, _, _, _ = O.assemble_divergence_p1(nd, X, f, c, by_parts=True)
+    # dimension 0 lost its face terms, the others kept them
+    assert np.abs(ct1[0] - ctn[0]).max() < 1e-17
+    assert np.abs(ct1[1:] - ct0[1:]).max() == 0.0
+    assert np.abs(rhs1).max() > 0.0
+
+
+def test_secondorder_pattern_is_the_structural_square(mesh4):
+    nd, X, f, c = mesh4
+    sf, sc = O.sparsity_secondorder(f, c)
+    A = sp.csr_matrix((np.ones(len(c)), c, f), shape=(len(X),) * 2)
+    B = (A @ A).tocsr()
+    B.sort_indices()
+    assert np.array_equal(B.indptr, sf) and np.array_equal(B.indices, sc)
+
+
+def test_row_products_match_the_triple_product(mesh4):
+    nd, X, f, c = mesh4
+    N = len(X)
+    ct, _, _, _ = O.assemble_divergence_p1(nd, X, f, c)
+    sf, sc = O.sparsity_secondorder(f, c)
+    w = np.random.default_rng(1).random((N, 3)) + 0.5
+    cmc = O.mult_div_vector_div_T(f, c, ct, w, ct, sf, sc)
+    blk = [sp.csr_matrix((ct[d], c, f), shape=(N, N)) for d in range(3)]
+    ref = sum(blk[d] @ sp.diags(w[:, d]) @ blk[d].T for d in range(3))
+    assert abs(sp.csr_matrix((cmc, sc, sf), shape=(N, N)) - ref).max() < 1e-15 * abs(ref).max()
+    ml = O.lumped_mass(nd, nd, X, N)
+    for theta in (1.0, 0.6):
+        kt, kmk = O.assemble_kmk(nd, X, f, c, ml, sf, sc, theta_pg=theta)
+        K = sp.csr_matrix((kt, c, f), shape=(N, N))
+        assert abs(K - K.T).max() < 1e-16
+        ref = K @ sp.diags(1.0 / (theta * ml)) @ K.T
+        got = sp.csr_matrix((kmk, sc, sf), shape=(N, N))
+        assert abs(got - ref).max() < 1e-13 * abs(ref).max()
