@@ -195,6 +195,9 @@ struct fl_mesh_t {
   fl::DevBuf<fl::ErrWord> err;       // 1 word
   fl::DevBuf<int32_t> tpos;          // per entry (k, j): position of (j, k) (built on first use)
   struct fl_mesh_t* so_parent = nullptr;  // second-order pattern handles: the mesh they square
+  fl::DevBuf<float2> bt;                  // second-order handles: transposed product operand
+  fl::DevBuf<int32_t> pair_off;           // second-order handles: pairs of each first-order entry
+  fl::DevBuf<uint8_t> pair_map;           // second-order handles: output slot of every pair
   fl::DevBuf<int32_t> face_cnt, face_ptr, face_list;  // node -> surface faces (divergence surface terms)
   fl::DevBuf<double> em;             // element matrices + rhs (coefficient-major scratch)
   // staging buffers of the host-pointer entry points (grow-only)

@@ -37,10 +37,12 @@
 //   k_so_rows    second-order pattern: one warp per row gathers the rows of
 //                its neighbours, sorts them bitonically in shared memory and
 //                keeps the distinct columns.
+//   k_bt_gather  b transposed along the pattern rows (through tpos), as
+//                double-float pairs: the product's loads of b are coalesced.
 //   k_rowprod    out(i,j) = sum_k sum_d a_d(i,k) w_d(k) b_d(j,k): one warp per
-//                output row, the row's columns and FP64 accumulators in shared
-//                memory; the two half-warps take two k at a time and add in
-//                a fixed order, so every sum is deterministic.
+//                output row, the row's columns and double-float accumulators
+//                in shared memory; the two half-warps take two k at a time and
+//                add in a fixed order, so every sum is deterministic.
 //   k_kmk_elem   FP64 P1 pressure-diffusion element matrix
 //                0.5 V grad N^T h_bar grad N with h_bar the element's edge-
 //                length tensor (closed form below); summed by the assembly's
@@ -451,117 +453,250 @@ __global__ void __launch_bounds__(kSoWarps * 32) k_so_rows(int32_t N, const int3
   }
 }
 
-constexpr int kPW = 8;      // warps per block of the product kernel
-constexpr int kPCap = 256;  // longest output row held in shared memory
+constexpr int kPW = 8;      // warps per block of the product kernel (two rows per warp)
+constexpr int kPCap = 192;  // longest output row held in shared memory
+
+// bt[d][r] = b_d(j, k) for the entry r = (k, j) of row k: B transposed along
+// the pattern's rows (a gather through tpos), as double-float pairs, so that
+// the product reads it with coalesced loads.
+template <int NDIM>
+__global__ void k_bt_gather(int64_t nnz, const int32_t* __restrict__ tpos, const double* __restrict__ b0,
+                            const double* __restrict__ b1, const double* __restrict__ b2, float2* __restrict__ bt) {
+  note_launch();
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nnz; r += (int64_t)gridDim.x * blockDim.x) {
+    const int t = __ldg(tpos + r);
+    const double* b[3] = {b0, b1, b2};
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+      const df x = df_from_double(__ldg(b[d] + t));
+      bt[d * nnz + r] = make_float2(x.hi, x.lo);
+    }
+  }
+}
+
+// Slot map of the row products: for the entry q = (i, k) of the first-order
+// pattern and the t-th entry (k, j) of row k, the position of j in output row
+// i, one byte per pair at pmap[poff[q] + t] (output rows hold at most kPCap
+// entries).  Built once per second-order pattern.
+__global__ void k_pair_count(int32_t N, const int32_t* __restrict__ fr, const int32_t* __restrict__ cm,
+                             int32_t* __restrict__ cnt) {
+  note_launch();
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < fr[N]; q += gridDim.x * blockDim.x) {
+    const int k = cm[q];
+    cnt[q] = fr[k + 1] - fr[k];
+  }
+}
+
+__global__ void k_pair_map(int32_t N, const int32_t* __restrict__ fr, const int32_t* __restrict__ cm,
+                           const int32_t* __restrict__ optr, const int32_t* __restrict__ ocol,
+                           const int32_t* __restrict__ poff, uint8_t* __restrict__ pmap, ErrWord* err) {
+  note_launch();
+  const int lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < N; i += nw) {
+    const int ob = optr[i], L = optr[i + 1] - ob;
+    if (L > kPCap) {
+      if (lane == 0) set_err(err, FL_ERR_UNSUPPORTED, i);
+      continue;
+    }
+    for (int q = fr[i]; q < fr[i + 1]; ++q) {
+      const int k = cm[q], kb = fr[k], len = fr[k + 1] - kb;
+      for (int t = lane; t < len; t += 32) {
+        const int j = cm[kb + t];
+        int lo = 0, hi = L;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (ocol[ob + mid] < j) lo = mid + 1;
+          else hi = mid;
+        }
+        if (lo >= L || ocol[ob + lo] != j) set_err(err, FL_ERR_OUTSIDE_PATTERN, i);
+        pmap[(int64_t)poff[q] + t] = (uint8_t)(lo < L ? lo : 0);
+      }
+    }
+  }
+}
 
 struct RowProdArgs {
   int32_t n;
+  int64_t annz;
   const int32_t* aptr;
   const int32_t* acol;
-  const int32_t* tpos;
   const int32_t* optr;
-  const int32_t* ocol;
+  const int32_t* poff;   // per first-order entry (i, k): start of its pairs in pmap
+  const uint8_t* pmap;   // output slot of every pair
   const double* a[3];
-  const double* b[3];
-  const double* w;  // NDIM values per node; the divisor s when DIV
-  double theta;     // DIV: the divisor is theta * s unless scale == 0
+  const float2* bt;  // NDIM blocks of annz pairs
+  const double* w;   // NDIM values per node; the divisor s when DIV
+  double theta;      // DIV: the divisor is theta * s when scale != 0
   int scale;
   double* out;
   ErrWord* err;
 };
 
+// Double-float arithmetic on the FP32 pipes (GB300's FP64 rate is 1/60 of
+// FP32).  One half-warp per output row i (two rows per warp): the lanes first
+// load the row's k data (column k, c_d = a_d(i,k) w_d(k) or a(i,k) / s(k),
+// the extent of row k) in one round, then walk the k in ascending order with
+// the next k's operand loads issued before the current k is summed; a lane
+// owns one entry (k, j) of row k, adds c . bt(k, j) to the slot of j in the
+// output row (shared memory, double-float), and the k are added one after
+// the other, so every sum has a fixed order.  Rows of more than 16 entries
+// take their k in groups of 16, and so do columns longer than 16.
 template <int NDIM, bool DIV>
-__global__ void __launch_bounds__(kPW * 32) k_rowprod(RowProdArgs P) {
+__global__ void __launch_bounds__(kPW * 32, 4) k_rowprod(RowProdArgs P) {
   note_launch();
-  __shared__ int32_t s_col_all[kPW][kPCap];
-  __shared__ double s_acc_all[kPW][kPCap];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
-  int32_t* s_col = s_col_all[w];
-  double* s_acc = s_acc_all[w];
-  for (int row = blockIdx.x * kPW + w; row < P.n; row += gridDim.x * kPW) {
-    const int ob = __ldg(P.optr + row), L = __ldg(P.optr + row + 1) - ob;
-    if (L > kPCap) {
-      if (lane == 0) set_err(P.err, FL_ERR_UNSUPPORTED, row);
-      __syncwarp();
-      continue;
+  __shared__ float2 s_acc_all[2 * kPW][kPCap];
+  const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+  const int hw = (threadIdx.x >> 5) * 2 + half;  // half-warp index in the block
+  float2* s_acc = s_acc_all[hw];
+  const int nrow_steps = (P.n + 2 * kPW * gridDim.x - 1) / (2 * kPW * gridDim.x);
+  for (int it = 0; it < nrow_steps; ++it) {
+    const int row = (it * gridDim.x + blockIdx.x) * 2 * kPW + hw;
+    const bool live = row < P.n;
+    int ob = 0, L = 0, qb = 0, qe = 0;
+    if (live) {
+      ob = __ldg(P.optr + row);
+      L = __ldg(P.optr + row + 1) - ob;
+      qb = __ldg(P.aptr + row);
+      qe = __ldg(P.aptr + row + 1);
     }
-    for (int t = lane; t < L; t += 32) {
-      s_col[t] = __ldg(P.ocol + ob + t);
-      s_acc[t] = 0.0;
+    if (L > kPCap) {  // the map build rejects such patterns
+      L = 0;
+      qe = qb;
     }
+    for (int t = hl; t < L; t += 16) s_acc[t] = make_float2(0.0f, 0.0f);
     __syncwarp();
-    const int qb = __ldg(P.aptr + row), qe = __ldg(P.aptr + row + 1);
-    for (int q0 = qb; q0 < qe; q0 += 2) {
-      const int q = q0 + half;
-      const bool act = q < qe;
-      int kb = 0, ke = 0;
-      double c[NDIM];
+    // both halves run the same number of k steps (the longer row's)
+    const int nk = qe - qb;
+    const int nk_max = max(nk, __shfl_xor_sync(0xffffffffu, nk, 16));
+    for (int g0 = 0; g0 < nk_max; g0 += 16) {
+      // this group's k data, one k per lane
+      const int qg = qb + g0 + hl;
+      const bool kact = qg < qe;
+      int kb = 0, klen = 0, po = 0;
+      df c[NDIM];
 #pragma unroll
-      for (int d = 0; d < NDIM; ++d) c[d] = 0.0;
-      if (act) {
-        const int k = __ldg(P.acol + q);
+      for (int d = 0; d < NDIM; ++d) c[d] = {0.0f, 0.0f};
+      if (kact) {
+        const int k = __ldg(P.acol + qg);
         kb = __ldg(P.aptr + k);
-        ke = __ldg(P.aptr + k + 1);
+        klen = __ldg(P.aptr + k + 1) - kb;
+        po = __ldg(P.poff + qg);
         if (DIV) {
           double sk = __ldg(P.w + k);
           if (P.scale) sk = sk * P.theta;
-          c[0] = __ldg(P.a[0] + q) / sk;
+          c[0] = df_mul(df_from_double(__ldg(P.a[0] + qg)), df_rcp(df_from_double(sk)));
         } else {
 #pragma unroll
-          for (int d = 0; d < NDIM; ++d) c[d] = __ldg(P.a[d] + q) * __ldg(P.w + NDIM * k + d);
+          for (int d = 0; d < NDIM; ++d)
+            c[d] = df_mul(df_from_double(__ldg(P.a[d] + qg)), df_from_double(__ldg(P.w + NDIM * k + d)));
         }
       }
-      const int len = ke - kb;
-      const int mlen = max(len, __shfl_xor_sync(0xffffffffu, len, 16));
-      for (int c0 = 0; c0 < mlen; c0 += 16) {
-        const int r = kb + c0 + hl;
-        bool has = act && r < ke;
-        double v = 0.0;
-        int slot = 0;
-        if (has) {
-          const int j = __ldg(P.acol + r);
-          const int tp = __ldg(P.tpos + r);
-          v = c[0] * __ldg(P.b[0] + tp);
+      const int gn = min(16, nk_max - g0);
+      // operand loads of step u: lane hl takes entry hl (+16 m) of column k_u
+      int u_kb = __shfl_sync(0xffffffffu, kb, 0, 16), u_len = __shfl_sync(0xffffffffu, klen, 0, 16);
+      int u_po = __shfl_sync(0xffffffffu, po, 0, 16);
+      int nslot = 0;
+      float2 nb[NDIM];
 #pragma unroll
-          for (int d = 1; d < NDIM; ++d) v = fma(c[d], __ldg(P.b[d] + tp), v);
-          int lo = 0, hi = L;
-          while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (s_col[mid] < j) lo = mid + 1;
-            else hi = mid;
-          }
-          slot = lo;
-          if (slot >= L || s_col[slot] != j) {
-            set_err(P.err, FL_ERR_OUTSIDE_PATTERN, row);
-            has = false;
+      for (int d = 0; d < NDIM; ++d) nb[d] = make_float2(0.0f, 0.0f);
+      if (hl < u_len) {
+        nslot = __ldg(P.pmap + u_po + hl);
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) nb[d] = __ldg(P.bt + d * P.annz + u_kb + hl);
+      }
+      for (int u = 0; u < gn; ++u) {
+        const int slot = nslot;
+        float2 b[NDIM];
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) b[d] = nb[d];
+        const int len = u_len, kbu = u_kb, pou = u_po;
+        df cu[NDIM];
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+          cu[d].hi = __shfl_sync(0xffffffffu, c[d].hi, u, 16);
+          cu[d].lo = __shfl_sync(0xffffffffu, c[d].lo, u, 16);
+        }
+        // issue the next step's loads before this step's arithmetic
+        if (u + 1 < gn) {
+          u_kb = __shfl_sync(0xffffffffu, kb, u + 1, 16);
+          u_len = __shfl_sync(0xffffffffu, klen, u + 1, 16);
+          u_po = __shfl_sync(0xffffffffu, po, u + 1, 16);
+          if (hl < u_len) {
+            nslot = __ldg(P.pmap + u_po + hl);
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) nb[d] = __ldg(P.bt + d * P.annz + u_kb + hl);
           }
         }
-        if (half == 0 && has) s_acc[slot] += v;
-        __syncwarp();
-        if (half == 1 && has) s_acc[slot] += v;
+        for (int m0 = 0; m0 < len; m0 += 16) {
+          int sl = slot;
+          float2 bb[NDIM];
+#pragma unroll
+          for (int d = 0; d < NDIM; ++d) bb[d] = b[d];
+          if (m0 > 0 && m0 + hl < len) {  // columns longer than 16: the further entries
+            sl = __ldg(P.pmap + pou + m0 + hl);
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) bb[d] = __ldg(P.bt + d * P.annz + kbu + m0 + hl);
+          }
+          if (m0 + hl < len) {
+            df v;
+            if (NDIM == 3)
+              v = df_dot3(cu[0], {bb[0].x, bb[0].y}, cu[NDIM > 1 ? 1 : 0], {bb[NDIM > 1 ? 1 : 0].x, bb[NDIM > 1 ? 1 : 0].y},
+                          cu[NDIM > 2 ? 2 : 0], {bb[NDIM > 2 ? 2 : 0].x, bb[NDIM > 2 ? 2 : 0].y});
+            else {
+              v = df_mul(cu[0], {bb[0].x, bb[0].y});
+#pragma unroll
+              for (int d = 1; d < NDIM; ++d) v = df_add(v, df_mul(cu[d], {bb[d].x, bb[d].y}));
+            }
+            const float2 o = s_acc[sl];
+            const df sum = df_add({o.x, o.y}, v);
+            s_acc[sl] = make_float2(sum.hi, sum.lo);
+          }
+        }
         __syncwarp();
       }
     }
-    for (int t = lane; t < L; t += 32) P.out[ob + t] = s_acc[t];
+    for (int t = hl; t < L; t += 16) {
+      const float2 o = s_acc[t];
+      P.out[ob + t] = df_to_double({o.x, o.y});
+    }
     __syncwarp();
   }
 }
 
 // ------------------------------------------------------------------- KMK --
-// Largest eigenvalue of a symmetric 3x3 matrix (m00, m01, m02, m11, m12, m22)
-// by the trigonometric solution of its characteristic cubic.
-__device__ __forceinline__ double lmax_sym3(const double* m) {
-  const double q = (m[0] + m[3] + m[5]) / 3.0;
-  const double p1 = m[1] * m[1] + m[2] * m[2] + m[4] * m[4];
-  const double d0 = m[0] - q, d1 = m[3] - q, d2 = m[5] - q;
-  const double p2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * p1;
-  if (!(p2 > 0.0)) return q;
-  const double p = sqrt(p2 / 6.0);
-  const double ip = 1.0 / p;
-  const double b0 = d0 * ip, b1 = m[1] * ip, b2 = m[2] * ip, b3 = d1 * ip, b4 = m[4] * ip, b5 = d2 * ip;
-  double r = 0.5 * (b0 * (b3 * b5 - b4 * b4) - b1 * (b1 * b5 - b4 * b2) + b2 * (b1 * b4 - b3 * b2));
-  r = fmin(1.0, fmax(-1.0, r));
-  return q + 2.0 * p * cos(acos(r) / 3.0);
+// Largest eigenvalue of a symmetric 3x3 matrix (m00, m01, m02, m11, m12, m22):
+// the trigonometric solution of the characteristic cubic in FP32, then one
+// FP64 Newton step on det(m - l I) = 0 (skipped when the step is not small,
+// i.e. at a nearly repeated root, where the products below only see the
+// eigenvalues through symmetric functions that a split error leaves
+// unchanged to first order).
+__device__ __forceinline__ double lmax_sym3(const double* m, double det_m) {
+  const float f0 = (float)m[0], f1 = (float)m[1], f2 = (float)m[2], f3 = (float)m[3], f4 = (float)m[4],
+              f5 = (float)m[5];
+  const float q = (f0 + f3 + f5) * (1.0f / 3.0f);
+  const float p1 = f1 * f1 + f2 * f2 + f4 * f4;
+  const float d0 = f0 - q, d1 = f3 - q, d2 = f5 - q;
+  const float p2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0f * p1;
+  float l = q;
+  if (p2 > 0.0f) {
+    const float p = sqrtf(p2 * (1.0f / 6.0f));
+    const float ip = 1.0f / p;
+    const float b0 = d0 * ip, b1 = f1 * ip, b2 = f2 * ip, b3 = d1 * ip, b4 = f4 * ip, b5 = d2 * ip;
+    float r = 0.5f * (b0 * (b3 * b5 - b4 * b4) - b1 * (b1 * b5 - b4 * b2) + b2 * (b1 * b4 - b3 * b2));
+    r = fminf(1.0f, fmaxf(-1.0f, r));
+    l = q + 2.0f * p * __cosf(acosf(r) * (1.0f / 3.0f));
+  }
+  const double i1 = m[0] + m[3] + m[5];
+  const double i2 = m[0] * m[3] - m[1] * m[1] + m[0] * m[5] - m[2] * m[2] + m[3] * m[5] - m[4] * m[4];
+  double x = (double)l;
+  const double f = ((x - i1) * x + i2) * x - det_m;
+  const double fp = (3.0 * x - 2.0 * i1) * x + i2;
+  if (fp != 0.0) {
+    const double st = f / fp;
+    if (fabs(st) < 1e-4 * fabs(x)) x -= st;
+  }
+  return x;
 }
 
 struct KmkArgs {
@@ -626,8 +761,9 @@ __global__ void __launch_bounds__(128) k_kmk_elem(KmkArgs A) {
       W[k] = 2.0 * (J[r][0] * J[s][0] + J[r][1] * J[s][1] + J[r][2] * J[s][2]) - 0.5 * j1[r] * j1[s];
       M[k] = im * (g[0][r] * g[0][s] + g[1][r] * g[1][s] + g[2][r] * g[2][s] + g[3][r] * g[3][s]);
     }
-    const double l1 = lmax_sym3(W), l3 = 1.0 / lmax_sym3(M);
-    const double l2 = 2.0 * det * det / (l1 * l3);
+    const double d2 = 2.0 * det * det;  // det W; det m = 1 / det W
+    const double l1 = lmax_sym3(W, d2), l3 = 1.0 / lmax_sym3(M, 1.0 / d2);
+    const double l2 = d2 / (l1 * l3);
     const double s1 = sqrt(l1), s2 = sqrt(l2), s3 = sqrt(l3);
     const double i1 = s1 + s2 + s3, i2 = s1 * s2 + s2 * s3 + s1 * s3, i3 = s1 * s2 * s3;
     const double cw = i1 * i1 - i2, ci = i1 * i3, den = 1.0 / (i1 * i2 - i3);
@@ -810,6 +946,23 @@ extern "C" int fl_gpu_secondorder_register(fl_mesh mesh, fl_mesh* out) {
       st = FL_ERR_CUDA;
       break;
     }
+    // slot map of the row products
+    const int64_t annz = mesh->nnz;
+    DevBuf<int32_t> pc;
+    if ((st = pc.reserve((size_t)annz + 1)) || (st = h->pair_off.reserve((size_t)annz + 1))) break;
+    k_pair_count<<<grid_for(annz, kT), kT, 0, s>>>(N, mesh->findrm.p, mesh->colm.p, pc.p);
+    if ((st = exclusive_scan_i32(pc.p, h->pair_off.p, annz, s)) != FL_OK) break;
+    int32_t npairs = 0;
+    if (cudaMemcpyAsync(&npairs, h->pair_off.p + annz, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      set_error("pair count read-back failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    if ((st = h->pair_map.reserve((size_t)std::max(npairs, 1)))) break;
+    k_pair_map<<<(unsigned)std::max(1, std::min((N + 7) / 8, num_sms() * 8)), 256, 0, s>>>(
+        N, mesh->findrm.p, mesh->colm.p, h->findrm.p, h->colm.p, h->pair_off.p, h->pair_map.p, h->err.p);
+    if ((st = check_err(h->err.p, s, "second-order row longer than the product's shared-memory row")) != FL_OK) break;
   } while (0);
   if (st != FL_OK) {
     fl_gpu_mesh_destroy(h);
@@ -863,29 +1016,41 @@ extern "C" int fl_dev_lumped_mass(fl_mesh m, double* lumped_mass, void* stream) 
 static int rowprod_launch(fl_mesh prod, int ndim, bool div, const double* const a[3], const double* w,
                           const double* const b[3], double theta, int scale, double* out, cudaStream_t s) {
   fl_mesh_t* par = prod->so_parent;
+  const int64_t annz = par->nnz;
+  FL_TRY(prod->bt.reserve((size_t)ndim * annz));
+  const unsigned gb = grid_for(annz, kT);
+  if (ndim == 1) k_bt_gather<1><<<gb, kT, 0, s>>>(annz, par->tpos.p, b[0], nullptr, nullptr, prod->bt.p);
+  else if (ndim == 2) k_bt_gather<2><<<gb, kT, 0, s>>>(annz, par->tpos.p, b[0], b[1], nullptr, prod->bt.p);
+  else k_bt_gather<3><<<gb, kT, 0, s>>>(annz, par->tpos.p, b[0], b[1], b[2], prod->bt.p);
   RowProdArgs P{};
   P.n = prod->N;
+  P.annz = annz;
   P.aptr = par->findrm.p;
   P.acol = par->colm.p;
-  P.tpos = par->tpos.p;
   P.optr = prod->findrm.p;
-  P.ocol = prod->colm.p;
-  for (int d = 0; d < 3; ++d) {
-    P.a[d] = d < ndim ? a[d] : nullptr;
-    P.b[d] = d < ndim ? b[d] : nullptr;
-  }
+  P.poff = prod->pair_off.p;
+  P.pmap = prod->pair_map.p;
+  for (int d = 0; d < 3; ++d) P.a[d] = d < ndim ? a[d] : nullptr;
+  P.bt = prod->bt.p;
   P.w = w;
   P.theta = theta;
   P.scale = scale;
   P.out = out;
   P.err = prod->err.p;
-  const unsigned g = (unsigned)std::max(1, std::min((P.n + kPW - 1) / kPW, num_sms() * 8));
-  if (div) k_rowprod<1, true><<<g, kPW * 32, 0, s>>>(P);
-  else if (ndim == 1) k_rowprod<1, false><<<g, kPW * 32, 0, s>>>(P);
-  else if (ndim == 2) k_rowprod<2, false><<<g, kPW * 32, 0, s>>>(P);
-  else k_rowprod<3, false><<<g, kPW * 32, 0, s>>>(P);
+  // one resident wave: blocks per SM from the occupancy of the instance
+  auto launch = [&](auto kern) -> int {
+    int per_sm = 0;
+    FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPW * 32, 0));
+    const unsigned g = (unsigned)std::max(1, std::min((P.n + 2 * kPW - 1) / (2 * kPW), num_sms() * std::max(1, per_sm)));
+    kern<<<g, kPW * 32, 0, s>>>(P);
+    return FL_OK;
+  };
+  if (div) FL_TRY(launch(k_rowprod<1, true>));
+  else if (ndim == 1) FL_TRY(launch(k_rowprod<1, false>));
+  else if (ndim == 2) FL_TRY(launch(k_rowprod<2, false>));
+  else FL_TRY(launch(k_rowprod<3, false>));
   FL_TRY_CUDA(cudaGetLastError());
-  return check_err(prod->err.p, s, "row product: output row longer than the shared-memory row or outside the pattern");
+  return FL_OK;
 }
 
 static int check_product(fl_mesh prod) {
