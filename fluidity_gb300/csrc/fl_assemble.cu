@@ -386,16 +386,22 @@ struct DfArgs {
 
 // Specialised on the term set (consistent mass, source, old field t,
 // diagonal kappa) so that each instance carries only its own work.
-// The records of a warp's 32 consecutive elements are one contiguous 6 kB
-// chunk: each thread stages its 12 float4 in shared memory and the warp
-// writes the chunk with coalesced 16-byte stores (blockDim/32 x 6 kB of
+// Element record: four row slices, slice a = {K_a0, K_a1 | K_a2, r_a} as
+// double-float pairs (32 B, one sector), plus {ms, 0} with a mass term (48
+// B), where ms = |detJ| (m0 + 3 m1) is the row sum of the element mass
+// matrix: K_a3 = ms - (K_a0 + K_a1 + K_a2) because the stiffness rows sum to
+// zero.  The records of a warp's 32 consecutive elements are one contiguous
+// chunk: each thread stages its float4s in shared memory and the warp writes
+// the chunk with coalesced 16-byte stores (blockDim/32 x 4 or 6 kB of
 // dynamic shared memory).
 template <bool MASS, bool SRC, bool TF, bool ANISO>
 __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   note_launch();
   extern __shared__ float4 stage_all[];
   const int lane = threadIdx.x & 31;
-  float4* stage = stage_all + (threadIdx.x >> 5) * 384;
+  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
+  constexpr int NREC = 4 * SL;      // float4 per element record
+  float4* stage = stage_all + (threadIdx.x >> 5) * (32 * NREC);
   for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
     const int e = base + lane;
     if (e < A.E) {
@@ -482,20 +488,29 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
         r[i] = df_sub(r[i], df_mul(s, rs));
       }
     }
-    // row-slice records: element e, local row i -> {K_i0, K_i1, K_i2, K_i3, r_i, 0}
-    float4* rec = stage + lane * 12;
+    float4* rec = stage + lane * NREC;
+    df ms = {0.0f, 0.0f};
+    if (MASS) ms = df_add(madet0, df_add(madet1, df_add(madet1, madet1)));
+    // row 3 (b < 3) as the row pass rebuilds column 3 of rows 0..2, so that
+    // K_3b and K_b3 are the same double-float value (an exactly symmetric matrix)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      df k3 = df_neg(df_add(df_add(K[b][0], K[b][1]), K[b][2]));
+      if (MASS) k3 = df_add(k3, ms);
+      K[3][b] = k3;
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      rec[3 * i + 0] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
-      rec[3 * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, K[i][3].hi, K[i][3].lo);
-      rec[3 * i + 2] = make_float4(r[i].hi, r[i].lo, 0.0f, 0.0f);
+      rec[SL * i + 0] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
+      rec[SL * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, r[i].hi, r[i].lo);
+      if (MASS) rec[SL * i + 2] = make_float4(ms.hi, ms.lo, 0.0f, 0.0f);
     }
     }
     __syncwarp();
-    float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * 12u;
-    const int nvalid = min(32, A.E - base) * 12;
+    float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
+    const int nvalid = min(32, A.E - base) * NREC;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) {
+    for (int k = 0; k < NREC; ++k) {
       const int idx = k * 32 + lane;
       if (idx < nvalid) out[idx] = stage[idx];
     }
@@ -661,12 +676,15 @@ struct PullArgs {
   ErrWord* err;
 };
 
-// Double-float version of the row pass: element values are (hi, lo) float
-// pairs; each row accumulates in double-float (shared memory, or in val for
-// rows longer than RMAX) and converts every entry to double once.
-template <int THREADS, int RMAX>
+// Double-float version of the row pass over the P1 element records: the
+// slice of (element, local row a) gives K_a0..K_a2 and r_a, and K_a3 is the
+// row's mass sum minus their sum; each row accumulates in double-float
+// (shared memory, or in val for rows longer than RMAX) and converts every
+// entry to double once.
+template <int THREADS, int RMAX, bool MASS>
 __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
   note_launch();
+  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
   extern __shared__ unsigned char smem_raw[];
   float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
   const float4* rec = reinterpret_cast<const float4*>(P.em);
@@ -693,36 +711,35 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
         inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
         pw[u] = ok ? __ldg(P.ne_pos + q0 + u) : 0u;
       }
-      float4 q[4][3];
+      float4 q[4][SL];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        // record of (element, local row) = inc>>4, inc&15: index 3*(4e + a)
-        const uint32_t ri = 3u * (uint32_t)(((inc[u] >> 4) << 2) | (inc[u] & 15));
-        if (q0 + u < ie) {
-          q[u][0] = __ldg(rec + ri);
-          q[u][1] = __ldg(rec + ri + 1);
-          q[u][2] = __ldg(rec + ri + 2);
-        } else {
-          q[u][0] = q[u][1] = q[u][2] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+        // slice of (element, local row) = inc>>4, inc&15
+        const uint32_t ri = (uint32_t)SL * (uint32_t)(((inc[u] >> 4) << 2) | (inc[u] & 15));
+#pragma unroll
+        for (int k = 0; k < SL; ++k) q[u][k] = q0 + u < ie ? __ldg(rec + ri + k) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (q0 + u >= ie) break;
-        const float2 v2[4] = {make_float2(q[u][0].x, q[u][0].y), make_float2(q[u][0].z, q[u][0].w),
-                              make_float2(q[u][1].x, q[u][1].y), make_float2(q[u][1].z, q[u][1].w)};
+        df v[4];
+        v[0] = {q[u][0].x, q[u][0].y};
+        v[1] = {q[u][0].z, q[u][0].w};
+        v[2] = {q[u][1].x, q[u][1].y};
+        v[3] = df_neg(df_add(df_add(v[0], v[1]), v[2]));
+        if (MASS) v[3] = df_add(v[3], {q[u][SL - 1].x, q[u][SL - 1].y});
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
           const int pos = (pw[u] >> (8 * b)) & 0xffu;
           if (in_smem) {
             const float2 c = acc[pos * THREADS + t];
-            const df sum = df_add({c.x, c.y}, {v2[b].x, v2[b].y});
+            const df sum = df_add({c.x, c.y}, v[b]);
             acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
           } else {
-            P.val[base + pos] += df_to_double({v2[b].x, v2[b].y});
+            P.val[base + pos] += df_to_double(v[b]);
           }
         }
-        r = df_add(r, {q[u][2].x, q[u][2].y});
+        r = df_add(r, {q[u][1].z, q[u][1].w});
       }
     }
     if (in_smem)
@@ -812,17 +829,17 @@ static int launch_pull_df10(const PullArgs& P, cudaStream_t s) {
   return FL_OK;
 }
 
-template <int THREADS, int RMAX>
+template <int THREADS, int RMAX, bool MASS>
 static int launch_pull_df(const PullArgs& P, cudaStream_t s) {
   const size_t smem = (size_t)RMAX * THREADS * sizeof(float2);
   static bool configured = false;
   if (!configured) {
-    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df<THREADS, RMAX>,
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df<THREADS, RMAX, MASS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = true;
   }
   const unsigned grid = (unsigned)((P.N + THREADS - 1) / THREADS);
-  k_rows_pull_df<THREADS, RMAX><<<grid, THREADS, smem, s>>>(P);
+  k_rows_pull_df<THREADS, RMAX, MASS><<<grid, THREADS, smem, s>>>(P);
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
@@ -909,23 +926,28 @@ __global__ void k_dirichlet(int32_t nb, const int32_t* __restrict__ nodes, int32
 // are sized to the mesh's longest row; longer rows, if any, accumulate in
 // place in val.  Every row is summed by one thread in incidence order, so the
 // tile changes no result.
-static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int max_row, int tile, cudaStream_t s) {
+template <bool MASS>
+static int launch_rows_p1_df(const PullArgs& P, int max_row, int tile, cudaStream_t s) {
+  if (max_row <= 16) {
+    if (tile == 0) return launch_pull_df<64, 16, MASS>(P, s);
+    if (tile == 2) return launch_pull_df<256, 16, MASS>(P, s);
+    return launch_pull_df<128, 16, MASS>(P, s);
+  }
+  if (tile == 0) return launch_pull_df<64, 32, MASS>(P, s);
+  if (tile == 2) return launch_pull_df<256, 32, MASS>(P, s);
+  return launch_pull_df<128, 32, MASS>(P, s);
+}
+
+static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int max_row, int tile, cudaStream_t s,
+                       bool mass = false) {
   if (loc == 10 && use_df) {
     if (max_row > 72) return launch_pull_df10<32, 128>(P, s);
     if (tile == 0) return launch_pull_df10<32, 72>(P, s);
     if (tile == 2) return launch_pull_df10<128, 72>(P, s);
     return launch_pull_df10<64, 72>(P, s);
   }
-  if (loc == 4 && use_df) {
-    if (max_row <= 16) {
-      if (tile == 0) return launch_pull_df<64, 16>(P, s);
-      if (tile == 2) return launch_pull_df<256, 16>(P, s);
-      return launch_pull_df<128, 16>(P, s);
-    }
-    if (tile == 0) return launch_pull_df<64, 32>(P, s);
-    if (tile == 2) return launch_pull_df<256, 32>(P, s);
-    return launch_pull_df<128, 32>(P, s);
-  }
+  if (loc == 4 && use_df)
+    return mass ? launch_rows_p1_df<true>(P, max_row, tile, s) : launch_rows_p1_df<false>(P, max_row, tile, s);
   if (loc == 4 && closed) {
     if (tile == 0) return launch_pull<4, true, 64, 32>(P, s);
     if (tile == 2) return launch_pull<4, true, 256, 32>(P, s);
@@ -999,7 +1021,8 @@ static bool use_p2_df(const fl_mesh_t* m, const fl_advdif_params* p) {
 }
 
 // Element-record storage per element, in doubles (a double-float pair counts
-// as one): P1 closed form 24 (row slices of 6 pairs), P2 double-float 120 (row
+// as one): P1 closed form 24 (the double-float record is 16 or 24 pairs;
+// the FP64 form takes 14 coefficients), P2 double-float 120 (row
 // slices of 12 pairs), general forms LOC*(LOC+1) coefficient-major.
 size_t assembly_scratch_doubles(const fl_mesh_t* m, const fl_advdif_params* p) {
   const int ncoef = use_p1_closed_form(m, p) ? 24 : use_p2_df(m, p) ? 120 : m->loc * m->loc + m->loc;
@@ -1125,7 +1148,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     D.have_mass = p->have_mass;
     D.have_src = p->have_source;
     const unsigned g = grid_for(m->E, eb, esm);
-    const size_t smem = (size_t)(eb / 32) * 384 * sizeof(float4);  // 6 kB per warp
+    const size_t smem = (size_t)(eb / 32) * 32 * (p->have_mass ? 12 : 8) * sizeof(float4);  // 4 or 6 kB per warp
     const int key = (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
     switch (key) {
 #define FL_DF_CASE(K, M, S, T, AN) \
@@ -1150,7 +1173,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   FL_TRY_CUDA(cudaGetLastError());
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
              em, val, rhs, m->err.p};
-  FL_TRY(launch_rows(P, loc, use_df, closed, m->max_row, m->tile_rows, s));
+  FL_TRY(launch_rows(P, loc, use_df, closed, m->max_row, m->tile_rows, s, p->have_mass != 0));
   if (m->timing) {
     FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
     m->timed = true;

@@ -30,6 +30,10 @@ module fl_gpu_bindings
             fl_gpu_assemble_advdif_cg, fl_gpu_apply_dirichlet, fl_gpu_petsc_solve, &
             fl_gpu_pattern_register, fl_dev_petsc_solve, fl_amg_create, fl_amg_solve, fl_amg_destroy, &
             fl_batch_create, fl_batch_add, fl_batch_run, fl_batch_destroy, fl_set_assembly_tiles
+  public :: fl_divergence_params, fl_gpu_secondorder_register, fl_dev_assemble_divergence_cg, &
+            fl_dev_lumped_mass, fl_dev_mult_div_vector_div_T, fl_dev_mult_div_invscalar_div_T, &
+            fl_dev_assemble_kmk, fl_dev_masslumped_poisson_rhs, fl_dev_correct_masslumped_velocity, &
+            fl_dev_csr_addto
   public :: gpu_check
 
   integer(c_int), parameter, public :: FL_OK = 0
@@ -59,6 +63,12 @@ module fl_gpu_bindings
      integer(c_int32_t) :: max_its, start_from_zero, precision
      real(c_double) :: inner_rtol
   end type fl_solver_opts
+
+  ! assemble_divergence_matrix_cg options and surface mesh (by parts)
+  type, bind(c) :: fl_divergence_params
+     integer(c_int32_t) :: integrate_by_parts, nfaces, index_base, pad
+     type(c_ptr) :: faces, face_ele, bc_type, bc_val
+  end type fl_divergence_params
 
   type, bind(c) :: fl_solve_report
      integer(c_int32_t) :: iterations, reason
@@ -231,6 +241,78 @@ module fl_gpu_bindings
        integer(c_int32_t), value :: elem_block, elem_blocks_per_sm, row_tile
        integer(c_int) :: st
      end function fl_set_assembly_tiles
+
+     ! pressure projection, P1 pressure and P1 velocity on one mesh
+     ! (device pointers; block_csr_matrix blocks as c_loc of each block's val)
+     function fl_gpu_secondorder_register(handle, out) bind(c, name="fl_gpu_secondorder_register") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: handle
+       type(c_ptr), intent(out) :: out
+       integer(c_int) :: st
+     end function fl_gpu_secondorder_register
+
+     function fl_dev_assemble_divergence_cg(handle, params, ct_val, ct_rhs, div_mass_lumped, &
+          grad_mass_lumped, stream) bind(c, name="fl_dev_assemble_divergence_cg") result(st)
+       import :: c_int, c_ptr, fl_divergence_params
+       type(c_ptr), value :: handle, ct_rhs, div_mass_lumped, grad_mass_lumped, stream
+       type(fl_divergence_params), intent(in) :: params
+       type(c_ptr), intent(in) :: ct_val(3)
+       integer(c_int) :: st
+     end function fl_dev_assemble_divergence_cg
+
+     function fl_dev_lumped_mass(handle, lumped_mass, stream) bind(c, name="fl_dev_lumped_mass") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: handle, lumped_mass, stream
+       integer(c_int) :: st
+     end function fl_dev_lumped_mass
+
+     function fl_dev_mult_div_vector_div_T(product, ndim, a_val, w, b_val, out, stream) &
+          bind(c, name="fl_dev_mult_div_vector_div_T") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: product, w, out, stream
+       integer(c_int32_t), value :: ndim
+       type(c_ptr), intent(in) :: a_val(3), b_val(3)
+       integer(c_int) :: st
+     end function fl_dev_mult_div_vector_div_T
+
+     function fl_dev_mult_div_invscalar_div_T(product, a_val, s_val, b_val, out, stream) &
+          bind(c, name="fl_dev_mult_div_invscalar_div_T") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: product, a_val, s_val, b_val, out, stream
+       integer(c_int) :: st
+     end function fl_dev_mult_div_invscalar_div_T
+
+     function fl_dev_assemble_kmk(handle, product, theta_pg, p_masslump, kt_val, kmk_val, stream) &
+          bind(c, name="fl_dev_assemble_kmk") result(st)
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: handle, product, p_masslump, kt_val, kmk_val, stream
+       real(c_double), value :: theta_pg
+       integer(c_int) :: st
+     end function fl_dev_assemble_kmk
+
+     function fl_dev_masslumped_poisson_rhs(handle, ctp_val, mom_rhs, ct_rhs, inverse_masslump, velocity, &
+          dt, theta_pg, poisson_rhs, stream) bind(c, name="fl_dev_masslumped_poisson_rhs") result(st)
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: handle, mom_rhs, ct_rhs, inverse_masslump, velocity, poisson_rhs, stream
+       type(c_ptr), intent(in) :: ctp_val(3)
+       real(c_double), value :: dt, theta_pg
+       integer(c_int) :: st
+     end function fl_dev_masslumped_poisson_rhs
+
+     function fl_dev_correct_masslumped_velocity(handle, ct_val, inverse_masslump, delta_p, velocity, stream) &
+          bind(c, name="fl_dev_correct_masslumped_velocity") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: handle, inverse_masslump, delta_p, velocity, stream
+       type(c_ptr), intent(in) :: ct_val(3)
+       integer(c_int) :: st
+     end function fl_dev_correct_masslumped_velocity
+
+     function fl_dev_csr_addto(pattern, val, other, scale, stream) bind(c, name="fl_dev_csr_addto") result(st)
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: pattern, val, other, stream
+       real(c_double), value :: scale
+       integer(c_int) :: st
+     end function fl_dev_csr_addto
   end interface
 
 contains
