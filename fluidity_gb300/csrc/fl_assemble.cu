@@ -23,6 +23,7 @@
 // same Lagrange basis (femtools/Shape_Functions.F90:128-329).  The regrouping
 // is exact in real arithmetic; results agree with the reference loops to
 // rounding.
+#include <climits>
 #include <cmath>
 #include <algorithm>
 #include <cstring>
@@ -394,6 +395,112 @@ struct DfArgs {
 // chunk: each thread stages its float4s in shared memory and the warp writes
 // the chunk with coalesced 16-byte stores (blockDim/32 x 4 or 6 kB of
 // dynamic shared memory).
+//
+// One element of the P1 double-float pass: its record (4 row slices) into rec.
+template <bool MASS, bool SRC, bool TF, bool ANISO>
+__device__ __forceinline__ void p1_df_element(const DfArgs& A, int e, float4* rec) {
+  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
+  const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+  const int vi[4] = {v.x, v.y, v.z, v.w};
+  double x[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+  df J[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
+  df cof[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+      cof[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
+    }
+  const df det = df_dot3(J[0][0], cof[0][0], J[1][0], cof[1][0], J[2][0], cof[2][0]);
+  const df adet = df_abs(det);
+  const df rdet = df_rcp(adet);
+  // gradient directions c_i = column i of cof; kappa applied to the second factor
+  df kc[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) kc[i][a] = ANISO ? df_mul(A.kdiag[a], cof[a][i]) : cof[a][i];
+  df G[4][4];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      G[i][j] = df_dot3(cof[0][i], kc[j][0], cof[1][i], kc[j][1], cof[2][i], kc[j][2]);
+      G[j][i] = G[i][j];
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    G[i][3] = df_neg(df_add(df_add(G[i][0], G[i][1]), G[i][2]));
+    G[3][i] = G[i][3];
+  }
+  G[3][3] = df_neg(df_add(df_add(G[0][3], G[1][3]), G[2][3]));
+  const df ks = df_mul(A.kscale, rdet);
+  df madet0 = {0.0f, 0.0f}, madet1 = {0.0f, 0.0f};
+  if (MASS) {
+    madet0 = df_mul(adet, A.m0);
+    madet1 = df_mul(adet, A.m1);
+  }
+  df K[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i; j < 4; ++j) {
+      df m = df_mul(G[i][j], ks);
+      if (MASS) m = df_add(m, i == j ? madet0 : madet1);
+      K[i][j] = m;
+      K[j][i] = m;
+    }
+  const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
+  const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
+  df r[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+  if (SRC) {
+    df fe[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) fe[i] = df_from_double(__ldg(A.f + tn[i]));
+    const df fsum = df_add(df_add(fe[0], fe[1]), df_add(fe[2], fe[3]));
+    const df q1 = df_mul(df_mul(adet, A.m1), fsum);
+    const df q2 = df_mul(adet, df_sub(A.m0, A.m1));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) r[i] = df_add(q1, df_mul(q2, fe[i]));
+  }
+  if (TF) {
+    df te[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) te[i] = df_from_double(__ldg(A.t + tn[i]));
+    const df rs = df_mul(A.rscale, rdet);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      df s = df_add(df_dot3(G[i][0], te[0], G[i][1], te[1], G[i][2], te[2]), df_mul(G[i][3], te[3]));
+      r[i] = df_sub(r[i], df_mul(s, rs));
+    }
+  }
+  df ms = {0.0f, 0.0f};
+  if (MASS) ms = df_add(madet0, df_add(madet1, df_add(madet1, madet1)));
+  // row 3 (b < 3) as the row pass rebuilds column 3 of rows 0..2, so that
+  // K_3b and K_b3 are the same double-float value (an exactly symmetric matrix)
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    df k3 = df_neg(df_add(df_add(K[b][0], K[b][1]), K[b][2]));
+    if (MASS) k3 = df_add(k3, ms);
+    K[3][b] = k3;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    rec[SL * i + 0] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
+    rec[SL * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, r[i].hi, r[i].lo);
+    if (MASS) rec[SL * i + 2] = make_float4(ms.hi, ms.lo, 0.0f, 0.0f);
+  }
+}
+
 template <bool MASS, bool SRC, bool TF, bool ANISO>
 __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   note_launch();
@@ -404,108 +511,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   float4* stage = stage_all + (threadIdx.x >> 5) * (32 * NREC);
   for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
     const int e = base + lane;
-    if (e < A.E) {
-    const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
-    const int vi[4] = {v.x, v.y, v.z, v.w};
-    double x[4][3];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
-    df J[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
-    df cof[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-        cof[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
-      }
-    const df det = df_dot3(J[0][0], cof[0][0], J[1][0], cof[1][0], J[2][0], cof[2][0]);
-    const df adet = df_abs(det);
-    const df rdet = df_rcp(adet);
-    // gradient directions c_i = column i of cof; kappa applied to the second factor
-    df kc[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int a = 0; a < 3; ++a) kc[i][a] = ANISO ? df_mul(A.kdiag[a], cof[a][i]) : cof[a][i];
-    df G[4][4];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = i; j < 3; ++j) {
-        G[i][j] = df_dot3(cof[0][i], kc[j][0], cof[1][i], kc[j][1], cof[2][i], kc[j][2]);
-        G[j][i] = G[i][j];
-      }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      G[i][3] = df_neg(df_add(df_add(G[i][0], G[i][1]), G[i][2]));
-      G[3][i] = G[i][3];
-    }
-    G[3][3] = df_neg(df_add(df_add(G[0][3], G[1][3]), G[2][3]));
-    const df ks = df_mul(A.kscale, rdet);
-    df madet0 = {0.0f, 0.0f}, madet1 = {0.0f, 0.0f};
-    if (MASS) {
-      madet0 = df_mul(adet, A.m0);
-      madet1 = df_mul(adet, A.m1);
-    }
-    df K[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = i; j < 4; ++j) {
-        df m = df_mul(G[i][j], ks);
-        if (MASS) m = df_add(m, i == j ? madet0 : madet1);
-        K[i][j] = m;
-        K[j][i] = m;
-      }
-    const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
-    const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
-    df r[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-    if (SRC) {
-      df fe[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) fe[i] = df_from_double(__ldg(A.f + tn[i]));
-      const df fsum = df_add(df_add(fe[0], fe[1]), df_add(fe[2], fe[3]));
-      const df q1 = df_mul(df_mul(adet, A.m1), fsum);
-      const df q2 = df_mul(adet, df_sub(A.m0, A.m1));
-#pragma unroll
-      for (int i = 0; i < 4; ++i) r[i] = df_add(q1, df_mul(q2, fe[i]));
-    }
-    if (TF) {
-      df te[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) te[i] = df_from_double(__ldg(A.t + tn[i]));
-      const df rs = df_mul(A.rscale, rdet);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        df s = df_add(df_dot3(G[i][0], te[0], G[i][1], te[1], G[i][2], te[2]), df_mul(G[i][3], te[3]));
-        r[i] = df_sub(r[i], df_mul(s, rs));
-      }
-    }
-    float4* rec = stage + lane * NREC;
-    df ms = {0.0f, 0.0f};
-    if (MASS) ms = df_add(madet0, df_add(madet1, df_add(madet1, madet1)));
-    // row 3 (b < 3) as the row pass rebuilds column 3 of rows 0..2, so that
-    // K_3b and K_b3 are the same double-float value (an exactly symmetric matrix)
-#pragma unroll
-    for (int b = 0; b < 3; ++b) {
-      df k3 = df_neg(df_add(df_add(K[b][0], K[b][1]), K[b][2]));
-      if (MASS) k3 = df_add(k3, ms);
-      K[3][b] = k3;
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      rec[SL * i + 0] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
-      rec[SL * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, r[i].hi, r[i].lo);
-      if (MASS) rec[SL * i + 2] = make_float4(ms.hi, ms.lo, 0.0f, 0.0f);
-    }
-    }
+    if (e < A.E) p1_df_element<MASS, SRC, TF, ANISO>(A, e, stage + lane * NREC);
     __syncwarp();
     float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
     const int nvalid = min(32, A.E - base) * NREC;
@@ -666,6 +672,7 @@ struct PullArgs {
   int32_t N, E;
   const int32_t* ne_ptr;
   const int32_t* ne_col;
+  const int32_t* ne_rec;  // fused P1 pass: record slice of every ne_col incidence
   const uint32_t* ne_pos;
   const int32_t* nd;
   const int32_t* findrm;
@@ -681,74 +688,314 @@ struct PullArgs {
 // row's mass sum minus their sum; each row accumulates in double-float
 // (shared memory, or in val for rows longer than RMAX) and converts every
 // entry to double once.
+// One row of the P1 double-float row pass.  FUSED: the record slice of each
+// incidence comes from P.ne_rec (records in element-item order) and is read
+// through L2 (written by other blocks of the same kernel); otherwise it is
+// (element, local row) of P.ne_col.
+template <int THREADS, int RMAX, bool MASS, bool FUSED>
+__device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, float2* acc, int t) {
+  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
+  const float4* rec = reinterpret_cast<const float4*>(P.em);
+  const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
+  const bool in_smem = L <= RMAX;
+  if (in_smem) {
+    for (int k = 0; k < L; ++k) acc[k * THREADS + t] = make_float2(0.0f, 0.0f);
+  } else {
+    for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
+  }
+  df r = {0.0f, 0.0f};
+  const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
+  // incidences in groups of four: all index and record loads of a group are
+  // issued before any accumulation (memory-level parallelism); the adds run
+  // in the group's order, so the colour order of the sum is kept
+  for (int q0 = ib; q0 < ie; q0 += 4) {
+    int inc[4];
+    uint32_t pw[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool ok = q0 + u < ie;
+      inc[u] = ok ? __ldg((FUSED ? P.ne_rec : P.ne_col) + q0 + u) : 0;
+      pw[u] = ok ? __ldg(P.ne_pos + q0 + u) : 0u;
+    }
+    float4 q[4][SL];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t slice = FUSED ? (uint32_t)inc[u] : (uint32_t)(((inc[u] >> 4) << 2) | (inc[u] & 15));
+      const uint32_t ri = (uint32_t)SL * slice;
+#pragma unroll
+      for (int k = 0; k < SL; ++k) {
+        if (q0 + u < ie) q[u][k] = FUSED ? __ldcg(rec + ri + k) : __ldg(rec + ri + k);
+        else q[u][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (q0 + u >= ie) break;
+      df v[4];
+      v[0] = {q[u][0].x, q[u][0].y};
+      v[1] = {q[u][0].z, q[u][0].w};
+      v[2] = {q[u][1].x, q[u][1].y};
+      v[3] = df_neg(df_add(df_add(v[0], v[1]), v[2]));
+      if (MASS) v[3] = df_add(v[3], {q[u][SL - 1].x, q[u][SL - 1].y});
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int pos = (pw[u] >> (8 * b)) & 0xffu;
+        if (in_smem) {
+          const float2 c = acc[pos * THREADS + t];
+          const df sum = df_add({c.x, c.y}, v[b]);
+          acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
+        } else {
+          P.val[base + pos] += df_to_double(v[b]);
+        }
+      }
+      r = df_add(r, {q[u][1].z, q[u][1].w});
+    }
+  }
+  if (in_smem)
+    for (int k = 0; k < L; ++k) {
+      const float2 c = acc[k * THREADS + t];
+      P.val[base + k] = df_to_double({c.x, c.y});
+    }
+  P.rhs[row] = df_to_double(r);
+}
+
 template <int THREADS, int RMAX, bool MASS>
 __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
   note_launch();
-  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
   extern __shared__ unsigned char smem_raw[];
   float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
-  const float4* rec = reinterpret_cast<const float4*>(P.em);
-  const int t = threadIdx.x;
-  for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
-    const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
-    const bool in_smem = L <= RMAX;
-    if (in_smem) {
-      for (int k = 0; k < L; ++k) acc[k * THREADS + t] = make_float2(0.0f, 0.0f);
+  for (int row = blockIdx.x * THREADS + threadIdx.x; row < P.N; row += gridDim.x * THREADS)
+    p1_df_row<THREADS, RMAX, MASS, false>(P, row, acc, threadIdx.x);
+}
+
+// ----------------------------------------- fused P1 element and row pass --
+// One persistent kernel over a work queue of element items (256 elements in
+// the order of their highest field node, one per thread) and row items (256
+// rows).  Element items are counted done per group of kFzGroup items; a row
+// item waits, with a bounded spin, until the groups holding the element items
+// of its incidences are complete (threadfence + atomic add on one side,
+// acquire loads on the other), then sums its rows exactly as the row pass
+// does, in colour order: the result is bit-identical to the two kernels.
+// Row items follow the element items they need at a distance of about one
+// resident wave, so the records they read were written moments earlier and
+// are still in L2 (read with ld.global.cg: other SMs wrote them during this
+// kernel).  Every group a row item waits for holds only items dequeued before
+// it by running blocks, so the queue always drains; a wait that runs out sets
+// FL_ERR_TIMEOUT.
+struct FusedArgs {
+  int32_t nitems;
+  int32_t ne;            // element items
+  const int32_t* items;  // k >= 0: element item k; -(j+1): row item j
+  const int32_t* perm;   // elements by (highest field node, element id)
+  const int32_t* need;   // per row item: [first, last] element item it reads
+  int32_t* gdone;        // per group of kFzGroup element items: items done
+  int32_t* ctl;          // [0] queue head
+  ErrWord* err;
+};
+constexpr int kFzItem = 256;             // elements or rows per item = threads per block
+constexpr int kFzGroup = 64;             // element items per completion counter
+constexpr unsigned kFzSpin = 1u << 22;   // polls of one counter before giving up
+
+template <bool MASS, bool SRC, bool TF, bool ANISO>
+__global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, FusedArgs F) {
+  note_launch();
+  extern __shared__ float4 fz_smem[];
+  constexpr int SL = MASS ? 3 : 2, NREC = 4 * SL;
+  __shared__ int s_item;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  float4* stage = fz_smem + w * (32 * NREC);
+  float2* acc = reinterpret_cast<float2*>(fz_smem);  // [16][kFzItem]
+  for (;;) {
+    if (t == 0) s_item = atomicAdd(F.ctl, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= F.nitems) break;
+    const int code = __ldg(F.items + it);
+    if (code >= 0) {
+      const int base = code * kFzItem + w * 32;  // this warp's 32 consecutive positions
+      if (base < A.E) {
+        const int pp = base + lane;
+        if (pp < A.E) p1_df_element<MASS, SRC, TF, ANISO>(A, __ldg(F.perm + pp), stage + lane * NREC);
+        __syncwarp();
+        float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
+        const int nvalid = min(32, A.E - base) * NREC;
+#pragma unroll
+        for (int k = 0; k < NREC; ++k) {
+          const int idx = k * 32 + lane;
+          if (idx < nvalid) out[idx] = stage[idx];
+        }
+      }
+      __syncthreads();
+      if (t == 0) {
+        __threadfence();
+        atomicAdd(F.gdone + code / kFzGroup, 1);
+      }
     } else {
-      for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
-    }
-    df r = {0.0f, 0.0f};
-    const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
-    // incidences in groups of four: all index and record loads of a group are
-    // issued before any accumulation (memory-level parallelism); the adds run
-    // in the group's order, so the colour order of the sum is kept
-    for (int q0 = ib; q0 < ie; q0 += 4) {
-      int inc[4];
-      uint32_t pw[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const bool ok = q0 + u < ie;
-        inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
-        pw[u] = ok ? __ldg(P.ne_pos + q0 + u) : 0u;
-      }
-      float4 q[4][SL];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        // slice of (element, local row) = inc>>4, inc&15
-        const uint32_t ri = (uint32_t)SL * (uint32_t)(((inc[u] >> 4) << 2) | (inc[u] & 15));
-#pragma unroll
-        for (int k = 0; k < SL; ++k) q[u][k] = q0 + u < ie ? __ldg(rec + ri + k) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        if (q0 + u >= ie) break;
-        df v[4];
-        v[0] = {q[u][0].x, q[u][0].y};
-        v[1] = {q[u][0].z, q[u][0].w};
-        v[2] = {q[u][1].x, q[u][1].y};
-        v[3] = df_neg(df_add(df_add(v[0], v[1]), v[2]));
-        if (MASS) v[3] = df_add(v[3], {q[u][SL - 1].x, q[u][SL - 1].y});
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const int pos = (pw[u] >> (8 * b)) & 0xffu;
-          if (in_smem) {
-            const float2 c = acc[pos * THREADS + t];
-            const df sum = df_add({c.x, c.y}, v[b]);
-            acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
-          } else {
-            P.val[base + pos] += df_to_double(v[b]);
+      const int j = -code - 1;
+      if (t == 0) {
+        const int first = __ldg(F.need + 2 * j), last = __ldg(F.need + 2 * j + 1);
+        unsigned spins = 0;
+        for (int g = first / kFzGroup; last >= 0 && g <= last / kFzGroup; ++g) {
+          const int target = min(kFzGroup, F.ne - g * kFzGroup);
+          while (ld_acquire(F.gdone + g) < target) {
+            if (++spins > kFzSpin) break;
+            __nanosleep(64);
+          }
+          if (spins > kFzSpin) {
+            set_err(F.err, FL_ERR_TIMEOUT, j);
+            break;
           }
         }
-        r = df_add(r, {q[u][1].z, q[u][1].w});
       }
+      __syncthreads();
+      const int row = j * kFzItem + t;
+      if (row < P.N) p1_df_row<kFzItem, 16, MASS, true>(P, row, acc, t);
     }
-    if (in_smem)
-      for (int k = 0; k < L; ++k) {
-        const float2 c = acc[k * THREADS + t];
-        P.val[base + k] = df_to_double({c.x, c.y});
-      }
-    P.rhs[row] = df_to_double(r);
+    __syncthreads();
   }
+}
+
+// Plan of the fused pass (once per mesh): element order, record slice of
+// every incidence, the row items' needs and the queue.
+__global__ void k_fz_maxv(int32_t E, const int32_t* __restrict__ nd, int32_t* __restrict__ maxv) {
+  note_launch();
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+    const int4 v = reinterpret_cast<const int4*>(nd)[e];
+    maxv[e] = max(max(v.x, v.y), max(v.z, v.w));
+  }
+}
+
+// pass 0: count the elements whose highest node is v; pass 1: place them in
+// ascending element order (the incidence list of v is ascending)
+__global__ void k_fz_place(int32_t N, const int32_t* __restrict__ ne_ptr, const int32_t* __restrict__ ne,
+                           const int32_t* __restrict__ maxv, int32_t* __restrict__ cnt,
+                           const int32_t* __restrict__ off, int32_t* __restrict__ perm, int32_t* __restrict__ pos,
+                           int pass) {
+  note_launch();
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x) {
+    int c = 0;
+    for (int q = ne_ptr[v]; q < ne_ptr[v + 1]; ++q) {
+      const int e = ne[q] >> 4;
+      if (maxv[e] != v) continue;
+      if (pass) {
+        perm[off[v] + c] = e;
+        pos[e] = off[v] + c;
+      }
+      ++c;
+    }
+    if (!pass) cnt[v] = c;
+  }
+}
+
+__global__ void k_fz_rec(int32_t N, const int32_t* __restrict__ ne_ptr, const int32_t* __restrict__ ne_col,
+                         const int32_t* __restrict__ pos, int32_t* __restrict__ rec, int32_t* __restrict__ rowrange) {
+  note_launch();
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N; v += gridDim.x * blockDim.x) {
+    int mx = -1, mn = INT_MAX;
+    for (int q = ne_ptr[v]; q < ne_ptr[v + 1]; ++q) {
+      const int inc = ne_col[q];
+      const int p = pos[inc >> 4];
+      rec[q] = 4 * p + (inc & 15);
+      mx = max(mx, p);
+      mn = min(mn, p);
+    }
+    rowrange[2 * v] = mn;
+    rowrange[2 * v + 1] = mx;
+  }
+}
+
+static int fused_plan(fl_mesh_t* m, cudaStream_t s) {
+  if (m->fz_state != 0) return FL_OK;
+  m->fz_state = -1;
+  const int N = m->N, E = m->E;
+  const int64_t ninc = (int64_t)4 * E;
+  DevBuf<int32_t> maxv, cnt, off, pos, rowmax;
+  FL_TRY(maxv.reserve(E));
+  FL_TRY(cnt.reserve((size_t)N + 1));
+  FL_TRY(off.reserve((size_t)N + 1));
+  FL_TRY(pos.reserve(E));
+  FL_TRY(rowmax.reserve((size_t)2 * N));
+  FL_TRY(m->fz_perm.reserve(E));
+  FL_TRY(m->fz_rec.reserve((size_t)ninc));
+  k_fz_maxv<<<grid_for(E, 256), 256, 0, s>>>(E, m->ndglno.p, maxv.p);
+  k_fz_place<<<grid_for(N, 256), 256, 0, s>>>(N, m->ne_ptr.p, m->ne.p, maxv.p, cnt.p, nullptr, nullptr, nullptr, 0);
+  FL_TRY(exclusive_scan_i32(cnt.p, off.p, N, s));
+  k_fz_place<<<grid_for(N, 256), 256, 0, s>>>(N, m->ne_ptr.p, m->ne.p, maxv.p, nullptr, off.p, m->fz_perm.p, pos.p,
+                                              1);
+  k_fz_rec<<<grid_for(N, 256), 256, 0, s>>>(N, m->ne_ptr.p, m->ne_col.p, pos.p, m->fz_rec.p, rowmax.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  std::vector<int32_t> hmax((size_t)2 * N);
+  int32_t placed = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(hmax.data(), rowmax.p, sizeof(int32_t) * 2 * N, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(&placed, off.p + N, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  if (placed != E) {
+    set_error("fused pass plan: %d of %d elements placed", placed, E);
+    return FL_ERR_ARG;
+  }
+  const int nE = (E + kFzItem - 1) / kFzItem, nR = (N + kFzItem - 1) / kFzItem;
+  // need[j] = number of element items up to the last one row item j reads;
+  // range[j] = its first and last element item (-1, -1 for rows without elements)
+  std::vector<int32_t> need(nR), order(nR), range((size_t)2 * nR);
+  for (int j = 0; j < nR; ++j) {
+    int mx = -1, mn = INT_MAX;
+    for (int i = j * kFzItem; i < std::min(N, (j + 1) * kFzItem); ++i) {
+      mx = std::max(mx, hmax[2 * i + 1]);
+      mn = std::min(mn, hmax[2 * i]);
+    }
+    need[j] = mx < 0 ? 0 : mx / kFzItem + 1;
+    range[2 * j] = mx < 0 ? -1 : mn / kFzItem;
+    range[2 * j + 1] = mx < 0 ? -1 : mx / kFzItem;
+    order[j] = j;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return need[a] < need[b]; });
+  // row items trail the element items they need by about three resident waves
+  // (at least a completion group, so a group a row item waits for was fully
+  // dequeued before it)
+  const int per_sm = 4;
+  const int lag = std::max(kFzGroup, 3 * num_sms() * per_sm);
+  std::vector<int32_t> items;
+  items.reserve((size_t)nE + nR);
+  size_t r = 0;
+  for (int k = 0; k < nE; ++k) {
+    items.push_back(k);
+    while (r < order.size() && need[order[r]] <= k + 1 - lag) items.push_back(-(order[r++] + 1));
+  }
+  while (r < order.size()) items.push_back(-(order[r++] + 1));
+  const int ng = (nE + kFzGroup - 1) / kFzGroup;
+  FL_TRY(m->fz_items.reserve(items.size()));
+  FL_TRY(m->fz_need.reserve((size_t)2 * nR));
+  FL_TRY(m->fz_ctl.reserve((size_t)1 + ng));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->fz_items.p, items.data(), sizeof(int32_t) * items.size(), cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->fz_need.p, range.data(), sizeof(int32_t) * 2 * nR, cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));  // host vectors and scratch are released on return
+  m->fz_nitems = (int32_t)items.size();
+  m->fz_state = 1;
+  return FL_OK;
+}
+
+template <bool MASS, bool SRC, bool TF, bool ANISO>
+static int launch_fused(fl_mesh_t* m, const DfArgs& D, const PullArgs& P, cudaStream_t s) {
+  constexpr int NREC = MASS ? 12 : 8;
+  const size_t smem = std::max((size_t)(kFzItem / 32) * 32 * NREC * sizeof(float4),
+                               (size_t)16 * kFzItem * sizeof(float2));
+  static bool configured = false;
+  if (!configured) {
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_asm_p1_fused<MASS, SRC, TF, ANISO>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  int per_sm = 0;
+  FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_asm_p1_fused<MASS, SRC, TF, ANISO>, kFzItem,
+                                                            smem));
+  const int ne = (m->E + kFzItem - 1) / kFzItem, ng = (ne + kFzGroup - 1) / kFzGroup;
+  // ctl[0] queue head, ctl[1..ng] group counters: zeroed per call
+  FusedArgs F{m->fz_nitems, ne, m->fz_items.p, m->fz_perm.p, m->fz_need.p, m->fz_ctl.p + 1, m->fz_ctl.p, m->err.p};
+  FL_TRY_CUDA(cudaMemsetAsync(m->fz_ctl.p, 0, sizeof(int32_t) * (1 + ng), s));
+  const unsigned g = (unsigned)std::max(1, std::min(m->fz_nitems, num_sms() * std::max(1, per_sm)));
+  k_asm_p1_fused<MASS, SRC, TF, ANISO><<<g, kFzItem, smem, s>>>(D, P, F);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
 }
 
 // Row pass of the P2 double-float records: slice (element, local row) =
@@ -965,7 +1212,7 @@ static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int
 
 int rows_p1_closed(fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s) {
   FL_CHECK_ARG(m && m->loc == 4 && m->E > 0, "a P1 mesh handle");
-  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
              em, val, rhs, m->err.p};
   return launch_rows(P, 4, false, true, m->max_row, m->tile_rows, s);
 }
@@ -1150,6 +1397,32 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     const unsigned g = grid_for(m->E, eb, esm);
     const size_t smem = (size_t)(eb / 32) * 32 * (p->have_mass ? 12 : 8) * sizeof(float4);  // 4 or 6 kB per warp
     const int key = (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
+    if (m->tile_rows == 3 && !em_override) {
+      // fused element + row pass (same sums, records kept in L2)
+      FL_TRY(fused_plan(m, s));
+      if (m->fz_state == 1) {
+        PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->fz_rec.p, m->ne_pos.p, m->ndglno.p, m->findrm.p,
+                   m->colm.p, em, val, rhs, m->err.p};
+        switch (key) {
+#define FL_FZ_CASE(K, M, S, T, AN) \
+  case K: FL_TRY((launch_fused<M, S, T, AN>(m, D, P, s))); break;
+          FL_FZ_CASE(0, false, false, false, false) FL_FZ_CASE(1, false, false, false, true)
+          FL_FZ_CASE(2, false, false, true, false) FL_FZ_CASE(3, false, false, true, true)
+          FL_FZ_CASE(4, false, true, false, false) FL_FZ_CASE(5, false, true, false, true)
+          FL_FZ_CASE(6, false, true, true, false) FL_FZ_CASE(7, false, true, true, true)
+          FL_FZ_CASE(8, true, false, false, false) FL_FZ_CASE(9, true, false, false, true)
+          FL_FZ_CASE(10, true, false, true, false) FL_FZ_CASE(11, true, false, true, true)
+          FL_FZ_CASE(12, true, true, false, false) FL_FZ_CASE(13, true, true, false, true)
+          FL_FZ_CASE(14, true, true, true, false) FL_FZ_CASE(15, true, true, true, true)
+#undef FL_FZ_CASE
+        }
+        if (m->timing) {
+          FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
+          m->timed = true;
+        }
+        return FL_OK;
+      }
+    }
     switch (key) {
 #define FL_DF_CASE(K, M, S, T, AN) \
   case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, smem, s>>>(D); break;
@@ -1171,7 +1444,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     k_asm_general<10><<<grid_for(m->E, 128, esm), 128, 0, s>>>(A);
   }
   FL_TRY_CUDA(cudaGetLastError());
-  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
              em, val, rhs, m->err.p};
   FL_TRY(launch_rows(P, loc, use_df, closed, m->max_row, m->tile_rows, s, p->have_mass != 0));
   if (m->timing) {
@@ -1231,7 +1504,8 @@ int autotune_assembly(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* 
     if (st != FL_OK) break;
     best = 1e30f;
     int br = m->tile_rows;
-    for (int r = 0; r < 3; ++r) {
+    const int nrt = (use_p1_closed_form(m, p) && diagonal_kappa(p)) ? 4 : 3;  // 3: fused P1 pass
+    for (int r = 0; r < nrt; ++r) {
       m->tile_rows = r;
       float ms = 0.f;
       if ((st = time_one(&ms)) != FL_OK) break;
@@ -1310,7 +1584,7 @@ extern "C" int fl_set_assembly_tiles(fl_mesh m, int32_t elem_block, int32_t elem
   FL_CHECK_ARG(m, "null mesh");
   FL_CHECK_ARG(elem_block == 128 || elem_block == 256, "element block 128 or 256");
   FL_CHECK_ARG(elem_blocks_per_sm >= 1 && elem_blocks_per_sm <= 64, "element blocks per SM 1..64");
-  FL_CHECK_ARG(row_tile >= 0 && row_tile <= 2, "row tile 0..2");
+  FL_CHECK_ARG(row_tile >= 0 && row_tile <= 3, "row tile 0..3 (3: fused P1 element and row pass)");
   m->tile_elem_block = elem_block;
   m->tile_elem_per_sm = elem_blocks_per_sm;
   m->tile_rows = row_tile;
@@ -1432,7 +1706,7 @@ extern "C" int fl_dev_assemble_p1_diffusion_noalloc(fl_mesh m, const fl_advdif_p
   A.have_src = p->have_source;
   k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
   FL_TRY_CUDA(cudaGetLastError());
-  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
              d->em, val, rhs, m->err.p};
   FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
   return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");

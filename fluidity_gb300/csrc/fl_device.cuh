@@ -28,6 +28,16 @@ __device__ __forceinline__ void st_relaxed(int* p, int v) {
   asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // First error wins; `where` records the element / row that raised it.
 __device__ __forceinline__ void set_err(ErrWord* err, int code, int where) {
   if (atomicCAS(&err->code, 0, code) == 0) err->where = where;

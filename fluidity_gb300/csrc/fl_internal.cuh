@@ -176,7 +176,7 @@ struct fl_mesh_t {
   // assembly tiles (set by the autotuner; results do not depend on them)
   int tile_elem_block = 256;  // threads per element-pass block
   int tile_elem_per_sm = 16;  // element-pass blocks per SM of the grid-stride grid
-  int tile_rows = 1;          // row-pass tile index (see launch_rows)
+  int tile_rows = 1;          // row-pass tile index (see launch_rows); 3: fused P1 pass
   bool tuned = false;
   cudaStream_t stream = nullptr;
 
@@ -194,6 +194,10 @@ struct fl_mesh_t {
   std::vector<int32_t> colour_ptr;   // ncolours+1 (host)
   fl::DevBuf<fl::ErrWord> err;       // 1 word
   fl::DevBuf<int32_t> tpos;          // per entry (k, j): position of (j, k) (built on first use)
+  // fused P1 element + row pass (built on first use)
+  int fz_state = 0;                  // 0 not built, 1 built, -1 not applicable
+  int32_t fz_nitems = 0;
+  fl::DevBuf<int32_t> fz_perm, fz_rec, fz_items, fz_need, fz_ctl;
   struct fl_mesh_t* so_parent = nullptr;  // second-order pattern handles: the mesh they square
   fl::DevBuf<float2> bt;                  // second-order handles: transposed product operand
   fl::DevBuf<int32_t> pair_off;           // second-order handles: pairs of each first-order entry

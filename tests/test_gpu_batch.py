@@ -141,9 +141,43 @@ def test_autotune_tiles_do_not_change_results(case):
     val0, rhs0 = ft.assemble_advection_diffusion_cg(m, p, **kw)
     val0, rhs0 = val0.clone(), rhs0.clone()
     val, rhs, tiles = ft.autotune_assembly(m, p, **kw)
-    assert tiles[0] in (128, 256) and tiles[1] in (4, 8, 16, 32) and tiles[2] in (0, 1, 2)
+    assert tiles[0] in (128, 256) and tiles[1] in (4, 8, 16, 32) and tiles[2] in (0, 1, 2, 3)
     assert torch.equal(val, val0) and torch.equal(rhs, rhs0)
-    for eb, esm, rt in ((128, 4, 0), (256, 32, 2), (128, 16, 1), (256, 8, 0)):
+    for eb, esm, rt in ((128, 4, 0), (256, 32, 2), (128, 16, 1), (256, 8, 0), (256, 16, 3)):
         ft.set_assembly_tiles(m, eb, esm, rt)
         v, r = ft.assemble_advection_diffusion_cg(m, p, **kw)
         assert torch.equal(v, val0) and torch.equal(r, rhs0), (eb, esm, rt)
+
+
+FUSED_CASES = {
+    "poisson": dict(diffusivity=1.0, have_source=True),
+    "aniso_mass_t": dict(diffusivity=[[1.0, 0, 0], [0, 1.0, 0], [0, 0, 1e-3]], have_source=True, have_mass=True,
+                         theta=0.5, dt=0.1),
+    "mass_t_only": dict(diffusivity=0.3, have_mass=True, theta=1.0, dt=0.05),
+}
+
+
+@pytest.mark.parametrize("n", [9, 40])
+@pytest.mark.parametrize("case", sorted(FUSED_CASES))
+def test_fused_p1_pass_is_bit_identical(n, case):
+    """The fused element + row pass (row tile 3) gives the two-kernel pass's
+    values and rhs bit for bit, on every call (the queue and the flags are
+    reset per call)."""
+    import torch
+    nd, X = M.cube_mesh(n)
+    m = ft.Mesh(nd, X)
+    kw0 = FUSED_CASES[case]
+    p = ft.advdif_params(quad_degree=2, **kw0)
+    kw = {}
+    if kw0.get("have_source"):
+        kw["source"] = torch.tensor(M.poisson_source(X), device="cuda")
+    if kw0.get("have_mass"):
+        kw["t"] = torch.tensor(M.gaussian_tracer(X), device="cuda")
+    ft.set_assembly_tiles(m, 256, 16, 1)
+    v0, r0 = ft.assemble_advection_diffusion_cg(m, p, **kw)
+    v0, r0 = v0.clone(), r0.clone()
+    ft.set_assembly_tiles(m, 256, 16, 3)
+    for _ in range(3):
+        v, r = ft.assemble_advection_diffusion_cg(m, p, **kw)
+        assert torch.equal(v, v0) and torch.equal(r, r0)
+    m.close()
