@@ -1210,6 +1210,13 @@ static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int
   return launch_pull<10, false, 64, 96>(P, s);
 }
 
+int rows_p1_df(fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s) {
+  FL_CHECK_ARG(m && m->loc == 4 && m->E > 0, "a P1 mesh handle");
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
+             em, val, rhs, m->err.p};
+  return launch_rows_p1_df<false>(P, m->max_row, m->tile_rows == 3 ? 1 : m->tile_rows, s);
+}
+
 int rows_p1_closed(fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s) {
   FL_CHECK_ARG(m && m->loc == 4 && m->E > 0, "a P1 mesh handle");
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,

@@ -149,6 +149,9 @@ int autotune_assembly(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl
 // Row pass of P1 FP64 element values in the symmetric coefficient-major layout
 // em[k*E + e] (ten matrix entries, then four rhs entries per element).
 int rows_p1_closed(struct ::fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s);
+// Row pass of P1 double-float row-slice records {K_a0, K_a1 | K_a2, r_a}
+// (K_a3 from the zero row sum), 32 B per (element, local row).
+int rows_p1_df(struct ::fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s);
 
 // Per-translation-unit launch counters and workspace release hooks.
 unsigned long long launches_mesh();

@@ -43,10 +43,11 @@
 //                output row, the row's columns and double-float accumulators
 //                in shared memory; the two half-warps take two k at a time and
 //                add in a fixed order, so every sum is deterministic.
-//   k_kmk_elem   FP64 P1 pressure-diffusion element matrix
+//   k_kmk_elem   P1 pressure-diffusion element matrix
 //                0.5 V grad N^T h_bar grad N with h_bar the element's edge-
-//                length tensor (closed form below); summed by the assembly's
-//                FP64 row pass.
+//                length tensor (closed form below), in double-float, written
+//                as the P1 assembly's row-slice records and summed by its
+//                double-float row pass.
 #include <algorithm>
 #include <cfloat>
 #include <climits>
@@ -665,15 +666,27 @@ __global__ void __launch_bounds__(kPW * 32, 4) k_rowprod(RowProdArgs P) {
 }
 
 // ------------------------------------------------------------------- KMK --
-// Largest eigenvalue of a symmetric 3x3 matrix (m00, m01, m02, m11, m12, m22):
-// the trigonometric solution of the characteristic cubic in FP32, then one
-// FP64 Newton step on det(m - l I) = 0 (skipped when the step is not small,
-// i.e. at a nearly repeated root, where the products below only see the
-// eigenvalues through symmetric functions that a split error leaves
-// unchanged to first order).
-__device__ __forceinline__ double lmax_sym3(const double* m, double det_m) {
-  const float f0 = (float)m[0], f1 = (float)m[1], f2 = (float)m[2], f3 = (float)m[3], f4 = (float)m[4],
-              f5 = (float)m[5];
+// Square root of a positive double-float: one Newton step from the FP32 root.
+__device__ __forceinline__ df df_sqrt(df x) {
+  const float s0 = sqrtf(x.hi);
+  const float p = s0 * s0;
+  const float pe = fmaf(s0, s0, -p);
+  const float res = ((x.hi - p) - pe) + x.lo;  // x - s0^2
+  return df_fast_two_sum(s0, res / (2.0f * s0));
+}
+
+__device__ __forceinline__ df df_scale(df x, float c) {  // exact for c a power of two only
+  return {x.hi * c, x.lo * c};
+}
+
+// Largest eigenvalue of a symmetric 3x3 double-float matrix (m00, m01, m02,
+// m11, m12, m22): the trigonometric solution of the characteristic cubic in
+// FP32, then one double-float Newton step on det(m - l I) = 0 (skipped when
+// the step is not small, i.e. at a nearly repeated root, where the products
+// below only see the eigenvalues through symmetric functions that a split
+// error leaves unchanged to first order).
+__device__ __forceinline__ df lmax_sym3(const df* m, df det_m) {
+  const float f0 = m[0].hi, f1 = m[1].hi, f2 = m[2].hi, f3 = m[3].hi, f4 = m[4].hi, f5 = m[5].hi;
   const float q = (f0 + f3 + f5) * (1.0f / 3.0f);
   const float p1 = f1 * f1 + f2 * f2 + f4 * f4;
   const float d0 = f0 - q, d1 = f3 - q, d2 = f5 - q;
@@ -687,14 +700,15 @@ __device__ __forceinline__ double lmax_sym3(const double* m, double det_m) {
     r = fminf(1.0f, fmaxf(-1.0f, r));
     l = q + 2.0f * p * __cosf(acosf(r) * (1.0f / 3.0f));
   }
-  const double i1 = m[0] + m[3] + m[5];
-  const double i2 = m[0] * m[3] - m[1] * m[1] + m[0] * m[5] - m[2] * m[2] + m[3] * m[5] - m[4] * m[4];
-  double x = (double)l;
-  const double f = ((x - i1) * x + i2) * x - det_m;
-  const double fp = (3.0 * x - 2.0 * i1) * x + i2;
-  if (fp != 0.0) {
-    const double st = f / fp;
-    if (fabs(st) < 1e-4 * fabs(x)) x -= st;
+  const df i1 = df_add(df_add(m[0], m[3]), m[5]);
+  const df i2 = df_add(df_add(df_mul_sub_mul(m[0], m[3], m[1], m[1]), df_mul_sub_mul(m[0], m[5], m[2], m[2])),
+                       df_mul_sub_mul(m[3], m[5], m[4], m[4]));
+  const df x = {l, 0.0f};
+  const df f = df_sub(df_mul(df_add(df_mul(df_sub(x, i1), x), i2), x), det_m);
+  const df fp = df_add(df_mul(df_sub(df_mul(x, {3.0f, 0.0f}), df_scale(i1, 2.0f)), x), i2);
+  if (fp.hi != 0.0f) {
+    const df st = df_mul(f, df_rcp(fp));
+    if (fabsf(st.hi) < 1e-4f * fabsf(l)) return df_sub(x, st);
   }
   return x;
 }
@@ -703,7 +717,7 @@ struct KmkArgs {
   int32_t E;
   const int32_t* xnd;
   const double* X;
-  double* em;  // [10][E] symmetric element entries (row pass layout)
+  float4* rec;  // P1 double-float row-slice records (2 float4 per slice)
 };
 
 // h_bar = edge_length_from_eigenvalue_metric(simplex_tensor(ele)) is
@@ -715,85 +729,120 @@ struct KmkArgs {
 // h_bar = W^(1/2) = (-W^2 + (i1^2 - i2) W + i1 i3 I) / (i1 i2 - i3) from the
 // invariants of the square roots of W's eigenvalues (Cayley-Hamilton); the
 // largest eigenvalue comes from W, the smallest as 1/lambda_max(m), the middle
-// one from det W, so none is a small difference of large ones.
-__global__ void __launch_bounds__(128) k_kmk_elem(KmkArgs A) {
+// one from det W, so none is a small difference of large ones.  The element
+// matrix 0.5 V g_a^T h_bar g_b is a stiffness matrix (its rows sum to zero),
+// written as the double-float row slices {K_a0, K_a1 | K_a2, 0} of the P1
+// assembly, all in double-float on the FP32 pipes.
+__global__ void __launch_bounds__(256) k_kmk_elem(KmkArgs A) {
   note_launch();
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
-    const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
-    const int vi[4] = {v.x, v.y, v.z, v.w};
-    double x[4][3];
+  extern __shared__ float4 kstage_all[];
+  const int lane = threadIdx.x & 31;
+  float4* stage = kstage_all + (threadIdx.x >> 5) * 256;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
+    const int e = base + lane;
+    if (e < A.E) {
+      const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+      const int vi[4] = {v.x, v.y, v.z, v.w};
+      double x[4][3];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
-    double J[3][3];
+        for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+      df J[3][3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+      for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int b = 0; b < 3; ++b) J[a][b] = x[b][a] - x[3][a];
-    double c[3][3];
+        for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
+      df c[3][3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+      for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-        c[i][k] = J[i1][k1] * J[i2][k2] - J[i2][k1] * J[i1][k2];
+        for (int k = 0; k < 3; ++k) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+          c[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
+        }
+      const df det = df_dot3(J[0][0], c[0][0], J[1][0], c[1][0], J[2][0], c[2][0]);
+      // g_b * det = column b of c; the fourth is minus their sum
+      df g[4][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        g[0][a] = c[a][0];
+        g[1][a] = c[a][1];
+        g[2][a] = c[a][2];
+        g[3][a] = df_neg(df_add(df_add(c[a][0], c[a][1]), c[a][2]));
       }
-    const double det = J[0][0] * c[0][0] + J[1][0] * c[1][0] + J[2][0] * c[2][0];
-    // g_b * det = column b of c; the fourth is minus their sum
-    double g[4][3];
+      df j1[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      g[0][a] = c[a][0];
-      g[1][a] = c[a][1];
-      g[2][a] = c[a][2];
-      g[3][a] = -(c[a][0] + c[a][1] + c[a][2]);
-    }
-    const int ix[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
-    double W[6], M[6];
-    double j1[3];
+      for (int a = 0; a < 3; ++a) j1[a] = df_add(df_add(J[a][0], J[a][1]), J[a][2]);
+      const df det2 = df_mul(det, det);
+      const df im = df_scale(df_rcp(det2), 0.5f);
+      df W[6], M[6];
+      const int ix[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
 #pragma unroll
-    for (int a = 0; a < 3; ++a) j1[a] = J[a][0] + J[a][1] + J[a][2];
-    const double im = 0.5 / (det * det);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const int r = ix[k][0], s = ix[k][1];
-      W[k] = 2.0 * (J[r][0] * J[s][0] + J[r][1] * J[s][1] + J[r][2] * J[s][2]) - 0.5 * j1[r] * j1[s];
-      M[k] = im * (g[0][r] * g[0][s] + g[1][r] * g[1][s] + g[2][r] * g[2][s] + g[3][r] * g[3][s]);
-    }
-    const double d2 = 2.0 * det * det;  // det W; det m = 1 / det W
-    const double l1 = lmax_sym3(W, d2), l3 = 1.0 / lmax_sym3(M, 1.0 / d2);
-    const double l2 = d2 / (l1 * l3);
-    const double s1 = sqrt(l1), s2 = sqrt(l2), s3 = sqrt(l3);
-    const double i1 = s1 + s2 + s3, i2 = s1 * s2 + s2 * s3 + s1 * s3, i3 = s1 * s2 * s3;
-    const double cw = i1 * i1 - i2, ci = i1 * i3, den = 1.0 / (i1 * i2 - i3);
-    // W^2 (symmetric)
-    const double w00 = W[0], w01 = W[1], w02 = W[2], w11 = W[3], w12 = W[4], w22 = W[5];
-    double H[3][3];
-    H[0][0] = (-(w00 * w00 + w01 * w01 + w02 * w02) + cw * w00 + ci) * den;
-    H[0][1] = (-(w00 * w01 + w01 * w11 + w02 * w12) + cw * w01) * den;
-    H[0][2] = (-(w00 * w02 + w01 * w12 + w02 * w22) + cw * w02) * den;
-    H[1][1] = (-(w01 * w01 + w11 * w11 + w12 * w12) + cw * w11 + ci) * den;
-    H[1][2] = (-(w01 * w02 + w11 * w12 + w12 * w22) + cw * w12) * den;
-    H[2][2] = (-(w02 * w02 + w12 * w12 + w22 * w22) + cw * w22 + ci) * den;
-    H[1][0] = H[0][1];
-    H[2][0] = H[0][2];
-    H[2][1] = H[1][2];
-    // 0.5 * V * g_a^T H g_b with g = c / det, V = |det| / 6
-    const double ks = 1.0 / (12.0 * fabs(det));
-    double hg[4][3];
-#pragma unroll
-    for (int b = 0; b < 4; ++b)
-#pragma unroll
-      for (int r = 0; r < 3; ++r) hg[b][r] = H[r][0] * g[b][0] + H[r][1] * g[b][1] + H[r][2] * g[b][2];
-    int k = 0;
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int b = a; b < 4; ++b) {
-        A.em[(int64_t)k * A.E + e] = ks * (g[a][0] * hg[b][0] + g[a][1] * hg[b][1] + g[a][2] * hg[b][2]);
-        ++k;
+      for (int k = 0; k < 6; ++k) {
+        const int r = ix[k][0], q = ix[k][1];
+        W[k] = df_sub(df_scale(df_dot3(J[r][0], J[q][0], J[r][1], J[q][1], J[r][2], J[q][2]), 2.0f),
+                      df_scale(df_mul(j1[r], j1[q]), 0.5f));
+        M[k] = df_mul(im, df_add(df_dot3(g[0][r], g[0][q], g[1][r], g[1][q], g[2][r], g[2][q]),
+                                 df_mul(g[3][r], g[3][q])));
       }
+      const df dW = df_scale(det2, 2.0f);  // det W; det m = 1 / det W
+      const df l1 = lmax_sym3(W, dW);
+      const df l3 = df_rcp(lmax_sym3(M, df_rcp(dW)));
+      const df l2 = df_mul(dW, df_rcp(df_mul(l1, l3)));
+      const df s1 = df_sqrt(l1), s2 = df_sqrt(l2), s3 = df_sqrt(l3);
+      const df i1 = df_add(df_add(s1, s2), s3);
+      const df i2 = df_add(df_add(df_mul(s1, s2), df_mul(s2, s3)), df_mul(s1, s3));
+      const df i3 = df_mul(df_mul(s1, s2), s3);
+      const df cw = df_sub(df_mul(i1, i1), i2), ci = df_mul(i1, i3);
+      const df den = df_rcp(df_sub(df_mul(i1, i2), i3));
+      // H = W^(1/2) (symmetric): (-W^2 + cw W + ci I) den
+      const df Wf[3][3] = {{W[0], W[1], W[2]}, {W[1], W[3], W[4]}, {W[2], W[4], W[5]}};
+      df H[3][3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int q = r; q < 3; ++q) {
+          const df w2 = df_dot3(Wf[r][0], Wf[0][q], Wf[r][1], Wf[1][q], Wf[r][2], Wf[2][q]);
+          df h = df_sub(df_mul(cw, Wf[r][q]), w2);
+          if (r == q) h = df_add(h, ci);
+          H[r][q] = df_mul(h, den);
+          H[q][r] = H[r][q];
+        }
+      // 0.5 * V * g_a^T H g_b with g = c / det, V = |det| / 6
+      const df ks = df_rcp(df_mul(df_abs(det), {12.0f, 0.0f}));
+      df hg[4][3];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) hg[b][r] = df_dot3(H[r][0], g[b][0], H[r][1], g[b][1], H[r][2], g[b][2]);
+      df K[4][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = a; b < 3; ++b) {
+          K[a][b] = df_mul(ks, df_dot3(g[a][0], hg[b][0], g[a][1], hg[b][1], g[a][2], hg[b][2]));
+          K[b][a] = K[a][b];
+        }
+      // row 3 as the row pass rebuilds column 3 (an exactly symmetric matrix)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) K[3][b] = df_neg(df_add(df_add(K[b][0], K[b][1]), K[b][2]));
+      float4* rec = stage + lane * 8;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        rec[2 * i] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
+        rec[2 * i + 1] = make_float4(K[i][2].hi, K[i][2].lo, 0.0f, 0.0f);
+      }
+    }
+    __syncwarp();
+    float4* out = A.rec + (uint32_t)base * 8u;
+    const int nvalid = min(32, A.E - base) * 8;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int idx = k * 32 + lane;
+      if (idx < nvalid) out[idx] = stage[idx];
+    }
+    __syncwarp();
   }
 }
 
@@ -1090,14 +1139,12 @@ extern "C" int fl_dev_assemble_kmk(fl_mesh m, fl_mesh prod, double theta_pg, con
     FL_TRY(m->st_val.reserve((size_t)m->nnz));
     kt = m->st_val.p;
   }
-  FL_TRY(m->em.reserve((size_t)m->E * 14));
-  // the row pass also sums four rhs slots per element: keep them zero
-  FL_TRY_CUDA(cudaMemsetAsync(m->em.p + (size_t)10 * m->E, 0, sizeof(double) * 4 * m->E, s));
-  KmkArgs K{m->E, m->xndglno.p, m->coords.p, m->em.p};
-  k_kmk_elem<<<grid_for(m->E, 128, 16), 128, 0, s>>>(K);
+  FL_TRY(m->em.reserve((size_t)m->E * 16));  // 128 B per element
+  KmkArgs K{m->E, m->xndglno.p, m->coords.p, reinterpret_cast<float4*>(m->em.p)};
+  k_kmk_elem<<<grid_for(m->E, 256, 8), 256, 8 * 256 * sizeof(float4), s>>>(K);
   FL_TRY_CUDA(cudaGetLastError());
   FL_TRY(m->st_rhs.reserve((size_t)m->N));
-  FL_TRY(rows_p1_closed(m, m->em.p, kt, m->st_rhs.p, s));
+  FL_TRY(rows_p1_df(m, m->em.p, kt, m->st_rhs.p, s));
   // by scaling masslump with theta, kmk is divided by theta (Momentum_CG.F90:2750-2762)
   const int scale = fabs(theta_pg - 1.0) < DBL_EPSILON ? 0 : 1;
   const double* a[3] = {kt, nullptr, nullptr};
