@@ -726,8 +726,13 @@ def run_ours(args, rank, ws, dist):
     def step():
         ft.assemble_advection_diffusion_cg(m, p, source=dsrc, val=val, rhs=rhs, stream=stream)
 
-    # tile choice by the project's autotuner (results do not depend on it)
-    _, _, tiles = ft.autotune_assembly(m, p, source=dsrc, val=val, rhs=rhs, stream=stream)
+    # tile choice by the project's autotuner (results do not depend on it),
+    # or fixed tiles (a profiler changes the autotuner's timings)
+    if args.tiles:
+        tiles = tuple(int(v) for v in args.tiles.split(","))
+        ft.set_assembly_tiles(m, *tiles)
+    else:
+        _, _, tiles = ft.autotune_assembly(m, p, source=dsrc, val=val, rhs=rhs, stream=stream)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -925,6 +930,8 @@ def main():
     ap.add_argument("--no-p2", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-projection", action="store_true")
+    ap.add_argument("--tiles", default="",
+                    help="fixed assembly tiles 'elem_block,elem_blocks_per_sm,row_tile' instead of the autotuner")
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--learned-sizes", default="64,128",
                     help="mesh sides of the learned-warm-start sequences")
