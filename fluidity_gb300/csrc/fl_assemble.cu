@@ -681,6 +681,7 @@ struct PullArgs {
   double* val;
   double* rhs;
   ErrWord* err;
+  int coalesce;  // P1 double-float rows: warp-cooperative stores of val (val in host memory)
 };
 
 // Double-float version of the row pass over the P1 element records: the
@@ -688,15 +689,24 @@ struct PullArgs {
 // row's mass sum minus their sum; each row accumulates in double-float
 // (shared memory, or in val for rows longer than RMAX) and converts every
 // entry to double once.
-// One row of the P1 double-float row pass.  FUSED: the record slice of each
-// incidence comes from P.ne_rec (records in element-item order) and is read
-// through L2 (written by other blocks of the same kernel); otherwise it is
-// (element, local row) of P.ne_col.
+// One row per lane of the P1 double-float row pass; all 32 lanes of a warp
+// call it together for 32 consecutive rows (live = false past the last row).
+// FUSED: the record slice of each incidence comes from P.ne_rec (records in
+// element-item order) and is read through L2 (written by other blocks of the
+// same kernel); otherwise it is (element, local row) of P.ne_col.  The warp
+// stores each row's entries; with P.coalesce (val in mapped host memory) the
+// warp stores its rows' entries, one contiguous range of val, with coalesced
+// stores instead.
 template <int THREADS, int RMAX, bool MASS, bool FUSED>
-__device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, float2* acc, int t) {
+__device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live, float2* acc, int t) {
   constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
   const float4* rec = reinterpret_cast<const float4*>(P.em);
-  const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
+  const int lane = t & 31;
+  int base = 0, L = 0;
+  if (live) {
+    base = __ldg(P.findrm + row);
+    L = __ldg(P.findrm + row + 1) - base;
+  }
   const bool in_smem = L <= RMAX;
   if (in_smem) {
     for (int k = 0; k < L; ++k) acc[k * THREADS + t] = make_float2(0.0f, 0.0f);
@@ -704,7 +714,7 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, float2* ac
     for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
   }
   df r = {0.0f, 0.0f};
-  const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
+  const int ib = live ? __ldg(P.ne_ptr + row) : 0, ie = live ? __ldg(P.ne_ptr + row + 1) : 0;
   // incidences in groups of four: all index and record loads of a group are
   // issued before any accumulation (memory-level parallelism); the adds run
   // in the group's order, so the colour order of the sum is kept
@@ -751,12 +761,39 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, float2* ac
       r = df_add(r, {q[u][1].z, q[u][1].w});
     }
   }
-  if (in_smem)
-    for (int k = 0; k < L; ++k) {
-      const float2 c = acc[k * THREADS + t];
-      P.val[base + k] = df_to_double({c.x, c.y});
+  if (!P.coalesce) {
+    if (in_smem)
+      for (int k = 0; k < L; ++k) {
+        const float2 c = acc[k * THREADS + t];
+        P.val[base + k] = df_to_double({c.x, c.y});
+      }
+  } else {
+    __syncwarp();
+    // the warp's rows [r0, r0 + 32) hold val[start, end): lane j of each pass
+    // stores entry start + 32 m + j, found in the accumulators of its row's lane
+    const int start = __shfl_sync(0xffffffffu, base, 0);
+    const int nlive = __popc(__ballot_sync(0xffffffffu, live));
+    const int end = nlive ? __shfl_sync(0xffffffffu, base + L, nlive - 1) : start;
+    const unsigned smem_rows = __ballot_sync(0xffffffffu, in_smem);
+    const int wt = t & ~31;  // thread index of lane 0
+    for (int p0 = start; p0 < end; p0 += 32) {
+      const int p = p0 + lane;
+      // owner: the last lane whose row starts at or before p (5 halvings)
+      int lo = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = lo + step;
+        const int cb = __shfl_sync(0xffffffffu, base, cand < nlive ? cand : 0);
+        if (cand < nlive && cb <= p) lo = cand;
+      }
+      const int ob = __shfl_sync(0xffffffffu, base, lo);
+      if (p < end && ((smem_rows >> lo) & 1u)) {
+        const float2 c = acc[(p - ob) * THREADS + wt + lo];
+        P.val[p] = df_to_double({c.x, c.y});
+      }
     }
-  P.rhs[row] = df_to_double(r);
+  }
+  if (live) P.rhs[row] = df_to_double(r);
 }
 
 template <int THREADS, int RMAX, bool MASS>
@@ -764,8 +801,10 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
   note_launch();
   extern __shared__ unsigned char smem_raw[];
   float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
-  for (int row = blockIdx.x * THREADS + threadIdx.x; row < P.N; row += gridDim.x * THREADS)
-    p1_df_row<THREADS, RMAX, MASS, false>(P, row, acc, threadIdx.x);
+  for (int r0 = blockIdx.x * THREADS; r0 < P.N; r0 += gridDim.x * THREADS) {
+    const int row = r0 + threadIdx.x;
+    p1_df_row<THREADS, RMAX, MASS, false>(P, row, row < P.N, acc, threadIdx.x);
+  }
 }
 
 // ----------------------------------------- fused P1 element and row pass --
@@ -849,7 +888,7 @@ __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, 
       }
       __syncthreads();
       const int row = j * kFzItem + t;
-      if (row < P.N) p1_df_row<kFzItem, 16, MASS, true>(P, row, acc, t);
+      p1_df_row<kFzItem, 16, MASS, true>(P, row, row < P.N, acc, t);
     }
     __syncthreads();
   }
@@ -1292,7 +1331,7 @@ int dirichlet_launch(fl_mesh_t* m, int32_t nb, const int32_t* nodes, int32_t bas
 }
 
 int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
-             cudaStream_t s, double* em_override) {
+             cudaStream_t s, double* em_override, bool host_out) {
   FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
   FL_CHECK_ARG(m->E > 0 && (m->loc == 4 || m->loc == 10), "the handle has no elements (pattern-only handle)");
   FL_CHECK_ARG(p->quad_degree >= 1 && p->quad_degree <= 4, "quadrature degree 1..4");
@@ -1409,7 +1448,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
       FL_TRY(fused_plan(m, s));
       if (m->fz_state == 1) {
         PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->fz_rec.p, m->ne_pos.p, m->ndglno.p, m->findrm.p,
-                   m->colm.p, em, val, rhs, m->err.p};
+                   m->colm.p, em, val, rhs, m->err.p, host_out ? 1 : 0};
         switch (key) {
 #define FL_FZ_CASE(K, M, S, T, AN) \
   case K: FL_TRY((launch_fused<M, S, T, AN>(m, D, P, s))); break;
@@ -1452,7 +1491,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   }
   FL_TRY_CUDA(cudaGetLastError());
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
-             em, val, rhs, m->err.p};
+             em, val, rhs, m->err.p, host_out ? 1 : 0};
   FL_TRY(launch_rows(P, loc, use_df, closed, m->max_row, m->tile_rows, s, p->have_mass != 0));
   if (m->timing) {
     FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
@@ -1549,12 +1588,31 @@ extern "C" int fl_dev_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, c
   return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
 }
 
+// Device view of a host array that is page-locked and mapped (cudaHostAlloc,
+// cudaHostRegister, or a pinned buffer of the caller's allocator); null for
+// pageable memory.
+static double* mapped_host(double* h) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? static_cast<double*>(a.devicePointer) : nullptr;
+}
+
 extern "C" int fl_gpu_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, const fl_fields* f,
                                          double* val, double* rhs) {
   FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
   cudaStream_t s = m->stream;
-  FL_TRY(m->st_val.reserve(m->nnz));
-  FL_TRY(m->st_rhs.reserve(m->N));
+  // Pinned output arrays: the row pass writes val and rhs into host memory
+  // itself (each entry once), so the transfer overlaps the row pass instead
+  // of following it.  Pageable arrays go through device staging buffers.
+  double* mval = mapped_host(val);
+  double* mrhs = mval ? mapped_host(rhs) : nullptr;
+  if (!mrhs) {
+    FL_TRY(m->st_val.reserve(m->nnz));
+    FL_TRY(m->st_rhs.reserve(m->N));
+  }
   fl_fields df{nullptr, nullptr, nullptr, nullptr};
   auto up = [&](const double* h, DevBuf<double>& d, size_t n, const double** out) -> int {
     if (!h) return FL_OK;
@@ -1567,6 +1625,11 @@ extern "C" int fl_gpu_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, c
   FL_TRY(up(p->have_advection ? f->velocity : nullptr, m->st_u, (size_t)3 * m->Nx, &df.velocity));
   FL_TRY(up(p->have_source ? f->source : nullptr, m->st_src, m->N, &df.source));
   FL_TRY(up(p->have_absorption ? f->absorption : nullptr, m->st_abs, m->N, &df.absorption));
+  if (mrhs) {
+    FL_TRY(assemble(m, p, &df, mval, mrhs, s, nullptr, true));
+    FL_TRY(check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern"));
+    return FL_OK;
+  }
   FL_TRY(fl_dev_assemble_advdif_cg(m, p, &df, m->st_val.p, m->st_rhs.p, s));
   FL_TRY_CUDA(cudaMemcpyAsync(val, m->st_val.p, sizeof(double) * m->nnz, cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaMemcpyAsync(rhs, m->st_rhs.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));

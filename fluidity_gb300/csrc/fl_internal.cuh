@@ -141,7 +141,7 @@ int csr_mult(struct ::fl_mesh_t* m, const double* val, const double* x, double* 
 // Assembly pieces used by batches (no synchronisation, no allocation).
 size_t assembly_scratch_doubles(const struct ::fl_mesh_t* m, const fl_advdif_params* p);
 int assemble(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
-             cudaStream_t s, double* em_override);
+             cudaStream_t s, double* em_override, bool host_out = false);
 int dirichlet_launch(struct ::fl_mesh_t* m, int32_t nb, const int32_t* nodes, int32_t base, const double* g,
                      const double* t, double dt, double* rhs, uint8_t* inactive, cudaStream_t s);
 int autotune_assembly(struct ::fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val,
