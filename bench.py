@@ -507,6 +507,25 @@ def bench_projection(args, dev, stream, m, X, n):
     torch.cuda.synchronize()
     solve_ms = e0.elapsed_time(e1)
     it_bytes = cg_iteration_bytes(N, nnz2)
+    # the same projection solve with the AMG preconditioner (FP32 V-cycle,
+    # unpreconditioned-norm test: rtol bounds the true residual)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    amg = ft.AmgPreconditioner(so, cmc, ina, stream=stream, unpreconditioned_norm=True)
+    amg.set_precision(True)
+    torch.cuda.synchronize()
+    amg_setup_ms = (time.perf_counter() - t0) * 1e3
+    dpa = torch.zeros(N, dtype=torch.float64, device=dev)
+    amg.solve(dpa, rhs, opts, stream=stream)
+    dpa.zero_()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    rep_amg = amg.solve(dpa, rhs, opts, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    amg_ms = e0.elapsed_time(e1)
+    amg_levels = amg.levels()
+    amg.close()
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
@@ -544,6 +563,10 @@ def bench_projection(args, dev, stream, m, X, n):
         "projection_solve": {"ms": solve_ms, "iterations": rep["iterations"], "reason": rep["reason_name"],
                              "true_rel_residual": rep["true_rel_residual"],
                              "cg_iteration_gbs": it_bytes * rep["iterations"] / (solve_ms * 1e-3) / 1e9},
+        "projection_solve_amg": {"ms": amg_ms, "setup_ms": amg_setup_ms, "iterations": rep_amg["iterations"],
+                                 "reason": rep_amg["reason_name"], "true_rel_residual": rep_amg["true_rel_residual"],
+                                 "levels": amg_levels, "cycle": "fp32",
+                                 "norm": "unpreconditioned ||r|| / ||b||"},
         "cpu_baseline": cpu,
     }
 

@@ -397,16 +397,38 @@ struct DfArgs {
 // dynamic shared memory).
 //
 // One element of the P1 double-float pass: its record (4 row slices) into rec.
-template <bool MASS, bool SRC, bool TF, bool ANISO>
-__device__ __forceinline__ void p1_df_element(const DfArgs& A, int e, float4* rec) {
-  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
+// The element's inputs: vertex coordinates, and the source and old-field
+// values at its nodes.  (Loading them one element ahead measured no faster at
+// 128^3: the registers it holds cost a quarter of the resident warps.)
+struct P1In {
+  double x[4][3];
+  double f[4];
+  double t[4];
+};
+
+template <bool SRC, bool TF>
+__device__ __forceinline__ void p1_df_load(const DfArgs& A, int e, P1In& in) {
   const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
   const int vi[4] = {v.x, v.y, v.z, v.w};
-  double x[4][3];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+    for (int a = 0; a < 3; ++a) in.x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+  if (SRC || TF) {
+    const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
+    const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (SRC) in.f[i] = __ldg(A.f + tn[i]);
+      if (TF) in.t[i] = __ldg(A.t + tn[i]);
+    }
+  }
+}
+
+template <bool MASS, bool SRC, bool TF, bool ANISO>
+__device__ __forceinline__ void p1_df_element(const DfArgs& A, const P1In& in, float4* rec) {
+  constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
+  const auto& x = in.x;
   df J[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -459,13 +481,11 @@ __device__ __forceinline__ void p1_df_element(const DfArgs& A, int e, float4* re
       K[i][j] = m;
       K[j][i] = m;
     }
-  const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
-  const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
   df r[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
   if (SRC) {
     df fe[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) fe[i] = df_from_double(__ldg(A.f + tn[i]));
+    for (int i = 0; i < 4; ++i) fe[i] = df_from_double(in.f[i]);
     const df fsum = df_add(df_add(fe[0], fe[1]), df_add(fe[2], fe[3]));
     const df q1 = df_mul(df_mul(adet, A.m1), fsum);
     const df q2 = df_mul(adet, df_sub(A.m0, A.m1));
@@ -475,7 +495,7 @@ __device__ __forceinline__ void p1_df_element(const DfArgs& A, int e, float4* re
   if (TF) {
     df te[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) te[i] = df_from_double(__ldg(A.t + tn[i]));
+    for (int i = 0; i < 4; ++i) te[i] = df_from_double(in.t[i]);
     const df rs = df_mul(A.rscale, rdet);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -511,7 +531,11 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   float4* stage = stage_all + (threadIdx.x >> 5) * (32 * NREC);
   for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
     const int e = base + lane;
-    if (e < A.E) p1_df_element<MASS, SRC, TF, ANISO>(A, e, stage + lane * NREC);
+    if (e < A.E) {
+      P1In in;
+      p1_df_load<SRC, TF>(A, e, in);
+      p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * NREC);
+    }
     __syncwarp();
     float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
     const int nvalid = min(32, A.E - base) * NREC;
@@ -854,7 +878,11 @@ __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, 
       const int base = code * kFzItem + w * 32;  // this warp's 32 consecutive positions
       if (base < A.E) {
         const int pp = base + lane;
-        if (pp < A.E) p1_df_element<MASS, SRC, TF, ANISO>(A, __ldg(F.perm + pp), stage + lane * NREC);
+        if (pp < A.E) {
+          P1In in;
+          p1_df_load<SRC, TF>(A, __ldg(F.perm + pp), in);
+          p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * NREC);
+        }
         __syncwarp();
         float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
         const int nvalid = min(32, A.E - base) * NREC;

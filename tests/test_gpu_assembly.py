@@ -146,3 +146,25 @@ def test_invalid_options_are_errors():
     val, rhs = ft.assemble_advection_diffusion_cg(m, _params(CASES["poisson"], 2),
                                                   source=np.ones(X.shape[0]))
     assert np.isfinite(val).all()
+
+
+@pytest.mark.parametrize("n", [5, 33])
+def test_host_pointer_assembly_pinned_and_pageable(n):
+    """The host-pointer entry point gives the device path's bits whether the
+    output arrays are pinned (written in place by the row pass) or pageable
+    (staged and copied)."""
+    import torch
+    nd, X = M.cube_mesh(n)
+    m = ft.Mesh(nd, X)
+    p = _params(CASES["poisson"], 2)
+    src = M.poisson_source(X)
+    dval, drhs = ft.assemble_advection_diffusion_cg(m, p, source=torch.tensor(src, device="cuda"))
+    dval, drhs = dval.cpu().numpy(), drhs.cpu().numpy()
+    pv = torch.empty(m.nnz, dtype=torch.float64).pin_memory().numpy()
+    pr = torch.empty(m.N, dtype=torch.float64).pin_memory().numpy()
+    pv[:] = np.nan
+    pr[:] = np.nan
+    ft.assemble_advection_diffusion_cg(m, p, source=src, val=pv, rhs=pr)
+    assert np.array_equal(pv, dval) and np.array_equal(pr, drhs)
+    hv, hr = ft.assemble_advection_diffusion_cg(m, p, source=src)
+    assert np.array_equal(hv, dval) and np.array_equal(hr, drhs)
