@@ -716,8 +716,12 @@ struct PullArgs {
 // One row per lane of the P1 double-float row pass; all 32 lanes of a warp
 // call it together for 32 consecutive rows (live = false past the last row).
 // FUSED: the record slice of each incidence comes from P.ne_rec (records in
-// element-item order) and is read through L2 (written by other blocks of the
-// same kernel); otherwise it is (element, local row) of P.ne_col.  The warp
+// element-item order); otherwise it is (element, local row) of P.ne_col.
+// The fused pass may read records through L1 although other blocks of the
+// same kernel wrote them: an item's records are one 128-B aligned block (256
+// records of 128 or 192 B), a row item touches an item's lines only after the
+// item is complete, and L1 starts every kernel empty, so no L1 line can hold
+// data older than the item that wrote it.  The warp
 // stores each row's entries; with P.coalesce (val in mapped host memory) the
 // warp stores its rows' entries, one contiguous range of val, with coalesced
 // stores instead.
@@ -758,7 +762,7 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
       const uint32_t ri = (uint32_t)SL * slice;
 #pragma unroll
       for (int k = 0; k < SL; ++k) {
-        if (q0 + u < ie) q[u][k] = FUSED ? __ldcg(rec + ri + k) : __ldg(rec + ri + k);
+        if (q0 + u < ie) q[u][k] = __ldg(rec + ri + k);
         else q[u][k] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
@@ -839,10 +843,9 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
 // of its incidences are complete (threadfence + atomic add on one side,
 // acquire loads on the other), then sums its rows exactly as the row pass
 // does, in colour order: the result is bit-identical to the two kernels.
-// Row items follow the element items they need at a distance of about one
-// resident wave, so the records they read were written moments earlier and
-// are still in L2 (read with ld.global.cg: other SMs wrote them during this
-// kernel).  Every group a row item waits for holds only items dequeued before
+// Row items follow the element items they need at a distance of about three
+// resident waves, so the records they read were written moments earlier and
+// are still in L2.  Every group a row item waits for holds only items dequeued before
 // it by running blocks, so the queue always drains; a wait that runs out sets
 // FL_ERR_TIMEOUT.
 struct FusedArgs {
