@@ -717,9 +717,10 @@ struct PullArgs {
 // call it together for 32 consecutive rows (live = false past the last row).
 // FUSED: the record slice of each incidence comes from P.ne_rec (records in
 // element-item order); otherwise it is (element, local row) of P.ne_col.
-// The fused pass may read records through L1 although other blocks of the
-// same kernel wrote them: an item's records are one 128-B aligned block (256
-// records of 128 or 192 B), a row item touches an item's lines only after the
+// The fused pass reads records through L1 (ld.global.ca, not the read-only
+// ld.global.nc path) although other blocks of the same kernel wrote them: an
+// item's records are one 128-B aligned block (256 records of 128 or 192 B),
+// written by one block, a row item touches an item's lines only after the
 // item is complete, and L1 starts every kernel empty, so no L1 line can hold
 // data older than the item that wrote it.  The warp
 // stores each row's entries; with P.coalesce (val in mapped host memory) the
@@ -762,7 +763,7 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
       const uint32_t ri = (uint32_t)SL * slice;
 #pragma unroll
       for (int k = 0; k < SL; ++k) {
-        if (q0 + u < ie) q[u][k] = __ldg(rec + ri + k);
+        if (q0 + u < ie) q[u][k] = FUSED ? __ldca(rec + ri + k) : __ldg(rec + ri + k);
         else q[u][k] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
     }
