@@ -107,3 +107,17 @@ def test_row_products_match_the_triple_product(mesh4):
         ref = K @ sp.diags(1.0 / (theta * ml)) @ K.T
         got = sp.csr_matrix((kmk, sc, sf), shape=(N, N))
         assert abs(got - ref).max() < 1e-13 * abs(ref).max()
+
+
+@pytest.mark.parametrize("n", [1, 3, 6])
+def test_boundary_faces_of_the_cube(n):
+    """The surface mesh of the six-tet cube: 2 triangles per boundary square,
+    each face a face of its element, lying on one cube face."""
+    nd, X = M.cube_mesh(n)
+    faces, fe = M.boundary_faces(nd)
+    assert len(faces) == 12 * n * n
+    for f, e in zip(faces, fe):
+        assert set(f.tolist()) < set(nd[e].tolist())
+        P = X[f]
+        on = [np.all(np.abs(P[:, a] - v) < 1e-14) for a in range(3) for v in (0.0, 1.0)]
+        assert sum(on) == 1
