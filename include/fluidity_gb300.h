@@ -23,6 +23,8 @@
  * default stream is passed as cudaStreamLegacy).  Every
  * function returns an fl_status; fl_last_error() describes the last failure
  * of the calling thread.  Indices follow `index_base` (1 = Fortran, 0 = C).
+ * The calls on one handle share its scratch buffers (element records, staging
+ * arrays): issue them on one stream, or order them across streams.
  */
 #ifndef FLUIDITY_GB300_H
 #define FLUIDITY_GB300_H
