@@ -77,3 +77,37 @@ def test_bad_connectivity_is_an_error():
     bad[3, 1] = X.shape[0] + 5
     with pytest.raises(ft._lib.FlError):
         ft.Mesh(bad, X, nodes=X.shape[0])
+
+
+def test_unused_nodes_and_shuffled_numbering(O):
+    """Ragged numbering: the nodes of a cube mesh permuted at random, plus three
+    node ids that no element uses (empty CSR rows, centrm -1).  Sparsity,
+    colouring and the assembled Poisson matrix match the oracle."""
+    nd, X = M.cube_mesh(4)
+    rng = np.random.default_rng(7)
+    N0 = X.shape[0]
+    perm = rng.permutation(N0 + 3)[:N0]          # old id -> new id, leaving 3 ids unused
+    nd2 = perm[nd].astype(np.int32)
+    N = N0 + 3
+    X2 = np.zeros((N, 3))
+    X2[perm] = X
+    m = ft.Mesh(nd2, X2, nodes=N)
+    s = m.sparsity()
+    f, c, ce = O.make_sparsity(nd2, N)
+    assert np.array_equal(s.findrm, f) and np.array_equal(s.colm, c) and np.array_equal(s.centrm, ce)
+    unused = np.setdiff1d(np.arange(N), perm)
+    assert np.all(np.diff(s.findrm)[unused] == 0) and np.all(s.centrm[unused] == -1)
+    col, _, _ = m.colouring()
+    ocol, ncol = O.colour_cg1(nd2, N)
+    assert np.array_equal(col, ocol) and m.ncolours == ncol
+    src = M.poisson_source(X2)
+    p = ft.advdif_params(diffusivity=1.0, have_source=True, quad_degree=2)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, p, source=src)
+    oval, orhs, st = O.assemble_advdif(ndglno_t=nd2, nt=N, ndglno_x=nd2, coords=X2, findrm=f, colm=c,
+                                       diffusivity=1.0, source=src, colours=O.colour_sets(ocol, ncol))
+    assert st == 0
+    scale = np.abs(oval).max()
+    assert np.abs(val - oval).max() <= 1e-12 * scale
+    assert np.abs(rhs - orhs).max() <= 1e-12 * np.abs(orhs).max()
+    assert np.all(rhs[unused] == 0.0)
+    m.close()

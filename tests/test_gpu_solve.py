@@ -208,3 +208,19 @@ def test_readnsolve_of_a_dump_matches_petsc_solve(O, tmp_path):
     assert drep["reason"] == 2 and abs(drep["iterations"] - rep["iterations"]) <= 1
     assert np.abs(y[act] - x[act]).max() <= 1e-8 * np.abs(x).max()
     assert np.abs(y[~act]).max() == 0.0
+
+
+def test_every_row_dirichlet(O):
+    """All rows inactive: the solution is the rhs on every row (ghost
+    semantics) after no iteration, for CG and GMRES, as in the oracle."""
+    m, Xf, val, rhs, ina = poisson(O, 3)
+    ina[:] = 1
+    g = np.linspace(-1.0, 1.0, m.N)
+    rhs = g.copy()
+    for ksp in ("cg", "gmres"):
+        x = np.full(m.N, 7.0)
+        rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(ksp=ksp, rtol=1e-10), inactive=ina)
+        assert np.array_equal(x, g)
+        ox, its, reason, _ = oracle_solve(O, m, val, rhs, ina, ksp=ksp)
+        assert np.array_equal(ox, g)
+        assert rep["iterations"] == its == 0
