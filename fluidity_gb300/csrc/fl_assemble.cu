@@ -557,7 +557,9 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
 // an exact regrouping of dshape_dot_dshape / dshape_tensor_dshape
 // (FETools.F90:391,668) over the quadrature rule, as for P1.  The tables
 // (55 symmetric pairs) travel as kernel parameters.  Each element writes ten
-// row slices {K_i0..K_i9, r_i, 0} of double-float pairs (96 B each).
+// row slices {K_i0..K_i9, r_i, 0} of double-float pairs (96 B each), stored
+// slice-major (slice i of element e at i E + e) so that a warp's slices i
+// form one contiguous run written with coalesced stores.
 struct DfP2Args {
   int32_t E;
   const int32_t* nd;   // P2 connectivity, 10 per element
@@ -599,9 +601,19 @@ __device__ __forceinline__ df df_dot(const df* a, const df* b) {
   return df_fast_two_sum(s, e);
 }
 
-__global__ void __launch_bounds__(128) k_asm_p2_diffusion_df(DfP2Args A) {
+constexpr int kP2Threads = 128;
+
+__global__ void __launch_bounds__(kP2Threads) k_asm_p2_diffusion_df(DfP2Args A) {
   note_launch();
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
+  __shared__ float4 stage_all[4][32 * 6];  // one 96-B slice per lane and warp
+  extern __shared__ float2 p2_dots[];      // [45][kP2Threads]: the strict upper d_ij
+  const int lane = threadIdx.x & 31;
+  float4* stage = stage_all[threadIdx.x >> 5];
+  float2* dots = p2_dots + threadIdx.x;
+  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
+    // lanes past the last element compute on element base (their slices are
+    // not stored)
+    const int e = base + lane < A.E ? base + lane : base;
     const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
     const int vi[4] = {v.x, v.y, v.z, v.w};
     double x[4][3];
@@ -653,20 +665,34 @@ __global__ void __launch_bounds__(128) k_asm_p2_diffusion_df(DfP2Args A) {
       fe[j] = A.have_src ? df_mul(adet, df_from_double(__ldg(A.f + tn[j]))) : df{0.0f, 0.0f};
       te[j] = A.t ? df_from_double(__ldg(A.t + tn[j])) : df{0.0f, 0.0f};
     }
-    float4* rec = A.em + (uint32_t)e * 60u;
+    // slice i of the warp's 32 elements is one contiguous run of the
+    // slice-major records: stage it and store it with coalesced 16-B stores
+    const int nvalid = min(32, A.E - base) * 6;
 #pragma unroll 1
     for (int i = 0; i < 10; ++i) {
+      // d_ij = q . S_ij is symmetric: row i computes j >= i and keeps j > i
+      // for the later rows in its own column of shared memory
       df K[10];
       df tsum = {0.0f, 0.0f};
 #pragma unroll
       for (int j = 0; j < 10; ++j) {
-        const df* Sp = A.S[sym10(i, j)];
-        if (A.t) {
-          const df op = df_dot<6>(qo, Sp);
-          K[j] = df_mul(op, A.qs);
-          tsum = df_add(tsum, df_mul(op, te[j]));
+        df d;
+        if (j >= i) {
+          d = df_dot<6>(A.t ? qo : qk, A.S[sym10(i, j)]);
+          if (j > i) {
+            const int u = i * 9 - i * (i - 1) / 2 + (j - i - 1);
+            dots[u * kP2Threads] = make_float2(d.hi, d.lo);
+          }
         } else {
-          K[j] = df_dot<6>(qk, Sp);
+          const int u = j * 9 - j * (j - 1) / 2 + (i - j - 1);
+          const float2 w = dots[u * kP2Threads];
+          d = {w.x, w.y};
+        }
+        if (A.t) {
+          K[j] = df_mul(d, A.qs);
+          tsum = df_add(tsum, df_mul(d, te[j]));
+        } else {
+          K[j] = d;
         }
         if (A.have_mass) K[j] = df_add(K[j], df_mul(adet, A.M[sym10(i, j)]));
       }
@@ -678,10 +704,19 @@ __global__ void __launch_bounds__(128) k_asm_p2_diffusion_df(DfP2Args A) {
         r = df_dot<10>(mrow, fe);
       }
       if (A.t) r = df_sub(r, tsum);
+      float4* rec = stage + lane * 6;
 #pragma unroll
       for (int k = 0; k < 5; ++k)
-        rec[6 * i + k] = make_float4(K[2 * k].hi, K[2 * k].lo, K[2 * k + 1].hi, K[2 * k + 1].lo);
-      rec[6 * i + 5] = make_float4(r.hi, r.lo, 0.0f, 0.0f);
+        rec[k] = make_float4(K[2 * k].hi, K[2 * k].lo, K[2 * k + 1].hi, K[2 * k + 1].lo);
+      rec[5] = make_float4(r.hi, r.lo, 0.0f, 0.0f);
+      __syncwarp();
+      float4* out = A.em + ((uint32_t)i * (uint32_t)A.E + (uint32_t)base) * 6u;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const int idx = k * 32 + lane;
+        if (idx < nvalid) out[idx] = stage[idx];
+      }
+      __syncwarp();
     }
   }
 }
@@ -1070,7 +1105,8 @@ static int launch_fused(fl_mesh_t* m, const DfArgs& D, const PullArgs& P, cudaSt
 }
 
 // Row pass of the P2 double-float records: slice (element, local row) =
-// 6 float4 {K_a0..K_a9, r_a, 0}; the row positions of the ten element nodes
+// 6 float4 {K_a0..K_a9, r_a, 0} at (local row) E + element; the row
+// positions of the ten element nodes
 // come from three ne_pos words per incidence.  Incidences are taken two at a
 // time (loads first, then the adds in colour order).
 template <int THREADS, int RMAX>
@@ -1100,7 +1136,8 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull_df10(PullArgs P) {
         inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
 #pragma unroll
         for (int w = 0; w < 3; ++w) pw[u][w] = ok ? __ldg(P.ne_pos + (int64_t)(q0 + u) * 3 + w) : 0u;
-        const uint32_t ri = 6u * (uint32_t)((inc[u] >> 4) * 10 + (inc[u] & 15));
+        // slice-major records: slice a of element e at (a E + e)
+        const uint32_t ri = 6u * ((uint32_t)(inc[u] & 15) * (uint32_t)P.E + (uint32_t)(inc[u] >> 4));
 #pragma unroll
         for (int k = 0; k < 6; ++k) q[u][k] = ok ? __ldg(rec + ri + k) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
@@ -1451,7 +1488,14 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
       D.kdiag[a] = df_host(p->isotropic_diffusivity ? p->diffusivity[0] : p->diffusivity[4 * a]);
     D.have_mass = p->have_mass;
     D.have_src = p->have_source;
-    k_asm_p2_diffusion_df<<<grid_for(m->E, 128, esm), 128, 0, s>>>(D);
+    const size_t dsmem = (size_t)45 * kP2Threads * sizeof(float2);
+    static bool p2_configured = false;
+    if (!p2_configured) {
+      FL_TRY_CUDA(cudaFuncSetAttribute(k_asm_p2_diffusion_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)dsmem));
+      p2_configured = true;
+    }
+    k_asm_p2_diffusion_df<<<grid_for(m->E, kP2Threads, esm), kP2Threads, dsmem, s>>>(D);
   } else if (use_df) {
     RefTensors h;
     build_tensors(1, p->quad_degree, h);
