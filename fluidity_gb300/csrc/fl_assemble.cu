@@ -383,6 +383,10 @@ struct DfArgs {
   df kdiag[3];   // diagonal kappa (ones if isotropic)
   df m0, m1;     // reference mass entries (diagonal, off-diagonal)
   int have_mass, have_src, aniso;
+  // element pass over record positions [p0, E): position q holds element
+  // perm[q] (identity when perm is null)
+  const int32_t* perm;
+  int32_t p0;
 };
 
 // Specialised on the term set (consistent mass, source, old field t,
@@ -529,11 +533,12 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
   constexpr int NREC = 4 * SL;      // float4 per element record
   float4* stage = stage_all + (threadIdx.x >> 5) * (32 * NREC);
-  for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
+  for (int base = A.p0 + blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E;
+       base += gridDim.x * blockDim.x) {
     const int e = base + lane;
     if (e < A.E) {
       P1In in;
-      p1_df_load<SRC, TF>(A, e, in);
+      p1_df_load<SRC, TF>(A, A.perm ? __ldg(A.perm + e) : e, in);
       p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * NREC);
     }
     __syncwarp();
@@ -741,6 +746,7 @@ struct PullArgs {
   double* rhs;
   ErrWord* err;
   int coalesce;  // P1 double-float rows: warp-cooperative stores of val (val in host memory)
+  int32_t row0;  // P1 double-float rows: the pass covers rows [row0, N)
 };
 
 // Double-float version of the row pass over the P1 element records: the
@@ -860,14 +866,15 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
   if (live) P.rhs[row] = df_to_double(r);
 }
 
-template <int THREADS, int RMAX, bool MASS>
+// PERM: records in the fused pass's element order (slices from P.ne_rec).
+template <int THREADS, int RMAX, bool MASS, bool PERM>
 __global__ void __launch_bounds__(THREADS) k_rows_pull_df(PullArgs P) {
   note_launch();
   extern __shared__ unsigned char smem_raw[];
   float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
-  for (int r0 = blockIdx.x * THREADS; r0 < P.N; r0 += gridDim.x * THREADS) {
+  for (int r0 = P.row0 + blockIdx.x * THREADS; r0 < P.N; r0 += gridDim.x * THREADS) {
     const int row = r0 + threadIdx.x;
-    p1_df_row<THREADS, RMAX, MASS, false>(P, row, row < P.N, acc, threadIdx.x);
+    p1_df_row<THREADS, RMAX, MASS, PERM>(P, row, row < P.N, acc, threadIdx.x);
   }
 }
 
@@ -897,6 +904,8 @@ struct FusedArgs {
 constexpr int kFzItem = 256;             // elements or rows per item = threads per block
 constexpr int kFzGroup = 64;             // element items per completion counter
 constexpr unsigned kFzSpin = 1u << 22;   // polls of one counter before giving up
+constexpr int64_t kCkBytes = 4 << 20;    // pipelined host output: val bytes per row chunk
+constexpr int64_t kCkMax = 16;           // and at most this many chunks
 
 template <bool MASS, bool SRC, bool TF, bool ANISO>
 __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, FusedArgs F) {
@@ -1038,6 +1047,52 @@ static int fused_plan(fl_mesh_t* m, cudaStream_t s) {
   if (placed != E) {
     set_error("fused pass plan: %d of %d elements placed", placed, E);
     return FL_ERR_ARG;
+  }
+  // Row chunks of the pipelined host-output assembly: about kCkBytes of val
+  // each (at most kCkMax), the first a quarter of the others so that the
+  // host link starts early; chunk k needs the element positions up to the
+  // highest one its rows (and all earlier rows) read, rounded up to a whole
+  // warp of records, and the field values up to the highest node of those
+  // elements (positions are in ascending highest-node order).
+  m->ck_rows.clear();
+  m->ck_elem.clear();
+  m->ck_val.clear();
+  m->ck_node.clear();
+  const int64_t K = std::min<int64_t>(kCkMax, m->nnz * (int64_t)sizeof(double) / kCkBytes);
+  const int64_t Q = 4 * K - 3;  // quarter chunks
+  if (K >= 2 && N >= Q) {
+    std::vector<int32_t> hf((size_t)N + 1);
+    FL_TRY_CUDA(cudaMemcpyAsync(hf.data(), m->findrm.p, sizeof(int32_t) * ((size_t)N + 1), cudaMemcpyDeviceToHost, s));
+    FL_TRY_CUDA(cudaStreamSynchronize(s));
+    m->ck_rows.push_back(0);
+    m->ck_elem.push_back(0);
+    m->ck_val.push_back(hf[0]);
+    m->ck_node.push_back(0);
+    int32_t need = 0;
+    int64_t k = 1;
+    for (int32_t i = 0; i < N; ++i) {
+      need = std::max(need, hmax[2 * (size_t)i + 1] + 1);
+      const int32_t rk = (int32_t)((int64_t)N * (4 * k - 3) / Q);
+      if (i + 1 == rk) {
+        m->ck_rows.push_back(rk);
+        m->ck_elem.push_back(k == K ? E : std::min(E, std::max(m->ck_elem.back(), (need + 31) & ~31)));
+        m->ck_val.push_back(hf[rk]);
+        ++k;
+      }
+    }
+    for (k = 1; k <= K; ++k) {
+      int32_t node = 0;
+      const int32_t q = m->ck_elem[k];
+      if (k == K) {
+        node = N;
+      } else if (q > 0) {
+        int32_t e = 0;
+        FL_TRY_CUDA(cudaMemcpy(&e, m->fz_perm.p + (q - 1), sizeof(int32_t), cudaMemcpyDeviceToHost));
+        FL_TRY_CUDA(cudaMemcpy(&node, maxv.p + e, sizeof(int32_t), cudaMemcpyDeviceToHost));
+        node += 1;
+      }
+      m->ck_node.push_back(std::max(m->ck_node.back(), node));
+    }
   }
   const int nE = (E + kFzItem - 1) / kFzItem, nR = (N + kFzItem - 1) / kFzItem;
   // need[j] = number of element items up to the last one row item j reads;
@@ -1184,17 +1239,18 @@ static int launch_pull_df10(const PullArgs& P, cudaStream_t s) {
   return FL_OK;
 }
 
-template <int THREADS, int RMAX, bool MASS>
+template <int THREADS, int RMAX, bool MASS, bool PERM>
 static int launch_pull_df(const PullArgs& P, cudaStream_t s) {
   const size_t smem = (size_t)RMAX * THREADS * sizeof(float2);
   static bool configured = false;
   if (!configured) {
-    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df<THREADS, RMAX, MASS>,
+    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df<THREADS, RMAX, MASS, PERM>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured = true;
   }
-  const unsigned grid = (unsigned)((P.N + THREADS - 1) / THREADS);
-  k_rows_pull_df<THREADS, RMAX, MASS><<<grid, THREADS, smem, s>>>(P);
+  const unsigned grid = (unsigned)((P.N - P.row0 + THREADS - 1) / THREADS);
+  if (grid == 0) return FL_OK;
+  k_rows_pull_df<THREADS, RMAX, MASS, PERM><<<grid, THREADS, smem, s>>>(P);
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
@@ -1281,16 +1337,16 @@ __global__ void k_dirichlet(int32_t nb, const int32_t* __restrict__ nodes, int32
 // are sized to the mesh's longest row; longer rows, if any, accumulate in
 // place in val.  Every row is summed by one thread in incidence order, so the
 // tile changes no result.
-template <bool MASS>
+template <bool MASS, bool PERM = false>
 static int launch_rows_p1_df(const PullArgs& P, int max_row, int tile, cudaStream_t s) {
   if (max_row <= 16) {
-    if (tile == 0) return launch_pull_df<64, 16, MASS>(P, s);
-    if (tile == 2) return launch_pull_df<256, 16, MASS>(P, s);
-    return launch_pull_df<128, 16, MASS>(P, s);
+    if (tile == 0) return launch_pull_df<64, 16, MASS, PERM>(P, s);
+    if (tile == 2) return launch_pull_df<256, 16, MASS, PERM>(P, s);
+    return launch_pull_df<128, 16, MASS, PERM>(P, s);
   }
-  if (tile == 0) return launch_pull_df<64, 32, MASS>(P, s);
-  if (tile == 2) return launch_pull_df<256, 32, MASS>(P, s);
-  return launch_pull_df<128, 32, MASS>(P, s);
+  if (tile == 0) return launch_pull_df<64, 32, MASS, PERM>(P, s);
+  if (tile == 2) return launch_pull_df<256, 32, MASS, PERM>(P, s);
+  return launch_pull_df<128, 32, MASS, PERM>(P, s);
 }
 
 static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int max_row, int tile, cudaStream_t s,
@@ -1399,6 +1455,54 @@ int dirichlet_launch(fl_mesh_t* m, int32_t nb, const int32_t* nodes, int32_t bas
   return FL_OK;
 }
 
+// Arguments of the P1 double-float element pass (records into em) and its
+// term-set key: mass 8, source 4, old field 2, anisotropic kappa 1.
+static int p1_df_args(const fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* em, DfArgs& D) {
+  RefTensors h;
+  build_tensors(1, p->quad_degree, h);
+  const double theta_dt = p->dt * p->theta;
+  const bool use_dt = fabs(theta_dt) > 2.220446049250313e-16;
+  D = DfArgs{};
+  D.E = m->E;
+  D.nd = m->ndglno.p;
+  D.xnd = m->xndglno.p;
+  D.X = m->coords.p;
+  D.t = f->t;
+  D.f = f->source;
+  D.em = reinterpret_cast<float2*>(em);
+  const double kap = p->isotropic_diffusivity ? p->diffusivity[0] : 1.0;
+  D.kscale = df_host(h.wsum * (use_dt ? theta_dt : 0.0) * kap);
+  D.rscale = df_host(h.wsum * kap);
+  D.aniso = p->isotropic_diffusivity ? 0 : 1;
+  for (int a = 0; a < 3; ++a) D.kdiag[a] = df_host(p->isotropic_diffusivity ? 1.0 : p->diffusivity[4 * a]);
+  D.m0 = df_host(h.M[0][0]);
+  D.m1 = df_host(h.M[0][1]);
+  D.have_mass = p->have_mass;
+  D.have_src = p->have_source;
+  return (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
+}
+
+// Record staging of the P1 double-float element pass: 4 or 6 kB per warp.
+static size_t p1_df_stage_bytes(int threads, bool mass) {
+  return (size_t)(threads / 32) * 32 * (mass ? 12 : 8) * sizeof(float4);
+}
+
+static void launch_p1_df_elems(int key, unsigned g, int eb, size_t smem, const DfArgs& D, cudaStream_t s) {
+  switch (key) {
+#define FL_DF_CASE(K, M, S, T, AN) \
+  case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, smem, s>>>(D); break;
+    FL_DF_CASE(0, false, false, false, false) FL_DF_CASE(1, false, false, false, true)
+    FL_DF_CASE(2, false, false, true, false) FL_DF_CASE(3, false, false, true, true)
+    FL_DF_CASE(4, false, true, false, false) FL_DF_CASE(5, false, true, false, true)
+    FL_DF_CASE(6, false, true, true, false) FL_DF_CASE(7, false, true, true, true)
+    FL_DF_CASE(8, true, false, false, false) FL_DF_CASE(9, true, false, false, true)
+    FL_DF_CASE(10, true, false, true, false) FL_DF_CASE(11, true, false, true, true)
+    FL_DF_CASE(12, true, true, false, false) FL_DF_CASE(13, true, true, false, true)
+    FL_DF_CASE(14, true, true, true, false) FL_DF_CASE(15, true, true, true, true)
+#undef FL_DF_CASE
+  }
+}
+
 int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double* val, double* rhs,
              cudaStream_t s, double* em_override, bool host_out) {
   FL_CHECK_ARG(m && p && f && val && rhs, "null argument");
@@ -1497,28 +1601,10 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     }
     k_asm_p2_diffusion_df<<<grid_for(m->E, kP2Threads, esm), kP2Threads, dsmem, s>>>(D);
   } else if (use_df) {
-    RefTensors h;
-    build_tensors(1, p->quad_degree, h);
     DfArgs D{};
-    D.E = m->E;
-    D.nd = m->ndglno.p;
-    D.xnd = m->xndglno.p;
-    D.X = m->coords.p;
-    D.t = f->t;
-    D.f = f->source;
-    D.em = reinterpret_cast<float2*>(em);
-    const double kap = p->isotropic_diffusivity ? p->diffusivity[0] : 1.0;
-    D.kscale = df_host(h.wsum * (A.use_dt ? A.theta_dt : 0.0) * kap);
-    D.rscale = df_host(h.wsum * kap);
-    D.aniso = p->isotropic_diffusivity ? 0 : 1;
-    for (int a = 0; a < 3; ++a) D.kdiag[a] = df_host(p->isotropic_diffusivity ? 1.0 : p->diffusivity[4 * a]);
-    D.m0 = df_host(h.M[0][0]);
-    D.m1 = df_host(h.M[0][1]);
-    D.have_mass = p->have_mass;
-    D.have_src = p->have_source;
+    const int key = p1_df_args(m, p, f, em, D);
     const unsigned g = grid_for(m->E, eb, esm);
-    const size_t smem = (size_t)(eb / 32) * 32 * (p->have_mass ? 12 : 8) * sizeof(float4);  // 4 or 6 kB per warp
-    const int key = (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
+    const size_t smem = p1_df_stage_bytes(eb, p->have_mass);
     if (m->tile_rows == 3 && !em_override) {
       // fused element + row pass (same sums, records kept in L2)
       FL_TRY(fused_plan(m, s));
@@ -1545,19 +1631,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
         return FL_OK;
       }
     }
-    switch (key) {
-#define FL_DF_CASE(K, M, S, T, AN) \
-  case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, smem, s>>>(D); break;
-      FL_DF_CASE(0, false, false, false, false) FL_DF_CASE(1, false, false, false, true)
-      FL_DF_CASE(2, false, false, true, false) FL_DF_CASE(3, false, false, true, true)
-      FL_DF_CASE(4, false, true, false, false) FL_DF_CASE(5, false, true, false, true)
-      FL_DF_CASE(6, false, true, true, false) FL_DF_CASE(7, false, true, true, true)
-      FL_DF_CASE(8, true, false, false, false) FL_DF_CASE(9, true, false, false, true)
-      FL_DF_CASE(10, true, false, true, false) FL_DF_CASE(11, true, false, true, true)
-      FL_DF_CASE(12, true, true, false, false) FL_DF_CASE(13, true, true, false, true)
-      FL_DF_CASE(14, true, true, true, false) FL_DF_CASE(15, true, true, true, true)
-#undef FL_DF_CASE
-    }
+    launch_p1_df_elems(key, g, eb, smem, D, s);
   } else if (closed) {
     k_asm_p1_diffusion<<<grid_for(m->E, eb, esm), eb, 0, s>>>(A);
   } else if (loc == 4) {
@@ -1573,6 +1647,112 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
     m->timed = true;
   }
+  return FL_OK;
+}
+
+// Pinned host outputs of the P1 double-float forms: the assembly runs in the
+// row chunks of the fused plan on three streams.  The copy stream uploads
+// each chunk's field values and takes each finished chunk's val and rhs
+// ranges back; the element pass of chunk k+1 (stream s) runs beside the row
+// pass of chunk k (the row stream).  The host link, the bound of this call,
+// so starts after the first (small) chunk instead of after the whole
+// assembly.  Element records sit in the fused plan's order and the row pass
+// reads them through its slice map, summing every row in the same order as
+// the device path: val and rhs are bit-identical to it.  *done stays false
+// (nothing enqueued) when the mesh or the form does not take this path.  The
+// caller synchronises the copy and row streams before the host arrays are
+// used.
+static int assemble_pipelined(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* hf, double* hval,
+                              double* hrhs, cudaStream_t s, bool* done) {
+  *done = false;
+  if (!(use_p1_closed_form(m, p) && diagonal_kappa(p))) return FL_OK;
+  FL_CHECK_ARG(!p->have_source || hf->source, "source field missing");
+  FL_TRY(fused_plan(m, s));
+  const int K = (int)m->ck_rows.size() - 1;
+  if (m->fz_state != 1 || K < 2) return FL_OK;
+  FL_TRY(m->em.reserve(assembly_scratch_doubles(m, p)));
+  FL_TRY(m->st_val.reserve(m->nnz));
+  FL_TRY(m->st_rhs.reserve(m->N));
+  for (cudaStream_t& q : m->ck_streams)
+    if (!q) FL_TRY_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+  // events: [k] rows of chunk k written, [K+k] its fields uploaded, [2K+k]
+  // its element records written, [3K] the call's start, [3K+1] all rows
+  while ((int)m->ck_ev.size() < 3 * K + 2) {
+    cudaEvent_t e = nullptr;
+    FL_TRY_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    m->ck_ev.push_back(e);
+  }
+  cudaEvent_t* ev = m->ck_ev.data();
+  const cudaStream_t cs = m->ck_streams[0], rs = m->ck_streams[1];
+  // the copy and row streams follow the work already on s (earlier calls'
+  // use of the staging buffers and records)
+  FL_TRY_CUDA(cudaEventRecord(ev[3 * K], s));
+  for (cudaStream_t q : m->ck_streams) FL_TRY_CUDA(cudaStreamWaitEvent(q, ev[3 * K], 0));
+  fl_fields f{nullptr, nullptr, nullptr, nullptr};
+  const double* src = p->have_source ? hf->source : nullptr;
+  if (src) FL_TRY(m->st_src.reserve(m->N));
+  if (hf->t) FL_TRY(m->st_t.reserve(m->N));
+  f.source = src ? m->st_src.p : nullptr;
+  f.t = hf->t ? m->st_t.p : nullptr;
+  for (int k = 0; k < K; ++k) {
+    const int32_t a = m->ck_node[k], b = m->ck_node[k + 1];
+    if (b > a) {
+      if (src)
+        FL_TRY_CUDA(cudaMemcpyAsync(m->st_src.p + a, src + a, sizeof(double) * (size_t)(b - a),
+                                    cudaMemcpyHostToDevice, cs));
+      if (hf->t)
+        FL_TRY_CUDA(cudaMemcpyAsync(m->st_t.p + a, hf->t + a, sizeof(double) * (size_t)(b - a),
+                                    cudaMemcpyHostToDevice, cs));
+    }
+    FL_TRY_CUDA(cudaEventRecord(ev[K + k], cs));
+  }
+  DfArgs D{};
+  const int key = p1_df_args(m, p, &f, m->em.p, D);
+  D.perm = m->fz_perm.p;
+  const int eb = m->tile_elem_block, esm = m->tile_elem_per_sm;
+  const int tile = m->tile_rows == 3 ? 1 : m->tile_rows;
+  const size_t smem = p1_df_stage_bytes(eb, p->have_mass);
+  PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->fz_rec.p, m->ne_pos.p, m->ndglno.p, m->findrm.p,
+             m->colm.p, m->em.p, m->st_val.p, m->st_rhs.p, m->err.p, 0, 0};
+  if (m->timing) {
+    if (!m->ev0) {
+      FL_TRY_CUDA(cudaEventCreate(&m->ev0));
+      FL_TRY_CUDA(cudaEventCreate(&m->ev1));
+    }
+    FL_TRY_CUDA(cudaEventRecord(m->ev0, s));
+  }
+  for (int k = 0; k < K; ++k) {
+    D.p0 = m->ck_elem[k];
+    D.E = m->ck_elem[k + 1];
+    FL_TRY_CUDA(cudaStreamWaitEvent(s, ev[K + k], 0));
+    if (D.E > D.p0) launch_p1_df_elems(key, grid_for(D.E - D.p0, eb, esm), eb, smem, D, s);
+    FL_TRY_CUDA(cudaGetLastError());
+    FL_TRY_CUDA(cudaEventRecord(ev[2 * K + k], s));
+    FL_TRY_CUDA(cudaStreamWaitEvent(rs, ev[2 * K + k], 0));
+    P.row0 = m->ck_rows[k];
+    P.N = m->ck_rows[k + 1];
+    if (p->have_mass) {
+      FL_TRY((launch_rows_p1_df<true, true>(P, m->max_row, tile, rs)));
+    } else {
+      FL_TRY((launch_rows_p1_df<false, true>(P, m->max_row, tile, rs)));
+    }
+    FL_TRY_CUDA(cudaEventRecord(ev[k], rs));
+    FL_TRY_CUDA(cudaStreamWaitEvent(cs, ev[k], 0));
+    const int64_t v0 = m->ck_val[k], v1 = m->ck_val[k + 1];
+    if (v1 > v0)
+      FL_TRY_CUDA(cudaMemcpyAsync(hval + v0, m->st_val.p + v0, sizeof(double) * (size_t)(v1 - v0),
+                                  cudaMemcpyDeviceToHost, cs));
+    FL_TRY_CUDA(cudaMemcpyAsync(hrhs + P.row0, m->st_rhs.p + P.row0, sizeof(double) * (size_t)(P.N - P.row0),
+                                cudaMemcpyDeviceToHost, cs));
+  }
+  // s (error word, timing, the next call) follows the row stream
+  FL_TRY_CUDA(cudaEventRecord(ev[3 * K + 1], rs));
+  FL_TRY_CUDA(cudaStreamWaitEvent(s, ev[3 * K + 1], 0));
+  if (m->timing) {
+    FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
+    m->timed = true;
+  }
+  *done = true;
   return FL_OK;
 }
 
@@ -1685,7 +1865,23 @@ extern "C" int fl_gpu_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, c
   // of following it.  Pageable arrays go through device staging buffers.
   double* mval = mapped_host(val);
   double* mrhs = mval ? mapped_host(rhs) : nullptr;
-  if (!mrhs) {
+  if (mrhs) {
+    // P1 double-float forms: chunked uploads, assembly and copies back
+    bool done = false;
+    int st = assemble_pipelined(m, p, f, val, rhs, s, &done);
+    if (st == FL_OK && done) st = check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
+    // row passes and copies still in flight (also after an error) end
+    // before the caller's arrays are touched
+    for (cudaStream_t q : m->ck_streams) {
+      if (!q) continue;
+      const cudaError_t e = cudaStreamSynchronize(q);
+      if (st == FL_OK && e != cudaSuccess) {
+        set_error("pipelined assembly: %s", cudaGetErrorString(e));
+        st = FL_ERR_CUDA;
+      }
+    }
+    if (st != FL_OK || done) return st;
+  } else {
     FL_TRY(m->st_val.reserve(m->nnz));
     FL_TRY(m->st_rhs.reserve(m->N));
   }
@@ -1703,8 +1899,7 @@ extern "C" int fl_gpu_assemble_advdif_cg(fl_mesh m, const fl_advdif_params* p, c
   FL_TRY(up(p->have_absorption ? f->absorption : nullptr, m->st_abs, m->N, &df.absorption));
   if (mrhs) {
     FL_TRY(assemble(m, p, &df, mval, mrhs, s, nullptr, true));
-    FL_TRY(check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern"));
-    return FL_OK;
+    return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
   }
   FL_TRY(fl_dev_assemble_advdif_cg(m, p, &df, m->st_val.p, m->st_rhs.p, s));
   FL_TRY_CUDA(cudaMemcpyAsync(val, m->st_val.p, sizeof(double) * m->nnz, cudaMemcpyDeviceToHost, s));

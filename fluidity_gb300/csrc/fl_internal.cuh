@@ -201,6 +201,15 @@ struct fl_mesh_t {
   int fz_state = 0;                  // 0 not built, 1 built, -1 not applicable
   int32_t fz_nitems = 0;
   fl::DevBuf<int32_t> fz_perm, fz_rec, fz_items, fz_need, fz_ctl;
+  // pipelined P1 assembly into pinned host arrays (built with the fused plan):
+  // row chunk k = rows [ck_rows[k], ck_rows[k+1]) needs the records at element
+  // positions below ck_elem[k+1], which read field values below ck_node[k+1];
+  // its entries are val[ck_val[k], ck_val[k+1])
+  std::vector<int32_t> ck_rows, ck_elem, ck_node;
+  std::vector<int64_t> ck_val;
+  // copy stream (field uploads, result copies) and row-pass stream
+  cudaStream_t ck_streams[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> ck_ev;  // per chunk: rows written, fields uploaded, records written
   struct fl_mesh_t* so_parent = nullptr;  // second-order pattern handles: the mesh they square
   fl::DevBuf<float2> bt;                  // second-order handles: transposed product operand
   fl::DevBuf<int32_t> pair_off;           // second-order handles: pairs of each first-order entry

@@ -749,6 +749,12 @@ extern "C" int fl_gpu_mesh_destroy(fl_mesh m) {
   release_krylov_work(m);
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
+  for (cudaStream_t q : m->ck_streams)
+    if (q) {
+      cudaStreamSynchronize(q);
+      cudaStreamDestroy(q);
+    }
+  for (cudaEvent_t e : m->ck_ev) cudaEventDestroy(e);
   cudaStreamDestroy(m->stream);
   delete m;
   return FL_OK;

@@ -168,3 +168,40 @@ def test_host_pointer_assembly_pinned_and_pageable(n):
     assert np.array_equal(pv, dval) and np.array_equal(pr, drhs)
     hv, hr = ft.assemble_advection_diffusion_cg(m, p, source=src)
     assert np.array_equal(hv, dval) and np.array_equal(hr, drhs)
+
+
+@pytest.mark.parametrize("case", ["poisson", "anisotropic", "diffusion_mass_t", "shuffled"])
+def test_host_pointer_pipelined_chunks(case):
+    """Pinned outputs of the P1 double-float forms on a 64^3 mesh (32 MB of
+    val) are assembled in row chunks, elements in highest-node order, each
+    chunk's val and rhs copied to the host while later chunks run: the device
+    path's bits, also under a random node numbering (chunks that need almost
+    every element) and with consistent mass and old-field terms."""
+    import torch
+    nd, X = M.cube_mesh(64)
+    if case == "shuffled":
+        perm = np.random.default_rng(17).permutation(len(X))
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(len(X))
+        nd, X = perm[nd].astype(nd.dtype), X[inv]
+    spec = {"poisson": CASES["poisson"], "anisotropic": CASES["anisotropic"], "shuffled": CASES["poisson"],
+            "diffusion_mass_t": dict(theta=0.5, dt=0.01, have_mass=True, T=True, diffusivity=1e-3,
+                                     source=True)}[case]
+    fl = _fields(X, spec)
+    kw = dict(source=fl.get("source"), t=fl.get("T"))
+    m = ft.Mesh(nd, X)
+    p = _params(spec, 2)
+    dkw = {k: (torch.tensor(v, device="cuda") if v is not None else None) for k, v in kw.items()}
+    dval, drhs = ft.assemble_advection_diffusion_cg(m, p, **dkw)
+    dval, drhs = dval.cpu().numpy(), drhs.cpu().numpy()
+    pv = torch.empty(m.nnz, dtype=torch.float64).pin_memory().numpy()
+    pr = torch.empty(m.N, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(2):
+        pv[:] = np.nan
+        pr[:] = np.nan
+        k0 = ft.kernel_launch_count()
+        ft.assemble_advection_diffusion_cg(m, p, val=pv, rhs=pr, **kw)
+        launches = ft.kernel_launch_count() - k0
+        assert np.array_equal(pv, dval) and np.array_equal(pr, drhs)
+    assert launches >= 8  # an element and a row launch per chunk
+    m.close()
