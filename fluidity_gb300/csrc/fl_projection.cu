@@ -535,21 +535,31 @@ struct RowProdArgs {
 };
 
 // Double-float arithmetic on the FP32 pipes (GB300's FP64 rate is 1/60 of
-// FP32).  One half-warp per output row i (two rows per warp): the lanes first
-// load the row's k data (column k, c_d = a_d(i,k) w_d(k) or a(i,k) / s(k),
-// the extent of row k) in one round, then walk the k in ascending order with
-// the next k's operand loads issued before the current k is summed; a lane
-// owns one entry (k, j) of row k, adds c . bt(k, j) to the slot of j in the
-// output row (shared memory, double-float), and the k are added one after
-// the other, so every sum has a fixed order.  Rows of more than 16 entries
-// take their k in groups of 16, and so do columns longer than 16.
+// FP32).  One half-warp per output row i (two rows per warp).  The k of row
+// i go in groups of 16: each lane loads one k's data (column k, the extent and
+// pair offset of row k, c_d = a_d(i,k) w_d(k) or a(i,k) / s(k)) into shared
+// memory, then the half-warp walks the group's k in ascending order, reading
+// each k's data as a shared-memory broadcast.  In step k, lane t owns entry t
+// of row k, (k, j), and adds c . bt(k, j) to the slot of j in the output row
+// (shared memory, double-float); the k are added one after the other, so
+// every sum has a fixed order.  The step has no branch: lanes past the end of
+// row k read the first entry and add into a dummy slot.  A group holding a
+// row k longer than 16 entries takes the general loop over its entries in
+// runs of 16.
 template <int NDIM, bool DIV>
 __global__ void __launch_bounds__(kPW * 32, 4) k_rowprod(RowProdArgs P) {
   note_launch();
-  __shared__ float2 s_acc_all[2 * kPW][kPCap];
+  __shared__ float2 s_acc_all[2 * kPW][kPCap + 1];  // + one dummy slot
+  __shared__ int4 s_k_all[2 * kPW][16];              // {row start, extent, pair offset, -}
+  __shared__ float2 s_c_all[2 * kPW][NDIM][16];
   const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
   const int hw = (threadIdx.x >> 5) * 2 + half;  // half-warp index in the block
   float2* s_acc = s_acc_all[hw];
+  int4* s_k = s_k_all[hw];
+  float2 (*s_c)[16] = s_c_all[hw];
+  const float2* bt[NDIM];
+#pragma unroll
+  for (int d = 0; d < NDIM; ++d) bt[d] = P.bt + d * P.annz;
   const int nrow_steps = (P.n + 2 * kPW * gridDim.x - 1) / (2 * kPW * gridDim.x);
   for (int it = 0; it < nrow_steps; ++it) {
     const int row = (it * gridDim.x + blockIdx.x) * 2 * kPW + hw;
@@ -571,14 +581,13 @@ __global__ void __launch_bounds__(kPW * 32, 4) k_rowprod(RowProdArgs P) {
     const int nk = qe - qb;
     const int nk_max = max(nk, __shfl_xor_sync(0xffffffffu, nk, 16));
     for (int g0 = 0; g0 < nk_max; g0 += 16) {
-      // this group's k data, one k per lane
+      // this group's k data, one k per lane, into shared memory
       const int qg = qb + g0 + hl;
-      const bool kact = qg < qe;
       int kb = 0, klen = 0, po = 0;
       df c[NDIM];
 #pragma unroll
       for (int d = 0; d < NDIM; ++d) c[d] = {0.0f, 0.0f};
-      if (kact) {
+      if (qg < qe) {
         const int k = __ldg(P.acol + qg);
         kb = __ldg(P.aptr + k);
         klen = __ldg(P.aptr + k + 1) - kb;
@@ -593,69 +602,95 @@ __global__ void __launch_bounds__(kPW * 32, 4) k_rowprod(RowProdArgs P) {
             c[d] = df_mul(df_from_double(__ldg(P.a[d] + qg)), df_from_double(__ldg(P.w + NDIM * k + d)));
         }
       }
+      s_k[hl] = make_int4(kb, klen, po, 0);
+#pragma unroll
+      for (int d = 0; d < NDIM; ++d) s_c[d][hl] = make_float2(c[d].hi, c[d].lo);
+      int lmax = klen;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) lmax = max(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+      __syncwarp();
       const int gn = min(16, nk_max - g0);
-      // operand loads of step u: lane hl takes entry hl (+16 m) of column k_u
-      int u_kb = __shfl_sync(0xffffffffu, kb, 0, 16), u_len = __shfl_sync(0xffffffffu, klen, 0, 16);
-      int u_po = __shfl_sync(0xffffffffu, po, 0, 16);
-      int nslot = 0;
-      float2 nb[NDIM];
-#pragma unroll
-      for (int d = 0; d < NDIM; ++d) nb[d] = make_float2(0.0f, 0.0f);
-      if (hl < u_len) {
-        nslot = __ldg(P.pmap + u_po + hl);
-#pragma unroll
-        for (int d = 0; d < NDIM; ++d) nb[d] = __ldg(P.bt + d * P.annz + u_kb + hl);
-      }
-      for (int u = 0; u < gn; ++u) {
-        const int slot = nslot;
+      if (lmax <= 16) {
+        // step u's slot and operands are loaded during step u-1's arithmetic
+        int slot;
         float2 b[NDIM];
+        {
+          const int4 kk = s_k[0];
+          const bool ok = hl < kk.y;
+          slot = ok ? (int)__ldg(P.pmap + kk.z + hl) : kPCap;
+          const int idx = kk.x + (ok ? hl : 0);
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) b[d] = nb[d];
-        const int len = u_len, kbu = u_kb, pou = u_po;
-        df cu[NDIM];
-#pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-          cu[d].hi = __shfl_sync(0xffffffffu, c[d].hi, u, 16);
-          cu[d].lo = __shfl_sync(0xffffffffu, c[d].lo, u, 16);
+          for (int d = 0; d < NDIM; ++d) b[d] = __ldg(bt[d] + idx);
         }
-        // issue the next step's loads before this step's arithmetic
-        if (u + 1 < gn) {
-          u_kb = __shfl_sync(0xffffffffu, kb, u + 1, 16);
-          u_len = __shfl_sync(0xffffffffu, klen, u + 1, 16);
-          u_po = __shfl_sync(0xffffffffu, po, u + 1, 16);
-          if (hl < u_len) {
-            nslot = __ldg(P.pmap + u_po + hl);
+        for (int u = 0; u < gn; ++u) {
+          int nslot = kPCap;
+          float2 nb[NDIM];
 #pragma unroll
-            for (int d = 0; d < NDIM; ++d) nb[d] = __ldg(P.bt + d * P.annz + u_kb + hl);
+          for (int d = 0; d < NDIM; ++d) nb[d] = b[d];
+          if (u + 1 < gn) {
+            const int4 kk = s_k[u + 1];
+            const bool ok = hl < kk.y;
+            nslot = ok ? (int)__ldg(P.pmap + kk.z + hl) : kPCap;
+            const int idx = kk.x + (ok ? hl : 0);
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) nb[d] = __ldg(bt[d] + idx);
           }
-        }
-        for (int m0 = 0; m0 < len; m0 += 16) {
-          int sl = slot;
-          float2 bb[NDIM];
+          df v;
+          if (NDIM == 3) {
+            const float2 c0 = s_c[0][u], c1 = s_c[NDIM > 1 ? 1 : 0][u], c2 = s_c[NDIM > 2 ? 2 : 0][u];
+            v = df_dot3({c0.x, c0.y}, {b[0].x, b[0].y}, {c1.x, c1.y}, {b[NDIM > 1 ? 1 : 0].x, b[NDIM > 1 ? 1 : 0].y},
+                        {c2.x, c2.y}, {b[NDIM > 2 ? 2 : 0].x, b[NDIM > 2 ? 2 : 0].y});
+          } else {
+            const float2 c0 = s_c[0][u];
+            v = df_mul({c0.x, c0.y}, {b[0].x, b[0].y});
 #pragma unroll
-          for (int d = 0; d < NDIM; ++d) bb[d] = b[d];
-          if (m0 > 0 && m0 + hl < len) {  // columns longer than 16: the further entries
-            sl = __ldg(P.pmap + pou + m0 + hl);
-#pragma unroll
-            for (int d = 0; d < NDIM; ++d) bb[d] = __ldg(P.bt + d * P.annz + kbu + m0 + hl);
-          }
-          if (m0 + hl < len) {
-            df v;
-            if (NDIM == 3)
-              v = df_dot3(cu[0], {bb[0].x, bb[0].y}, cu[NDIM > 1 ? 1 : 0], {bb[NDIM > 1 ? 1 : 0].x, bb[NDIM > 1 ? 1 : 0].y},
-                          cu[NDIM > 2 ? 2 : 0], {bb[NDIM > 2 ? 2 : 0].x, bb[NDIM > 2 ? 2 : 0].y});
-            else {
-              v = df_mul(cu[0], {bb[0].x, bb[0].y});
-#pragma unroll
-              for (int d = 1; d < NDIM; ++d) v = df_add(v, df_mul(cu[d], {bb[d].x, bb[d].y}));
+            for (int d = 1; d < NDIM; ++d) {
+              const float2 cd = s_c[d][u];
+              v = df_add(v, df_mul({cd.x, cd.y}, {b[d].x, b[d].y}));
             }
-            const float2 o = s_acc[sl];
-            const df sum = df_add({o.x, o.y}, v);
-            s_acc[sl] = make_float2(sum.hi, sum.lo);
+          }
+          const float2 o = s_acc[slot];
+          const df sum = df_add({o.x, o.y}, v);
+          s_acc[slot] = make_float2(sum.hi, sum.lo);
+          __syncwarp();  // the next k may add to the same slots from other lanes
+          slot = nslot;
+#pragma unroll
+          for (int d = 0; d < NDIM; ++d) b[d] = nb[d];
+        }
+      } else {
+        for (int u = 0; u < gn; ++u) {
+          const int4 kk = s_k[u];
+          df cu[NDIM];
+#pragma unroll
+          for (int d = 0; d < NDIM; ++d) cu[d] = {s_c[d][u].x, s_c[d][u].y};
+          for (int m0 = 0; m0 < kk.y; m0 += 16) {
+            const int e = m0 + hl;
+            if (e < kk.y) {
+              const int sl = __ldg(P.pmap + kk.z + e);
+              df v;
+              if (NDIM == 3) {
+                const float2 b0 = __ldg(bt[0] + kk.x + e), b1 = __ldg(bt[NDIM > 1 ? 1 : 0] + kk.x + e),
+                             b2 = __ldg(bt[NDIM > 2 ? 2 : 0] + kk.x + e);
+                v = df_dot3(cu[0], {b0.x, b0.y}, cu[NDIM > 1 ? 1 : 0], {b1.x, b1.y}, cu[NDIM > 2 ? 2 : 0],
+                            {b2.x, b2.y});
+              } else {
+                const float2 b0 = __ldg(bt[0] + kk.x + e);
+                v = df_mul(cu[0], {b0.x, b0.y});
+#pragma unroll
+                for (int d = 1; d < NDIM; ++d) {
+                  const float2 bd = __ldg(bt[d] + kk.x + e);
+                  v = df_add(v, df_mul(cu[d], {bd.x, bd.y}));
+                }
+              }
+              const float2 o = s_acc[sl];
+              const df sum = df_add({o.x, o.y}, v);
+              s_acc[sl] = make_float2(sum.hi, sum.lo);
+            }
+            __syncwarp(0xffffu << (half * 16));
           }
         }
-        __syncwarp();
       }
+      __syncwarp();
     }
     for (int t = hl; t < L; t += 16) {
       const float2 o = s_acc[t];
