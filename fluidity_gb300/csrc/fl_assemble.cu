@@ -1161,80 +1161,98 @@ static int launch_fused(fl_mesh_t* m, const DfArgs& D, const PullArgs& P, cudaSt
 
 // Row pass of the P2 double-float records: slice (element, local row) =
 // 6 float4 {K_a0..K_a9, r_a, 0} at (local row) E + element; the row
-// positions of the ten element nodes
-// come from three ne_pos words per incidence.  Incidences are taken two at a
-// time (loads first, then the adds in colour order).
-template <int THREADS, int RMAX>
-__global__ void __launch_bounds__(THREADS) k_rows_pull_df10(PullArgs P) {
+// positions of the ten element nodes come from three ne_pos words per
+// incidence.  One half-warp per row: in each incidence step
+// lane b (0..9) adds K_ab into the slot of node b's column and lane 10 takes
+// r_a, so a row's accumulators (shared memory, up to kP2HwSlots entries; longer
+// rows add into val) cost one row's worth of shared memory, not one per
+// thread, and the row's val range is stored with coalesced stores.  The
+// incidences go in colour order and the ten positions of one incidence are
+// distinct, so every entry is summed in colour order, as one thread per row
+// would.  The next incidence's index and positions are loaded during the
+// current step.
+constexpr int kP2HwSlots = 128;
+constexpr int kP2HwWarps = 8;
+
+__global__ void __launch_bounds__(kP2HwWarps * 32) k_rows_p2_hw(PullArgs P) {
   note_launch();
-  extern __shared__ unsigned char smem_raw[];
-  float2* acc = reinterpret_cast<float2*>(smem_raw);  // [RMAX][THREADS]
-  const float4* rec = reinterpret_cast<const float4*>(P.em);
-  const int t = threadIdx.x;
-  for (int row = blockIdx.x * THREADS + t; row < P.N; row += gridDim.x * THREADS) {
-    const int base = __ldg(P.findrm + row), L = __ldg(P.findrm + row + 1) - base;
-    const bool in_smem = L <= RMAX;
-    if (in_smem) {
-      for (int k = 0; k < L; ++k) acc[k * THREADS + t] = make_float2(0.0f, 0.0f);
-    } else {
-      for (int k = 0; k < L; ++k) P.val[base + k] = 0.0;
+  __shared__ float2 acc_all[2 * kP2HwWarps][kP2HwSlots];
+  const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+  const int hw = (threadIdx.x >> 5) * 2 + half;
+  float2* acc = acc_all[hw];
+  const float2* rec = reinterpret_cast<const float2*>(P.em);  // slices of 12 pairs
+  const int nhw = gridDim.x * 2 * kP2HwWarps;
+  const int nsteps = (P.N + nhw - 1) / nhw;  // the same for every half-warp
+  for (int it = 0; it < nsteps; ++it) {
+    const int row = it * nhw + blockIdx.x * 2 * kP2HwWarps + hw;
+    const bool live = row < P.N;
+    int base = 0, L = 0, ib = 0, ie = 0;
+    if (live) {
+      base = __ldg(P.findrm + row);
+      L = __ldg(P.findrm + row + 1) - base;
+      ib = __ldg(P.ne_ptr + row);
+      ie = __ldg(P.ne_ptr + row + 1);
     }
+    const bool in_smem = L <= kP2HwSlots;
+    if (in_smem) {
+      for (int t = hl; t < L; t += 16) acc[t] = make_float2(0.0f, 0.0f);
+    } else {
+      for (int t = hl; t < L; t += 16) P.val[base + t] = 0.0;
+    }
+    __syncwarp();
+    const int n = ie - ib;
+    const int nmax = max(n, __shfl_xor_sync(0xffffffffu, n, 16));
     df r = {0.0f, 0.0f};
-    const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
-    for (int q0 = ib; q0 < ie; q0 += 2) {
-      int inc[2];
-      uint32_t pw[2][3];
-      float4 q[2][6];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const bool ok = q0 + u < ie;
-        inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
-#pragma unroll
-        for (int w = 0; w < 3; ++w) pw[u][w] = ok ? __ldg(P.ne_pos + (int64_t)(q0 + u) * 3 + w) : 0u;
-        // slice-major records: slice a of element e at (a E + e)
-        const uint32_t ri = 6u * ((uint32_t)(inc[u] & 15) * (uint32_t)P.E + (uint32_t)(inc[u] >> 4));
-#pragma unroll
-        for (int k = 0; k < 6; ++k) q[u][k] = ok ? __ldg(rec + ri + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool val_lane = hl < 10, rhs_lane = hl == 10;
+    int inc = 0;
+    uint32_t pw = 0u;
+    if (n > 0) {
+      inc = __ldg(P.ne_col + ib);
+      if (val_lane) pw = __ldg(P.ne_pos + (int64_t)ib * 3 + (hl >> 2));
+    }
+    for (int q = 0; q < nmax; ++q) {
+      const bool ok = q < n;
+      float2 v = make_float2(0.0f, 0.0f);
+      if (ok && (val_lane || rhs_lane)) {
+        const uint32_t slice = (uint32_t)(inc & 15) * (uint32_t)P.E + (uint32_t)(inc >> 4);
+        v = __ldg(rec + 12u * slice + hl);
       }
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (q0 + u >= ie) break;
-#pragma unroll
-        for (int b = 0; b < 10; ++b) {
-          const float4 c4 = q[u][b >> 1];
-          const df v = (b & 1) ? df{c4.z, c4.w} : df{c4.x, c4.y};
-          const int pos = (pw[u][b >> 2] >> (8 * (b & 3))) & 0xffu;
-          if (in_smem) {
-            const float2 c = acc[pos * THREADS + t];
-            const df sum = df_add({c.x, c.y}, v);
-            acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
-          } else {
-            P.val[base + pos] += df_to_double(v);
-          }
+      const uint32_t cpw = pw;
+      if (q + 1 < n) {
+        inc = __ldg(P.ne_col + ib + q + 1);
+        if (val_lane) pw = __ldg(P.ne_pos + (int64_t)(ib + q + 1) * 3 + (hl >> 2));
+      }
+      if (ok && val_lane) {
+        const int pos = (cpw >> (8 * (hl & 3))) & 0xffu;
+        if (in_smem) {
+          const float2 c = acc[pos];
+          const df sum = df_add({c.x, c.y}, {v.x, v.y});
+          acc[pos] = make_float2(sum.hi, sum.lo);
+        } else {
+          P.val[base + pos] += df_to_double({v.x, v.y});
         }
-        r = df_add(r, {q[u][5].x, q[u][5].y});
+      } else if (ok && rhs_lane) {
+        r = df_add(r, {v.x, v.y});
       }
+      __syncwarp();
     }
     if (in_smem)
-      for (int k = 0; k < L; ++k) {
-        const float2 c = acc[k * THREADS + t];
-        P.val[base + k] = df_to_double({c.x, c.y});
+      for (int t = hl; t < L; t += 16) {
+        const float2 c = acc[t];
+        P.val[base + t] = df_to_double({c.x, c.y});
       }
-    P.rhs[row] = df_to_double(r);
+    if (live && rhs_lane) P.rhs[row] = df_to_double(r);
+    __syncwarp();
   }
 }
 
-template <int THREADS, int RMAX>
-static int launch_pull_df10(const PullArgs& P, cudaStream_t s) {
-  const size_t smem = (size_t)RMAX * THREADS * sizeof(float2);
-  static bool configured = false;
-  if (!configured) {
-    FL_TRY_CUDA(cudaFuncSetAttribute(k_rows_pull_df10<THREADS, RMAX>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured = true;
-  }
-  const unsigned grid = (unsigned)((P.N + THREADS - 1) / THREADS);
-  k_rows_pull_df10<THREADS, RMAX><<<grid, THREADS, smem, s>>>(P);
+static int launch_rows_p2_hw(const PullArgs& P, cudaStream_t s) {
+  int per_sm = 0;
+  FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rows_p2_hw, kP2HwWarps * 32, 0));
+  const int rows_per_block = 2 * kP2HwWarps;
+  const unsigned grid = (unsigned)std::max(
+      1, std::min((P.N + rows_per_block - 1) / rows_per_block, num_sms() * std::max(1, per_sm)));
+  k_rows_p2_hw<<<grid, kP2HwWarps * 32, 0, s>>>(P);
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
@@ -1351,12 +1369,7 @@ static int launch_rows_p1_df(const PullArgs& P, int max_row, int tile, cudaStrea
 
 static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int max_row, int tile, cudaStream_t s,
                        bool mass = false) {
-  if (loc == 10 && use_df) {
-    if (max_row > 72) return launch_pull_df10<32, 128>(P, s);
-    if (tile == 0) return launch_pull_df10<32, 72>(P, s);
-    if (tile == 2) return launch_pull_df10<128, 72>(P, s);
-    return launch_pull_df10<64, 72>(P, s);
-  }
+  if (loc == 10 && use_df) return launch_rows_p2_hw(P, s);
   if (loc == 4 && use_df)
     return mass ? launch_rows_p1_df<true>(P, max_row, tile, s) : launch_rows_p1_df<false>(P, max_row, tile, s);
   if (loc == 4 && closed) {
