@@ -1176,11 +1176,15 @@ constexpr int kP2HwWarps = 8;
 
 __global__ void __launch_bounds__(kP2HwWarps * 32) k_rows_p2_hw(PullArgs P) {
   note_launch();
-  __shared__ float2 acc_all[2 * kP2HwWarps][kP2HwSlots];
+  // per row: kP2HwSlots accumulators, then the rhs slot and a dummy slot
+  __shared__ float2 acc_all[2 * kP2HwWarps][kP2HwSlots + 2];
   const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
   const int hw = (threadIdx.x >> 5) * 2 + half;
   float2* acc = acc_all[hw];
   const float2* rec = reinterpret_cast<const float2*>(P.em);  // slices of 12 pairs
+  constexpr int kRhs = kP2HwSlots, kDummy = kP2HwSlots + 1;
+  const bool val_lane = hl < 10, rhs_lane = hl == 10;
+  const int own = rhs_lane ? kRhs : kDummy;  // slot of lanes 10..15
   const int nhw = gridDim.x * 2 * kP2HwWarps;
   const int nsteps = (P.N + nhw - 1) / nhw;  // the same for every half-warp
   for (int it = 0; it < nsteps; ++it) {
@@ -1196,14 +1200,15 @@ __global__ void __launch_bounds__(kP2HwWarps * 32) k_rows_p2_hw(PullArgs P) {
     const bool in_smem = L <= kP2HwSlots;
     if (in_smem) {
       for (int t = hl; t < L; t += 16) acc[t] = make_float2(0.0f, 0.0f);
+      if (rhs_lane) acc[kRhs] = make_float2(0.0f, 0.0f);
     } else {
       for (int t = hl; t < L; t += 16) P.val[base + t] = 0.0;
     }
     __syncwarp();
     const int n = ie - ib;
     const int nmax = max(n, __shfl_xor_sync(0xffffffffu, n, 16));
+    const bool uniform = __all_sync(0xffffffffu, in_smem);
     df r = {0.0f, 0.0f};
-    const bool val_lane = hl < 10, rhs_lane = hl == 10;
     int inc = 0;
     uint32_t pw = 0u;
     if (n > 0) {
@@ -1212,35 +1217,40 @@ __global__ void __launch_bounds__(kP2HwWarps * 32) k_rows_p2_hw(PullArgs P) {
     }
     for (int q = 0; q < nmax; ++q) {
       const bool ok = q < n;
-      float2 v = make_float2(0.0f, 0.0f);
-      if (ok && (val_lane || rhs_lane)) {
-        const uint32_t slice = (uint32_t)(inc & 15) * (uint32_t)P.E + (uint32_t)(inc >> 4);
-        v = __ldg(rec + 12u * slice + hl);
-      }
+      const uint32_t slice = (uint32_t)(inc & 15) * (uint32_t)P.E + (uint32_t)(inc >> 4);
+      // lanes past 10 and steps past the row's end read the slice's first pair
+      float2 v = __ldg(rec + 12u * slice + (hl <= 10 ? hl : 0));
       const uint32_t cpw = pw;
       if (q + 1 < n) {
         inc = __ldg(P.ne_col + ib + q + 1);
         if (val_lane) pw = __ldg(P.ne_pos + (int64_t)(ib + q + 1) * 3 + (hl >> 2));
       }
-      if (ok && val_lane) {
-        const int pos = (cpw >> (8 * (hl & 3))) & 0xffu;
+      const int slot = !ok ? kDummy : val_lane ? (int)((cpw >> (8 * (hl & 3))) & 0xffu) : own;
+      if (uniform) {
+        // every lane adds into its slot (distinct for lanes 0..10)
+        const float2 c = acc[slot];
+        const df sum = df_add({c.x, c.y}, {v.x, v.y});
+        acc[slot] = make_float2(sum.hi, sum.lo);
+      } else if (ok && val_lane) {
         if (in_smem) {
-          const float2 c = acc[pos];
+          const float2 c = acc[slot];
           const df sum = df_add({c.x, c.y}, {v.x, v.y});
-          acc[pos] = make_float2(sum.hi, sum.lo);
+          acc[slot] = make_float2(sum.hi, sum.lo);
         } else {
-          P.val[base + pos] += df_to_double({v.x, v.y});
+          P.val[base + slot] += df_to_double({v.x, v.y});
         }
       } else if (ok && rhs_lane) {
         r = df_add(r, {v.x, v.y});
       }
       __syncwarp();
     }
-    if (in_smem)
+    if (in_smem) {
       for (int t = hl; t < L; t += 16) {
         const float2 c = acc[t];
         P.val[base + t] = df_to_double({c.x, c.y});
       }
+      if (uniform && rhs_lane) r = {acc[kRhs].x, acc[kRhs].y};
+    }
     if (live && rhs_lane) P.rhs[row] = df_to_double(r);
     __syncwarp();
   }
