@@ -160,9 +160,10 @@ typedef struct {
  * element's matrix and right-hand side into the csr_matrix values (pattern of
  * the handle) colour by colour, elements ascending within a colour, so the
  * sums are deterministic.  Host pointers: val(nnz), rhs(N).  With page-locked
- * val and rhs the P1 diffusion forms (diagonal diffusivity) run in row
- * chunks: field uploads, assembly and the copies of finished chunks back
- * overlap, and the results are the bits of the device entry point. */
+ * val and rhs, the P1 diffusion forms (diagonal diffusivity) on meshes of at
+ * least about 1 M matrix entries run in row chunks of about 4 MB of val:
+ * field uploads, assembly and the copies of finished chunks back overlap,
+ * and the results are the bits of the device entry point. */
 int fl_gpu_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
                               const fl_fields* fields, double* val, double* rhs);
 /* Device-pointer form of the same call (all field pointers device). */
