@@ -9,9 +9,15 @@
 * ``oracle_goldens.npz`` -- outputs of the CPU oracle on small inputs (sparsity,
   colouring, P2 numbering, assembled P1 Poisson / P1 advection-diffusion
   systems, a CG solve), so a change to the oracle is caught by the CPU suite.
+* ``projection_goldens.npz`` -- the oracle's pressure-projection pieces on the
+  2^3 six-tet cube: lumped mass, divergence matrix (both forms, surface terms
+  of every boundary-condition type), second-order pattern, C M_l^-1 C^T, KMK
+  (theta 1 and 0.7) and the projection vectors.
 
 Run from the repository root in an environment that has the reference checkout:
     python tests/golden/make_golden.py /root/reference
+(``--projection`` writes only the projection fixtures, which need no reference
+files.)
 """
 from __future__ import annotations
 
@@ -79,5 +85,57 @@ def main(ref_root: str) -> None:
     print("wrote fixtures to", HERE)
 
 
+def projection_inputs():
+    """Inputs of the projection fixtures (also used by the test that checks them)."""
+    from fluidity_gb300 import meshgen as M
+
+    nd, X = M.cube_mesh(2)
+    faces, fe = M.boundary_faces(nd)
+    rng = np.random.default_rng(20261204)
+    ty = np.zeros((len(faces), 3), np.int32)
+    ty[::5, 0] = 1   # weak Dirichlet in x
+    ty[1::5, 1] = 1  # weak Dirichlet in y
+    ty[2::7, 2] = 2  # no_normal_flow: face skipped
+    ty[3::4, 0] = 5  # prescribed normal flow
+    g = rng.random((len(faces), 3, 3))
+    mom = rng.random((X.shape[0], 3))
+    ctr = rng.random(X.shape[0])
+    dp = rng.random(X.shape[0])
+    return dict(nd=nd, X=X, faces=faces, face_ele=fe, bc_type=ty, bc_val=g, mom=mom, ctr=ctr, dp=dp,
+                u=M.advdif_velocity(X), bnodes=M.boundary_nodes(X))
+
+
+def projection_goldens(inp=None):
+    """The oracle's projection outputs on projection_inputs()."""
+    from oracle import oracle as O
+
+    inp = inp or projection_inputs()
+    nd, X = inp["nd"], inp["X"]
+    N = X.shape[0]
+    f, c, _ = O.make_sparsity(nd)
+    g = {}
+    g["ml"] = O.lumped_mass(nd, nd, X, N)
+    ct, rhs, dml, gml = O.assemble_divergence_p1(nd, X, f, c)
+    g["ct"], g["dml"] = ct, dml
+    ctb, rhsb, _, _ = O.assemble_divergence_p1(nd, X, f, c, by_parts=True, faces=inp["faces"],
+                                               face_ele=inp["face_ele"], bc_type=inp["bc_type"],
+                                               bc_val=inp["bc_val"])
+    g["ct_by_parts"], g["ct_rhs_by_parts"] = ctb, rhsb
+    sf, sc = O.sparsity_secondorder(f, c)
+    g["so_findrm"], g["so_colm"] = sf, sc
+    inv = np.repeat((1.0 / gml)[:, None], 3, axis=1)
+    inv[inp["bnodes"]] = 0.0
+    g["cmc"] = O.mult_div_vector_div_T(f, c, ct, inv, ct, sf, sc)
+    for name, theta in (("kmk1", 1.0), ("kmk07", 0.7)):
+        kt, kmk = O.assemble_kmk(nd, X, f, c, g["ml"], sf, sc, theta_pg=theta)
+        g[name + "_kt"], g[name] = kt, kmk
+    g["poisson_rhs"] = O.masslumped_poisson_rhs(f, c, ct, inp["mom"], inp["ctr"], inv, inp["u"], 0.1, 0.5)
+    g["corrected_u"] = O.correct_masslumped_velocity(f, c, ct, inv, inp["dp"], inp["u"])
+    return g
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if "--projection" not in sys.argv:
+        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    np.savez_compressed(os.path.join(HERE, "projection_goldens.npz"), **projection_goldens())
+    print("wrote projection fixtures to", HERE)

@@ -121,3 +121,27 @@ def test_boundary_faces_of_the_cube(n):
         P = X[f]
         on = [np.all(np.abs(P[:, a] - v) < 1e-14) for a in range(3) for v in (0.0, 1.0)]
         assert sum(on) == 1
+
+
+def test_projection_goldens():
+    """The oracle's projection pieces on the 2^3 cube reproduce the committed
+    fixtures (tests/golden/projection_goldens.npz, written by
+    tests/golden/make_golden.py --projection): integer arrays bit-exact,
+    values to 1e-14 of each array's largest magnitude."""
+    import importlib.util
+    import os
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(here, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    want = np.load(os.path.join(here, "projection_goldens.npz"))
+    got = mg.projection_goldens()
+    assert sorted(got) == sorted(want.files)
+    for k in want.files:
+        w, g = want[k], np.asarray(got[k])
+        assert g.shape == w.shape, k
+        if w.dtype.kind in "iu":
+            assert np.array_equal(g, w), k
+        else:
+            assert np.abs(g - w).max() <= 1e-14 * max(np.abs(w).max(), 1e-300), k
