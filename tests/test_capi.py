@@ -38,3 +38,25 @@ def test_every_entry_point_has_a_full_ctypes_signature():
         fn = getattr(lib, name)
         assert fn.argtypes is not None, name
         assert fn.restype is not None, name
+
+
+# Entry points whose null call is not an error: queries without arguments,
+# destroy of a null handle (a no-op, as free(NULL)), and the size of no batch.
+_NULL_OK = {"fl_last_error", "fl_kernel_launch_count", "fl_gnn_num_params", "fl_gpu_mesh_destroy",
+            "fl_batch_destroy", "fl_gnn_destroy", "fl_amg_destroy", "fl_batch_size"}
+
+
+def test_null_arguments_are_usage_errors():
+    """Every entry point given null pointers and zero sizes returns the usage
+    error status (1, where the reference aborts with FLAbort) and a message,
+    before any device work: no GPU is needed and nothing crashes."""
+    lib = _lib.load()
+    for name in declared_symbols():
+        res, args = _lib._SIGNATURES[name]
+        vals = [0 if a in (ctypes.c_int32, ctypes.c_int, ctypes.c_int64)
+                else 0.0 if a in (ctypes.c_double, ctypes.c_float) else None for a in args]
+        st = getattr(lib, name)(*vals)
+        if name in _NULL_OK:
+            continue
+        assert st == 1, (name, st)
+        assert lib.fl_last_error(), name
