@@ -132,6 +132,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, dist, device):
+    """The largest x over all ranks (the slowest rank's time); x itself
+    without a process group."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -771,11 +782,7 @@ def run_ours(args, rank, ws, dist):
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = ft.kernel_launch_count() - l0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, dev)
 
     # element-loop device time (all colours) per assembly, CUDA events on the stream
     import ctypes as C
@@ -803,11 +810,7 @@ def run_ours(args, rank, ws, dist):
     e2e_steps = max(3, min(50, args.steps // 2))
     for _ in range(e2e_steps):
         ft.assemble_advection_diffusion_cg(m, p, source=hsrc_np, val=hval_np, rhs=hrhs_np)
-    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
-    if dist:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / e2e_steps * 1e3, dist, dev)
     assert np.array_equal(hval_np, val.cpu().numpy()), "host and device paths differ"
     # device time of one host-pointer call (chunked uploads, passes and copies
     # overlap: the element passes' start to the last row pass's end)
@@ -966,7 +969,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=128, help="hexes per side")
+    ap.add_argument("--n", "--hexes", dest="n", type=int, default=128, help="hexes per side")
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
