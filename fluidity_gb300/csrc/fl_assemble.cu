@@ -1400,14 +1400,14 @@ static int launch_rows(const PullArgs& P, int loc, bool use_df, bool closed, int
 int rows_p1_df(fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s) {
   FL_CHECK_ARG(m && m->loc == 4 && m->E > 0, "a P1 mesh handle");
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
-             em, val, rhs, m->err.p};
+             em, val, rhs, m->err.p, 0, 0};
   return launch_rows_p1_df<false>(P, m->max_row, m->tile_rows == 3 ? 1 : m->tile_rows, s);
 }
 
 int rows_p1_closed(fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s) {
   FL_CHECK_ARG(m && m->loc == 4 && m->E > 0, "a P1 mesh handle");
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
-             em, val, rhs, m->err.p};
+             em, val, rhs, m->err.p, 0, 0};
   return launch_rows(P, 4, false, true, m->max_row, m->tile_rows, s);
 }
 
@@ -1633,7 +1633,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
       FL_TRY(fused_plan(m, s));
       if (m->fz_state == 1) {
         PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->fz_rec.p, m->ne_pos.p, m->ndglno.p, m->findrm.p,
-                   m->colm.p, em, val, rhs, m->err.p, host_out ? 1 : 0};
+                   m->colm.p, em, val, rhs, m->err.p, host_out ? 1 : 0, 0};
         switch (key) {
 #define FL_FZ_CASE(K, M, S, T, AN) \
   case K: FL_TRY((launch_fused<M, S, T, AN>(m, D, P, s))); break;
@@ -1664,7 +1664,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   }
   FL_TRY_CUDA(cudaGetLastError());
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
-             em, val, rhs, m->err.p, host_out ? 1 : 0};
+             em, val, rhs, m->err.p, host_out ? 1 : 0, 0};
   FL_TRY(launch_rows(P, loc, use_df, closed, m->max_row, m->tile_rows, s, p->have_mass != 0));
   if (m->timing) {
     FL_TRY_CUDA(cudaEventRecord(m->ev1, s));
@@ -2071,7 +2071,7 @@ extern "C" int fl_dev_assemble_p1_diffusion_noalloc(fl_mesh m, const fl_advdif_p
   k_asm_p1_diffusion<<<grid_for(m->E, 256, 16), 256, 0, s>>>(A);
   FL_TRY_CUDA(cudaGetLastError());
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, nullptr, m->ne_pos.p, m->ndglno.p, m->findrm.p, m->colm.p,
-             d->em, val, rhs, m->err.p};
+             d->em, val, rhs, m->err.p, 0, 0};
   FL_TRY((launch_pull<4, true, 128, 32>(P, s)));
   return check_err(m->err.p, s, "Attempting to set value in matrix outside sparsity pattern");
 }

@@ -153,12 +153,12 @@ __global__ void k_check_conn(const int32_t* __restrict__ nd, int64_t n, int32_t 
   }
 }
 
-__global__ void k_rebase(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
-                         int32_t base) {
+// In place: every entry is read and rewritten by one thread.
+__global__ void k_rebase(int32_t* v, int64_t n, int32_t base) {
   note_launch();
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x)
-    out[k] = in[k] - base;
+    v[k] -= base;
 }
 
 __global__ void k_count_incidence(const int32_t* __restrict__ nd, int64_t n,
@@ -599,7 +599,7 @@ static int upload_conn(const int32_t* host, int64_t n, int32_t base, int32_t nod
   FL_TRY(dst.reserve(n));
   FL_TRY_CUDA(cudaMemcpyAsync(dst.p, host, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
   if (base != 0) {
-    k_rebase<<<grid_for(n, 256), 256, 0, s>>>(dst.p, dst.p, n, base);
+    k_rebase<<<grid_for(n, 256), 256, 0, s>>>(dst.p, n, base);
     FL_TRY_CUDA(cudaGetLastError());
   }
   k_check_conn<<<grid_for(n, 256), 256, 0, s>>>(dst.p, n, nodes, d_err);
