@@ -1689,6 +1689,7 @@ static int assemble_pipelined(fl_mesh_t* m, const fl_advdif_params* p, const fl_
                               double* hrhs, cudaStream_t s, bool* done) {
   *done = false;
   if (!(use_p1_closed_form(m, p) && diagonal_kappa(p))) return FL_OK;
+  if (m->nnz * (int64_t)sizeof(double) / kCkBytes < 2) return FL_OK;  // fewer than two chunks
   FL_CHECK_ARG(!p->have_source || hf->source, "source field missing");
   FL_TRY(fused_plan(m, s));
   const int K = (int)m->ck_rows.size() - 1;
