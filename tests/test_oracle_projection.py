@@ -145,3 +145,39 @@ def test_projection_goldens():
             assert np.array_equal(g, w), k
         else:
             assert np.abs(g - w).max() <= 1e-14 * max(np.abs(w).max(), 1e-300), k
+
+
+def test_projection_identities_on_the_unstructured_mesh(aniso_mesh):
+    """On the reference's own unstructured tet mesh
+    (tests/data/cube_anisotropic.msh):
+    - the lumped mass sums to the volume;
+    - C^T by parts with its surface terms equals C^T not by parts;
+    - the second-order pattern is the structural square;
+    - both row products equal scipy's triple products."""
+    nd, X = aniso_mesh
+    N = X.shape[0]
+    f, c, _ = O.make_sparsity(nd)
+    ml = O.lumped_mass(nd, nd, X, N)
+    assert (ml > 0).all()
+    # the mesh fills the unit cube
+    assert abs(ml.sum() - 1.0) < 1e-12
+    ct, _, dml, _ = O.assemble_divergence_p1(nd, X, f, c)
+    faces, fe = M.boundary_faces(nd)
+    ctb, rhsb, _, _ = O.assemble_divergence_p1(nd, X, f, c, by_parts=True, faces=faces, face_ele=fe)
+    assert np.abs(ct - ctb).max() < 1e-12 * np.abs(ct).max()
+    assert not rhsb.any()
+    sf, sc = O.sparsity_secondorder(f, c)
+    A = sp.csr_matrix((np.ones(len(c)), c, f), shape=(N, N))
+    B = (A @ A).tocsr()
+    B.sort_indices()
+    assert np.array_equal(B.indptr, sf) and np.array_equal(B.indices, sc)
+    w = np.random.default_rng(2).random((N, 3)) + 0.5
+    cmc = O.mult_div_vector_div_T(f, c, ct, w, ct, sf, sc)
+    blk = [sp.csr_matrix((ct[d], c, f), shape=(N, N)) for d in range(3)]
+    ref = sum(blk[d] @ sp.diags(w[:, d]) @ blk[d].T for d in range(3))
+    assert abs(sp.csr_matrix((cmc, sc, sf), shape=(N, N)) - ref).max() < 1e-14 * abs(ref).max()
+    kt, kmk = O.assemble_kmk(nd, X, f, c, ml, sf, sc, theta_pg=1.0)
+    K = sp.csr_matrix((kt, c, f), shape=(N, N))
+    assert abs(K - K.T).max() <= 1e-15 * abs(K).max()
+    ref = K @ sp.diags(1.0 / ml) @ K.T
+    assert abs(sp.csr_matrix((kmk, sc, sf), shape=(N, N)) - ref).max() < 1e-13 * abs(ref).max()
