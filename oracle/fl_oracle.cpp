@@ -1389,6 +1389,96 @@ int orc_assemble_divergence_p1(int E, const int* ndglno, const double* coords, i
   return ORC_OK;
 }
 
+// make_sparsity(rowmesh, colmesh) (femtools/Sparsity_Patterns.F90:47-85 ->
+// make_sparsity_lists :299-379) for two meshes on the same elements: row node
+// i of the row mesh holds every column-mesh node of the elements containing
+// i, ascending.  The pattern of ct_m (pressure rows, velocity columns).
+// Two-call protocol as orc_make_sparsity.
+int64_t orc_make_sparsity_rect(int nrows, int E, int loc_r, const int* nd_r, int loc_c, const int* nd_c,
+                               int64_t* findrm, int* colm, int64_t cap) {
+  std::vector<std::vector<int>> rows(nrows);
+  for (int e = 0; e < E; ++e) {
+    const int* er = nd_r + (int64_t)loc_r * e;
+    const int* ec = nd_c + (int64_t)loc_c * e;
+    for (int i = 0; i < loc_r; ++i) {
+      std::vector<int>& r = rows[er[i]];
+      for (int j = 0; j < loc_c; ++j) {
+        auto it = std::lower_bound(r.begin(), r.end(), ec[j]);
+        if (it == r.end() || *it != ec[j]) r.insert(it, ec[j]);
+      }
+    }
+  }
+  int64_t nnz = 0;
+  for (int i = 0; i < nrows; ++i) nnz += (int64_t)rows[i].size();
+  if (!colm || cap < nnz) return nnz;
+  int64_t p = 0;
+  for (int i = 0; i < nrows; ++i) {
+    findrm[i] = p;
+    for (int c : rows[i]) colm[p++] = c;
+  }
+  findrm[nrows] = p;
+  return nnz;
+}
+
+// assemble_divergence_matrix_cg (assemble/Divergence_Matrix_CG.F90:67-375)
+// for P1 pressure and P2 velocity (Taylor-Hood) on one affine mesh, single
+// phase, the element terms:
+//   not by parts: ele_mat(d, i, j) = shape_dshape(N_p, dN_u, detwei)   (FETools.F90:332)
+//   by parts:     ele_mat(d, i, j) = -dshape_shape(dN_p, N_u, detwei)  (FETools.F90:364)
+// with i over the 4 pressure nodes and j over the 10 velocity nodes, added
+// into the blocks ct(d) on the pattern of orc_make_sparsity_rect(p, u).  The
+// pressure nodes are the coordinate mesh's vertices (ndglno_p indexes
+// coords).  The surface terms of the by-parts form are not restated here.
+int orc_assemble_divergence_p2p1(int E, const int* ndglno_p, const int* ndglno_u, const double* coords, int Np,
+                                 const int64_t* findrm, const int* colm, int quad_degree, int by_parts,
+                                 double* ct) {
+  Quad q;
+  if (!make_tet_quad(quad_degree, q)) return ORC_ERR_ARG;
+  Shape ps, us;
+  make_shape(1, q, ps);
+  make_shape(2, q, us);
+  const int64_t nnz = findrm[Np] - findrm[0];
+  std::memset(ct, 0, sizeof(double) * 3 * nnz);
+  for (int e = 0; e < E; ++e) {
+    const int* pn = ndglno_p + 4 * (int64_t)e;
+    const int* un = ndglno_u + 10 * (int64_t)e;
+    double X[12];
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) X[3 * i + a] = coords[3 * (int64_t)pn[i] + a];
+    Geo g;
+    element_geometry(X, ps, g);
+    double detwei[16];
+    for (int gi = 0; gi < q.ngi; ++gi) detwei[gi] = std::fabs(g.detJ) * q.w[gi];
+    // physical derivatives of both bases at the quadrature points
+    double dp[4][16][3], du[10][16][3];
+    for (int gi = 0; gi < q.ngi; ++gi)
+      for (int a = 0; a < 3; ++a) {
+        for (int i = 0; i < 4; ++i) {
+          double v = 0.0;
+          for (int b = 0; b < 3; ++b) v += ps.dn[i][gi][b] * g.invJ[a][b];
+          dp[i][gi][a] = v;
+        }
+        for (int j = 0; j < 10; ++j) {
+          double v = 0.0;
+          for (int b = 0; b < 3; ++b) v += us.dn[j][gi][b] * g.invJ[a][b];
+          du[j][gi][a] = v;
+        }
+      }
+    for (int d = 0; d < 3; ++d)
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 10; ++j) {
+          double v = 0.0;
+          for (int gi = 0; gi < q.ngi; ++gi)
+            v += detwei[gi] * (by_parts ? dp[i][gi][d] * us.n[j][gi] : ps.n[i][gi] * du[j][gi][d]);
+          if (by_parts) v = -v;
+          const int64_t p = csr_pos(findrm, colm, pn[i], un[j]);
+          if (p < 0) return ORC_ERR_OUTSIDE_PATTERN;
+          ct[d * nnz + p] += v;
+        }
+  }
+  return ORC_OK;
+}
+
 // make_sparsity_transpose (femtools/Sparsity_Patterns.F90:87-148) for one
 // mesh: for every node i, every pair (j, k) of the nodes sharing an element
 // with i (row i of the first-order pattern) puts k in row j, ascending

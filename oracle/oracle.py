@@ -276,6 +276,48 @@ def assemble_divergence_p1(ndglno, coords, findrm, colm, *, by_parts=False, face
     return ct, ct_rhs, dml, gml
 
 
+def make_sparsity_rect(nd_rows, nd_cols, nrows: int | None = None):
+    """(findrm int64, colm int32) of make_sparsity(rowmesh, colmesh)
+    (Sparsity_Patterns.F90:47-85): rows of the row mesh, columns of the
+    column mesh's nodes sharing an element, ascending."""
+    r = np.ascontiguousarray(nd_rows, dtype=np.int32)
+    c = np.ascontiguousarray(nd_cols, dtype=np.int32)
+    E, lr = r.shape
+    lc = c.shape[1]
+    if nrows is None:
+        nrows = int(r.max()) + 1
+    fn = lib().orc_make_sparsity_rect
+    fn.restype = C.c_int64
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                   C.c_int64]
+    f = np.zeros(nrows + 1, dtype=np.int64)
+    nnz = fn(nrows, E, lr, _p(r), lc, _p(c), _p(f), None, 0)
+    colm = np.zeros(nnz, dtype=np.int32)
+    fn(nrows, E, lr, _p(r), lc, _p(c), _p(f), _p(colm), nnz)
+    return f, colm
+
+
+def assemble_divergence_p2p1(ndglno_p, ndglno_u, coords, findrm, colm, *, by_parts=False, quad_degree=4):
+    """ct (3, nnz) -- the element terms of assemble_divergence_matrix_cg
+    (Divergence_Matrix_CG.F90:67-375) for P1 pressure (rows, the coordinate
+    mesh's vertices) and P2 velocity (columns) on the pattern of
+    make_sparsity_rect."""
+    p_ = np.ascontiguousarray(ndglno_p, dtype=np.int32)
+    u_ = np.ascontiguousarray(ndglno_u, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    fn = lib().orc_assemble_divergence_p2p1
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                   C.c_int, C.c_void_p]
+    ct = np.zeros((3, c.size))
+    st = fn(p_.shape[0], _p(p_), _p(u_), _p(X), f.size - 1, _p(f), _p(c), quad_degree, int(bool(by_parts)),
+            _p(ct))
+    assert st == 0, st
+    return ct
+
+
 def sparsity_secondorder(findrm, colm):
     """(findrm int64, colm int32) of make_sparsity_transpose (Sparsity_Patterns.F90:87-148)."""
     f = np.ascontiguousarray(findrm, dtype=np.int64)

@@ -12,7 +12,8 @@
 * ``projection_goldens.npz`` -- the oracle's pressure-projection pieces on the
   2^3 six-tet cube: lumped mass, divergence matrix (both forms, surface terms
   of every boundary-condition type), second-order pattern, C M_l^-1 C^T, KMK
-  (theta 1 and 0.7) and the projection vectors.
+  (theta 1 and 0.7), the projection vectors, and the P2-velocity / P1-pressure
+  (Taylor-Hood) divergence pattern and element terms.
 
 Run from the repository root in an environment that has the reference checkout:
     python tests/golden/make_golden.py /root/reference
@@ -131,6 +132,12 @@ def projection_goldens(inp=None):
         g[name + "_kt"], g[name] = kt, kmk
     g["poisson_rhs"] = O.masslumped_poisson_rhs(f, c, ct, inp["mom"], inp["ctr"], inv, inp["u"], 0.1, 0.5)
     g["corrected_u"] = O.correct_masslumped_velocity(f, c, ct, inv, inp["dp"], inp["u"])
+    # P2 velocity / P1 pressure (Taylor-Hood): pattern and element terms
+    nd2, _ = O.make_global_numbering_p2(nd)
+    tf, tc = O.make_sparsity_rect(nd, nd2)
+    g["th_findrm"], g["th_colm"] = tf, tc
+    g["th_ct"] = O.assemble_divergence_p2p1(nd, nd2, X, tf, tc)
+    g["th_ct_by_parts"] = O.assemble_divergence_p2p1(nd, nd2, X, tf, tc, by_parts=True)
     return g
 
 

@@ -181,3 +181,58 @@ def test_projection_identities_on_the_unstructured_mesh(aniso_mesh):
     assert abs(K - K.T).max() <= 1e-15 * abs(K).max()
     ref = K @ sp.diags(1.0 / ml) @ K.T
     assert abs(sp.csr_matrix((kmk, sc, sf), shape=(N, N)) - ref).max() < 1e-13 * abs(ref).max()
+
+
+def _taylor_hood(nd, X):
+    nd2, n2 = O.make_global_numbering_p2(nd)
+    f, c = O.make_sparsity_rect(nd, nd2)
+    X2 = M.p2_coordinates(nd, nd2, X, O.tet_counts(2))
+    return nd2, n2, f, c, X2
+
+
+@pytest.mark.parametrize("which", ["cube", "unstructured"])
+def test_taylor_hood_divergence_pins(which, aniso_mesh):
+    """Divergence matrix of P2 velocity / P1 pressure (oracle only; the GPU
+    kernel is the next step of this row), pinned by exact identities:
+    - the pattern is make_sparsity(p_mesh, u_mesh): each pressure row holds the
+      velocity nodes of its elements;
+    - C_d applied to the P2 interpolant of x_e is delta_de times the P1 lumped
+      pressure mass (integral of N_i), and of x_0^2 it is integral(N_i 2 x_0)
+      = sum_e 2 V_e / 20 (x_i + sum_k x_k), both exact at this quadrature;
+    - column sums vanish for velocity nodes off the boundary (sum_i N_i = 1);
+    - by parts without surface terms equals not by parts for velocities that
+      vanish on the boundary."""
+    nd, X = M.cube_mesh(3) if which == "cube" else aniso_mesh
+    N = X.shape[0]
+    nd2, n2, f, c, X2 = _taylor_hood(nd, X)
+    want = [set() for _ in range(N)]
+    for e in range(len(nd)):
+        for i in nd[e]:
+            want[i].update(nd2[e].tolist())
+    for i in range(N):
+        assert c[f[i]:f[i + 1]].tolist() == sorted(want[i])
+    ct = O.assemble_divergence_p2p1(nd, nd2, X, f, c)
+    C3 = [sp.csr_matrix((ct[d], c, f), shape=(N, n2)) for d in range(3)]
+    ml = O.lumped_mass(nd, nd, X, N)
+    for d in range(3):
+        for a in range(3):
+            got = C3[d] @ X2[:, a]
+            assert np.abs(got - (ml if a == d else 0.0)).max() < 1e-14 * ml.max()
+    J = np.stack([X[nd[:, k]] - X[nd[:, 3]] for k in range(3)], axis=1)   # (E, 3, 3)
+    vol = np.abs(np.linalg.det(J)) / 6.0
+    ref = np.zeros(N)
+    xs = X[nd, 0].sum(axis=1)
+    for k in range(4):
+        np.add.at(ref, nd[:, k], 2.0 * vol / 20.0 * (X[nd[:, k], 0] + xs))
+    assert np.abs(C3[0] @ (X2[:, 0] ** 2) - ref).max() < 1e-14 * np.abs(ref).max()
+    interior = np.ones(n2, bool)
+    interior[M.boundary_nodes(X2)] = False
+    for d in range(3):
+        colsum = np.asarray(C3[d].sum(axis=0)).ravel()
+        assert np.abs(colsum[interior]).max() < 1e-14 * np.abs(ct[d]).max()
+    ctb = O.assemble_divergence_p2p1(nd, nd2, X, f, c, by_parts=True)
+    u = np.prod(X2 * (1.0 - X2), axis=1) * 64.0 * (1.0 + X2[:, 1])
+    u[~interior] = 0.0
+    for d in range(3):
+        Cb = sp.csr_matrix((ctb[d], c, f), shape=(N, n2))
+        assert np.abs(Cb @ u - C3[d] @ u).max() < 1e-13 * np.abs(C3[d] @ u).max()
