@@ -2001,6 +2001,9 @@ static __device__ __align__(256) RefTensors g_noalloc_ref[4];  // quadrature deg
 
 // Host-side device addresses of the arrays above, resolved once per device by
 // cudaGetSymbolAddress (the array's name in host code is not a device address).
+// They belong to the device's current context: cudaDeviceReset discards them
+// (and the uploaded tables) together with every mesh handle, so a process that
+// resets a device must unload and reload the library before calling again.
 struct NoAllocDevice {
   bool ready = false;
   double* em = nullptr;
@@ -2025,6 +2028,11 @@ static int noalloc_setup(int dev, NoAllocDevice** out) {
       FL_TRY_CUDA(cudaMemcpyToSymbol(g_noalloc_ref, &h, sizeof(RefTensors), sizeof(RefTensors) * (q - 1),
                                      cudaMemcpyHostToDevice));
     }
+    // cudaMemcpyToSymbol from pageable memory may return before the data has
+    // reached the device, and it is ordered on the legacy default stream only:
+    // the assembly's stream (often non-blocking) must not start before the
+    // tables are complete.  This runs once per device.
+    FL_TRY_CUDA(cudaDeviceSynchronize());
     d.ready = true;
   }
   *out = &d;

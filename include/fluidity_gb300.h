@@ -181,10 +181,16 @@ int fl_dev_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
  * scratch is a fixed array inside the library sized for at most 131072
  * elements (14.7 MB held on every GPU that loads the library); larger meshes
  * are rejected with FL_ERR_ARG.  The first call on a device also looks up
- * that array's device address and uploads the reference-element tables, so
- * make the first call on each device before any stream capture.  Every call
- * shares the array, so calls whose GPU work overlaps (other streams or
- * threads) race.  Device pointers; results equal fl_dev_assemble_advdif_cg's. */
+ * that array's device address and uploads the reference-element tables
+ * (then waits for the device), so make the first call on each device before
+ * any stream capture.  Every call waits for its stream before it returns (it
+ * reads the pattern-error flag back).  Every call shares the array, so calls
+ * whose GPU work overlaps (other streams or threads) race.  After
+ * cudaDeviceReset the library must be unloaded and loaded again, like every
+ * mesh handle.  Device pointers; the results agree with
+ * fl_dev_assemble_advdif_cg's within rounding (that entry point computes the
+ * isotropic and diagonal-diffusivity forms in double-float, this one in
+ * FP64), and bitwise for a full diffusivity tensor. */
 int fl_dev_assemble_p1_diffusion_noalloc(fl_mesh mesh, const fl_advdif_params* params,
                                          const fl_fields* fields, double* val, double* rhs,
                                          void* stream);

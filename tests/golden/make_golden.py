@@ -15,8 +15,9 @@
   (theta 1 and 0.7), the projection vectors, and the P2-velocity / P1-pressure
   (Taylor-Hood) divergence pattern and element terms.
 
-Run from the repository root in an environment that has the reference checkout:
-    python tests/golden/make_golden.py /root/reference
+Run from the repository root in an environment that has the reference
+checkout, giving the checkout's root directory as the argument:
+    python tests/golden/make_golden.py <reference checkout>
 (``--projection`` writes only the projection fixtures, which need no reference
 files.)
 """
@@ -143,6 +144,8 @@ def projection_goldens(inp=None):
 
 if __name__ == "__main__":
     if "--projection" not in sys.argv:
-        main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+        if len(sys.argv) < 2 or sys.argv[1].startswith("-"):
+            sys.exit("usage: make_golden.py <reference checkout> | --projection")
+        main(sys.argv[1])
     np.savez_compressed(os.path.join(HERE, "projection_goldens.npz"), **projection_goldens())
     print("wrote projection fixtures to", HERE)

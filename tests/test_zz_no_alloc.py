@@ -41,7 +41,7 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls():
     torch.cuda.synchronize()
     ref_val, ref_rhs = ref_val.cpu().numpy(), ref_rhs.cpu().numpy()
     fields = _lib.Fields(None, None, src.data_ptr(), None)
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = ft._stream_ptr(torch.cuda.current_stream())
     for _ in range(2):
         val = torch.full((m.nnz,), float("nan"), dtype=torch.float64, device="cuda")
         rhs = torch.full((m.N,), float("nan"), dtype=torch.float64, device="cuda")
@@ -57,7 +57,7 @@ def test_noalloc_after_another_mesh_and_with_mass():
     """The shared scratch keeps the previous call's contents; results must not depend on them."""
     import torch
     lib = _lib.load()
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = ft._stream_ptr(torch.cuda.current_stream())
     p = ft.advdif_params(theta=0.5, dt=0.1, diffusivity=np.diag([1.0, 1.0, 1e-3]), have_mass=True,
                          have_source=True, quad_degree=2)
     for n in (12, 7):
@@ -86,6 +86,6 @@ def test_noalloc_rejects_meshes_above_the_limit():
     val = torch.empty(m.nnz, dtype=torch.float64, device="cuda")
     rhs = torch.empty(m.N, dtype=torch.float64, device="cuda")
     st = _noalloc(lib, m, p, _lib.Fields(None, None, None, None), val, rhs,
-                  torch.cuda.current_stream().cuda_stream)
+                  ft._stream_ptr(torch.cuda.current_stream()))
     assert st == 1  # FL_ERR_ARG
     assert b"allocation-free limit" in lib.fl_last_error()
