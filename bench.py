@@ -89,7 +89,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -99,11 +99,23 @@ class ClockSampler:
             self.lines.clear()
         except Exception:
             self.proc = None
+        self.t_start = time.time()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def hold(self, step, min_s=1.0):
+        """Keep running `step` (the timed region's own work) until the sampler
+        has covered at least `min_s` seconds since the timed region began, so a
+        timed region shorter than the sampling interval still gets samples
+        taken under the same load."""
+        import torch
+        while time.time() - self.t_start < min_s:
+            for _ in range(8):
+                step()
+            torch.cuda.synchronize()
 
     def __exit__(self, *a):
         if self.proc:
@@ -159,6 +171,43 @@ def dist_setup(args):
     return 0, 1, None
 
 
+def workload_name(n):
+    """The headline workload's name, the same string in both arms."""
+    return f"P1 Poisson assembly, {n}^3 six-tet cube, jitter 0.2h"
+
+
+def row_scaled_err(a, b, findrm):
+    """max over entries of |a - b| / max_j |b(i, j)| (row-scaled relative error)."""
+    findrm = np.asarray(findrm, dtype=np.int64)
+    lens = np.diff(findrm)
+    ab = np.abs(b)
+    rowmax = np.zeros(lens.size)
+    nz = lens > 0
+    rowmax[nz] = np.maximum.reduceat(ab, findrm[:-1][nz])
+    rowmax[rowmax == 0] = 1.0
+    return float(np.max(np.abs(a - b) / np.repeat(rowmax, lens))) if a.size else 0.0
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b|."""
+    sc = float(np.abs(b).max()) or 1.0
+    return float(np.abs(a - b).max() / sc)
+
+
+def sig(x, d=4):
+    """x rounded to d significant digits (compact summary values)."""
+    if x is None or isinstance(x, (bool, str)):
+        return x
+    if isinstance(x, (list, tuple)):
+        return [sig(v, d) for v in x]
+    if isinstance(x, dict):
+        return {k: sig(v, d) for k, v in x.items()}
+    if isinstance(x, int):
+        return x
+    x = float(x)
+    return 0.0 if x == 0 else float(f"{x:.{d}g}")
+
+
 def workload(n):
     from fluidity_gb300 import meshgen as M
     nd, X = M.cube_mesh(n)
@@ -198,7 +247,7 @@ def cpu_advdif_steps(n=16, nsteps=10, nthreads=0):
     bn = M.boundary_nodes(X)
     T = M.gaussian_tracer(X)
     t0 = time.perf_counter()
-    its = []
+    its, Ts = [], []
     for _ in range(nsteps):
         val, rhs, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X,
                                          findrm=findrm, colm=colm, theta=0.5, dt=0.01,
@@ -211,7 +260,8 @@ def cpu_advdif_steps(n=16, nsteps=10, nthreads=0):
                                           ksp="gmres", restart=30, rtol=1e-10)
         its.append(int(it))
         T = T + 0.01 * dx
-    return (time.perf_counter() - t0) / nsteps * 1e3, its
+        Ts.append(T)
+    return (time.perf_counter() - t0) / nsteps * 1e3, its, Ts
 
 
 def run_reference(args, rank, ws, dist):
@@ -243,7 +293,7 @@ def run_reference(args, rank, ws, dist):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"P1 Poisson assembly, {args.n}^3 six-tet cube", "elements": E,
+        "config": {"workload": workload_name(args.n), "elements": E,
                    "nodes": int(X.shape[0]), "nnz": int(colm.size), "cpu_setup_s": setup},
         "cpu_baseline": {"value": value, "unit": "Melem/s", "cores": thr, "kind": "port",
                          "sample": f"full {args.n}^3 assembly per step, OpenMP over "
@@ -340,6 +390,12 @@ def bench_batch(args, dev, stream):
     seq_ms = float(min(seq_times))
     identical = all(torch.equal(a, c) for a, c in zip(xb, xs))
     its = [r["iterations"] for r in reps]
+    keep = {}
+    for k, (mm, pp, oo, bnd, ff) in ((0, members[0]), (nt, members[nt])):
+        r = regs[k]
+        keep[k] = {"val": r["val"].cpu().numpy(), "rhs": r["rhs"].cpu().numpy(),
+                   "inactive": r["inactive"].cpu().numpy(), "x": xb[k].cpu().numpy(),
+                   "iterations": reps[k]["iterations"]}
     out = {
         "workload": f"{nt} tracers (GMRES(30), rtol 1e-10) on one 64^3 mesh + 8 Poisson meshes "
                     f"n={list(M.BATCH_MESH_SIDES)} (CG, rtol 1e-10), one step each",
@@ -356,7 +412,7 @@ def bench_batch(args, dev, stream):
                                                       [(shared.tiles())] + [mm.tiles() for mm in meshes])},
     }
     b.close()
-    return out
+    return out, keep
 
 
 def p2_algorithmic_bytes(E, N1, N2, nnz):
@@ -407,6 +463,9 @@ def bench_p2(args, dev, stream, n=64):
     alg = p2_algorithmic_bytes(m.E, X.shape[0], m.N, m.nnz)
     peak, _ = measured_peak_hbm()
     achieved = alg / (kernel_ms * 1e-3) / 1e9
+    sp2 = m.sparsity()
+    host = {"nd": nd, "X": X, "nd2": nd2, "n2": n2, "src": M.poisson_source(X2), "val": val.cpu().numpy(),
+            "rhs": rhs.cpu().numpy(), "findrm": sp2.findrm, "colm": sp2.colm, "centrm": sp2.centrm}
     ina = torch.zeros(m.N, dtype=torch.uint8, device=dev)
     bn = M.boundary_nodes(X2)
     step()
@@ -416,7 +475,7 @@ def bench_p2(args, dev, stream, n=64):
     solve = {}
     for prec in ("fp64", "reliable"):
         x = torch.zeros(m.N, dtype=torch.float64, device=dev)
-        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000, precision=prec)
+        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000, precision=prec, norm="unpreconditioned")
         torch.cuda.synchronize()
         e0.record(stream)
         rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
@@ -436,7 +495,7 @@ def bench_p2(args, dev, stream, n=64):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "algorithmic_bytes": alg},
         "solve": solve, "max_err_vs_analytic": float((x - xa).abs().max()),
-    }
+    }, host
 
 
 def bench_projection(args, dev, stream, m, X, n):
@@ -508,7 +567,7 @@ def bench_projection(args, dev, stream, m, X, n):
     ina[N // 2] = 1
     rhs[N // 2] = 0.0
     dp = torch.zeros(N, dtype=torch.float64, device=dev)
-    opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000)
+    opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000, norm="unpreconditioned")
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -606,7 +665,7 @@ def bench_advdif_steps(args, dev, stream, n=16, nsteps=10):
 
     def run():
         t = torch.from_numpy(M.gaussian_tracer(X)).to(dev)
-        its = []
+        its, ts = [], []
         for _ in range(nsteps):
             ft.assemble_advection_diffusion_cg(m, p, t=t, velocity=u, val=val, rhs=rhs, stream=stream)
             ina.zero_()
@@ -615,18 +674,20 @@ def bench_advdif_steps(args, dev, stream, n=16, nsteps=10):
             rep = ft.petsc_solve(m, dT, val, rhs, opts, inactive=ina, stream=stream)
             its.append(rep["iterations"])
             t = t + p.dt * dT
-        return t, its
+            ts.append(t)
+        return t, its, ts
 
     run()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    t, its = run()
+    t, its, ts = run()
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    return {"workload": f"advection-diffusion, {n}^3 six-tet cube, {nsteps} steps, GMRES(30)+Jacobi rtol 1e-10",
-            "ms_per_step": ms / nsteps, "iterations": its, "tracer_max_final": float(t.max())}
+    out = {"workload": f"advection-diffusion, {n}^3 six-tet cube, {nsteps} steps, GMRES(30)+Jacobi rtol 1e-10",
+           "ms_per_step": ms / nsteps, "iterations": its, "tracer_max_final": float(t.max())}
+    return out, [v.cpu().numpy() for v in ts]
 
 
 def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
@@ -684,7 +745,7 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
     torch.cuda.synchronize()
     amg_setup_ms = (time.perf_counter() - t0) * 1e3
     res = {k: {"ms": [], "iterations": [], "err": [], "true_rel_residual": []} for k in variants}
-    tight = ft.solver_options(ksp="cg", rtol=1e-13, max_its=50000)
+    tight = ft.solver_options(ksp="cg", rtol=1e-13, max_its=50000, norm="unpreconditioned")
     x = torch.empty_like(ps[0])
     for t in range(ntrain, nsteps):
         val, rhs, ina = seq.system(t)
@@ -693,7 +754,7 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
         scale = ref.abs().max()
         for k, (prec, guess) in variants.items():
             opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000,
-                                     precision="fp64" if prec == "amg" else prec)
+                                     precision="fp64" if prec == "amg" else prec, norm="unpreconditioned")
             torch.cuda.synchronize()
             e0.record(stream)
             if guess == "zero":
@@ -737,10 +798,217 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
     }
 
 
+def bench_solves(args, dev, stream, m, val, rhs, ina, xa, peak, kappa_name):
+    """CG + Jacobi to rtol 1e-10 on one assembled Poisson system: FP64, the
+    two mixed-precision forms and AMG, every one with the unpreconditioned
+    test (rtol bounds the true relative residual); plus FP64 with PETSc's
+    default preconditioned-norm test, and an FP64 solve to rtol 1e-13 as the
+    reference of every solution's error."""
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+
+    N = m.N
+    out = {}
+    xs = {}
+
+    def timed(opts):
+        x = torch.zeros(N, dtype=torch.float64, device=dev)
+        ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)  # warm-up
+        x.zero_()
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        return x, rep, s0.elapsed_time(s1)
+
+    xt = torch.zeros(N, dtype=torch.float64, device=dev)
+    ft.petsc_solve(m, xt, val, rhs, ft.solver_options(ksp="cg", rtol=1e-13, max_its=100000,
+                                                       norm="unpreconditioned", start_from_zero=True),
+                   inactive=ina, stream=stream)
+    scale = float(xt.abs().max())
+    variants = (("fp64", "fp64", "unpreconditioned"), ("fp64_pc_norm", "fp64", "preconditioned"),
+                ("mixed", "mixed", "unpreconditioned"), ("reliable", "reliable", "unpreconditioned"))
+    for key, prec, norm in variants:
+        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=100000, precision=prec, norm=norm,
+                                 start_from_zero=True)
+        x, rep, sms = timed(opts)
+        xs[key] = x
+        out[key] = {"ms": sms, "iterations": rep["iterations"], "reason": rep["reason_name"],
+                    "outer": rep["outer_iterations"], "norm": norm,
+                    "true_rel_residual": rep["true_rel_residual"],
+                    "err_vs_fp64_tight": float((x - xt).abs().max()) / scale}
+    if not getattr(args, "no_amg", False):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        amg = ft.AmgPreconditioner(m, val, ina, stream=stream, unpreconditioned_norm=True)
+        torch.cuda.synchronize()
+        amg_setup = time.perf_counter() - t0
+        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=20000, start_from_zero=True)
+        for key, fp32 in (("amg", False), ("amg_fp32_cycle", True)):
+            amg.set_precision(fp32)
+            xg = torch.zeros(N, dtype=torch.float64, device=dev)
+            amg.solve(xg, rhs, opts, stream=stream)
+            xg.zero_()
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            rep = amg.solve(xg, rhs, opts, stream=stream)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            out[key] = {"ms": s0.elapsed_time(s1), "setup_ms": amg_setup * 1e3, "iterations": rep["iterations"],
+                        "reason": rep["reason_name"], "levels": amg.levels(), "norm": "unpreconditioned",
+                        "cycle": "fp32" if fp32 else "fp64", "true_rel_residual": rep["true_rel_residual"],
+                        "err_vs_fp64_tight": float((xg - xt).abs().max()) / scale}
+        amg.close()
+    it_bytes = cg_iteration_bytes(N, m.nnz)
+    f64 = out["fp64"]
+    f64["achieved_gbs"] = it_bytes * f64["iterations"] / (f64["ms"] * 1e-3) / 1e9
+    f64["frac_of_hbm"] = f64["achieved_gbs"] / peak
+    if xa is not None:
+        f64["max_err_vs_analytic"] = float((xs["fp64"] - xa).abs().max())
+    for k in list(out):
+        if k != "fp64" and isinstance(out[k], dict):
+            out[f"speedup_{k}_vs_fp64"] = f64["ms"] / out[k]["ms"]
+    out["max_true_rel_residual_unpreconditioned"] = max(
+        v["true_rel_residual"] for k, v in out.items() if isinstance(v, dict) and v.get("norm") == "unpreconditioned")
+    out["diffusivity"] = kappa_name
+    return out
+
+
+def cpu_legs(args, m, nd, X, src, gpu):
+    """The oracle on the host cores (rank 0, one GPU): the timed CPU baselines
+    of this run, and the checker of this run's GPU outputs at the benchmark
+    sizes (integer arrays bit for bit; assembled entries row-scaled)."""
+    from fluidity_gb300 import meshgen as M
+    from oracle import oracle as O
+
+    ncores = len(os.sched_getaffinity(0))
+    par = {}
+    # 128^3 P1: the oracle's own pattern and colouring against the GPU's
+    t0 = time.perf_counter()
+    f, c, ce = O.make_sparsity(nd)
+    ocol, ncol = O.colour_cg1(nd)
+    cs = O.colour_sets(ocol, ncol)
+    setup_s = time.perf_counter() - t0
+    s = m.sparsity()
+    col, ptr, el = m.colouring()
+    par["p1_sparsity_bit_exact"] = bool(np.array_equal(s.findrm, f) and np.array_equal(s.colm, c)
+                                        and np.array_equal(s.centrm, ce))
+    par["p1_colouring_bit_exact"] = bool(m.ncolours == ncol and np.array_equal(col, ocol)
+                                         and np.array_equal(ptr, cs[0]) and np.array_equal(el, cs[1]))
+
+    def oracle_asm(nthreads, **kw):
+        t0 = time.perf_counter()
+        v, r, st = O.assemble_advdif(ndglno_t=nd, nt=X.shape[0], ndglno_x=nd, coords=X, findrm=f, colm=c,
+                                     source=src, colours=cs, nthreads=nthreads, **kw)
+        assert st == 0
+        return v, r, time.perf_counter() - t0
+
+    oval, orhs, secs = oracle_asm(ncores, diffusivity=1.0)
+    _, _, secs1 = oracle_asm(1, diffusivity=1.0)
+    E = nd.shape[0]
+    par["p1_max_row_scaled_err"] = row_scaled_err(gpu["val"], oval, f)
+    par["p1_rhs_rel_err"] = rel_err(gpu["rhs"], orhs)
+    del oval, orhs
+    if gpu.get("aniso_val") is not None:
+        aval, arhs, _ = oracle_asm(ncores, diffusivity=np.diag([1.0, 1.0, 1e-3]))
+        par["p1_aniso_max_row_scaled_err"] = row_scaled_err(gpu["aniso_val"], aval, f)
+        par["p1_aniso_rhs_rel_err"] = rel_err(gpu["aniso_rhs"], arhs)
+        del aval, arhs
+    cpu = {"value": E / secs / 1e6, "unit": "Melem/s", "cores": ncores, "kind": "port",
+           "sample": f"one full {args.n}^3 assembly ({secs:.2f} s), OpenMP over {ncol} colours, oracle "
+                     f"restatement of the reference loop",
+           "value_1_core": E / secs1 / 1e6, "sample_1_core": f"one full {args.n}^3 assembly ({secs1:.2f} s)",
+           "oracle_sparsity_and_colouring_s": setup_s}
+    # 64^3 P2
+    p2 = gpu.get("p2")
+    if p2 is not None:
+        ond2, on2 = O.make_global_numbering_p2(p2["nd"])
+        par["p2_numbering_bit_exact"] = bool(on2 == p2["n2"] and np.array_equal(ond2, p2["nd2"]))
+        f2, c2, ce2 = O.make_sparsity(ond2, on2)
+        par["p2_sparsity_bit_exact"] = bool(np.array_equal(f2, p2["findrm"]) and np.array_equal(c2, p2["colm"])
+                                            and np.array_equal(ce2, p2["centrm"]))
+        pc, pn = O.colour_cg1(p2["nd"])
+        t0 = time.perf_counter()
+        v2, r2, st = O.assemble_advdif(ndglno_t=ond2, nt=on2, ndglno_x=p2["nd"], coords=p2["X"], findrm=f2,
+                                       colm=c2, diffusivity=1.0, source=p2["src"], colours=O.colour_sets(pc, pn),
+                                       quad_degree=4, t_degree=2, nthreads=ncores)
+        p2s = time.perf_counter() - t0
+        assert st == 0
+        par["p2_max_row_scaled_err"] = row_scaled_err(p2["val"], v2, f2)
+        par["p2_rhs_rel_err"] = rel_err(p2["rhs"], r2)
+        cpu["p2_64_melem_per_s"] = p2["nd"].shape[0] / p2s / 1e6
+        del v2, r2
+    # the 16^3 advection-diffusion workload, ten steps
+    adv_ms, adv_its, adv_T = cpu_advdif_steps(nthreads=ncores)
+    cpu["advdif_16_ten_steps_ms_per_step"] = adv_ms
+    cpu["advdif_16_ten_steps_iterations"] = adv_its
+    st16 = gpu.get("steps16")
+    if st16 is not None:
+        gT, gits = st16
+        par["advdif16_max_step_rel_diff"] = max(rel_err(a, b) for a, b in zip(gT, adv_T))
+        par["advdif16_max_iteration_diff"] = int(max(abs(a - b) for a, b in zip(gits, adv_its)))
+    # batch members: the first tracer on the 64^3 mesh and the Poisson member on the n=24 mesh
+    bk = gpu.get("batch")
+    if bk is not None:
+        kap, sc = M.batch_tracer_params(args.batch_fields)
+        worst = {"val": 0.0, "rhs": 0.0, "x": 0.0, "its": 0, "inactive_equal": True}
+        for k, (ndm, Xm) in bk["meshes"].items():
+            fm, cm, _ = O.make_sparsity(ndm)
+            cc, cn = O.colour_cg1(ndm)
+            bn = M.boundary_nodes(Xm)
+            if k == 0:
+                T0 = M.gaussian_tracer(Xm)
+                kw = dict(theta=0.5, dt=0.01, have_mass=True, velocity=sc[0] * M.advdif_velocity(Xm), T=T0,
+                          diffusivity=float(kap[0]))
+                ksp = "gmres"
+            else:
+                T0 = None
+                kw = dict(diffusivity=1.0, source=M.poisson_source(Xm))
+                ksp = "cg"
+            ov, orr, st = O.assemble_advdif(ndglno_t=ndm, nt=Xm.shape[0], ndglno_x=ndm, coords=Xm, findrm=fm,
+                                            colm=cm, colours=O.colour_sets(cc, cn), nthreads=ncores, **kw)
+            assert st == 0
+            oina = np.zeros(Xm.shape[0], dtype=np.uint8)
+            O.apply_dirichlet(bn, np.zeros(bn.size), T0, kw.get("dt", 1.0), orr, oina)
+            ox, oits, oreason, _ = O.petsc_solve(fm, cm, ov, oina, orr, ksp=ksp, restart=30, rtol=1e-10,
+                                                 max_its=20000, nthreads=ncores)
+            g = bk["members"][k]
+            worst["val"] = max(worst["val"], row_scaled_err(g["val"], ov, fm))
+            worst["rhs"] = max(worst["rhs"], rel_err(g["rhs"], orr))
+            worst["x"] = max(worst["x"], rel_err(g["x"], ox))
+            worst["its"] = max(worst["its"], abs(g["iterations"] - oits))
+            worst["inactive_equal"] = worst["inactive_equal"] and bool(np.array_equal(g["inactive"], oina))
+        par["batch_members"] = "tracer 0 on 64^3 (GMRES) and the n=24 Poisson mesh (CG)"
+        par["batch_max_row_scaled_err"] = worst["val"]
+        par["batch_rhs_rel_err"] = worst["rhs"]
+        par["batch_solution_rel_err"] = worst["x"]
+        par["batch_max_iteration_diff"] = int(worst["its"])
+        par["batch_dirichlet_rows_equal"] = worst["inactive_equal"]
+    par["tolerances"] = ("integer arrays equal; entries <= 1e-12 row-scaled; rhs <= 1e-12 of max; "
+                         "solutions at rtol 1e-10 <= 1e-7 of max; iterations +-1")
+    par["pass"] = bool(par["p1_sparsity_bit_exact"] and par["p1_colouring_bit_exact"]
+                       and par["p1_max_row_scaled_err"] <= 1e-12 and par["p1_rhs_rel_err"] <= 1e-12
+                       and par.get("p1_aniso_max_row_scaled_err", 0) <= 1e-12
+                       and par.get("p2_numbering_bit_exact", True) and par.get("p2_sparsity_bit_exact", True)
+                       and par.get("p2_max_row_scaled_err", 0) <= 1e-12
+                       and par.get("advdif16_max_step_rel_diff", 0) <= 1e-9
+                       and par.get("advdif16_max_iteration_diff", 0) <= 1
+                       and par.get("batch_max_row_scaled_err", 0) <= 1e-12
+                       and par.get("batch_solution_rel_err", 0) <= 1e-7
+                       and par.get("batch_max_iteration_diff", 0) <= 1
+                       and par.get("batch_dirichlet_rows_equal", True))
+    return cpu, par
+
+
 def run_ours(args, rank, ws, dist):
     import torch
 
     from fluidity_gb300 import femtools as ft
+    from fluidity_gb300 import meshgen as M
 
     dev = torch.device("cuda", torch.cuda.current_device())
     nd, X, src, bn = workload(args.n)
@@ -781,8 +1049,11 @@ def run_ours(args, rank, ws, dist):
             step()
         ev1.record(stream)
         torch.cuda.synchronize()
-    launches = ft.kernel_launch_count() - l0
+        launches = ft.kernel_launch_count() - l0
+        clk.hold(step, min_s=1.0)
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, dev)
+    clocks = clk.summary()
+    clocks["window"] = "the timed region, then untimed repeats of the same step to 1 s in all"
 
     # element-loop device time (all colours) per assembly, CUDA events on the stream
     import ctypes as C
@@ -811,7 +1082,8 @@ def run_ours(args, rank, ws, dist):
     for _ in range(e2e_steps):
         ft.assemble_advection_diffusion_cg(m, p, source=hsrc_np, val=hval_np, rhs=hrhs_np)
     e2e_ms = max_over_ranks((time.perf_counter() - t0) / e2e_steps * 1e3, dist, dev)
-    assert np.array_equal(hval_np, val.cpu().numpy()), "host and device paths differ"
+    gpu = {"val": val.cpu().numpy(), "rhs": rhs.cpu().numpy()}
+    assert np.array_equal(hval_np, gpu["val"]), "host and device paths differ"
     # device time of one host-pointer call (chunked uploads, passes and copies
     # overlap: the element passes' start to the last row pass's end)
     lib.fl_set_kernel_timing(m.handle, 1)
@@ -832,79 +1104,38 @@ def run_ours(args, rank, ws, dist):
         link.append(c0.elapsed_time(c1))
     link_ms = min(link)
 
-    # solve: Dirichlet + CG to 1e-10 (fp64 and mixed)
-    solve = None
+    # solves: Dirichlet + CG to 1e-10 (fp64, mixed, AMG), isotropic and anisotropic
+    solve = aniso = None
     if not args.no_solve:
         ina = torch.zeros(N, dtype=torch.uint8, device=dev)
         dbn = torch.from_numpy(bn).to(dev)
         dg = torch.zeros(bn.size, dtype=torch.float64, device=dev)
         step()
         ft.apply_dirichlet_conditions(m, rhs, ina, dbn, dg, dt=1.0, stream=stream)
-        out = {}
-        xs = {}
-        for prec in ("fp64", "mixed", "reliable"):
-            x = torch.zeros(N, dtype=torch.float64, device=dev)
-            opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=20000, precision=prec,
-                                     start_from_zero=True)
-            ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)  # warm-up
-            x.zero_()
-            torch.cuda.synchronize()
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina, stream=stream)
-            s1.record(stream)
-            torch.cuda.synchronize()
-            sms = s0.elapsed_time(s1)
-            xs[prec] = x
-            out[prec] = {"ms": sms, "iterations": rep["iterations"], "reason": rep["reason_name"],
-                         "outer": rep["outer_iterations"],
-                         "true_rel_residual": rep["true_rel_residual"],
-                         "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None}
-        # smoothed-aggregation AMG preconditioner: hierarchy once, then CG
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        amg = ft.AmgPreconditioner(m, val, ina, stream=stream, unpreconditioned_norm=True)
-        torch.cuda.synchronize()
-        amg_setup = time.perf_counter() - t0
-        opts = ft.solver_options(ksp="cg", rtol=1e-10, max_its=20000, start_from_zero=True)
-        for key, fp32 in (("amg", False), ("amg_fp32_cycle", True)):
-            amg.set_precision(fp32)
-            xg = torch.zeros(N, dtype=torch.float64, device=dev)
-            amg.solve(xg, rhs, opts, stream=stream)
-            xg.zero_()
-            torch.cuda.synchronize()
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record(stream)
-            rep = amg.solve(xg, rhs, opts, stream=stream)
-            s1.record(stream)
-            torch.cuda.synchronize()
-            out[key] = {"ms": s0.elapsed_time(s1), "setup_ms": amg_setup * 1e3, "iterations": rep["iterations"],
-                        "reason": rep["reason_name"], "levels": amg.levels(),
-                        "norm": "unpreconditioned ||r|| / ||b|| (true residual target 1e-10)",
-                        "cycle": "fp32" if fp32 else "fp64",
-                        "true_rel_residual": rep["true_rel_residual"],
-                        "final_rnorm_rel": rep["final_rnorm"] / rep["rnorm0"] if rep["rnorm0"] else None,
-                        "rel_diff_vs_fp64": None}
-            xs[key] = xg
-        amg.close()
-        it_bytes = cg_iteration_bytes(N, nnz)
-        f64 = out["fp64"]
-        f64["achieved_gbs"] = it_bytes * f64["iterations"] / (f64["ms"] * 1e-3) / 1e9
-        f64["frac_of_hbm"] = f64["achieved_gbs"] / peak
         xa = torch.from_numpy(src / (3 * np.pi ** 2)).to(dev)
-        out["fp64"]["max_err_vs_analytic"] = float((xs["fp64"] - xa).abs().max())
-        for prec in ("mixed", "reliable", "amg", "amg_fp32_cycle"):
-            out[prec]["rel_diff_vs_fp64"] = float(
-                (xs[prec] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
-            out[f"speedup_{prec}_vs_fp64"] = f64["ms"] / out[prec]["ms"]
-        solve = out
+        solve = bench_solves(args, dev, stream, m, val, rhs, ina, xa, peak, "1 (isotropic)")
+        # the anisotropic variant kappa = diag(1, 1, 1e-3)
+        pa = ft.advdif_params(diffusivity=np.diag([1.0, 1.0, 1e-3]), have_source=True, quad_degree=2)
+        aval = torch.empty(nnz, dtype=torch.float64, device=dev)
+        arhs = torch.empty(N, dtype=torch.float64, device=dev)
+        ft.assemble_advection_diffusion_cg(m, pa, source=dsrc, val=aval, rhs=arhs, stream=stream)
+        torch.cuda.synchronize()
+        gpu["aniso_val"], gpu["aniso_rhs"] = aval.cpu().numpy(), arhs.cpu().numpy()
+        ina.zero_()
+        ft.apply_dirichlet_conditions(m, arhs, ina, dbn, dg, dt=1.0, stream=stream)
+        aniso = bench_solves(args, dev, stream, m, aval, arhs, ina, None, peak, "diag(1, 1, 1e-3)")
+        del aval, arhs
 
-    p2 = None if args.no_p2 else bench_p2(args, dev, stream)
+    p2 = None
+    if not args.no_p2:
+        p2, gpu["p2"] = bench_p2(args, dev, stream)
     projection = None if args.no_projection else bench_projection(args, dev, stream, m, X, args.n)
-    steps16 = bench_advdif_steps(args, dev, stream)
+    steps16, ts16 = bench_advdif_steps(args, dev, stream)
+    gpu["steps16"] = (ts16, steps16["iterations"])
     batch = None
     if not args.no_batch:
-        batch = bench_batch(args, dev, stream)
+        batch, keep = bench_batch(args, dev, stream)
+        gpu["batch"] = {"members": keep, "meshes": {0: M.cube_mesh(64), args.batch_fields: M.batch_mesh(0)}}
     learned = None
     if not args.no_learned:
         sizes = [int(v) for v in args.learned_sizes.split(",") if v]
@@ -914,53 +1145,87 @@ def run_ours(args, rank, ws, dist):
 
     if rank != 0:
         return
-    cpu = None
+    cpu = parity = None
     if not args.no_cpu and ws == 1:
-        s = m.sparsity()
-        col, ptr, el = m.colouring()
-        ncores = len(os.sched_getaffinity(0))
-        rate, thr, secs = cpu_assembly_rate(nd, X, src, colours=(ptr.astype(np.int64), el),
-                                            findrm=s.findrm.astype(np.int64), colm=s.colm,
-                                            nthreads=ncores)
-        adv_ms, adv_its = cpu_advdif_steps(nthreads=ncores)
-        rate1, _, secs1 = cpu_assembly_rate(nd, X, src, colours=(ptr.astype(np.int64), el),
-                                            findrm=s.findrm.astype(np.int64), colm=s.colm,
-                                            nthreads=1)
-        cpu = {"value": rate, "unit": "Melem/s", "cores": thr, "kind": "port",
-               "sample": f"one full {args.n}^3 assembly ({secs:.2f} s), OpenMP over "
-                         f"{m.ncolours} colours, oracle restatement of the reference loop",
-               "value_1_core": rate1, "sample_1_core": f"one full {args.n}^3 assembly ({secs1:.2f} s)",
-               "advdif_16_ten_steps_ms_per_step": adv_ms, "advdif_16_ten_steps_iterations": adv_its}
+        cpu, parity = cpu_legs(args, m, nd, X, src, gpu)
     value = E * ws / (ms * 1e-3) / 1e6
+    e2e = {"value": E * ws / (e2e_ms * 1e-3) / 1e6, "unit": "Melem/s",
+           "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * nnz + 8 * N,
+           "ms_per_step": e2e_ms, "assembly_ms_within": e2e_compute_ms, "d2h_copy_ms": link_ms}
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": ncu_traffic(f"assembly_p1_poisson_{args.n}"),
+                "peak_kind": peak_kind,
+                "kernel": "assembly: k_asm_p1_diffusion_df + k_rows_pull_df",
+                "kernel_ms": kernel_ms, "algorithmic_bytes": alg}
     line = {
         "metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"P1 Poisson assembly, {args.n}^3 six-tet cube, jitter 0.2h",
+        "vs_baseline": None, "dtype": "f64 (double-float element arithmetic)", "data": "synthetic",
+        "config": {"workload": workload_name(args.n),
                    "elements": E, "nodes": N, "nnz": nnz, "colours": m.ncolours,
                    "parallelism": f"replicas{ws}", "l2": "inputs larger than L2 (no flush)",
                    "assembly_tiles": list(tiles),
                    "gpu_setup_s (sparsity+colouring)": setup_s},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": ncu_traffic(f"assembly_p1_poisson_{args.n}"),
-                     "peak_kind": peak_kind,
-                     "kernel": "assembly: k_asm_p1_diffusion_df + k_rows_pull_df",
-                     "kernel_ms": kernel_ms, "algorithmic_bytes": alg},
+        "roofline": roofline,
         "cpu_baseline": cpu,
-        "e2e": {"value": E * ws / (e2e_ms * 1e-3) / 1e6, "unit": "Melem/s",
-                "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * nnz + 8 * N,
-                "ms_per_step": e2e_ms, "assembly_ms_within": e2e_compute_ms,
-                "d2h_copy_ms": link_ms},
+        "e2e": e2e,
         "gpu_launches": int(launches),
-        "clocks": clk.summary(),
+        "clocks": clocks,
+        "parity": parity,
         "solve": solve,
+        "solve_anisotropic": aniso,
         "p2": p2,
         "projection": projection,
         "advdif_16_ten_steps": steps16,
         "batch": batch,
         "learned": learned,
     }
+    line["summary"] = compact_summary(line)
     print(json.dumps(line), flush=True)
+
+
+def compact_summary(line):
+    """The headline numbers of every section in a few hundred bytes, last in the
+    line so a truncated log still holds them."""
+    def pick(d, *keys):
+        return {k: sig(d[k]) for k in keys if d and k in d}
+
+    out = {"assembly_p1_melem_s": sig(line["value"]), "e2e_melem_s": sig(line["e2e"]["value"]),
+           "roofline_frac": sig(line["roofline"]["frac"]), "kernel_ms": sig(line["roofline"]["kernel_ms"])}
+    par = line.get("parity")
+    if par:
+        out["parity"] = {k: sig(v, 2) for k, v in par.items() if k not in ("tolerances", "batch_members")}
+    for key in ("solve", "solve_anisotropic"):
+        sv = line.get(key)
+        if sv:
+            out[key] = {k: [sig(sv[k]["ms"]), sv[k]["iterations"], sig(sv[k]["true_rel_residual"], 3)]
+                        for k in ("fp64", "fp64_pc_norm", "mixed", "reliable", "amg_fp32_cycle") if k in sv}
+            out[key]["fields"] = "ms, iterations, true relative residual"
+    p2 = line.get("p2")
+    if p2:
+        out["p2_64"] = {"melem_s": sig(p2["melem_per_s"]), "frac": sig(p2["roofline"]["frac"]),
+                        "cg_fp64_ms": sig(p2["solve"]["fp64"]["ms"]), "cg_reliable_ms": sig(p2["solve"]["reliable"]["ms"])}
+    st = line.get("advdif_16_ten_steps")
+    if st:
+        out["advdif16_ms_per_step"] = sig(st["ms_per_step"])
+    b = line.get("batch")
+    if b:
+        out["batch"] = pick(b, "batch_ms", "sequential_ms", "speedup_vs_sequential")
+    pr = line.get("projection")
+    if pr:
+        out["projection_128"] = {"div_ms": sig(pr["divergence"]["ms"]), "cmc_ms": sig(pr["cmc_product"]["ms"]),
+                                 "kmk_ms": sig(pr["kmk_ms"]), "solve_ms": sig(pr["projection_solve"]["ms"]),
+                                 "amg_solve_ms": sig(pr["projection_solve_amg"]["ms"])}
+    ln = line.get("learned")
+    if ln:
+        for k, v in ln.items():
+            vs = v["variants"]
+            out[f"learned_{k}"] = {name: sig(vs[name]["mean_ms"]) for name in
+                                  ("fp64_zero", "fp64_previous", "fp64_learned", "mixed_previous", "mixed_learned",
+                                   "amg_previous") if name in vs}
+            out[f"learned_{k}"]["predict_ms"] = sig(v["predict_ms"])
+            out[f"learned_{k}"]["max_true_rel_residual"] = sig(max(x["max_true_rel_residual"] for x in vs.values()), 3)
+    return out
 
 
 def main():

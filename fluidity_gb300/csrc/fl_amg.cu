@@ -1511,7 +1511,7 @@ int build_hierarchy(fl_amg_t* H, cudaStream_t s) {
 }
 
 // K iterations of AMG-preconditioned CG (capturable; no host interaction)
-void amg_iterations(fl_amg_t* H, int K, cudaStream_t c) {
+void amg_iterations(fl_amg_t* H, int K, int unprec, cudaStream_t c) {
   AmgLevel& L0 = *H->L[0];
   const int n = L0.A.n, G = L0.G;
   const Op A = op_of(L0.A);
@@ -1525,7 +1525,7 @@ void amg_iterations(fl_amg_t* H, int K, cudaStream_t c) {
     k_amg_alpha<<<1, kT, 0, c>>>(st, H->part.p, (int)gl);
     k_amg_xr<<<gv, kT, 0, c>>>(n, st, H->p.p, H->w.p, H->y.p, H->r.p);
     precondition(H, H->r.p, H->z.p, c);
-    const double* nv = H->unprec ? H->r.p : H->z.p;  // the norm of the convergence test
+    const double* nv = unprec ? H->r.p : H->z.p;  // the norm of the convergence test
     k_dots<<<gv, kT, 0, c>>>(n, nv, nv, H->z.p, H->r.p, H->part.p);
     k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 0, nullptr);
     k_amg_p<<<gv, kT, 0, c>>>(n, st, H->z.p, H->p.p);
@@ -1604,6 +1604,9 @@ extern "C" int fl_amg_solve(fl_amg H, const fl_solver_opts* o, const double* rhs
   FL_CHECK_ARG(o->ksp_type == 0, "the AMG preconditioner is used with CG");
   FL_CHECK_ARG(o->precision == 0, "the AMG-preconditioned solve runs in FP64");
   FL_CHECK_ARG(o->max_its >= 0, "max_its");
+  FL_CHECK_ARG(o->norm_type == 0 || o->norm_type == 1, "norm_type 0 or 1");
+  // the unpreconditioned test when the handle or the options ask for it
+  const int unprec = (H->unprec || o->norm_type == 1) ? 1 : 0;
   fl_mesh_t* m = H->m;
   AmgLevel& L0 = *H->L[0];
   const int n = L0.A.n, G = L0.G;
@@ -1636,14 +1639,14 @@ extern "C" int fl_amg_solve(fl_amg H, const fl_solver_opts* o, const double* rhs
   FL_AMG_G(G, k_resid, gs, c, A, H->bb.p, H->y.p, H->r.p);
   const double* bn = nullptr;
   if (!h.guess_zero) {  // rnorm0 = ||B b|| (or ||b||) with a nonzero guess (KSPConvergedDefault)
-    if (!H->unprec) precondition(H, H->bb.p, H->z.p, c);
-    const double* v = H->unprec ? H->bb.p : H->z.p;
+    if (!unprec) precondition(H, H->bb.p, H->z.p, c);
+    const double* v = unprec ? H->bb.p : H->z.p;
     k_dots<<<gv, kT, 0, c>>>(n, v, v, nullptr, nullptr, H->part.p);
     k_amg_norm_b<<<1, kT, 0, c>>>(H->part.p, (int)gv, H->bnorm.p);
     bn = H->bnorm.p;
   }
   precondition(H, H->r.p, H->z.p, c);
-  const double* nv = H->unprec ? H->r.p : H->z.p;
+  const double* nv = unprec ? H->r.p : H->z.p;
   k_dots<<<gv, kT, 0, c>>>(n, nv, nv, H->z.p, H->r.p, H->part.p);
   k_amg_beta<<<1, kT, 0, c>>>(st, H->part.p, (int)gv, 1, bn);
   k_amg_p<<<gv, kT, 0, c>>>(n, st, H->z.p, H->p.p);
@@ -1653,7 +1656,7 @@ extern "C" int fl_amg_solve(fl_amg H, const fl_solver_opts* o, const double* rhs
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ex = nullptr;
   FL_TRY_CUDA(cudaStreamBeginCapture(c, cudaStreamCaptureModeThreadLocal));
-  amg_iterations(H, K, c);
+  amg_iterations(H, K, unprec, c);
   cudaError_t e = cudaStreamEndCapture(c, &g);
   if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
   if (g) cudaGraphDestroy(g);

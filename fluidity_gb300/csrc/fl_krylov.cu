@@ -42,7 +42,9 @@ struct KspState {
   // convergence test (KSPConvergedDefault)
   double rtol, atol, dtol, rnorm0, ttol, snorm_b;
   double rnorm;          // last residual norm tested
+  double znorm;          // preconditioned norm ||B r|| of the last residual (CG starts)
   int its, max_its, reason, done, guess_zero;
+  int unprec;            // 1: the test runs on ||r|| (KSP_NORM_UNPRECONDITIONED, CG only)
   int cg_i;              // CG iteration index (advanced on the device)
   // CG scalars
   double beta, betaold, dpi, dpiold, alpha, pcoef, dpi_next, beta_n, betaold_n;
@@ -358,9 +360,10 @@ __global__ void k_init_resid(SpArgs A, const double* __restrict__ b, const doubl
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
   if (A.st->done) return;  // a restart after convergence (device-driven GMRES)
-  double zz = 0.0, bb = 0.0, zr = 0.0;
+  double zz = 0.0, bb = 0.0, zr = 0.0, rr = 0.0, bu = 0.0;
   const double piv = A.st->pivot;
   const bool gz = A.st->guess_zero;
+  const bool unprec = A.st->unprec;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
     double ay = 0.0;
@@ -375,15 +378,27 @@ __global__ void k_init_resid(SpArgs A, const double* __restrict__ b, const doubl
       zz += zi * zi;
       bb += bi * bi;
       zr += zi * ri;
+      if (unprec) {
+        rr += ri * ri;
+        bu += b[row] * b[row];
+      }
     }
   }
   zz = block_sum<kThreads>(zz, red);
   bb = block_sum<kThreads>(bb, red);
   zr = block_sum<kThreads>(zr, red);
+  if (unprec) {
+    rr = block_sum<kThreads>(rr, red);
+    bu = block_sum<kThreads>(bu, red);
+  }
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[nparts + blockIdx.x] = bb;
     part[2 * nparts + blockIdx.x] = zr;
+    if (unprec) {
+      part[3 * nparts + blockIdx.x] = rr;
+      part[4 * nparts + blockIdx.x] = bu;
+    }
   }
 }
 
@@ -393,13 +408,20 @@ __global__ void k_cg_start(KspState* st, const double* __restrict__ part, int np
   const double zz = reduce_partials(part, nparts, red);
   const double bb = reduce_partials(part + nparts, nparts, red);
   const double zr = reduce_partials(part + 2 * nparts, nparts, red);
+  const bool unprec = st->unprec;
+  double rr = 0.0, bu = 0.0;
+  if (unprec) {
+    rr = reduce_partials(part + 3 * nparts, nparts, red);
+    bu = reduce_partials(part + 4 * nparts, nparts, red);
+  }
   if (threadIdx.x == 0) {
     KspState& S = *st;
-    S.snorm_b = sqrt(bb);
+    S.snorm_b = sqrt(unprec ? bu : bb);
     S.its = 0;
     S.reason = 0;
     S.done = 0;
-    converged_test(S, 0, sqrt(zz));
+    S.znorm = sqrt(zz);
+    converged_test(S, 0, sqrt(unprec ? rr : zz));
     S.beta = zr;
     S.betaold = 0.0;
     S.dpi = 0.0;
@@ -569,7 +591,8 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
   if (st->done) return;
   const int i = st->cg_i;
   const double a = st->alpha;
-  double zz = 0.0, zr = 0.0;
+  const bool unprec = st->unprec;
+  double zz = 0.0, zr = 0.0, rr = 0.0;
   // two rows per thread (16-byte accesses); the last odd row by the last thread
   const int n2 = n >> 1;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
@@ -589,6 +612,10 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
     zz += z1 * z1;
     zr += z0 * r0;
     zr += z1 * r1;
+    if (unprec) {
+      rr += r0 * r0;
+      rr += r1 * r1;
+    }
   }
   if ((n & 1) && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {
     const int k = n - 1;
@@ -599,19 +626,24 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
     z[k] = zk;
     zz += zk * zk;
     zr += zk * rk;
+    rr += rk * rk;
   }
   zz = block_sum_df<kThreads>(zz, redf);
   zr = block_sum_df<kThreads>(zr, redf);
+  if (unprec) rr = block_sum_df<kThreads>(rr, redf);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[gridDim.x + blockIdx.x] = zr;
+    if (unprec) part[2 * gridDim.x + blockIdx.x] = rr;
   }
   if (!last_block(ticket)) return;
   const double zzs = reduce_partials(part, gridDim.x, red);
   const double zrs = reduce_partials(part + gridDim.x, gridDim.x, red);
+  const double rrs = unprec ? reduce_partials(part + 2 * gridDim.x, gridDim.x, red) : 0.0;
   if (threadIdx.x == 0) {
     KspState& S = *st;
-    converged_test(S, i + 1, sqrt(zzs));  // KSPConvergedDefault at iteration i+1
+    // KSPConvergedDefault at iteration i+1, on ||B r|| or ||r||
+    converged_test(S, i + 1, sqrt(unprec ? rrs : zzs));
     if (!S.done) {
       S.beta = zrs;
       if (i + 1 >= S.max_its) {
@@ -1023,7 +1055,9 @@ __global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, cons
   __shared__ float2 redf[kThreads / 32];
   const int i = st->cg_i;
   const float a = (float)st->alpha;
-  df zzd = {0.0f, 0.0f}, zrd = {0.0f, 0.0f};
+  // reliable updates with the unpreconditioned test trigger on ||r|| as well
+  const bool unprec = st->rel && st->unprec;
+  df zzd = {0.0f, 0.0f}, zrd = {0.0f, 0.0f}, rrd = {0.0f, 0.0f};
   // four rows per thread (16-byte accesses); the last n % 4 rows by the last thread
   const int n4 = n >> 2;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += gridDim.x * blockDim.x) {
@@ -1043,6 +1077,7 @@ __global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, cons
       zo[u] = ro[u] * da[u];
       zzd = df_fma_ff(zo[u], zo[u], zzd);
       zrd = df_fma_ff(zo[u], ro[u], zrd);
+      if (unprec) rrd = df_fma_ff(ro[u], ro[u], rrd);
     }
     reinterpret_cast<float4*>(d)[k] = make_float4(co[0], co[1], co[2], co[3]);
     reinterpret_cast<float4*>(r)[k] = make_float4(ro[0], ro[1], ro[2], ro[3]);
@@ -1057,20 +1092,24 @@ __global__ void k_cg32_xr(int n, KspState* st, const float* __restrict__ p, cons
       z[k] = zk;
       zzd = df_fma_ff(zk, zk, zzd);
       zrd = df_fma_ff(zk, rk, zrd);
+      rrd = df_fma_ff(rk, rk, rrd);
     }
   const double zz = block_sum_df<kThreads>(zzd, redf);
   const double zr = block_sum_df<kThreads>(zrd, redf);
+  const double rr = unprec ? block_sum_df<kThreads>(rrd, redf) : 0.0;
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[gridDim.x + blockIdx.x] = zr;
+    if (unprec) part[2 * gridDim.x + blockIdx.x] = rr;
   }
   if (!last_block(ticket)) return;
   const double zzs = reduce_partials(part, gridDim.x, red);
   const double zrs = reduce_partials(part + gridDim.x, gridDim.x, red);
+  const double rrs = unprec ? reduce_partials(part + 2 * gridDim.x, gridDim.x, red) : 0.0;
   if (threadIdx.x == 0) {
     KspState& S = *st;
     S.its = i + 1;
-    S.rnorm = sqrt(zzs);
+    S.rnorm = sqrt(unprec ? rrs : zzs);
     if (!(S.rnorm == S.rnorm)) {
       S.reason = FL_DIVERGED_NANORINF;
       S.done = 1;
@@ -1110,7 +1149,8 @@ __global__ void k_outer_resid(SpArgs A, const double* __restrict__ b, const doub
   const double piv = A.st->pivot;
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
-  double zz = 0.0, bb = 0.0, zr = 0.0;
+  const bool unprec = A.st->unprec;
+  double zz = 0.0, bb = 0.0, zr = 0.0, rr = 0.0, bu = 0.0;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
     double s = 0.0;
@@ -1126,15 +1166,27 @@ __global__ void k_outer_resid(SpArgs A, const double* __restrict__ b, const doub
       zz += zi * zi;
       bb += bi * bi;
       zr += zi * ri;
+      if (unprec) {
+        rr += ri * ri;
+        bu += b[row] * b[row];
+      }
     }
   }
   zz = block_sum<kThreads>(zz, red);
   bb = block_sum<kThreads>(bb, red);
   zr = block_sum<kThreads>(zr, red);
+  if (unprec) {
+    rr = block_sum<kThreads>(rr, red);
+    bu = block_sum<kThreads>(bu, red);
+  }
   if (threadIdx.x == 0) {
     part[blockIdx.x] = zz;
     part[nparts + blockIdx.x] = bb;
     part[2 * nparts + blockIdx.x] = zr;
+    if (unprec) {
+      part[3 * nparts + blockIdx.x] = rr;
+      part[4 * nparts + blockIdx.x] = bu;
+    }
   }
 }
 
@@ -1148,11 +1200,17 @@ __global__ void k_rel_commit(KspState* st, const double* __restrict__ part, int 
   const double zz = reduce_partials(part, nparts, red);
   const double bb = reduce_partials(part + nparts, nparts, red);
   const double zr = reduce_partials(part + 2 * nparts, nparts, red);
+  const bool unprec = st->unprec;
+  double rr = 0.0, bu = 0.0;
+  if (unprec) {
+    rr = reduce_partials(part + 3 * nparts, nparts, red);
+    bu = reduce_partials(part + 4 * nparts, nparts, red);
+  }
   if (threadIdx.x != 0) return;
   KspState& S = *st;
-  const double rn = sqrt(zz);
+  const double rn = sqrt(unprec ? rr : zz);
   if (S.cg_i == 0 && S.outer == 0 && !S.hold) {
-    S.snorm_b = sqrt(bb);
+    S.snorm_b = sqrt(unprec ? bu : bb);
     S.its = 0;
     S.reason = 0;
     S.done = 0;
@@ -1268,6 +1326,9 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   FL_CHECK_ARG(restart <= kMaxRestart, "gmres restart above 64");
   FL_CHECK_ARG(o->precision == 0 || o->ksp_type == 0, "mixed precision is a CG refinement");
   FL_CHECK_ARG(o->precision >= 0 && o->precision <= 2, "precision 0 (fp64), 1 or 2 (mixed)");
+  FL_CHECK_ARG(o->norm_type == 0 || o->norm_type == 1, "norm_type 0 (preconditioned) or 1 (unpreconditioned)");
+  FL_CHECK_ARG(o->norm_type == 0 || o->ksp_type == 0,
+               "the unpreconditioned norm needs CG (left-preconditioned GMRES tests the preconditioned norm)");
   KrylovWork* W = work_of(m);
   if (!W) return FL_ERR_NOMEM;
   const int n = m->N;
@@ -1290,6 +1351,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   h.dtol = o->dtol > 0 ? o->dtol : 1e5;
   h.max_its = o->max_its;
   h.guess_zero = o->start_from_zero ? 1 : 0;
+  h.unprec = o->norm_type == 1 ? 1 : 0;
   FL_TRY_CUDA(cudaMemcpyAsync(W->st.p, &h, sizeof(KspState), cudaMemcpyHostToDevice, s));
   KspState* st = W->st.p;
   SpArgs A{n, m->findrm.p, m->colm.p, val, ghost, st};
@@ -1474,7 +1536,9 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
       if (rn <= ttol) { reason = rn < o->atol ? FL_CONVERGED_ATOL : FL_CONVERGED_RTOL; break; }
       if (total_inner >= o->max_its) { reason = FL_DIVERGED_ITS; break; }
       // inner solve B A d = B r in fp32 from d = 0 to inner_rtol * ||B r||
-      hs.ttol = inner_rtol * rn;
+      // (the inner test is on the preconditioned fp32 residual whichever
+      // norm the outer test uses)
+      hs.ttol = inner_rtol * hs.znorm;
       hs.done = 0;
       hs.reason = 0;
       hs.dpi = 0.0;
@@ -1531,10 +1595,12 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
 }
 
 // ------------------------------------------------- batched / graph CG --
-__global__ void k_state_init(KspState* st, double rtol, double atol, double dtol, int max_its, int guess_zero) {
+__global__ void k_state_init(KspState* st, double rtol, double atol, double dtol, int max_its, int guess_zero,
+                             int unprec) {
   note_launch();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   KspState& S = *st;
+  S.unprec = unprec;
   S.rtol = rtol;
   S.atol = atol;
   S.dtol = dtol;
@@ -1561,6 +1627,8 @@ int cg_prepare(CgPlan& P, fl_mesh_t* m, const fl_solver_opts* o, const double* v
   FL_CHECK_ARG(m && o && val && rhs && x, "null argument");
   FL_CHECK_ARG((o->ksp_type == 0 || o->ksp_type == 1) && o->precision == 0,
                "graph-batched solves are FP64 CG or GMRES");
+  FL_CHECK_ARG(o->norm_type == 0 || (o->norm_type == 1 && o->ksp_type == 0),
+               "norm_type 0, or 1 (unpreconditioned) with CG");
   FL_CHECK_ARG(o->max_its >= 0, "max_its");
   const int restart = o->restart > 0 ? o->restart : 30;
   FL_CHECK_ARG(restart <= kMaxRestart, "gmres restart above 64");
@@ -1610,7 +1678,7 @@ void cg_setup_launch(CgPlan& P, cudaStream_t s) {
   const int G = P.G;
   const unsigned gsp = P.gsp;
   k_state_init<<<1, 32, 0, s>>>(st, P.o.rtol, P.o.atol, P.o.dtol > 0 ? P.o.dtol : 1e5, P.o.max_its,
-                                 P.o.start_from_zero ? 1 : 0);
+                                 P.o.start_from_zero ? 1 : 0, P.o.norm_type == 1 ? 1 : 0);
   k_diag<<<P.gv, kThreads, 0, s>>>(P.A, P.m->centrm.p, W->dinv.p, W->part.p, W->part.p + P.np);
   k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + P.np, (int)P.gv);
   k_dinv<<<P.gv, kThreads, 0, s>>>(P.n, P.ghost, st, W->dinv.p, nullptr);

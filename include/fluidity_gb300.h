@@ -228,6 +228,12 @@ typedef struct {
                                 Krylov space; the convergence test runs on
                                 the fp64 residual (CG only)                  */
   double inner_rtol;         /* inner relative tolerance (precision = 1)    */
+  int32_t norm_type;         /* KSPSetNormType: 0 = preconditioned ||B r||
+                                (PETSc's default for CG and GMRES with left
+                                Jacobi); 1 = unpreconditioned ||r||, CG only
+                                (every precision), so rtol bounds the true
+                                relative residual ||b - A x|| / ||b||        */
+  int32_t pad;
 } fl_solver_opts;
 
 typedef struct {

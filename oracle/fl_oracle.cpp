@@ -808,7 +808,7 @@ int orc_petsc_solve(int n, const int64_t* findrm, const int* colm, const double*
                     int ksp_type /*0 cg, 1 gmres*/, int restart, double rtol, double atol,
                     double dtol, int max_its, int start_from_zero, int* its_out,
                     int* reason_out, double* final_rnorm, double* history, int hist_cap,
-                    int nthreads) {
+                    int nthreads, int norm_type) {
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -858,9 +858,13 @@ int orc_petsc_solve(int n, const int64_t* findrm, const int* colm, const double*
     for (int i = 0; i < n; ++i) z[i] = r[i] * dinv[i];
   };
   Conv C{rtol, atol, dtol, 0, 0, max_its, guess_zero};
+  // KSPSetNormType: the preconditioned norm ||B r|| (PETSc's default for CG
+  // and left-preconditioned GMRES) or, for CG, the unpreconditioned ||r||;
+  // the nonzero-guess scale of KSPConvergedDefault is ||B b|| or ||b|| alike.
+  const bool unprec = norm_type == 1 && ksp_type == 0;
   std::vector<double> tmpz(n);
   pc(b.data(), tmpz.data());
-  double snorm_b = std::sqrt(dot(n, tmpz.data(), tmpz.data()));
+  double snorm_b = unprec ? std::sqrt(dot(n, b.data(), b.data())) : std::sqrt(dot(n, tmpz.data(), tmpz.data()));
   int nh = 0;
   auto log = [&](double r) { if (history && nh < hist_cap) history[nh] = r; ++nh; };
   int reason = 0, its = 0;
@@ -875,7 +879,7 @@ int orc_petsc_solve(int n, const int64_t* findrm, const int* colm, const double*
       r = b;
     }
     pc(r.data(), z.data());
-    double dp = std::sqrt(dot(n, z.data(), z.data()));
+    double dp = unprec ? std::sqrt(dot(n, r.data(), r.data())) : std::sqrt(dot(n, z.data(), z.data()));
     rn = dp;
     log(dp);
     reason = converged(C, 0, dp, snorm_b);
@@ -905,7 +909,7 @@ int orc_petsc_solve(int n, const int64_t* findrm, const int* colm, const double*
           r[k] -= a * w[k];
         }
         pc(r.data(), z.data());
-        dp = std::sqrt(dot(n, z.data(), z.data()));
+        dp = unprec ? std::sqrt(dot(n, r.data(), r.data())) : std::sqrt(dot(n, z.data(), z.data()));
         rn = dp;
         log(dp);
         reason = converged(C, i + 1, dp, snorm_b);

@@ -208,8 +208,12 @@ def apply_dirichlet(nodes, g, T, dt, rhs, inactive):
 
 def petsc_solve(findrm, colm, val, inactive, rhs, x0=None, *, ksp="cg", restart=30,
                 rtol=1e-10, atol=0.0, dtol=1e5, max_its=10000, start_from_zero=True,
-                nthreads=0, history=False):
-    """(x, its, reason, final_rnorm[, history]) -- Solvers.F90:111-1302 + PETSc KSP."""
+                nthreads=0, history=False, norm="preconditioned"):
+    """(x, its, reason, final_rnorm[, history]) -- Solvers.F90:111-1302 + PETSc KSP.
+
+    ``norm`` is KSPSetNormType's choice for the convergence test:
+    "preconditioned" (||B r||, PETSc's default) or, for CG, "unpreconditioned"
+    (||r||, so rtol bounds the true relative residual)."""
     n = findrm.size - 1
     f = np.ascontiguousarray(findrm, dtype=np.int64)
     c = np.ascontiguousarray(colm, dtype=np.int32)
@@ -223,7 +227,8 @@ def petsc_solve(findrm, colm, val, inactive, rhs, x0=None, *, ksp="cg", restart=
     nh = lib().orc_petsc_solve(
         n, _p(f), _p(c), _p(v), _p(ina), _p(b), _p(x), 0 if ksp == "cg" else 1, int(restart),
         C.c_double(rtol), C.c_double(atol), C.c_double(dtol), int(max_its), int(bool(start_from_zero)),
-        C.byref(its), C.byref(reason), C.byref(rn), _p(hist), cap, int(nthreads))
+        C.byref(its), C.byref(reason), C.byref(rn), _p(hist), cap, int(nthreads),
+        1 if norm == "unpreconditioned" else 0)
     if history:
         return x, its.value, reason.value, rn.value, hist[: min(nh, cap)]
     return x, its.value, reason.value, rn.value

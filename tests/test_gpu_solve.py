@@ -130,6 +130,50 @@ def test_mixed_precision_reaches_fp64_tolerance(O, kappa, precision):
         assert rm["iterations"] <= 1.25 * r64["iterations"] + 5
 
 
+@pytest.mark.parametrize("start_from_zero", [True, False])
+def test_unpreconditioned_norm_cg_matches_oracle(O, start_from_zero):
+    """KSP_NORM_UNPRECONDITIONED: the test on ||r|| against the oracle's CG
+    with the same norm (iterations +-1, same solution), and the true relative
+    residual at the tolerance (the recurrence residual of FP64 CG drifts from
+    the true one only by rounding)."""
+    m, X, val, rhs, ina = poisson(O, 10, kappa=np.diag([1.0, 1.0, 1e-3]))
+    x0 = np.zeros(m.N) if start_from_zero else 1e-3 * np.cos(3 * X[:, 1])
+    x = x0.copy()
+    opts = ft.solver_options(rtol=1e-10, norm="unpreconditioned", start_from_zero=start_from_zero)
+    rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina)
+    ox, oits, oreason, orn = oracle_solve(O, m, val, rhs, ina, x0=x0, rtol=1e-10, norm="unpreconditioned",
+                                          start_from_zero=start_from_zero)
+    assert rep["reason"] == oreason == 2
+    assert abs(rep["iterations"] - oits) <= 1
+    assert np.abs(x - ox).max() <= 1e-7 * np.abs(ox).max()
+    assert rep["true_rel_residual"] <= 1.05e-10
+    # the preconditioned test stops earlier or later, at another iteration
+    _, pits, _, _ = oracle_solve(O, m, val, rhs, ina, x0=x0, rtol=1e-10, start_from_zero=start_from_zero)
+    assert pits != oits
+
+
+@pytest.mark.parametrize("precision", ["mixed", "reliable"])
+def test_unpreconditioned_norm_mixed_meets_true_tolerance(O, precision):
+    """Mixed precision with the unpreconditioned test: the outer test runs on
+    the FP64 residual ||b - A x||, so the reported true relative residual is at
+    most rtol."""
+    m, X, val, rhs, ina = poisson(O, 14, kappa=np.diag([1.0, 1.0, 1e-3]))
+    xm = np.zeros(m.N)
+    rm = ft.petsc_solve(m, xm, val, rhs, ft.solver_options(rtol=1e-10, precision=precision,
+                                                           norm="unpreconditioned"), inactive=ina)
+    assert rm["reason"] == 2 and rm["outer_iterations"] >= 2
+    assert rm["true_rel_residual"] <= 1e-10 * (1 + 1e-9)
+    xd = direct(m, val, rhs, ina)
+    assert np.abs(xm - xd).max() <= 1e-7 * np.abs(xd).max()
+
+
+def test_unpreconditioned_norm_needs_cg(O):
+    m, X, val, rhs, ina = poisson(O, 3)
+    with pytest.raises(RuntimeError, match="unpreconditioned"):
+        ft.petsc_solve(m, np.zeros(m.N), val, rhs,
+                       ft.solver_options(ksp="gmres", norm="unpreconditioned"), inactive=ina)
+
+
 def test_reliable_updates_from_a_guess_and_iteration_limit(O):
     m, X, val, rhs, ina = poisson(O, 12)
     xd = direct(m, val, rhs, ina)

@@ -122,3 +122,22 @@ def test_failure_reasons(O):
     bad[np.nonzero(ina == 0)[0][0]] = np.nan
     x, its, reason, rn = O.petsc_solve(f, c, val, ina, bad, ksp="cg")
     assert reason == -9  # KSP_DIVERGED_NANORINF
+
+
+def test_unpreconditioned_norm_bounds_true_residual(O):
+    """KSPSetNormType(KSP_NORM_UNPRECONDITIONED) for CG: the test runs on ||r||,
+    so the true relative residual ||b - A x|| / ||b|| of the ghost-reduced
+    system is at rtol when the solve stops, and the solution is the direct
+    one."""
+    nd, X, Xf, f, c, val, rhs, ina, bn = poisson_system(O, 8)
+    x, its, reason, rn = O.petsc_solve(f, c, val, ina, rhs, ksp="cg", rtol=1e-10, norm="unpreconditioned")
+    assert reason == 2
+    n = f.size - 1
+    A = sp.csr_matrix((val, c, f), shape=(n, n))
+    act, gh = np.nonzero(ina == 0)[0], np.nonzero(ina)[0]
+    b = rhs[act] - A[act][:, gh] @ rhs[gh]
+    r = b - A[act][:, act] @ x[act]
+    assert np.linalg.norm(r) <= 1.05e-10 * np.linalg.norm(b)
+    assert rn <= 1e-10 * np.linalg.norm(b)
+    xd = reduced_direct(f, c, val, rhs, ina)
+    assert np.abs(x - xd).max() <= 1e-8 * np.abs(xd).max()
