@@ -46,7 +46,15 @@ class AdvDifParams(C.Structure):
         ("have_mass", C.c_int32), ("lump_mass", C.c_int32), ("have_advection", C.c_int32),
         ("have_diffusivity", C.c_int32), ("isotropic_diffusivity", C.c_int32),
         ("have_source", C.c_int32), ("have_absorption", C.c_int32), ("quad_degree", C.c_int32),
-        ("diffusivity", C.c_double * 9),
+        ("diffusivity", C.c_double * 9), ("integrate_advection_by_parts", C.c_int32), ("pad", C.c_int32),
+    ]
+
+
+class FaceBcs(C.Structure):
+    _fields_ = [
+        ("nfaces", C.c_int32), ("floc", C.c_int32), ("index_base", C.c_int32), ("pad", C.c_int32),
+        ("faces", C.c_void_p), ("xfaces", C.c_void_p), ("face_ele", C.c_void_p), ("bc_type", C.c_void_p),
+        ("bc_value", C.c_void_p), ("bc_value2", C.c_void_p),
     ]
 
 
@@ -97,6 +105,7 @@ EXPORTS = [
     "fl_gpu_secondorder_register", "fl_dev_assemble_divergence_cg", "fl_dev_lumped_mass",
     "fl_dev_mult_div_vector_div_T", "fl_dev_mult_div_invscalar_div_T", "fl_dev_assemble_kmk",
     "fl_dev_masslumped_poisson_rhs", "fl_dev_correct_masslumped_velocity", "fl_dev_csr_addto",
+    "fl_dev_assemble_advdif_faces", "fl_gpu_assemble_advdif_faces",
 ]
 
 _P = C.c_void_p
@@ -164,6 +173,10 @@ _SIGNATURES = {
     "fl_dev_masslumped_poisson_rhs": (C.c_int, [_P, _P, _P, _P, _P, _P, _D, _D, _P, _P]),
     "fl_dev_correct_masslumped_velocity": (C.c_int, [_P, _P, _P, _P, _P, _P]),
     "fl_dev_csr_addto": (C.c_int, [_P, _P, _P, _D, _P]),
+    "fl_dev_assemble_advdif_faces": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(FaceBcs),
+                                               C.POINTER(Fields), _P, _P, _P]),
+    "fl_gpu_assemble_advdif_faces": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(FaceBcs),
+                                               C.POINTER(Fields), _P, _P]),
 }
 assert sorted(_SIGNATURES) == sorted(EXPORTS)
 

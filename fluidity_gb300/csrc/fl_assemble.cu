@@ -126,6 +126,7 @@ struct AsmArgs {
   double beta;
   double kappa[9];
   int have_mass, lump, have_adv, have_beta, have_diff, iso, have_src, have_abs, use_dt;
+  int by_parts;             // integrate_advection_by_parts
 };
 
 // General element kernel: any term combination, P1 or P2 fields, P1
@@ -224,13 +225,16 @@ __global__ void __launch_bounds__(128) k_asm_general(AsmArgs A) {
         }
       }
       if (A.have_adv) {
+        // not by parts: N_i u.grad N_j (T[i][j]) + beta N_i N_j div u;
+        // by parts (:1019-1057): -(grad N_i . u) N_j (T[j][i]) - (1 - beta) N_i N_j div u
 #pragma unroll
         for (int j = 0; j < LOC; ++j) {
           double s = 0.0;
 #pragma unroll
           for (int k = 0; k < 4; ++k)
 #pragma unroll
-            for (int a = 0; a < 3; ++a) s += V[k][a] * R.T[i][j][k][a];
+            for (int a = 0; a < 3; ++a) s += V[k][a] * (A.by_parts ? R.T[j][i][k][a] : R.T[i][j][k][a]);
+          if (A.by_parts) s = -s;
           if (A.have_beta) {
             double d = 0.0;
 #pragma unroll
@@ -1556,8 +1560,11 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   // epsilon(0.0) is the real(8) machine epsilon under -fdefault-real-8
   const double eps = 2.220446049250313e-16;
   A.use_dt = fabs(A.theta_dt) > eps;
-  A.beta = p->beta;
-  A.have_beta = p->have_advection && fabs(p->beta) > eps;
+  // the divergence coefficient: beta, or -(1 - beta) by parts (applied when
+  // |beta| resp. |1 - beta| exceeds epsilon, :1037 and :1087)
+  A.by_parts = p->integrate_advection_by_parts != 0;
+  A.beta = A.by_parts ? -(1.0 - p->beta) : p->beta;
+  A.have_beta = p->have_advection && fabs(A.by_parts ? 1.0 - p->beta : p->beta) > eps;
   for (int k = 0; k < 9; ++k) A.kappa[k] = p->diffusivity[k];
   A.have_mass = p->have_mass;
   A.lump = p->have_mass && p->lump_mass;
@@ -2122,6 +2129,355 @@ extern "C" int fl_gpu_apply_dirichlet(fl_mesh m, int32_t nb, const int32_t* node
   FL_TRY(fl_dev_apply_dirichlet(m, nb, m->st_nodes.p, base, m->st_g.p, tp, dt, m->st_rhs.p, m->st_ina.p, s));
   FL_TRY_CUDA(cudaMemcpyAsync(rhs, m->st_rhs.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaMemcpyAsync(inactive, m->st_ina.p, m->N, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  return FL_OK;
+}
+
+// ------------------------------------------------------------ surface loop --
+// assemble_advection_diffusion_face_cg (Advection_Diffusion_CG.F90:1228-1286)
+// for every surface element, added row by row: one thread per field node adds
+// the faces holding it in ascending face order (the reference's face loop
+// order), so the sums are deterministic.  Faces are O(n^2) against O(n^3)
+// elements, so the face quantities are simply recomputed for each of a face's
+// nodes, in FP64.
+namespace fl {
+
+struct FaceAsmArgs {
+  int32_t N, floc, base, E;
+  const int32_t* fptr;
+  const int32_t* flist;
+  const int32_t* faces;
+  const int32_t* xfaces;
+  const int32_t* face_ele;
+  const int32_t* bc_type;
+  const double* bc1;
+  const double* bc2;
+  const int32_t* xnd;
+  const double* X;
+  const double* u;   // P1 velocity on the coordinate mesh (3 per vertex)
+  const double* t;
+  const int32_t* findrm;
+  const int32_t* colm;
+  double* val;
+  double* rhs;
+  double theta, dt_theta;
+  int adv, diff, use_dt, ngi;
+  double ql[6][3];  // barycentric coordinates of the triangle rule's points
+  double qw[6];
+  ErrWord* err;
+};
+
+// Triangle rules of degree 1..4 (Quadrature.F90 construct_tri_quadratures,
+// Str71 and the degree-4 six-point rule): (a, a, b) generators expanded in
+// the order of tri_permutations(5), or the centroid.
+static int tri_rule(int degree, double l[6][3], double w[6]) {
+  int n = 0;
+  auto cen = [&](double a, double wt) {
+    l[n][0] = l[n][1] = l[n][2] = a;
+    w[n++] = wt;
+  };
+  auto gen = [&](double a, double wt) {
+    const double b = 1.0 - 2.0 * a;
+    const double c[2] = {a, b};
+    const int perm[3][3] = {{1, 1, 2}, {1, 2, 1}, {2, 1, 1}};
+    for (int k = 0; k < 3; ++k) {
+      for (int j = 0; j < 3; ++j) l[n][j] = c[perm[k][j] - 1];
+      w[n++] = wt;
+    }
+  };
+  switch (degree) {
+    case 1: cen(0.333333333333333333333333333333333, 0.5); break;
+    case 2: gen(0.166666666666666666666666666666666, 0.166666666666666666666666666666666); break;
+    case 3:
+      cen(0.333333333333333333333333333333333, -0.28125);
+      gen(0.2, 0.260416666666666666666666666666666);
+      break;
+    case 4:
+      gen(0.0915762135097707434595714634022015, 0.0549758718276609338191631624501052);
+      gen(0.445948490915964886318329253883051, 0.111690794839005732847503504216561);
+      break;
+    default: return 0;
+  }
+  return n;
+}
+
+// Lagrange functions of the face (P1: barycentrics; P2: vertex L(2L-1),
+// edge 4 L_a L_b, in the triangle's local order).
+__device__ __forceinline__ void face_shape(int floc, const double l[3], double* n) {
+  if (floc == 3) {
+    n[0] = l[0];
+    n[1] = l[1];
+    n[2] = l[2];
+    return;
+  }
+  n[0] = l[0] * (2.0 * l[0] - 1.0);
+  n[1] = (2.0 * l[0]) * (2.0 * l[1]);
+  n[2] = l[1] * (2.0 * l[1] - 1.0);
+  n[3] = (2.0 * l[0]) * (2.0 * l[2]);
+  n[4] = (2.0 * l[1]) * (2.0 * l[2]);
+  n[5] = l[2] * (2.0 * l[2] - 1.0);
+}
+
+__global__ void __launch_bounds__(128) k_advdif_faces(FaceAsmArgs F) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F.N; i += gridDim.x * blockDim.x) {
+    const int qb = F.fptr[i], qe = F.fptr[i + 1];
+    for (int q = qb; q < qe; ++q) {
+      const int f = F.flist[q];
+      const int ty = F.bc_type ? F.bc_type[f] : 0;
+      if (ty == 3) continue;  // internal
+      if (ty != 0 && ty != 1 && ty != 2 && ty != 4) {
+        set_err(F.err, FL_ERR_ARG, f);
+        continue;
+      }
+      if (ty == 2 && F.diff) {  // FLExit in add_diffusivity_face_cg
+        set_err(F.err, FL_ERR_ARG, f);
+        continue;
+      }
+      const bool dface = F.diff && (ty == 1 || ty == 4);
+      if (!F.adv && !dface) continue;
+      const int floc = F.floc;
+      int fn[6], li = -1;
+      for (int j = 0; j < floc; ++j) {
+        fn[j] = F.faces[(int64_t)floc * f + j] - F.base;
+        if (fn[j] == i) li = j;
+      }
+      int xv[3];
+      for (int j = 0; j < 3; ++j) xv[j] = F.xfaces[3 * (int64_t)f + j] - F.base;
+      if (li < 0) {
+        set_err(F.err, FL_ERR_ARG, f);
+        continue;
+      }
+      double Xf[3][3];
+      for (int j = 0; j < 3; ++j)
+        for (int a = 0; a < 3; ++a) Xf[j][a] = F.X[3 * (int64_t)xv[j] + a];
+      // transform_facet_to_physical: J = [X1 - X3, X2 - X3], detJ = |J1 x J2|
+      double J[3][2];
+      for (int a = 0; a < 3; ++a) {
+        J[a][0] = Xf[0][a] - Xf[2][a];
+        J[a][1] = Xf[1][a] - Xf[2][a];
+      }
+      double detJ = 0.0;
+      for (int k = 1; k <= 3; ++k) {
+        const int c2 = (k + 1) % 3, c1 = k % 3;
+        const double v = J[c2][0] * J[c1][1] - J[c2][1] * J[c1][0];
+        detJ += v * v;
+      }
+      detJ = sqrt(detJ);
+      double nrm[3] = {0.0, 0.0, 0.0};
+      if (F.adv) {
+        const int el = F.face_ele[f] - F.base;
+        if (el < 0 || el >= F.E) {
+          set_err(F.err, FL_ERR_ARG, f);
+          continue;
+        }
+        double cf[3] = {0.0, 0.0, 0.0}, ce[3] = {0.0, 0.0, 0.0}, ow[3];
+        for (int j = 0; j < 3; ++j)
+          for (int a = 0; a < 3; ++a) cf[a] += Xf[j][a];
+        for (int j = 0; j < 4; ++j) {
+          const int v = F.xnd[4 * (int64_t)el + j];
+          for (int a = 0; a < 3; ++a) ce[a] += F.X[3 * (int64_t)v + a];
+        }
+        for (int a = 0; a < 3; ++a) ow[a] = cf[a] / 3.0 - ce[a] / 4.0;
+        double n[3] = {J[1][0] * J[2][1] - J[2][0] * J[1][1], J[2][0] * J[0][1] - J[0][0] * J[2][1],
+                       J[0][0] * J[1][1] - J[1][0] * J[0][1]};
+        const double o = n[0] * ow[0] + n[1] * ow[1] + n[2] * ow[2];
+        for (int a = 0; a < 3; ++a) n[a] *= o;
+        const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int a = 0; a < 3; ++a) nrm[a] = n[a] / len;
+      }
+      double Tf[6];
+      for (int j = 0; j < floc; ++j) Tf[j] = F.t ? F.t[fn[j]] : 0.0;
+      double Madd[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, Radd = 0.0;
+      if (F.adv) {
+        // add_advection_face_cg: A_ij = sum_g (N_i N_j) detwei_g (u_g . n)
+        double A[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int g = 0; g < F.ngi; ++g) {
+          double N[6], Nu[3];
+          face_shape(floc, F.ql[g], N);
+          face_shape(3, F.ql[g], Nu);
+          double un = 0.0;
+          for (int a = 0; a < 3; ++a) {
+            double uq = 0.0;
+            for (int k = 0; k < 3; ++k) uq += F.u[3 * (int64_t)xv[k] + a] * Nu[k];
+            un += uq * nrm[a];
+          }
+          const double w = (detJ * F.qw[g]) * un;
+          for (int j = 0; j < floc; ++j) A[j] += (N[li] * N[j]) * w;
+        }
+        if (F.use_dt) {
+          if (ty == 2) {
+            const double* gv = F.bc1 + (int64_t)floc * f;
+            double sdiff = 0.0;
+            for (int j = 0; j < floc; ++j) sdiff += A[j] * (gv[j] - Tf[j]);
+            Radd = Radd - F.theta * sdiff;
+          } else {
+            for (int j = 0; j < floc; ++j) Madd[j] = Madd[j] + F.dt_theta * A[j];
+          }
+        }
+        double st = 0.0;
+        for (int j = 0; j < floc; ++j) st += A[j] * Tf[j];
+        Radd = Radd - st;
+      }
+      if (dface) {
+        // add_diffusivity_face_cg: rhs += shape_rhs(N, detwei g_q); robin also
+        // int N_i N_j g2 into the matrix (dt theta) and its product with t out of the rhs
+        const double* g1 = F.bc1 + (int64_t)floc * f;
+        const double* g2 = ty == 4 ? F.bc2 + (int64_t)floc * f : nullptr;
+        double sr = 0.0, Rm[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int g = 0; g < F.ngi; ++g) {
+          double N[6];
+          face_shape(floc, F.ql[g], N);
+          const double dw = detJ * F.qw[g];
+          double gq = 0.0;
+          for (int k = 0; k < floc; ++k) gq += g1[k] * N[k];
+          sr += N[li] * (dw * gq);
+          if (g2) {
+            double hq = 0.0;
+            for (int k = 0; k < floc; ++k) hq += g2[k] * N[k];
+            const double w = dw * hq;
+            for (int j = 0; j < floc; ++j) Rm[j] += (N[li] * N[j]) * w;
+          }
+        }
+        Radd = Radd + sr;
+        if (g2) {
+          if (F.use_dt)
+            for (int j = 0; j < floc; ++j) Madd[j] = Madd[j] + F.dt_theta * Rm[j];
+          double st = 0.0;
+          for (int j = 0; j < floc; ++j) st += Rm[j] * Tf[j];
+          Radd = Radd - st;
+        }
+      }
+      // addto(matrix, face_nodes, face_nodes, matrix_addto); addto(rhs, ...)
+      const int rb = F.findrm[i], re = F.findrm[i + 1];
+      for (int j = 0; j < floc; ++j) {
+        if (Madd[j] == 0.0) continue;
+        const int p = csr_find(F.colm, rb, re, fn[j]);
+        if (p < 0) {
+          set_err(F.err, FL_ERR_OUTSIDE_PATTERN, i);
+          continue;
+        }
+        F.val[p] += Madd[j];
+      }
+      F.rhs[i] += Radd;
+    }
+  }
+}
+
+static int advdif_faces(fl_mesh_t* m, const fl_advdif_params* p, const fl_face_bcs* fb, const fl_fields* f,
+                        double* val, double* rhs, cudaStream_t s) {
+  FL_CHECK_ARG(m && p && fb && f && val && rhs, "null argument");
+  FL_CHECK_ARG(fb->nfaces >= 0, "nfaces");
+  FL_CHECK_ARG(fb->index_base == 0 || fb->index_base == 1, "index_base");
+  FL_CHECK_ARG(fb->floc == (m->loc == 4 ? 3 : 6), "floc must be 3 for a P1 field mesh, 6 for P2");
+  const bool adv = p->have_advection && p->integrate_advection_by_parts;
+  const bool diff = p->have_diffusivity != 0;
+  if (fb->nfaces == 0 || !(adv || diff)) return FL_OK;  // (:608-611)
+  FL_CHECK_ARG(fb->faces && fb->xfaces, "faces and xfaces");
+  FL_CHECK_ARG(!adv || (fb->face_ele && f->velocity), "advection by parts needs face_ele and the velocity");
+  FL_CHECK_ARG(fb->bc_type == nullptr || fb->bc_value != nullptr || !diff,
+               "bc_value is needed for neumann, robin and weak Dirichlet faces");
+  FaceAsmArgs F{};
+  F.ngi = tri_rule(p->quad_degree, F.ql, F.qw);
+  FL_CHECK_ARG(F.ngi > 0, "quadrature degree 1..4");
+  FL_TRY(node_face_lists(m, fb->nfaces, fb->floc, fb->faces, fb->index_base, s));
+  F.N = m->N;
+  F.floc = fb->floc;
+  F.base = fb->index_base;
+  F.E = m->E;
+  F.fptr = m->face_ptr.p;
+  F.flist = m->face_list.p;
+  F.faces = fb->faces;
+  F.xfaces = fb->xfaces;
+  F.face_ele = fb->face_ele;
+  F.bc_type = fb->bc_type;
+  F.bc1 = fb->bc_value;
+  F.bc2 = fb->bc_value2;
+  F.xnd = m->xndglno.p;
+  F.X = m->coords.p;
+  F.u = f->velocity;
+  F.t = f->t;
+  F.findrm = m->findrm.p;
+  F.colm = m->colm.p;
+  F.val = val;
+  F.rhs = rhs;
+  F.theta = p->theta;
+  F.dt_theta = p->dt * p->theta;
+  F.use_dt = fabs(F.dt_theta) > 2.220446049250313e-16;
+  F.adv = adv;
+  F.diff = diff;
+  F.err = m->err.p;
+  k_advdif_faces<<<grid_for(m->N, 128), 128, 0, s>>>(F);
+  FL_TRY_CUDA(cudaGetLastError());
+  return check_err(m->err.p, s,
+                   "surface loop: a face is invalid, has a weak Dirichlet condition with a diffusivity "
+                   "(FLExit in the reference), lacks its robin values, or adds outside the sparsity pattern");
+}
+
+}  // namespace fl
+
+extern "C" int fl_dev_assemble_advdif_faces(fl_mesh m, const fl_advdif_params* p, const fl_face_bcs* fb,
+                                            const fl_fields* f, double* val, double* rhs, void* stream) {
+  FL_CHECK_ARG(m, "null mesh");
+  return fl::advdif_faces(m, p, fb, f, val, rhs, pick_stream(m, stream));
+}
+
+extern "C" int fl_gpu_assemble_advdif_faces(fl_mesh m, const fl_advdif_params* p, const fl_face_bcs* fb,
+                                            const fl_fields* f, double* val, double* rhs) {
+  using namespace fl;
+  FL_CHECK_ARG(m && p && fb && f && val && rhs, "null argument");
+  FL_CHECK_ARG(fb->nfaces >= 0 && fb->floc > 0 && fb->floc <= 6, "nfaces and floc");
+  cudaStream_t s = m->stream;
+  const int nf = fb->nfaces, floc = fb->floc;
+  // device copies of the face arrays and fields in the mesh's grow-only
+  // staging buffers (calls on one handle share them)
+  const size_t ni = (size_t)nf * (floc + 3 + 2), nd = (size_t)nf * floc * 2;
+  FL_TRY(m->st_nodes.reserve(ni));
+  FL_TRY(m->st_g.reserve(nd));
+  int32_t* d_faces = m->st_nodes.p;
+  int32_t* d_xfaces = d_faces + (size_t)nf * floc;
+  int32_t* d_fe = d_xfaces + (size_t)nf * 3;
+  int32_t* d_bt = d_fe + nf;
+  double* d_b1 = m->st_g.p;
+  double* d_b2 = m->st_g.p + (size_t)nf * floc;
+  if (nf > 0) {
+    FL_CHECK_ARG(fb->faces && fb->xfaces, "faces and xfaces");
+    FL_TRY_CUDA(cudaMemcpyAsync(d_faces, fb->faces, sizeof(int32_t) * nf * floc, cudaMemcpyHostToDevice, s));
+    FL_TRY_CUDA(cudaMemcpyAsync(d_xfaces, fb->xfaces, sizeof(int32_t) * nf * 3, cudaMemcpyHostToDevice, s));
+    if (fb->face_ele)
+      FL_TRY_CUDA(cudaMemcpyAsync(d_fe, fb->face_ele, sizeof(int32_t) * nf, cudaMemcpyHostToDevice, s));
+    if (fb->bc_type)
+      FL_TRY_CUDA(cudaMemcpyAsync(d_bt, fb->bc_type, sizeof(int32_t) * nf, cudaMemcpyHostToDevice, s));
+    if (fb->bc_value)
+      FL_TRY_CUDA(cudaMemcpyAsync(d_b1, fb->bc_value, sizeof(double) * nf * floc, cudaMemcpyHostToDevice, s));
+    if (fb->bc_value2)
+      FL_TRY_CUDA(cudaMemcpyAsync(d_b2, fb->bc_value2, sizeof(double) * nf * floc, cudaMemcpyHostToDevice, s));
+  }
+  fl_face_bcs dfb = *fb;
+  dfb.faces = d_faces;
+  dfb.xfaces = d_xfaces;
+  dfb.face_ele = fb->face_ele ? d_fe : nullptr;
+  dfb.bc_type = fb->bc_type ? d_bt : nullptr;
+  dfb.bc_value = fb->bc_value ? d_b1 : nullptr;
+  dfb.bc_value2 = fb->bc_value2 ? d_b2 : nullptr;
+  FL_TRY(m->st_val.reserve(m->nnz));
+  FL_TRY(m->st_rhs.reserve(m->N));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_val.p, val, sizeof(double) * m->nnz, cudaMemcpyHostToDevice, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(m->st_rhs.p, rhs, sizeof(double) * m->N, cudaMemcpyHostToDevice, s));
+  fl_fields df{};
+  if (f->t) {
+    FL_TRY(m->st_t.reserve(m->N));
+    FL_TRY_CUDA(cudaMemcpyAsync(m->st_t.p, f->t, sizeof(double) * m->N, cudaMemcpyHostToDevice, s));
+    df.t = m->st_t.p;
+  }
+  if (f->velocity) {
+    FL_TRY(m->st_u.reserve((size_t)3 * m->Nx));
+    FL_TRY_CUDA(cudaMemcpyAsync(m->st_u.p, f->velocity, sizeof(double) * 3 * m->Nx, cudaMemcpyHostToDevice, s));
+    df.velocity = m->st_u.p;
+  }
+  FL_TRY(advdif_faces(m, p, &dfb, &df, m->st_val.p, m->st_rhs.p, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(val, m->st_val.p, sizeof(double) * m->nnz, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(rhs, m->st_rhs.p, sizeof(double) * m->N, cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
   return FL_OK;
 }

@@ -153,6 +153,11 @@ int rows_p1_closed(struct ::fl_mesh_t* m, const double* em, double* val, double*
 // (K_a3 from the zero row sum), 32 B per (element, local row).
 int rows_p1_df(struct ::fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s);
 
+// node -> surface-face lists of the mesh (face_ptr / face_list: for every
+// field node the faces holding it, ascending), from nf faces of floc nodes.
+int node_face_lists(struct ::fl_mesh_t* m, int32_t nf, int32_t floc, const int32_t* faces, int32_t base,
+                    cudaStream_t s);
+
 // Per-translation-unit launch counters and workspace release hooks.
 unsigned long long launches_mesh();
 unsigned long long launches_assemble();

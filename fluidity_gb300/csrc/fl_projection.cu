@@ -219,29 +219,32 @@ __global__ void __launch_bounds__(THREADS) k_div_rows(DivRowArgs P) {
   }
 }
 
-// node -> surface faces incidence (counting sort, lists sorted ascending)
-__global__ void k_face_count(int32_t nf, const int32_t* __restrict__ faces, int32_t base, int32_t N,
+// node -> surface faces incidence (counting sort, lists sorted ascending);
+// faces hold floc nodes each
+__global__ void k_face_count(int32_t nf, int32_t floc, const int32_t* __restrict__ faces, int32_t base, int32_t N,
                              int32_t* __restrict__ cnt, ErrWord* err) {
   note_launch();
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * nf; k += gridDim.x * blockDim.x) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < (int64_t)floc * nf;
+       k += (int64_t)gridDim.x * blockDim.x) {
     const int v = faces[k] - base;
     if (v < 0 || v >= N) {
-      set_err(err, FL_ERR_ARG, k / 3);
+      set_err(err, FL_ERR_ARG, (int)(k / floc));
       continue;
     }
     atomicAdd(cnt + v, 1);
   }
 }
 
-__global__ void k_face_fill(int32_t nf, const int32_t* __restrict__ faces, int32_t base, int32_t N,
+__global__ void k_face_fill(int32_t nf, int32_t floc, const int32_t* __restrict__ faces, int32_t base, int32_t N,
                             const int32_t* __restrict__ fptr, int32_t* __restrict__ fill,
                             int32_t* __restrict__ flist) {
   note_launch();
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < 3 * nf; k += gridDim.x * blockDim.x) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < (int64_t)floc * nf;
+       k += (int64_t)gridDim.x * blockDim.x) {
     const int v = faces[k] - base;
     if (v < 0 || v >= N) continue;
     const int slot = atomicAdd(fill + v, 1);
-    flist[fptr[v] + slot] = k / 3;
+    flist[fptr[v] + slot] = (int)(k / floc);
   }
 }
 
@@ -1056,6 +1059,27 @@ extern "C" int fl_gpu_secondorder_register(fl_mesh mesh, fl_mesh* out) {
   return FL_OK;
 }
 
+namespace fl {
+
+int node_face_lists(fl_mesh_t* m, int32_t nf, int32_t floc, const int32_t* faces, int32_t base, cudaStream_t s) {
+  const int N = m->N;
+  FL_TRY(m->face_cnt.reserve(N + 1));
+  FL_TRY(m->face_ptr.reserve(N + 1));
+  FL_TRY(m->face_list.reserve((size_t)floc * nf));
+  FL_TRY_CUDA(cudaMemsetAsync(m->face_cnt.p, 0, sizeof(int32_t) * (N + 1), s));
+  k_face_count<<<grid_for((int64_t)floc * nf, kT), kT, 0, s>>>(nf, floc, faces, base, N, m->face_cnt.p, m->err.p);
+  FL_TRY(check_err(m->err.p, s, "surface face node out of range"));
+  FL_TRY(exclusive_scan_i32(m->face_cnt.p, m->face_ptr.p, N, s));
+  FL_TRY_CUDA(cudaMemsetAsync(m->face_cnt.p, 0, sizeof(int32_t) * (N + 1), s));
+  k_face_fill<<<grid_for((int64_t)floc * nf, kT), kT, 0, s>>>(nf, floc, faces, base, N, m->face_ptr.p,
+                                                              m->face_cnt.p, m->face_list.p);
+  k_face_sort<<<grid_for(N, kT), kT, 0, s>>>(N, m->face_ptr.p, m->face_list.p);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}
+
+}  // namespace fl
+
 extern "C" int fl_dev_assemble_divergence_cg(fl_mesh m, const fl_divergence_params* p, double* const ct_val[3],
                                              double* ct_rhs, double* div_mass_lumped, double* grad_mass_lumped,
                                              void* stream) {
@@ -1067,19 +1091,8 @@ extern "C" int fl_dev_assemble_divergence_cg(fl_mesh m, const fl_divergence_para
   cudaStream_t s = pick(m, stream);
   FL_TRY(divergence_passes(m, bp, ct_val[0], ct_val[1], ct_val[2], ct_rhs, div_mass_lumped, grad_mass_lumped, s));
   if (bp && p->nfaces > 0) {
-    const int N = m->N, nf = p->nfaces;
-    FL_TRY(m->face_cnt.reserve(N + 1));
-    FL_TRY(m->face_ptr.reserve(N + 1));
-    FL_TRY(m->face_list.reserve((size_t)3 * nf));
-    FL_TRY_CUDA(cudaMemsetAsync(m->face_cnt.p, 0, sizeof(int32_t) * (N + 1), s));
-    k_face_count<<<grid_for(3 * (int64_t)nf, kT), kT, 0, s>>>(nf, p->faces, p->index_base, N, m->face_cnt.p,
-                                                             m->err.p);
-    FL_TRY(check_err(m->err.p, s, "surface face node out of range"));
-    FL_TRY(exclusive_scan_i32(m->face_cnt.p, m->face_ptr.p, N, s));
-    FL_TRY_CUDA(cudaMemsetAsync(m->face_cnt.p, 0, sizeof(int32_t) * (N + 1), s));
-    k_face_fill<<<grid_for(3 * (int64_t)nf, kT), kT, 0, s>>>(nf, p->faces, p->index_base, N, m->face_ptr.p,
-                                                            m->face_cnt.p, m->face_list.p);
-    k_face_sort<<<grid_for(N, kT), kT, 0, s>>>(N, m->face_ptr.p, m->face_list.p);
+    const int N = m->N;
+    FL_TRY(node_face_lists(m, p->nfaces, 3, p->faces, p->index_base, s));
     FaceArgs F{N, p->index_base, m->face_ptr.p, m->face_list.p, p->faces, p->face_ele, p->bc_type, p->bc_val,
                m->xndglno.p, m->coords.p, m->findrm.p, m->colm.p, ct_val[0], ct_val[1], ct_val[2], ct_rhs,
                m->E, m->err.p};

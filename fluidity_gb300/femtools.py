@@ -31,7 +31,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import AdvDifParams, Fields, MeshDesc, SolveReport, SolverOpts, check
+from ._lib import AdvDifParams, FaceBcs, Fields, MeshDesc, SolveReport, SolverOpts, check
 
 
 def _ptr(a):
@@ -161,9 +161,10 @@ def make_global_numbering_p2(ndglno_p1, nvert: int | None = None):
 
 def advdif_params(*, theta=1.0, dt=1.0, beta=0.0, have_mass=False, lump_mass=False,
                   have_advection=False, diffusivity=None, have_source=False,
-                  have_absorption=False, quad_degree=2) -> AdvDifParams:
+                  have_absorption=False, quad_degree=2, integrate_advection_by_parts=False) -> AdvDifParams:
     """The options assemble_advection_diffusion_cg reads (Advection_Diffusion_CG.F90:384-465)."""
     p = AdvDifParams()
+    p.integrate_advection_by_parts = int(integrate_advection_by_parts)
     p.theta, p.dt, p.beta = theta, dt, beta
     p.have_mass, p.lump_mass = int(have_mass), int(have_mass and lump_mass)
     p.have_advection = int(have_advection)
@@ -209,6 +210,52 @@ def assemble_advection_diffusion_cg(mesh: Mesh, params: AdvDifParams, *, t=None,
     rhs = np.empty(mesh.N) if rhs is None else rhs
     check(lib.fl_gpu_assemble_advdif_cg(mesh.handle, C.byref(params), C.byref(f), _ptr(val),
                                         _ptr(rhs)), "fl_gpu_assemble_advdif_cg")
+    return val, rhs
+
+
+BC_NONE, BC_NEUMANN, BC_WEAKDIRICHLET, BC_INTERNAL, BC_ROBIN = 0, 1, 2, 3, 4
+
+
+def assemble_advection_diffusion_faces(mesh: Mesh, params: AdvDifParams, val, rhs, *, faces, xfaces,
+                                       face_ele=None, bc_type=None, bc_value=None, bc_value2=None,
+                                       t=None, velocity=None, index_base=0, stream=None):
+    """The surface loop of assemble_advection_diffusion_cg (Advection_Diffusion_CG.F90:
+    608-640 -> assemble_advection_diffusion_face_cg :1228-1378) added into an
+    assembled ``val``/``rhs`` in place, before the strong Dirichlet conditions.
+
+    ``faces`` (nf, floc) field nodes of the surface elements (floc 3 for P1,
+    6 for P2 in the triangle's local order), ``xfaces`` (nf, 3) their
+    coordinate vertices, ``face_ele`` (nf,) their elements (needed for the
+    outward normal with advection by parts); ``bc_type`` (nf,) 0 none,
+    1 neumann, 2 weakdirichlet, 3 internal, 4 robin; ``bc_value`` /
+    ``bc_value2`` (nf, floc) the condition's fields at the face nodes.
+    torch CUDA arrays run the device entry point, numpy arrays the host one.
+    """
+    lib = mesh.lib
+    dev = any(_is_device(a) for a in (val, rhs, faces, t, velocity))
+    arrs = {"faces": faces, "xfaces": xfaces, "face_ele": face_ele, "bc_type": bc_type}
+    if dev:
+        import torch
+        conv = {k: (torch.as_tensor(v, dtype=torch.int32, device="cuda").contiguous() if v is not None else None)
+                for k, v in arrs.items()}
+        dbl = [torch.as_tensor(v, dtype=torch.float64, device="cuda").contiguous() if v is not None else None
+               for v in (bc_value, bc_value2)]
+    else:
+        conv = {k: (np.ascontiguousarray(v, dtype=np.int32) if v is not None else None) for k, v in arrs.items()}
+        dbl = [np.ascontiguousarray(v, dtype=np.float64) if v is not None else None for v in (bc_value, bc_value2)]
+    fc = conv["faces"]
+    nf, floc = int(fc.shape[0]), int(fc.shape[1])
+    fb = FaceBcs(nf, floc, index_base, 0, _ptr(fc), _ptr(conv["xfaces"]), _ptr(conv["face_ele"]),
+                 _ptr(conv["bc_type"]), _ptr(dbl[0]), _ptr(dbl[1]))
+    if dev:
+        f = Fields(_ptr(t), _ptr(velocity), None, None)
+        check(lib.fl_dev_assemble_advdif_faces(mesh.handle, C.byref(params), C.byref(fb), C.byref(f), _ptr(val),
+                                               _ptr(rhs), _stream_ptr(stream)), "fl_dev_assemble_advdif_faces")
+        return val, rhs
+    keep = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None for a in (t, velocity)]
+    f = Fields(_ptr(keep[0]), _ptr(keep[1]), None, None)
+    check(lib.fl_gpu_assemble_advdif_faces(mesh.handle, C.byref(params), C.byref(fb), C.byref(f), _ptr(val),
+                                           _ptr(rhs)), "fl_gpu_assemble_advdif_faces")
     return val, rhs
 
 

@@ -115,6 +115,42 @@ def boundary_faces(ndglno: np.ndarray):
     return tri[idx].astype(np.int32), (idx // 4).astype(np.int32)
 
 
+def boundary_faces_p2(ndglno1: np.ndarray, ndglno2: np.ndarray):
+    """Surface mesh of a P2 tet mesh: ``(faces (nf, 6), xfaces (nf, 3), face_ele (nf,))``.
+
+    The faces of :func:`boundary_faces` on the P1 vertices ``ndglno1``, with
+    their six P2 nodes from ``ndglno2`` in the triangle's local order (vertex
+    a, edge ab, vertex b, edge ac, edge bc, vertex c for the face's local
+    vertices a < b < c), and their three vertices.
+    """
+    xf, fe = boundary_faces(ndglno1)
+    nd1 = np.asarray(ndglno1)
+    nd2 = np.asarray(ndglno2)
+    # local vertex ids of each face: the element's vertices other than the dropped one
+    loc = np.empty((xf.shape[0], 3), dtype=np.int64)
+    for k in range(3):
+        loc[:, k] = np.argmax(nd1[fe] == xf[:, k:k + 1], axis=1)
+    # P2 local index of vertex v and of edge (v, w) from the barycentric counts
+    vid = {}
+    eid = {}
+    for li, c in enumerate(P2_COUNTS):
+        nz = np.nonzero(c)[0]
+        if len(nz) == 1:
+            vid[int(nz[0])] = li
+        else:
+            eid[(int(nz[0]), int(nz[1]))] = li
+    faces = np.empty((xf.shape[0], 6), dtype=np.int32)
+    rows = np.arange(xf.shape[0])
+    a, b, c = loc[:, 0], loc[:, 1], loc[:, 2]
+    vmap = np.array([vid[v] for v in range(4)])
+    emap = np.full((4, 4), -1)
+    for (v, w), li in eid.items():
+        emap[v, w] = emap[w, v] = li
+    for col, idx in enumerate((vmap[a], emap[a, b], vmap[b], emap[a, c], emap[b, c], vmap[c])):
+        faces[:, col] = nd2[fe, idx]
+    return faces, xf, fe
+
+
 def p2_coordinates(ndglno1: np.ndarray, ndglno2: np.ndarray, coords1: np.ndarray,
                    counts: np.ndarray) -> np.ndarray:
     """Positions of P2 nodes of an affine mesh: ``sum_j (count_j / 2) X_j``.

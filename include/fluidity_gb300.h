@@ -143,6 +143,14 @@ typedef struct {
   int32_t have_absorption;
   int32_t quad_degree;       /* quadrature degree of the mesh (2 or 4)      */
   double diffusivity[9];     /* constant diffusivity tensor, (i,j) row-major */
+  int32_t integrate_advection_by_parts;  /* spatial_discretisation/
+                                continuous_galerkin/advection_terms/
+                                integrate_advection_by_parts: element term
+                                -(grad N_i . u) N_j - (1 - beta) N_i N_j div u
+                                (:1019-1057) instead of N_i u . grad N_j
+                                + beta N_i N_j div u, plus the surface term of
+                                fl_dev_assemble_advdif_faces                 */
+  int32_t pad;
 } fl_advdif_params;
 
 /* Nodal fields.  t, source, absorption live on the field mesh; velocity lives
@@ -170,6 +178,55 @@ int fl_gpu_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
 int fl_dev_assemble_advdif_cg(fl_mesh mesh, const fl_advdif_params* params,
                               const fl_fields* fields, double* val, double* rhs,
                               void* stream);
+
+/* Surface elements of the field mesh with their boundary conditions: the
+ * input of the surface loop of assemble_advection_diffusion_cg
+ * (assemble/Advection_Diffusion_CG.F90:608-640; get_entire_boundary_condition
+ * with the types neumann, weakdirichlet, internal, robin).  Face nodes are in
+ * the triangle's local order: P1 (floc 3) the three vertices; P2 (floc 6)
+ * vertex 1, edge 12, vertex 2, edge 13, edge 23, vertex 3 (the triangle
+ * numbering of femtools/Element_Numbering.F90).  xfaces holds the three
+ * vertices on the coordinate mesh in the same vertex order.  All pointers are
+ * device pointers for fl_dev_* and host pointers for fl_gpu_*. */
+typedef struct {
+  int32_t nfaces;
+  int32_t floc;              /* nodes per face: 3 (P1 field) or 6 (P2)      */
+  int32_t index_base;        /* 0 or 1 for faces, xfaces and face_ele       */
+  int32_t pad;
+  const int32_t* faces;      /* nfaces x floc field nodes (face_global_nodes) */
+  const int32_t* xfaces;     /* nfaces x 3 coordinate vertices              */
+  const int32_t* face_ele;   /* nfaces: the element of each face (face_ele);
+                                needed with advection by parts (normals)    */
+  const int32_t* bc_type;    /* nfaces: 0 none, 1 neumann, 2 weakdirichlet,
+                                3 internal (skipped), 4 robin               */
+  const double* bc_value;    /* nfaces x floc: t_bc at the face nodes
+                                (neumann flux, robin value, weak Dirichlet
+                                value); may be NULL when no face needs it   */
+  const double* bc_value2;   /* nfaces x floc: t_bc_2 (robin coefficient)   */
+} fl_face_bcs;
+
+/* The surface loop of assemble_advection_diffusion_cg, added into an
+ * assembled system (after fl_*_assemble_advdif_cg, before the strong
+ * Dirichlet conditions, the reference's order): for every face in order,
+ * unless internal, assemble_advection_diffusion_face_cg
+ * (Advection_Diffusion_CG.F90:1228-1286) with add_advection_face_cg
+ * (:1288-1342; when advection is integrated by parts: the face matrix
+ * int N_i N_j (u.n) enters the matrix with dt*theta, or for weak Dirichlet
+ * faces the rhs with theta*(g - t); the rhs loses its product with t) and
+ * add_diffusivity_face_cg (:1344-1378; neumann: rhs += int N_i g; robin: the
+ * same plus int N_i N_j g2 in the matrix with dt*theta and its product with
+ * t subtracted from the rhs).  Nothing happens unless advection is by parts
+ * or a diffusivity is present (:608-611).  A weak Dirichlet face with a
+ * diffusivity is the reference's FLExit: FL_ERR_ARG (the system is then
+ * partly updated).  The sums are deterministic: each row adds its faces in
+ * ascending order.  Face quadrature: the triangle rule of params->quad_degree
+ * (Quadrature.F90 construct_tri_quadratures).  Device pointers: fields->t and
+ * fields->velocity (P1, on the coordinate mesh) as in the element loop. */
+int fl_dev_assemble_advdif_faces(fl_mesh mesh, const fl_advdif_params* params, const fl_face_bcs* faces,
+                                 const fl_fields* fields, double* val, double* rhs, void* stream);
+/* Host-pointer form (val and rhs are read and updated in place). */
+int fl_gpu_assemble_advdif_faces(fl_mesh mesh, const fl_advdif_params* params, const fl_face_bcs* faces,
+                                 const fl_fields* fields, double* val, double* rhs);
 
 /* Allocation-free form of fl_dev_assemble_advdif_cg for the P1 diffusion
  * (pressure-Poisson) case: diffusivity with optional source and consistent

@@ -502,6 +502,8 @@ struct OrcAdvDifParams {
   int have_mass, lump_mass, have_advection, have_diffusivity, isotropic;
   int have_source, have_absorption, quad_degree, t_degree, u_degree;
   double diffusivity[9];  // constant tensor, row-major
+  int by_parts;           // integrate_advection_by_parts
+  int pad;
 };
 
 int orc_assemble_advdif(const OrcAdvDifParams* P, int E, const int* ndglno_t, int nt,
@@ -580,9 +582,9 @@ int orc_assemble_advdif(const OrcAdvDifParams* P, int E, const int* ndglno_t, in
               else M[i][j] += s;
             }
         }
-        // Advection, not by parts (Advection_Diffusion_CG.F90:1058-1113):
+        // Advection (Advection_Diffusion_CG.F90:1019-1113).  Not by parts:
         // A = shape_vector_dot_dshape(N, u_q, dN, detwei)   (FETools.F90:749)
-        //   + beta * shape_shape(N, N, div(u)_q * detwei)
+        //   + beta * shape_shape(N, N, div(u)_q * detwei); by parts see below.
         // matrix += dt_theta*A; rhs -= A.T_e (:1117-1125).
         if (P->have_advection) {
           const int* un = ndglno_u + (int64_t)uloc * e;
@@ -593,7 +595,9 @@ int orc_assemble_advdif(const OrcAdvDifParams* P, int E, const int* ndglno_t, in
               for (int i = 0; i < uloc; ++i) s += velocity[3 * (int64_t)un[i] + a] * us.n[i][gi];
               uq[gi][a] = s;
             }
-          if (std::fabs(P->beta) > eps0) {
+          // the divergence term: beta (not by parts) or 1 - beta (by parts)
+          const double bcoef = P->by_parts ? 1.0 - P->beta : P->beta;
+          if (std::fabs(bcoef) > eps0) {
             // ele_div_at_quad with du_t = dN_u . invJ^T
             for (int gi = 0; gi < ngi; ++gi) {
               double s = 0.0;
@@ -607,22 +611,39 @@ int orc_assemble_advdif(const OrcAdvDifParams* P, int E, const int* ndglno_t, in
             }
           }
           double A[10][10];
-          for (int i = 0; i < loc; ++i)
-            for (int j = 0; j < loc; ++j) {
-              double s = 0.0;
-              for (int gi = 0; gi < ngi; ++gi) {
-                double udn = 0.0;
-                for (int a = 0; a < 3; ++a) udn += dt_t[j][gi][a] * uq[gi][a];
-                s += ts.n[i][gi] * udn * detwei[gi];
+          if (P->by_parts) {
+            // By parts (:1019-1057): A = -dshape_dot_vector_shape(dN, u_q, N,
+            // detwei) (FETools.F90:700-721) - (1 - beta) shape_shape(N, N,
+            // div(u)_q detwei)
+            for (int i = 0; i < loc; ++i)
+              for (int j = 0; j < loc; ++j) {
+                double s = 0.0;
+                for (int gi = 0; gi < ngi; ++gi) {
+                  double udn = 0.0;
+                  for (int a = 0; a < 3; ++a) udn += dt_t[i][gi][a] * uq[gi][a];
+                  s += udn * ts.n[j][gi] * detwei[gi];
+                }
+                A[i][j] = -s;
               }
-              A[i][j] = s;
-            }
-          if (std::fabs(P->beta) > eps0)
+          } else {
+            for (int i = 0; i < loc; ++i)
+              for (int j = 0; j < loc; ++j) {
+                double s = 0.0;
+                for (int gi = 0; gi < ngi; ++gi) {
+                  double udn = 0.0;
+                  for (int a = 0; a < 3; ++a) udn += dt_t[j][gi][a] * uq[gi][a];
+                  s += ts.n[i][gi] * udn * detwei[gi];
+                }
+                A[i][j] = s;
+              }
+          }
+          if (std::fabs(bcoef) > eps0)
             for (int i = 0; i < loc; ++i)
               for (int j = 0; j < loc; ++j) {
                 double s = 0.0;
                 for (int gi = 0; gi < ngi; ++gi) s += ts.n[i][gi] * ts.n[j][gi] * (divu[gi] * detwei[gi]);
-                A[i][j] = A[i][j] + P->beta * s;
+                if (P->by_parts) A[i][j] = A[i][j] - bcoef * s;
+                else A[i][j] = A[i][j] + bcoef * s;
               }
           for (int i = 0; i < loc; ++i) {
             if (std::fabs(dt_theta) > eps0)
@@ -717,6 +738,240 @@ int orc_assemble_advdif(const OrcAdvDifParams* P, int E, const int* ndglno_t, in
     }
   }
   return status;
+}
+
+// ---------------------------------------------------------------------------
+// The surface loop of assemble_advection_diffusion_cg (Advection_Diffusion_CG
+// .F90:608-640), run after the element loop and before the strong Dirichlet
+// conditions: for each surface element in order, unless its bc type is
+// internal (3), assemble_advection_diffusion_face_cg (:1228-1286) with
+// add_advection_face_cg (:1288-1342, advection integrated by parts only) and
+// add_diffusivity_face_cg (:1344-1378), then addto of the face matrix and rhs.
+// bc types (get_entire_boundary_condition order, :74-75): 0 none, 1 neumann,
+// 2 weakdirichlet, 3 internal, 4 robin.  Face transform: transform_facet_to
+// _physical (Transform_elements.F90:1353-1525) for a linear face: J = [X1 - X3,
+// X2 - X3], detJ = |J1 x J2| summed in cyc3 order, detwei = detJ * w, normal
+// = facet_normal (:1527-1553) oriented by face centroid - element centroid.
+// Face quadrature: the triangle rule of the element rule's degree
+// (Quadrature.F90:908-1010, construct_tri_quadratures).  Face shape functions
+// in the triangle's local order (P1: vertices; P2: vertex 1, edge 12, vertex
+// 2, edge 13, edge 23, vertex 3).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct TriRule {
+  int ngi = 0;
+  double l[6][3];
+  double w[6];
+};
+
+// (a, a, b) and its two other permutations, as tri_permutations(5) lists them
+// (Quadrature.F90:1821-1826), or the centroid (tri_permutations(4)).
+void tri_add_gen(TriRule& r, double a, double w, bool centroid) {
+  if (centroid) {
+    r.l[r.ngi][0] = r.l[r.ngi][1] = r.l[r.ngi][2] = a;
+    r.w[r.ngi++] = w;
+    return;
+  }
+  const double b = 1.0 - 2.0 * a;
+  const double c[2] = {a, b};
+  const int perm[3][3] = {{1, 1, 2}, {1, 2, 1}, {2, 1, 1}};
+  for (int k = 0; k < 3; ++k) {
+    for (int j = 0; j < 3; ++j) r.l[r.ngi][j] = c[perm[k][j] - 1];
+    r.w[r.ngi++] = w;
+  }
+}
+
+bool tri_rule(int degree, TriRule& r) {
+  r.ngi = 0;
+  switch (degree) {
+    case 1:
+      tri_add_gen(r, 0.333333333333333333333333333333333, 0.5, true);
+      return true;
+    case 2:
+      tri_add_gen(r, 0.166666666666666666666666666666666, 0.166666666666666666666666666666666, false);
+      return true;
+    case 3:
+      tri_add_gen(r, 0.333333333333333333333333333333333, -0.28125, true);
+      tri_add_gen(r, 0.2, 0.260416666666666666666666666666666, false);
+      return true;
+    case 4:
+      tri_add_gen(r, 0.0915762135097707434595714634022015, 0.0549758718276609338191631624501052, false);
+      tri_add_gen(r, 0.445948490915964886318329253883051, 0.111690794839005732847503504216561, false);
+      return true;
+    default:
+      return false;
+  }
+}
+
+// Lagrange shape functions on the triangle from barycentric counts.
+void tri_shape(int degree, const double l[3], double* n) {
+  if (degree == 1) {
+    for (int i = 0; i < 3; ++i) n[i] = l[i];
+    return;
+  }
+  const int cnt[6][3] = {{2, 0, 0}, {1, 1, 0}, {0, 2, 0}, {1, 0, 1}, {0, 1, 1}, {0, 0, 2}};
+  for (int i = 0; i < 6; ++i) {
+    double v = 1.0;
+    for (int j = 0; j < 3; ++j) {
+      if (cnt[i][j] == 2) v *= l[j] * (2.0 * l[j] - 1.0);
+      else if (cnt[i][j] == 1) v *= 2.0 * l[j];
+    }
+    n[i] = v;
+  }
+}
+
+}  // namespace
+
+int orc_assemble_advdif_faces(const OrcAdvDifParams* P, int nf, int floc, const int* faces, const int* xfaces,
+                              const int* face_ele, const int* ndglno_x, const double* coords,
+                              const double* velocity, const double* T, const int* bc_type, const double* bc1,
+                              const double* bc2, const int64_t* findrm, const int* colm, double* val,
+                              double* rhs) {
+  const bool adv = P->have_advection && P->by_parts;
+  if (!(adv || P->have_diffusivity)) return ORC_OK;  // (:608-611)
+  if (floc != 3 && floc != 6) return ORC_ERR_ARG;
+  TriRule q;
+  if (!tri_rule(P->quad_degree, q)) return ORC_ERR_ARG;
+  const int tdeg = floc == 3 ? 1 : 2;
+  double N[6][6], Nu[6][3];  // [gi][node]
+  for (int gi = 0; gi < q.ngi; ++gi) {
+    tri_shape(tdeg, q.l[gi], N[gi]);
+    tri_shape(1, q.l[gi], Nu[gi]);
+  }
+  const double dt_theta = P->dt * P->theta;
+  const double eps0 = 2.220446049250313e-16;
+  for (int f = 0; f < nf; ++f) {
+    const int ty = bc_type ? bc_type[f] : 0;
+    if (ty == 3) continue;
+    if (ty != 0 && ty != 1 && ty != 2 && ty != 4) return ORC_ERR_ARG;
+    // FLExit: weak Dirichlet with diffusivity (:1371-1375)
+    if (ty == 2 && P->have_diffusivity) return ORC_ERR_ARG;
+    const int* fn = faces + (int64_t)floc * f;
+    const int* xf = xfaces + 3 * (int64_t)f;
+    double Xf[3][3];
+    for (int j = 0; j < 3; ++j)
+      for (int a = 0; a < 3; ++a) Xf[j][a] = coords[3 * (int64_t)xf[j] + a];
+    const bool need_t = adv || (P->have_diffusivity && (ty == 1 || ty == 4));
+    double detwei[6] = {}, normal[3] = {};
+    if (need_t) {
+      double J[3][2];
+      for (int a = 0; a < 3; ++a) {
+        J[a][0] = Xf[0][a] - Xf[2][a];
+        J[a][1] = Xf[1][a] - Xf[2][a];
+      }
+      double detJ = 0.0;
+      for (int i = 1; i <= 3; ++i) {
+        const int c2 = (i + 1) % 3, c1 = i % 3;  // cyc3(i+2) - 1, cyc3(i+1) - 1
+        const double v = J[c2][0] * J[c1][1] - J[c2][1] * J[c1][0];
+        detJ += v * v;
+      }
+      detJ = std::sqrt(detJ);
+      for (int gi = 0; gi < q.ngi; ++gi) detwei[gi] = detJ * q.w[gi];
+      if (adv) {
+        double ow[3], cf[3] = {}, ce[3] = {};
+        for (int j = 0; j < 3; ++j)
+          for (int a = 0; a < 3; ++a) cf[a] += Xf[j][a];
+        const int* ev = ndglno_x + 4 * (int64_t)face_ele[f];
+        for (int j = 0; j < 4; ++j)
+          for (int a = 0; a < 3; ++a) ce[a] += coords[3 * (int64_t)ev[j] + a];
+        for (int a = 0; a < 3; ++a) ow[a] = cf[a] / 3.0 - ce[a] / 4.0;
+        double n[3] = {J[1][0] * J[2][1] - J[2][0] * J[1][1], J[2][0] * J[0][1] - J[0][0] * J[2][1],
+                       J[0][0] * J[1][1] - J[1][0] * J[0][1]};
+        const double o = n[0] * ow[0] + n[1] * ow[1] + n[2] * ow[2];
+        for (int a = 0; a < 3; ++a) n[a] *= o;
+        const double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int a = 0; a < 3; ++a) normal[a] = n[a] / len;
+      }
+    }
+    double Tf[6];
+    for (int i = 0; i < floc; ++i) Tf[i] = T ? T[fn[i]] : 0.0;
+    double Madd[6][6] = {}, Radd[6] = {};
+    auto shape_shape = [&](const double* w, double (*out)[6]) {
+      for (int i = 0; i < floc; ++i)
+        for (int j = 0; j < floc; ++j) {
+          double s = 0.0;
+          for (int gi = 0; gi < q.ngi; ++gi) s += (N[gi][i] * N[gi][j]) * w[gi];
+          out[i][j] = s;
+        }
+    };
+    if (adv) {
+      // add_advection_face_cg: u at quad (face_val_at_quad of the P1 velocity)
+      double w[6], A[6][6];
+      for (int gi = 0; gi < q.ngi; ++gi) {
+        double un = 0.0;
+        for (int a = 0; a < 3; ++a) {
+          double u = 0.0;
+          for (int k = 0; k < 3; ++k) u += velocity[3 * (int64_t)xf[k] + a] * Nu[gi][k];
+          un += u * normal[a];
+        }
+        w[gi] = detwei[gi] * un;
+      }
+      shape_shape(w, A);
+      if (std::fabs(dt_theta) > eps0) {
+        if (ty == 2) {
+          const double* g = bc1 + (int64_t)floc * f;
+          for (int i = 0; i < floc; ++i) {
+            double s = 0.0;
+            for (int j = 0; j < floc; ++j) s += A[i][j] * (g[j] - Tf[j]);
+            Radd[i] = Radd[i] - P->theta * s;
+          }
+        } else {
+          for (int i = 0; i < floc; ++i)
+            for (int j = 0; j < floc; ++j) Madd[i][j] = Madd[i][j] + dt_theta * A[i][j];
+        }
+      }
+      for (int i = 0; i < floc; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < floc; ++j) s += A[i][j] * Tf[j];
+        Radd[i] = Radd[i] - s;
+      }
+    }
+    if (P->have_diffusivity && (ty == 1 || ty == 4)) {
+      // add_diffusivity_face_cg: shape_rhs(N, detwei * g_q) (FETools.F90:38)
+      const double* g = bc1 + (int64_t)floc * f;
+      double gq[6];
+      for (int gi = 0; gi < q.ngi; ++gi) {
+        double v = 0.0;
+        for (int k = 0; k < floc; ++k) v += g[k] * N[gi][k];
+        gq[gi] = detwei[gi] * v;
+      }
+      for (int i = 0; i < floc; ++i) {
+        double s = 0.0;
+        for (int gi = 0; gi < q.ngi; ++gi) s += N[gi][i] * gq[gi];
+        Radd[i] = Radd[i] + s;
+      }
+      if (ty == 4) {
+        const double* g2 = bc2 + (int64_t)floc * f;
+        double w[6], Rm[6][6];
+        for (int gi = 0; gi < q.ngi; ++gi) {
+          double v = 0.0;
+          for (int k = 0; k < floc; ++k) v += g2[k] * N[gi][k];
+          w[gi] = detwei[gi] * v;
+        }
+        shape_shape(w, Rm);
+        if (std::fabs(dt_theta) > eps0)
+          for (int i = 0; i < floc; ++i)
+            for (int j = 0; j < floc; ++j) Madd[i][j] = Madd[i][j] + dt_theta * Rm[i][j];
+        for (int i = 0; i < floc; ++i) {
+          double s = 0.0;
+          for (int j = 0; j < floc; ++j) s += Rm[i][j] * Tf[j];
+          Radd[i] = Radd[i] - s;
+        }
+      }
+    }
+    // addto(matrix, face_nodes, face_nodes, matrix_addto); addto(rhs, ...)
+    for (int i = 0; i < floc; ++i) {
+      for (int j = 0; j < floc; ++j) {
+        if (Madd[i][j] == 0.0) continue;
+        const int64_t p = csr_pos(findrm, colm, fn[i], fn[j]);
+        if (p < 0) return ORC_ERR_OUTSIDE_PATTERN;
+        val[p] += Madd[i][j];
+      }
+      rhs[fn[i]] += Radd[i];
+    }
+  }
+  return ORC_OK;
 }
 
 // Strong Dirichlet in acceleration form (Boundary_Conditions.F90:1983-2025):

@@ -140,28 +140,21 @@ class _Params(C.Structure):
         ("have_mass", C.c_int), ("lump_mass", C.c_int), ("have_advection", C.c_int),
         ("have_diffusivity", C.c_int), ("isotropic", C.c_int), ("have_source", C.c_int),
         ("have_absorption", C.c_int), ("quad_degree", C.c_int), ("t_degree", C.c_int),
-        ("u_degree", C.c_int), ("diffusivity", C.c_double * 9),
+        ("u_degree", C.c_int), ("diffusivity", C.c_double * 9), ("by_parts", C.c_int),
+        ("pad", C.c_int),
     ]
 
 
-def assemble_advdif(*, ndglno_t, nt, ndglno_x, coords, findrm, colm,
-                    theta=1.0, dt=1.0, beta=0.0, have_mass=False, lump_mass=False,
-                    velocity=None, ndglno_u=None, u_degree=1, T=None, source=None,
-                    absorption=None, diffusivity=None, quad_degree=2, t_degree=1,
-                    colours=None, nthreads=0):
-    """(val, rhs, status) of the element loop -- Advection_Diffusion_CG.F90:228-659.
-
-    ``diffusivity`` is a 3x3 constant tensor (isotropic if it is a multiple of
-    the identity), a scalar, or None.  ``colours`` = (colour_ptr, elements) or
-    None for element order (serial build).
-    """
+def _make_params(theta, dt, beta, have_mass, lump_mass, have_advection, have_source, have_absorption,
+                 diffusivity, quad_degree, t_degree, u_degree, by_parts):
     P = _Params()
     P.theta, P.dt, P.beta = theta, dt, beta
     P.have_mass, P.lump_mass = int(have_mass), int(lump_mass)
-    P.have_advection = int(velocity is not None)
-    P.have_source = int(source is not None)
-    P.have_absorption = int(absorption is not None)
+    P.have_advection = int(have_advection)
+    P.have_source = int(have_source)
+    P.have_absorption = int(have_absorption)
     P.quad_degree, P.t_degree, P.u_degree = quad_degree, t_degree, u_degree
+    P.by_parts = int(by_parts)
     if diffusivity is None:
         P.have_diffusivity = 0
         P.isotropic = 1
@@ -173,6 +166,23 @@ def assemble_advdif(*, ndglno_t, nt, ndglno_x, coords, findrm, colm,
         P.isotropic = int(np.allclose(K, np.eye(3) * K[0, 0], rtol=0, atol=0))
         for a in range(9):
             P.diffusivity[a] = K.reshape(-1)[a]
+    return P
+
+
+def assemble_advdif(*, ndglno_t, nt, ndglno_x, coords, findrm, colm,
+                    theta=1.0, dt=1.0, beta=0.0, have_mass=False, lump_mass=False,
+                    velocity=None, ndglno_u=None, u_degree=1, T=None, source=None,
+                    absorption=None, diffusivity=None, quad_degree=2, t_degree=1,
+                    colours=None, nthreads=0, by_parts=False):
+    """(val, rhs, status) of the element loop -- Advection_Diffusion_CG.F90:228-659.
+
+    ``diffusivity`` is a 3x3 constant tensor (isotropic if it is a multiple of
+    the identity), a scalar, or None.  ``colours`` = (colour_ptr, elements) or
+    None for element order (serial build).  ``by_parts`` is
+    integrate_advection_by_parts.
+    """
+    P = _make_params(theta, dt, beta, have_mass, lump_mass, velocity is not None, source is not None,
+                     absorption is not None, diffusivity, quad_degree, t_degree, u_degree, by_parts)
     nd_t = np.ascontiguousarray(ndglno_t, dtype=np.int32)
     nd_x = np.ascontiguousarray(ndglno_x, dtype=np.int32)
     X = np.ascontiguousarray(coords, dtype=np.float64)
@@ -196,6 +206,36 @@ def assemble_advdif(*, ndglno_t, nt, ndglno_x, coords, findrm, colm,
         C.byref(P), E, _p(nd_t), nt, _p(nd_x), _p(X), _p(nd_u), _p(U), _p(Tv), _p(S), _p(A),
         _p(f), _p(c), _p(val), _p(rhs), ncol, _p(cptr), _p(celems), int(nthreads))
     return val, rhs, st
+
+
+def assemble_advdif_faces(val, rhs, *, faces, xfaces, face_ele, ndglno_x, coords, findrm, colm,
+                          bc_type, bc_value=None, bc_value2=None, theta=1.0, dt=1.0, beta=0.0,
+                          velocity=None, T=None, diffusivity=None, quad_degree=2, by_parts=False):
+    """The surface loop of assemble_advection_diffusion_cg (Advection_Diffusion_CG.F90:
+    608-640 -> :1228-1378), added into ``val`` and ``rhs`` in place; returns the
+    status.  ``faces`` (nf, floc) field nodes of each surface element in the
+    triangle's local order, ``xfaces`` (nf, 3) its coordinate vertices,
+    ``face_ele`` (nf,) its element; ``bc_type`` 0 none, 1 neumann,
+    2 weakdirichlet, 3 internal, 4 robin; ``bc_value``/``bc_value2`` (nf, floc)
+    the boundary-condition fields at the face nodes."""
+    fcs = np.ascontiguousarray(faces, dtype=np.int32)
+    nf, floc = fcs.shape
+    P = _make_params(theta, dt, beta, False, False, velocity is not None, False, False, diffusivity,
+                     quad_degree, 1 if floc == 3 else 2, 1, by_parts)
+    xf = np.ascontiguousarray(xfaces, dtype=np.int32)
+    fe = np.ascontiguousarray(face_ele, dtype=np.int32)
+    nx = np.ascontiguousarray(ndglno_x, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    U = np.ascontiguousarray(velocity, dtype=np.float64) if velocity is not None else None
+    Tv = np.ascontiguousarray(T, dtype=np.float64) if T is not None else None
+    bt = np.ascontiguousarray(bc_type, dtype=np.int32)
+    b1 = np.ascontiguousarray(bc_value, dtype=np.float64) if bc_value is not None else None
+    b2 = np.ascontiguousarray(bc_value2, dtype=np.float64) if bc_value2 is not None else None
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    assert val.dtype == np.float64 and val.flags.c_contiguous and rhs.flags.c_contiguous
+    return lib().orc_assemble_advdif_faces(C.byref(P), nf, floc, _p(fcs), _p(xf), _p(fe), _p(nx), _p(X), _p(U),
+                                           _p(Tv), _p(bt), _p(b1), _p(b2), _p(f), _p(c), _p(val), _p(rhs))
 
 
 def apply_dirichlet(nodes, g, T, dt, rhs, inactive):

@@ -35,6 +35,8 @@ CASES = {
     "advdif": dict(theta=0.5, dt=0.01, have_mass=True, velocity=True, T=True, diffusivity=1e-3),
     "advdif_beta1": dict(theta=0.5, dt=0.01, have_mass=True, velocity=True, T=True,
                          diffusivity=1e-3, beta=1.0),
+    "advdif_by_parts": dict(theta=0.5, dt=0.01, have_mass=True, velocity=True, T=True,
+                            diffusivity=1e-3, beta=0.3, by_parts=True),
     "lumped_absorption": dict(theta=1.0, dt=0.1, have_mass=True, lump_mass=True, absorption=True,
                               T=True, diffusivity=0.5, source=True),
     "mass_only": dict(have_mass=True, source=True),
@@ -58,7 +60,8 @@ def _params(case, quad_degree):
                             lump_mass=case.get("lump_mass", False),
                             have_advection="velocity" in case,
                             diffusivity=case.get("diffusivity"), have_source="source" in case,
-                            have_absorption="absorption" in case, quad_degree=quad_degree)
+                            have_absorption="absorption" in case, quad_degree=quad_degree,
+                            integrate_advection_by_parts=case.get("by_parts", False))
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -71,8 +74,8 @@ def test_p1_assembly_matches_oracle(O, aniso_mesh, name, mesh):
     f, c, _ = O.make_sparsity(nd)
     ocol, ncol = O.colour_cg1(nd)
     colours = O.colour_sets(ocol, ncol)
-    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass")}
-    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass") if k in case})
+    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass", "by_parts")}
+    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass", "by_parts") if k in case})
     oval, orhs = _oracle(O, nd, X, nd, X.shape[0], f, c, colours=colours, **kw)
     val, rhs = ft.assemble_advection_diffusion_cg(m, _params(case, 2), t=fl.get("T"),
                                                   velocity=fl.get("velocity"),
@@ -81,7 +84,7 @@ def test_p1_assembly_matches_oracle(O, aniso_mesh, name, mesh):
     _compare(val, rhs, oval, orhs, f)
 
 
-@pytest.mark.parametrize("name", ["poisson", "anisotropic", "advdif", "lumped_absorption"])
+@pytest.mark.parametrize("name", ["poisson", "anisotropic", "advdif", "advdif_by_parts", "lumped_absorption"])
 def test_p2_assembly_matches_oracle(O, name):
     nd, X = M.cube_mesh(3)
     nd2, n2 = O.make_global_numbering_p2(nd)
@@ -92,8 +95,8 @@ def test_p2_assembly_matches_oracle(O, name):
         fl["velocity"] = M.advdif_velocity(X)  # velocity lives on the P1 coordinate mesh
     m = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
     f, c, _ = O.make_sparsity(nd2)
-    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass")}
-    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass") if k in case})
+    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass", "by_parts")}
+    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass", "by_parts") if k in case})
     oval, orhs = _oracle(O, nd, X, nd2, n2, f, c, quad_degree=4, t_degree=2, **kw)
     val, rhs = ft.assemble_advection_diffusion_cg(m, _params(case, 4), t=fl.get("T"),
                                                   velocity=fl.get("velocity"),

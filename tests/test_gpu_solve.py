@@ -147,9 +147,8 @@ def test_unpreconditioned_norm_cg_matches_oracle(O, start_from_zero):
     assert abs(rep["iterations"] - oits) <= 1
     assert np.abs(x - ox).max() <= 1e-7 * np.abs(ox).max()
     assert rep["true_rel_residual"] <= 1.05e-10
-    # the preconditioned test stops earlier or later, at another iteration
-    _, pits, _, _ = oracle_solve(O, m, val, rhs, ina, x0=x0, rtol=1e-10, start_from_zero=start_from_zero)
-    assert pits != oits
+    # the tested norm is ||r||: the recurrence residual it reports is the true one
+    assert abs(rep["final_rnorm"] / rep["rnorm0"] - rep["true_rel_residual"]) <= 1e-12
 
 
 @pytest.mark.parametrize("precision", ["mixed", "reliable"])
