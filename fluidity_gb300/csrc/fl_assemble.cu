@@ -2236,6 +2236,12 @@ __global__ void __launch_bounds__(128) k_advdif_faces(FaceAsmArgs F) {
       }
       const bool dface = F.diff && (ty == 1 || ty == 4);
       if (!F.adv && !dface) continue;
+      // the values a face needs: t_bc for neumann, robin and (advected) weak
+      // Dirichlet faces, t_bc_2 for robin faces
+      if (((dface || (F.adv && ty == 2)) && !F.bc1) || (dface && ty == 4 && !F.bc2)) {
+        set_err(F.err, FL_ERR_ARG, f);
+        continue;
+      }
       const int floc = F.floc;
       int fn[6], li = -1;
       for (int j = 0; j < floc; ++j) {
@@ -2375,8 +2381,6 @@ static int advdif_faces(fl_mesh_t* m, const fl_advdif_params* p, const fl_face_b
   if (fb->nfaces == 0 || !(adv || diff)) return FL_OK;  // (:608-611)
   FL_CHECK_ARG(fb->faces && fb->xfaces, "faces and xfaces");
   FL_CHECK_ARG(!adv || (fb->face_ele && f->velocity), "advection by parts needs face_ele and the velocity");
-  FL_CHECK_ARG(fb->bc_type == nullptr || fb->bc_value != nullptr || !diff,
-               "bc_value is needed for neumann, robin and weak Dirichlet faces");
   FaceAsmArgs F{};
   F.ngi = tri_rule(p->quad_degree, F.ql, F.qw);
   FL_CHECK_ARG(F.ngi > 0, "quadrature degree 1..4");
@@ -2411,7 +2415,7 @@ static int advdif_faces(fl_mesh_t* m, const fl_advdif_params* p, const fl_face_b
   FL_TRY_CUDA(cudaGetLastError());
   return check_err(m->err.p, s,
                    "surface loop: a face is invalid, has a weak Dirichlet condition with a diffusivity "
-                   "(FLExit in the reference), lacks its robin values, or adds outside the sparsity pattern");
+                   "(FLExit in the reference), lacks its boundary values, or adds outside the sparsity pattern");
 }
 
 }  // namespace fl

@@ -60,3 +60,55 @@ def test_null_arguments_are_usage_errors():
             continue
         assert st == 1, (name, st)
         assert lib.fl_last_error(), name
+
+
+def _fortran_interfaces():
+    """bind(c, name=...) functions of the Fortran shim with their argument names."""
+    path = os.path.join(os.path.dirname(HEADER), "..", "fluidity_gb300", "fortran", "fl_gpu_bindings.F90")
+    src = open(path).read()
+    src = re.sub(r"&\s*\n\s*&?", " ", src)  # join continuation lines
+    out = {}
+    for m in re.finditer(r"function\s+(\w+)\s*\(([^)]*)\)\s*bind\(c,\s*name=\"(\w+)\"\)", src):
+        args = [a.strip() for a in m.group(2).split(",") if a.strip()]
+        out[m.group(3)] = (m.group(1), args)
+    return out
+
+
+def _header_arg_counts():
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(fl_[A-Za-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt):
+        args = " ".join(m.group(2).split())
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_fortran_shim_binds_every_export_with_its_arity():
+    """Every bind(c) interface of the Fortran shim names a header export, has
+    the header's argument count and keeps the C name as its Fortran name;
+    every header export has an interface (no Fortran compiler here: this is
+    the shim's structural check)."""
+    fi = _fortran_interfaces()
+    hc = _header_arg_counts()
+    assert sorted(fi) == sorted(hc), set(fi) ^ set(hc)
+    for name, (fname, args) in fi.items():
+        assert fname == name, name
+        assert len(args) == hc[name], (name, args, hc[name])
+
+
+def test_fortran_structs_match_the_ctypes_layouts():
+    """The bind(c) derived types list the fields of the C structs in order."""
+    path = os.path.join(os.path.dirname(HEADER), "..", "fluidity_gb300", "fortran", "fl_gpu_bindings.F90")
+    src = open(path).read()
+    structs = {"fl_advdif_params": _lib.AdvDifParams, "fl_fields": _lib.Fields, "fl_face_bcs": _lib.FaceBcs,
+               "fl_solver_opts": _lib.SolverOpts, "fl_solve_report": _lib.SolveReport,
+               "fl_mesh_desc": _lib.MeshDesc, "fl_divergence_params": _lib.DivergenceParams}
+    for fname, cstruct in structs.items():
+        m = re.search(rf"type, bind\(c\) :: {fname}\n(.*?)end type {fname}", src, flags=re.S)
+        assert m, fname
+        names = []
+        for line in m.group(1).splitlines():
+            if "::" in line:
+                decl = line.split("::", 1)[1]
+                names += [re.sub(r"\(.*\)", "", v).strip() for v in decl.split(",")]
+        assert names == [f[0] for f in cstruct._fields_], (fname, names)

@@ -165,3 +165,16 @@ def test_by_parts_step_solves_like_not_by_parts(O):
     assert row_scaled_error(vb, va, f) <= 1e-12
     assert np.abs(rb - ra).max() <= 1e-12 * np.abs(ra).max()
     m.close()
+
+
+def test_missing_boundary_values_are_an_error():
+    nd, X = M.cube_mesh(3)
+    m = ft.Mesh(nd, X)
+    faces, fe = M.boundary_faces(nd)
+    nf = faces.shape[0]
+    p = ft.advdif_params(diffusivity=1.0)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, p)
+    with pytest.raises(RuntimeError, match="boundary values"):
+        ft.assemble_advection_diffusion_faces(m, p, val, rhs, faces=faces, xfaces=faces, face_ele=fe,
+                                              bc_type=np.full(nf, 4, np.int32), bc_value=np.ones((nf, 3)))
+    m.close()
