@@ -105,7 +105,7 @@ EXPORTS = [
     "fl_gpu_secondorder_register", "fl_dev_assemble_divergence_cg", "fl_dev_lumped_mass",
     "fl_dev_mult_div_vector_div_T", "fl_dev_mult_div_invscalar_div_T", "fl_dev_assemble_kmk",
     "fl_dev_masslumped_poisson_rhs", "fl_dev_correct_masslumped_velocity", "fl_dev_csr_addto",
-    "fl_dev_assemble_advdif_faces", "fl_gpu_assemble_advdif_faces",
+    "fl_dev_assemble_advdif_faces", "fl_gpu_assemble_advdif_faces", "fl_set_wait_test",
 ]
 
 _P = C.c_void_p
@@ -177,6 +177,7 @@ _SIGNATURES = {
                                                C.POINTER(Fields), _P, _P, _P]),
     "fl_gpu_assemble_advdif_faces": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(FaceBcs),
                                                C.POINTER(Fields), _P, _P]),
+    "fl_set_wait_test": (C.c_int, [_I32, _D]),
 }
 assert sorted(_SIGNATURES) == sorted(EXPORTS)
 

@@ -904,6 +904,8 @@ struct FusedArgs {
   int32_t* gdone;        // per group of kFzGroup element items: items done
   int32_t* ctl;          // [0] queue head
   ErrWord* err;
+  unsigned spin_limit;   // polls of one counter before giving up
+  int32_t withhold;      // failure-injection test: this group never counts complete
 };
 constexpr int kFzItem = 256;             // elements or rows per item = threads per block
 constexpr int kFzGroup = 64;             // element items per completion counter
@@ -955,12 +957,12 @@ __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, 
         const int first = __ldg(F.need + 2 * j), last = __ldg(F.need + 2 * j + 1);
         unsigned spins = 0;
         for (int g = first / kFzGroup; last >= 0 && g <= last / kFzGroup; ++g) {
-          const int target = min(kFzGroup, F.ne - g * kFzGroup);
+          const int target = min(kFzGroup, F.ne - g * kFzGroup) + (g == F.withhold ? 1 : 0);
           while (ld_acquire(F.gdone + g) < target) {
-            if (++spins > kFzSpin) break;
+            if (++spins > F.spin_limit) break;
             __nanosleep(64);
           }
-          if (spins > kFzSpin) {
+          if (spins > F.spin_limit) {
             set_err(F.err, FL_ERR_TIMEOUT, j);
             break;
           }
@@ -1155,7 +1157,11 @@ static int launch_fused(fl_mesh_t* m, const DfArgs& D, const PullArgs& P, cudaSt
                                                             smem));
   const int ne = (m->E + kFzItem - 1) / kFzItem, ng = (ne + kFzGroup - 1) / kFzGroup;
   // ctl[0] queue head, ctl[1..ng] group counters: zeroed per call
-  FusedArgs F{m->fz_nitems, ne, m->fz_items.p, m->fz_perm.p, m->fz_need.p, m->fz_ctl.p + 1, m->fz_ctl.p, m->err.p};
+  const WaitTest& wt = wait_test();
+  // about 0.5 us per poll (a 64 ns sleep and an L2 load)
+  const unsigned spin = wt.wait_ms > 0.0 ? (unsigned)std::max(1.0, wt.wait_ms * 2000.0) : kFzSpin;
+  FusedArgs F{m->fz_nitems, ne, m->fz_items.p, m->fz_perm.p, m->fz_need.p, m->fz_ctl.p + 1, m->fz_ctl.p, m->err.p,
+              spin, wt.withhold};
   FL_TRY_CUDA(cudaMemsetAsync(m->fz_ctl.p, 0, sizeof(int32_t) * (1 + ng), s));
   const unsigned g = (unsigned)std::max(1, std::min(m->fz_nitems, num_sms() * std::max(1, per_sm)));
   k_asm_p1_fused<MASS, SRC, TF, ANISO><<<g, kFzItem, smem, s>>>(D, P, F);

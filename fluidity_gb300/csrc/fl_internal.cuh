@@ -153,6 +153,16 @@ int rows_p1_closed(struct ::fl_mesh_t* m, const double* em, double* val, double*
 // (K_a3 from the zero row sum), 32 B per (element, local row).
 int rows_p1_df(struct ::fl_mesh_t* m, const double* em, double* val, double* rhs, cudaStream_t s);
 
+// Failure injection for tests of the bounded device waits (fl_set_wait_test):
+// withhold >= 0 keeps one flag unset (colouring: that element never publishes
+// its colour; fused P1 pass: that element-item group never counts complete);
+// wait_ms > 0 bounds each wait to about that time instead of the defaults.
+struct WaitTest {
+  int32_t withhold = -1;
+  double wait_ms = 0.0;
+};
+WaitTest& wait_test();
+
 // node -> surface-face lists of the mesh (face_ptr / face_list: for every
 // field node the faces holding it, ascending), from nf faces of floc nodes.
 int node_face_lists(struct ::fl_mesh_t* m, int32_t nf, int32_t floc, const int32_t* faces, int32_t base,

@@ -119,7 +119,8 @@ int check_err(ErrWord* d_err, cudaStream_t s, const char* what) {
   if (h.code == FL_OK) return FL_OK;
   FL_TRY_CUDA(cudaMemsetAsync(d_err, 0, sizeof(ErrWord), s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
-  set_error("%s (status %d at index %d)", what, h.code, h.where);
+  set_error("%s%s (status %d at index %d)", h.code == FL_ERR_TIMEOUT ? "a bounded device wait ran out: " : "",
+            what, h.code, h.where);
   return h.code;
 }
 
@@ -337,7 +338,7 @@ constexpr int kMaxColourWords = 8;  // up to 256 colours
 __global__ void k_colour_dataflow(const int32_t* __restrict__ vne_ptr, const int32_t* __restrict__ vne,
                                   const int32_t* __restrict__ xnd, int32_t E,
                                   int32_t* __restrict__ colour, int32_t* __restrict__ ticket,
-                                  ErrWord* err, long long wait_cycles) {
+                                  ErrWord* err, long long wait_cycles, int32_t withhold) {
   note_launch();
   const int lane = threadIdx.x & 31;
   while (true) {
@@ -388,7 +389,7 @@ __global__ void k_colour_dataflow(const int32_t* __restrict__ vne_ptr, const int
       uint32_t m = __reduce_or_sync(0xffffffffu, mask[k]);
       if (!mine && m != 0xffffffffu) mine = 32 * k + __ffs(~m);
     }
-    if (lane == 0) {
+    if (lane == 0 && e != withhold) {  // a withheld element (failure-injection test) never publishes
       if (mine == 0) {
         set_err(err, FL_ERR_COLOURS, e);
         st_relaxed(&colour[e], 1 << 30);  // unblock waiters; status reports the failure
@@ -475,6 +476,11 @@ __global__ void k_incidence_positions(const int32_t* __restrict__ ne_ptr, const 
   }
 }
 
+WaitTest& wait_test() {
+  static WaitTest w;
+  return w;
+}
+
 static int build_colouring(fl_mesh_t* m, cudaStream_t s) {
   const int32_t E = m->E;
   FL_TRY(m->vne_ptr.reserve(m->Nx + 1));
@@ -487,9 +493,11 @@ static int build_colouring(fl_mesh_t* m, cudaStream_t s) {
   int dev = 0, clk_khz = 2000000;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&clk_khz, cudaDevAttrClockRate, dev);
-  const long long wait_cycles = (long long)clk_khz * 1000LL * 2;  // ~2 s per wait
+  const WaitTest& wt = wait_test();
+  const long long wait_cycles = wt.wait_ms > 0.0 ? (long long)(clk_khz * wt.wait_ms)
+                                                 : (long long)clk_khz * 1000LL * 2;  // ~2 s per wait
   k_colour_dataflow<<<num_sms() * 8, 256, 0, s>>>(m->vne_ptr.p, m->vne.p, m->xndglno.p, E,
-                                                   m->colour.p, ticket.p, m->err.p, wait_cycles);
+                                                   m->colour.p, ticket.p, m->err.p, wait_cycles, wt.withhold);
   FL_TRY_CUDA(cudaGetLastError());
   FL_TRY(check_err(m->err.p, s, "colouring"));
   // colour sets: histogram, offsets, stable per-colour compaction
@@ -863,5 +871,15 @@ extern "C" int fl_gpu_make_global_numbering_p2(int32_t nv, int32_t E, const int3
   FL_TRY_CUDA(cudaMemcpyAsync(nd2_host, nd2.p, sizeof(int32_t) * (size_t)E * 10, cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
   *n2 = nv + nedges;
+  return FL_OK;
+}
+
+extern "C" int fl_set_wait_test(int32_t withhold, double wait_ms) {
+  using namespace fl;
+  FL_CHECK_ARG(withhold >= -1, "withhold is a flag index, or -1 to switch the hook off");
+  FL_CHECK_ARG(wait_ms >= 0.0 && wait_ms <= 60000.0, "wait_ms in [0, 60000]");
+  FL_CHECK_ARG(withhold == -1 || wait_ms > 0.0, "a withheld flag needs a wait limit (wait_ms > 0)");
+  wait_test().withhold = withhold;
+  wait_test().wait_ms = wait_ms;
   return FL_OK;
 }

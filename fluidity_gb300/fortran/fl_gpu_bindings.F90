@@ -66,7 +66,7 @@ module fl_gpu_bindings
             fl_dev_assemble_divergence_cg, fl_dev_lumped_mass, fl_dev_mult_div_vector_div_T, &
             fl_dev_mult_div_invscalar_div_T, fl_dev_assemble_kmk, fl_dev_masslumped_poisson_rhs, &
             fl_dev_correct_masslumped_velocity, fl_dev_csr_addto, fl_kernel_launch_count, &
-            fl_set_kernel_timing, fl_last_assembly_kernel_ms
+            fl_set_kernel_timing, fl_last_assembly_kernel_ms, fl_set_wait_test
   public :: gpu_check, gpu_mesh_handle, gpu_advdif_cg_supported, gpu_assemble_advection_diffusion_cg, &
             gpu_petsc_solve_supported, gpu_petsc_solve_scalar, gpu_solve_field_equation_cg
 
@@ -550,6 +550,14 @@ module fl_gpu_bindings
        real(c_float), intent(out) :: ms
        integer(c_int) :: st
      end function fl_last_assembly_kernel_ms
+
+     ! failure injection for tests of the bounded device waits
+     function fl_set_wait_test(withhold, wait_ms) bind(c, name="fl_set_wait_test") result(st)
+       import :: c_int, c_int32_t, c_double
+       integer(c_int32_t), value :: withhold
+       real(c_double), value :: wait_ms
+       integer(c_int) :: st
+     end function fl_set_wait_test
   end interface
 
 contains

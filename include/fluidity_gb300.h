@@ -228,6 +228,22 @@ int fl_dev_assemble_advdif_faces(fl_mesh mesh, const fl_advdif_params* params, c
 int fl_gpu_assemble_advdif_faces(fl_mesh mesh, const fl_advdif_params* params, const fl_face_bcs* faces,
                                  const fl_fields* fields, double* val, double* rhs);
 
+/* Failure injection for tests of the bounded device waits (no counterpart in
+ * the reference, whose loops do not wait on other threads).  Two kernels wait
+ * on flags other threads set: the colouring dataflow of fl_gpu_mesh_register
+ * (an element waits for the colours of its lower neighbours; limit about
+ * 2 s) and the fused P1 pass (row tile 3; a row item waits for the element
+ * items it reads; limit 2^22 polls).  After this call, in this process:
+ * wait_ms > 0 bounds each such wait to about wait_ms milliseconds, and
+ * withhold >= 0 keeps one flag unset -- the colour of element `withhold`, or
+ * the completion of element-item group `withhold` -- so that the waits on it
+ * run out.  The waiting side then records FL_ERR_TIMEOUT and stops; every
+ * kernel finishes, the call returns FL_ERR_TIMEOUT ("a bounded device wait ran
+ * out"), the CUDA context and other handles stay usable, and the next call
+ * without the hook gives the normal results.  fl_set_wait_test(-1, 0) switches
+ * the hook off; a withheld flag needs wait_ms > 0. */
+int fl_set_wait_test(int32_t withhold, double wait_ms);
+
 /* Allocation-free form of fl_dev_assemble_advdif_cg for the P1 diffusion
  * (pressure-Poisson) case: diffusivity with optional source and consistent
  * mass, no advection or absorption, on a P1 field mesh.  No counterpart in the
