@@ -670,6 +670,40 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
   }
 }
 
+// Confirmation of an unpreconditioned-norm convergence on the recomputed
+// residual.  k_cg_reopen lets k_init_resid form r = b - A y and z = B r from
+// the iterate (done and guess_zero cleared); k_cg_confirm then keeps the
+// convergence when ||b - A y|| <= ttol, or else continues CG from the same
+// search direction with the recomputed residual (residual replacement: beta
+// from the new z.r), so rtol bounds the true residual and not only the
+// recurrence's, which drifts from it by rounding.
+__global__ void k_cg_reopen(KspState* st) {
+  note_launch();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  st->done = 0;
+  st->guess_zero = 0;
+}
+
+__global__ void k_cg_confirm(KspState* st, const double* __restrict__ part, int nparts) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  const double zr = reduce_partials(part + 2 * nparts, nparts, red);
+  const double rr = reduce_partials(part + 3 * nparts, nparts, red);
+  if (threadIdx.x != 0) return;
+  KspState& S = *st;
+  const double rn = sqrt(rr);
+  S.rnorm = rn;
+  if (!(rn > S.ttol) || S.its >= S.max_its) {  // confirmed (or out of iterations: the reason stands)
+    S.done = 1;
+    return;
+  }
+  S.reason = 0;
+  S.beta = zr;
+  S.pcoef = zr / S.betaold;
+  S.cg_i = S.cg_i + 1;
+  S.its = S.cg_i + 1;
+}
+
 // Opening checks of iteration 0 (beta of the initial residual).
 __global__ void k_cg_open(KspState* st) {
   note_launch();
@@ -1389,11 +1423,29 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     FL_TRY(gr.build([&](cudaStream_t c) {
       for (int k = 0; k < chunk; ++k) cg_iteration(n, st, SA, W, gv, gsl, np, c);
     }));
-    for (int i = 0; i < o->max_its; i += chunk) {
-      FL_TRY(gr.launch());
-      int done = 0;
-      FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, W->cs));
+    // with the unpreconditioned norm a convergence is confirmed on the
+    // recomputed residual (at most a few replacements; each normally passes)
+    for (int confirm = 0; confirm < (o->norm_type == 1 ? 4 : 1); ++confirm) {
+      for (int i = 0; i < o->max_its; i += chunk) {
+        FL_TRY(gr.launch());
+        int done = 0;
+        FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, W->cs));
+        FL_TRY_CUDA(cudaStreamSynchronize(W->cs));
+        if (done) break;
+      }
+      if (o->norm_type != 1) break;
+      int hr[2] = {0, 0};
+      FL_TRY_CUDA(cudaMemcpyAsync(hr, &st->reason, sizeof(int) * 2, cudaMemcpyDeviceToHost, W->cs));
       FL_TRY_CUDA(cudaStreamSynchronize(W->cs));
+      if (hr[0] != FL_CONVERGED_RTOL) break;
+      const cudaStream_t c = W->cs;
+      k_cg_reopen<<<1, 32, 0, c>>>(st);
+      FL_SPMV_DISPATCH_S(G, c, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
+      k_cg_confirm<<<1, kThreads, 0, c>>>(st, W->part.p, (int)gsp);
+      FL_TRY_CUDA(cudaGetLastError());
+      int done = 0;
+      FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, c));
+      FL_TRY_CUDA(cudaStreamSynchronize(c));
       if (done) break;
     }
     FL_TRY(gr.join());

@@ -146,8 +146,8 @@ def test_unpreconditioned_norm_cg_matches_oracle(O, start_from_zero):
     assert rep["reason"] == oreason == 2
     assert abs(rep["iterations"] - oits) <= 1
     assert np.abs(x - ox).max() <= 1e-7 * np.abs(ox).max()
-    assert rep["true_rel_residual"] <= 1.05e-10
-    # the tested norm is ||r||: the recurrence residual it reports is the true one
+    # the convergence is confirmed on the recomputed residual: rtol bounds it
+    assert rep["true_rel_residual"] <= 1e-10 * (1 + 1e-9)
     assert abs(rep["final_rnorm"] / rep["rnorm0"] - rep["true_rel_residual"]) <= 1e-12
 
 
