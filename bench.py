@@ -732,10 +732,15 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
 
     variants = {
         "fp64_zero": ("fp64", "zero"), "fp64_previous": ("fp64", "previous"),
-        "fp64_learned": ("fp64", "learned"), "mixed_previous": ("reliable", "previous"),
-        "mixed_learned": ("reliable", "learned"), "mixed_zero": ("reliable", "zero"),
+        "fp64_learned": ("fp64", "learned"), "fp64_projection": ("fp64", "projection"),
+        "fp64_learned_projection": ("fp64", "learned_projection"),
+        "mixed_previous": ("reliable", "previous"), "mixed_learned": ("reliable", "learned"),
+        "mixed_zero": ("reliable", "zero"), "mixed_projection": ("reliable", "projection"),
+        "mixed_learned_projection": ("reliable", "learned_projection"),
         "amg_zero": ("amg", "zero"), "amg_previous": ("amg", "previous"), "amg_learned": ("amg", "learned"),
+        "amg_projection": ("amg", "projection"), "amg_learned_projection": ("amg", "learned_projection"),
     }
+    nproj = 6  # earlier solutions in the projection basis (Fischer's method)
     # one AMG hierarchy serves the whole sequence (the matrix does not change)
     seq.system(ntrain)
     torch.cuda.synchronize()
@@ -745,6 +750,7 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
     torch.cuda.synchronize()
     amg_setup_ms = (time.perf_counter() - t0) * 1e3
     res = {k: {"ms": [], "iterations": [], "err": [], "true_rel_residual": []} for k in variants}
+    pred = torch.empty_like(ps[0])
     tight = ft.solver_options(ksp="cg", rtol=1e-13, max_its=50000, norm="unpreconditioned")
     x = torch.empty_like(ps[0])
     for t in range(ntrain, nsteps):
@@ -761,8 +767,14 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
                 x.zero_()
             elif guess == "previous":
                 x.copy_(ps[t - 1])
-            else:
+            elif guess == "learned":
                 net.predict(ps[t - 1], ps[t - 2], bs[t], out=x, stream=stream)
+            else:
+                basis = [ps[t - j] for j in range(1, nproj + 1)]
+                if guess == "learned_projection":
+                    net.predict(ps[t - 1], ps[t - 2], bs[t], out=pred, stream=stream)
+                    basis = [pred] + basis[:-1]
+                ft.projected_guess(m, val, rhs, basis, inactive=ina, out=x, stream=stream)
             if prec == "amg":
                 rep = amg.solve(x, rhs, ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000), stream=stream)
             else:
@@ -795,6 +807,9 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
         / summary["mixed_learned"]["mean_ms"],
         "speedup_fp64_learned_vs_fp64_previous": summary["fp64_previous"]["mean_ms"]
         / summary["fp64_learned"]["mean_ms"],
+        "projection": f"Fischer's projection onto the {nproj} previous solutions (learned_projection: the "
+                      f"network's prediction and the {nproj - 1} previous solutions), A-norm optimal, "
+                      "timed with the guess",
     }
 
 
@@ -1220,9 +1235,12 @@ def compact_summary(line):
     if ln:
         for k, v in ln.items():
             vs = v["variants"]
-            out[f"learned_{k}"] = {name: sig(vs[name]["mean_ms"]) for name in
-                                  ("fp64_zero", "fp64_previous", "fp64_learned", "mixed_previous", "mixed_learned",
-                                   "amg_previous") if name in vs}
+            out[f"learned_{k}"] = {name: [sig(vs[name]["mean_ms"]), sig(vs[name]["mean_iterations"], 3)] for name in
+                                  ("fp64_zero", "fp64_previous", "fp64_learned", "fp64_projection",
+                                   "fp64_learned_projection", "mixed_previous", "mixed_learned",
+                                   "mixed_projection", "mixed_learned_projection", "amg_previous",
+                                   "amg_projection", "amg_learned_projection") if name in vs}
+            out[f"learned_{k}"]["fields"] = "mean ms, mean iterations"
             out[f"learned_{k}"]["predict_ms"] = sig(v["predict_ms"])
             out[f"learned_{k}"]["max_true_rel_residual"] = sig(max(x["max_true_rel_residual"] for x in vs.values()), 3)
     return out

@@ -1891,3 +1891,188 @@ extern "C" int fl_dev_csr_mult(fl_mesh m, const double* val, const double* x, do
   cudaStream_t s = stream ? (cudaStream_t)stream : m->stream;
   return csr_mult(m, val, x, y, s);
 }
+
+// ------------------------------------------------ projected initial guess --
+// The projection method for sequences of right-hand sides (P. F. Fischer,
+// "Projection techniques for iterative solution of Ax = b with successive
+// right-hand sides", Comput. Methods Appl. Mech. Engrg. 163, 1998): given
+// basis vectors v_1..v_k (earlier solutions, a predicted solution), the
+// initial guess x0 = V a with (V^T A V) a = V^T b minimises the A-norm of the
+// error over span(V) -- the norm CG minimises.  A and b are the ghost-reduced
+// system the solve runs on (inactive rows and columns dropped, b lifted), so
+// the sums run over active rows only and ghost rows of x0 take the rhs.
+namespace fl {
+
+constexpr int kProjMax = 8;
+constexpr int kProjVals = kProjMax * (kProjMax + 1) / 2 + kProjMax;
+
+struct ProjArgs {
+  int32_t n, k;
+  const int32_t* findrm;
+  const int32_t* colm;
+  const double* val;
+  const uint8_t* ghost;
+  const double* rhs;
+  const double* v[kProjMax];
+  double* part;  // per block: the k(k+1)/2 Gram entries (upper triangle, row-major), then the k entries of V^T b
+};
+
+// One thread per row: w_l = (A v_l)(row) over active columns, b(row) lifted;
+// the row's products v_l w_m (l <= m) and v_l b, summed per block in a fixed
+// tree; the blocks' partials are summed in block order by k_proj_reduce.
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_proj_gram(ProjArgs P) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  constexpr int NV = K * (K + 1) / 2 + K;
+  double acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < P.n; row += gridDim.x * blockDim.x) {
+    if (P.ghost && P.ghost[row]) continue;
+    double w[K], lift = 0.0;
+#pragma unroll
+    for (int l = 0; l < K; ++l) w[l] = 0.0;
+    const int b = __ldg(P.findrm + row), e = __ldg(P.findrm + row + 1);
+    for (int q = b; q < e; ++q) {
+      const int j = __ldg(P.colm + q);
+      const double a = __ldg(P.val + q);
+      if (P.ghost && P.ghost[j]) {
+        lift += a * P.rhs[j];
+        continue;
+      }
+#pragma unroll
+      for (int l = 0; l < K; ++l) w[l] += a * __ldg(P.v[l] + j);
+    }
+    const double bi = P.rhs[row] - lift;
+    double vi[K];
+#pragma unroll
+    for (int l = 0; l < K; ++l) vi[l] = __ldg(P.v[l] + row);
+    int q = 0;
+#pragma unroll
+    for (int l = 0; l < K; ++l)
+#pragma unroll
+      for (int m = l; m < K; ++m) acc[q++] += vi[l] * w[m];
+#pragma unroll
+    for (int l = 0; l < K; ++l) acc[q++] += vi[l] * bi;
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const double s = block_sum<kThreads>(acc[q], red);
+    if (threadIdx.x == 0) P.part[(int64_t)blockIdx.x * NV + q] = s;
+  }
+}
+
+// The blocks' partials of each value summed in block order (one block).
+__global__ void k_proj_reduce(const double* __restrict__ part, int nblocks, int nv, double* __restrict__ out) {
+  note_launch();
+  __shared__ double red[kThreads / 32];
+  for (int q = 0; q < nv; ++q) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += kThreads) s += part[(int64_t)b * nv + q];
+    s = block_sum<kThreads>(s, red);
+    if (threadIdx.x == 0) out[q] = s;
+  }
+}
+
+struct ProjCoef {
+  double a[kProjMax];
+};
+
+__global__ void k_proj_combine(int n, int k, ProjCoef C, ProjArgs P, double* __restrict__ x0) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (P.ghost && P.ghost[i]) {
+      x0[i] = P.rhs[i];
+      continue;
+    }
+    double s = 0.0;
+    for (int l = 0; l < k; ++l) s += C.a[l] * P.v[l][i];
+    x0[i] = s;
+  }
+}
+
+// (V^T A V) a = V^T b by an LDL^T factorisation that drops a basis vector
+// whose pivot is below 1e-13 of its diagonal (it lies in the span of the
+// earlier ones): the earlier vectors take precedence.
+static void proj_solve(int k, const double* vals, double* a) {
+  double G[kProjMax][kProjMax], c[kProjMax], L[kProjMax][kProjMax] = {}, D[kProjMax];
+  bool keep[kProjMax];
+  int q = 0;
+  for (int l = 0; l < k; ++l)
+    for (int m = l; m < k; ++m) G[l][m] = G[m][l] = vals[q++];
+  for (int l = 0; l < k; ++l) c[l] = vals[q++];
+  for (int i = 0; i < k; ++i) {
+    double d = G[i][i];
+    for (int j = 0; j < i; ++j)
+      if (keep[j]) d -= L[i][j] * L[i][j] * D[j];
+    keep[i] = G[i][i] > 0.0 && d > 1e-13 * G[i][i];
+    D[i] = keep[i] ? d : 0.0;
+    L[i][i] = 1.0;
+    for (int r = i + 1; r < k; ++r) {
+      double s = G[r][i];
+      for (int j = 0; j < i; ++j)
+        if (keep[j]) s -= L[r][j] * L[i][j] * D[j];
+      L[r][i] = keep[i] ? s / D[i] : 0.0;
+    }
+  }
+  double y[kProjMax];
+  for (int i = 0; i < k; ++i) {  // L y = c
+    double s = c[i];
+    for (int j = 0; j < i; ++j) s -= L[i][j] * y[j];
+    y[i] = keep[i] ? s : 0.0;
+  }
+  for (int i = 0; i < k; ++i) y[i] = keep[i] ? y[i] / D[i] : 0.0;
+  for (int i = k - 1; i >= 0; --i) {  // L^T a = y
+    double s = y[i];
+    for (int j = i + 1; j < k; ++j) s -= L[j][i] * a[j];
+    a[i] = keep[i] ? s : 0.0;
+  }
+}
+
+}  // namespace fl
+
+extern "C" int fl_dev_projected_guess(fl_mesh m, const double* val, const uint8_t* inactive, const double* rhs,
+                                      int32_t k, const double* const* basis, double* x0, double* coef,
+                                      void* stream) {
+  using namespace fl;
+  FL_CHECK_ARG(m && val && rhs && basis && x0, "null argument");
+  FL_CHECK_ARG(k >= 1 && k <= kProjMax, "1 to 8 basis vectors");
+  for (int l = 0; l < k; ++l) FL_CHECK_ARG(basis[l], "null basis vector");
+  cudaStream_t s = stream ? (cudaStream_t)stream : m->stream;
+  KrylovWork* W = work_of(m);
+  if (!W) return FL_ERR_NOMEM;
+  const unsigned g = grid_for(m->N, kThreads, 4);
+  const int nv = k * (k + 1) / 2 + k;
+  FL_TRY(W->part.reserve((size_t)g * kProjVals + kProjVals));
+  ProjArgs P{};
+  P.n = m->N;
+  P.k = k;
+  P.findrm = m->findrm.p;
+  P.colm = m->colm.p;
+  P.val = val;
+  P.ghost = inactive;
+  P.rhs = rhs;
+  for (int l = 0; l < k; ++l) P.v[l] = basis[l];
+  P.part = W->part.p;
+  double* sums = W->part.p + (size_t)g * kProjVals;
+  switch (k) {
+#define FL_PROJ_CASE(K) \
+  case K: k_proj_gram<K><<<g, kThreads, 0, s>>>(P); break;
+    FL_PROJ_CASE(1) FL_PROJ_CASE(2) FL_PROJ_CASE(3) FL_PROJ_CASE(4)
+    FL_PROJ_CASE(5) FL_PROJ_CASE(6) FL_PROJ_CASE(7) FL_PROJ_CASE(8)
+#undef FL_PROJ_CASE
+  }
+  k_proj_reduce<<<1, kThreads, 0, s>>>(P.part, (int)g, nv, sums);
+  FL_TRY_CUDA(cudaGetLastError());
+  double vals[kProjVals];
+  FL_TRY_CUDA(cudaMemcpyAsync(vals, sums, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  ProjCoef C{};
+  proj_solve(k, vals, C.a);
+  if (coef)
+    for (int l = 0; l < k; ++l) coef[l] = C.a[l];
+  k_proj_combine<<<g, kThreads, 0, s>>>(m->N, k, C, P, x0);
+  FL_TRY_CUDA(cudaGetLastError());
+  return FL_OK;
+}

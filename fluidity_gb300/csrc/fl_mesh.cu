@@ -883,3 +883,56 @@ extern "C" int fl_set_wait_test(int32_t withhold, double wait_ms) {
   wait_test().wait_ms = wait_ms;
   return FL_OK;
 }
+
+// make_sparsity(pressure mesh, velocity mesh) (femtools/Sparsity_Patterns.F90
+// :47-85) for P1 pressure on the vertices and P2 velocity of one P2 mesh
+// handle: row v (a vertex of the coordinate mesh) holds the P2 nodes of the
+// elements containing v, ascending -- the first-order builder run over the
+// vertex -> element incidences with the P2 connectivity as candidates.
+extern "C" int fl_gpu_rect_register(fl_mesh m, fl_mesh* out) {
+  using namespace fl;
+  FL_CHECK_ARG(m && out, "null argument");
+  FL_CHECK_ARG(m->loc == 10 && m->E > 0 && m->vne_ptr.p, "a registered P2 mesh handle");
+  fl_mesh_t* h = new fl_mesh_t();
+  int st = FL_OK;
+  do {
+    cudaGetDevice(&h->device);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      set_error("cudaStreamCreate failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+    cudaStream_t s = h->stream;
+    h->N = m->Nx;
+    h->so_parent = m;
+    if ((st = h->err.reserve(1)) != FL_OK) break;
+    if (cudaMemsetAsync(h->err.p, 0, sizeof(ErrWord), s) != cudaSuccess) {
+      st = FL_ERR_CUDA;
+      break;
+    }
+    // the velocity mesh's incidences are complete on its own stream
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) {
+      st = FL_ERR_CUDA;
+      break;
+    }
+    if ((st = build_sparsity(m->ndglno.p, 10, m->Nx, m->vne_ptr, m->vne, h->findrm, h->colm, h->centrm, &h->nnz,
+                             h->err.p, s)) != FL_OK)
+      break;
+    DevBuf<int32_t> mr;
+    if ((st = mr.reserve(1)) != FL_OK) break;
+    cudaMemsetAsync(mr.p, 0, sizeof(int32_t), s);
+    k_max_row<<<grid_for(h->N, 256), 256, 0, s>>>(h->findrm.p, h->N, mr.p);
+    if (cudaMemcpyAsync(&h->max_row, mr.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      set_error("rectangular pattern: row length read failed");
+      st = FL_ERR_CUDA;
+      break;
+    }
+  } while (0);
+  if (st != FL_OK) {
+    fl_gpu_mesh_destroy(h);
+    return st;
+  }
+  *out = h;
+  return FL_OK;
+}

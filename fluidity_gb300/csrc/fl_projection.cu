@@ -57,6 +57,7 @@
 #include "fl_internal.cuh"
 #include "fl_device.cuh"
 #include "fl_df64.cuh"
+#include "fl_refelem.h"
 
 namespace fl {
 
@@ -975,6 +976,129 @@ int divergence_passes(fl_mesh_t* m, bool by_parts, double* ct0, double* ct1, dou
   return by_parts ? launch_div_rows<64, 32, true, true>(R, s) : launch_div_rows<64, 32, true, false>(R, s);
 }
 
+// ------------------------------------------- Taylor-Hood divergence (P2/P1) --
+// assemble_divergence_matrix_cg (Divergence_Matrix_CG.F90:67-375) for P1
+// pressure on the vertices and P2 velocity, the element terms: with the
+// divergence element records (sign(det) cof / 24 per element, double-float),
+//   not by parts: C_d(a, j) = int N_a dN_j/dx_d = sum_c 24 T(a, j, c) rec(d, c),
+//                 T(a, j, c) = sum_g w_g N_a(g) dN_j/dL_c(g)
+//   by parts:     C_d(a, j) = -int dN_a/dx_d N_j = -sum_c 24 Tb(a, j, c) rec(d, c),
+//                 Tb(a, j, c) = sum_g w_g dN_a/dL_c(g) N_j(g)
+// (dN/dx_d = sum_c dN/dL_c cof(d, c) / det).  One warp per pressure row adds
+// its elements in ascending element order (the reference's element loop
+// order); lanes (d, j) of an element write distinct slots of the row's
+// double-float accumulators in shared memory.
+struct ThTensor {
+  float2 t[4][10][3];  // 24 T or -24 Tb, double-float
+};
+
+struct ThArgs {
+  int32_t Np;
+  const int32_t* vne_ptr;
+  const int32_t* vne;      // vertex -> element << 4 | local vertex, element ascending
+  const int32_t* nd2;      // P2 connectivity, 10 per element
+  const int32_t* findrm;   // rectangular pattern
+  const int32_t* colm;
+  const float4* rec;       // 5 float4 per element
+  double* ct0;
+  double* ct1;
+  double* ct2;
+  ErrWord* err;
+};
+
+constexpr int kThWarps = 4;
+constexpr int kThMaxRow = 192;
+
+__global__ void __launch_bounds__(kThWarps * 32) k_div_rows_th(ThArgs A, ThTensor T) {
+  note_launch();
+  __shared__ int32_t cols[kThWarps][kThMaxRow];
+  __shared__ float2 acc[kThWarps][3][kThMaxRow];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = lane % 10, d = lane / 10;  // lanes 0..29: (component, velocity node)
+  for (int row = blockIdx.x * kThWarps + w; row < A.Np; row += gridDim.x * kThWarps) {
+    const int base = __ldg(A.findrm + row), L = __ldg(A.findrm + row + 1) - base;
+    if (L > kThMaxRow) {
+      if (lane == 0) set_err(A.err, FL_ERR_UNSUPPORTED, row);
+      continue;
+    }
+    for (int k = lane; k < L; k += 32) {
+      cols[w][k] = __ldg(A.colm + base + k);
+      acc[w][0][k] = acc[w][1][k] = acc[w][2][k] = make_float2(0.0f, 0.0f);
+    }
+    __syncwarp();
+    const int ib = __ldg(A.vne_ptr + row), ie = __ldg(A.vne_ptr + row + 1);
+    for (int q = ib; q < ie; ++q) {
+      const int inc = __ldg(A.vne + q);
+      const int e = inc >> 4, a = inc & 15;
+      int pos = -1;
+      if (lane < 10) {
+        const int node = __ldg(A.nd2 + (int64_t)e * 10 + lane);
+        int lo = 0, hi = L - 1;
+        while (lo <= hi) {
+          const int mid = (lo + hi) >> 1, c = cols[w][mid];
+          if (c == node) {
+            pos = mid;
+            break;
+          }
+          if (c < node) lo = mid + 1;
+          else hi = mid - 1;
+        }
+      }
+      const int pj = __shfl_sync(0xffffffffu, pos, j);
+      if (lane < 30) {
+        const float4* r = A.rec + (uint32_t)e * 5u;
+        float v[6];
+        const float4 r0 = __ldg(r + (3 * d) / 2), r1 = __ldg(r + (3 * d) / 2 + 1);
+        // record entries 3d..3d+2 (two per float4: hi, lo pairs)
+        v[0] = r0.x; v[1] = r0.y; v[2] = r0.z; v[3] = r0.w; v[4] = r1.x; v[5] = r1.y;
+        const int o = (3 * d) & 1;  // entry 3d starts in the second half of its float4 when odd
+        df c[3];
+        if (o == 0) {
+          c[0] = {v[0], v[1]}; c[1] = {v[2], v[3]}; c[2] = {v[4], v[5]};
+        } else {
+          const float4 r2 = __ldg(r + (3 * d) / 2 + 1);
+          c[0] = {v[2], v[3]}; c[1] = {r2.x, r2.y}; c[2] = {r2.z, r2.w};
+        }
+        const float2 t0 = T.t[a][j][0], t1 = T.t[a][j][1], t2 = T.t[a][j][2];
+        const df val = df_dot3({t0.x, t0.y}, c[0], {t1.x, t1.y}, c[1], {t2.x, t2.y}, c[2]);
+        if (pj < 0) {
+          set_err(A.err, FL_ERR_OUTSIDE_PATTERN, row);
+        } else {
+          const float2 s0 = acc[w][d][pj];
+          const df sum = df_add({s0.x, s0.y}, val);
+          acc[w][d][pj] = make_float2(sum.hi, sum.lo);
+        }
+      }
+      __syncwarp();
+    }
+    for (int k = lane; k < L; k += 32) {
+      const float2 x0 = acc[w][0][k], x1 = acc[w][1][k], x2 = acc[w][2][k];
+      A.ct0[base + k] = df_to_double({x0.x, x0.y});
+      A.ct1[base + k] = df_to_double({x1.x, x1.y});
+      A.ct2[base + k] = df_to_double({x2.x, x2.y});
+    }
+    __syncwarp();
+  }
+}
+
+static int th_tensor(int quad_degree, bool by_parts, ThTensor& T) {
+  TetQuad q;
+  if (!tet_quadrature(quad_degree, q)) return FL_ERR_ARG;
+  TetShape p1, p2;
+  tet_shape(1, q, p1);
+  tet_shape(2, q, p2);
+  for (int a = 0; a < 4; ++a)
+    for (int jj = 0; jj < 10; ++jj)
+      for (int c = 0; c < 3; ++c) {
+        double s = 0.0;
+        for (int g = 0; g < q.ngi; ++g)
+          s += q.w[g] * (by_parts ? p1.dn[a][g][c] * p2.n[jj][g] : p1.n[a][g] * p2.dn[jj][g][c]);
+        const df h = df_host(by_parts ? -24.0 * s : 24.0 * s);
+        T.t[a][jj][c] = make_float2(h.hi, h.lo);
+      }
+  return FL_OK;
+}
+
 }  // namespace
 }  // namespace fl
 
@@ -1235,4 +1359,25 @@ extern "C" int fl_dev_csr_addto(fl_mesh pattern, double* val, const double* othe
   k_axpy<<<grid_for(pattern->nnz, kT), kT, 0, s>>>(pattern->nnz, scale, other, val);
   FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
+}
+
+extern "C" int fl_dev_assemble_divergence_p2p1(fl_mesh m, fl_mesh rect, int32_t integrate_by_parts,
+                                              int32_t quad_degree, double* const ct_val[3], void* stream) {
+  FL_CHECK_ARG(m && rect && ct_val && ct_val[0] && ct_val[1] && ct_val[2], "null argument");
+  FL_CHECK_ARG(m->loc == 10 && m->E > 0, "a P2 (velocity) mesh handle");
+  FL_CHECK_ARG(rect->so_parent == m && rect->N == m->Nx, "the rectangular pattern of this mesh (fl_gpu_rect_register)");
+  FL_CHECK_ARG(quad_degree >= 1 && quad_degree <= 4, "quadrature degree 1..4");
+  cudaStream_t s = pick(m, stream);
+  ThTensor T;
+  FL_TRY(th_tensor(quad_degree, integrate_by_parts != 0, T));
+  FL_TRY(m->em.reserve((size_t)m->E * 10));  // 80 B per element
+  DivElemArgs D{m->E, m->xndglno.p, m->coords.p, reinterpret_cast<float4*>(m->em.p), df_host(1.0 / 24.0)};
+  k_div_elem<<<grid_for(m->E, 256, 16), 256, (256 / 32) * 160 * sizeof(float4), s>>>(D);
+  FL_TRY_CUDA(cudaGetLastError());
+  ThArgs A{rect->N, m->vne_ptr.p, m->vne.p, m->ndglno.p, rect->findrm.p, rect->colm.p,
+           reinterpret_cast<const float4*>(m->em.p), ct_val[0], ct_val[1], ct_val[2], m->err.p};
+  k_div_rows_th<<<grid_for(rect->N, kThWarps * 32, 8), kThWarps * 32, 0, s>>>(A, T);
+  FL_TRY_CUDA(cudaGetLastError());
+  return check_err(m->err.p, s, "Taylor-Hood divergence: a row longer than the kernel's row scratch, or a "
+                                "velocity node outside the pattern");
 }

@@ -360,6 +360,23 @@ class AmgPreconditioner:
             pass
 
 
+def projected_guess(mesh: Mesh, val, rhs, basis, inactive=None, out=None, stream=None):
+    """Initial guess x0 = V a minimising the A-norm error over span(basis)
+    (the projection method for successive right-hand sides, Fischer 1998) on
+    the ghost-reduced system petsc_solve solves; device tensors.  Returns
+    (x0, a)."""
+    import torch
+    k = len(basis)
+    ptrs = (C.c_void_p * k)(*[b.data_ptr() for b in basis])
+    coef = np.zeros(k)
+    if out is None:
+        out = torch.empty(mesh.N, dtype=torch.float64, device="cuda")
+    check(mesh.lib.fl_dev_projected_guess(mesh.handle, _ptr(val), _ptr(inactive), _ptr(rhs), k, ptrs,
+                                          _ptr(out), coef.ctypes.data, _stream_ptr(stream)),
+          "fl_dev_projected_guess")
+    return out, coef
+
+
 def csr_mult(mesh: Mesh, val, x, y, stream=None):
     """y = A x (device tensors)."""
     check(mesh.lib.fl_dev_csr_mult(mesh.handle, _ptr(val), _ptr(x), _ptr(y), _stream_ptr(stream)),

@@ -66,7 +66,8 @@ module fl_gpu_bindings
             fl_dev_assemble_divergence_cg, fl_dev_lumped_mass, fl_dev_mult_div_vector_div_T, &
             fl_dev_mult_div_invscalar_div_T, fl_dev_assemble_kmk, fl_dev_masslumped_poisson_rhs, &
             fl_dev_correct_masslumped_velocity, fl_dev_csr_addto, fl_kernel_launch_count, &
-            fl_set_kernel_timing, fl_last_assembly_kernel_ms, fl_set_wait_test
+            fl_set_kernel_timing, fl_last_assembly_kernel_ms, fl_set_wait_test, fl_dev_projected_guess, &
+            fl_gpu_rect_register, fl_dev_assemble_divergence_p2p1
   public :: gpu_check, gpu_mesh_handle, gpu_advdif_cg_supported, gpu_assemble_advection_diffusion_cg, &
             gpu_petsc_solve_supported, gpu_petsc_solve_scalar, gpu_solve_field_equation_cg
 
@@ -478,6 +479,23 @@ module fl_gpu_bindings
        integer(c_int) :: st
      end function fl_dev_assemble_divergence_cg
 
+     ! Taylor-Hood pair: P2 velocity (the mesh), P1 pressure on its vertices
+     function fl_gpu_rect_register(mesh, out) bind(c, name="fl_gpu_rect_register") result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: mesh
+       type(c_ptr), intent(out) :: out
+       integer(c_int) :: st
+     end function fl_gpu_rect_register
+
+     function fl_dev_assemble_divergence_p2p1(mesh, pattern, integrate_by_parts, quad_degree, ct_val, stream) &
+          bind(c, name="fl_dev_assemble_divergence_p2p1") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: mesh, pattern, stream
+       integer(c_int32_t), value :: integrate_by_parts, quad_degree
+       type(c_ptr), intent(in) :: ct_val(3)
+       integer(c_int) :: st
+     end function fl_dev_assemble_divergence_p2p1
+
      function fl_dev_lumped_mass(mesh, lumped_mass, stream) bind(c, name="fl_dev_lumped_mass") result(st)
        import :: c_int, c_ptr
        type(c_ptr), value :: mesh, lumped_mass, stream
@@ -550,6 +568,17 @@ module fl_gpu_bindings
        real(c_float), intent(out) :: ms
        integer(c_int) :: st
      end function fl_last_assembly_kernel_ms
+
+     ! projected initial guess from earlier solutions (device pointers;
+     ! basis is an array of k device addresses)
+     function fl_dev_projected_guess(mesh, val, inactive, rhs, k, basis, x0, coef, stream) &
+          bind(c, name="fl_dev_projected_guess") result(st)
+       import :: c_int, c_ptr, c_int32_t
+       type(c_ptr), value :: mesh, val, inactive, rhs, x0, coef, stream
+       integer(c_int32_t), value :: k
+       type(c_ptr), intent(in) :: basis(*)
+       integer(c_int) :: st
+     end function fl_dev_projected_guess
 
      ! failure injection for tests of the bounded device waits
      function fl_set_wait_test(withhold, wait_ms) bind(c, name="fl_set_wait_test") result(st)

@@ -73,6 +73,40 @@ def get_csr_sparsity_secondorder(mesh: ft.Mesh) -> SecondOrderPattern:
     return SecondOrderPattern(mesh)
 
 
+class TaylorHoodPattern(ft.Mesh):
+    """make_sparsity(pressure mesh, velocity mesh) of a P2 velocity mesh with
+    P1 pressure on its vertices (fl_gpu_rect_register): rows are the
+    vertices, columns the P2 nodes.  A pattern-only handle; it keeps its
+    mesh alive."""
+
+    def __init__(self, mesh: ft.Mesh):
+        self.lib = _lib.load()
+        self.parent = mesh
+        h = C.c_void_p()
+        check(self.lib.fl_gpu_rect_register(mesh.handle, C.byref(h)), "fl_gpu_rect_register")
+        self.handle = h
+        nnz, ncol = C.c_int64(), C.c_int32()
+        check(self.lib.fl_gpu_mesh_info(h, C.byref(nnz), C.byref(ncol)), "fl_gpu_mesh_info")
+        self.N, self.E, self.loc, self.Nx = mesh.Nx, 0, 0, 0
+        self.nnz, self.ncolours = nnz.value, 0
+        self._sparsity = None
+
+
+def assemble_divergence_matrix_p2p1(mesh: ft.Mesh, pattern: TaylorHoodPattern, *, integrate_by_parts=False,
+                                    quad_degree=4, ct=None, stream=None):
+    """The element terms of C^T for P2 velocity (mesh) and P1 pressure on its
+    vertices, blocks (1, dim) on the Taylor-Hood pattern: a (3, nnz) device
+    tensor."""
+    torch = _torch()
+    if ct is None:
+        ct = torch.empty((3, pattern.nnz), dtype=torch.float64, device="cuda")
+    check(_lib.load().fl_dev_assemble_divergence_p2p1(mesh.handle, pattern.handle, int(bool(integrate_by_parts)),
+                                                      int(quad_degree), _ptrs([ct[0], ct[1], ct[2]]),
+                                                      ft._stream_ptr(stream)),
+          "fl_dev_assemble_divergence_p2p1")
+    return ct
+
+
 def assemble_divergence_matrix_cg(mesh: ft.Mesh, *, integrate_by_parts=False, faces=None, face_ele=None,
                                   bc_type=None, bc_val=None, ct=None, ct_rhs=None, div_mass_lumped=None,
                                   grad_mass_lumped=None, stream=None):

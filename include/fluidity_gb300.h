@@ -334,6 +334,21 @@ int fl_dev_petsc_solve(fl_mesh mesh, const fl_solver_opts* opts, const double* v
                        const uint8_t* inactive, const double* rhs, double* x,
                        fl_solve_report* report, void* stream);
 
+/* Initial guess for a solve in a sequence of solves (no counterpart in the
+ * reference, which starts from the previous solution or from zero): the
+ * projection method of P. F. Fischer (1998).  Given k (1..8) basis vectors
+ * -- earlier solutions, a network's prediction -- x0 = V a where
+ * (V^T A V) a = V^T b, with A and b the ghost-reduced system
+ * fl_dev_petsc_solve solves (inactive rows and columns dropped, b = rhs
+ * lifted by the inactive values), minimises the A-norm of x0's error over
+ * span(V), the norm CG minimises; ghost rows of x0 take the rhs.  Basis
+ * vectors in the span of earlier ones are dropped (LDL^T pivot below 1e-13
+ * of its diagonal).  basis: a host array of k device pointers; coef (host,
+ * k values, may be NULL) receives a.  Device pointers otherwise; the call
+ * waits for its stream once (the k x k system is solved on the host). */
+int fl_dev_projected_guess(fl_mesh mesh, const double* val, const uint8_t* inactive, const double* rhs,
+                           int32_t k, const double* const* basis, double* x0, double* coef, void* stream);
+
 /* y = A x on the handle's pattern (csr_mult, femtools/Sparse_Tools.F90:3822);
  * device pointers. */
 int fl_dev_csr_mult(fl_mesh mesh, const double* val, const double* x, double* y, void* stream);
@@ -493,6 +508,21 @@ typedef struct {
 int fl_dev_assemble_divergence_cg(fl_mesh mesh, const fl_divergence_params* params, double* const ct_val[3],
                                   double* ct_rhs, double* div_mass_lumped, double* grad_mass_lumped,
                                   void* stream);
+
+/* Taylor-Hood pair: P2 velocity (the mesh) and P1 pressure on its vertices.
+ * fl_gpu_rect_register builds make_sparsity(pressure mesh, velocity mesh)
+ * (femtools/Sparsity_Patterns.F90:47-85) on the GPU: row v, a vertex of the
+ * coordinate mesh, holds the P2 nodes of the elements containing v,
+ * ascending; a pattern-only handle with one row per vertex.
+ * fl_dev_assemble_divergence_p2p1 assembles the element terms of
+ * assemble_divergence_matrix_cg (assemble/Divergence_Matrix_CG.F90:67-375)
+ * for that pair into the three blocks of ct_m (shape_dshape, or
+ * -dshape_shape by parts), each row summed in ascending element order;
+ * quad_degree is the rule's degree (4 for P2).  The by-parts surface terms
+ * are not included.  Device pointers. */
+int fl_gpu_rect_register(fl_mesh mesh, fl_mesh* out);
+int fl_dev_assemble_divergence_p2p1(fl_mesh mesh, fl_mesh pattern, int32_t integrate_by_parts,
+                                    int32_t quad_degree, double* const ct_val[3], void* stream);
 
 /* compute_lumped_mass (femtools/FEFields.F90:161-214) of a P1 mesh with unit
  * density, as get_lumped_mass (femtools/State_Fields.F90:124-152) caches it. */

@@ -267,3 +267,39 @@ def test_every_row_dirichlet(O):
         ox, its, reason, _ = oracle_solve(O, m, val, rhs, ina, ksp=ksp)
         assert np.array_equal(ox, g)
         assert rep["iterations"] == its == 0
+
+
+def test_projected_guess_is_the_a_norm_minimiser(O):
+    """fl_dev_projected_guess against a dense restatement of the projection
+    method on the ghost-reduced system, and the minimising property: the
+    guess's A-norm error is below each basis vector's."""
+    import torch
+    m, X, val, rhs, ina = poisson(O, 7)
+    xd = direct(m, val, rhs, ina)
+    rng = np.random.default_rng(5)
+    basis = [xd * (1 + 0.1 * rng.standard_normal(m.N)), np.sin(3 * X[:, 0]) * xd, rng.standard_normal(m.N),
+             xd * (1 + 0.1 * rng.standard_normal(m.N))]
+    dev = [torch.from_numpy(b).cuda() for b in basis]
+    x0, a = ft.projected_guess(m, torch.from_numpy(val).cuda(), torch.from_numpy(rhs).cuda(), dev,
+                               inactive=torch.from_numpy(ina).cuda())
+    x0 = x0.cpu().numpy()
+    s = m.sparsity()
+    A = sp.csr_matrix((val, s.colm, s.findrm), shape=(m.N, m.N))
+    act, gh = np.nonzero(ina == 0)[0], np.nonzero(ina)[0]
+    Aa = A[act][:, act]
+    b = rhs[act] - A[act][:, gh] @ rhs[gh]
+    V = np.stack([v[act] for v in basis], axis=1)
+    ad = np.linalg.solve(V.T @ (Aa @ V), V.T @ b)
+    assert np.abs(a - ad).max() <= 1e-8 * np.abs(ad).max()
+    assert np.abs(x0[act] - V @ ad).max() <= 1e-10 * np.abs(xd).max()
+    assert np.array_equal(x0[gh], rhs[gh])
+
+    def anorm(v):
+        e = v[act] - xd[act]
+        return float(np.sqrt(e @ (Aa @ e)))
+    assert all(anorm(x0) <= anorm(v) for v in basis)
+    # a vector in the span of earlier ones is dropped, the result unchanged
+    x1, a1 = ft.projected_guess(m, torch.from_numpy(val).cuda(), torch.from_numpy(rhs).cuda(),
+                                dev + [dev[0] * 2.0], inactive=torch.from_numpy(ina).cuda())
+    assert a1[-1] == 0.0
+    assert np.abs(x1.cpu().numpy() - x0).max() <= 1e-12 * np.abs(xd).max()
