@@ -773,7 +773,7 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
                 basis = [ps[t - j] for j in range(1, nproj + 1)]
                 if guess == "learned_projection":
                     net.predict(ps[t - 1], ps[t - 2], bs[t], out=pred, stream=stream)
-                    basis = [pred] + basis[:-1]
+                    basis = basis + [pred]
                 ft.projected_guess(m, val, rhs, basis, inactive=ina, out=x, stream=stream)
             if prec == "amg":
                 rep = amg.solve(x, rhs, ft.solver_options(ksp="cg", rtol=1e-10, max_its=50000), stream=stream)
@@ -807,9 +807,8 @@ def bench_learned(args, dev, stream, n, epochs, nsteps=240, ntrain=200):
         / summary["mixed_learned"]["mean_ms"],
         "speedup_fp64_learned_vs_fp64_previous": summary["fp64_previous"]["mean_ms"]
         / summary["fp64_learned"]["mean_ms"],
-        "projection": f"Fischer's projection onto the {nproj} previous solutions (learned_projection: the "
-                      f"network's prediction and the {nproj - 1} previous solutions), A-norm optimal, "
-                      "timed with the guess",
+        "projection": f"Fischer's projection onto the {nproj} previous solutions (learned_projection: the same "
+                      f"and the network's prediction), A-norm optimal, timed with the guess",
     }
 
 

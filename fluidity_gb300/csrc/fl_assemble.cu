@@ -433,6 +433,26 @@ __device__ __forceinline__ void p1_df_load(const DfArgs& A, int e, P1In& in) {
   }
 }
 
+// The same loads from connectivity already in registers (xv: vertices, tv:
+// field nodes), for the element pass that fetches the next element's
+// connectivity one iteration ahead.
+template <bool SRC, bool TF>
+__device__ __forceinline__ void p1_df_load_from(const DfArgs& A, int4 xv, int4 tv, P1In& in) {
+  const int vi[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) in.x[i][a] = __ldg(A.X + (uint32_t)(3 * vi[i] + a));
+  if (SRC || TF) {
+    const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (SRC) in.f[i] = __ldg(A.f + tn[i]);
+      if (TF) in.t[i] = __ldg(A.t + tn[i]);
+    }
+  }
+}
+
 template <bool MASS, bool SRC, bool TF, bool ANISO>
 __device__ __forceinline__ void p1_df_element(const DfArgs& A, const P1In& in, float4* rec) {
   constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
@@ -537,12 +557,24 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
   constexpr int NREC = 4 * SL;      // float4 per element record
   float4* stage = stage_all + (threadIdx.x >> 5) * (32 * NREC);
-  for (int base = A.p0 + blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E;
-       base += gridDim.x * blockDim.x) {
+  const int stride = gridDim.x * blockDim.x;
+  // the connectivity of the element after this one is fetched while this one
+  // is computed (one dependent load round trip fewer per element)
+  int4 xv = make_int4(0, 0, 0, 0), tv = xv;
+  auto fetch = [&](int e) {
+    const int ee = A.perm ? __ldg(A.perm + e) : e;
+    xv = __ldg(reinterpret_cast<const int4*>(A.xnd) + ee);
+    if (SRC || TF) tv = __ldg(reinterpret_cast<const int4*>(A.nd) + ee);
+  };
+  int base = A.p0 + blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  if (base + lane < A.E) fetch(base + lane);
+  for (; base < A.E; base += stride) {
     const int e = base + lane;
+    const int4 cxv = xv, ctv = tv;
+    if (base + stride + lane < A.E) fetch(base + stride + lane);
     if (e < A.E) {
       P1In in;
-      p1_df_load<SRC, TF>(A, A.perm ? __ldg(A.perm + e) : e, in);
+      p1_df_load_from<SRC, TF>(A, cxv, ctv, in);
       p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * NREC);
     }
     __syncwarp();
@@ -790,16 +822,27 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
   df r = {0.0f, 0.0f};
   const int ib = live ? __ldg(P.ne_ptr + row) : 0, ie = live ? __ldg(P.ne_ptr + row + 1) : 0;
   // incidences in groups of four: all index and record loads of a group are
-  // issued before any accumulation (memory-level parallelism); the adds run
-  // in the group's order, so the colour order of the sum is kept
+  // issued before any accumulation (memory-level parallelism), and the next
+  // group's indices are loaded while this group's records are in flight
+  // (software pipelining: one dependent round trip per group instead of
+  // two); the adds run in the group's order, so the colour order of the sum
+  // is kept
+  const int32_t* incl = FUSED ? P.ne_rec : P.ne_col;
+  int ninc[4];
+  uint32_t npw[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const bool ok = ib + u < ie;
+    ninc[u] = ok ? __ldg(incl + ib + u) : 0;
+    npw[u] = ok ? __ldg(P.ne_pos + ib + u) : 0u;
+  }
   for (int q0 = ib; q0 < ie; q0 += 4) {
     int inc[4];
     uint32_t pw[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const bool ok = q0 + u < ie;
-      inc[u] = ok ? __ldg((FUSED ? P.ne_rec : P.ne_col) + q0 + u) : 0;
-      pw[u] = ok ? __ldg(P.ne_pos + q0 + u) : 0u;
+      inc[u] = ninc[u];
+      pw[u] = npw[u];
     }
     float4 q[4][SL];
 #pragma unroll
@@ -811,6 +854,12 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
         if (q0 + u < ie) q[u][k] = FUSED ? __ldca(rec + ri + k) : __ldg(rec + ri + k);
         else q[u][k] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool ok = q0 + 4 + u < ie;
+      ninc[u] = ok ? __ldg(incl + q0 + 4 + u) : 0;
+      npw[u] = ok ? __ldg(P.ne_pos + q0 + 4 + u) : 0u;
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
