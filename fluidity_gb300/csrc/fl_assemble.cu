@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
   const int lane = threadIdx.x & 31;
   constexpr int SL = MASS ? 3 : 2;  // float4 per row slice
   constexpr int NREC = 4 * SL;      // float4 per element record
-  float4* stage = stage_all + (threadIdx.x >> 5) * (32 * NREC);
+  float4* stage = stage_all + (threadIdx.x >> 5) * (32 * (NREC + 1));
   const int stride = gridDim.x * blockDim.x;
   // the connectivity of the element after this one is fetched while this one
   // is computed (one dependent load round trip fewer per element)
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
     if (e < A.E) {
       P1In in;
       p1_df_load_from<SRC, TF>(A, cxv, ctv, in);
-      p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * NREC);
+      p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * (NREC + 1));
     }
     __syncwarp();
     float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(256) k_asm_p1_diffusion_df(DfArgs A) {
 #pragma unroll
     for (int k = 0; k < NREC; ++k) {
       const int idx = k * 32 + lane;
-      if (idx < nvalid) out[idx] = stage[idx];
+      if (idx < nvalid) out[idx] = stage[stage_pos<NREC>(k, lane)];
     }
     __syncwarp();
   }
@@ -646,7 +646,7 @@ constexpr int kP2Threads = 128;
 
 __global__ void __launch_bounds__(kP2Threads) k_asm_p2_diffusion_df(DfP2Args A) {
   note_launch();
-  __shared__ float4 stage_all[4][32 * 6];  // one 96-B slice per lane and warp
+  __shared__ float4 stage_all[4][32 * 7];  // one 96-B slice per lane and warp, padded
   extern __shared__ float2 p2_dots[];      // [45][kP2Threads]: the strict upper d_ij
   const int lane = threadIdx.x & 31;
   float4* stage = stage_all[threadIdx.x >> 5];
@@ -745,7 +745,7 @@ __global__ void __launch_bounds__(kP2Threads) k_asm_p2_diffusion_df(DfP2Args A) 
         r = df_dot<10>(mrow, fe);
       }
       if (A.t) r = df_sub(r, tsum);
-      float4* rec = stage + lane * 6;
+      float4* rec = stage + lane * 7;
 #pragma unroll
       for (int k = 0; k < 5; ++k)
         rec[k] = make_float4(K[2 * k].hi, K[2 * k].lo, K[2 * k + 1].hi, K[2 * k + 1].lo);
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(kP2Threads) k_asm_p2_diffusion_df(DfP2Args A) 
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         const int idx = k * 32 + lane;
-        if (idx < nvalid) out[idx] = stage[idx];
+        if (idx < nvalid) out[idx] = stage[stage_pos<6>(k, lane)];
       }
       __syncwarp();
     }
@@ -870,16 +870,25 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
       v[2] = {q[u][1].x, q[u][1].y};
       v[3] = df_neg(df_add(df_add(v[0], v[1]), v[2]));
       if (MASS) v[3] = df_add(v[3], {q[u][SL - 1].x, q[u][SL - 1].y});
+      if (in_smem) {
+        // an element's four nodes are four different columns of the row, so
+        // the four accumulators are read together, then written together
+        // (one shared-memory round trip per incidence instead of four)
+        int pos[4];
+        float2 c[4];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int pos = (pw[u] >> (8 * b)) & 0xffu;
-        if (in_smem) {
-          const float2 c = acc[pos * THREADS + t];
-          const df sum = df_add({c.x, c.y}, v[b]);
-          acc[pos * THREADS + t] = make_float2(sum.hi, sum.lo);
-        } else {
-          P.val[base + pos] += df_to_double(v[b]);
+        for (int b = 0; b < 4; ++b) {
+          pos[b] = ((pw[u] >> (8 * b)) & 0xffu) * THREADS + t;
+          c[b] = acc[pos[b]];
         }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const df sum = df_add({c[b].x, c[b].y}, v[b]);
+          acc[pos[b]] = make_float2(sum.hi, sum.lo);
+        }
+      } else {
+#pragma unroll
+        for (int b = 0; b < 4; ++b) P.val[base + ((pw[u] >> (8 * b)) & 0xffu)] += df_to_double(v[b]);
       }
       r = df_add(r, {q[u][1].z, q[u][1].w});
     }
@@ -969,7 +978,7 @@ __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, 
   constexpr int SL = MASS ? 3 : 2, NREC = 4 * SL;
   __shared__ int s_item;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  float4* stage = fz_smem + w * (32 * NREC);
+  float4* stage = fz_smem + w * (32 * (NREC + 1));
   float2* acc = reinterpret_cast<float2*>(fz_smem);  // [16][kFzItem]
   for (;;) {
     if (t == 0) s_item = atomicAdd(F.ctl, 1);
@@ -984,7 +993,7 @@ __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, 
         if (pp < A.E) {
           P1In in;
           p1_df_load<SRC, TF>(A, __ldg(F.perm + pp), in);
-          p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * NREC);
+          p1_df_element<MASS, SRC, TF, ANISO>(A, in, stage + lane * (NREC + 1));
         }
         __syncwarp();
         float4* out = reinterpret_cast<float4*>(A.em) + (uint32_t)base * NREC;
@@ -992,7 +1001,7 @@ __global__ void __launch_bounds__(kFzItem) k_asm_p1_fused(DfArgs A, PullArgs P, 
 #pragma unroll
         for (int k = 0; k < NREC; ++k) {
           const int idx = k * 32 + lane;
-          if (idx < nvalid) out[idx] = stage[idx];
+          if (idx < nvalid) out[idx] = stage[stage_pos<NREC>(k, lane)];
         }
       }
       __syncthreads();
@@ -1193,7 +1202,7 @@ static int fused_plan(fl_mesh_t* m, cudaStream_t s) {
 template <bool MASS, bool SRC, bool TF, bool ANISO>
 static int launch_fused(fl_mesh_t* m, const DfArgs& D, const PullArgs& P, cudaStream_t s) {
   constexpr int NREC = MASS ? 12 : 8;
-  const size_t smem = std::max((size_t)(kFzItem / 32) * 32 * NREC * sizeof(float4),
+  const size_t smem = std::max((size_t)(kFzItem / 32) * 32 * (NREC + 1) * sizeof(float4),
                                (size_t)16 * kFzItem * sizeof(float2));
   static bool configured = false;
   if (!configured) {
@@ -1564,15 +1573,26 @@ static int p1_df_args(const fl_mesh_t* m, const fl_advdif_params* p, const fl_fi
   return (D.have_mass ? 8 : 0) | (D.have_src ? 4 : 0) | (D.t ? 2 : 0) | D.aniso;
 }
 
-// Record staging of the P1 double-float element pass: 4 or 6 kB per warp.
-static size_t p1_df_stage_bytes(int threads, bool mass) {
-  return (size_t)(threads / 32) * 32 * (mass ? 12 : 8) * sizeof(float4);
+// Record staging of the P1 double-float element pass: 4.5 or 6.5 kB per warp.
+static size_t p1_df_stage_bytes(int threads, int key) {
+  return (size_t)(threads / 32) * 32 * ((key & 8) ? 13 : 9) * sizeof(float4);
+}
+
+template <bool M, bool S, bool T, bool AN>
+static void launch_p1_df_elem(unsigned g, int eb, size_t smem, const DfArgs& D, cudaStream_t s) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_asm_p1_diffusion_df<M, S, T, AN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)p1_df_stage_bytes(256, M ? 8 : 0));
+    configured = true;
+  }
+  k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, smem, s>>>(D);
 }
 
 static void launch_p1_df_elems(int key, unsigned g, int eb, size_t smem, const DfArgs& D, cudaStream_t s) {
   switch (key) {
 #define FL_DF_CASE(K, M, S, T, AN) \
-  case K: k_asm_p1_diffusion_df<M, S, T, AN><<<g, eb, smem, s>>>(D); break;
+  case K: launch_p1_df_elem<M, S, T, AN>(g, eb, smem, D, s); break;
     FL_DF_CASE(0, false, false, false, false) FL_DF_CASE(1, false, false, false, true)
     FL_DF_CASE(2, false, false, true, false) FL_DF_CASE(3, false, false, true, true)
     FL_DF_CASE(4, false, true, false, false) FL_DF_CASE(5, false, true, false, true)
@@ -1689,7 +1709,7 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     DfArgs D{};
     const int key = p1_df_args(m, p, f, em, D);
     const unsigned g = grid_for(m->E, eb, esm);
-    const size_t smem = p1_df_stage_bytes(eb, p->have_mass);
+    const size_t smem = p1_df_stage_bytes(eb, key);
     if (m->tile_rows == 3 && !em_override) {
       // fused element + row pass (same sums, records kept in L2)
       FL_TRY(fused_plan(m, s));
@@ -1797,7 +1817,7 @@ static int assemble_pipelined(fl_mesh_t* m, const fl_advdif_params* p, const fl_
   D.perm = m->fz_perm.p;
   const int eb = m->tile_elem_block, esm = m->tile_elem_per_sm;
   const int tile = m->tile_rows == 3 ? 1 : m->tile_rows;
-  const size_t smem = p1_df_stage_bytes(eb, p->have_mass);
+  const size_t smem = p1_df_stage_bytes(eb, key);
   PullArgs P{m->N, m->E, m->ne_ptr.p, m->ne_col.p, m->fz_rec.p, m->ne_pos.p, m->ndglno.p, m->findrm.p,
              m->colm.p, m->em.p, m->st_val.p, m->st_rhs.p, m->err.p, 0, 0};
   if (m->timing) {

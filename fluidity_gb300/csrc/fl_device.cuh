@@ -38,6 +38,26 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// The records of a warp's 32 elements are staged in shared memory for a
+// coalesced copy-out, lane l's record at stage + l (NREC + 1): with the one
+// float4 of padding, the eight lanes of one shared-memory wavefront (16-B
+// stores) write eight different bank groups (records 128 or 192 B apart
+// would put them all in one or two).  stage_pos maps a position of the
+// warp's contiguous record run (position 32 k + lane, k unrolled) to its
+// padded place, idx + idx / NREC, written so that a lane keeps one or three
+// offset registers and k enters as an immediate: 36 k + lane + lane / 8 for
+// 8-float4 records; for 12- (6-) float4 records every 3 k cover 8 (16)
+// records, 104 (112) padded float4.  The P2 pass stages 6-float4 row slices
+// the same way (lanes 96 B apart would share two bank groups per four), the
+// pressure-stabilisation pass its 8-float4 records.
+template <int NREC>
+__device__ __forceinline__ int stage_pos(int k, int lane) {
+  static_assert(NREC == 6 || NREC == 8 || NREC == 12, "staged records are 6, 8 or 12 float4");
+  if (NREC == 8) return 36 * k + lane + (lane >> 3);
+  const int r = 32 * (k % 3) + lane;
+  return 96 / NREC * (NREC + 1) * (k / 3) + r + (int)((unsigned)r / (unsigned)NREC);
+}
+
 // First error wins; `where` records the element / row that raised it.
 __device__ __forceinline__ void set_err(ErrWord* err, int code, int where) {
   if (atomicCAS(&err->code, 0, code) == 0) err->where = where;

@@ -776,7 +776,7 @@ __global__ void __launch_bounds__(256) k_kmk_elem(KmkArgs A) {
   note_launch();
   extern __shared__ float4 kstage_all[];
   const int lane = threadIdx.x & 31;
-  float4* stage = kstage_all + (threadIdx.x >> 5) * 256;
+  float4* stage = kstage_all + (threadIdx.x >> 5) * (32 * 9);  // padded records
   for (int base = blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < A.E; base += gridDim.x * blockDim.x) {
     const int e = base + lane;
     if (e < A.E) {
@@ -866,7 +866,7 @@ __global__ void __launch_bounds__(256) k_kmk_elem(KmkArgs A) {
       // row 3 as the row pass rebuilds column 3 (an exactly symmetric matrix)
 #pragma unroll
       for (int b = 0; b < 3; ++b) K[3][b] = df_neg(df_add(df_add(K[b][0], K[b][1]), K[b][2]));
-      float4* rec = stage + lane * 8;
+      float4* rec = stage + lane * 9;
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         rec[2 * i] = make_float4(K[i][0].hi, K[i][0].lo, K[i][1].hi, K[i][1].lo);
@@ -879,7 +879,7 @@ __global__ void __launch_bounds__(256) k_kmk_elem(KmkArgs A) {
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       const int idx = k * 32 + lane;
-      if (idx < nvalid) out[idx] = stage[idx];
+      if (idx < nvalid) out[idx] = stage[stage_pos<8>(k, lane)];
     }
     __syncwarp();
   }
@@ -1313,7 +1313,7 @@ extern "C" int fl_dev_assemble_kmk(fl_mesh m, fl_mesh prod, double theta_pg, con
   }
   FL_TRY(m->em.reserve((size_t)m->E * 16));  // 128 B per element
   KmkArgs K{m->E, m->xndglno.p, m->coords.p, reinterpret_cast<float4*>(m->em.p)};
-  k_kmk_elem<<<grid_for(m->E, 256, 8), 256, 8 * 256 * sizeof(float4), s>>>(K);
+  k_kmk_elem<<<grid_for(m->E, 256, 8), 256, 8 * 32 * 9 * sizeof(float4), s>>>(K);
   FL_TRY_CUDA(cudaGetLastError());
   FL_TRY(m->st_rhs.reserve((size_t)m->N));
   FL_TRY(rows_p1_df(m, m->em.p, kt, m->st_rhs.p, s));
