@@ -849,10 +849,16 @@ __device__ __forceinline__ void p1_df_row(const PullArgs& P, int row, bool live,
     for (int u = 0; u < 4; ++u) {
       const uint32_t slice = FUSED ? (uint32_t)inc[u] : (uint32_t)(((inc[u] >> 4) << 2) | (inc[u] & 15));
       const uint32_t ri = (uint32_t)SL * slice;
+      if (!MASS && !FUSED) {
+        // a 32-B slice (32-B aligned) in one 256-bit load
+        if (q0 + u < ie) ldg256(rec + ri, q[u][0], q[u][1]);
+        else q[u][0] = q[u][1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
 #pragma unroll
-      for (int k = 0; k < SL; ++k) {
-        if (q0 + u < ie) q[u][k] = FUSED ? __ldca(rec + ri + k) : __ldg(rec + ri + k);
-        else q[u][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < SL; ++k) {
+          if (q0 + u < ie) q[u][k] = FUSED ? __ldca(rec + ri + k) : __ldg(rec + ri + k);
+          else q[u][k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
       }
     }
 #pragma unroll

@@ -58,6 +58,14 @@ __device__ __forceinline__ int stage_pos(int k, int lane) {
   return 96 / NREC * (NREC + 1) * (k / 3) + r + (int)((unsigned)r / (unsigned)NREC);
 }
 
+// 32 bytes from a 32-byte aligned global address that no thread writes
+// during the kernel, in one 256-bit load (ld.global.nc.v8, sm_100 and later).
+__device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 // First error wins; `where` records the element / row that raised it.
 __device__ __forceinline__ void set_err(ErrWord* err, int code, int where) {
   if (atomicCAS(&err->code, 0, code) == 0) err->where = where;
