@@ -2248,40 +2248,6 @@ struct FaceAsmArgs {
   ErrWord* err;
 };
 
-// Triangle rules of degree 1..4 (Quadrature.F90 construct_tri_quadratures,
-// Str71 and the degree-4 six-point rule): (a, a, b) generators expanded in
-// the order of tri_permutations(5), or the centroid.
-static int tri_rule(int degree, double l[6][3], double w[6]) {
-  int n = 0;
-  auto cen = [&](double a, double wt) {
-    l[n][0] = l[n][1] = l[n][2] = a;
-    w[n++] = wt;
-  };
-  auto gen = [&](double a, double wt) {
-    const double b = 1.0 - 2.0 * a;
-    const double c[2] = {a, b};
-    const int perm[3][3] = {{1, 1, 2}, {1, 2, 1}, {2, 1, 1}};
-    for (int k = 0; k < 3; ++k) {
-      for (int j = 0; j < 3; ++j) l[n][j] = c[perm[k][j] - 1];
-      w[n++] = wt;
-    }
-  };
-  switch (degree) {
-    case 1: cen(0.333333333333333333333333333333333, 0.5); break;
-    case 2: gen(0.166666666666666666666666666666666, 0.166666666666666666666666666666666); break;
-    case 3:
-      cen(0.333333333333333333333333333333333, -0.28125);
-      gen(0.2, 0.260416666666666666666666666666666);
-      break;
-    case 4:
-      gen(0.0915762135097707434595714634022015, 0.0549758718276609338191631624501052);
-      gen(0.445948490915964886318329253883051, 0.111690794839005732847503504216561);
-      break;
-    default: return 0;
-  }
-  return n;
-}
-
 // Lagrange functions of the face (P1: barycentrics; P2: vertex L(2L-1),
 // edge 4 L_a L_b, in the triangle's local order).
 __device__ __forceinline__ void face_shape(int floc, const double l[3], double* n) {

@@ -374,6 +374,105 @@ __global__ void k_div_faces(FaceArgs F) {
   }
 }
 
+// Surface terms of the integrated-by-parts Taylor-Hood divergence (the same
+// loop, Divergence_Matrix_CG.F90:312-366, with P1 pressure test functions and
+// P2 velocity field functions on each face): one thread per pressure row,
+// its faces in ascending order.  The face integrals are detJ T(i, j) with
+// T(i, j) = sum_g w_g L_i N_j over the triangle rule (P1 x P2, computed on
+// the host), normal = facet_normal as in k_div_faces.
+struct ThFaceArgs {
+  FaceArgs F;          // faces = pressure (vertex) nodes; findrm / colm = the rectangular pattern
+  const int32_t* vfaces;  // six P2 velocity nodes per face
+  double T[3][6];
+};
+
+__global__ void k_div_faces_th(ThFaceArgs A) {
+  note_launch();
+  const FaceArgs& F = A.F;
+  double* ct[3] = {F.ct0, F.ct1, F.ct2};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < F.N; i += gridDim.x * blockDim.x) {
+    const int qb = F.fptr[i], qe = F.fptr[i + 1];
+    for (int q = qb; q < qe; ++q) {
+      const int f = F.flist[q];
+      int ty[3];
+      bool skip = false;
+      for (int d = 0; d < 3; ++d) {
+        ty[d] = F.bc_type ? F.bc_type[3 * f + d] : 0;
+        skip = skip || ty[d] == 2 || ty[d] == 3 || ty[d] == 4;
+      }
+      if (skip) continue;
+      int fn[3], li = -1;
+      for (int j = 0; j < 3; ++j) {
+        fn[j] = F.faces[3 * f + j] - F.base;
+        if (fn[j] == i) li = j;
+      }
+      const int el = F.face_ele[f] - F.base;
+      if (li < 0 || el < 0 || el >= F.E) {
+        set_err(F.err, FL_ERR_ARG, f);
+        continue;
+      }
+      double Xf[3][3], cf[3] = {0.0, 0.0, 0.0}, ce[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < 3; ++j)
+        for (int a = 0; a < 3; ++a) {
+          Xf[j][a] = F.X[3 * fn[j] + a];
+          cf[a] += Xf[j][a];
+        }
+      for (int j = 0; j < 4; ++j) {
+        const int v = F.xnd[4 * el + j];
+        for (int a = 0; a < 3; ++a) ce[a] += F.X[3 * v + a];
+      }
+      double J0[3], J1[3], ow[3];
+      for (int a = 0; a < 3; ++a) {
+        J0[a] = Xf[0][a] - Xf[2][a];
+        J1[a] = Xf[1][a] - Xf[2][a];
+        ow[a] = cf[a] / 3.0 - ce[a] / 4.0;
+      }
+      double n[3] = {J0[1] * J1[2] - J0[2] * J1[1], J0[2] * J1[0] - J0[0] * J1[2], J0[0] * J1[1] - J0[1] * J1[0]};
+      const double detJ = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      const double o = n[0] * ow[0] + n[1] * ow[1] + n[2] * ow[2];
+      for (int a = 0; a < 3; ++a) n[a] *= o;
+      const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      for (int a = 0; a < 3; ++a) n[a] /= len;
+      double mrow[6];
+      for (int j = 0; j < 6; ++j) mrow[j] = detJ * A.T[li][j];
+      const double* bv = F.bc_val ? F.bc_val + 18 * (int64_t)f : nullptr;
+      if (ty[0] == 5 && F.ct_rhs) {
+        if (!bv) {
+          set_err(F.err, FL_ERR_ARG, f);
+          continue;
+        }
+        double r = 0.0;
+        for (int j = 0; j < 6; ++j) r += mrow[j] * bv[3 * j];
+        F.ct_rhs[i] -= r;
+        continue;
+      }
+      int vn[6];
+      for (int j = 0; j < 6; ++j) vn[j] = A.vfaces[6 * f + j] - F.base;
+      const int rb = F.findrm[i], re = F.findrm[i + 1];
+      for (int d = 0; d < 3; ++d) {
+        if (ty[d] == 1 && F.ct_rhs) {
+          if (!bv) {
+            set_err(F.err, FL_ERR_ARG, f);
+            continue;
+          }
+          double r = 0.0;
+          for (int j = 0; j < 6; ++j) r += n[d] * mrow[j] * bv[3 * j + d];
+          F.ct_rhs[i] -= r;
+        } else {
+          for (int j = 0; j < 6; ++j) {
+            const int p = csr_find(F.colm, rb, re, vn[j]);
+            if (p < 0) {
+              set_err(F.err, FL_ERR_OUTSIDE_PATTERN, i);
+              continue;
+            }
+            ct[d][p] += n[d] * mrow[j];
+          }
+        }
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------- pattern products --
 // tpos[p] for the entry p = (k, j) of row k: the position of (j, k) in row j.
 __global__ void k_tpos(int32_t N, const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
@@ -1224,6 +1323,40 @@ extern "C" int fl_dev_assemble_divergence_cg(fl_mesh m, const fl_divergence_para
     FL_TRY_CUDA(cudaGetLastError());
   }
   return check_err(m->err.p, s, "divergence assembly");
+}
+
+extern "C" int fl_dev_assemble_divergence_p2p1_faces(fl_mesh m, fl_mesh rect, const fl_divergence_params* p,
+                                                    const int32_t* vfaces, int32_t quad_degree,
+                                                    double* const ct_val[3], double* ct_rhs, void* stream) {
+  FL_CHECK_ARG(m && rect && p && ct_val && ct_val[0] && ct_val[1] && ct_val[2], "null argument");
+  FL_CHECK_ARG(m->loc == 10 && m->E > 0, "a P2 (velocity) mesh handle");
+  FL_CHECK_ARG(rect->so_parent == m && rect->N == m->Nx, "the rectangular pattern of this mesh (fl_gpu_rect_register)");
+  FL_CHECK_ARG(p->index_base == 0 || p->index_base == 1, "index_base");
+  if (p->nfaces <= 0) return FL_OK;
+  FL_CHECK_ARG(p->faces && p->face_ele && vfaces, "faces, face_ele and vfaces");
+  ThFaceArgs A{};
+  double l[6][3], w[6];
+  const int ngi = tri_rule(quad_degree, l, w);
+  FL_CHECK_ARG(ngi > 0, "quadrature degree 1..4");
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 6; ++j) A.T[i][j] = 0.0;
+  for (int g = 0; g < ngi; ++g) {
+    double Lp[3], Nu[6];
+    tri_lagrange(3, l[g], Lp);
+    tri_lagrange(6, l[g], Nu);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 6; ++j) A.T[i][j] += w[g] * (Lp[i] * Nu[j]);
+  }
+  cudaStream_t s = pick(m, stream);
+  const int N = rect->N;
+  FL_TRY(node_face_lists(rect, p->nfaces, 3, p->faces, p->index_base, s));
+  A.F = FaceArgs{N, p->index_base, rect->face_ptr.p, rect->face_list.p, p->faces, p->face_ele, p->bc_type,
+                 p->bc_val, m->xndglno.p, m->coords.p, rect->findrm.p, rect->colm.p, ct_val[0], ct_val[1],
+                 ct_val[2], ct_rhs, m->E, rect->err.p};
+  A.vfaces = vfaces;
+  k_div_faces_th<<<grid_for(N, 128), 128, 0, s>>>(A);
+  FL_TRY_CUDA(cudaGetLastError());
+  return check_err(rect->err.p, s, "Taylor-Hood divergence surface terms");
 }
 
 extern "C" int fl_dev_lumped_mass(fl_mesh m, double* lumped_mass, void* stream) {

@@ -132,4 +132,56 @@ inline void tet_shape(int degree, const TetQuad& q, TetShape& s) {
     }
 }
 
+// Triangle rules of degree 1..4 (Quadrature.F90 construct_tri_quadratures,
+// Str71 and the degree-4 six-point rule): (a, a, b) generators expanded in
+// the order of tri_permutations(5), or the centroid.
+inline int tri_rule(int degree, double l[6][3], double w[6]) {
+  int n = 0;
+  auto cen = [&](double a, double wt) {
+    l[n][0] = l[n][1] = l[n][2] = a;
+    w[n++] = wt;
+  };
+  auto gen = [&](double a, double wt) {
+    const double b = 1.0 - 2.0 * a;
+    const double c[2] = {a, b};
+    const int perm[3][3] = {{1, 1, 2}, {1, 2, 1}, {2, 1, 1}};
+    for (int k = 0; k < 3; ++k) {
+      for (int j = 0; j < 3; ++j) l[n][j] = c[perm[k][j] - 1];
+      w[n++] = wt;
+    }
+  };
+  switch (degree) {
+    case 1: cen(0.333333333333333333333333333333333, 0.5); break;
+    case 2: gen(0.166666666666666666666666666666666, 0.166666666666666666666666666666666); break;
+    case 3:
+      cen(0.333333333333333333333333333333333, -0.28125);
+      gen(0.2, 0.260416666666666666666666666666666);
+      break;
+    case 4:
+      gen(0.0915762135097707434595714634022015, 0.0549758718276609338191631624501052);
+      gen(0.445948490915964886318329253883051, 0.111690794839005732847503504216561);
+      break;
+    default: return 0;
+  }
+  return n;
+}
+
+// Lagrange functions of a face triangle at barycentric point l, host side
+// (P1: the barycentrics; P2: vertex L(2L-1), edge 4 L_a L_b in the local
+// order vertex 1, edge 12, vertex 2, edge 13, edge 23, vertex 3).
+inline void tri_lagrange(int floc, const double l[3], double* n) {
+  if (floc == 3) {
+    n[0] = l[0];
+    n[1] = l[1];
+    n[2] = l[2];
+    return;
+  }
+  n[0] = l[0] * (2.0 * l[0] - 1.0);
+  n[1] = (2.0 * l[0]) * (2.0 * l[1]);
+  n[2] = l[1] * (2.0 * l[1] - 1.0);
+  n[3] = (2.0 * l[0]) * (2.0 * l[2]);
+  n[4] = (2.0 * l[1]) * (2.0 * l[2]);
+  n[5] = l[2] * (2.0 * l[2] - 1.0);
+}
+
 }  // namespace fl

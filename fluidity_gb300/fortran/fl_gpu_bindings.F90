@@ -67,7 +67,7 @@ module fl_gpu_bindings
             fl_dev_mult_div_invscalar_div_T, fl_dev_assemble_kmk, fl_dev_masslumped_poisson_rhs, &
             fl_dev_correct_masslumped_velocity, fl_dev_csr_addto, fl_kernel_launch_count, &
             fl_set_kernel_timing, fl_last_assembly_kernel_ms, fl_set_wait_test, fl_dev_projected_guess, &
-            fl_gpu_rect_register, fl_dev_assemble_divergence_p2p1
+            fl_gpu_rect_register, fl_dev_assemble_divergence_p2p1, fl_dev_assemble_divergence_p2p1_faces
   public :: gpu_check, gpu_mesh_handle, gpu_advdif_cg_supported, gpu_assemble_advection_diffusion_cg, &
             gpu_petsc_solve_supported, gpu_petsc_solve_scalar, gpu_solve_field_equation_cg
 
@@ -495,6 +495,18 @@ module fl_gpu_bindings
        type(c_ptr), intent(in) :: ct_val(3)
        integer(c_int) :: st
      end function fl_dev_assemble_divergence_p2p1
+
+     ! its by-parts surface loop: params%faces = pressure (vertex) face nodes,
+     ! vfaces(6, nfaces) = the velocity face nodes, bc_val(3, 6, nfaces)
+     function fl_dev_assemble_divergence_p2p1_faces(mesh, pattern, params, vfaces, quad_degree, ct_val, &
+          ct_rhs, stream) bind(c, name="fl_dev_assemble_divergence_p2p1_faces") result(st)
+       import :: c_int, c_ptr, c_int32_t, fl_divergence_params
+       type(c_ptr), value :: mesh, pattern, vfaces, ct_rhs, stream
+       type(fl_divergence_params), intent(in) :: params
+       integer(c_int32_t), value :: quad_degree
+       type(c_ptr), intent(in) :: ct_val(3)
+       integer(c_int) :: st
+     end function fl_dev_assemble_divergence_p2p1_faces
 
      function fl_dev_lumped_mass(mesh, lumped_mass, stream) bind(c, name="fl_dev_lumped_mass") result(st)
        import :: c_int, c_ptr

@@ -107,6 +107,37 @@ def assemble_divergence_matrix_p2p1(mesh: ft.Mesh, pattern: TaylorHoodPattern, *
     return ct
 
 
+def assemble_divergence_faces_p2p1(mesh: ft.Mesh, pattern: TaylorHoodPattern, ct, *, faces, vfaces, face_ele,
+                                   bc_type=None, bc_val=None, ct_rhs=None, quad_degree=4, index_base=0,
+                                   stream=None):
+    """The by-parts surface terms of C^T for the Taylor-Hood pair, added to ct
+    (3, nnz) and subtracted from ct_rhs (pressure nodes, or None): faces (nf, 3)
+    pressure (vertex) nodes, vfaces (nf, 6) velocity nodes in the P2
+    triangle's order, face_ele (nf,), bc_type (nf, 3), bc_val (nf, 6, 3)."""
+    torch = _torch()
+
+    def dev(a, dt):
+        return _dev(np.asarray(a, dtype=np.int32 if dt == torch.int32 else np.float64)
+                    if isinstance(a, np.ndarray) else a, dt)
+
+    fa, va, fe = dev(faces, torch.int32), dev(vfaces, torch.int32), dev(face_ele, torch.int32)
+    ty = dev(bc_type, torch.int32) if bc_type is not None else None
+    bv = dev(bc_val, torch.float64) if bc_val is not None else None
+    P = DivergenceParams()
+    P.integrate_by_parts = 1
+    P.index_base = int(index_base)
+    P.nfaces = int(fa.shape[0])
+    P.faces, P.face_ele = fa.data_ptr(), fe.data_ptr()
+    P.bc_type = ty.data_ptr() if ty is not None else None
+    P.bc_val = bv.data_ptr() if bv is not None else None
+    check(_lib.load().fl_dev_assemble_divergence_p2p1_faces(
+        mesh.handle, pattern.handle, C.byref(P), va.data_ptr(), int(quad_degree), _ptrs([ct[0], ct[1], ct[2]]),
+        ct_rhs.data_ptr() if ct_rhs is not None else None, ft._stream_ptr(stream)),
+        "fl_dev_assemble_divergence_p2p1_faces")
+    del fa, va, fe, ty, bv
+    return ct
+
+
 def assemble_divergence_matrix_cg(mesh: ft.Mesh, *, integrate_by_parts=False, faces=None, face_ele=None,
                                   bc_type=None, bc_val=None, ct=None, ct_rhs=None, div_mass_lumped=None,
                                   grad_mass_lumped=None, stream=None):

@@ -519,10 +519,25 @@ int fl_dev_assemble_divergence_cg(fl_mesh mesh, const fl_divergence_params* para
  * for that pair into the three blocks of ct_m (shape_dshape, or
  * -dshape_shape by parts), each row summed in ascending element order;
  * quad_degree is the rule's degree (4 for P2).  The by-parts surface terms
- * are not included.  Device pointers. */
+ * are fl_dev_assemble_divergence_p2p1_faces.  Device pointers. */
 int fl_gpu_rect_register(fl_mesh mesh, fl_mesh* out);
 int fl_dev_assemble_divergence_p2p1(fl_mesh mesh, fl_mesh pattern, int32_t integrate_by_parts,
                                     int32_t quad_degree, double* const ct_val[3], void* stream);
+
+/* The by-parts surface loop of assemble_divergence_matrix_cg
+ * (assemble/Divergence_Matrix_CG.F90:312-366) for the same Taylor-Hood pair:
+ * params->faces(3, nfaces) are the pressure (vertex) nodes of each surface
+ * triangle, vfaces(6, nfaces) its P2 velocity nodes (face_global_nodes of the
+ * velocity mesh in the triangle's local order: vertex 1, edge 12, vertex 2,
+ * edge 13, edge 23, vertex 3), face_ele and bc_type as in
+ * fl_divergence_params, and bc_val(3, 6, nfaces) the velocity bc per velocity
+ * face node (types 1 and 5 only).  Adds into ct_val (the pattern's nnz each)
+ * and subtracts from ct_rhs (pressure nodes, as the caller initialised it;
+ * may be null), each pressure row's faces in ascending order; quad_degree
+ * selects the triangle rule.  Device pointers. */
+int fl_dev_assemble_divergence_p2p1_faces(fl_mesh mesh, fl_mesh pattern, const fl_divergence_params* params,
+                                          const int32_t* vfaces, int32_t quad_degree, double* const ct_val[3],
+                                          double* ct_rhs, void* stream);
 
 /* compute_lumped_mass (femtools/FEFields.F90:161-214) of a P1 mesh with unit
  * density, as get_lumped_mass (femtools/State_Fields.F90:124-152) caches it. */

@@ -1738,6 +1738,106 @@ int orc_assemble_divergence_p2p1(int E, const int* ndglno_p, const int* ndglno_u
   return ORC_OK;
 }
 
+// The by-parts surface loop of assemble_divergence_matrix_cg (assemble/
+// Divergence_Matrix_CG.F90:312-366) for P1 pressure (test) and P2 velocity
+// (field) faces: faces whose bc types include 2, 3 or 4 are skipped; type 5
+// in dimension 1 (prescribed normal flow) subtracts shape_rhs(N_p, detwei *
+// g) from ct_rhs, g the first component of the velocity bc interpolated with
+// the P2 face functions; otherwise ele_mat_bdy = shape_shape_vector(N_p, N_u,
+// detwei, normal) (FETools.F90:228) goes, per dimension, into ct_rhs against
+// the weak-Dirichlet values (type 1) or into ct_m.  Face transform and
+// normal as in orc_assemble_divergence_p1; the triangle rule of quad_degree.
+// pfaces: 3 pressure (vertex) nodes per face; ufaces: the 6 velocity nodes
+// in the P2 triangle's local order; bc_type [face][dim]; bc_val [face][velocity
+// face node][dim].  Adds to ct (the three blocks over the rectangular
+// pattern) and ct_rhs (may be null).
+int orc_assemble_divergence_p2p1_faces(int nf, const int* pfaces, const int* ufaces, const int* face_ele,
+                                       const int* ndglno_x, const double* coords, int Np, const int64_t* findrm,
+                                       const int* colm, int quad_degree, const int* bc_type,
+                                       const double* bc_val, double* ct, double* ct_rhs) {
+  TriRule t;
+  if (!tri_rule(quad_degree, t)) return ORC_ERR_ARG;
+  double Np_[6][3], Nu[6][6];  // [gi][node]
+  for (int gi = 0; gi < t.ngi; ++gi) {
+    tri_shape(1, t.l[gi], Np_[gi]);
+    tri_shape(2, t.l[gi], Nu[gi]);
+  }
+  const int64_t nnz = findrm[Np] - findrm[0];
+  for (int f = 0; f < nf; ++f) {
+    const int* ty = bc_type + 3 * (int64_t)f;
+    bool skip = false;
+    for (int d = 0; d < 3; ++d) skip = skip || ty[d] == 2 || ty[d] == 3 || ty[d] == 4;
+    if (skip) continue;
+    const int* fp = pfaces + 3 * (int64_t)f;
+    const int* fu = ufaces + 6 * (int64_t)f;
+    double Xf[3][3], cf[3] = {0, 0, 0}, ce[3] = {0, 0, 0};
+    for (int i = 0; i < 3; ++i)
+      for (int a = 0; a < 3; ++a) {
+        Xf[i][a] = coords[3 * (int64_t)fp[i] + a];
+        cf[a] += Xf[i][a];
+      }
+    const int* en = ndglno_x + 4 * (int64_t)face_ele[f];
+    for (int i = 0; i < 4; ++i)
+      for (int a = 0; a < 3; ++a) ce[a] += coords[3 * (int64_t)en[i] + a];
+    double J[3][2], outward[3];
+    for (int a = 0; a < 3; ++a) {
+      J[a][0] = Xf[0][a] - Xf[2][a];
+      J[a][1] = Xf[1][a] - Xf[2][a];
+      outward[a] = cf[a] / 3.0 - ce[a] / 4.0;
+    }
+    double detJ = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double c = J[cyc3[i + 2]][0] * J[cyc3[i + 1]][1] - J[cyc3[i + 2]][1] * J[cyc3[i + 1]][0];
+      detJ += c * c;
+    }
+    detJ = std::sqrt(detJ);
+    double nrm[3] = {J[1][0] * J[2][1] - J[2][0] * J[1][1], J[2][0] * J[0][1] - J[0][0] * J[2][1],
+                     J[0][0] * J[1][1] - J[1][0] * J[0][1]};
+    const double o = nrm[0] * outward[0] + nrm[1] * outward[1] + nrm[2] * outward[2];
+    for (int a = 0; a < 3; ++a) nrm[a] *= o;
+    const double len = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+    for (int a = 0; a < 3; ++a) nrm[a] /= len;
+    double dw[6];
+    for (int gi = 0; gi < t.ngi; ++gi) dw[gi] = detJ * t.w[gi];
+    const double* bv = bc_val ? bc_val + 18 * (int64_t)f : nullptr;
+    if (ty[0] == 5 && ct_rhs) {
+      if (!bv) return ORC_ERR_ARG;
+      for (int i = 0; i < 3; ++i) {
+        double r = 0.0;
+        for (int gi = 0; gi < t.ngi; ++gi) {
+          double g = 0.0;
+          for (int j = 0; j < 6; ++j) g += bv[3 * j + 0] * Nu[gi][j];
+          r += Np_[gi][i] * (dw[gi] * g);
+        }
+        ct_rhs[fp[i]] -= r;
+      }
+      continue;
+    }
+    for (int d = 0; d < 3; ++d)
+      for (int i = 0; i < 3; ++i) {
+        double mrow[6];
+        for (int j = 0; j < 6; ++j) {
+          double v = 0.0;
+          for (int gi = 0; gi < t.ngi; ++gi) v += nrm[d] * (Np_[gi][i] * Nu[gi][j]) * dw[gi];
+          mrow[j] = v;
+        }
+        if (ty[d] == 1 && ct_rhs) {
+          if (!bv) return ORC_ERR_ARG;
+          double r = 0.0;
+          for (int j = 0; j < 6; ++j) r += mrow[j] * bv[3 * j + d];
+          ct_rhs[fp[i]] -= r;
+        } else {
+          for (int j = 0; j < 6; ++j) {
+            const int64_t p = csr_pos(findrm, colm, fp[i], fu[j]);
+            if (p < 0) return ORC_ERR_OUTSIDE_PATTERN;
+            ct[d * nnz + p] += mrow[j];
+          }
+        }
+      }
+  }
+  return ORC_OK;
+}
+
 // make_sparsity_transpose (femtools/Sparsity_Patterns.F90:87-148) for one
 // mesh: for every node i, every pair (j, k) of the nodes sharing an element
 // with i (row i of the first-order pattern) puts k in row j, ascending

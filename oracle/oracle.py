@@ -363,6 +363,29 @@ def assemble_divergence_p2p1(ndglno_p, ndglno_u, coords, findrm, colm, *, by_par
     return ct
 
 
+def assemble_divergence_p2p1_faces(ct, ct_rhs, *, pfaces, ufaces, face_ele, ndglno_x, coords, findrm, colm,
+                                   bc_type=None, bc_val=None, quad_degree=4):
+    """Adds the by-parts surface terms of assemble_divergence_matrix_cg
+    (Divergence_Matrix_CG.F90:312-366) for P1 pressure / P2 velocity faces to
+    ct (3, nnz) and ct_rhs (pressure nodes, or None)."""
+    pf = np.ascontiguousarray(pfaces, dtype=np.int32)
+    uf = np.ascontiguousarray(ufaces, dtype=np.int32)
+    fe = np.ascontiguousarray(face_ele, dtype=np.int32)
+    nd = np.ascontiguousarray(ndglno_x, dtype=np.int32)
+    X = np.ascontiguousarray(coords, dtype=np.float64)
+    f = np.ascontiguousarray(findrm, dtype=np.int64)
+    c = np.ascontiguousarray(colm, dtype=np.int32)
+    nf = pf.shape[0]
+    ty = np.ascontiguousarray(bc_type if bc_type is not None else np.zeros((nf, 3)), dtype=np.int32)
+    bv = None if bc_val is None else np.ascontiguousarray(bc_val, dtype=np.float64)
+    assert ct.flags.c_contiguous and ct.dtype == np.float64
+    fn = lib().orc_assemble_divergence_p2p1_faces
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int] + [C.c_void_p] * 5 + [C.c_int, C.c_void_p, C.c_void_p, C.c_int] + [C.c_void_p] * 4
+    return fn(nf, _p(pf), _p(uf), _p(fe), _p(nd), _p(X), f.size - 1, _p(f), _p(c), quad_degree, _p(ty),
+              _p(bv) if bv is not None else None, _p(ct), _p(ct_rhs) if ct_rhs is not None else None)
+
+
 def sparsity_secondorder(findrm, colm):
     """(findrm int64, colm int32) of make_sparsity_transpose (Sparsity_Patterns.F90:87-148)."""
     f = np.ascontiguousarray(findrm, dtype=np.int64)

@@ -238,3 +238,52 @@ def test_taylor_hood_divergence_matches_oracle(O, torch, aniso_mesh, which):
         assert torch.equal(again, ct)  # deterministic
     pat.close()
     mesh.close()
+
+
+@pytest.mark.parametrize("which", ["cube4", "unstructured"])
+def test_taylor_hood_surface_terms_match_oracle(O, torch, aniso_mesh, which):
+    """The by-parts surface loop of the Taylor-Hood divergence
+    (fl_dev_assemble_divergence_p2p1_faces) against
+    orc_assemble_divergence_p2p1_faces, with a mix of face types (none, weak
+    Dirichlet, prescribed normal flow, no-normal-flow), 1-based faces too;
+    and by parts with every face's terms equals not by parts.
+    Tolerance: 1e-12 row-scaled on ct, 1e-12 of max |ct_rhs|."""
+    nd, X = M.cube_mesh(4) if which == "cube4" else aniso_mesh
+    nd2, n2 = O.make_global_numbering_p2(nd)
+    mesh = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    pat = PR.TaylorHoodPattern(mesh)
+    f, c = O.make_sparsity_rect(nd, nd2, X.shape[0])
+    N = X.shape[0]
+    faces6, xf, fe = M.boundary_faces_p2(nd, nd2)
+    nf = xf.shape[0]
+    rng = np.random.default_rng(23)
+    ty = np.zeros((nf, 3), np.int32)
+    kind = rng.integers(0, 4, nf)
+    ty[kind == 1] = 1
+    ty[kind == 2, 0] = 5
+    ty[kind == 3, 1] = 2
+    bv = rng.standard_normal((nf, 6, 3))
+    kw = dict(pfaces=xf, ufaces=faces6, face_ele=fe, ndglno_x=nd, coords=X, findrm=f, colm=c)
+    octb = O.assemble_divergence_p2p1(nd, nd2, X, f, c, by_parts=True)
+    orhs = np.zeros(N)
+    assert O.assemble_divergence_p2p1_faces(octb, orhs, bc_type=ty, bc_val=bv, **kw) == 0
+    for base in (0, 1):
+        ct = PR.assemble_divergence_matrix_p2p1(mesh, pat, integrate_by_parts=True)
+        rhs = torch.zeros(N, dtype=torch.float64, device="cuda")
+        PR.assemble_divergence_faces_p2p1(mesh, pat, ct, faces=xf + base, vfaces=faces6 + base, face_ele=fe + base,
+                                          bc_type=ty, bc_val=bv, ct_rhs=rhs, index_base=base)
+        torch.cuda.synchronize()
+        got = ct.cpu().numpy()
+        for d in range(3):
+            assert row_scaled_error(got[d], octb[d], f) <= TOL, (base, d)
+        assert np.abs(rhs.cpu().numpy() - orhs).max() <= TOL * np.abs(orhs).max()
+    # every face type 0: the by-parts matrix equals the direct one
+    ct = PR.assemble_divergence_matrix_p2p1(mesh, pat, integrate_by_parts=True)
+    PR.assemble_divergence_faces_p2p1(mesh, pat, ct, faces=xf, vfaces=faces6, face_ele=fe)
+    direct = PR.assemble_divergence_matrix_p2p1(mesh, pat, integrate_by_parts=False)
+    torch.cuda.synchronize()
+    got, want = ct.cpu().numpy(), direct.cpu().numpy()
+    for d in range(3):
+        assert row_scaled_error(got[d], want[d], f) <= 1e-12
+    pat.close()
+    mesh.close()

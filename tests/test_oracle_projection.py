@@ -236,3 +236,68 @@ def test_taylor_hood_divergence_pins(which, aniso_mesh):
     for d in range(3):
         Cb = sp.csr_matrix((ctb[d], c, f), shape=(N, n2))
         assert np.abs(Cb @ u - C3[d] @ u).max() < 1e-13 * np.abs(C3[d] @ u).max()
+
+
+def _outward_normals(nd, X, xf, fe):
+    a, b, c = X[xf[:, 0]], X[xf[:, 1]], X[xf[:, 2]]
+    n = np.cross(a - c, b - c)
+    out = (a + b + c) / 3.0 - X[nd[fe]].mean(axis=1)
+    n *= np.sign(np.einsum("ij,ij->i", n, out))[:, None]
+    return n / np.linalg.norm(n, axis=1)[:, None]
+
+
+@pytest.mark.parametrize("which", ["cube", "unstructured"])
+def test_taylor_hood_surface_terms_pins(which, aniso_mesh):
+    """The by-parts surface loop for P1 pressure / P2 velocity faces, pinned by
+    integration by parts, which the rules integrate exactly (element integrands
+    of degree <= 2, face integrands of degree <= 3):
+    - by parts with every face's terms (type 0) equals not by parts, entry by
+      entry;
+    - weak-Dirichlet faces (type 1 in every dimension) with the boundary values
+      of a field u move exactly the face terms of u into ct_rhs:
+      C_bp u - ct_rhs = C u;
+    - prescribed normal flow (type 5) with g = u . n at the face nodes does the
+      same through the normal-flow integral;
+    - faces with a type 2, 3 or 4 in any dimension add nothing."""
+    nd, X = M.cube_mesh(3) if which == "cube" else aniso_mesh
+    N = X.shape[0]
+    nd2, n2, f, c, X2 = _taylor_hood(nd, X)
+    faces6, xf, fe = M.boundary_faces_p2(nd, nd2)
+    nf = xf.shape[0]
+    kw = dict(pfaces=xf, ufaces=faces6, face_ele=fe, ndglno_x=nd, coords=X, findrm=f, colm=c)
+    ct = O.assemble_divergence_p2p1(nd, nd2, X, f, c)
+    ctb = O.assemble_divergence_p2p1(nd, nd2, X, f, c, by_parts=True)
+    full = ctb.copy()
+    assert O.assemble_divergence_p2p1_faces(full, None, **kw) == 0
+    for d in range(3):
+        assert np.abs(full[d] - ct[d]).max() <= 1e-13 * np.abs(ct[d]).max()
+    u = np.stack([np.sin(1.0 + X2[:, 0] + 2 * X2[:, 1]), X2[:, 2] ** 2 - X2[:, 0], np.cos(X2[:, 1] * X2[:, 2])],
+                 axis=1)
+    Cu = np.stack([sp.csr_matrix((ct[d], c, f), shape=(N, n2)) @ u[:, d] for d in range(3)]).sum(axis=0)
+    Cbu = np.stack([sp.csr_matrix((ctb[d], c, f), shape=(N, n2)) @ u[:, d] for d in range(3)]).sum(axis=0)
+    tol = 1e-13 * np.abs(Cu).max()
+    # weak Dirichlet everywhere
+    rhs = np.zeros(N)
+    cw = ctb.copy()
+    bv = u[faces6]  # (nf, 6, 3)
+    assert O.assemble_divergence_p2p1_faces(cw, rhs, bc_type=np.ones((nf, 3), np.int32), bc_val=bv, **kw) == 0
+    assert np.array_equal(cw, ctb)
+    assert np.abs(Cbu - rhs - Cu).max() <= tol
+    # prescribed normal flow everywhere
+    nrm = _outward_normals(nd, X, xf, fe)
+    g = np.zeros((nf, 6, 3))
+    g[:, :, 0] = np.einsum("fjd,fd->fj", bv, nrm)
+    rhs5 = np.zeros(N)
+    c5 = ctb.copy()
+    ty5 = np.zeros((nf, 3), np.int32)
+    ty5[:, 0] = 5
+    assert O.assemble_divergence_p2p1_faces(c5, rhs5, bc_type=ty5, bc_val=g, **kw) == 0
+    assert np.array_equal(c5, ctb)
+    assert np.abs(Cbu - rhs5 - Cu).max() <= tol
+    # skipped types
+    for t in (2, 3, 4):
+        ty = np.zeros((nf, 3), np.int32)
+        ty[:, 2] = t
+        cs, rs = ctb.copy(), np.zeros(N)
+        assert O.assemble_divergence_p2p1_faces(cs, rs, bc_type=ty, bc_val=bv, **kw) == 0
+        assert np.array_equal(cs, ctb) and not rs.any()
