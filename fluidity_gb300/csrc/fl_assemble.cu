@@ -646,7 +646,7 @@ constexpr int kP2Threads = 128;
 
 __global__ void __launch_bounds__(kP2Threads) k_asm_p2_diffusion_df(DfP2Args A) {
   note_launch();
-  __shared__ float4 stage_all[4][32 * 7];  // one 96-B slice per lane and warp, padded
+  __shared__ float4 stage_all[kP2Threads / 32][32 * 7];  // one 96-B slice per lane and warp, padded
   extern __shared__ float2 p2_dots[];      // [45][kP2Threads]: the strict upper d_ij
   const int lane = threadIdx.x & 31;
   float4* stage = stage_all[threadIdx.x >> 5];
