@@ -107,7 +107,7 @@ EXPORTS = [
     "fl_dev_masslumped_poisson_rhs", "fl_dev_correct_masslumped_velocity", "fl_dev_csr_addto",
     "fl_dev_assemble_advdif_faces", "fl_gpu_assemble_advdif_faces", "fl_set_wait_test",
     "fl_dev_projected_guess", "fl_gpu_rect_register", "fl_dev_assemble_divergence_p2p1",
-    "fl_dev_assemble_divergence_p2p1_faces",
+    "fl_dev_assemble_divergence_p2p1_faces", "fl_gpu_rect_secondorder_register",
 ]
 
 _P = C.c_void_p
@@ -184,6 +184,7 @@ _SIGNATURES = {
     "fl_gpu_rect_register": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "fl_dev_assemble_divergence_p2p1": (C.c_int, [_P, _P, _I32, _I32, _P, _P]),
     "fl_dev_assemble_divergence_p2p1_faces": (C.c_int, [_P, _P, _P, _P, _I32, _P, _P, _P]),
+    "fl_gpu_rect_secondorder_register": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
 }
 assert sorted(_SIGNATURES) == sorted(EXPORTS)
 

@@ -226,6 +226,11 @@ struct fl_mesh_t {
   cudaStream_t ck_streams[2] = {nullptr, nullptr};
   std::vector<cudaEvent_t> ck_ev;  // per chunk: rows written, fields uploaded, records written
   struct fl_mesh_t* so_parent = nullptr;  // second-order pattern handles: the mesh they square
+  // second-order handles of a rectangular factor C (fl_gpu_rect_secondorder_register): the handle
+  // holding C's pattern, and C's pattern transposed (column -> rows, ascending) with the position
+  // of every transposed entry in C
+  struct fl_mesh_t* a_pat = nullptr;
+  fl::DevBuf<int32_t> tr_ptr, tr_col, tr_pos;
   fl::DevBuf<float2> bt;                  // second-order handles: transposed product operand
   fl::DevBuf<int32_t> pair_off;           // second-order handles: pairs of each first-order entry
   fl::DevBuf<uint8_t> pair_map;           // second-order handles: output slot of every pair

@@ -494,6 +494,8 @@ constexpr int kSoCap = 1024;  // gathered candidates of one row
 // pass 1: the columns, ascending, and the diagonal position.
 __global__ void __launch_bounds__(kSoWarps * 32) k_so_rows(int32_t N, const int32_t* __restrict__ fr,
                                                           const int32_t* __restrict__ cm,
+                                                          const int32_t* __restrict__ tr,
+                                                          const int32_t* __restrict__ tc,
                                                           const int32_t* __restrict__ optr,
                                                           int32_t* __restrict__ cnt, int32_t* __restrict__ ocol,
                                                           int32_t* __restrict__ ocentre, int32_t* maxrow,
@@ -507,9 +509,9 @@ __global__ void __launch_bounds__(kSoWarps * 32) k_so_rows(int32_t N, const int3
     const int qb = fr[row], qe = fr[row + 1];
     for (int q = qb; q < qe; ++q) {
       const int k = cm[q];
-      const int kb = fr[k], len = fr[k + 1] - kb;
+      const int kb = tr[k], len = tr[k + 1] - kb;
       for (int t = lane; t < len; t += 32)
-        if (nc + t < kSoCap) keys[nc + t] = cm[kb + t];
+        if (nc + t < kSoCap) keys[nc + t] = tc[kb + t];
       nc += len;
     }
     if (nc > kSoCap) {
@@ -583,15 +585,16 @@ __global__ void k_bt_gather(int64_t nnz, const int32_t* __restrict__ tpos, const
 // i, one byte per pair at pmap[poff[q] + t] (output rows hold at most kPCap
 // entries).  Built once per second-order pattern.
 __global__ void k_pair_count(int32_t N, const int32_t* __restrict__ fr, const int32_t* __restrict__ cm,
-                             int32_t* __restrict__ cnt) {
+                             const int32_t* __restrict__ tr, int32_t* __restrict__ cnt) {
   note_launch();
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < fr[N]; q += gridDim.x * blockDim.x) {
     const int k = cm[q];
-    cnt[q] = fr[k + 1] - fr[k];
+    cnt[q] = tr[k + 1] - tr[k];
   }
 }
 
 __global__ void k_pair_map(int32_t N, const int32_t* __restrict__ fr, const int32_t* __restrict__ cm,
+                           const int32_t* __restrict__ tr, const int32_t* __restrict__ tc,
                            const int32_t* __restrict__ optr, const int32_t* __restrict__ ocol,
                            const int32_t* __restrict__ poff, uint8_t* __restrict__ pmap, ErrWord* err) {
   note_launch();
@@ -604,9 +607,9 @@ __global__ void k_pair_map(int32_t N, const int32_t* __restrict__ fr, const int3
       continue;
     }
     for (int q = fr[i]; q < fr[i + 1]; ++q) {
-      const int k = cm[q], kb = fr[k], len = fr[k + 1] - kb;
+      const int k = cm[q], kb = tr[k], len = tr[k + 1] - kb;
       for (int t = lane; t < len; t += 32) {
-        const int j = cm[kb + t];
+        const int j = tc[kb + t];
         int lo = 0, hi = L;
         while (lo < hi) {
           const int mid = (lo + hi) >> 1;
@@ -625,6 +628,7 @@ struct RowProdArgs {
   int64_t annz;
   const int32_t* aptr;
   const int32_t* acol;
+  const int32_t* tptr;  // the second factor's rows: aptr for a square symmetric pattern
   const int32_t* optr;
   const int32_t* poff;   // per first-order entry (i, k): start of its pairs in pmap
   const uint8_t* pmap;   // output slot of every pair
@@ -692,8 +696,8 @@ __global__ void __launch_bounds__(kPW * 32, 4) k_rowprod(RowProdArgs P) {
       for (int d = 0; d < NDIM; ++d) c[d] = {0.0f, 0.0f};
       if (qg < qe) {
         const int k = __ldg(P.acol + qg);
-        kb = __ldg(P.aptr + k);
-        klen = __ldg(P.aptr + k + 1) - kb;
+        kb = __ldg(P.tptr + k);
+        klen = __ldg(P.tptr + k + 1) - kb;
         po = __ldg(P.poff + qg);
         if (DIV) {
           double sk = __ldg(P.w + k);
@@ -1201,6 +1205,114 @@ static int th_tensor(int quad_degree, bool by_parts, ThTensor& T) {
 }  // namespace
 }  // namespace fl
 
+namespace fl {
+namespace {
+
+// The product handle h of a first factor with pattern (fr, cm) (N rows, annz
+// entries) and a second factor whose rows, transposed, are (tr, tc): the
+// output pattern (make_sparsity_transpose, femtools/Sparsity_Patterns.F90:
+// 87-148) and the slot map of the row products.
+int build_product(fl_mesh_t* h, int N, const int32_t* fr, const int32_t* cm, int64_t annz, const int32_t* tr,
+                  const int32_t* tc, cudaStream_t s) {
+  h->N = N;
+  DevBuf<int32_t> cnt, mr;
+  FL_TRY(h->err.reserve(1));
+  FL_TRY(cnt.reserve(N + 1));
+  FL_TRY(mr.reserve(1));
+  FL_TRY(h->findrm.reserve(N + 1));
+  FL_TRY(h->centrm.reserve(N));
+  FL_TRY_CUDA(cudaMemsetAsync(h->err.p, 0, sizeof(ErrWord), s));
+  FL_TRY_CUDA(cudaMemsetAsync(mr.p, 0, sizeof(int32_t), s));
+  const unsigned g = (unsigned)std::max(1, std::min((N + kSoWarps - 1) / kSoWarps, num_sms() * 16));
+  k_so_rows<<<g, kSoWarps * 32, 0, s>>>(N, fr, cm, tr, tc, nullptr, cnt.p, nullptr, nullptr, mr.p, h->err.p, 0);
+  FL_TRY(check_err(h->err.p, s, "second-order row with more candidates than the row scratch holds"));
+  FL_TRY(exclusive_scan_i32(cnt.p, h->findrm.p, N, s));
+  int32_t nnz = 0, maxrow = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&nnz, h->findrm.p + N, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(&maxrow, mr.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  h->nnz = nnz;
+  h->max_row = maxrow;
+  FL_TRY(h->colm.reserve((size_t)std::max(nnz, 1)));
+  k_fill_i32<<<grid_for(N, kT), kT, 0, s>>>(h->centrm.p, N, -1);
+  k_so_rows<<<g, kSoWarps * 32, 0, s>>>(N, fr, cm, tr, tc, h->findrm.p, nullptr, h->colm.p, h->centrm.p, mr.p,
+                                        h->err.p, 1);
+  FL_TRY_CUDA(cudaGetLastError());
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  // slot map of the row products
+  DevBuf<int32_t> pc;
+  FL_TRY(pc.reserve((size_t)annz + 1));
+  FL_TRY(h->pair_off.reserve((size_t)annz + 1));
+  k_pair_count<<<grid_for(annz, kT), kT, 0, s>>>(N, fr, cm, tr, pc.p);
+  FL_TRY(exclusive_scan_i32(pc.p, h->pair_off.p, annz, s));
+  int32_t npairs = 0;
+  FL_TRY_CUDA(cudaMemcpyAsync(&npairs, h->pair_off.p + annz, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaStreamSynchronize(s));
+  FL_TRY(h->pair_map.reserve((size_t)std::max(npairs, 1)));
+  k_pair_map<<<(unsigned)std::max(1, std::min((N + 7) / 8, num_sms() * 8)), 256, 0, s>>>(
+      N, fr, cm, tr, tc, h->findrm.p, h->colm.p, h->pair_off.p, h->pair_map.p, h->err.p);
+  return check_err(h->err.p, s, "second-order row longer than the product's shared-memory row");
+}
+
+fl_mesh_t* new_product_handle(int* st) {
+  fl_mesh_t* h = new fl_mesh_t();
+  cudaGetDevice(&h->device);
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    *st = FL_ERR_CUDA;
+  }
+  return h;
+}
+
+// C's pattern transposed: per column k the rows holding it (ascending) and
+// the position of each such entry in C.
+__global__ void k_tr_count(int32_t N, const int32_t* __restrict__ fr, const int32_t* __restrict__ cm, int32_t ncol,
+                           int32_t* __restrict__ cnt, ErrWord* err) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    for (int p = fr[i]; p < fr[i + 1]; ++p) {
+      const int k = cm[p];
+      if (k < 0 || k >= ncol) set_err(err, FL_ERR_ARG, i);
+      else atomicAdd(cnt + k, 1);
+    }
+}
+
+__global__ void k_tr_fill(int32_t N, const int32_t* __restrict__ fr, const int32_t* __restrict__ cm, int32_t ncol,
+                          const int32_t* __restrict__ tptr, int32_t* __restrict__ fill, int32_t* __restrict__ tcol,
+                          int32_t* __restrict__ tpos) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    for (int p = fr[i]; p < fr[i + 1]; ++p) {
+      const int k = cm[p];
+      if (k < 0 || k >= ncol) continue;
+      const int slot = tptr[k] + atomicAdd(fill + k, 1);
+      tcol[slot] = i;
+      tpos[slot] = p;
+    }
+}
+
+__global__ void k_tr_sort(int32_t ncol, const int32_t* __restrict__ tptr, int32_t* __restrict__ tcol,
+                          int32_t* __restrict__ tpos) {
+  note_launch();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ncol; k += gridDim.x * blockDim.x) {
+    const int b = tptr[k], e = tptr[k + 1];
+    for (int a = b + 1; a < e; ++a) {
+      const int x = tcol[a], y = tpos[a];
+      int j = a - 1;
+      while (j >= b && tcol[j] > x) {
+        tcol[j + 1] = tcol[j];
+        tpos[j + 1] = tpos[j];
+        --j;
+      }
+      tcol[j + 1] = x;
+      tpos[j + 1] = y;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace fl
+
 using namespace fl;
 
 // The second-order pattern of a P1 mesh as a pattern-only handle.
@@ -1209,70 +1321,63 @@ extern "C" int fl_gpu_secondorder_register(fl_mesh mesh, fl_mesh* out) {
   FL_CHECK_ARG(mesh->N > 0 && mesh->findrm.p && mesh->colm.p, "the mesh has no pattern");
   cudaStream_t s = mesh->stream;
   FL_TRY(ensure_tpos(mesh, s));
-  fl_mesh_t* h = new fl_mesh_t();
   int st = FL_OK;
-  do {
-    cudaGetDevice(&h->device);
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
-      set_error("cudaStreamCreate failed");
-      st = FL_ERR_CUDA;
-      break;
-    }
-    const int N = mesh->N;
-    h->N = N;
+  fl_mesh_t* h = new_product_handle(&st);
+  if (st == FL_OK) {
     h->so_parent = mesh;
-    DevBuf<int32_t> cnt, mr;
-    if ((st = h->err.reserve(1)) || (st = cnt.reserve(N + 1)) || (st = mr.reserve(1)) ||
-        (st = h->findrm.reserve(N + 1)) || (st = h->centrm.reserve(N)))
+    st = build_product(h, mesh->N, mesh->findrm.p, mesh->colm.p, mesh->nnz, mesh->findrm.p, mesh->colm.p, s);
+  }
+  if (st != FL_OK) {
+    fl_gpu_mesh_destroy(h);
+    return st;
+  }
+  *out = h;
+  return FL_OK;
+}
+
+// The product pattern C C^T of a Taylor-Hood divergence pattern (pressure
+// rows, P2 velocity columns), the pattern of its cmc_m.
+extern "C" int fl_gpu_rect_secondorder_register(fl_mesh pattern, fl_mesh* out) {
+  FL_CHECK_ARG(pattern && out, "null argument");
+  FL_CHECK_ARG(pattern->so_parent && pattern->so_parent->loc == 10 && pattern->N == pattern->so_parent->Nx,
+               "a Taylor-Hood pattern (fl_gpu_rect_register)");
+  const int ncol = pattern->so_parent->N;
+  const int64_t annz = pattern->nnz;
+  cudaStream_t s = pattern->so_parent->stream;
+  int st = FL_OK;
+  fl_mesh_t* h = new_product_handle(&st);
+  do {
+    if (st != FL_OK) break;
+    h->a_pat = pattern;
+    DevBuf<int32_t> cnt;
+    if ((st = h->err.reserve(1)) || (st = cnt.reserve((size_t)ncol + 1)) ||
+        (st = h->tr_ptr.reserve((size_t)ncol + 1)) || (st = h->tr_col.reserve((size_t)std::max<int64_t>(annz, 1))) ||
+        (st = h->tr_pos.reserve((size_t)std::max<int64_t>(annz, 1))))
       break;
     if (cudaMemsetAsync(h->err.p, 0, sizeof(ErrWord), s) != cudaSuccess ||
-        cudaMemsetAsync(mr.p, 0, sizeof(int32_t), s) != cudaSuccess) {
+        cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)ncol + 1), s) != cudaSuccess) {
       set_error("memset failed");
       st = FL_ERR_CUDA;
       break;
     }
-    const unsigned g = (unsigned)std::max(1, std::min((N + kSoWarps - 1) / kSoWarps, num_sms() * 16));
-    k_so_rows<<<g, kSoWarps * 32, 0, s>>>(N, mesh->findrm.p, mesh->colm.p, nullptr, cnt.p, nullptr, nullptr, mr.p,
-                                          h->err.p, 0);
-    if ((st = check_err(h->err.p, s, "second-order row with more candidates than the row scratch holds")) != FL_OK)
-      break;
-    if ((st = exclusive_scan_i32(cnt.p, h->findrm.p, N, s)) != FL_OK) break;
-    int32_t nnz = 0, maxrow = 0;
-    if (cudaMemcpyAsync(&nnz, h->findrm.p + N, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(&maxrow, mr.p, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-      set_error("pattern size read-back failed");
+    k_tr_count<<<grid_for(pattern->N, kT), kT, 0, s>>>(pattern->N, pattern->findrm.p, pattern->colm.p, ncol, cnt.p,
+                                                      h->err.p);
+    if ((st = check_err(h->err.p, s, "a pattern column outside the velocity nodes")) != FL_OK) break;
+    if ((st = exclusive_scan_i32(cnt.p, h->tr_ptr.p, ncol, s)) != FL_OK) break;
+    if (cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * ((size_t)ncol + 1), s) != cudaSuccess) {
+      set_error("memset failed");
       st = FL_ERR_CUDA;
       break;
     }
-    h->nnz = nnz;
-    h->max_row = maxrow;
-    if ((st = h->colm.reserve((size_t)std::max(nnz, 1)))) break;
-    k_fill_i32<<<grid_for(N, kT), kT, 0, s>>>(h->centrm.p, N, -1);
-    k_so_rows<<<g, kSoWarps * 32, 0, s>>>(N, mesh->findrm.p, mesh->colm.p, h->findrm.p, nullptr, h->colm.p,
-                                          h->centrm.p, mr.p, h->err.p, 1);
-    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
-      set_error("second-order pattern fill failed");
+    k_tr_fill<<<grid_for(pattern->N, kT), kT, 0, s>>>(pattern->N, pattern->findrm.p, pattern->colm.p, ncol,
+                                                     h->tr_ptr.p, cnt.p, h->tr_col.p, h->tr_pos.p);
+    k_tr_sort<<<grid_for(ncol, kT), kT, 0, s>>>(ncol, h->tr_ptr.p, h->tr_col.p, h->tr_pos.p);
+    if (cudaGetLastError() != cudaSuccess) {
+      set_error("transposed pattern failed");
       st = FL_ERR_CUDA;
       break;
     }
-    // slot map of the row products
-    const int64_t annz = mesh->nnz;
-    DevBuf<int32_t> pc;
-    if ((st = pc.reserve((size_t)annz + 1)) || (st = h->pair_off.reserve((size_t)annz + 1))) break;
-    k_pair_count<<<grid_for(annz, kT), kT, 0, s>>>(N, mesh->findrm.p, mesh->colm.p, pc.p);
-    if ((st = exclusive_scan_i32(pc.p, h->pair_off.p, annz, s)) != FL_OK) break;
-    int32_t npairs = 0;
-    if (cudaMemcpyAsync(&npairs, h->pair_off.p + annz, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-      set_error("pair count read-back failed");
-      st = FL_ERR_CUDA;
-      break;
-    }
-    if ((st = h->pair_map.reserve((size_t)std::max(npairs, 1)))) break;
-    k_pair_map<<<(unsigned)std::max(1, std::min((N + 7) / 8, num_sms() * 8)), 256, 0, s>>>(
-        N, mesh->findrm.p, mesh->colm.p, h->findrm.p, h->colm.p, h->pair_off.p, h->pair_map.p, h->err.p);
-    if ((st = check_err(h->err.p, s, "second-order row longer than the product's shared-memory row")) != FL_OK) break;
+    st = build_product(h, pattern->N, pattern->findrm.p, pattern->colm.p, annz, h->tr_ptr.p, h->tr_col.p, s);
   } while (0);
   if (st != FL_OK) {
     fl_gpu_mesh_destroy(h);
@@ -1369,18 +1474,22 @@ extern "C" int fl_dev_lumped_mass(fl_mesh m, double* lumped_mass, void* stream) 
 
 static int rowprod_launch(fl_mesh prod, int ndim, bool div, const double* const a[3], const double* w,
                           const double* const b[3], double theta, int scale, double* out, cudaStream_t s) {
-  fl_mesh_t* par = prod->so_parent;
+  // first factor's pattern, and the second factor's rows transposed (for a
+  // structurally symmetric square pattern, the pattern itself)
+  fl_mesh_t* par = prod->a_pat ? prod->a_pat : prod->so_parent;
   const int64_t annz = par->nnz;
+  const int32_t* tpos = prod->a_pat ? prod->tr_pos.p : par->tpos.p;
   FL_TRY(prod->bt.reserve((size_t)ndim * annz));
   const unsigned gb = grid_for(annz, kT);
-  if (ndim == 1) k_bt_gather<1><<<gb, kT, 0, s>>>(annz, par->tpos.p, b[0], nullptr, nullptr, prod->bt.p);
-  else if (ndim == 2) k_bt_gather<2><<<gb, kT, 0, s>>>(annz, par->tpos.p, b[0], b[1], nullptr, prod->bt.p);
-  else k_bt_gather<3><<<gb, kT, 0, s>>>(annz, par->tpos.p, b[0], b[1], b[2], prod->bt.p);
+  if (ndim == 1) k_bt_gather<1><<<gb, kT, 0, s>>>(annz, tpos, b[0], nullptr, nullptr, prod->bt.p);
+  else if (ndim == 2) k_bt_gather<2><<<gb, kT, 0, s>>>(annz, tpos, b[0], b[1], nullptr, prod->bt.p);
+  else k_bt_gather<3><<<gb, kT, 0, s>>>(annz, tpos, b[0], b[1], b[2], prod->bt.p);
   RowProdArgs P{};
   P.n = prod->N;
   P.annz = annz;
   P.aptr = par->findrm.p;
   P.acol = par->colm.p;
+  P.tptr = prod->a_pat ? prod->tr_ptr.p : par->findrm.p;
   P.optr = prod->findrm.p;
   P.poff = prod->pair_off.p;
   P.pmap = prod->pair_map.p;
@@ -1408,8 +1517,10 @@ static int rowprod_launch(fl_mesh prod, int ndim, bool div, const double* const 
 }
 
 static int check_product(fl_mesh prod) {
-  FL_CHECK_ARG(prod && prod->so_parent, "a second-order pattern handle (fl_gpu_secondorder_register)");
-  FL_CHECK_ARG(prod->so_parent->tpos.p, "the parent mesh has no transpose map");
+  FL_CHECK_ARG(prod && (prod->so_parent || prod->a_pat),
+               "a second-order pattern handle (fl_gpu_secondorder_register, fl_gpu_rect_secondorder_register)");
+  FL_CHECK_ARG(prod->a_pat ? prod->tr_pos.p != nullptr : prod->so_parent->tpos.p != nullptr,
+               "the parent pattern has no transpose map");
   return FL_OK;
 }
 

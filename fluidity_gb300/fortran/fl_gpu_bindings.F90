@@ -67,7 +67,8 @@ module fl_gpu_bindings
             fl_dev_mult_div_invscalar_div_T, fl_dev_assemble_kmk, fl_dev_masslumped_poisson_rhs, &
             fl_dev_correct_masslumped_velocity, fl_dev_csr_addto, fl_kernel_launch_count, &
             fl_set_kernel_timing, fl_last_assembly_kernel_ms, fl_set_wait_test, fl_dev_projected_guess, &
-            fl_gpu_rect_register, fl_dev_assemble_divergence_p2p1, fl_dev_assemble_divergence_p2p1_faces
+            fl_gpu_rect_register, fl_dev_assemble_divergence_p2p1, fl_dev_assemble_divergence_p2p1_faces, &
+            fl_gpu_rect_secondorder_register
   public :: gpu_check, gpu_mesh_handle, gpu_advdif_cg_supported, gpu_assemble_advection_diffusion_cg, &
             gpu_petsc_solve_supported, gpu_petsc_solve_scalar, gpu_solve_field_equation_cg
 
@@ -507,6 +508,15 @@ module fl_gpu_bindings
        type(c_ptr), intent(in) :: ct_val(3)
        integer(c_int) :: st
      end function fl_dev_assemble_divergence_p2p1_faces
+
+     ! the pattern of its cmc_m (C C^T through the velocity nodes)
+     function fl_gpu_rect_secondorder_register(pattern, out) bind(c, name="fl_gpu_rect_secondorder_register") &
+          result(st)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: pattern
+       type(c_ptr), intent(out) :: out
+       integer(c_int) :: st
+     end function fl_gpu_rect_secondorder_register
 
      function fl_dev_lumped_mass(mesh, lumped_mass, stream) bind(c, name="fl_dev_lumped_mass") result(st)
        import :: c_int, c_ptr

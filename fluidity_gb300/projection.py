@@ -92,6 +92,26 @@ class TaylorHoodPattern(ft.Mesh):
         self._sparsity = None
 
 
+class TaylorHoodProductPattern(ft.Mesh):
+    """The pattern of the Taylor-Hood cmc_m (fl_gpu_rect_secondorder_register):
+    C C^T of a TaylorHoodPattern through the velocity nodes, pressure rows and
+    columns.  A pattern-only handle for mult_div_vector_div_T, solves and
+    SpMVs; it keeps its pattern alive."""
+
+    def __init__(self, pattern: TaylorHoodPattern):
+        self.lib = _lib.load()
+        self.parent = pattern
+        h = C.c_void_p()
+        check(self.lib.fl_gpu_rect_secondorder_register(pattern.handle, C.byref(h)),
+              "fl_gpu_rect_secondorder_register")
+        self.handle = h
+        nnz, ncol = C.c_int64(), C.c_int32()
+        check(self.lib.fl_gpu_mesh_info(h, C.byref(nnz), C.byref(ncol)), "fl_gpu_mesh_info")
+        self.N, self.E, self.loc, self.Nx = pattern.N, 0, 0, 0
+        self.nnz, self.ncolours = nnz.value, 0
+        self._sparsity = None
+
+
 def assemble_divergence_matrix_p2p1(mesh: ft.Mesh, pattern: TaylorHoodPattern, *, integrate_by_parts=False,
                                     quad_degree=4, ct=None, stream=None):
     """The element terms of C^T for P2 velocity (mesh) and P1 pressure on its

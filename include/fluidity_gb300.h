@@ -539,6 +539,18 @@ int fl_dev_assemble_divergence_p2p1_faces(fl_mesh mesh, fl_mesh pattern, const f
                                           const int32_t* vfaces, int32_t quad_degree, double* const ct_val[3],
                                           double* ct_rhs, void* stream);
 
+/* The pattern of the Taylor-Hood cmc_m: get_csr_sparsity_secondorder(state,
+ * p_mesh, u_mesh) (femtools/Sparsity_Patterns_Meshes.F90:122-148), i.e.
+ * make_sparsity_transpose of the divergence pattern with itself (pressure
+ * rows, pressure columns through the shared P2 velocity nodes), built on the
+ * GPU as a pattern-only handle.  fl_dev_mult_div_vector_div_T on it forms
+ * C_P^T diag(w) C with a and b on the pattern of fl_gpu_rect_register and w
+ * per velocity node (assemble_masslumped_cmc, assemble/Assemble_CMC.F90:119-
+ * 135, with the P2 lumped velocity mass); solves, SpMVs and Dirichlet
+ * conditions run on it as on any pattern-only handle.  The pattern handle
+ * must outlive it. */
+int fl_gpu_rect_secondorder_register(fl_mesh pattern, fl_mesh* out);
+
 /* compute_lumped_mass (femtools/FEFields.F90:161-214) of a P1 mesh with unit
  * density, as get_lumped_mass (femtools/State_Fields.F90:124-152) caches it. */
 int fl_dev_lumped_mass(fl_mesh mesh, double* lumped_mass, void* stream);

@@ -287,3 +287,42 @@ def test_taylor_hood_surface_terms_match_oracle(O, torch, aniso_mesh, which):
         assert row_scaled_error(got[d], want[d], f) <= 1e-12
     pat.close()
     mesh.close()
+
+
+@pytest.mark.parametrize("which", ["cube4", "unstructured"])
+def test_taylor_hood_cmc_matches_scipy(O, torch, aniso_mesh, which):
+    """cmc_m of the Taylor-Hood pair (fl_gpu_rect_secondorder_register and
+    fl_dev_mult_div_vector_div_T): the pattern equals the structure of C C^T
+    through the velocity nodes, bit for bit, and C^T diag(w) C with a weight
+    per velocity node and dimension agrees with scipy's FP64 triple product
+    within 1e-12 row-scaled; symmetric and deterministic."""
+    nd, X = M.cube_mesh(4) if which == "cube4" else aniso_mesh
+    N = X.shape[0]
+    nd2, n2 = O.make_global_numbering_p2(nd)
+    mesh = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    pat = PR.TaylorHoodPattern(mesh)
+    prod = PR.TaylorHoodProductPattern(pat)
+    f, c = O.make_sparsity_rect(nd, nd2, N)
+    S = sp.csr_matrix((np.ones(c.size), c, f), shape=(N, n2))
+    P = (S @ S.T).tocsr()
+    P.sort_indices()
+    s = prod.sparsity()
+    assert prod.N == N and prod.nnz == P.nnz
+    assert np.array_equal(s.findrm, P.indptr) and np.array_equal(s.colm, P.indices)
+    ct = PR.assemble_divergence_matrix_p2p1(mesh, pat)
+    w = torch.tensor(np.random.default_rng(4).random((n2, 3)) + 0.5, device="cuda")
+    cmc = PR.mult_div_vector_div_T(prod, ct, w.reshape(-1), ct)
+    torch.cuda.synchronize()
+    cth, wh = ct.cpu().numpy(), w.cpu().numpy()
+    ref = sum(sp.csr_matrix((cth[d], c, f), shape=(N, n2)) @ sp.diags(wh[:, d])
+              @ sp.csr_matrix((cth[d], c, f), shape=(N, n2)).T for d in range(3)).toarray()
+    rows = np.repeat(np.arange(N), np.diff(P.indptr))
+    want = ref[rows, P.indices]
+    got = cmc.cpu().numpy()
+    assert row_scaled_error(got, want, P.indptr) <= TOL
+    A = sp.csr_matrix((got, P.indices, P.indptr), shape=(N, N))
+    assert abs(A - A.T).max() <= 1e-14 * abs(A).max()
+    assert torch.equal(cmc, PR.mult_div_vector_div_T(prod, ct, w.reshape(-1), ct))
+    prod.close()
+    pat.close()
+    mesh.close()
