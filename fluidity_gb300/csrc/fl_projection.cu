@@ -1464,11 +1464,69 @@ extern "C" int fl_dev_assemble_divergence_p2p1_faces(fl_mesh m, fl_mesh rect, co
   return check_err(rect->err.p, s, "Taylor-Hood divergence surface terms");
 }
 
+namespace fl {
+namespace {
+
+// compute_lumped_mass of a P2 mesh (unit density): the row sums of
+// shape_shape over the rule, |detJ| sum_g w_g N_i(g) sum_j N_j(g) =
+// |detJ| W_i with W_i = sum_g w_g N_i(g) (the P2 functions sum to one; the
+// degree-4 rule is exact: W = -1/120 at the vertices, 1/30 at the edges).
+// One thread per node over its elements in ascending order (the element
+// loop's order of the reference's addto).
+struct LumpP2Args {
+  int32_t N;
+  const int32_t* ne_ptr;
+  const int32_t* ne;
+  const int32_t* xnd;
+  const double* X;
+  double W[10];
+  double* out;
+};
+
+__global__ void k_lumped_p2(LumpP2Args A) {
+  note_launch();
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A.N; v += gridDim.x * blockDim.x) {
+    double sum = 0.0;
+    for (int q = A.ne_ptr[v]; q < A.ne_ptr[v + 1]; ++q) {
+      const int inc = A.ne[q], e = inc >> 4, a = inc & 15;
+      double x[4][3];
+      for (int i = 0; i < 4; ++i)
+        for (int c = 0; c < 3; ++c) x[i][c] = A.X[3 * A.xnd[4 * e + i] + c];
+      double J[3][3];
+      for (int c = 0; c < 3; ++c)
+        for (int b = 0; b < 3; ++b) J[c][b] = x[b][c] - x[3][c];
+      const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                         J[1][0] * (J[0][1] * J[2][2] - J[2][1] * J[0][2]) +
+                         J[2][0] * (J[0][1] * J[1][2] - J[1][1] * J[0][2]);
+      sum += fabs(det) * A.W[a];
+    }
+    A.out[v] = sum;
+  }
+}
+
+}  // namespace
+}  // namespace fl
+
 extern "C" int fl_dev_lumped_mass(fl_mesh m, double* lumped_mass, void* stream) {
-  FL_CHECK_ARG(p1_mesh(m), "a P1 mesh handle");
+  FL_CHECK_ARG(m && m->E > 0 && (m->loc == 4 || m->loc == 10), "a P1 or P2 mesh handle");
   FL_CHECK_ARG(lumped_mass, "null argument");
   cudaStream_t s = pick(m, stream);
-  FL_TRY(divergence_passes(m, false, nullptr, nullptr, nullptr, nullptr, lumped_mass, nullptr, s));
+  if (m->loc == 4) {
+    FL_TRY(divergence_passes(m, false, nullptr, nullptr, nullptr, nullptr, lumped_mass, nullptr, s));
+    return FL_OK;
+  }
+  TetQuad q;
+  tet_quadrature(4, q);
+  TetShape sh;
+  tet_shape(2, q, sh);
+  LumpP2Args A{m->N, m->ne_ptr.p, m->ne.p, m->xndglno.p, m->coords.p, {}, lumped_mass};
+  for (int i = 0; i < 10; ++i) {
+    double w = 0.0;
+    for (int g = 0; g < q.ngi; ++g) w += q.w[g] * sh.n[i][g];
+    A.W[i] = w;
+  }
+  k_lumped_p2<<<grid_for(m->N, kT), kT, 0, s>>>(A);
+  FL_TRY_CUDA(cudaGetLastError());
   return FL_OK;
 }
 

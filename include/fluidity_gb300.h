@@ -551,8 +551,10 @@ int fl_dev_assemble_divergence_p2p1_faces(fl_mesh mesh, fl_mesh pattern, const f
  * must outlive it. */
 int fl_gpu_rect_secondorder_register(fl_mesh pattern, fl_mesh* out);
 
-/* compute_lumped_mass (femtools/FEFields.F90:161-214) of a P1 mesh with unit
- * density, as get_lumped_mass (femtools/State_Fields.F90:124-152) caches it. */
+/* compute_lumped_mass (femtools/FEFields.F90:161-214) of a P1 or P2 mesh with
+ * unit density, as get_lumped_mass (femtools/State_Fields.F90:124-152) caches
+ * it: the row sums of the consistent mass matrix (for P2, negative at the
+ * vertices), each node's elements summed in ascending order. */
 int fl_dev_lumped_mass(fl_mesh mesh, double* lumped_mass, void* stream);
 
 /* mult_div_vector_div_T (femtools/Sparse_Matrices_Fields.F90:590-671):

@@ -326,3 +326,26 @@ def test_taylor_hood_cmc_matches_scipy(O, torch, aniso_mesh, which):
     prod.close()
     pat.close()
     mesh.close()
+
+
+@pytest.mark.parametrize("which", ["cube4", "unstructured"])
+def test_p2_lumped_mass_matches_oracle(O, torch, aniso_mesh, which):
+    """compute_lumped_mass of the P2 velocity mesh (the weights of the
+    Taylor-Hood cmc_m): within 1e-13 of orc_lumped_mass (degree 2, the
+    degree-4 rule), -V/20 at the vertices and V/5 at the edges of every
+    element, summing to the domain's volume."""
+    nd, X = M.cube_mesh(4) if which == "cube4" else aniso_mesh
+    nd2, n2 = O.make_global_numbering_p2(nd)
+    mesh = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    ml = PR.compute_lumped_mass(mesh)
+    torch.cuda.synchronize()
+    got = ml.cpu().numpy()
+    want = O.lumped_mass(nd2, nd, X, n2, degree=2, quad_degree=4)
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    J = np.stack([X[nd[:, k]] - X[nd[:, 3]] for k in range(3)], axis=1)
+    vol = np.abs(np.linalg.det(J)) / 6.0
+    assert abs(got.sum() - vol.sum()) <= 1e-13 * vol.sum()
+    vert = np.zeros(n2, bool)
+    vert[np.unique(nd2[:, [0, 2, 5, 9]])] = True
+    assert (got[vert] < 0).all() and (got[~vert] > 0).all()
+    mesh.close()
