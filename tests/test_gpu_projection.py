@@ -349,3 +349,32 @@ def test_p2_lumped_mass_matches_oracle(O, torch, aniso_mesh, which):
     vert[np.unique(nd2[:, [0, 2, 5, 9]])] = True
     assert (got[vert] < 0).all() and (got[~vert] > 0).all()
     mesh.close()
+
+
+def test_taylor_hood_error_paths(O):
+    """Weak-Dirichlet or normal-flow faces without boundary values, and a
+    product pattern asked of a handle that is not a Taylor-Hood pattern, are
+    argument errors, and the handles stay usable."""
+    import torch
+    nd, X = M.cube_mesh(3)
+    nd2, n2 = O.make_global_numbering_p2(nd)
+    mesh = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    pat = PR.TaylorHoodPattern(mesh)
+    faces6, xf, fe = M.boundary_faces_p2(nd, nd2)
+    nf = xf.shape[0]
+    ct = PR.assemble_divergence_matrix_p2p1(mesh, pat, integrate_by_parts=True)
+    rhs = torch.zeros(X.shape[0], dtype=torch.float64, device="cuda")
+    for t in (1, 5):
+        ty = np.zeros((nf, 3), np.int32)
+        ty[:, 0] = t
+        with pytest.raises(RuntimeError, match="surface terms"):
+            PR.assemble_divergence_faces_p2p1(mesh, pat, ct, faces=xf, vfaces=faces6, face_ele=fe, bc_type=ty,
+                                              ct_rhs=rhs)
+    with pytest.raises(RuntimeError, match="Taylor-Hood pattern"):
+        PR.TaylorHoodProductPattern(mesh)
+    ct2 = PR.assemble_divergence_matrix_p2p1(mesh, pat, integrate_by_parts=True)
+    PR.assemble_divergence_faces_p2p1(mesh, pat, ct2, faces=xf, vfaces=faces6, face_ele=fe)
+    torch.cuda.synchronize()
+    assert torch.isfinite(ct2).all()
+    pat.close()
+    mesh.close()
