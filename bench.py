@@ -498,6 +498,89 @@ def bench_p2(args, dev, stream, n=64):
     }, host
 
 
+def bench_taylor_hood(args, dev, stream, n=64):
+    """The Taylor-Hood pair (P2 velocity, P1 pressure) on the n^3 six-tet
+    cube: the divergence element terms (by parts) and surface loop, the P2
+    lumped velocity mass and C M_l^-1 C^T on its product pattern, by CUDA
+    events on the stream; and, as a size-independent check, the by-parts
+    matrix with every face's terms against the direct form (integration by
+    parts, exact at these rules), row-scaled."""
+    import torch
+
+    from fluidity_gb300 import femtools as ft
+    from fluidity_gb300 import meshgen as M
+    from fluidity_gb300 import projection as PR
+
+    nd, X = M.cube_mesh(n)
+    nd2, n2 = ft.make_global_numbering_p2(nd)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m = ft.Mesh(nd2, X, x_ndglno=nd, nodes=n2)
+    pat = PR.TaylorHoodPattern(m)
+    prod = PR.TaylorHoodProductPattern(pat)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    faces6, xf, fe = M.boundary_faces_p2(nd, nd2)
+    dfaces = torch.from_numpy(xf.astype(np.int32)).to(dev)
+    dv = torch.from_numpy(faces6.astype(np.int32)).to(dev)
+    dfe = torch.from_numpy(fe.astype(np.int32)).to(dev)
+    ct = torch.empty((3, pat.nnz), dtype=torch.float64, device=dev)
+    ml = torch.empty(m.N, dtype=torch.float64, device=dev)
+    cmc = torch.empty(prod.nnz, dtype=torch.float64, device=dev)
+    reps = max(3, min(10, args.steps))
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def elem():
+        PR.assemble_divergence_matrix_p2p1(m, pat, integrate_by_parts=True, ct=ct, stream=stream)
+
+    def faces():
+        PR.assemble_divergence_faces_p2p1(m, pat, ct, faces=dfaces, vfaces=dv, face_ele=dfe, stream=stream)
+
+    def lumped():
+        PR.compute_lumped_mass(m, out=ml, stream=stream)
+
+    elem_ms, faces_ms, lumped_ms = timed(elem), timed(faces), timed(lumped)
+    w = torch.stack([1.0 / ml] * 3, dim=1).reshape(-1).contiguous()
+
+    def cmcf():
+        PR.mult_div_vector_div_T(prod, ct, w, ct, out=cmc, stream=stream)
+
+    cmc_ms = timed(cmcf)
+    # by parts + every face (type 0) against the direct form
+    elem()
+    faces()
+    direct = PR.assemble_divergence_matrix_p2p1(m, pat, integrate_by_parts=False, stream=stream)
+    torch.cuda.synchronize()
+    f = pat.sparsity().findrm
+    rows = torch.from_numpy(np.repeat(np.arange(pat.N), np.diff(f))).to(dev)
+    err = 0.0
+    for d in range(3):
+        rowmax = torch.zeros(pat.N, dtype=torch.float64, device=dev).scatter_reduce(
+            0, rows, direct[d].abs(), reduce="amax")
+        diff = (ct[d] - direct[d]).abs() / rowmax[rows].clamp_min(1e-300)
+        err = max(err, float(diff.max()))
+    out = {"workload": f"Taylor-Hood pair on the {n}^3 six-tet cube (P2 velocity, P1 pressure)",
+           "elements": m.E, "velocity_nodes": m.N, "pressure_nodes": pat.N, "faces": int(xf.shape[0]),
+           "nnz_divergence": pat.nnz, "nnz_cmc": prod.nnz, "pattern_setup_s": setup_s,
+           "divergence_elements_ms": elem_ms, "divergence_faces_ms": faces_ms, "lumped_mass_ms": lumped_ms,
+           "cmc_product_ms": cmc_ms, "by_parts_identity_max_row_scaled_err": err}
+    prod.close()
+    pat.close()
+    m.close()
+    return out
+
+
 def bench_projection(args, dev, stream, m, X, n):
     """P1-P1 pressure projection on the mesh of the headline workload: the
     divergence matrix C^T, the second-order pattern, C M_l^-1 C^T, the KMK
@@ -1144,6 +1227,8 @@ def run_ours(args, rank, ws, dist):
     if not args.no_p2:
         p2, gpu["p2"] = bench_p2(args, dev, stream)
     projection = None if args.no_projection else bench_projection(args, dev, stream, m, X, args.n)
+    if projection is not None and not args.no_p2:
+        projection["taylor_hood_64"] = bench_taylor_hood(args, dev, stream, 64)
     steps16, ts16 = bench_advdif_steps(args, dev, stream)
     gpu["steps16"] = (ts16, steps16["iterations"])
     batch = None
@@ -1230,6 +1315,11 @@ def compact_summary(line):
         out["projection_128"] = {"div_ms": sig(pr["divergence"]["ms"]), "cmc_ms": sig(pr["cmc_product"]["ms"]),
                                  "kmk_ms": sig(pr["kmk_ms"]), "solve_ms": sig(pr["projection_solve"]["ms"]),
                                  "amg_solve_ms": sig(pr["projection_solve_amg"]["ms"])}
+        th = pr.get("taylor_hood_64")
+        if th:
+            out["taylor_hood_64"] = {"div_ms": sig(th["divergence_elements_ms"]), "faces_ms": sig(th["divergence_faces_ms"]),
+                                     "cmc_ms": sig(th["cmc_product_ms"]),
+                                     "identity_err": sig(th["by_parts_identity_max_row_scaled_err"], 2)}
     ln = line.get("learned")
     if ln:
         for k, v in ln.items():

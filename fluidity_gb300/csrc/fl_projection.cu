@@ -1477,28 +1477,37 @@ struct LumpP2Args {
   int32_t N;
   const int32_t* ne_ptr;
   const int32_t* ne;
-  const int32_t* xnd;
-  const double* X;
+  const double* adet;  // |detJ| of every element
   double W[10];
   double* out;
 };
+
+// |detJ| of every element, once (FP64: one determinant per element instead
+// of one per incidence)
+__global__ void k_abs_det(int32_t E, const int32_t* __restrict__ xnd, const double* __restrict__ X,
+                          double* __restrict__ adet) {
+  note_launch();
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+    double x[4][3];
+    for (int i = 0; i < 4; ++i)
+      for (int c = 0; c < 3; ++c) x[i][c] = X[3 * xnd[4 * e + i] + c];
+    double J[3][3];
+    for (int c = 0; c < 3; ++c)
+      for (int b = 0; b < 3; ++b) J[c][b] = x[b][c] - x[3][c];
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                       J[1][0] * (J[0][1] * J[2][2] - J[2][1] * J[0][2]) +
+                       J[2][0] * (J[0][1] * J[1][2] - J[1][1] * J[0][2]);
+    adet[e] = fabs(det);
+  }
+}
 
 __global__ void k_lumped_p2(LumpP2Args A) {
   note_launch();
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < A.N; v += gridDim.x * blockDim.x) {
     double sum = 0.0;
     for (int q = A.ne_ptr[v]; q < A.ne_ptr[v + 1]; ++q) {
-      const int inc = A.ne[q], e = inc >> 4, a = inc & 15;
-      double x[4][3];
-      for (int i = 0; i < 4; ++i)
-        for (int c = 0; c < 3; ++c) x[i][c] = A.X[3 * A.xnd[4 * e + i] + c];
-      double J[3][3];
-      for (int c = 0; c < 3; ++c)
-        for (int b = 0; b < 3; ++b) J[c][b] = x[b][c] - x[3][c];
-      const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
-                         J[1][0] * (J[0][1] * J[2][2] - J[2][1] * J[0][2]) +
-                         J[2][0] * (J[0][1] * J[1][2] - J[1][1] * J[0][2]);
-      sum += fabs(det) * A.W[a];
+      const int inc = A.ne[q];
+      sum += A.adet[inc >> 4] * A.W[inc & 15];
     }
     A.out[v] = sum;
   }
@@ -1519,7 +1528,9 @@ extern "C" int fl_dev_lumped_mass(fl_mesh m, double* lumped_mass, void* stream) 
   tet_quadrature(4, q);
   TetShape sh;
   tet_shape(2, q, sh);
-  LumpP2Args A{m->N, m->ne_ptr.p, m->ne.p, m->xndglno.p, m->coords.p, {}, lumped_mass};
+  FL_TRY(m->em.reserve((size_t)m->E));
+  k_abs_det<<<grid_for(m->E, kT), kT, 0, s>>>(m->E, m->xndglno.p, m->coords.p, m->em.p);
+  LumpP2Args A{m->N, m->ne_ptr.p, m->ne.p, m->em.p, {}, lumped_mass};
   for (int i = 0; i < 10; ++i) {
     double w = 0.0;
     for (int g = 0; g < q.ngi; ++g) w += q.w[g] * sh.n[i][g];
