@@ -23,6 +23,8 @@
 // All scalars live on the device; reductions use a fixed block partition and
 // a fixed summation tree, so results are deterministic run to run.
 #include <cmath>
+#include <cstddef>
+#include <cstdint>
 #include <cstdlib>
 #include <vector>
 
@@ -68,6 +70,15 @@ struct KspState {
   double true_r2, b2;
 };
 
+// An instantiated graph and the launch arguments it was captured with.
+struct GraphSlot {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uintptr_t> key;
+  ~GraphSlot() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
 // Workspace cached on a mesh handle (grow-only).
 struct KrylovWork {
   DevBuf<double> b, y, r, z, p, w, w2, dinv, part;
@@ -90,6 +101,10 @@ struct KrylovWork {
   // stream on which iteration chunks are captured and replayed as graphs
   cudaStream_t cs = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  // instantiated iteration graphs kept between solves: the FP64 CG chunk and
+  // the GMRES cycle, each reused while the buffers and sizes it was captured
+  // with are unchanged
+  GraphSlot g_cg, g_gmres;
   ~KrylovWork() {
     if (cs) cudaStreamDestroy(cs);
     if (ev_in) cudaEventDestroy(ev_in);
@@ -105,11 +120,12 @@ struct IterGraph {
   KrylovWork* W;
   cudaStream_t caller;
   cudaGraphExec_t exec = nullptr;
+  bool owned = true;  // false: the exec belongs to a workspace slot
   ~IterGraph() {
-    if (exec) cudaGraphExecDestroy(exec);
+    if (owned && exec) cudaGraphExecDestroy(exec);
   }
-  template <class Body>
-  int build(Body body) {
+  // the graph stream starts after the work enqueued so far on the caller's
+  int order_after_caller() {
     if (!W->cs) {
       FL_TRY_CUDA(cudaStreamCreateWithFlags(&W->cs, cudaStreamNonBlocking));
       FL_TRY_CUDA(cudaEventCreateWithFlags(&W->ev_in, cudaEventDisableTiming));
@@ -117,6 +133,10 @@ struct IterGraph {
     }
     FL_TRY_CUDA(cudaEventRecord(W->ev_in, caller));
     FL_TRY_CUDA(cudaStreamWaitEvent(W->cs, W->ev_in, 0));
+    return FL_OK;
+  }
+  template <class Body>
+  int capture(Body body, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     FL_TRY_CUDA(cudaStreamBeginCapture(W->cs, cudaStreamCaptureModeThreadLocal));
     body(W->cs);
@@ -126,12 +146,34 @@ struct IterGraph {
       set_error("iteration graph capture: %s", cudaGetErrorString(e));
       return FL_ERR_CUDA;
     }
-    const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+    const cudaError_t ei = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (ei != cudaSuccess) {
+      *out = nullptr;
       set_error("iteration graph instantiation: %s", cudaGetErrorString(ei));
       return FL_ERR_CUDA;
     }
+    return FL_OK;
+  }
+  template <class Body>
+  int build(Body body) {
+    FL_TRY(order_after_caller());
+    return capture(body, &exec);
+  }
+  // build() through a workspace slot: the slot's graph is replayed when it
+  // was captured with the same key (the launch arguments of the body)
+  template <class Body>
+  int build_cached(GraphSlot& slot, const std::vector<uintptr_t>& key, Body body) {
+    FL_TRY(order_after_caller());
+    owned = false;
+    if (!slot.exec || slot.key != key) {
+      if (slot.exec) cudaGraphExecDestroy(slot.exec);
+      slot.exec = nullptr;
+      slot.key.clear();
+      FL_TRY(capture(body, &slot.exec));
+      slot.key = key;
+    }
+    exec = slot.exec;
     return FL_OK;
   }
   int launch() {
@@ -720,123 +762,167 @@ __global__ void k_cg_open(KspState* st) {
 }
 
 // --------------------------------------------------------------- GMRES --
-// v_out = B (A v_in) -- KSP_PCApplyBAorAB with left preconditioning.
+// One Arnoldi step of KSPGMRESCycle in three launches, each global reduction
+// finished by the last block to retire (last_block: block order, so the sums
+// are deterministic):
+//   k_gmres_arnoldi: v_{it+1} = B (A v_it) (KSP_PCApplyBAorAB, left
+//                    preconditioning) and the partials of v_{it+1} . v_j,
+//                    j = 0..it; last block: h_j (VecMDot, classical
+//                    Gram-Schmidt)
+//   k_gmres_orth:    v_{it+1} -= sum_j h_j v_j (VecMAXPY), partials of
+//                    ||v_{it+1}||^2; last block: gmres_step (Hessenberg
+//                    column, rotations, convergence test)
+//   k_scale_vec:     v_{it+1} /= ||v_{it+1}|| (VecNormalize)
+// A launch whose state is `done` returns at once.
 template <int G>
-__global__ void k_apply_BA(SpArgs A, const double* __restrict__ dinv, const double* __restrict__ vin,
-                           double* __restrict__ vout) {
+__global__ void __launch_bounds__(kThreads) k_gmres_arnoldi(SpArgs A, const double* __restrict__ dinv, double* V,
+                                                            int64_t ld, int it, double* __restrict__ part,
+                                                            unsigned* ticket) {
   note_launch();
-  if (A.st->done) return;
-  const double piv = A.st->pivot;
-  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
-  const int gpb = blockDim.x / G;
+  __shared__ double sw[kThreads / G];
+  __shared__ double sacc[kMaxRestart + 1];
+  KspState* st = A.st;
+  if (st->done) return;
+  const double piv = st->pivot;
+  const double* vin = V + it * ld;
+  double* vout = V + (it + 1) * ld;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5, gpb = blockDim.x / G;
+  for (int j = threadIdx.x; j <= it; j += blockDim.x) sacc[j] = 0.0;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
-    double s = 0.0;
-    s = row_dot<G>(A.findrm, A.colm, A.val, vin, row, sub, row < A.n);
+    double s = row_dot<G>(A.findrm, A.colm, A.val, vin, row, sub, row < A.n);
     if (row < A.n && sub == 0) {
       if (A.ghost && A.ghost[row]) s = piv * vin[row];
-      vout[row] = s * dinv[row];
+      s *= dinv[row];
+      vout[row] = s;
+      sw[threadIdx.x / G] = s;
+    }
+    __syncthreads();
+    // the pass's rows dotted with each v_j: warp j % nw owns h_j
+    const int nr = min(gpb, A.n - base);
+    for (int j = warp; j <= it; j += nw) {
+      const double* vj = V + j * ld + base;
+      double a = 0.0;
+      for (int r = lane; r < nr; r += 32) a += sw[r] * vj[r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) sacc[j] += a;
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j <= it; j += blockDim.x) part[(int64_t)j * gridDim.x + blockIdx.x] = sacc[j];
+  if (!last_block(ticket)) return;
+  const int nb = gridDim.x;
+  for (int j = warp; j <= it; j += nw) {
+    const double* pj = part + (int64_t)j * nb;
+    double a = 0.0;
+    for (int b = lane; b < nb; b += 32) a += __ldcg(pj + b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) st->lhh[j] = a;
+  }
+}
+
+// Hessenberg column of iteration `it` from h_j (lhh) and ||v_{it+1}||^2 = nn,
+// happy breakdown, KSPGMRESUpdateHessenberg and the convergence test (the
+// body of KSPGMRESCycle after the orthogonalisation).  Called by every thread
+// of one block: the column and the earlier rotations are staged in shared
+// memory so the serial rotation chain runs at shared-memory latency.
+__device__ void gmres_step(KspState& S, double nn, int it, int restart) {
+  __shared__ double col[kMaxRestart + 2], rc[kMaxRestart + 1], rs[kMaxRestart + 1];
+  const int ld = restart + 1;
+  double* hc = S.hh + (int64_t)it * ld;
+  for (int j = threadIdx.x; j <= it; j += blockDim.x) col[j] = S.lhh[j];
+  for (int j = threadIdx.x; j < it; j += blockDim.x) {
+    rc[j] = S.cc[j];
+    rs[j] = S.ss[j];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double tt = sqrt(nn);
+    S.tt = tt;
+    col[it + 1] = tt;
+    double hapbnd = fabs(tt / S.grs[it]);
+    if (hapbnd > 1e-30) hapbnd = 1e-30;
+    const bool hapend = tt < hapbnd;
+    for (int j = 1; j <= it; ++j) {
+      const double h0 = col[j - 1], h1 = col[j];
+      col[j - 1] = rc[j - 1] * h0 + rs[j - 1] * h1;
+      col[j] = rc[j - 1] * h1 - rs[j - 1] * h0;
+    }
+    bool null_col = false;
+    double res = 0.0;
+    if (!hapend) {
+      const double h0 = col[it], h1 = col[it + 1];
+      const double rr = sqrt(h0 * h0 + h1 * h1);
+      if (rr == 0.0) {
+        S.reason = FL_DIVERGED_NULL;
+        S.done = 1;
+        S.it = it;  // this column is not used
+        null_col = true;
+      } else {
+        const double c = h0 / rr, sn = h1 / rr;
+        S.cc[it] = c;
+        S.ss[it] = sn;
+        const double g = S.grs[it];
+        S.grs[it + 1] = -(sn * g);
+        S.grs[it] = c * g;
+        col[it] = c * h0 + sn * h1;
+        res = fabs(S.grs[it + 1]);
+      }
+    }
+    if (!null_col) {
+      S.it = it + 1;
+      S.its += 1;
+      converged_test(S, S.its, res);
+      if (hapend && !S.reason) {
+        S.reason = FL_DIVERGED_BREAKDOWN;
+        S.done = 1;
+      }
+      if (!S.done && S.its >= S.max_its) {
+        S.reason = FL_DIVERGED_ITS;  // KSPSolve_GMRES: itcount >= max_it
+        S.done = 1;
+      }
     }
   }
+  __syncthreads();
+  for (int j = threadIdx.x; j <= it + 1; j += blockDim.x) hc[j] = col[j];
 }
 
-// Partials of v_new . v_j for j = 0..it (VecMDot in classical Gram-Schmidt).
-__global__ void k_mdot(int n, const KspState* st, const double* __restrict__ V, int64_t ld, int it,
-                       double* __restrict__ part, int nparts) {
+__global__ void __launch_bounds__(kThreads) k_gmres_orth(int n, KspState* st, double* __restrict__ V, int64_t ld,
+                                                         int it, int restart, double* __restrict__ part,
+                                                         unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
+  __shared__ double sh[kMaxRestart + 1];
   if (st->done) return;
-  const double* vn = V + (int64_t)(it + 1) * ld;
-  for (int j = 0; j <= it; ++j) {
-    const double* vj = V + (int64_t)j * ld;
-    double s = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += vn[i] * vj[i];
-    s = block_sum<kThreads>(s, red);
-    if (threadIdx.x == 0) part[(int64_t)j * nparts + blockIdx.x] = s;
-  }
-}
-
-__global__ void k_gs_coeffs(KspState* st, const double* __restrict__ part, int nparts, int it) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  for (int j = 0; j <= it; ++j) {
-    const double h = reduce_partials(part + (int64_t)j * nparts, nparts, red);
-    if (threadIdx.x == 0) st->lhh[j] = h;
-  }
-}
-
-// v_new -= sum_j h_j v_j (VecMAXPY), partial of ||v_new||^2.
-__global__ void k_gs_update(int n, const KspState* st, double* __restrict__ V, int64_t ld, int it,
-                            double* __restrict__ part) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
+  for (int j = threadIdx.x; j <= it; j += blockDim.x) sh[j] = st->lhh[j];
+  __syncthreads();
   double* vn = V + (int64_t)(it + 1) * ld;
   double nn = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    // subtraction order j = 0..it; the loads of four basis vectors are
+    // issued together
     double s = vn[i];
-    for (int j = 0; j <= it; ++j) s -= st->lhh[j] * V[(int64_t)j * ld + i];
+    int j = 0;
+    for (; j + 3 <= it; j += 4) {
+      const double a0 = V[(int64_t)j * ld + i], a1 = V[(int64_t)(j + 1) * ld + i];
+      const double a2 = V[(int64_t)(j + 2) * ld + i], a3 = V[(int64_t)(j + 3) * ld + i];
+      s -= sh[j] * a0;
+      s -= sh[j + 1] * a1;
+      s -= sh[j + 2] * a2;
+      s -= sh[j + 3] * a3;
+    }
+    for (; j <= it; ++j) s -= sh[j] * V[(int64_t)j * ld + i];
     vn[i] = s;
     nn += s * s;
   }
   nn = block_sum<kThreads>(nn, red);
   if (threadIdx.x == 0) part[blockIdx.x] = nn;
-}
-
-// VecNormalize, Hessenberg column, happy breakdown, KSPGMRESUpdateHessenberg,
-// convergence test (KSPGMRESCycle body after the orthogonalisation).
-__global__ void k_gmres_step(KspState* st, const double* __restrict__ part, int nparts, int it, int restart) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  if (st->done) return;
-  const double nn = reduce_partials(part, nparts, red);
-  if (threadIdx.x != 0) return;
-  KspState& S = *st;
-  const int ld = restart + 1;
-  auto HH = [&](int i, int j) -> double& { return S.hh[j * ld + i]; };
-  const double tt = sqrt(nn);
-  S.tt = tt;
-  for (int j = 0; j <= it; ++j) HH(j, it) = S.lhh[j];
-  HH(it + 1, it) = tt;
-  double hapbnd = fabs(tt / S.grs[it]);
-  if (hapbnd > 1e-30) hapbnd = 1e-30;
-  const bool hapend = tt < hapbnd;
-  for (int j = 1; j <= it; ++j) {
-    const double h0 = HH(j - 1, it), h1 = HH(j, it);
-    HH(j - 1, it) = S.cc[j - 1] * h0 + S.ss[j - 1] * h1;
-    HH(j, it) = S.cc[j - 1] * h1 - S.ss[j - 1] * h0;
-  }
-  double res;
-  if (!hapend) {
-    const double h0 = HH(it, it), h1 = HH(it + 1, it);
-    const double rr = sqrt(h0 * h0 + h1 * h1);
-    if (rr == 0.0) {
-      S.reason = FL_DIVERGED_NULL;
-      S.done = 1;
-      S.it = it;  // this column is not used
-      return;
-    }
-    S.cc[it] = h0 / rr;
-    S.ss[it] = h1 / rr;
-    S.grs[it + 1] = -(S.ss[it] * S.grs[it]);
-    S.grs[it] = S.cc[it] * S.grs[it];
-    HH(it, it) = S.cc[it] * h0 + S.ss[it] * h1;
-    res = fabs(S.grs[it + 1]);
-  } else {
-    res = 0.0;
-  }
-  S.it = it + 1;
-  S.its += 1;
-  converged_test(S, S.its, res);
-  if (hapend && !S.reason) {
-    S.reason = FL_DIVERGED_BREAKDOWN;
-    S.done = 1;
-  }
-  if (!S.done && S.its >= S.max_its) {
-    S.reason = FL_DIVERGED_ITS;  // KSPSolve_GMRES: itcount >= max_it
-    S.done = 1;
-  }
+  if (!last_block(ticket)) return;
+  nn = reduce_partials(part, gridDim.x, red);
+  gmres_step(*st, nn, it, restart);
 }
 
 __global__ void k_scale_vec(int n, const KspState* st, double* __restrict__ v) {
@@ -907,34 +993,55 @@ __global__ void k_norm2_pair(int n, const double* __restrict__ v, const double* 
   }
 }
 
-// KSPGMRESBuildSoln: back substitution on the rotated Hessenberg system.
+// KSPGMRESBuildSoln: back substitution on the rotated Hessenberg system, one
+// warp: lane l keeps the right-hand sides t_l, t_{l+32}; after nrs_k is
+// known every row above it subtracts H(i,k) nrs_k (column k of H is
+// contiguous, so each step is one coalesced load).
 __global__ void k_gmres_backsolve(KspState* st, int restart) {
   note_launch();
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
   KspState& S = *st;
   if (!S.live) return;
   const int ld = restart + 1;
-  auto HH = [&](int i, int j) -> double { return S.hh[j * ld + i]; };
   const int last = S.it - 1;
   if (last < 0) return;
-  S.nrs[last] = HH(last, last) != 0.0 ? S.grs[last] / HH(last, last) : 0.0;
-  for (int ii = 1; ii <= last; ++ii) {
-    const int k = last - ii;
-    double t = S.grs[k];
-    for (int j = k + 1; j <= last; ++j) t -= HH(k, j) * S.nrs[j];
-    S.nrs[k] = HH(k, k) != 0.0 ? t / HH(k, k) : 0.0;
+  const int lane = threadIdx.x;
+  double t0 = lane <= last ? S.grs[lane] : 0.0;
+  double t1 = lane + 32 <= last ? S.grs[lane + 32] : 0.0;
+  for (int k = last; k >= 0; --k) {
+    const double* hk = S.hh + (int64_t)k * ld;
+    const double h0 = lane < k ? hk[lane] : 0.0;
+    const double h1 = lane + 32 < k ? hk[lane + 32] : 0.0;
+    const double tk = __shfl_sync(0xffffffffu, k < 32 ? t0 : t1, k & 31);
+    const double hkk = hk[k];
+    const double y = hkk != 0.0 ? tk / hkk : 0.0;
+    if (lane == 0) S.nrs[k] = y;
+    t0 -= h0 * y;
+    t1 -= h1 * y;
   }
 }
 
 __global__ void k_gmres_update_x(int n, const KspState* st, const double* __restrict__ V, int64_t ld,
                                  double* __restrict__ y) {
   note_launch();
+  __shared__ double sy[kMaxRestart + 1];
   if (!st->live) return;
   const int last = st->it - 1;
   if (last < 0) return;
+  for (int j = threadIdx.x; j <= last; j += blockDim.x) sy[j] = st->nrs[j];
+  __syncthreads();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int j = 0; j <= last; ++j) s += st->nrs[j] * V[(int64_t)j * ld + i];
+    int j = 0;
+    for (; j + 3 <= last; j += 4) {
+      const double a0 = V[(int64_t)j * ld + i], a1 = V[(int64_t)(j + 1) * ld + i];
+      const double a2 = V[(int64_t)(j + 2) * ld + i], a3 = V[(int64_t)(j + 3) * ld + i];
+      s += sy[j] * a0;
+      s += sy[j + 1] * a1;
+      s += sy[j + 2] * a2;
+      s += sy[j + 3] * a3;
+    }
+    for (; j <= last; ++j) s += sy[j] * V[(int64_t)j * ld + i];
     y[i] += s;
   }
 }
@@ -1351,6 +1458,29 @@ static void cg_iteration(int n, KspState* st, const SellArgs& SA, KrylovWork* W,
                                    W->ticket.p + 1);
 }
 
+// One GMRES(restart) cycle with the restart decisions on the device
+// (k_gmres_cycle_start with first = -1 takes the first-cycle flag from the
+// state, k_gmres_cycle_end applies the iteration limit and clears the zero
+// guess); every launch returns at once when the solve has converged, so
+// cycles may be replayed past convergence.  No host interaction (capturable).
+static void gmres_cycle_launch(int G, const SpArgs& A, KrylovWork* W, int n, int restart, unsigned gsp,
+                               unsigned gv, cudaStream_t s) {
+  KspState* st = A.st;
+  const int64_t ld = n;
+  double* V = W->V.p;
+  FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, V, W->part.p, (int)gsp);
+  k_gmres_cycle_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, -1);
+  k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V);
+  for (int it = 0; it < restart; ++it) {
+    FL_SPMV_DISPATCH(G, k_gmres_arnoldi, A, W->dinv.p, V, ld, it, W->part.p, W->ticket.p + 2);
+    k_gmres_orth<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, restart, W->part.p, W->ticket.p + 3);
+    k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V + (it + 1) * ld);
+  }
+  k_gmres_backsolve<<<1, 32, 0, s>>>(st, restart);
+  k_gmres_update_x<<<gv, kThreads, 0, s>>>(n, st, V, ld, W->y.p);
+  k_gmres_cycle_end<<<1, 32, 0, s>>>(st);
+}
+
 int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_t* ghost, const double* rhs,
           double* x, fl_solve_report* rep, cudaStream_t s) {
   FL_CHECK_ARG(m && o && val && rhs && x && rep, "null argument");
@@ -1386,7 +1516,10 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   h.max_its = o->max_its;
   h.guess_zero = o->start_from_zero ? 1 : 0;
   h.unprec = o->norm_type == 1 ? 1 : 0;
-  FL_TRY_CUDA(cudaMemcpyAsync(W->st.p, &h, sizeof(KspState), cudaMemcpyHostToDevice, s));
+  h.gm_first = 1;
+  // the scalars only: the GMRES arrays behind them are written before they
+  // are read in every cycle
+  FL_TRY_CUDA(cudaMemcpyAsync(W->st.p, &h, offsetof(KspState, grs), cudaMemcpyHostToDevice, s));
   KspState* st = W->st.p;
   SpArgs A{n, m->findrm.p, m->colm.p, val, ghost, st};
 
@@ -1420,7 +1553,12 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     // reports convergence or the iteration limit (iterations past the end
     // of the solve return at once)
     IterGraph gr{W, s};
-    FL_TRY(gr.build([&](cudaStream_t c) {
+    const std::vector<uintptr_t> key{
+        (uintptr_t)n,        (uintptr_t)gv,       (uintptr_t)gsl,      (uintptr_t)np,      (uintptr_t)ghost,
+        (uintptr_t)st,       (uintptr_t)SA.sptr,  (uintptr_t)SA.scol,  (uintptr_t)SA.soff, (uintptr_t)W->z.p,
+        (uintptr_t)W->p.p,   (uintptr_t)W->w2.p,  (uintptr_t)W->part.p, (uintptr_t)W->ticket.p,
+        (uintptr_t)W->dinv.p, (uintptr_t)W->y.p,  (uintptr_t)W->r.p,   (uintptr_t)W->sval.p};
+    FL_TRY(gr.build_cached(W->g_cg, key, [&](cudaStream_t c) {
       for (int k = 0; k < chunk; ++k) cg_iteration(n, st, SA, W, gv, gsl, np, c);
     }));
     // with the unpreconditioned norm a convergence is confirmed on the
@@ -1451,49 +1589,30 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     FL_TRY(gr.join());
     FL_TRY_CUDA(cudaGetLastError());
   } else if (!mixed) {
-    // GMRES(restart)
-    const int64_t ld = n;
+    // GMRES(restart): one cycle with the restarts decided on the device,
+    // captured as a graph and replayed until the device reports the end of
+    // the solve (each cycle either ends it or advances the iteration count,
+    // and the iteration limit ends it)
     FL_TRY(W->V.reserve((size_t)(restart + 1) * n));
-    double* V = W->V.p;
-    bool first = true;
-    while (true) {
-      // v0 = B (b - A y)   (KSPInitialResidual; zero guess: B b)
-      FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, V, W->part.p, (int)gsp);
-      k_gmres_cycle_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, first ? 1 : 0);
-      k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V);
-      FL_TRY_CUDA(cudaGetLastError());
-      for (int it = 0; it < restart; ++it) {
-        FL_SPMV_DISPATCH(G, k_apply_BA, A, W->dinv.p, V + it * ld, V + (it + 1) * ld);
-        k_mdot<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p, (int)gv);
-        k_gs_coeffs<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it);
-        k_gs_update<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p);
-        k_gmres_step<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it, restart);
-        k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V + (it + 1) * ld);
-        if ((it + 1) % 8 == 0 || it + 1 == restart) {
-          FL_TRY_CUDA(cudaGetLastError());
-          KspState hs;
-          FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
-          FL_TRY_CUDA(cudaStreamSynchronize(s));
-          if (hs.done) break;
-        }
-      }
-      k_gmres_backsolve<<<1, 32, 0, s>>>(st, restart);
-      k_gmres_update_x<<<gv, kThreads, 0, s>>>(n, st, V, ld, W->y.p);
-      FL_TRY_CUDA(cudaGetLastError());
-      KspState hs;
-      FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
-      FL_TRY_CUDA(cudaStreamSynchronize(s));
-      if (hs.done) break;
-      if (hs.its >= o->max_its) {
-        hs.reason = FL_DIVERGED_ITS;
-        FL_TRY_CUDA(cudaMemcpyAsync(&st->reason, &hs.reason, sizeof(int), cudaMemcpyHostToDevice, s));
-        break;
-      }
-      // restart: KSPInitialResidual with the updated guess
-      int gz = 0;
-      FL_TRY_CUDA(cudaMemcpyAsync(&st->guess_zero, &gz, sizeof(int), cudaMemcpyHostToDevice, s));
-      first = false;
+    FL_TRY(W->ticket.reserve(4));
+    FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s));
+    IterGraph gr{W, s};
+    const std::vector<uintptr_t> key{
+        (uintptr_t)n,       (uintptr_t)G,        (uintptr_t)gsp,       (uintptr_t)gv,       (uintptr_t)restart,
+        (uintptr_t)val,     (uintptr_t)ghost,    (uintptr_t)m->findrm.p, (uintptr_t)m->colm.p, (uintptr_t)st,
+        (uintptr_t)W->b.p,  (uintptr_t)W->y.p,   (uintptr_t)W->r.p,    (uintptr_t)W->dinv.p, (uintptr_t)W->V.p,
+        (uintptr_t)W->part.p, (uintptr_t)W->ticket.p};
+    FL_TRY(gr.build_cached(W->g_gmres, key,
+                           [&](cudaStream_t c) { gmres_cycle_launch(G, A, W, n, restart, gsp, gv, c); }));
+    for (int cycle = 0; cycle <= o->max_its; ++cycle) {
+      FL_TRY(gr.launch());
+      int done = 0;
+      FL_TRY_CUDA(cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, W->cs));
+      FL_TRY_CUDA(cudaStreamSynchronize(W->cs));
+      if (done) break;
     }
+    FL_TRY(gr.join());
+    FL_TRY_CUDA(cudaGetLastError());
   } else {
     // Mixed precision: fp32 inner CG (rtol inner_rtol) inside fp64 refinement
     FL_TRY(W->r32.reserve(n));
@@ -1735,39 +1854,18 @@ void cg_setup_launch(CgPlan& P, cudaStream_t s) {
   k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + P.np, (int)P.gv);
   k_dinv<<<P.gv, kThreads, 0, s>>>(P.n, P.ghost, st, W->dinv.p, nullptr);
   FL_SPMV_DISPATCH(G, k_lift, P.A, P.rhs, P.x, P.o.start_from_zero ? 1 : 0, W->b.p, W->y.p);
+  cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s);
   if (P.ksp == 1) return;  // GMRES: the first cycle computes the initial residual
   FL_SPMV_DISPATCH(G, k_init_resid, P.A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
   k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
-  cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s);
   cudaMemsetAsync(W->p.p, 0, sizeof(double) * P.n, s);
   k_sell_values<<<grid_for(P.sell_len, kThreads), kThreads, 0, s>>>(P.sell_len, P.smap, P.val, W->sval.p, nullptr);
   k_cg_open<<<1, 32, 0, s>>>(st);
 }
 
-// One GMRES(restart) cycle with the restart decisions on the device: the same
-// launches as solve()'s host-driven cycle; every launch returns at once when
-// the solve has converged, so cycles may be replayed past convergence.
+// One GMRES(restart) cycle of a batched plan.
 static void gmres_cycle(CgPlan& P, cudaStream_t s) {
-  KrylovWork* W = P.W;
-  KspState* st = W->st.p;
-  const int G = P.G, n = P.n, restart = P.restart;
-  const unsigned gsp = P.gsp, gv = P.gv;
-  const int64_t ld = n;
-  double* V = W->V.p;
-  FL_SPMV_DISPATCH(G, k_init_resid, P.A, W->b.p, W->y.p, W->dinv.p, W->r.p, V, W->part.p, (int)gsp);
-  k_gmres_cycle_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, -1);
-  k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V);
-  for (int it = 0; it < restart; ++it) {
-    FL_SPMV_DISPATCH(G, k_apply_BA, P.A, W->dinv.p, V + it * ld, V + (it + 1) * ld);
-    k_mdot<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p, (int)gv);
-    k_gs_coeffs<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it);
-    k_gs_update<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, W->part.p);
-    k_gmres_step<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gv, it, restart);
-    k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V + (it + 1) * ld);
-  }
-  k_gmres_backsolve<<<1, 32, 0, s>>>(st, restart);
-  k_gmres_update_x<<<gv, kThreads, 0, s>>>(n, st, V, ld, W->y.p);
-  k_gmres_cycle_end<<<1, 32, 0, s>>>(st);
+  gmres_cycle_launch(P.G, P.A, P.W, P.n, P.restart, P.gsp, P.gv, s);
 }
 
 void cg_iterate(CgPlan& P, cudaStream_t s) {
