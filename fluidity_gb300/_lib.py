@@ -68,7 +68,7 @@ class SolverOpts(C.Structure):
         ("ksp_type", C.c_int32), ("restart", C.c_int32), ("rtol", C.c_double),
         ("atol", C.c_double), ("dtol", C.c_double), ("max_its", C.c_int32),
         ("start_from_zero", C.c_int32), ("precision", C.c_int32), ("inner_rtol", C.c_double),
-        ("norm_type", C.c_int32), ("pad", C.c_int32),
+        ("norm_type", C.c_int32), ("schedule", C.c_int32),
     ]
 
 

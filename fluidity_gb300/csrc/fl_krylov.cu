@@ -60,14 +60,16 @@ struct KspState {
   // fp32 CG with reliable updates
   int rel, hold, outer;  // reliable mode; an update is pending; updates done
   double rmax, rdelta;   // largest recurrence residual since the last update; trigger ratio
+  // true residual report
+  double true_r2, b2;
+  // GMRES arrays (written before they are read in every cycle, so only the
+  // scalars above are uploaded and read back)
   double grs[kMaxRestart + 2];
   double cc[kMaxRestart + 1], ss[kMaxRestart + 1];
   double hh[(kMaxRestart + 1) * (kMaxRestart + 1)];   // column-major, ld = restart+1
   double lhh[kMaxRestart + 1];                        // current Gram-Schmidt coefficients
   double nrs[kMaxRestart + 1];
   double tt;
-  // true residual report
-  double true_r2, b2;
 };
 
 // An instantiated graph and the launch arguments it was captured with.
@@ -223,7 +225,7 @@ __device__ __forceinline__ df warp_sum_df(df v) {
 }
 
 template <int THREADS>
-__device__ __forceinline__ double block_sum_df(df v, float2* red) {
+__device__ __forceinline__ df block_sum_dfv(df v, float2* red) {
   v = warp_sum_df(v);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) red[w] = make_float2(v.hi, v.lo);
@@ -233,7 +235,12 @@ __device__ __forceinline__ double block_sum_df(df v, float2* red) {
     v = warp_sum_df({q.x, q.y});
   }
   __syncthreads();
-  return df_to_double(v);
+  return v;  // valid in thread 0
+}
+
+template <int THREADS>
+__device__ __forceinline__ double block_sum_df(df v, float2* red) {
+  return df_to_double(block_sum_dfv<THREADS>(v, red));
 }
 
 template <int THREADS>
@@ -827,9 +834,20 @@ __global__ void __launch_bounds__(kThreads) k_gmres_arnoldi(SpArgs A, const doub
 // Hessenberg column of iteration `it` from h_j (lhh) and ||v_{it+1}||^2 = nn,
 // happy breakdown, KSPGMRESUpdateHessenberg and the convergence test (the
 // body of KSPGMRESCycle after the orthogonalisation).  Called by every thread
-// of one block: the column and the earlier rotations are staged in shared
-// memory so the serial rotation chain runs at shared-memory latency.
-__device__ void gmres_step(KspState& S, double nn, int it, int restart) {
+// of one block; warp 0 works.  A dependent FP64 operation takes ~64 SM cycles
+// on GB300 (a square root or a division ~650), so the serial part is kept
+// short:
+//  - the earlier rotations applied to the new column are the linear
+//    recurrence carry_j = -s_{j-1} carry_{j-1} + c_{j-1} h_j (carry_0 = h_0,
+//    rotated h_{j-1} = c_{j-1} carry_{j-1} + s_{j-1} h_j, rotated h_it =
+//    carry_it), evaluated as a warp scan of the affine maps (32 rotations
+//    per five shuffle steps) instead of `it` dependent steps;
+//  - the happy-breakdown quotient |tt / grs| is only formed when tt < 1e-30,
+//    where it can decide the test;
+//  - 1 / tt (the caller's scaling, when `inv` is given) and the new rotation's
+//    1 / rr come from rsqrt beside the square roots.
+// The arithmetic is KSPGMRESUpdateHessenberg's up to rounding.
+__device__ void gmres_step(KspState& S, double nn, int it, int restart, double* inv = nullptr) {
   __shared__ double col[kMaxRestart + 2], rc[kMaxRestart + 1], rs[kMaxRestart + 1];
   const int ld = restart + 1;
   double* hc = S.hh + (int64_t)it * ld;
@@ -839,50 +857,75 @@ __device__ void gmres_step(KspState& S, double nn, int it, int restart) {
     rs[j] = S.ss[j];
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
     const double tt = sqrt(nn);
-    S.tt = tt;
-    col[it + 1] = tt;
-    double hapbnd = fabs(tt / S.grs[it]);
-    if (hapbnd > 1e-30) hapbnd = 1e-30;
-    const bool hapend = tt < hapbnd;
-    for (int j = 1; j <= it; ++j) {
-      const double h0 = col[j - 1], h1 = col[j];
-      col[j - 1] = rc[j - 1] * h0 + rs[j - 1] * h1;
-      col[j] = rc[j - 1] * h1 - rs[j - 1] * h0;
+    if (lane == 0) {
+      S.tt = tt;
+      if (inv) *inv = nn > 0.0 ? rsqrt(nn) : 1.0;
     }
-    bool null_col = false;
-    double res = 0.0;
-    if (!hapend) {
-      const double h0 = col[it], h1 = col[it + 1];
-      const double rr = sqrt(h0 * h0 + h1 * h1);
-      if (rr == 0.0) {
-        S.reason = FL_DIVERGED_NULL;
-        S.done = 1;
-        S.it = it;  // this column is not used
-        null_col = true;
-      } else {
-        const double c = h0 / rr, sn = h1 / rr;
-        S.cc[it] = c;
-        S.ss[it] = sn;
-        const double g = S.grs[it];
-        S.grs[it + 1] = -(sn * g);
-        S.grs[it] = c * g;
-        col[it] = c * h0 + sn * h1;
-        res = fabs(S.grs[it + 1]);
+    // earlier rotations: scan of x -> A x + B over the chunk's rotations
+    double carry = col[0];
+    for (int c0 = 1; c0 <= it; c0 += 32) {
+      const int j = c0 + lane;
+      const bool act = j <= it;
+      const double cj = act ? rc[j - 1] : 1.0, sj = act ? rs[j - 1] : 0.0, hj = act ? col[j] : 0.0;
+      double A = act ? -sj : 1.0, B = act ? cj * hj : 0.0;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const double Ap = __shfl_up_sync(0xffffffffu, A, d), Bp = __shfl_up_sync(0xffffffffu, B, d);
+        if (lane >= d) {
+          B = fma(A, Bp, B);
+          A = A * Ap;
+        }
       }
+      const double cur = fma(A, carry, B);  // carry_j
+      double prev = __shfl_up_sync(0xffffffffu, cur, 1);
+      if (lane == 0) prev = carry;
+      __syncwarp();
+      if (act) col[j - 1] = fma(cj, prev, sj * hj);
+      carry = __shfl_sync(0xffffffffu, cur, min(31, it - c0));
+      __syncwarp();
     }
-    if (!null_col) {
-      S.it = it + 1;
-      S.its += 1;
-      converged_test(S, S.its, res);
-      if (hapend && !S.reason) {
-        S.reason = FL_DIVERGED_BREAKDOWN;
-        S.done = 1;
+    if (lane == 0) {
+      col[it] = carry;
+      col[it + 1] = tt;
+      // hapbnd = min(|tt / grs(it)|, 1e-30); hapend = tt < hapbnd
+      const bool hapend = tt < 1e-30 && tt < fabs(tt / S.grs[it]);
+      bool null_col = false;
+      double res = 0.0;
+      if (!hapend) {
+        const double h0 = carry, h1 = tt;
+        const double r2 = h0 * h0 + h1 * h1;
+        if (r2 == 0.0) {
+          S.reason = FL_DIVERGED_NULL;
+          S.done = 1;
+          S.it = it;  // this column is not used
+          null_col = true;
+        } else {
+          const double ri = rsqrt(r2);
+          const double c = h0 * ri, sn = h1 * ri;
+          S.cc[it] = c;
+          S.ss[it] = sn;
+          const double g = S.grs[it];
+          S.grs[it + 1] = -(sn * g);
+          S.grs[it] = c * g;
+          col[it] = c * h0 + sn * h1;
+          res = fabs(S.grs[it + 1]);
+        }
       }
-      if (!S.done && S.its >= S.max_its) {
-        S.reason = FL_DIVERGED_ITS;  // KSPSolve_GMRES: itcount >= max_it
-        S.done = 1;
+      if (!null_col) {
+        S.it = it + 1;
+        S.its += 1;
+        converged_test(S, S.its, res);
+        if (hapend && !S.reason) {
+          S.reason = FL_DIVERGED_BREAKDOWN;
+          S.done = 1;
+        }
+        if (!S.done && S.its >= S.max_its) {
+          S.reason = FL_DIVERGED_ITS;  // KSPSolve_GMRES: itcount >= max_it
+          S.done = 1;
+        }
       }
     }
   }
@@ -997,15 +1040,11 @@ __global__ void k_norm2_pair(int n, const double* __restrict__ v, const double* 
 // warp: lane l keeps the right-hand sides t_l, t_{l+32}; after nrs_k is
 // known every row above it subtracts H(i,k) nrs_k (column k of H is
 // contiguous, so each step is one coalesced load).
-__global__ void k_gmres_backsolve(KspState* st, int restart) {
-  note_launch();
-  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
-  KspState& S = *st;
-  if (!S.live) return;
+__device__ void gmres_backsolve_warp(KspState& S, int restart) {
   const int ld = restart + 1;
   const int last = S.it - 1;
   if (last < 0) return;
-  const int lane = threadIdx.x;
+  const int lane = threadIdx.x & 31;
   double t0 = lane <= last ? S.grs[lane] : 0.0;
   double t1 = lane + 32 <= last ? S.grs[lane + 32] : 0.0;
   for (int k = last; k >= 0; --k) {
@@ -1019,6 +1058,13 @@ __global__ void k_gmres_backsolve(KspState* st, int restart) {
     t0 -= h0 * y;
     t1 -= h1 * y;
   }
+}
+
+__global__ void k_gmres_backsolve(KspState* st, int restart) {
+  note_launch();
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  if (!st->live) return;
+  gmres_backsolve_warp(*st, restart);
 }
 
 __global__ void k_gmres_update_x(int n, const KspState* st, const double* __restrict__ V, int64_t ld,
@@ -1059,6 +1105,361 @@ __global__ void k_gmres_cycle_end(KspState* st) {
     S.done = 1;
   }
   S.guess_zero = 0;
+}
+
+// ------------------------------------------- GMRES in one cooperative launch --
+// The whole of KSPSolve_GMRES for a small system in one launch, for systems
+// where a launch per Arnoldi phase costs more than the phase.  Each block
+// owns fixed rows (passes of kPRows rows, kPG lanes per row: row group
+// blockIdx.x + k nb) and keeps their slice of the Krylov basis in shared
+// memory, so only the SpMV gathers and the reduction partials cross blocks.
+// Every block also keeps an identical copy of the solver state in shared
+// memory: after each grid barrier every block sums the same partials in the
+// same order, so all copies take the same decisions (convergence, restarts)
+// without a broadcast.  One Arnoldi step is two phases and two barriers:
+//   A: w = B A v_it on the block's rows, gathering the unnormalised U and
+//      scaling the row sums by inv = 1 / ||U||; the rows of v_it = U inv
+//      stored; the block's partials of w . v_j, j <= it
+//   B: h_j from the partials; U = w - sum_j h_j v_j (VecMAXPY) on the
+//      block's rows, published for the next gathers; partials of ||U||^2
+//   then every block: tt = ||U||, the Hessenberg column, rotations and the
+//   convergence test (gmres_step).
+// FP64 latency shapes the layout (a dependent FP64 operation ~64 SM cycles
+// on GB300): short FMA chains (kPG lanes per row; dot products lane-per-basis-
+// vector over a warp's rows, then a tree over the warps), and the cross-block
+// partials published and summed in double-float on the FP32 pipes.  The
+// Krylov space and the tests are KSPGMRESCycle's; the sums run in another
+// order than the launch-per-phase schedule's, so results agree to rounding.
+// Data that other blocks write during the launch (U, y, the partials) is
+// read at L2 (__ldcg).
+constexpr unsigned long long kBarrierWaitNs = 1000000000ull;  // a grid barrier gives up after 1 s
+constexpr int kPG = 8;                   // lanes per row
+constexpr int kPRows = kThreads / kPG;   // rows per pass
+
+struct PersistArgs {
+  SpArgs A;                      // A.st: the global state (read at the start, published at the end)
+  const double* dinv;            // Jacobi inverse diagonal (ghost rows 1 / pivot)
+  const double* b;               // right-hand side with the ghost rows lifted
+  double* y;                     // iterate
+  double* U;                     // unnormalised next basis vector (gathered by the SpMV)
+  float2* part;                  // double-float partials: (kMaxRestart + 1) * nb of h, then 2 * nb
+  unsigned long long* bar;       // [0] arrivals (monotonic), [1] error flag
+  int restart;
+  int npass;                     // row passes per block
+  int withhold;                  // failure-injection test: this block never arrives (-1: none)
+  unsigned long long wait_ns;    // limit of one barrier wait
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long atom_add_acq_rel_u64(unsigned long long* p, unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
+
+// Barrier over the blocks of a cooperative launch (all co-resident): an
+// arrival counter that only grows, barrier k complete once it reaches k nb.
+// The block's writes are ordered before its arrival by __syncthreads and the
+// release half of the atomic; the acquiring load orders the reads after.  The
+// wait is bounded: after wait_ns (kBarrierWaitNs unless a test shortens it),
+// or once another block has raised the error flag, the block raises the flag
+// and every thread gets false (the caller leaves its loops and returns; the
+// host reads the flag).
+__device__ bool grid_barrier(unsigned long long* bar, unsigned long long wait_ns) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int good = 1;
+    const unsigned long long nb = gridDim.x;
+    const unsigned long long old = atom_add_acq_rel_u64(bar, 1ull);
+    const unsigned long long target = (old / nb + 1) * nb;
+    if (old + 1 < target) {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_u64(bar) < target) {
+        if (global_ns() - t0 > wait_ns || ld_acquire_u64(bar + 1) != 0ull) {
+          atomicExch(bar + 1, 1ull);
+          good = 0;
+          break;
+        }
+      }
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Row sum of A x over G lanes, x read at L2.
+template <int G>
+__device__ __forceinline__ double row_dot_cg(const int32_t* __restrict__ findrm, const int32_t* __restrict__ colm,
+                                             const double* __restrict__ val, const double* x, int row, int sub,
+                                             bool valid) {
+  int b = 0, e = 0;
+  if (valid) {
+    b = __ldg(findrm + row);
+    e = __ldg(findrm + row + 1);
+  }
+  double s = 0.0;
+  for (int k = b + sub; k < e; k += G) s = fma(__ldg(val + k), __ldcg(x + __ldg(colm + k)), s);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
+__device__ __forceinline__ float2 df_pack(df v) { return make_float2(v.hi, v.lo); }
+
+// Shared memory of k_gmres_persistent beyond its static arrays: the block's
+// rows of v_0..v_restart (row stride rows + 1, odd, so lanes reading one row
+// of different vectors fall in different banks), of w and of U (rows past N
+// hold zeros).
+inline size_t persist_smem_bytes(int restart, int npass) {
+  const size_t rows = (size_t)npass * kPRows;
+  return ((size_t)(restart + 1) * (rows + 1) + 2 * rows) * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_gmres_persistent(PersistArgs P) {
+  note_launch();
+  __shared__ KspState S;
+  __shared__ float2 redf[kThreads / 32];
+  __shared__ double red8[kThreads / 32][2 * 32];  // dot partials of the warps, j < 64
+  __shared__ double sred[2];
+  __shared__ double sinv;
+  extern __shared__ double dyn[];
+  const SpArgs& A = P.A;
+  const int n = A.n, nb = gridDim.x, restart = P.restart;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int sub = lane & (kPG - 1);
+  const int rows = P.npass * kPRows, vs = rows + 1;
+  double* Vs = dyn;  // [j * vs + lr]; local row lr = k kPRows + r <-> row (blockIdx.x + k nb) kPRows + r
+  double* Ws = dyn + (size_t)(restart + 1) * vs;
+  double* Us = Ws + rows;
+  double* U = P.U;
+  float2* part_h = P.part;                                    // [j * nb + b]
+  float2* part_n = P.part + (int64_t)(kMaxRestart + 1) * nb;  // [b], [nb + b]
+  auto grow = [&](int lr) { return (blockIdx.x + (lr / kPRows) * nb) * kPRows + lr % kPRows; };
+  if ((int)blockIdx.x == P.withhold) return;  // failure-injection test: the others' first barrier runs out
+  {
+    const int* src = reinterpret_cast<const int*>(A.st);
+    int* dst = reinterpret_cast<int*>(&S);
+    for (int k = tid; k < (int)(offsetof(KspState, grs) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const double piv = S.pivot;
+  bool ok = true;
+  for (int cycle = 0; ok && cycle <= S.max_its; ++cycle) {
+    // KSPInitialResidual: U = B (b - A y) (zero guess: B b); ||U||^2, ||B b||^2
+    const bool gz = S.guess_zero;
+    double zz = 0.0, bb = 0.0;
+    for (int k = 0; k < P.npass; ++k) {
+      const int lr = k * kPRows + tid / kPG, row = grow(lr);
+      double ay = 0.0;
+      if (!gz) ay = row_dot_cg<kPG>(A.findrm, A.colm, A.val, P.y, row, sub, row < n);
+      if (sub == 0) {
+        double zi = 0.0;
+        if (row < n) {
+          if (A.ghost && A.ghost[row]) ay = piv * __ldcg(P.y + row);
+          const double bi0 = P.b[row], di = P.dinv[row];
+          zi = (bi0 - ay) * di;
+          const double bi = bi0 * di;
+          U[row] = zi;
+          zz = fma(zi, zi, zz);
+          bb = fma(bi, bi, bb);
+        }
+        Us[lr] = zi;
+      }
+    }
+    {
+      const df zs = block_sum_dfv<kThreads>(df_from_double(zz), redf);
+      const df bs = block_sum_dfv<kThreads>(df_from_double(bb), redf);
+      if (tid == 0) {
+        part_n[blockIdx.x] = df_pack(zs);
+        part_n[nb + blockIdx.x] = df_pack(bs);
+      }
+    }
+    if (!(ok = grid_barrier(P.bar, P.wait_ns))) break;
+    {
+      // the cycle start of k_gmres_cycle_start, on every block's copy
+      if (warp < 2) {
+        const float2* p = part_n + warp * nb;
+        df a = {0.0f, 0.0f};
+        for (int b = lane; b < nb; b += 32) {
+          const float2 q = __ldcg(p + b);
+          a = df_add(a, {q.x, q.y});
+        }
+        a = warp_sum_df(a);
+        if (lane == 0) sred[warp] = df_to_double(a);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const int first = S.gm_first;
+        S.gm_first = 0;
+        const double res = sqrt(sred[0]);
+        if (first) {
+          S.snorm_b = sqrt(sred[1]);
+          S.its = 0;
+          S.reason = 0;
+          S.done = 0;
+        }
+        S.grs[0] = res;
+        S.it = 0;
+        S.hapend = 0;
+        S.tt = res;
+        if (res == 0.0) {
+          S.reason = FL_CONVERGED_ATOL;
+          S.done = 1;
+          S.rnorm = 0.0;
+          if (first) S.rnorm0 = 0.0;
+        } else {
+          converged_test(S, S.its, res);
+        }
+        sinv = res != 0.0 ? 1.0 / res : 1.0;
+      }
+      __syncthreads();
+    }
+    for (int it = 0; it < restart && !S.done; ++it) {
+      // phase A: w = B A v_it on the block's rows, v_it's rows scaled
+      const double inv = sinv;
+      double* Vi = Vs + (size_t)it * vs;
+      for (int k = 0; k < P.npass; ++k) {
+        const int lr = k * kPRows + tid / kPG, row = grow(lr);
+        double s = row_dot_cg<kPG>(A.findrm, A.colm, A.val, U, row, sub, row < n);
+        if (sub == 0) {
+          const double ui = Us[lr] * inv;
+          if (row < n) {
+            s = (A.ghost && A.ghost[row]) ? piv * ui : s * inv;
+            s *= P.dinv[row];
+          } else {
+            s = 0.0;
+          }
+          Ws[lr] = s;
+          Vi[lr] = ui;
+        }
+      }
+      __syncthreads();
+      // partials of w . v_j: lane j (and j + 32) over the warp's rows, then
+      // a tree over the warps
+      {
+        const int cr = rows / nw;
+        double a0 = 0.0, a1 = 0.0;
+        for (int lr = warp * cr; lr < (warp + 1) * cr; ++lr) {
+          const double wr = Ws[lr];
+          if (lane <= it) a0 = fma(wr, Vs[(size_t)lane * vs + lr], a0);
+          if (lane + 32 <= it) a1 = fma(wr, Vs[(size_t)(lane + 32) * vs + lr], a1);
+        }
+        red8[warp][lane] = a0;
+        red8[warp][lane + 32] = a1;
+        __syncthreads();
+        const int j = tid & 63, w2 = tid >> 6;
+        red8[w2][j] += red8[w2 + 4][j];
+        __syncthreads();
+        if (tid < 128) red8[w2][j] += red8[w2 + 2][j];
+        __syncthreads();
+        if (tid < 64 && j <= it) part_h[(int64_t)j * nb + blockIdx.x] = df_pack(df_from_double(red8[0][j] + red8[1][j]));
+      }
+      if (!(ok = grid_barrier(P.bar, P.wait_ns))) break;
+      // phase B: h_j (classical Gram-Schmidt): warp j % nw sums the blocks'
+      // partials of h_j, four j at a time
+      for (int j0 = warp; j0 <= it; j0 += 4 * nw) {
+        df a[4] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+        for (int b = lane; b < nb; b += 32) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int j = j0 + q * nw;
+            if (j <= it) {
+              const float2 v = __ldcg(part_h + (int64_t)j * nb + b);
+              a[q] = df_add(a[q], {v.x, v.y});
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const df t = warp_sum_df(a[q]);
+          if (lane == 0 && j0 + q * nw <= it) S.lhh[j0 + q * nw] = df_to_double(t);
+        }
+      }
+      __syncthreads();
+      // U = w - sum_j h_j v_j: kPG threads per row, thread t8 takes j = t8 (mod kPG)
+      double nn = 0.0;
+      for (int k = 0; k < P.npass; ++k) {
+        const int lr = k * kPRows + tid / kPG, row = grow(lr);
+        double sum = 0.0;
+        for (int j = sub; j <= it; j += kPG) sum = fma(S.lhh[j], Vs[(size_t)j * vs + lr], sum);
+#pragma unroll
+        for (int o = kPG / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, kPG);
+        if (sub == 0) {
+          double u = 0.0;
+          if (row < n) {
+            u = Ws[lr] - sum;
+            U[row] = u;
+          }
+          Us[lr] = u;
+          nn = fma(u, u, nn);
+        }
+      }
+      {
+        const df ns = block_sum_dfv<kThreads>(df_from_double(nn), redf);
+        if (tid == 0) part_n[blockIdx.x] = df_pack(ns);
+      }
+      if (!(ok = grid_barrier(P.bar, P.wait_ns))) break;
+      // every block: ||U||, Hessenberg column, rotations, convergence test
+      if (warp == 0) {
+        df a = {0.0f, 0.0f};
+        for (int b = lane; b < nb; b += 32) {
+          const float2 q = __ldcg(part_n + b);
+          a = df_add(a, {q.x, q.y});
+        }
+        a = warp_sum_df(a);
+        if (lane == 0) sred[0] = df_to_double(a);
+      }
+      __syncthreads();
+      gmres_step(S, sred[0], it, restart, &sinv);
+    }
+    if (!ok) break;
+    // KSPGMRESBuildSoln: y += V nrs on the block's rows
+    if (S.it > 0) {
+      if (warp == 0) gmres_backsolve_warp(S, restart);
+      __syncthreads();
+      const int last = S.it - 1;
+      for (int k = 0; k < P.npass; ++k) {
+        const int lr = k * kPRows + tid / kPG, row = grow(lr);
+        double sum = 0.0;
+        for (int j = sub; j <= last; j += kPG) sum = fma(S.nrs[j], Vs[(size_t)j * vs + lr], sum);
+#pragma unroll
+        for (int o = kPG / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o, kPG);
+        if (sub == 0 && row < n) P.y[row] = __ldcg(P.y + row) + sum;
+      }
+    }
+    // cycle end: KSPSolve_GMRES's itcount >= max_it; the restart's guess is nonzero
+    if (tid == 0) {
+      if (!S.done && S.its >= S.max_its) {
+        S.reason = FL_DIVERGED_ITS;
+        S.done = 1;
+      }
+      S.guess_zero = 0;
+    }
+    __syncthreads();
+    if (S.done) break;
+    if (!(ok = grid_barrier(P.bar, P.wait_ns))) break;
+  }
+  // publish the scalars (every copy is the same; block 0 writes them)
+  if (blockIdx.x == 0) {
+    if (tid == 0 && !ok) S.done = 1;
+    __syncthreads();
+    const int* src = reinterpret_cast<const int*>(&S);
+    int* dst = reinterpret_cast<int*>(A.st);
+    for (int k = tid; k < (int)(offsetof(KspState, grs) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  }
 }
 
 // ------------------------------------------------------------- finalise --
@@ -1534,6 +1935,34 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
 
   int outer = 0;
   const int chunk = 16;
+  // FP64 GMRES in one cooperative launch: schedule 2, or 0 up to
+  // FL_PERSIST_MAX_ROWS rows; one block per group of kThreads / G rows, at
+  // most one per SM, and only when that many blocks can be co-resident
+  bool persistent = false;
+  int pnb = 0, npass = 0;
+  size_t psmem = 0;
+  unsigned long long barrier_fault = 0;
+  if (o->ksp_type == 1 && !mixed && (o->schedule == 2 || (o->schedule == 0 && n <= FL_PERSIST_MAX_ROWS))) {
+    const void* fn = (const void*)k_gmres_persistent;
+    int per_sm = 0;
+    FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
+    const int groups = (n + kPRows - 1) / kPRows;
+    const int cap = std::max(1, per_sm) * num_sms();
+    npass = (groups + cap - 1) / cap;
+    pnb = (groups + npass - 1) / npass;
+    psmem = persist_smem_bytes(restart, npass);
+    cudaFuncAttributes fa;
+    FL_TRY_CUDA(cudaFuncGetAttributes(&fa, fn));
+    int dev = 0, optin = 0;
+    FL_TRY_CUDA(cudaGetDevice(&dev));
+    FL_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (fa.sharedSizeBytes + psmem <= (size_t)optin) {
+      FL_TRY_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
+      FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, psmem));
+      persistent = (int64_t)per_sm * num_sms() >= pnb;
+    }
+    if (persistent) FL_TRY(W->part.reserve((size_t)std::max(np, pnb) * (kMaxRestart + 3)));
+  }
   FL_TRY(ensure_sell(m, W, s));
   SellArgs SA{n, W->sptr.p, W->scol.p, ghost, st, W->sell16 ? W->soff.p : nullptr};
   const unsigned gsl = grid_for(n, kThreads, 8);
@@ -1588,6 +2017,18 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     }
     FL_TRY(gr.join());
     FL_TRY_CUDA(cudaGetLastError());
+  } else if (!mixed && persistent) {
+    // GMRES(restart) in one cooperative launch (k_gmres_persistent)
+    FL_TRY(W->ticket.reserve(4));
+    FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s));
+    const WaitTest& wt = wait_test();
+    PersistArgs P{A,      W->dinv.p, W->b.p, W->y.p, W->w.p, reinterpret_cast<float2*>(W->part.p),
+                  reinterpret_cast<unsigned long long*>(W->ticket.p), restart, npass, wt.withhold,
+                  wt.wait_ms > 0.0 ? (unsigned long long)(wt.wait_ms * 1e6) : kBarrierWaitNs};
+    void* args[] = {&P};
+    FL_TRY_CUDA(cudaLaunchCooperativeKernel((const void*)k_gmres_persistent, dim3(pnb), dim3(kThreads), args, psmem, s));
+    FL_TRY_CUDA(cudaMemcpyAsync(&barrier_fault, W->ticket.p + 2, sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, s));
   } else if (!mixed) {
     // GMRES(restart): one cycle with the restarts decided on the device,
     // captured as a graph and replayed until the device reports the end of
@@ -1753,8 +2194,12 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   k_copy_back<<<gv, kThreads, 0, s>>>(n, ghost, rhs, W->y.p, x);
   FL_TRY_CUDA(cudaGetLastError());
   KspState hs;
-  FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, sizeof(KspState), cudaMemcpyDeviceToHost, s));
+  FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, offsetof(KspState, grs), cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
+  if (barrier_fault) {
+    set_error("a bounded device wait ran out: a grid barrier of the cooperative GMRES solve");
+    return FL_ERR_TIMEOUT;
+  }
   rep->iterations = hs.its;
   rep->reason = hs.reason ? hs.reason : (o->max_its == 0 ? FL_DIVERGED_ITS : 0);
   rep->final_rnorm = hs.rnorm;

@@ -279,12 +279,16 @@ def apply_dirichlet_conditions(mesh: Mesh, rhs, inactive, nodes, values, t=None,
 
 def solver_options(*, ksp="cg", restart=30, rtol=1e-10, atol=0.0, dtol=1e5, max_its=10000,
                    start_from_zero=False, precision="fp64", inner_rtol=1e-5,
-                   norm="preconditioned") -> SolverOpts:
+                   norm="preconditioned", schedule="auto") -> SolverOpts:
     """solver/ options of the field (Solvers.F90:1566-1660); pc is always jacobi.
 
     ``norm`` is the residual norm of the convergence test (KSPSetNormType):
     "preconditioned" ||B r|| is PETSc's default; "unpreconditioned" ||r||
-    (CG only) makes rtol bound the true relative residual ||b - Ax|| / ||b||."""
+    (CG only) makes rtol bound the true relative residual ||b - Ax|| / ||b||.
+    ``schedule`` picks how an FP64 GMRES solve is launched: "graph" (a launch
+    per Arnoldi phase, cycles replayed as CUDA graphs), "persistent" (one
+    cooperative launch for the whole solve) or "auto" (persistent up to
+    FL_PERSIST_MAX_ROWS rows)."""
     o = SolverOpts()
     o.ksp_type = {"cg": 0, "gmres": 1}[ksp]
     o.restart, o.rtol, o.atol, o.dtol = restart, rtol, atol, dtol
@@ -292,6 +296,7 @@ def solver_options(*, ksp="cg", restart=30, rtol=1e-10, atol=0.0, dtol=1e5, max_
     o.precision = {"fp64": 0, "mixed": 1, "reliable": 2}[precision]
     o.inner_rtol = inner_rtol
     o.norm_type = {"preconditioned": 0, "unpreconditioned": 1}[norm]
+    o.schedule = {"auto": 0, "graph": 1, "persistent": 2}[schedule]
     return o
 
 

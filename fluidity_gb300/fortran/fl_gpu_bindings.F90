@@ -106,7 +106,7 @@ module fl_gpu_bindings
      real(c_double) :: rtol, atol, dtol
      integer(c_int32_t) :: max_its, start_from_zero, precision
      real(c_double) :: inner_rtol
-     integer(c_int32_t) :: norm_type, pad
+     integer(c_int32_t) :: norm_type, schedule
   end type fl_solver_opts
 
   ! assemble_divergence_matrix_cg options and surface mesh (by parts)
@@ -974,7 +974,7 @@ contains
     opts%precision = 0
     opts%inner_rtol = 1.0e-5
     opts%norm_type = 0
-    opts%pad = 0
+    opts%schedule = 0
 
     n = size(matrix, 1)
     inactive_ptr = c_null_ptr

@@ -229,14 +229,17 @@ int fl_gpu_assemble_advdif_faces(fl_mesh mesh, const fl_advdif_params* params, c
                                  const fl_fields* fields, double* val, double* rhs);
 
 /* Failure injection for tests of the bounded device waits (no counterpart in
- * the reference, whose loops do not wait on other threads).  Two kernels wait
- * on flags other threads set: the colouring dataflow of fl_gpu_mesh_register
- * (an element waits for the colours of its lower neighbours; limit about
- * 2 s) and the fused P1 pass (row tile 3; a row item waits for the element
- * items it reads; limit 2^22 polls).  After this call, in this process:
- * wait_ms > 0 bounds each such wait to about wait_ms milliseconds, and
- * withhold >= 0 keeps one flag unset -- the colour of element `withhold`, or
- * the completion of element-item group `withhold` -- so that the waits on it
+ * the reference, whose loops do not wait on other threads).  Three kernels
+ * wait on flags other threads set: the colouring dataflow of
+ * fl_gpu_mesh_register (an element waits for the colours of its lower
+ * neighbours; limit about 2 s), the fused P1 pass (row tile 3; a row item
+ * waits for the element items it reads; limit 2^22 polls) and the
+ * cooperative GMRES solve (schedule 2; its blocks meet at grid barriers;
+ * limit 1 s per barrier).  After this call, in this process: wait_ms > 0
+ * bounds each such wait to about wait_ms milliseconds, and withhold >= 0
+ * keeps one flag unset -- the colour of element `withhold`, the completion of
+ * element-item group `withhold`, or the barrier arrivals of block `withhold`
+ * of the cooperative solve (which leaves at once) -- so that the waits on it
  * run out.  The waiting side then records FL_ERR_TIMEOUT and stops; every
  * kernel finishes, the call returns FL_ERR_TIMEOUT ("a bounded device wait ran
  * out"), the CUDA context and other handles stay usable, and the next call
@@ -306,8 +309,18 @@ typedef struct {
                                 Jacobi); 1 = unpreconditioned ||r||, CG only
                                 (every precision), so rtol bounds the true
                                 relative residual ||b - A x|| / ||b||        */
-  int32_t pad;
+  int32_t schedule;          /* how an FP64 GMRES solve is launched:
+                                0 = automatic (1 above FL_PERSIST_MAX_ROWS
+                                rows, else 2); 1 = one kernel launch per
+                                Arnoldi phase, each restart cycle replayed
+                                as a CUDA graph; 2 = the whole solve in one
+                                cooperative launch, the blocks meeting at
+                                grid barriers (latency-bound small systems).
+                                Other solves ignore it.                      */
 } fl_solver_opts;
+
+/* Largest system (rows) that schedule 0 solves in one cooperative launch. */
+#define FL_PERSIST_MAX_ROWS 24576
 
 typedef struct {
   int32_t iterations;        /* KSPGetIterationNumber (inner total if mixed) */

@@ -37,7 +37,8 @@ def _members():
     out = []
     for k in range(2):
         p, T0, u = _tracer(X, kap[k], sc[k])
-        out.append((shared, p, ft.solver_options(ksp="gmres", restart=30, rtol=1e-10),
+        # the batch replays graph cycles: bitwise equal to the graph schedule
+        out.append((shared, p, ft.solver_options(ksp="gmres", restart=30, rtol=1e-10, schedule="graph"),
                     M.boundary_nodes(X),
                     {"t": torch.tensor(T0, device="cuda"), "u": torch.tensor(u, device="cuda")}))
     pois = ft.advdif_params(diffusivity=1.0, have_source=True, quad_degree=2)
@@ -100,8 +101,8 @@ def test_batch_converged_member_is_stable():
     b.add(m, slow, ft.solver_options(ksp="cg", rtol=1e-12), bc_nodes=bn,
           bc_values=np.zeros(bn.size), source=ff)
     reps = b.run()
-    _, _, _, x, urep = _unbatched(torch, m, fast, ft.solver_options(ksp="gmres", restart=5,
-                                                                    rtol=1e-10), bn, t=tt, u=uu)
+    _, _, _, x, urep = _unbatched(torch, m, fast, ft.solver_options(ksp="gmres", restart=5, rtol=1e-10,
+                                                                    schedule="graph"), bn, t=tt, u=uu)
     assert reps[0]["iterations"] == urep["iterations"] < reps[1]["iterations"]
     assert torch.equal(r_fast["x"], x)
     b.close()

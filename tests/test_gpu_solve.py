@@ -303,3 +303,76 @@ def test_projected_guess_is_the_a_norm_minimiser(O):
                                 dev + [dev[0] * 2.0], inactive=torch.from_numpy(ina).cuda())
     assert a1[-1] == 0.0
     assert np.abs(x1.cpu().numpy() - x0).max() <= 1e-12 * np.abs(xd).max()
+
+
+def _advdif_system(n):
+    nd, X = M.cube_mesh(n)
+    m = ft.Mesh(nd, X)
+    T0 = M.gaussian_tracer(X)
+    p = ft.advdif_params(theta=0.5, dt=0.01, have_mass=True, have_advection=True, diffusivity=1e-3)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, p, t=T0, velocity=M.advdif_velocity(X))
+    ina = np.zeros(m.N, dtype=np.uint8)
+    bn = M.boundary_nodes(X)
+    ft.apply_dirichlet_conditions(m, rhs, ina, bn, np.zeros(bn.size), t=T0, dt=0.01)
+    return m, val, rhs, ina
+
+
+@pytest.mark.parametrize("n,restart", [(8, 30), (8, 4), (32, 30), (32, 7)])
+def test_gmres_schedules_agree(O, n, restart):
+    """The cooperative single-launch GMRES and the graph-replayed one run the
+    same algorithm (same Krylov space, reductions in another order): same
+    reason, iterations within one, solutions within the solve tolerance; the
+    32^3 case (35,937 rows) takes several row passes per block."""
+    m, val, rhs, ina = _advdif_system(n)
+    x0 = np.random.default_rng(1).standard_normal(m.N) * 1e-2
+    res = {}
+    for sched in ("graph", "persistent"):
+        for guess in (False, True):
+            x = x0.copy() if guess else np.zeros(m.N)
+            o = ft.solver_options(ksp="gmres", restart=restart, rtol=1e-10, schedule=sched,
+                                  start_from_zero=not guess)
+            rep = ft.petsc_solve(m, x, val, rhs, o, inactive=ina)
+            res[sched, guess] = (x, rep)
+    for guess in (False, True):
+        (xg, rg), (xp, rp) = res["graph", guess], res["persistent", guess]
+        assert rg["reason"] == rp["reason"] == 2
+        assert abs(rg["iterations"] - rp["iterations"]) <= 1
+        scale = np.abs(xg).max()
+        assert np.abs(xg - xp).max() <= 1e-8 * scale
+        assert rp["true_rel_residual"] <= 1e-8
+    if n == 8:
+        ox, oits, oreason, _ = oracle_solve(O, m, val, rhs, ina, ksp="gmres", restart=restart, rtol=1e-10)
+        x, rep = res["persistent", False]
+        assert rep["reason"] == oreason and abs(rep["iterations"] - oits) <= 1
+        assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
+
+
+@pytest.mark.parametrize("sched", ["graph", "persistent"])
+def test_gmres_schedule_edge_cases(O, sched):
+    """Iteration limit inside and at the end of a cycle, a NaN right-hand
+    side, a zero right-hand side (converged at the first test) and every row
+    inactive, through both launch schedules."""
+    m, val, rhs, ina = _advdif_system(6)
+    for max_its in (3, 4, 8):
+        x = np.zeros(m.N)
+        rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(ksp="gmres", restart=4, rtol=1e-14,
+                                                               max_its=max_its, schedule=sched),
+                             inactive=ina)
+        assert rep["reason"] == -3 and rep["iterations"] == max_its
+    bad = rhs.copy()
+    bad[np.nonzero(ina == 0)[0][0]] = np.nan
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, bad, ft.solver_options(ksp="gmres", schedule=sched), inactive=ina)
+    assert rep["reason"] == -9
+    x = np.zeros(m.N)
+    zero = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, zero, ft.solver_options(ksp="gmres", schedule=sched, start_from_zero=True),
+                         inactive=ina)
+    ox, its, reason, _ = oracle_solve(O, m, val, zero, ina, ksp="gmres")
+    assert rep["reason"] == reason and rep["iterations"] == its == 0
+    assert np.array_equal(x, ox)
+    ina2 = np.ones(m.N, dtype=np.uint8)
+    g = np.linspace(-1.0, 1.0, m.N)
+    x = np.full(m.N, 7.0)
+    rep = ft.petsc_solve(m, x, val, g, ft.solver_options(ksp="gmres", schedule=sched), inactive=ina2)
+    assert np.array_equal(x, g) and rep["iterations"] == 0

@@ -70,3 +70,32 @@ def test_hook_arguments(hook):
     assert hook.fl_set_wait_test(3, 0.0) == 1        # a withheld flag needs a limit
     assert hook.fl_set_wait_test(-2, 1.0) == 1
     assert hook.fl_set_wait_test(-1, 0.0) == 0
+
+
+def test_gmres_grid_barrier_runs_out(O, hook):
+    """The cooperative GMRES solve: block 1 never arrives at a grid barrier,
+    the other blocks' waits run out, every block leaves, the solve reports
+    FL_ERR_TIMEOUT; the next solve in the same context matches the oracle."""
+    nd, X = M.cube_mesh(16)
+    m = ft.Mesh(nd, X)
+    T0 = M.gaussian_tracer(X)
+    p = ft.advdif_params(theta=0.5, dt=0.01, have_mass=True, have_advection=True, diffusivity=1e-3)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, p, t=T0, velocity=M.advdif_velocity(X))
+    ina = np.zeros(m.N, dtype=np.uint8)
+    bn = M.boundary_nodes(X)
+    ft.apply_dirichlet_conditions(m, rhs, ina, bn, np.zeros(bn.size), t=T0, dt=0.01)
+    opts = ft.solver_options(ksp="gmres", restart=30, rtol=1e-10, schedule="persistent")
+    assert hook.fl_set_wait_test(1, 5.0) == 0       # block 1 of the cooperative solve never arrives
+    with pytest.raises(_lib.FlError) as err:
+        ft.petsc_solve(m, np.zeros(m.N), val, rhs, opts, inactive=ina)
+    assert err.value.status == FL_ERR_TIMEOUT
+    assert "bounded device wait ran out" in str(err.value)
+    assert hook.fl_set_wait_test(-1, 0.0) == 0
+    x = np.zeros(m.N)
+    rep = ft.petsc_solve(m, x, val, rhs, opts, inactive=ina)
+    s = m.sparsity()
+    ox, oits, oreason, _ = O.petsc_solve(s.findrm.astype(np.int64), s.colm, val, ina, rhs, ksp="gmres",
+                                         restart=30, rtol=1e-10)
+    assert rep["reason"] == oreason == 2 and abs(rep["iterations"] - oits) <= 1
+    assert np.abs(x - ox).max() <= 1e-8 * np.abs(ox).max()
+    m.close()
