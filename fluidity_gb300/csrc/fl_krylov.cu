@@ -248,6 +248,14 @@ __device__ __forceinline__ double block_sum_df(double v, float2* red) {
   return block_sum_df<THREADS>(df_from_double(v), red);
 }
 
+// acc + a*b in double-float: the product of the 48-bit splits of a and b
+// (relative error ~2^-47), summed in double-float.  GB300 runs FP64 FMAs at
+// about 1/70 of its FP32 rate (measured 1.6 per SM clock), so the Krylov dot
+// products run here and the FP64 pipe keeps the vector updates and the SpMV.
+__device__ __forceinline__ df df_dot_acc(df acc, double a, double b) {
+  return df_add(acc, df_mul(df_from_double(a), df_from_double(b)));
+}
+
 // Exact product of two floats accumulated in double-float.
 __device__ __forceinline__ df df_fma_ff(float a, float b, df acc) {
   const float p = a * b;
@@ -605,16 +613,16 @@ __global__ void k_cg_ap(SellArgs A, const double* __restrict__ sval, const doubl
   if (st->done) return;
   const int i = st->cg_i;
   const double piv = st->pivot;
-  double pw = 0.0;
+  df pw = {0.0f, 0.0f};
   for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x) {
     double s = sell_row_dot(A, sval, p, row);
     const double pi = p[row];
     if (A.ghost && A.ghost[row]) s = piv * pi;
     w[row] = s;
-    pw += pi * s;
+    pw = df_dot_acc(pw, pi, s);
   }
-  pw = block_sum_df<kThreads>(pw, redf);
-  if (threadIdx.x == 0) part[blockIdx.x] = pw;
+  const double pws = block_sum_df<kThreads>(pw, redf);
+  if (threadIdx.x == 0) part[blockIdx.x] = pws;
   if (!last_block(ticket)) return;
   const double dpi = reduce_partials(part, gridDim.x, red);
   if (threadIdx.x == 0) {
@@ -641,7 +649,7 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
   const int i = st->cg_i;
   const double a = st->alpha;
   const bool unprec = st->unprec;
-  double zz = 0.0, zr = 0.0, rr = 0.0;
+  df zz = {0.0f, 0.0f}, zr = {0.0f, 0.0f}, rr = {0.0f, 0.0f};
   // two rows per thread (16-byte accesses); the last odd row by the last thread
   const int n2 = n >> 1;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2; k += gridDim.x * blockDim.x) {
@@ -657,14 +665,11 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
     reinterpret_cast<double2*>(y)[k] = yv;
     reinterpret_cast<double2*>(r)[k] = make_double2(r0, r1);
     reinterpret_cast<double2*>(z)[k] = make_double2(z0, z1);
-    zz += z0 * z0;
-    zz += z1 * z1;
-    zr += z0 * r0;
-    zr += z1 * r1;
-    if (unprec) {
-      rr += r0 * r0;
-      rr += r1 * r1;
-    }
+    const df z0d = df_from_double(z0), z1d = df_from_double(z1);
+    const df r0d = df_from_double(r0), r1d = df_from_double(r1);
+    zz = df_add(zz, df_add(df_mul(z0d, z0d), df_mul(z1d, z1d)));
+    zr = df_add(zr, df_add(df_mul(z0d, r0d), df_mul(z1d, r1d)));
+    if (unprec) rr = df_add(rr, df_add(df_mul(r0d, r0d), df_mul(r1d, r1d)));
   }
   if ((n & 1) && blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) {
     const int k = n - 1;
@@ -673,17 +678,17 @@ __global__ void k_cg_xr(int n, KspState* st, const double* __restrict__ p, const
     const double zk = rk * dinv[k];
     r[k] = rk;
     z[k] = zk;
-    zz += zk * zk;
-    zr += zk * rk;
-    rr += rk * rk;
+    zz = df_dot_acc(zz, zk, zk);
+    zr = df_dot_acc(zr, zk, rk);
+    rr = df_dot_acc(rr, rk, rk);
   }
-  zz = block_sum_df<kThreads>(zz, redf);
-  zr = block_sum_df<kThreads>(zr, redf);
-  if (unprec) rr = block_sum_df<kThreads>(rr, redf);
+  const double zzb = block_sum_df<kThreads>(zz, redf);
+  const double zrb = block_sum_df<kThreads>(zr, redf);
+  const double rrb = unprec ? block_sum_df<kThreads>(rr, redf) : 0.0;
   if (threadIdx.x == 0) {
-    part[blockIdx.x] = zz;
-    part[gridDim.x + blockIdx.x] = zr;
-    if (unprec) part[2 * gridDim.x + blockIdx.x] = rr;
+    part[blockIdx.x] = zzb;
+    part[gridDim.x + blockIdx.x] = zrb;
+    if (unprec) part[2 * gridDim.x + blockIdx.x] = rrb;
   }
   if (!last_block(ticket)) return;
   const double zzs = reduce_partials(part, gridDim.x, red);
