@@ -311,6 +311,25 @@ __device__ __forceinline__ double row_dot(const int32_t* __restrict__ findrm, co
 }
 
 
+// row_dot of the gathered vector x * scale (the rounded products are the
+// values of the scaled vector).
+template <int G>
+__device__ __forceinline__ double row_dot_scaled(const int32_t* __restrict__ findrm,
+                                                 const int32_t* __restrict__ colm, const double* __restrict__ val,
+                                                 const double* __restrict__ x, double scale, int row, int sub,
+                                                 bool valid = true) {
+  int b = 0, e = 0;
+  if (valid) {
+    b = __ldg(findrm + row);
+    e = __ldg(findrm + row + 1);
+  }
+  double s = 0.0;
+  for (int k = b + sub; k < e; k += G) s += __ldg(val + k) * (__ldg(x + __ldg(colm + k)) * scale);
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+  return s;
+}
+
 // ---------------------------------------------------------------- setup --
 // diag / ghost pivot inputs: min and max of |diag| over all rows.
 __global__ void k_diag(SpArgs A, const int32_t* __restrict__ centrm, double* __restrict__ dinv,
@@ -774,41 +793,49 @@ __global__ void k_cg_open(KspState* st) {
 }
 
 // --------------------------------------------------------------- GMRES --
-// One Arnoldi step of KSPGMRESCycle in three launches, each global reduction
+// One Arnoldi step of KSPGMRESCycle in two launches, each global reduction
 // finished by the last block to retire (last_block: block order, so the sums
-// are deterministic):
-//   k_gmres_arnoldi: v_{it+1} = B (A v_it) (KSP_PCApplyBAorAB, left
-//                    preconditioning) and the partials of v_{it+1} . v_j,
-//                    j = 0..it; last block: h_j (VecMDot, classical
-//                    Gram-Schmidt)
-//   k_gmres_orth:    v_{it+1} -= sum_j h_j v_j (VecMAXPY), partials of
-//                    ||v_{it+1}||^2; last block: gmres_step (Hessenberg
-//                    column, rotations, convergence test)
-//   k_scale_vec:     v_{it+1} /= ||v_{it+1}|| (VecNormalize)
-// A launch whose state is `done` returns at once.
+// are deterministic).  The orthogonalised next vector is kept unnormalised
+// in U, and the step that uses it normalises it on the fly (VecNormalize):
+//   k_gmres_arnoldi: inv = 1 / ||U||; v_it = U inv on the block's rows;
+//                    w = B (A v_it) (KSP_PCApplyBAorAB, left preconditioning)
+//                    gathering U * inv, the same rounded values as the scaled
+//                    v_it; the partials of w . v_j, j = 0..it; last block:
+//                    h_j (VecMDot, classical Gram-Schmidt)
+//   k_gmres_orth:    U = w - sum_j h_j v_j (VecMAXPY), partials of ||U||^2;
+//                    last block: gmres_step (Hessenberg column, rotations,
+//                    convergence test; ||U|| into the state)
+// w is written to v_{it+1}'s slot, which the next step overwrites with the
+// scaled vector; no launch reads and writes the same vector.  A launch whose
+// state is `done` returns at once.
 template <int G>
 __global__ void __launch_bounds__(kThreads) k_gmres_arnoldi(SpArgs A, const double* __restrict__ dinv, double* V,
-                                                            int64_t ld, int it, double* __restrict__ part,
-                                                            unsigned* ticket) {
+                                                            const double* __restrict__ U, int64_t ld, int it,
+                                                            double* __restrict__ part, unsigned* ticket) {
   note_launch();
-  __shared__ double sw[kThreads / G];
+  __shared__ double sw[kThreads / G], su[kThreads / G];
   __shared__ double sacc[kMaxRestart + 1];
   KspState* st = A.st;
   if (st->done) return;
   const double piv = st->pivot;
-  const double* vin = V + it * ld;
+  const double tt = st->tt;
+  const double inv = tt != 0.0 ? 1.0 / tt : 1.0;
+  double* vin = V + it * ld;
   double* vout = V + (it + 1) * ld;
   const int lane = threadIdx.x & 31, sub = lane & (G - 1), warp = threadIdx.x >> 5;
   const int nw = blockDim.x >> 5, gpb = blockDim.x / G;
   for (int j = threadIdx.x; j <= it; j += blockDim.x) sacc[j] = 0.0;
   for (int base = blockIdx.x * gpb; base < A.n; base += gridDim.x * gpb) {
     const int row = base + threadIdx.x / G;
-    double s = row_dot<G>(A.findrm, A.colm, A.val, vin, row, sub, row < A.n);
+    double s = row_dot_scaled<G>(A.findrm, A.colm, A.val, U, inv, row, sub, row < A.n);
     if (row < A.n && sub == 0) {
-      if (A.ghost && A.ghost[row]) s = piv * vin[row];
+      const double ui = U[row] * inv;
+      if (A.ghost && A.ghost[row]) s = piv * ui;
       s *= dinv[row];
+      vin[row] = ui;
       vout[row] = s;
       sw[threadIdx.x / G] = s;
+      su[threadIdx.x / G] = ui;
     }
     __syncthreads();
     // the pass's rows dotted with each v_j: warp j % nw owns h_j
@@ -816,7 +843,11 @@ __global__ void __launch_bounds__(kThreads) k_gmres_arnoldi(SpArgs A, const doub
     for (int j = warp; j <= it; j += nw) {
       const double* vj = V + j * ld + base;
       double a = 0.0;
-      for (int r = lane; r < nr; r += 32) a += sw[r] * vj[r];
+      if (j < it) {
+        for (int r = lane; r < nr; r += 32) a += sw[r] * vj[r];
+      } else {
+        for (int r = lane; r < nr; r += 32) a += sw[r] * su[r];
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
       if (lane == 0) sacc[j] += a;
@@ -938,16 +969,16 @@ __device__ void gmres_step(KspState& S, double nn, int it, int restart, double* 
   for (int j = threadIdx.x; j <= it + 1; j += blockDim.x) hc[j] = col[j];
 }
 
-__global__ void __launch_bounds__(kThreads) k_gmres_orth(int n, KspState* st, double* __restrict__ V, int64_t ld,
-                                                         int it, int restart, double* __restrict__ part,
-                                                         unsigned* ticket) {
+__global__ void __launch_bounds__(kThreads) k_gmres_orth(int n, KspState* st, const double* __restrict__ V,
+                                                         double* __restrict__ U, int64_t ld, int it, int restart,
+                                                         double* __restrict__ part, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   __shared__ double sh[kMaxRestart + 1];
   if (st->done) return;
   for (int j = threadIdx.x; j <= it; j += blockDim.x) sh[j] = st->lhh[j];
   __syncthreads();
-  double* vn = V + (int64_t)(it + 1) * ld;
+  const double* vn = V + (int64_t)(it + 1) * ld;
   double nn = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     // subtraction order j = 0..it; the loads of four basis vectors are
@@ -963,7 +994,7 @@ __global__ void __launch_bounds__(kThreads) k_gmres_orth(int n, KspState* st, do
       s -= sh[j + 3] * a3;
     }
     for (; j <= it; ++j) s -= sh[j] * V[(int64_t)j * ld + i];
-    vn[i] = s;
+    U[i] = s;
     nn += s * s;
   }
   nn = block_sum<kThreads>(nn, red);
@@ -971,14 +1002,6 @@ __global__ void __launch_bounds__(kThreads) k_gmres_orth(int n, KspState* st, do
   if (!last_block(ticket)) return;
   nn = reduce_partials(part, gridDim.x, red);
   gmres_step(*st, nn, it, restart);
-}
-
-__global__ void k_scale_vec(int n, const KspState* st, double* __restrict__ v) {
-  note_launch();
-  const double tt = st->tt;
-  if (tt == 0.0) return;
-  const double inv = 1.0 / tt;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] *= inv;
 }
 
 // Cycle start: res = ||v0||, grs(0) = res, test; v0 normalised.  first < 0
@@ -1874,13 +1897,12 @@ static void gmres_cycle_launch(int G, const SpArgs& A, KrylovWork* W, int n, int
   KspState* st = A.st;
   const int64_t ld = n;
   double* V = W->V.p;
-  FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, V, W->part.p, (int)gsp);
+  double* U = W->w.p;  // the unnormalised next basis vector
+  FL_SPMV_DISPATCH(G, k_init_resid, A, W->b.p, W->y.p, W->dinv.p, W->r.p, U, W->part.p, (int)gsp);
   k_gmres_cycle_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp, -1);
-  k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V);
   for (int it = 0; it < restart; ++it) {
-    FL_SPMV_DISPATCH(G, k_gmres_arnoldi, A, W->dinv.p, V, ld, it, W->part.p, W->ticket.p + 2);
-    k_gmres_orth<<<gv, kThreads, 0, s>>>(n, st, V, ld, it, restart, W->part.p, W->ticket.p + 3);
-    k_scale_vec<<<gv, kThreads, 0, s>>>(n, st, V + (it + 1) * ld);
+    FL_SPMV_DISPATCH(G, k_gmres_arnoldi, A, W->dinv.p, V, U, ld, it, W->part.p, W->ticket.p + 2);
+    k_gmres_orth<<<gv, kThreads, 0, s>>>(n, st, V, U, ld, it, restart, W->part.p, W->ticket.p + 3);
   }
   k_gmres_backsolve<<<1, 32, 0, s>>>(st, restart);
   k_gmres_update_x<<<gv, kThreads, 0, s>>>(n, st, V, ld, W->y.p);
@@ -2047,7 +2069,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
         (uintptr_t)n,       (uintptr_t)G,        (uintptr_t)gsp,       (uintptr_t)gv,       (uintptr_t)restart,
         (uintptr_t)val,     (uintptr_t)ghost,    (uintptr_t)m->findrm.p, (uintptr_t)m->colm.p, (uintptr_t)st,
         (uintptr_t)W->b.p,  (uintptr_t)W->y.p,   (uintptr_t)W->r.p,    (uintptr_t)W->dinv.p, (uintptr_t)W->V.p,
-        (uintptr_t)W->part.p, (uintptr_t)W->ticket.p};
+        (uintptr_t)W->part.p, (uintptr_t)W->ticket.p, (uintptr_t)W->w.p};
     FL_TRY(gr.build_cached(W->g_gmres, key,
                            [&](cudaStream_t c) { gmres_cycle_launch(G, A, W, n, restart, gsp, gv, c); }));
     for (int cycle = 0; cycle <= o->max_its; ++cycle) {
@@ -2273,7 +2295,10 @@ int cg_prepare(CgPlan& P, fl_mesh_t* m, const fl_solver_opts* o, const double* v
   P.np = (int)std::max(P.gsp, P.gv);
   P.ksp = o->ksp_type;
   P.restart = restart;
-  if (P.ksp == 1) FL_TRY(W->V.reserve((size_t)(restart + 1) * n));
+  if (P.ksp == 1) {
+    FL_TRY(W->V.reserve((size_t)(restart + 1) * n));
+    FL_TRY(W->w.reserve(n));
+  }
   FL_TRY(W->b.reserve(n));
   FL_TRY(W->y.reserve(n));
   FL_TRY(W->r.reserve(n));
