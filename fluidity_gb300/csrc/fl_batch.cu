@@ -6,11 +6,13 @@
 // GMRES(restart) + Jacobi solve with petsc_solve's ghost semantics.  The
 // members are independent branches of one graph: the first graph runs every
 // member's assembly, boundary conditions, solver set-up and a first chunk of
-// iterations (CG: `chunk` iterations; GMRES: one restart cycle); a second
-// graph holds one more chunk of every member and is replayed until every
-// member's device-side convergence flag is set (the launches of a member that
-// has converged return at once).  The host reads one small array of flags
-// between replays.  Results equal the members' individual solves bit for bit:
+// iterations (CG: `chunk` iterations; GMRES: one restart cycle); then each
+// member's graph of one more chunk is replayed, on the member's own stream,
+// for the members whose device-side convergence flag is still clear.  The
+// host reads one small array of flags between rounds, so a member that has
+// converged costs nothing more (a graph of every member replayed as one
+// would still launch its ~65-75 no-op kernels each round).  Results equal the
+// members' individual solves bit for bit:
 // each member has its own scratch and workspace, and every kernel sums in a
 // fixed order.
 #include <cstring>
@@ -45,7 +47,7 @@ struct fl_batch_t {
   std::vector<fl::BatchMember*> mem;
   int chunk = 25;                       // iterations per replay of the iteration graph
   cudaGraphExec_t first = nullptr;      // assembly + set-up + first chunk
-  cudaGraphExec_t iter = nullptr;       // one chunk of iterations of every member
+  std::vector<cudaGraphExec_t> iter;    // one chunk of iterations, per member
   fl::DevBuf<fl::KspState*> states;     // device array of member states
   fl::DevBuf<int> done;                 // gathered convergence flags
   int* h_done = nullptr;                // pinned host copy
@@ -58,8 +60,10 @@ using namespace fl;
 
 static void destroy_graphs(fl_batch_t* b) {
   if (b->first) cudaGraphExecDestroy(b->first);
-  if (b->iter) cudaGraphExecDestroy(b->iter);
-  b->first = b->iter = nullptr;
+  for (cudaGraphExec_t e : b->iter)
+    if (e) cudaGraphExecDestroy(e);
+  b->first = nullptr;
+  b->iter.clear();
   b->built = false;
 }
 
@@ -201,10 +205,20 @@ static int build(fl_batch_t* b, cudaStream_t s0) {
     for (int k = 0; k < steps(m); ++k) cg_iterate(m->plan, m->s);
     return FL_OK;
   }));
-  FL_TRY(capture(b, s0, &b->iter, [&](BatchMember* m) -> int {
+  b->iter.assign(nm, nullptr);
+  for (int i = 0; i < nm; ++i) {
+    BatchMember* m = b->mem[i];
+    cudaGraph_t g = nullptr;
+    FL_TRY_CUDA(cudaStreamBeginCapture(m->s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps(m); ++k) cg_iterate(m->plan, m->s);
-    return FL_OK;
-  }));
+    cudaError_t e = cudaStreamEndCapture(m->s, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->iter[i], g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      set_error("graph capture failed: %s", cudaGetErrorString(e));
+      return FL_ERR_CUDA;
+    }
+  }
   b->built = true;
   return FL_OK;
 }
@@ -240,7 +254,17 @@ extern "C" int fl_batch_run(fl_batch b, void* stream, fl_solve_report* reports) 
       bool all = true;
       for (int i = 0; i < nm; ++i) all = all && b->h_done[i];
       if (all) break;
-      if (cudaGraphLaunch(b->iter, s0) != cudaSuccess) { st = FL_ERR_CUDA; break; }
+      // one more chunk of every member still running, each on its own stream
+      if (cudaEventRecord(b->fork, s0) != cudaSuccess) { st = FL_ERR_CUDA; break; }
+      for (int i = 0; i < nm && st == FL_OK; ++i) {
+        if (b->h_done[i]) continue;
+        BatchMember* m = b->mem[i];
+        if (cudaStreamWaitEvent(m->s, b->fork, 0) != cudaSuccess || cudaGraphLaunch(b->iter[i], m->s) != cudaSuccess ||
+            cudaEventRecord(m->ev, m->s) != cudaSuccess || cudaStreamWaitEvent(s0, m->ev, 0) != cudaSuccess)
+          st = FL_ERR_CUDA;
+      }
+      if (st != FL_OK) break;
+      gather_done(b->states.p, nm, b->done.p, s0);
     }
     if (st != FL_OK) break;
     for (BatchMember* m : b->mem) cg_finish_launch(m->plan, s0);
