@@ -282,6 +282,168 @@ __global__ void __launch_bounds__(128) k_asm_general(AsmArgs A) {
   }
 }
 
+// P1 advection-diffusion element matrices in closed form, in double-float on
+// the FP32 pipes: k_asm_general<4> spends ~520 FP64 operations per element,
+// and GB300 runs FP64 FMAs at ~1/70 of its FP32 rate.  With P1 coordinates
+// and a P1 velocity every reference tensor of the general kernel factors
+// through the reference mass (m0 on the diagonal, m1 off it: the tet rules
+// are symmetric under vertex permutations) and the constant reference
+// gradients dn_j, exactly: T[i][j][k][a] = M[i][k] dn_j[a], D[i][j][k][a] =
+// M[i][j] dn_k[a], R[i][j][a][b] = wsum dn_i[a] dn_j[b].  With c_j the
+// cofactor columns (invJ dn_j = c_j / det, c_3 = -(c_0 + c_1 + c_2)),
+// s = sign(det) and uc[k][j] = u_k . c_j:
+//   advection   A_ij = s (m1 S_j + (m0 - m1) uc[i][j]),  S_j = sum_k uc[k][j]
+//   by parts    A_ij = -s (m1 S_i + (m0 - m1) uc[j][i])
+//   divergence  beta s M_ij sum_k uc[k][k]   (beta = -(1 - beta) by parts)
+//   diffusion   K_ij = wsum (c_i . kappa c_j) / |det|   (diagonal kappa)
+//   mass        |det| M_ij, or |det| (m0 + 3 m1) on the diagonal (lumped)
+// and, as in k_asm_general<4>, the matrix M + theta dt op and the rhs
+// -op T + |det| M f, written in the same em layout (k = 4 i + j, 16 + i).
+struct AdvDfArgs {
+  int32_t E;
+  const int32_t* nd;   // field connectivity (int4 per element)
+  const int32_t* xnd;  // coordinate connectivity (int4 per element)
+  const double* X;
+  const double* t;
+  const double* u;
+  const double* f;
+  double* em;
+  df m0, m1, dm, ml;   // reference mass: diagonal, off-diagonal, m0 - m1, m0 + 3 m1
+  df kd[3];            // wsum * kappa_aa
+  df qs;               // theta * dt (zero without the time term)
+  df beta;             // divergence coefficient
+  int have_mass, lump, by_parts, have_beta, have_diff, have_src;
+};
+
+template <bool ADV>
+__global__ void __launch_bounds__(128) k_asm_p1_advdif_df(AdvDfArgs A) {
+  note_launch();
+  const int64_t E = A.E;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += gridDim.x * blockDim.x) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(A.xnd) + e);
+    const int vi[4] = {v.x, v.y, v.z, v.w};
+    df c[4][3];
+    df det;
+    {
+      double x[4][3];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) x[i][a] = __ldg(A.X + 3 * (int64_t)vi[i] + a);
+      df J[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) J[a][b] = df_from_double(x[b][a] - x[3][a]);
+      df cof[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+          cof[i][k] = df_mul_sub_mul(J[i1][k1], J[i2][k2], J[i2][k1], J[i1][k2]);
+        }
+      det = df_dot3(J[0][0], cof[0][0], J[1][0], cof[1][0], J[2][0], cof[2][0]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) c[i][a] = cof[a][i];
+        c[3][a] = df_neg(df_add(df_add(c[0][a], c[1][a]), c[2][a]));
+      }
+    }
+    const bool neg = det.hi < 0.0f;
+    const df adet = df_abs(det);
+    df op[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) op[i][j] = {0.0f, 0.0f};
+    if (A.have_diff) {
+      const df rdet = df_rcp(adet);
+      df kc[3][3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) kc[j][a] = df_mul(A.kd[a], c[j][a]);
+      df G[4][4];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j) {
+          G[i][j] = df_dot3(c[i][0], kc[j][0], c[i][1], kc[j][1], c[i][2], kc[j][2]);
+          G[j][i] = G[i][j];
+        }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        G[i][3] = df_neg(df_add(df_add(G[i][0], G[i][1]), G[i][2]));
+        G[3][i] = G[i][3];
+      }
+      G[3][3] = df_neg(df_add(df_add(G[0][3], G[1][3]), G[2][3]));
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) op[i][j] = df_mul(G[i][j], rdet);
+    }
+    if (ADV) {
+      df uc[4][4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        df uk[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) uk[a] = df_from_double(__ldg(A.u + 3 * (int64_t)vi[k] + a));
+#pragma unroll
+        for (int j = 0; j < 4; ++j) uc[k][j] = df_dot3(uk[0], c[j][0], uk[1], c[j][1], uk[2], c[j][2]);
+      }
+      df S[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) S[j] = df_add(df_add(uc[0][j], uc[1][j]), df_add(uc[2][j], uc[3][j]));
+      const bool flip = neg != (A.by_parts != 0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          df a = A.by_parts ? df_add(df_mul(A.m1, S[i]), df_mul(A.dm, uc[j][i]))
+                            : df_add(df_mul(A.m1, S[j]), df_mul(A.dm, uc[i][j]));
+          if (flip) a = df_neg(a);
+          op[i][j] = df_add(op[i][j], a);
+        }
+      if (A.have_beta) {
+        df dv = df_add(df_add(uc[0][0], uc[1][1]), df_add(uc[2][2], uc[3][3]));
+        if (neg) dv = df_neg(dv);
+        const df bd = df_mul(A.beta, dv);
+        const df b0 = df_mul(bd, A.m0), b1 = df_mul(bd, A.m1);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) op[i][j] = df_add(op[i][j], i == j ? b0 : b1);
+      }
+    }
+    const int4 tv = __ldg(reinterpret_cast<const int4*>(A.nd) + e);
+    const int tn[4] = {tv.x, tv.y, tv.z, tv.w};
+    df T[4], fa[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      T[j] = A.t ? df_from_double(__ldg(A.t + tn[j])) : df{0.0f, 0.0f};
+      fa[j] = A.have_src ? df_mul(adet, df_from_double(__ldg(A.f + tn[j]))) : df{0.0f, 0.0f};
+    }
+    const df fs = df_add(df_add(fa[0], fa[1]), df_add(fa[2], fa[3]));
+    const df md = df_mul(adet, A.lump ? A.ml : A.m0), mo = df_mul(adet, A.m1);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      df r = {0.0f, 0.0f};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        df m = A.have_mass ? (i == j ? md : (A.lump ? df{0.0f, 0.0f} : mo)) : df{0.0f, 0.0f};
+        m = df_add(m, df_mul(A.qs, op[i][j]));
+        A.em[(int64_t)(4 * i + j) * E + e] = df_to_double(m);
+        r = df_sub(r, df_mul(op[i][j], T[j]));
+      }
+      if (A.have_src) r = df_add(r, df_add(df_mul(A.m1, fs), df_mul(A.dm, fa[i])));
+      A.em[(int64_t)(16 + i) * E + e] = df_to_double(r);
+    }
+  }
+}
+
 // Symmetric storage index of (i, j) in a 4x4 matrix: 0..9.
 __host__ __device__ constexpr int sym4(int i, int j) {
   return i <= j ? i * 4 - (i * (i - 1)) / 2 + (j - i) : j * 4 - (j * (j - 1)) / 2 + (i - j);
@@ -1530,6 +1692,21 @@ static bool diagonal_kappa(const fl_advdif_params* p) {
   return true;
 }
 
+// The double-float P1 advection-diffusion kernel: P1 field, no absorption,
+// a diagonal (or isotropic) kappa, and a symmetric reference mass (every tet
+// rule in use; checked).  The pure diffusion forms keep the record kernels.
+static bool use_p1_advdif_df(const fl_mesh_t* m, const fl_advdif_params* p, const RefTensors& h) {
+  if (m->loc != 4 || diffusion_form(p) || p->have_absorption) return false;
+  if (p->have_diffusivity && !diagonal_kappa(p)) return false;
+  const double m0 = h.M[0][0], m1 = h.M[0][1];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      const double ref = i == j ? m0 : m1;
+      if (fabs(h.M[i][j] - ref) > 1e-14 * fabs(ref)) return false;
+    }
+  return true;
+}
+
 // The double-float P2 kernel: the diffusion form with a diagonal kappa.
 static bool use_p2_df(const fl_mesh_t* m, const fl_advdif_params* p) {
   return m->loc == 10 && diffusion_form(p) && diagonal_kappa(p);
@@ -1656,6 +1833,12 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
   A.have_abs = p->have_absorption;
   const bool closed = use_p1_closed_form(m, p);
   const bool p2df = use_p2_df(m, p);
+  RefTensors h1;
+  bool p1adv = false;
+  if (m->loc == 4 && !diffusion_form(p) && !p->have_absorption) {
+    build_tensors(1, p->quad_degree, h1);
+    p1adv = use_p1_advdif_df(m, p, h1);
+  }
   const int loc = m->loc;
   double* em = em_override;
   if (!em) {
@@ -1745,6 +1928,32 @@ int assemble(fl_mesh_t* m, const fl_advdif_params* p, const fl_fields* f, double
     launch_p1_df_elems(key, g, eb, smem, D, s);
   } else if (closed) {
     k_asm_p1_diffusion<<<grid_for(m->E, eb, esm), eb, 0, s>>>(A);
+  } else if (p1adv) {
+    AdvDfArgs D{};
+    D.E = m->E;
+    D.nd = m->ndglno.p;
+    D.xnd = m->xndglno.p;
+    D.X = m->coords.p;
+    D.t = f->t;
+    D.u = f->velocity;
+    D.f = f->source;
+    D.em = em;
+    D.m0 = df_host(h1.M[0][0]);
+    D.m1 = df_host(h1.M[0][1]);
+    D.dm = df_host(h1.M[0][0] - h1.M[0][1]);
+    D.ml = df_host(h1.M[0][0] + 3.0 * h1.M[0][1]);
+    for (int a = 0; a < 3; ++a)
+      D.kd[a] = df_host(h1.wsum * (p->isotropic_diffusivity ? p->diffusivity[0] : p->diffusivity[4 * a]));
+    D.qs = df_host(A.use_dt ? A.theta_dt : 0.0);
+    D.beta = df_host(A.beta);
+    D.have_mass = A.have_mass;
+    D.lump = A.lump;
+    D.by_parts = A.by_parts;
+    D.have_beta = A.have_beta;
+    D.have_diff = A.have_diff;
+    D.have_src = A.have_src;
+    if (A.have_adv) k_asm_p1_advdif_df<true><<<grid_for(m->E, 128, esm), 128, 0, s>>>(D);
+    else k_asm_p1_advdif_df<false><<<grid_for(m->E, 128, esm), 128, 0, s>>>(D);
   } else if (loc == 4) {
     k_asm_general<4><<<grid_for(m->E, 128, esm), 128, 0, s>>>(A);
   } else {

@@ -40,6 +40,14 @@ CASES = {
     "lumped_absorption": dict(theta=1.0, dt=0.1, have_mass=True, lump_mass=True, absorption=True,
                               T=True, diffusivity=0.5, source=True),
     "mass_only": dict(have_mass=True, source=True),
+    # the double-float P1 advection-diffusion kernel: lumped mass with a
+    # divergence term, a diagonal kappa with a source, no diffusion
+    "advdif_lumped_beta": dict(theta=0.5, dt=0.01, have_mass=True, lump_mass=True, velocity=True, T=True,
+                               diffusivity=1e-3, beta=0.5),
+    "advdif_diag_kappa_source": dict(theta=1.0, dt=0.05, have_mass=True, velocity=True, T=True,
+                                     diffusivity=np.diag([1e-2, 1e-3, 1e-4]), source=True),
+    "advection_only_by_parts": dict(theta=1.0, dt=0.1, have_mass=True, velocity=True, T=True, beta=0.2,
+                                    by_parts=True),
 }
 
 
@@ -81,6 +89,25 @@ def test_p1_assembly_matches_oracle(O, aniso_mesh, name, mesh):
                                                   velocity=fl.get("velocity"),
                                                   source=fl.get("source"),
                                                   absorption=fl.get("absorption"))
+    _compare(val, rhs, oval, orhs, f)
+
+
+@pytest.mark.parametrize("qdeg", [1, 3, 4])
+@pytest.mark.parametrize("name", ["advdif", "advdif_by_parts"])
+def test_p1_advdif_quadrature_degrees(O, name, qdeg):
+    """The P1 advection-diffusion terms under every tet rule (the closed form
+    takes the rule's reference mass; degree 1 is not exact for it)."""
+    nd, X = M.cube_mesh(4)
+    case = CASES[name]
+    fl = _fields(X, case)
+    m = ft.Mesh(nd, X)
+    f, c, _ = O.make_sparsity(nd)
+    ocol, ncol = O.colour_cg1(nd)
+    kw = {k: v for k, v in fl.items() if k not in ("theta", "dt", "beta", "have_mass", "lump_mass", "by_parts")}
+    kw.update({k: case[k] for k in ("theta", "dt", "beta", "have_mass", "lump_mass", "by_parts") if k in case})
+    oval, orhs = _oracle(O, nd, X, nd, X.shape[0], f, c, colours=O.colour_sets(ocol, ncol), quad_degree=qdeg, **kw)
+    val, rhs = ft.assemble_advection_diffusion_cg(m, _params(case, qdeg), t=fl.get("T"),
+                                                  velocity=fl.get("velocity"), source=fl.get("source"))
     _compare(val, rhs, oval, orhs, f)
 
 
