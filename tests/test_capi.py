@@ -5,6 +5,8 @@ import os
 import re
 import subprocess
 
+import pytest
+
 from fluidity_gb300 import _lib, build
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
@@ -112,3 +114,17 @@ def test_fortran_structs_match_the_ctypes_layouts():
                 decl = line.split("::", 1)[1]
                 names += [re.sub(r"\(.*\)", "", v).strip() for v in decl.split(",")]
         assert names == [f[0] for f in cstruct._fields_], (fname, names)
+
+
+def test_solver_options_schedule_field():
+    """fl_solver_opts.schedule (the GMRES launch schedule) and the size limit
+    of the automatic choice, as the header declares them."""
+    from fluidity_gb300 import femtools as ft
+    assert ft.solver_options(ksp="gmres").schedule == 0
+    assert ft.solver_options(ksp="gmres", schedule="graph").schedule == 1
+    assert ft.solver_options(ksp="gmres", schedule="persistent").schedule == 2
+    with pytest.raises(KeyError):
+        ft.solver_options(schedule="sometimes")
+    src = open(HEADER).read()
+    assert re.search(r"#define FL_PERSIST_MAX_ROWS \d+", src)
+    assert [f[0] for f in _lib.SolverOpts._fields_][-1] == "schedule"
