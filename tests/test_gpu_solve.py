@@ -376,3 +376,23 @@ def test_gmres_schedule_edge_cases(O, sched):
     x = np.full(m.N, 7.0)
     rep = ft.petsc_solve(m, x, val, g, ft.solver_options(ksp="gmres", schedule=sched), inactive=ina2)
     assert np.array_equal(x, g) and rep["iterations"] == 0
+
+
+@pytest.mark.parametrize("sched", ["graph", "persistent"])
+def test_gmres_long_restart_matches_oracle(O, sched):
+    """GMRES(60) on a Poisson system that needs more than 32 iterations in its
+    first cycle: the Hessenberg update's second chunk of 32 rotations and the
+    cooperative kernel's second lane of dot products run; reason, iterations
+    (within two: the sums run in another order than the oracle's) and the
+    solution match the oracle, and a restart inside the solve (restart 40)
+    as well."""
+    m, X, val, rhs, ina = poisson(O, 14)
+    for restart in (60, 40):
+        x = np.zeros(m.N)
+        rep = ft.petsc_solve(m, x, val, rhs, ft.solver_options(ksp="gmres", restart=restart, rtol=1e-10,
+                                                               schedule=sched), inactive=ina)
+        ox, oits, oreason, _ = oracle_solve(O, m, val, rhs, ina, ksp="gmres", restart=restart, rtol=1e-10)
+        assert oits > 32
+        assert rep["reason"] == oreason == 2
+        assert abs(rep["iterations"] - oits) <= 2
+        assert np.abs(x - ox).max() <= 1e-7 * np.abs(ox).max()
