@@ -1138,7 +1138,7 @@ __global__ void k_gmres_cycle_end(KspState* st) {
 // ------------------------------------------- GMRES in one cooperative launch --
 // The whole of KSPSolve_GMRES for a small system in one launch, for systems
 // where a launch per Arnoldi phase costs more than the phase.  Each block
-// owns fixed rows (passes of kPRows rows, kPG lanes per row: row group
+// owns fixed rows (passes of kThreads / PG rows, PG lanes per row: row group
 // blockIdx.x + k nb) and keeps their slice of the Krylov basis in shared
 // memory, so only the SpMV gathers and the reduction partials cross blocks.
 // Every block also keeps an identical copy of the solver state in shared
@@ -1153,7 +1153,7 @@ __global__ void k_gmres_cycle_end(KspState* st) {
 //   then every block: tt = ||U||, the Hessenberg column, rotations and the
 //   convergence test (gmres_step).
 // FP64 latency shapes the layout (a dependent FP64 operation ~64 SM cycles
-// on GB300): short FMA chains (kPG lanes per row; dot products lane-per-basis-
+// on GB300): short FMA chains (PG lanes per row; dot products lane-per-basis-
 // vector over a warp's rows, then a tree over the warps), and the cross-block
 // partials published and summed in double-float on the FP32 pipes.  The
 // Krylov space and the tests are KSPGMRESCycle's; the sums run in another
@@ -1161,8 +1161,9 @@ __global__ void k_gmres_cycle_end(KspState* st) {
 // Data that other blocks write during the launch (U, y, the partials) is
 // read at L2 (__ldcg).
 constexpr unsigned long long kBarrierWaitNs = 1000000000ull;  // a grid barrier gives up after 1 s
-constexpr int kPG = 8;                   // lanes per row
-constexpr int kPRows = kThreads / kPG;   // rows per pass
+// PG lanes per row: the host takes the most (8, 4, 2) that keep the row
+// groups of kThreads / PG rows within one per SM, so that a block makes one
+// pass where it can (measured: 4,913 rows best at 4, 15,625 and 35,937 at 2).
 
 struct PersistArgs {
   SpArgs A;                      // A.st: the global state (read at the start, published at the end)
@@ -1251,12 +1252,14 @@ __device__ __forceinline__ float2 df_pack(df v) { return make_float2(v.hi, v.lo)
 // rows of v_0..v_restart (row stride rows + 1, odd, so lanes reading one row
 // of different vectors fall in different banks), of w and of U (rows past N
 // hold zeros).
-inline size_t persist_smem_bytes(int restart, int npass) {
-  const size_t rows = (size_t)npass * kPRows;
+inline size_t persist_smem_bytes(int restart, int npass, int pg) {
+  const size_t rows = (size_t)npass * (kThreads / pg);
   return ((size_t)(restart + 1) * (rows + 1) + 2 * rows) * sizeof(double);
 }
 
+template <int PG>
 __global__ void __launch_bounds__(kThreads, 1) k_gmres_persistent(PersistArgs P) {
+  constexpr int kPG = PG, kPRows = kThreads / PG;
   note_launch();
   __shared__ KspState S;
   __shared__ float2 redf[kThreads / 32];
@@ -1417,7 +1420,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_gmres_persistent(PersistArgs P)
         }
       }
       __syncthreads();
-      // U = w - sum_j h_j v_j: kPG threads per row, thread t8 takes j = t8 (mod kPG)
+      // U = w - sum_j h_j v_j: kPG threads per row, thread sub takes j = sub (mod kPG)
       double nn = 0.0;
       for (int k = 0; k < P.npass; ++k) {
         const int lr = k * kPRows + tid / kPG, row = grow(lr);
@@ -1966,18 +1969,22 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   // FL_PERSIST_MAX_ROWS rows; one block per group of kThreads / G rows, at
   // most one per SM, and only when that many blocks can be co-resident
   bool persistent = false;
-  int pnb = 0, npass = 0;
+  int pnb = 0, npass = 0, ppg = 8;
   size_t psmem = 0;
   unsigned long long barrier_fault = 0;
   if (o->ksp_type == 1 && !mixed && (o->schedule == 2 || (o->schedule == 0 && n <= FL_PERSIST_MAX_ROWS))) {
-    const void* fn = (const void*)k_gmres_persistent;
+    const int sms = num_sms();
+    ppg = (n + kThreads / 8 - 1) / (kThreads / 8) <= sms ? 8 : (n + kThreads / 4 - 1) / (kThreads / 4) <= sms ? 4 : 2;
+    const void* fn = ppg == 8 ? (const void*)k_gmres_persistent<8>
+                   : ppg == 4 ? (const void*)k_gmres_persistent<4> : (const void*)k_gmres_persistent<2>;
     int per_sm = 0;
     FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
-    const int groups = (n + kPRows - 1) / kPRows;
-    const int cap = std::max(1, per_sm) * num_sms();
+    const int rows_per_pass = kThreads / ppg;
+    const int groups = (n + rows_per_pass - 1) / rows_per_pass;
+    const int cap = std::max(1, per_sm) * sms;
     npass = (groups + cap - 1) / cap;
     pnb = (groups + npass - 1) / npass;
-    psmem = persist_smem_bytes(restart, npass);
+    psmem = persist_smem_bytes(restart, npass, ppg);
     cudaFuncAttributes fa;
     FL_TRY_CUDA(cudaFuncGetAttributes(&fa, fn));
     int dev = 0, optin = 0;
@@ -1986,7 +1993,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     if (fa.sharedSizeBytes + psmem <= (size_t)optin) {
       FL_TRY_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
       FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, psmem));
-      persistent = (int64_t)per_sm * num_sms() >= pnb;
+      persistent = (int64_t)per_sm * sms >= pnb;
     }
     if (persistent) FL_TRY(W->part.reserve((size_t)std::max(np, pnb) * (kMaxRestart + 3)));
   }
@@ -2053,7 +2060,9 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
                   reinterpret_cast<unsigned long long*>(W->ticket.p), restart, npass, wt.withhold,
                   wt.wait_ms > 0.0 ? (unsigned long long)(wt.wait_ms * 1e6) : kBarrierWaitNs};
     void* args[] = {&P};
-    FL_TRY_CUDA(cudaLaunchCooperativeKernel((const void*)k_gmres_persistent, dim3(pnb), dim3(kThreads), args, psmem, s));
+    const void* fn = ppg == 8 ? (const void*)k_gmres_persistent<8>
+                   : ppg == 4 ? (const void*)k_gmres_persistent<4> : (const void*)k_gmres_persistent<2>;
+    FL_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(pnb), dim3(kThreads), args, psmem, s));
     FL_TRY_CUDA(cudaMemcpyAsync(&barrier_fault, W->ticket.p + 2, sizeof(unsigned long long),
                                 cudaMemcpyDeviceToHost, s));
   } else if (!mixed) {

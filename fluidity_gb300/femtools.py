@@ -288,7 +288,7 @@ def solver_options(*, ksp="cg", restart=30, rtol=1e-10, atol=0.0, dtol=1e5, max_
     ``schedule`` picks how an FP64 GMRES solve is launched: "graph" (a launch
     per Arnoldi phase, cycles replayed as CUDA graphs), "persistent" (one
     cooperative launch for the whole solve) or "auto" (persistent up to
-    FL_PERSIST_MAX_ROWS rows)."""
+    FL_PERSIST_MAX_ROWS = 81,920 rows)."""
     o = SolverOpts()
     o.ksp_type = {"cg": 0, "gmres": 1}[ksp]
     o.restart, o.rtol, o.atol, o.dtol = restart, rtol, atol, dtol

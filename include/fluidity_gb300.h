@@ -320,7 +320,7 @@ typedef struct {
 } fl_solver_opts;
 
 /* Largest system (rows) that schedule 0 solves in one cooperative launch. */
-#define FL_PERSIST_MAX_ROWS 24576
+#define FL_PERSIST_MAX_ROWS 81920
 
 typedef struct {
   int32_t iterations;        /* KSPGetIterationNumber (inner total if mixed) */
