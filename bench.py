@@ -740,23 +740,18 @@ def bench_advdif_steps(args, dev, stream, n=16, nsteps=10):
     bn = M.boundary_nodes(X)
     nodes = torch.from_numpy(bn).to(dev)
     g = torch.zeros(bn.size, dtype=torch.float64, device=dev)
-    val = torch.empty(m.nnz, dtype=torch.float64, device=dev)
-    rhs = torch.empty(m.N, dtype=torch.float64, device=dev)
-    ina = torch.zeros(m.N, dtype=torch.uint8, device=dev)
-    dT = torch.zeros(m.N, dtype=torch.float64, device=dev)
 
     def run(schedule="auto"):
+        # one fl_dev_solve_field_equation_cg call per step: assembly, strong
+        # Dirichlet conditions in rate-of-change form, GMRES from zero change
+        # and t + dt delta, one error check per step
         opts = ft.solver_options(ksp="gmres", restart=30, rtol=1e-10, max_its=10000, schedule=schedule)
         t = torch.from_numpy(M.gaussian_tracer(X)).to(dev)
         its, ts = [], []
         for _ in range(nsteps):
-            ft.assemble_advection_diffusion_cg(m, p, t=t, velocity=u, val=val, rhs=rhs, stream=stream)
-            ina.zero_()
-            ft.apply_dirichlet_conditions(m, rhs, ina, nodes, g, t=t, dt=p.dt, stream=stream)
-            dT.zero_()
-            rep = ft.petsc_solve(m, dT, val, rhs, opts, inactive=ina, stream=stream)
+            t, rep = ft.solve_field_equation_cg_device(m, t, p, opts, bc_nodes=nodes, bc_values=g, velocity=u,
+                                                       stream=stream)
             its.append(rep["iterations"])
-            t = t + p.dt * dT
             ts.append(t)
         return t, its, ts
 

@@ -93,7 +93,8 @@ EXPORTS = [
     "fl_last_error", "fl_gpu_mesh_register", "fl_gpu_mesh_destroy", "fl_gpu_mesh_info",
     "fl_gpu_sparsity_copy", "fl_gpu_colouring_copy", "fl_gpu_make_global_numbering_p2",
     "fl_gpu_assemble_advdif_cg", "fl_dev_assemble_advdif_cg", "fl_gpu_apply_dirichlet",
-    "fl_dev_apply_dirichlet", "fl_gpu_petsc_solve", "fl_dev_petsc_solve", "fl_dev_csr_mult",
+    "fl_dev_apply_dirichlet", "fl_gpu_petsc_solve", "fl_dev_petsc_solve", "fl_dev_solve_field_equation_cg",
+    "fl_dev_csr_mult",
     "fl_kernel_launch_count", "fl_set_kernel_timing", "fl_last_assembly_kernel_ms",
     "fl_dev_assemble_p1_diffusion_noalloc", "fl_dev_autotune_assembly", "fl_set_assembly_tiles",
     "fl_get_assembly_tiles",
@@ -136,6 +137,9 @@ _SIGNATURES = {
                                      C.POINTER(SolveReport)]),
     "fl_dev_petsc_solve": (C.c_int, [_P, C.POINTER(SolverOpts), _P, _P, _P, _P,
                                      C.POINTER(SolveReport), _P]),
+    "fl_dev_solve_field_equation_cg": (C.c_int, [_P, C.POINTER(AdvDifParams), C.POINTER(Fields), _I32, _P, _I32,
+                                                 _P, C.POINTER(SolverOpts), _P, _P, _P, _P, _P,
+                                                 C.POINTER(SolveReport), _P]),
     "fl_dev_csr_mult": (C.c_int, [_P, _P, _P, _P, _P]),
     "fl_kernel_launch_count": (C.c_int64, []),
     "fl_set_kernel_timing": (C.c_int, [_P, _I32]),

@@ -2446,6 +2446,39 @@ extern "C" int fl_dev_petsc_solve(fl_mesh m, const fl_solver_opts* o, const doub
   return solve(m, o, val, inactive, rhs, x, rep, s);
 }
 
+namespace fl {
+// t_new = t + dt delta (the acceleration-form update of solve_field_equation_cg),
+// the product rounded before the sum as the separate statement rounds it
+// (no FMA contraction)
+__global__ void k_field_update(int n, const double* __restrict__ t, double dt, const double* __restrict__ d,
+                               double* __restrict__ out) {
+  note_launch();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = __dadd_rn(t ? t[i] : 0.0, __dmul_rn(dt, d[i]));
+}
+}  // namespace fl
+
+extern "C" int fl_dev_solve_field_equation_cg(fl_mesh m, const fl_advdif_params* p, const fl_fields* f, int32_t nb,
+                                              const int32_t* bc_nodes, int32_t index_base, const double* bc_values,
+                                              const fl_solver_opts* o, double* val, double* rhs, uint8_t* inactive,
+                                              double* delta, double* t_new, fl_solve_report* rep, void* stream) {
+  FL_CHECK_ARG(m && p && f && o && val && rhs && inactive && delta && t_new && rep, "null argument");
+  FL_CHECK_ARG(nb >= 0 && (nb == 0 || (bc_nodes && bc_values)), "boundary node list");
+  cudaStream_t s = stream ? (cudaStream_t)stream : m->stream;
+  // assemble (M + theta dt (A + K)) delta = rhs
+  FL_TRY(assemble(m, p, f, val, rhs, s, nullptr));
+  // strong Dirichlet conditions in rate-of-change form: rhs = (g - t) / dt
+  FL_TRY_CUDA(cudaMemsetAsync(inactive, 0, (size_t)m->N, s));
+  FL_TRY(dirichlet_launch(m, nb, bc_nodes, index_base, bc_values, f->t, p->dt, rhs, inactive, s));
+  // petsc_solve(delta_t, ...) from zero change
+  FL_TRY_CUDA(cudaMemsetAsync(delta, 0, sizeof(double) * (size_t)m->N, s));
+  FL_TRY(solve(m, o, val, inactive, rhs, delta, rep, s));
+  k_field_update<<<grid_for(m->N, kThreads, 4), kThreads, 0, s>>>(m->N, f->t, p->dt, delta, t_new);
+  FL_TRY_CUDA(cudaGetLastError());
+  // pattern misses and out-of-range boundary nodes, reported once for the step
+  return check_err(m->err.p, s, "assembly or Dirichlet conditions of solve_field_equation_cg");
+}
+
 extern "C" int fl_gpu_petsc_solve(fl_mesh m, const fl_solver_opts* o, const double* val, const uint8_t* inactive,
                                   const double* rhs, double* x, fl_solve_report* rep) {
   FL_CHECK_ARG(m && o && val && rhs && x && rep, "null argument");

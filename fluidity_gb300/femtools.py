@@ -405,6 +405,34 @@ def solve_field_equation_cg(mesh: Mesh, t, params: AdvDifParams, options: Solver
     return t + params.dt * delta, rep
 
 
+def solve_field_equation_cg_device(mesh: Mesh, t, params: AdvDifParams, options: SolverOpts, *, bc_nodes,
+                                   bc_values, velocity=None, source=None, absorption=None, t_out=None,
+                                   stream=None) -> tuple:
+    """The device form of solve_field_equation_cg (device tensors): one
+    fl_dev_solve_field_equation_cg call assembles, applies the strong
+    Dirichlet conditions in rate-of-change form, solves for the change from
+    zero and returns (t + dt * delta, solve report), with one error check
+    for the whole step.  Scratch (val, rhs, inactive, delta) is kept on the
+    mesh object between calls."""
+    import torch
+    sc = getattr(mesh, "_sfe_scratch", None)
+    if sc is None or sc["val"].numel() != mesh.nnz:
+        dev = t.device
+        sc = {"val": torch.empty(mesh.nnz, dtype=torch.float64, device=dev),
+              "rhs": torch.empty(mesh.N, dtype=torch.float64, device=dev),
+              "inactive": torch.empty(mesh.N, dtype=torch.uint8, device=dev),
+              "delta": torch.empty(mesh.N, dtype=torch.float64, device=dev)}
+        mesh._sfe_scratch = sc
+    out = t_out if t_out is not None else torch.empty_like(t)
+    f = Fields(_ptr(t), _ptr(velocity), _ptr(source), _ptr(absorption))
+    rep = SolveReport()
+    check(mesh.lib.fl_dev_solve_field_equation_cg(
+        mesh.handle, C.byref(params), C.byref(f), int(len(bc_nodes)), _ptr(bc_nodes), 0, _ptr(bc_values),
+        C.byref(options), _ptr(sc["val"]), _ptr(sc["rhs"]), _ptr(sc["inactive"]), _ptr(sc["delta"]),
+        _ptr(out), C.byref(rep), _stream_ptr(stream)), "fl_dev_solve_field_equation_cg")
+    return out, _report_dict(rep)
+
+
 def _report_dict(rep: SolveReport) -> dict:
     return {
         "iterations": rep.iterations, "reason": rep.reason,

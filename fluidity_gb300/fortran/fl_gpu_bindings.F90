@@ -57,7 +57,8 @@ module fl_gpu_bindings
             fl_gpu_make_global_numbering_p2, fl_gpu_assemble_advdif_cg, fl_dev_assemble_advdif_cg, &
             fl_dev_assemble_advdif_faces, fl_gpu_assemble_advdif_faces, &
             fl_dev_assemble_p1_diffusion_noalloc, fl_gpu_apply_dirichlet, fl_dev_apply_dirichlet, &
-            fl_gpu_petsc_solve, fl_dev_petsc_solve, fl_dev_csr_mult, fl_dev_autotune_assembly, &
+            fl_gpu_petsc_solve, fl_dev_petsc_solve, fl_dev_solve_field_equation_cg, fl_dev_csr_mult, &
+            fl_dev_autotune_assembly, &
             fl_set_assembly_tiles, fl_get_assembly_tiles, fl_batch_create, fl_batch_add, fl_batch_run, &
             fl_batch_size, fl_batch_destroy, fl_amg_create, fl_amg_solve, fl_amg_levels, &
             fl_amg_set_norm, fl_amg_set_precision, fl_amg_destroy, fl_gnn_num_params, fl_gnn_create, &
@@ -284,6 +285,22 @@ module fl_gpu_bindings
        type(fl_solve_report), intent(out) :: report
        integer(c_int) :: st
      end function fl_dev_petsc_solve
+
+     function fl_dev_solve_field_equation_cg(mesh, params, fields, nb, bc_nodes, index_base, bc_values, &
+          opts, val, rhs, inactive, delta, t_new, report, stream) &
+          bind(c, name="fl_dev_solve_field_equation_cg") result(st)
+       import :: c_int, c_ptr, c_int32_t, fl_advdif_params, fl_fields, fl_solver_opts, fl_solve_report
+       type(c_ptr), value :: mesh
+       type(fl_advdif_params), intent(in) :: params
+       type(fl_fields), intent(in) :: fields
+       integer(c_int32_t), value :: nb, index_base
+       type(c_ptr), value :: bc_nodes, bc_values
+       type(fl_solver_opts), intent(in) :: opts
+       type(c_ptr), value :: val, rhs, inactive, delta, t_new
+       type(fl_solve_report), intent(out) :: report
+       type(c_ptr), value :: stream
+       integer(c_int) :: st
+     end function fl_dev_solve_field_equation_cg
 
      function fl_dev_csr_mult(mesh, val, x, y, stream) bind(c, name="fl_dev_csr_mult") result(st)
        import :: c_int, c_ptr

@@ -347,6 +347,21 @@ int fl_dev_petsc_solve(fl_mesh mesh, const fl_solver_opts* opts, const double* v
                        const uint8_t* inactive, const double* rhs, double* x,
                        fl_solve_report* report, void* stream);
 
+/* One step of solve_field_equation_cg on the device
+ * (assemble/Advection_Diffusion_CG.F90:127-174): fl_dev_assemble_advdif_cg
+ * into val/rhs, fl_dev_apply_dirichlet in rate-of-change form (inactive
+ * cleared first; rhs = (g - t) / dt with fields->t and params->dt),
+ * fl_dev_petsc_solve for delta from zero change, then t_new = t + dt delta
+ * (t_new may be fields->t).  val(nnz), rhs(N), inactive(N) and delta(N) are
+ * caller-owned device scratch.  The same kernels as the three calls, so the
+ * same bits; a pattern miss or a boundary node out of range is reported once,
+ * after the step, instead of after each stage. */
+int fl_dev_solve_field_equation_cg(fl_mesh mesh, const fl_advdif_params* params, const fl_fields* fields,
+                                   int32_t nb, const int32_t* bc_nodes, int32_t index_base,
+                                   const double* bc_values, const fl_solver_opts* opts, double* val,
+                                   double* rhs, uint8_t* inactive, double* delta, double* t_new,
+                                   fl_solve_report* report, void* stream);
+
 /* Initial guess for a solve in a sequence of solves (no counterpart in the
  * reference, which starts from the previous solution or from zero): the
  * projection method of P. F. Fischer (1998).  Given k (1..8) basis vectors

@@ -396,3 +396,40 @@ def test_gmres_long_restart_matches_oracle(O, sched):
         assert rep["reason"] == oreason == 2
         assert abs(rep["iterations"] - oits) <= 2
         assert np.abs(x - ox).max() <= 1e-7 * np.abs(ox).max()
+
+
+def test_fused_field_step_matches_the_three_calls(O):
+    """fl_dev_solve_field_equation_cg (assembly, rate-of-change Dirichlet
+    conditions, solve from zero change, t + dt delta in one call) gives the
+    bits of the three separate calls, step after step; a boundary node out of
+    range is reported after the step and the next step still works."""
+    import torch
+    from fluidity_gb300 import _lib
+    nd, X = M.cube_mesh(8)
+    m = ft.Mesh(nd, X)
+    p = ft.advdif_params(theta=0.5, dt=0.01, have_mass=True, have_advection=True, diffusivity=1e-3)
+    u = torch.tensor(M.advdif_velocity(X), device="cuda")
+    bn = torch.tensor(M.boundary_nodes(X), device="cuda")
+    g = torch.zeros(bn.numel(), dtype=torch.float64, device="cuda")
+    opts = ft.solver_options(ksp="gmres", restart=30, rtol=1e-10)
+    t0 = torch.tensor(M.gaussian_tracer(X), device="cuda")
+    ta, tb = t0.clone(), t0.clone()
+    val = torch.empty(m.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(m.N, dtype=torch.float64, device="cuda")
+    ina = torch.zeros(m.N, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        ft.assemble_advection_diffusion_cg(m, p, t=ta, velocity=u, val=val, rhs=rhs)
+        ina.zero_()
+        ft.apply_dirichlet_conditions(m, rhs, ina, bn, g, t=ta, dt=p.dt)
+        d = torch.zeros(m.N, dtype=torch.float64, device="cuda")
+        rep_a = ft.petsc_solve(m, d, val, rhs, opts, inactive=ina)
+        ta = ta + p.dt * d
+        tb, rep_b = ft.solve_field_equation_cg_device(m, tb, p, opts, bc_nodes=bn, bc_values=g, velocity=u)
+        assert rep_a["iterations"] == rep_b["iterations"] and rep_b["reason"] == 2
+        assert torch.equal(ta, tb)
+    bad = bn.clone()
+    bad[0] = m.N + 5
+    with pytest.raises(_lib.FlError):
+        ft.solve_field_equation_cg_device(m, tb, p, opts, bc_nodes=bad, bc_values=g, velocity=u)
+    tc, rep = ft.solve_field_equation_cg_device(m, tb, p, opts, bc_nodes=bn, bc_values=g, velocity=u)
+    assert rep["reason"] == 2 and torch.isfinite(tc).all()
