@@ -315,7 +315,9 @@ typedef struct {
                                 Arnoldi phase, each restart cycle replayed
                                 as a CUDA graph; 2 = the whole solve in one
                                 cooperative launch, the blocks meeting at
-                                grid barriers (latency-bound small systems).
+                                grid barriers (latency-bound small systems;
+                                when the blocks' slices of the Krylov basis
+                                do not fit in shared memory, 1 is used).
                                 Other solves ignore it.                      */
 } fl_solver_opts;
 
