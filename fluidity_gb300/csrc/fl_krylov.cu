@@ -26,6 +26,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "fl_internal.cuh"
@@ -1975,26 +1976,52 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   if (o->ksp_type == 1 && !mixed && (o->schedule == 2 || (o->schedule == 0 && n <= FL_PERSIST_MAX_ROWS))) {
     const int sms = num_sms();
     ppg = (n + kThreads / 8 - 1) / (kThreads / 8) <= sms ? 8 : (n + kThreads / 4 - 1) / (kThreads / 4) <= sms ? 4 : 2;
-    const void* fn = ppg == 8 ? (const void*)k_gmres_persistent<8>
-                   : ppg == 4 ? (const void*)k_gmres_persistent<4> : (const void*)k_gmres_persistent<2>;
-    int per_sm = 0;
-    FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
     const int rows_per_pass = kThreads / ppg;
     const int groups = (n + rows_per_pass - 1) / rows_per_pass;
-    const int cap = std::max(1, per_sm) * sms;
-    npass = (groups + cap - 1) / cap;
-    pnb = (groups + npass - 1) / npass;
-    psmem = persist_smem_bytes(restart, npass, ppg);
-    cudaFuncAttributes fa;
-    FL_TRY_CUDA(cudaFuncGetAttributes(&fa, fn));
-    int dev = 0, optin = 0;
-    FL_TRY_CUDA(cudaGetDevice(&dev));
-    FL_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    if (fa.sharedSizeBytes + psmem <= (size_t)optin) {
-      FL_TRY_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psmem));
-      FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, psmem));
-      persistent = (int64_t)per_sm * sms >= pnb;
+    // launch shape of this (lanes per row, rows, restart), worked out once
+    // per process (occupancy queries and the shared-memory attribute)
+    struct Shape {
+      int pg, groups, restart, npass, pnb, ok;
+      size_t smem;
+    };
+    static std::vector<Shape> shapes;
+    static std::mutex shapes_mu;
+    std::lock_guard<std::mutex> lock(shapes_mu);
+    const Shape* hit = nullptr;
+    for (const Shape& c : shapes)
+      if (c.pg == ppg && c.groups == groups && c.restart == restart) hit = &c;
+    if (!hit) {
+      const void* fn = ppg == 8 ? (const void*)k_gmres_persistent<8>
+                     : ppg == 4 ? (const void*)k_gmres_persistent<4> : (const void*)k_gmres_persistent<2>;
+      Shape c{ppg, groups, restart, 0, 0, 0, 0};
+      int per_sm = 0;
+      FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0));
+      const int cap = std::max(1, per_sm) * sms;
+      c.npass = (groups + cap - 1) / cap;
+      c.pnb = (groups + c.npass - 1) / c.npass;
+      c.smem = persist_smem_bytes(restart, c.npass, ppg);
+      cudaFuncAttributes fa;
+      FL_TRY_CUDA(cudaFuncGetAttributes(&fa, fn));
+      int dev = 0, optin = 0;
+      FL_TRY_CUDA(cudaGetDevice(&dev));
+      FL_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+      if (fa.sharedSizeBytes + c.smem <= (size_t)optin) {
+        // the attribute only grows, so a smaller shape cached earlier stays valid
+        int cur = 0;
+        cudaFuncAttributes fb;
+        FL_TRY_CUDA(cudaFuncGetAttributes(&fb, fn));
+        cur = fb.maxDynamicSharedSizeBytes;
+        if ((int)c.smem > cur) FL_TRY_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem));
+        FL_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, c.smem));
+        c.ok = (int64_t)per_sm * sms >= c.pnb ? 1 : 0;
+      }
+      shapes.push_back(c);
+      hit = &shapes.back();
     }
+    persistent = hit->ok != 0;
+    npass = hit->npass;
+    pnb = hit->pnb;
+    psmem = hit->smem;
     if (persistent) FL_TRY(W->part.reserve((size_t)std::max(np, pnb) * (kMaxRestart + 3)));
   }
   FL_TRY(ensure_sell(m, W, s));
