@@ -568,9 +568,13 @@ __device__ __forceinline__ double sell_row_dot(const SellArgs& A, const V* __res
   const int sl = r / kSlice, lane = r % kSlice;
   const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
   double s = 0.0;
+  // unrolled so that several slices' value, offset and gather loads are in
+  // flight together (the products are still added in slice order)
   if (A.soff) {
+#pragma unroll 4
     for (int k = b; k < e; k += kSlice) s += (double)__ldg(sval + k) * (double)x[r + __ldg(A.soff + k)];
   } else {
+#pragma unroll 4
     for (int k = b; k < e; k += kSlice) s += (double)__ldg(sval + k) * (double)x[__ldg(A.scol + k)];
   }
   return s;
@@ -1595,8 +1599,10 @@ __global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv,
     const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
     float s = 0.0f;
     if (A.soff) {
+#pragma unroll 4
       for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[row + __ldg(A.soff + k)], s);
     } else {
+#pragma unroll 4
       for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[__ldg(A.scol + k)], s);
     }
     const float pi = p[row];
