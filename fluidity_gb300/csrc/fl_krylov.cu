@@ -1599,8 +1599,24 @@ __global__ void k_cg32_ap(SellArgs A, const float* __restrict__ sval, float piv,
     const int b = __ldg(A.sptr + sl) + lane, e = __ldg(A.sptr + sl + 1);
     float s = 0.0f;
     if (A.soff) {
-#pragma unroll 4
-      for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[row + __ldg(A.soff + k)], s);
+      // eight slices at a time: their offsets and values first, then the
+      // eight gathers, then the products added in slice order
+      int k = b;
+      for (; k + 7 * kSlice < e; k += 8 * kSlice) {
+        float a[8];
+        int c[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          a[u] = __ldg(sval + k + u * kSlice);
+          c[u] = row + __ldg(A.soff + k + u * kSlice);
+        }
+        float xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) xv[u] = p[c[u]];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s = fmaf(a[u], xv[u], s);
+      }
+      for (; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[row + __ldg(A.soff + k)], s);
     } else {
 #pragma unroll 4
       for (int k = b; k < e; k += kSlice) s = fmaf(__ldg(sval + k), p[__ldg(A.scol + k)], s);
