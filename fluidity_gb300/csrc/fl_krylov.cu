@@ -26,6 +26,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -108,10 +109,19 @@ struct KrylovWork {
   // the GMRES cycle, each reused while the buffers and sizes it was captured
   // with are unchanged
   GraphSlot g_cg, g_gmres;
+  // page-locked host copy of the state's scalars (the upload at the start of
+  // a solve and the report read at its end are then plain DMA copies) and of
+  // the cooperative GMRES's barrier flag
+  struct HostPin {
+    KspState st;
+    unsigned long long fault;
+  };
+  HostPin* pin = nullptr;
   ~KrylovWork() {
     if (cs) cudaStreamDestroy(cs);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
+    if (pin) cudaFreeHost(pin);
   }
 };
 
@@ -1963,7 +1973,12 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   FL_TRY(W->dinv.reserve(n));
   FL_TRY(W->part.reserve((size_t)np * (kMaxRestart + 2)));
   FL_TRY(W->st.reserve(1));
-  KspState h{};
+  if (!W->pin) FL_TRY_CUDA(cudaMallocHost(&W->pin, sizeof(KrylovWork::HostPin)));
+  // the previous solve on this workspace ended with a synchronisation, so
+  // the pinned buffer is free
+  KspState& h = W->pin->st;
+  std::memset(&h, 0, offsetof(KspState, grs));
+  W->pin->fault = 0;
   h.rtol = o->rtol;
   h.atol = o->atol;
   h.dtol = o->dtol > 0 ? o->dtol : 1e5;
@@ -1994,7 +2009,6 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   bool persistent = false;
   int pnb = 0, npass = 0, ppg = 8;
   size_t psmem = 0;
-  unsigned long long barrier_fault = 0;
   if (o->ksp_type == 1 && !mixed && (o->schedule == 2 || (o->schedule == 0 && n <= FL_PERSIST_MAX_ROWS))) {
     const int sms = num_sms();
     ppg = (n + kThreads / 8 - 1) / (kThreads / 8) <= sms ? 8 : (n + kThreads / 4 - 1) / (kThreads / 4) <= sms ? 4 : 2;
@@ -2112,7 +2126,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
     const void* fn = ppg == 8 ? (const void*)k_gmres_persistent<8>
                    : ppg == 4 ? (const void*)k_gmres_persistent<4> : (const void*)k_gmres_persistent<2>;
     FL_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(pnb), dim3(kThreads), args, psmem, s));
-    FL_TRY_CUDA(cudaMemcpyAsync(&barrier_fault, W->ticket.p + 2, sizeof(unsigned long long),
+    FL_TRY_CUDA(cudaMemcpyAsync(&W->pin->fault, W->ticket.p + 2, sizeof(unsigned long long),
                                 cudaMemcpyDeviceToHost, s));
   } else if (!mixed) {
     // GMRES(restart): one cycle with the restarts decided on the device,
@@ -2278,10 +2292,10 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   k_true_resid_final<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
   k_copy_back<<<gv, kThreads, 0, s>>>(n, ghost, rhs, W->y.p, x);
   FL_TRY_CUDA(cudaGetLastError());
-  KspState hs;
+  KspState& hs = W->pin->st;
   FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, offsetof(KspState, grs), cudaMemcpyDeviceToHost, s));
   FL_TRY_CUDA(cudaStreamSynchronize(s));
-  if (barrier_fault) {
+  if (W->pin->fault) {
     set_error("a bounded device wait ran out: a grid barrier of the cooperative GMRES solve");
     return FL_ERR_TIMEOUT;
   }
