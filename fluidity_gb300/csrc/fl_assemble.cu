@@ -1538,23 +1538,45 @@ __global__ void __launch_bounds__(THREADS) k_rows_pull(PullArgs P) {
     }
     double r = 0.0;
     const int ib = __ldg(P.ne_ptr + row), ie = __ldg(P.ne_ptr + row + 1);
-    for (int q = ib; q < ie; ++q) {
-      const int inc = __ldg(P.ne_col + q);
-      const int e = inc >> 4, a = inc & 15;
-      uint32_t pw[PW];
+    // incidences in groups of NG: the group's index loads, then all its
+    // element-matrix loads, then the adds in incidence order (the same sums,
+    // with NG incidences' memory round trips overlapped instead of one)
+    constexpr int NG = LOC == 4 ? 4 : 2;
+    for (int q0 = ib; q0 < ie; q0 += NG) {
+      int inc[NG];
+      uint32_t pw[NG][PW];
 #pragma unroll
-      for (int w = 0; w < PW; ++w) pw[w] = __ldg(P.ne_pos + (int64_t)q * PW + w);
+      for (int u = 0; u < NG; ++u) {
+        const bool ok = q0 + u < ie;
+        inc[u] = ok ? __ldg(P.ne_col + q0 + u) : 0;
 #pragma unroll
-      for (int b = 0; b < LOC; ++b) {
-        int k;
-        if (SYM) k = a <= b ? a * LOC - (a * (a - 1)) / 2 + (b - a) : b * LOC - (b * (b - 1)) / 2 + (a - b);
-        else k = a * LOC + b;
-        const double v = __ldg(P.em + (int64_t)k * E + e);
-        const int pos = (pw[b >> 2] >> (8 * (b & 3))) & 0xffu;
-        if (in_smem) acc[pos * THREADS + t] += v;
-        else P.val[base + pos] += v;
+        for (int w = 0; w < PW; ++w) pw[u][w] = ok ? __ldg(P.ne_pos + (int64_t)(q0 + u) * PW + w) : 0u;
       }
-      r += __ldg(P.em + (int64_t)(NK + a) * E + e);
+      double v[NG][LOC], rr[NG];
+#pragma unroll
+      for (int u = 0; u < NG; ++u) {
+        const int e = inc[u] >> 4, a = inc[u] & 15;
+        const bool ok = q0 + u < ie;
+#pragma unroll
+        for (int b = 0; b < LOC; ++b) {
+          int k;
+          if (SYM) k = a <= b ? a * LOC - (a * (a - 1)) / 2 + (b - a) : b * LOC - (b * (b - 1)) / 2 + (a - b);
+          else k = a * LOC + b;
+          v[u][b] = ok ? __ldg(P.em + (int64_t)k * E + e) : 0.0;
+        }
+        rr[u] = ok ? __ldg(P.em + (int64_t)(NK + a) * E + e) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < NG; ++u) {
+        if (q0 + u >= ie) break;
+#pragma unroll
+        for (int b = 0; b < LOC; ++b) {
+          const int pos = (pw[u][b >> 2] >> (8 * (b & 3))) & 0xffu;
+          if (in_smem) acc[pos * THREADS + t] += v[u][b];
+          else P.val[base + pos] += v[u][b];
+        }
+        r += rr[u];
+      }
     }
     if (in_smem)
       for (int k = 0; k < L; ++k) P.val[base + k] = acc[k * THREADS + t];
