@@ -343,8 +343,14 @@ __device__ __forceinline__ double row_dot_scaled(const int32_t* __restrict__ fin
 
 // ---------------------------------------------------------------- setup --
 // diag / ghost pivot inputs: min and max of |diag| over all rows.
+// (declared here, defined with the CG kernels)
+__device__ __forceinline__ bool last_block(unsigned* ticket);
+
+// Raw diagonal and the per-block min / max of |diagonal|; the last block to
+// retire forms the ghost pivot sqrt((max + min) max / 2) from the blocks'
+// partials in block order (Petsc_Tools.F90:960-985).
 __global__ void k_diag(SpArgs A, const int32_t* __restrict__ centrm, double* __restrict__ dinv,
-                       double* __restrict__ part_min, double* __restrict__ part_max) {
+                       double* __restrict__ part_min, double* __restrict__ part_max, unsigned* ticket) {
   note_launch();
   __shared__ double rmin[kThreads / 32], rmax[kThreads / 32];
   double mn = HUGE_VAL, mx = -HUGE_VAL;
@@ -374,40 +380,28 @@ __global__ void k_diag(SpArgs A, const int32_t* __restrict__ centrm, double* __r
     part_min[blockIdx.x] = fmin(rmin[0], mn);
     part_max[blockIdx.x] = fmax(rmax[0], mx);
   }
-}
-
-__global__ void k_pivot(KspState* st, const double* __restrict__ pmin, const double* __restrict__ pmax, int nb) {
-  note_launch();
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double mn = HUGE_VAL, mx = -HUGE_VAL;
+  if (!last_block(ticket)) return;
+  if (threadIdx.x == 0) {
+    const int nb = gridDim.x;
+    double pmn = HUGE_VAL, pmx = -HUGE_VAL;
     for (int k = 0; k < nb; ++k) {
-      mn = fmin(mn, pmin[k]);
-      mx = fmax(mx, pmax[k]);
+      pmn = fmin(pmn, __ldcg(part_min + k));
+      pmx = fmax(pmx, __ldcg(part_max + k));
     }
-    st->mind = mn;
-    st->maxd = mx;
-    st->pivot = sqrt((mx + mn) * mx / 2.0);
+    KspState* st = A.st;
+    st->mind = pmn;
+    st->maxd = pmx;
+    st->pivot = sqrt((pmx + pmn) * pmx / 2.0);
   }
 }
 
-// PCJACOBI inverse diagonal (ghost rows: the pivot; a zero diagonal acts as 1,
-// as PCSetUp_Jacobi does).
-__global__ void k_dinv(int n, const uint8_t* __restrict__ ghost, const KspState* st, double* __restrict__ dinv,
-                       float* __restrict__ dinv32) {
-  note_launch();
-  const double piv = st->pivot;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double d = (ghost && ghost[i]) ? piv : dinv[i];
-    double v = d != 0.0 ? 1.0 / d : 1.0;
-    dinv[i] = v;
-    if (dinv32) dinv32[i] = (float)v;
-  }
-}
-
-// b = rhs - A*(rhs on ghosts) on active rows, 0 on ghost rows; y = guess.
+// b = rhs - A*(rhs on ghosts) on active rows, 0 on ghost rows; y = guess;
+// and the PCJACOBI inverse diagonal in place of the raw one (ghost rows: the
+// pivot; a zero diagonal acts as 1, as PCSetUp_Jacobi does).
 template <int G>
 __global__ void k_lift(SpArgs A, const double* __restrict__ rhs, const double* __restrict__ x0, int guess_zero,
-                       double* __restrict__ b, double* __restrict__ y) {
+                       double* __restrict__ b, double* __restrict__ y, double* __restrict__ dinv,
+                       float* __restrict__ dinv32) {
   note_launch();
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int gpb = blockDim.x / G;
@@ -432,6 +426,10 @@ __global__ void k_lift(SpArgs A, const double* __restrict__ rhs, const double* _
     if (valid && sub == 0) {
       b[row] = g ? 0.0 : rhs[row] - s;
       y[row] = (guess_zero || g) ? 0.0 : x0[row];
+      const double d = g ? A.st->pivot : dinv[row];
+      const double v = d != 0.0 ? 1.0 / d : 1.0;
+      dinv[row] = v;
+      if (dinv32) dinv32[row] = (float)v;
     }
   }
 }
@@ -1510,8 +1508,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_gmres_persistent(PersistArgs P)
 
 // ------------------------------------------------------------- finalise --
 template <int G>
+// ||b - A y||^2 and ||b||^2 (the report's true residual), the last block
+// summing the partials in block order; and x = y on active rows, the rhs on
+// ghost rows (Petsc_Tools.F90:726-730).
 __global__ void k_true_resid(SpArgs A, const double* __restrict__ b, const double* __restrict__ y,
-                             double* __restrict__ part, int nparts) {
+                             double* __restrict__ part, int nparts, const double* __restrict__ rhs,
+                             double* __restrict__ x, unsigned* ticket) {
   note_launch();
   __shared__ double red[kThreads / 32];
   const double piv = A.st->pivot;
@@ -1523,10 +1525,12 @@ __global__ void k_true_resid(SpArgs A, const double* __restrict__ b, const doubl
     double s = 0.0;
     s = row_dot<G>(A.findrm, A.colm, A.val, y, row, sub, row < A.n);
     if (row < A.n && sub == 0) {
-      if (A.ghost && A.ghost[row]) s = piv * y[row];
+      const bool g = A.ghost && A.ghost[row];
+      if (g) s = piv * y[row];
       const double ri = b[row] - s;
       rr += ri * ri;
       bb += b[row] * b[row];
+      x[row] = g ? rhs[row] : y[row];
     }
   }
   rr = block_sum<kThreads>(rr, red);
@@ -1535,24 +1539,13 @@ __global__ void k_true_resid(SpArgs A, const double* __restrict__ b, const doubl
     part[blockIdx.x] = rr;
     part[nparts + blockIdx.x] = bb;
   }
-}
-
-__global__ void k_true_resid_final(KspState* st, const double* __restrict__ part, int nparts) {
-  note_launch();
-  __shared__ double red[kThreads / 32];
-  const double rr = reduce_partials(part, nparts, red);
-  const double bb = reduce_partials(part + nparts, nparts, red);
+  if (!last_block(ticket)) return;
+  rr = reduce_partials(part, nparts, red);
+  bb = reduce_partials(part + nparts, nparts, red);
   if (threadIdx.x == 0) {
-    st->true_r2 = rr;
-    st->b2 = bb;
+    A.st->true_r2 = rr;
+    A.st->b2 = bb;
   }
-}
-
-__global__ void k_copy_back(int n, const uint8_t* __restrict__ ghost, const double* __restrict__ rhs,
-                            const double* __restrict__ y, double* __restrict__ x) {
-  note_launch();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    x[i] = (ghost && ghost[i]) ? rhs[i] : y[i];
 }
 
 // ----------------------------------------------------------- mixed (fp32) --
@@ -1993,12 +1986,13 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
   SpArgs A{n, m->findrm.p, m->colm.p, val, ghost, st};
 
   // Jacobi diagonal and ghost pivot
-  k_diag<<<gv, kThreads, 0, s>>>(A, m->centrm.p, W->dinv.p, W->part.p, W->part.p + np);
-  k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + np, (int)gv);
+  // retire tickets: [0..3] the Krylov kernels, [4] the diagonal pass, [5] the true residual
+  FL_TRY(W->ticket.reserve(6));
+  FL_TRY_CUDA(cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 6, s));
+  k_diag<<<gv, kThreads, 0, s>>>(A, m->centrm.p, W->dinv.p, W->part.p, W->part.p + np, W->ticket.p + 4);
   const bool mixed = o->precision != 0;
   if (mixed) FL_TRY(W->dinv32.reserve(n));
-  k_dinv<<<gv, kThreads, 0, s>>>(n, ghost, st, W->dinv.p, mixed ? W->dinv32.p : nullptr);
-  FL_SPMV_DISPATCH(G, k_lift, A, rhs, x, h.guess_zero, W->b.p, W->y.p);
+  FL_SPMV_DISPATCH(G, k_lift, A, rhs, x, h.guess_zero, W->b.p, W->y.p, W->dinv.p, mixed ? W->dinv32.p : nullptr);
   FL_TRY_CUDA(cudaGetLastError());
 
   int outer = 0;
@@ -2288,9 +2282,7 @@ int solve(fl_mesh_t* m, const fl_solver_opts* o, const double* val, const uint8_
       FL_TRY_CUDA(cudaMemcpyAsync(&st->rnorm0, &hs.rnorm0, sizeof(double), cudaMemcpyHostToDevice, s));
     }
   }
-  FL_SPMV_DISPATCH(G, k_true_resid, A, W->b.p, W->y.p, W->part.p, (int)gsp);
-  k_true_resid_final<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
-  k_copy_back<<<gv, kThreads, 0, s>>>(n, ghost, rhs, W->y.p, x);
+  FL_SPMV_DISPATCH(G, k_true_resid, A, W->b.p, W->y.p, W->part.p, (int)gsp, rhs, x, W->ticket.p + 5);
   FL_TRY_CUDA(cudaGetLastError());
   KspState& hs = W->pin->st;
   FL_TRY_CUDA(cudaMemcpyAsync(&hs, st, offsetof(KspState, grs), cudaMemcpyDeviceToHost, s));
@@ -2380,7 +2372,7 @@ int cg_prepare(CgPlan& P, fl_mesh_t* m, const fl_solver_opts* o, const double* v
   FL_TRY(W->dinv.reserve(n));
   FL_TRY(W->part.reserve((size_t)P.np * (kMaxRestart + 2)));
   FL_TRY(W->st.reserve(1));
-  FL_TRY(W->ticket.reserve(4));
+  FL_TRY(W->ticket.reserve(6));
   FL_TRY(W->sval.reserve(M->sell_len));
   P.sell_len = M->sell_len;
   P.smap = M->smap.p;
@@ -2397,11 +2389,9 @@ void cg_setup_launch(CgPlan& P, cudaStream_t s) {
   const unsigned gsp = P.gsp;
   k_state_init<<<1, 32, 0, s>>>(st, P.o.rtol, P.o.atol, P.o.dtol > 0 ? P.o.dtol : 1e5, P.o.max_its,
                                  P.o.start_from_zero ? 1 : 0, P.o.norm_type == 1 ? 1 : 0);
-  k_diag<<<P.gv, kThreads, 0, s>>>(P.A, P.m->centrm.p, W->dinv.p, W->part.p, W->part.p + P.np);
-  k_pivot<<<1, 32, 0, s>>>(st, W->part.p, W->part.p + P.np, (int)P.gv);
-  k_dinv<<<P.gv, kThreads, 0, s>>>(P.n, P.ghost, st, W->dinv.p, nullptr);
-  FL_SPMV_DISPATCH(G, k_lift, P.A, P.rhs, P.x, P.o.start_from_zero ? 1 : 0, W->b.p, W->y.p);
-  cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 4, s);
+  cudaMemsetAsync(W->ticket.p, 0, sizeof(unsigned) * 6, s);
+  k_diag<<<P.gv, kThreads, 0, s>>>(P.A, P.m->centrm.p, W->dinv.p, W->part.p, W->part.p + P.np, W->ticket.p + 4);
+  FL_SPMV_DISPATCH(G, k_lift, P.A, P.rhs, P.x, P.o.start_from_zero ? 1 : 0, W->b.p, W->y.p, W->dinv.p, nullptr);
   if (P.ksp == 1) return;  // GMRES: the first cycle computes the initial residual
   FL_SPMV_DISPATCH(G, k_init_resid, P.A, W->b.p, W->y.p, W->dinv.p, W->r.p, W->z.p, W->part.p, (int)gsp);
   k_cg_start<<<1, kThreads, 0, s>>>(st, W->part.p, (int)gsp);
@@ -2424,9 +2414,7 @@ void cg_finish_launch(CgPlan& P, cudaStream_t s) {
   KrylovWork* W = P.W;
   const int G = P.G;
   const unsigned gsp = P.gsp;
-  FL_SPMV_DISPATCH(G, k_true_resid, P.A, W->b.p, W->y.p, W->part.p, (int)gsp);
-  k_true_resid_final<<<1, kThreads, 0, s>>>(W->st.p, W->part.p, (int)gsp);
-  k_copy_back<<<P.gv, kThreads, 0, s>>>(P.n, P.ghost, P.rhs, W->y.p, P.x);
+  FL_SPMV_DISPATCH(G, k_true_resid, P.A, W->b.p, W->y.p, W->part.p, (int)gsp, P.rhs, P.x, W->ticket.p + 5);
 }
 
 int cg_report(CgPlan& P, fl_solve_report* rep, cudaStream_t s) {
